@@ -1,0 +1,720 @@
+// FP64 CPU restatement of PBAT's Vertex Block Descent path.
+//
+// TEST INFRASTRUCTURE ONLY: this file is the parity oracle.  Only the test suite, the smoke check
+// and the CPU-baseline leg of the benchmark load it; the product (the CUDA library) never does.
+//
+// Every function cites the reference function it restates (paths relative to the reference's
+// `source/pbat/`).  The arithmetic is FP64, the per-colour vertex loop is OpenMP-parallel (the
+// reference's `tbb::parallel_for`, sim/vbd/Integrator.cpp:82-85); vertices of one colour share no
+// tetrahedron, so the result does not depend on the thread count.
+//
+// Pinned by: the reference headers themselves, compiled into `oracle/_ref` by `oracle/Makefile`
+// (tests compare this file's SNH derivatives, per-vertex solve, initialisation strategies,
+// Chebyshev weights and greedy colouring with the reference's own code), and by the reference
+// doctest known-answer values committed under tests/golden/.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+using Real = double;
+
+// ---------------------------------------------------------------------------------------------
+// Small dense helpers (column-major 3x3: A[3*c + r]).
+// ---------------------------------------------------------------------------------------------
+
+inline Real det3(Real const* A)
+{
+    // math/linalg/mini/Determinant.h:31-35 (cofactor expansion along the first row).
+    return A[0] * (A[4] * A[8] - A[5] * A[7]) - A[3] * (A[1] * A[8] - A[2] * A[7]) +
+           A[6] * (A[1] * A[5] - A[2] * A[4]);
+}
+
+inline void cross3(Real const* a, Real const* b, Real* c)
+{
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Inverse of a 3x3 by cofactors / determinant (math/linalg/mini/Inverse.h:40-55 computes the same
+// closed form).
+inline void inv3(Real const* A, Real* Ai)
+{
+    Real c0[3], c1[3], c2[3];
+    // Rows of the inverse are cross products of the columns of A divided by det.
+    cross3(A + 3, A + 6, c0);
+    cross3(A + 6, A + 0, c1);
+    cross3(A + 0, A + 3, c2);
+    Real const d = A[0] * c0[0] + A[1] * c0[1] + A[2] * c0[2];
+    Real const s = Real(1) / d;
+    for (int k = 0; k < 3; ++k)
+    {
+        Ai[3 * k + 0] = c0[k] * s;
+        Ai[3 * k + 1] = c1[k] * s;
+        Ai[3 * k + 2] = c2[k] * s;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Stable Neo-Hookean energy (physics/StableNeoHookeanEnergy.h:621-1325).
+//   Psi(F) = mu/2 (tr(F^T F) - 3) + lambda/2 (det F - 1 - mu/lambda)^2
+// F is a column-major 9-vector.  Derivatives are written from the formula:
+//   dPsi/dF   = mu F + lambda (J - alpha) cof(F)
+//   d2Psi/dF2 = mu I9 + lambda vec(cof F) vec(cof F)^T + lambda (J - alpha) d2J/dF2
+// with alpha = 1 + mu/lambda and d2J/dF_a dF_b = -[F_c]x for (a,b,c) a cyclic permutation of
+// (0,1,2) (its transpose for the anti-cyclic order, zero on the diagonal blocks).
+// ---------------------------------------------------------------------------------------------
+
+inline void cofactor(Real const* F, Real* C)
+{
+    cross3(F + 3, F + 6, C + 0);
+    cross3(F + 6, F + 0, C + 3);
+    cross3(F + 0, F + 3, C + 6);
+}
+
+Real snh_eval(Real const* F, Real mu, Real lambda)
+{
+    Real I2 = 0;
+    for (int k = 0; k < 9; ++k)
+        I2 += F[k] * F[k];
+    Real const a = det3(F) - Real(1) - mu / lambda;
+    return Real(0.5) * lambda * a * a + Real(0.5) * mu * (I2 - Real(3));
+}
+
+void snh_grad(Real const* F, Real mu, Real lambda, Real* g)
+{
+    Real C[9];
+    cofactor(F, C);
+    Real const J = F[0] * C[0] + F[1] * C[1] + F[2] * C[2];
+    Real const s = lambda * (J - Real(1) - mu / lambda);
+    for (int k = 0; k < 9; ++k)
+        g[k] = mu * F[k] + s * C[k];
+}
+
+// Skew matrix [v]x (column-major) scaled by s, added into the 3x3 block (rows r0.., cols c0..)
+// of a 9x9 row-major matrix H.
+inline void add_skew(Real* H, int r0, int c0, Real const* v, Real s)
+{
+    // [v]x = [[0, -v2, v1], [v2, 0, -v0], [-v1, v0, 0]]
+    Real const S[3][3] = {{0, -v[2], v[1]}, {v[2], 0, -v[0]}, {-v[1], v[0], 0}};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            H[(r0 + i) * 9 + (c0 + j)] += s * S[i][j];
+}
+
+void snh_grad_hessian(Real const* F, Real mu, Real lambda, Real* g, Real* H)
+{
+    Real C[9];
+    cofactor(F, C);
+    Real const J  = F[0] * C[0] + F[1] * C[1] + F[2] * C[2];
+    Real const Ja = J - Real(1) - mu / lambda;
+    for (int k = 0; k < 9; ++k)
+        g[k] = mu * F[k] + lambda * Ja * C[k];
+    for (int r = 0; r < 9; ++r)
+        for (int c = 0; c < 9; ++c)
+            H[r * 9 + c] = lambda * C[r] * C[c] + (r == c ? mu : Real(0));
+    Real const s = lambda * Ja;
+    // Off-diagonal column blocks of d2J/dF2.
+    int const cyc[3][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}};
+    for (auto const& t : cyc)
+    {
+        int const a = t[0], b = t[1], c = t[2];
+        add_skew(H, 3 * a, 3 * b, F + 3 * c, -s); // block(a,b) = -[F_c]x
+        add_skew(H, 3 * b, 3 * a, F + 3 * c, s);  // block(b,a) = +[F_c]x
+    }
+}
+
+} // namespace
+
+#include "orc_problem.h"
+
+extern "C" {
+
+// ---- Lame coefficients (physics/HyperElasticity.cpp:6-11) -----------------------------------
+void orc_lame(double E, double nu, double* mu, double* lambda)
+{
+    *mu     = E / (2. * (1. + nu));
+    *lambda = (E * nu) / ((1. + nu) * (1. - 2. * nu));
+}
+
+// ---- SNH entry points for tests --------------------------------------------------------------
+double orc_snh_eval(double const* F, double mu, double lambda)
+{
+    return snh_eval(F, mu, lambda);
+}
+void orc_snh_grad(double const* F, double mu, double lambda, double* g)
+{
+    snh_grad(F, mu, lambda, g);
+}
+void orc_snh_grad_hessian(double const* F, double mu, double lambda, double* g, double* H)
+{
+    snh_grad_hessian(F, mu, lambda, g, H);
+}
+
+// ---- Data::Construct precompute (sim/vbd/Data.cpp:179-243) ----------------------------------
+//
+// Outputs (caller-allocated): m[nV], GP[nT*12], wg[nT], GVGp[nV+1], GVGe[4nT], GVGilocal[4nT],
+// colors[nV], Pptr[>= 129], Padj[nV].  Returns 0 on success, 1 on a degenerate/inverted tet,
+// 2 on an out-of-range index, 3 when the colour palette (128) overflows.
+int orc_construct(
+    int32_t nV,
+    int32_t nT,
+    double const* X,
+    int32_t const* T,
+    double const* rhoe,
+    int32_t const* dbc,
+    int32_t nDbc,
+    int32_t ordering,
+    int32_t selection,
+    double* m,
+    double* GP,
+    double* wg,
+    int32_t* GVGp,
+    int32_t* GVGe,
+    int32_t* GVGilocal,
+    int32_t* colors,
+    int32_t* Pptr,
+    int32_t* nPartitions,
+    int32_t* Padj,
+    int32_t* nPadj)
+{
+    for (int64_t k = 0; k < int64_t(nT) * 4; ++k)
+        if (T[k] < 0 || T[k] >= nV)
+            return 2;
+    // Element geometry: fem/ShapeFunctions.h:267-296 (GP = GN J^-1 for the linear tet),
+    // fem/MeshQuadrature.h:75-88 (order-1 weight = |det J|/6), fem/Mass.h:357-397 with
+    // Data.cpp:210-219 (lumped mass = rho V / 4 per incident tet).
+    std::fill(m, m + nV, 0.0);
+    for (int32_t e = 0; e < nT; ++e)
+    {
+        int32_t const* t = T + 4 * e;
+        Real J[9];
+        for (int d = 0; d < 3; ++d)
+            for (int r = 0; r < 3; ++r)
+                J[3 * d + r] = X[3 * t[d + 1] + r] - X[3 * t[0] + r];
+        Real const detJ = det3(J);
+        if (!(detJ > 0))
+            return 1;
+        Real Ji[9];
+        inv3(J, Ji);
+        double* G = GP + 12 * e;
+        // Row a (a = 1..3) of GP is row a-1 of J^-1; row 0 is minus their sum.
+        for (int a = 1; a < 4; ++a)
+            for (int d = 0; d < 3; ++d)
+                G[3 * a + d] = Ji[3 * d + (a - 1)];
+        for (int d = 0; d < 3; ++d)
+            G[d] = -(G[3 + d] + G[6 + d] + G[9 + d]);
+        wg[e]         = std::abs(detJ) / 6.0;
+        Real const me = rhoe[e] * wg[e] / 4.0;
+        for (int a = 0; a < 4; ++a)
+            m[t[a]] += me;
+    }
+    // Vertex -> tet adjacency, tets ascending per vertex (graph/Mesh.h:42-104 transposed,
+    // Data.cpp:223-226).
+    std::fill(GVGp, GVGp + nV + 1, 0);
+    for (int64_t k = 0; k < int64_t(nT) * 4; ++k)
+        ++GVGp[T[k] + 1];
+    for (int32_t i = 0; i < nV; ++i)
+        GVGp[i + 1] += GVGp[i];
+    {
+        std::vector<int32_t> fill(GVGp, GVGp + nV);
+        for (int32_t e = 0; e < nT; ++e)
+            for (int a = 0; a < 4; ++a)
+            {
+                int32_t const i = T[4 * e + a];
+                GVGe[fill[i]]      = e;
+                GVGilocal[fill[i]] = a;
+                ++fill[i];
+            }
+    }
+    // Primal vertex graph G G^T (graph/Mesh.h:117-123): neighbours incl. self, no duplicates.
+    std::vector<int32_t> Gp(nV + 1, 0), Gv;
+    {
+        std::vector<int32_t> mark(nV, -1), nb;
+        Gv.reserve(size_t(nV) * 16);
+        for (int32_t i = 0; i < nV; ++i)
+        {
+            nb.clear();
+            for (int32_t k = GVGp[i]; k < GVGp[i + 1]; ++k)
+            {
+                int32_t const* t = T + 4 * GVGe[k];
+                for (int a = 0; a < 4; ++a)
+                    if (mark[t[a]] != i)
+                    {
+                        mark[t[a]] = i;
+                        nb.push_back(t[a]);
+                    }
+            }
+            std::sort(nb.begin(), nb.end());
+            Gv.insert(Gv.end(), nb.begin(), nb.end());
+            Gp[i + 1] = int32_t(Gv.size());
+        }
+    }
+    // Greedy colouring (graph/Color.h:45-135).  Visiting order: stable argsort of degree
+    // (common/ArgSort.h:31-39); selection: LeastUsed (least-used usable colour, ties to the lowest
+    // index, i.e. std::min_element semantics) or FirstAvailable.
+    std::vector<int32_t> order(nV);
+    std::iota(order.begin(), order.end(), 0);
+    auto degree = [&](int32_t i) { return Gp[i + 1] - Gp[i]; };
+    if (ordering == 1) // SmallestDegree
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+            return degree(a) < degree(b);
+        });
+    else if (ordering == 2) // LargestDegree
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+            return degree(a) > degree(b);
+        });
+    std::fill(colors, colors + nV, -1);
+    int constexpr kPalette = 128;
+    std::vector<int32_t> palette;
+    std::vector<char> usable;
+    for (int32_t u : order)
+    {
+        std::fill(usable.begin(), usable.end(), 1);
+        int nUnusable = 0;
+        for (int32_t k = Gp[u]; k < Gp[u + 1]; ++k)
+        {
+            int32_t const cv = colors[Gv[k]];
+            if (cv >= 0 && usable[cv])
+            {
+                usable[cv] = 0;
+                ++nUnusable;
+            }
+        }
+        if (nUnusable == int(palette.size()))
+        {
+            if (int(palette.size()) == kPalette)
+                return 3;
+            colors[u] = int32_t(palette.size());
+            palette.push_back(1);
+            usable.push_back(0);
+        }
+        else
+        {
+            int best = 0;
+            for (int c = 1; c < int(palette.size()); ++c)
+            {
+                bool less;
+                if (usable[c] && usable[best])
+                    less = (selection == 0) ? palette[c] < palette[best] : c < best;
+                else
+                    less = usable[c];
+                if (less)
+                    best = c;
+            }
+            colors[u] = best;
+            ++palette[best];
+        }
+    }
+    // Partitions: stable argsort by colour (graph/Adjacency.h:172-181), then drop Dirichlet
+    // vertices (Data.cpp:236-243, graph/Adjacency.h:307-342).
+    int32_t const nC = nV > 0 ? *std::max_element(colors, colors + nV) + 1 : 0;
+    std::vector<char> pinned(nV, 0);
+    for (int32_t k = 0; k < nDbc; ++k)
+        if (dbc[k] >= 0 && dbc[k] < nV)
+            pinned[dbc[k]] = 1;
+    Pptr[0] = 0;
+    int32_t n = 0;
+    for (int32_t c = 0; c < nC; ++c)
+    {
+        for (int32_t i = 0; i < nV; ++i)
+            if (colors[i] == c && !pinned[i])
+                Padj[n++] = i;
+        Pptr[c + 1] = n;
+    }
+    *nPartitions = nC;
+    *nPadj       = n;
+    return 0;
+}
+
+// ---- Integrator ---------------------------------------------------------------------------
+
+static void initial_positions(
+    Real const* xt,
+    Real const* vtm1,
+    Real const* vt,
+    Real const* a,
+    Real dt,
+    Real dt2,
+    int strategy,
+    Real* x)
+{
+    // sim/vbd/Kernels.h:39-94 (InitialPositionsForSolve).
+    if (strategy == 0) // Position
+    {
+        for (int d = 0; d < 3; ++d)
+            x[d] = xt[d];
+        return;
+    }
+    if (strategy == 1) // Inertia
+    {
+        for (int d = 0; d < 3; ++d)
+            x[d] = xt[d] + dt * vt[d];
+        return;
+    }
+    if (strategy == 2) // KineticEnergyMinimum
+    {
+        for (int d = 0; d < 3; ++d)
+            x[d] = xt[d] + dt * vt[d] + dt2 * a[d];
+        return;
+    }
+    Real const an2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+    Real at        = 0;
+    if (an2 != Real(0))
+    {
+        if (strategy == 3) // AdaptiveVbd
+        {
+            Real dot = 0;
+            for (int d = 0; d < 3; ++d)
+                dot += ((vt[d] - vtm1[d]) / dt) * a[d];
+            at = std::min(std::max(dot / an2, Real(0)), Real(1));
+        }
+        else // AdaptivePbat
+        {
+            Real const vn =
+                std::sqrt(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]) +
+                std::numeric_limits<Real>::min();
+            Real dot = 0;
+            for (int d = 0; d < 3; ++d)
+                dot += (vt[d] / vn) * a[d];
+            at = std::min(std::abs(dot / an2), Real(1));
+        }
+    }
+    for (int d = 0; d < 3; ++d)
+        x[d] = xt[d] + dt * vt[d] + dt2 * at * a[d];
+}
+
+void orc_initial_positions(
+    double const* xt,
+    double const* vtm1,
+    double const* vt,
+    double const* a,
+    double dt,
+    double dt2,
+    int32_t strategy,
+    double* x)
+{
+    initial_positions(xt, vtm1, vt, a, dt, dt2, strategy, x);
+}
+
+// Accumulate the elastic gradient and 3x3 Hessian of vertex i (sim/vbd/Integrator.cpp:102-121,
+// sim/vbd/Kernels.h:131-171), then damping, inertia and the Newton step (Kernels.h:179-191,
+// 310-339).  x is updated in place.
+static void solve_vertex(orc_problem const& P, int32_t i, Real const* xt, Real const* xtilde, Real* x, Real sdt, Real sdt2)
+{
+    Real H[9] = {0}, g[3] = {0};
+    for (int32_t n = P.GVGp[i]; n < P.GVGp[i + 1]; ++n)
+    {
+        int32_t const e    = P.GVGe[n];
+        int32_t const il   = P.GVGilocal[n];
+        int32_t const* t   = P.T + 4 * e;
+        double const* GPe  = P.GP + 12 * e;
+        Real F[9]          = {0};
+        for (int a = 0; a < 4; ++a)
+            for (int d = 0; d < 3; ++d)
+                for (int r = 0; r < 3; ++r)
+                    F[3 * d + r] += x[3 * t[a] + r] * GPe[3 * a + d];
+        Real gF[9], HF[81];
+        snh_grad_hessian(F, P.mu[e], P.lambda[e], gF, HF);
+        Real const w = P.wg[e];
+        for (int kj = 0; kj < 3; ++kj)
+            for (int ki = 0; ki < 3; ++ki)
+            {
+                Real const s = w * GPe[3 * il + ki] * GPe[3 * il + kj];
+                for (int r = 0; r < 3; ++r)
+                    for (int c = 0; c < 3; ++c)
+                        H[3 * c + r] += s * HF[(3 * ki + r) * 9 + (3 * kj + c)];
+            }
+        for (int k = 0; k < 3; ++k)
+        {
+            Real const s = w * GPe[3 * il + k];
+            for (int r = 0; r < 3; ++r)
+                g[r] += s * gF[3 * k + r];
+        }
+    }
+    Real* xi        = x + 3 * i;
+    Real const* xti = xt + 3 * i;
+    // AddDamping (Kernels.h:179-191)
+    Real const D = P.kD / sdt;
+    for (int r = 0; r < 3; ++r)
+    {
+        Real hx = 0;
+        for (int c = 0; c < 3; ++c)
+            hx += H[3 * c + r] * (xi[c] - xti[c]);
+        g[r] += D * hx;
+    }
+    for (int k = 0; k < 9; ++k)
+        H[k] *= Real(1) + D;
+    // AddInertiaDerivatives (Kernels.h:310-322)
+    Real const K = P.m[i] / sdt2;
+    for (int r = 0; r < 3; ++r)
+    {
+        H[3 * r + r] += K;
+        g[r] += K * (xi[r] - xtilde[3 * i + r]);
+    }
+    // IntegratePositions (Kernels.h:329-339)
+    if (std::abs(det3(H)) <= P.detHZero)
+        return;
+    Real Hi[9];
+    inv3(H, Hi);
+    for (int r = 0; r < 3; ++r)
+    {
+        Real dx = 0;
+        for (int c = 0; c < 3; ++c)
+            dx += Hi[3 * c + r] * g[c];
+        xi[r] -= dx;
+    }
+}
+
+// Chebyshev weight (sim/vbd/Kernels.h:96-102).  formula 0 keeps the reference's expression as
+// written, `4/4 - rho2*omega` (= 1 - rho2*omega); formula 1 is the textbook 4/(4 - rho2*omega).
+double orc_chebyshev_omega(int32_t k, double rho2, double omega, int32_t formula)
+{
+    if (k == 0)
+        return 1.0;
+    if (k == 1)
+        return 2.0 / (2.0 - rho2);
+    return formula == 0 ? (4.0 / 4.0 - rho2 * omega) : 4.0 / (4.0 - rho2 * omega);
+}
+
+// Advance `nsteps` time steps in place: x, v (nV x 3), vprev (nV x 3, GPU semantics only: the
+// velocity of the previous step, initially zero).  sim/vbd/Integrator.cpp:22-96 and
+// ChebyshevIntegrator.cpp:15-32.
+int orc_run(orc_problem const* Pp, double* x, double* v, double* vprev, double dt, int32_t iterations, int32_t substeps, int32_t nsteps)
+{
+    orc_problem const& P = *Pp;
+    int32_t const nV     = P.nV;
+#ifdef _OPENMP
+    int const nthreads = P.nthreads > 0 ? P.nthreads : omp_get_max_threads();
+#else
+    int const nthreads = 1;
+#endif
+    (void)nthreads;
+    std::vector<Real> xt(size_t(nV) * 3), xtilde(size_t(nV) * 3), xkm1, xkm2, vtm1(size_t(nV) * 3);
+    if (P.acceleration == 1)
+    {
+        xkm1.assign(x, x + size_t(nV) * 3);
+        xkm2.assign(x, x + size_t(nV) * 3);
+    }
+    Real const sdt  = dt / Real(substeps);
+    Real const sdt2 = sdt * sdt;
+    for (int32_t step = 0; step < nsteps; ++step)
+        for (int32_t s = 0; s < substeps; ++s)
+        {
+            // xt <- x, vt <- v; with CPU semantics the previous velocity is lost here
+            // (Integrator.cpp:31-32), so InitializeSolve sees vtm1 = vt = v.
+            std::memcpy(xt.data(), x, sizeof(Real) * 3 * size_t(nV));
+            if (P.semantics == 1)
+                std::memcpy(vtm1.data(), vprev, sizeof(Real) * 3 * size_t(nV));
+            else
+                std::memcpy(vtm1.data(), v, sizeof(Real) * 3 * size_t(nV));
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+            for (int32_t i = 0; i < nV; ++i)
+            {
+                // InertialTarget (Kernels.h:24-37), InitializeSolve (Integrator.cpp:54-71)
+                for (int d = 0; d < 3; ++d)
+                    xtilde[3 * i + d] = xt[3 * i + d] + sdt * v[3 * i + d] + sdt2 * P.aext[3 * i + d];
+                initial_positions(
+                    &xt[3 * size_t(i)],
+                    &vtm1[3 * size_t(i)],
+                    v + 3 * size_t(i),
+                    P.aext + 3 * size_t(i),
+                    sdt,
+                    sdt2,
+                    P.strategy,
+                    x + 3 * size_t(i));
+            }
+            Real const rho2 = P.rho * P.rho;
+            Real omega      = 0;
+            for (int32_t k = 0; k < iterations; ++k)
+            {
+                // RunVbdIteration (Integrator.cpp:73-87): colours in sequence, vertices of a
+                // colour in parallel.
+                for (int32_t p = 0; p < P.nPartitions; ++p)
+                {
+                    int32_t const b = P.Pptr[p], e = P.Pptr[p + 1];
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+                    for (int32_t kk = b; kk < e; ++kk)
+                        solve_vertex(P, P.Padj[kk], xt.data(), xtilde.data(), x, sdt, sdt2);
+                }
+                if (P.acceleration == 1)
+                {
+                    omega = orc_chebyshev_omega(k, rho2, omega, P.chebyshev_formula);
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+                    for (int64_t q = 0; q < int64_t(nV) * 3; ++q)
+                    {
+                        if (k > 1)
+                            x[q] = omega * (x[q] - xkm2[q]) + xkm2[q];
+                        xkm2[q] = xkm1[q];
+                        xkm1[q] = x[q];
+                    }
+                }
+            }
+            // IntegrateVelocity (Kernels.h:121-129); GPU UpdateBdfState keeps the old velocity.
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+            for (int64_t q = 0; q < int64_t(nV) * 3; ++q)
+            {
+                if (vprev)
+                    vprev[q] = v[q];
+                v[q] = (x[q] - xt[q]) / sdt;
+            }
+        }
+    return 0;
+}
+
+// Backward-Euler objective and gradient (sim/vbd/Integrator.cpp:138-200):
+//   f(x) = 1/2 (x - xtilde)^T M (x - xtilde) + dt^2 sum_e wg_e Psi(F_e)
+double orc_objective(orc_problem const* Pp, double const* x, double const* xtilde, double dt)
+{
+    orc_problem const& P = *Pp;
+    Real Ek              = 0;
+    for (int32_t i = 0; i < P.nV; ++i)
+        for (int d = 0; d < 3; ++d)
+        {
+            Real const dx = x[3 * i + d] - xtilde[3 * i + d];
+            Ek += 0.5 * P.m[i] * dx * dx;
+        }
+    Real Ep = 0;
+    for (int32_t e = 0; e < P.nT; ++e)
+    {
+        int32_t const* t  = P.T + 4 * e;
+        double const* GPe = P.GP + 12 * e;
+        Real F[9]         = {0};
+        for (int a = 0; a < 4; ++a)
+            for (int d = 0; d < 3; ++d)
+                for (int r = 0; r < 3; ++r)
+                    F[3 * d + r] += x[3 * t[a] + r] * GPe[3 * a + d];
+        Ep += P.wg[e] * snh_eval(F, P.mu[e], P.lambda[e]);
+    }
+    return Ek + dt * dt * Ep;
+}
+
+void orc_gradient(orc_problem const* Pp, double const* x, double const* xtilde, double dt, double* grad)
+{
+    orc_problem const& P = *Pp;
+    for (int32_t i = 0; i < P.nV; ++i)
+        for (int d = 0; d < 3; ++d)
+            grad[3 * i + d] = P.m[i] * (x[3 * i + d] - xtilde[3 * i + d]);
+    for (int32_t e = 0; e < P.nT; ++e)
+    {
+        int32_t const* t  = P.T + 4 * e;
+        double const* GPe = P.GP + 12 * e;
+        Real F[9]         = {0};
+        for (int a = 0; a < 4; ++a)
+            for (int d = 0; d < 3; ++d)
+                for (int r = 0; r < 3; ++r)
+                    F[3 * d + r] += x[3 * t[a] + r] * GPe[3 * a + d];
+        Real gF[9];
+        snh_grad(F, P.mu[e], P.lambda[e], gF);
+        // fem::GradientWrtDofs: dPsi/dx_a = gF (as 3x3, column-major) * GP(a,:)^T
+        for (int a = 0; a < 4; ++a)
+            for (int r = 0; r < 3; ++r)
+            {
+                Real s = 0;
+                for (int d = 0; d < 3; ++d)
+                    s += gF[3 * d + r] * GPe[3 * a + d];
+                grad[3 * t[a] + r] += dt * dt * P.wg[e] * s;
+            }
+    }
+}
+
+// One vertex solve on explicit inputs, for comparison with the reference's kernels.
+// xe: 3 x 4 column-major positions per incidence (n incidences), GPs: n x 12, il, wg, mu, lambda.
+void orc_vertex_solve(
+    int32_t n,
+    double const* xe,
+    double const* GPs,
+    int32_t const* il,
+    double const* wgs,
+    double const* mus,
+    double const* lambdas,
+    double const* xti,
+    double const* xtildei,
+    double mi,
+    double kD,
+    double sdt,
+    double sdt2,
+    double detHZero,
+    double* xi,
+    double* gout,
+    double* Hout)
+{
+    Real H[9] = {0}, g[3] = {0};
+    for (int32_t q = 0; q < n; ++q)
+    {
+        double const* x4  = xe + 12 * q;
+        double const* GPe = GPs + 12 * q;
+        Real F[9]         = {0};
+        for (int a = 0; a < 4; ++a)
+            for (int d = 0; d < 3; ++d)
+                for (int r = 0; r < 3; ++r)
+                    F[3 * d + r] += x4[3 * a + r] * GPe[3 * a + d];
+        Real gF[9], HF[81];
+        snh_grad_hessian(F, mus[q], lambdas[q], gF, HF);
+        for (int kj = 0; kj < 3; ++kj)
+            for (int ki = 0; ki < 3; ++ki)
+            {
+                Real const s = wgs[q] * GPe[3 * il[q] + ki] * GPe[3 * il[q] + kj];
+                for (int r = 0; r < 3; ++r)
+                    for (int c = 0; c < 3; ++c)
+                        H[3 * c + r] += s * HF[(3 * ki + r) * 9 + (3 * kj + c)];
+            }
+        for (int k = 0; k < 3; ++k)
+            for (int r = 0; r < 3; ++r)
+                g[r] += wgs[q] * GPe[3 * il[q] + k] * gF[3 * k + r];
+    }
+    Real const D = kD / sdt;
+    Real gd[3];
+    for (int r = 0; r < 3; ++r)
+    {
+        Real hx = 0;
+        for (int c = 0; c < 3; ++c)
+            hx += H[3 * c + r] * (xi[c] - xti[c]);
+        gd[r] = g[r] + D * hx;
+    }
+    for (int k = 0; k < 9; ++k)
+        H[k] *= Real(1) + D;
+    Real const K = mi / sdt2;
+    for (int r = 0; r < 3; ++r)
+    {
+        H[3 * r + r] += K;
+        gd[r] += K * (xi[r] - xtildei[r]);
+    }
+    for (int r = 0; r < 3; ++r)
+        gout[r] = gd[r];
+    for (int k = 0; k < 9; ++k)
+        Hout[k] = H[k];
+    if (std::abs(det3(H)) <= detHZero)
+        return;
+    Real Hi[9];
+    inv3(H, Hi);
+    for (int r = 0; r < 3; ++r)
+    {
+        Real dx = 0;
+        for (int c = 0; c < 3; ++c)
+            dx += Hi[3 * c + r] * gd[c];
+        xi[r] -= dx;
+    }
+}
+
+int32_t orc_num_threads()
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+} // extern "C"

@@ -1,0 +1,244 @@
+"""ctypes access to the FP64 oracle (``oracle/_build/liboracle_vbd.so``) and, where it was built,
+to the reference harness (``oracle/_ref/libpbat_ref.so``).
+
+Test infrastructure: imported by the tests, the smoke check and the benchmark's CPU-baseline leg
+only.  ``build_oracle()`` compiles the oracle on first use (g++ -fopenmp, a few seconds).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import pathlib
+import subprocess
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+ORACLE_DIR = ROOT / "oracle"
+ORACLE_SO = ORACLE_DIR / "_build" / "liboracle_vbd.so"
+REF_SO = ORACLE_DIR / "_ref" / "libpbat_ref.so"
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+class OrcProblem(C.Structure):
+    """Mirror of ``orc_problem`` (oracle/orc_problem.h)."""
+
+    _fields_ = [
+        ("nV", C.c_int32),
+        ("nT", C.c_int32),
+        ("X", C.c_void_p),
+        ("T", C.c_void_p),
+        ("m", C.c_void_p),
+        ("GP", C.c_void_p),
+        ("wg", C.c_void_p),
+        ("mu", C.c_void_p),
+        ("lam", C.c_void_p),
+        ("GVGp", C.c_void_p),
+        ("GVGe", C.c_void_p),
+        ("GVGilocal", C.c_void_p),
+        ("nPartitions", C.c_int32),
+        ("Pptr", C.c_void_p),
+        ("Padj", C.c_void_p),
+        ("aext", C.c_void_p),
+        ("strategy", C.c_int32),
+        ("kD", C.c_double),
+        ("detHZero", C.c_double),
+        ("acceleration", C.c_int32),
+        ("rho", C.c_double),
+        ("chebyshev_formula", C.c_int32),
+        ("semantics", C.c_int32),
+        ("nthreads", C.c_int32),
+    ]
+
+
+def build_oracle(ref: bool = False) -> None:
+    """Compile the oracle (and the reference harness when ``ref`` and the reference exist)."""
+    targets = ["all"]
+    if ref:
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), *targets], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not ORACLE_SO.exists():
+            build_oracle()
+        L = C.CDLL(str(ORACLE_SO))
+        L.orc_construct.restype = C.c_int
+        L.orc_construct.argtypes = [
+            C.c_int32, C.c_int32, _f64p, _i32p, _f64p, _i32p, C.c_int32, C.c_int32, C.c_int32,
+            _f64p, _f64p, _f64p, _i32p, _i32p, _i32p, _i32p, _i32p,
+            C.POINTER(C.c_int32), _i32p, C.POINTER(C.c_int32),
+        ]
+        L.orc_run.restype = C.c_int
+        L.orc_run.argtypes = [
+            C.POINTER(OrcProblem), _f64p, _f64p, C.c_void_p, C.c_double, C.c_int32, C.c_int32,
+            C.c_int32,
+        ]
+        L.orc_objective.restype = C.c_double
+        L.orc_objective.argtypes = [C.POINTER(OrcProblem), _f64p, _f64p, C.c_double]
+        L.orc_gradient.restype = None
+        L.orc_gradient.argtypes = [C.POINTER(OrcProblem), _f64p, _f64p, C.c_double, _f64p]
+        L.orc_snh_eval.restype = C.c_double
+        L.orc_snh_eval.argtypes = [_f64p, C.c_double, C.c_double]
+        L.orc_snh_grad.argtypes = [_f64p, C.c_double, C.c_double, _f64p]
+        L.orc_snh_grad_hessian.argtypes = [_f64p, C.c_double, C.c_double, _f64p, _f64p]
+        L.orc_chebyshev_omega.restype = C.c_double
+        L.orc_chebyshev_omega.argtypes = [C.c_int32, C.c_double, C.c_double, C.c_int32]
+        L.orc_initial_positions.argtypes = [
+            _f64p, _f64p, _f64p, _f64p, C.c_double, C.c_double, C.c_int32, _f64p,
+        ]
+        L.orc_vertex_solve.argtypes = [
+            C.c_int32, _f64p, _f64p, _i32p, _f64p, _f64p, _f64p, _f64p, _f64p, C.c_double,
+            C.c_double, C.c_double, C.c_double, C.c_double, _f64p, _f64p, _f64p,
+        ]
+        L.orc_num_threads.restype = C.c_int32
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return REF_SO.exists()
+
+
+def ref():
+    """The reference harness, or None where it was not built (e.g. without the reference)."""
+    global _ref
+    if _ref is None:
+        if not REF_SO.exists():
+            return None
+        L = C.CDLL(str(REF_SO))
+        L.ref_snh_eval.restype = C.c_double
+        L.ref_snh_eval.argtypes = [_f64p, C.c_double, C.c_double]
+        L.ref_snh_grad.argtypes = [_f64p, C.c_double, C.c_double, _f64p]
+        L.ref_snh_grad_hessian.argtypes = [_f64p, C.c_double, C.c_double, _f64p, _f64p]
+        L.ref_chebyshev_omega.restype = C.c_double
+        L.ref_chebyshev_omega.argtypes = [C.c_int32, C.c_double, C.c_double]
+        L.ref_initial_positions.argtypes = [
+            _f64p, _f64p, _f64p, _f64p, C.c_double, C.c_double, C.c_int32, _f64p,
+        ]
+        L.ref_vertex_solve.argtypes = lib().orc_vertex_solve.argtypes
+        L.ref_greedy_color.argtypes = [C.c_int32, _i32p, _i32p, C.c_int32, C.c_int32, _i32p]
+        L.ref_morton3d.restype = C.c_uint32
+        L.ref_morton3d.argtypes = [C.c_float, C.c_float, C.c_float]
+        L.ref_run.restype = C.c_int
+        L.ref_run.argtypes = lib().orc_run.argtypes
+        fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        L.ref_vertex_triangle_contact.restype = C.c_float
+        L.ref_vertex_triangle_contact.argtypes = [
+            fp, fp, fp, fp, C.c_float, C.c_float, C.c_float, C.c_float, fp, fp,
+        ]
+        _ref = L
+    return _ref
+
+
+def construct(X, T, rho, dbc, ordering=2, selection=0):
+    """Oracle ``Data::Construct`` precompute.  X: nV x 3, T: nT x 4 (row per entity)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.int32)
+    rho = np.ascontiguousarray(rho, dtype=np.float64)
+    dbc = np.ascontiguousarray(dbc, dtype=np.int32)
+    nV, nT = X.shape[0], T.shape[0]
+    out = dict(
+        m=np.zeros(nV),
+        GP=np.zeros(nT * 12),
+        wg=np.zeros(nT),
+        GVGp=np.zeros(nV + 1, np.int32),
+        GVGe=np.zeros(4 * nT, np.int32),
+        GVGilocal=np.zeros(4 * nT, np.int32),
+        colors=np.zeros(nV, np.int32),
+        Pptr=np.zeros(130, np.int32),
+        Padj=np.zeros(max(nV, 1), np.int32),
+    )
+    nP = C.c_int32()
+    nA = C.c_int32()
+    rc = lib().orc_construct(
+        nV, nT, X, T, rho, dbc, dbc.size, ordering, selection,
+        out["m"], out["GP"], out["wg"], out["GVGp"], out["GVGe"], out["GVGilocal"],
+        out["colors"], out["Pptr"], C.byref(nP), out["Padj"], C.byref(nA),
+    )
+    if rc != 0:
+        raise ValueError(f"orc_construct failed with status {rc}")
+    out["Pptr"] = out["Pptr"][: nP.value + 1].copy()
+    out["Padj"] = out["Padj"][: nA.value].copy()
+    out["GP"] = out["GP"].reshape(nT, 4, 3)
+    return out
+
+
+class OracleVbd:
+    """FP64 CPU VBD integrator on a constructed problem (reference CPU semantics by default)."""
+
+    def __init__(self, X, T, rho, mu, lam, dbc, v=None, aext=None, strategy=4, kD=0.0,
+                 detHZero=1e-7, rho_chebyshev=None, chebyshev_formula=0, semantics=0,
+                 nthreads=0, ordering=2, selection=0, data=None):
+        self.X = np.ascontiguousarray(X, dtype=np.float64)
+        self.T = np.ascontiguousarray(T, dtype=np.int32)
+        nV = self.X.shape[0]
+        self.data = data if data is not None else construct(self.X, self.T, rho, dbc, ordering, selection)
+        self.mu = np.ascontiguousarray(mu, dtype=np.float64)
+        self.lam = np.ascontiguousarray(lam, dtype=np.float64)
+        dbc = np.asarray(dbc, dtype=np.int64)
+        self.x = self.X.copy()
+        self.v = np.zeros((nV, 3)) if v is None else np.array(v, dtype=np.float64)
+        self.aext = np.tile([0.0, 0.0, -9.81], (nV, 1)) if aext is None else np.array(aext, dtype=np.float64)
+        # Data::Construct zeroes velocity and external acceleration on Dirichlet vertices.
+        self.v[dbc] = 0.0
+        self.aext[dbc] = 0.0
+        self.aext = np.ascontiguousarray(self.aext)
+        self.vprev = np.zeros_like(self.v)
+        self.GP = np.ascontiguousarray(self.data["GP"].reshape(-1))
+        P = OrcProblem()
+        P.nV, P.nT = nV, self.T.shape[0]
+        keep = [self.X, self.T, self.data["m"], self.GP, self.data["wg"], self.mu, self.lam,
+                self.data["GVGp"], self.data["GVGe"], self.data["GVGilocal"], self.data["Pptr"],
+                self.data["Padj"], self.aext]
+        self._keep = keep
+        (P.X, P.T, P.m, P.GP, P.wg, P.mu, P.lam, P.GVGp, P.GVGe, P.GVGilocal, P.Pptr, P.Padj,
+         P.aext) = [a.ctypes.data for a in keep]
+        P.nPartitions = self.data["Pptr"].size - 1
+        P.strategy = strategy
+        P.kD = kD
+        P.detHZero = detHZero
+        P.acceleration = 0 if rho_chebyshev is None else 1
+        P.rho = 1.0 if rho_chebyshev is None else rho_chebyshev
+        P.chebyshev_formula = chebyshev_formula
+        P.semantics = semantics
+        P.nthreads = nthreads
+        self.P = P
+
+    def step(self, dt, iterations, substeps=1, nsteps=1, use_ref=False):
+        L = ref() if use_ref else lib()
+        rc = L.ref_run(C.byref(self.P), self.x, self.v, self.vprev.ctypes.data, dt, iterations,
+                       substeps, nsteps) if use_ref else L.orc_run(
+            C.byref(self.P), self.x, self.v, self.vprev.ctypes.data, dt, iterations, substeps,
+            nsteps)
+        if rc != 0:
+            raise RuntimeError(f"oracle run failed: {rc}")
+
+    def objective(self, x, xtilde, dt):
+        return lib().orc_objective(C.byref(self.P), np.ascontiguousarray(x), np.ascontiguousarray(xtilde), dt)
+
+    def gradient(self, x, xtilde, dt):
+        g = np.zeros(self.X.shape[0] * 3)
+        lib().orc_gradient(C.byref(self.P), np.ascontiguousarray(x), np.ascontiguousarray(xtilde), dt, g)
+        return g
+
+
+def primal_graph(T, nV):
+    """CSR vertex graph (neighbours including self, ascending) of a tet mesh."""
+    T = np.asarray(T, dtype=np.int64)
+    rows = np.repeat(T, 4, axis=1).ravel()
+    cols = np.tile(T, (1, 4)).ravel()
+    key = np.unique(rows * nV + cols)
+    r, c = key // nV, key % nV
+    ptr = np.zeros(nV + 1, np.int32)
+    np.add.at(ptr, r + 1, 1)
+    return np.cumsum(ptr).astype(np.int32), c.astype(np.int32)
