@@ -1,0 +1,398 @@
+#!/usr/bin/env python3
+"""Benchmark of the VBD step on one GB300 (replicas on N GPUs under torchrun).
+
+Workload (default ``beam``): the [0,4]x[0,1]x[0,1] beam as a 160x40x40 hex grid split into 6 tets
+per hex (270,641 vertices, 1,536,000 tets), E=5e5, nu=0.48, density 1000, x=0 face pinned,
+initial velocities U(-0.1, 0.1) from a seed, gravity on; Chebyshev acceleration rho=0.95 (the
+reference's weight recurrence), 50 iterations per step, dt=1/60.  A "step" is one time step.
+Metric: vertex-updates/s = free vertices x iterations x substeps x steps / time.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the reference algorithm's CPU implementation (the FP64 oracle port, all
+host threads) on the same workload and prints the same JSON line with "impl": "reference".
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "VBD vertex-updates/s, batched vs single-launch at ≤1e-4 rel err; bwd/fwd time"
+UNIT = "vertex-updates/s"
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+L2_FLUSH_BYTES = 512 << 20
+
+
+def workload_beam(args):
+    from physicsbasedanimationtoolkit_gb300 import meshgen
+
+    w = meshgen.beam_workload(nx=args.nx, ny=args.ny, nz=args.nz, seed=0)
+    return w
+
+
+def make_data(pbat, w, rho=0.95):
+    return (
+        pbat.sim.vbd.Data()
+        .with_volume_mesh(w["X"].T, w["T"].T)
+        .with_material(w["rho"], w["mu"], w["lam"])
+        .with_dirichlet_vertices(w["dbc"])
+        .with_velocity(w["v"].T)
+        .with_chebyshev_acceleration(rho)
+        .construct()
+    )
+
+
+def algorithmic_bytes(data):
+    """Sum over free vertices of (60 + 120 deg(i)) bytes: one vertex-update's FP32/int32 inputs and
+    output (CSR pair 8, mass 4, xt 12, xtilde 12, x read 12 and written 12; per incident tet:
+    (e, ilocal) 8, 4 indices 16, GP 48, (mu, lambda) 8, wg 4, three other positions 36)."""
+    deg = np.diff(data.GVGp)[data.Padj]
+    return int(60 * deg.size + 120 * int(deg.sum()))
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons while running."""
+
+    FIELDS = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peak_hbm():
+    try:
+        p = json.loads(PEAKS_FILE.read_text())
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_from_profiles():
+    """DRAM bytes per sweep launch from the committed ncu summary (None if absent)."""
+    f = ROOT / "profiles" / "vbd_sweep_beam160x40x40.md"
+    try:
+        for line in f.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(w, iterations, seconds_budget=20.0):
+    """The FP64 oracle (port of the reference's CPU integrator) on all host threads, on a bounded
+    sample of the same workload: whole time steps while they fit the budget, else one step with
+    fewer iterations."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib as O
+
+    O.build_oracle()
+    threads = O.lib().orc_num_threads()
+    I = O.OracleVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], v=w["v"], rho_chebyshev=0.95)
+    n_free = I.data["Padj"].size
+    # Probe with a few iterations to size the sample.
+    t0 = time.perf_counter()
+    I.step(1 / 60, 2, 1, 1)
+    t_iter = (time.perf_counter() - t0) / 2
+    iters = max(1, min(iterations, int(seconds_budget / max(t_iter, 1e-9))))
+    steps = max(1, int(seconds_budget / max(t_iter * iters, 1e-9))) if iters == iterations else 1
+    steps = min(steps, 3)
+    t0 = time.perf_counter()
+    I.step(1 / 60, iters, 1, steps)
+    dt = time.perf_counter() - t0
+    updates = n_free * iters * steps
+    sample = (f"{steps} time step(s) x {iters} iterations of the {w['X'].shape[0]}-vertex beam "
+              f"(Chebyshev rho=0.95), FP64, {threads} OpenMP threads")
+    return {"value": updates / dt, "unit": UNIT, "cores": int(threads), "kind": "port", "sample": sample,
+            "seconds": dt}
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation of the path (oracle port), rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    w = workload_beam(args)
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib as O
+
+    O.build_oracle()
+    threads = O.lib().orc_num_threads()
+    I = O.OracleVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], v=w["v"], rho_chebyshev=0.95)
+    n_free = I.data["Padj"].size
+    # Each step is a bounded sample of the workload: one time step with at most `iters` iterations
+    # so that warmup + steps fit a few minutes.
+    t0 = time.perf_counter()
+    I.step(1 / 60, 1, 1, 1)
+    t_iter = time.perf_counter() - t0
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    iters = max(1, min(args.iterations, int(budget / max(t_iter, 1e-9))))
+    for _ in range(args.warmup):
+        I.step(1 / 60, iters, 1, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        I.step(1 / 60, iters, 1, 1)
+    el = time.perf_counter() - t0
+    value = n_free * iters * args.steps / el
+    sample = (f"each step: 1 time step x {iters} of {args.iterations} iterations of the "
+              f"{w['X'].shape[0]}-vertex beam, FP64, {threads} OpenMP threads")
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": config_of(args, w),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(threads), "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def config_of(args, w):
+    return {
+        "workload": f"beam [0,4]x[0,1]^2 {args.nx}x{args.ny}x{args.nz} hexes x 6 tets, Chebyshev rho=0.95",
+        "n_vertices": int(w["X"].shape[0]),
+        "n_tets": int(w["T"].shape[0]),
+        "iterations": args.iterations,
+        "substeps": 1,
+        "dt": 1 / 60,
+        "material": "SNH E=5e5 nu=0.48 rho=1000",
+        "parallelism": f"replicas x{args.gpus}",
+        "l2": "working set > L2 (129 MB); L2 flushed (512 MB write) between timed steps",
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--iterations", type=int, default=50)
+    ap.add_argument("--nx", type=int, default=160)
+    ap.add_argument("--ny", type=int, default=40)
+    ap.add_argument("--nz", type=int, default=40)
+    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    from physicsbasedanimationtoolkit_gb300 import _capi, pbat
+
+    w = workload_beam(args)
+    data = make_data(pbat, w)
+    vbd = pbat.gpu.vbd.Integrator(data)
+    if args.lanes:
+        vbd.lanes_per_vertex = args.lanes
+    L = _capi.lib()
+    h = vbd.handle
+    n_free = vbd.n_free
+    _capi.check(L.pbgb_vbd_set_sweep_timing(h, 1), h)
+    sp = C.c_void_p()
+    _capi.check(L.pbgb_vbd_stream(h, C.byref(sp)), h)
+    stream = torch.cuda.ExternalStream(sp.value)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    dt, iters = 1 / 60, args.iterations
+
+    for _ in range(args.warmup):
+        vbd.step(dt, iters, 1)
+    vbd.synchronize()
+
+    # ---- device-resident throughput -------------------------------------------------------------
+    t_total = 0.0
+    sweep_ms = 0.0
+    sweep_launches = 0
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            flush.add_(1.0)  # L2 flush outside the timed interval
+            torch.cuda.synchronize()
+            ev0[k].record(stream)
+            vbd.step(dt, iters, 1)
+            ev1[k].record(stream)
+            vbd.synchronize()
+            t_total += ev0[k].elapsed_time(ev1[k])
+            ms = C.c_double()
+            nl = C.c_int64()
+            _capi.check(L.pbgb_vbd_sweep_timing(h, C.byref(ms), C.byref(nl)), h)
+            sweep_ms += ms.value
+            sweep_launches += nl.value
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+        t = torch.tensor([t_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_total = float(t.item())
+    ms_per_step = t_total / args.steps
+    updates_per_step = n_free * iters
+    value = world * updates_per_step * args.steps / (t_total * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers -----------------------------------------
+    _capi.check(L.pbgb_vbd_set_sweep_timing(h, 0), h)
+    nV = vbd.n_vertices
+    xh = torch.empty((nV, 3), dtype=torch.float32, pin_memory=True)
+    vh = torch.empty((nV, 3), dtype=torch.float32, pin_memory=True)
+    _capi.check(L.pbgb_vbd_get_positions(h, xh.data_ptr()), h)
+    _capi.check(L.pbgb_vbd_get_velocities(h, vh.data_ptr()), h)
+    vbd.step(dt, iters, 1)  # re-capture the graph without timing events
+    vbd.synchronize()
+    e2e_steps = max(3, args.steps // 2)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        _capi.check(L.pbgb_vbd_set_positions(h, xh.data_ptr()), h)
+        _capi.check(L.pbgb_vbd_set_velocities(h, vh.data_ptr()), h)
+        _capi.check(L.pbgb_vbd_step(h, dt, iters, 1), h)
+        _capi.check(L.pbgb_vbd_get_positions(h, xh.data_ptr()), h)
+        _capi.check(L.pbgb_vbd_get_velocities(h, vh.data_ptr()), h)
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * updates_per_step * e2e_steps / e2e_s
+    io_bytes = nV * 3 * 4 * 2
+
+    if rank == 0:
+        peak, peak_kind = peak_hbm()
+        bytes_per_iter = algorithmic_bytes(data)
+        n_sweeps_per_iter = sweep_launches / max(1, iters * args.steps)
+        bytes_per_launch = bytes_per_iter / max(n_sweeps_per_iter, 1)
+        avg_launch_ms = sweep_ms / max(1, sweep_launches)
+        achieved = bytes_per_launch / (avg_launch_ms * 1e-3) / 1e9
+        traffic = traffic_from_profiles()
+        cpu = None if args.no_cpu_baseline else cpu_baseline(w, iters)
+        launches = vbd.launches_per_step(iters, 1) * args.steps
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_per_step,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic",
+            "config": config_of(args, w),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes,
+                    "d2h_bytes_per_step": io_bytes,
+                    "path": "C ABI pbgb_vbd_set_positions/velocities + step + get_positions/velocities, pinned host buffers"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_kind": peak_kind,
+                         "kernel": "sweep_kernel (per-colour vertex Newton sweep)",
+                         "algorithmic_bytes_per_launch": bytes_per_launch,
+                         "avg_launch_us": avg_launch_ms * 1e3},
+            "cpu_baseline": cpu,
+            "gpu_launches": int(launches),
+            "clocks": clocks.summary(),
+            "n_free_vertices": n_free,
+            "n_colors": vbd.n_colors,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,216 @@
+/*
+ * pbat_gb300.h — C ABI of the GB300-native Vertex Block Descent (VBD) library.
+ *
+ * One hot path of PhysicsBasedAnimationToolkit (PBAT) is implemented here: the VBD time step of
+ * tetrahedral Stable Neo-Hookean meshes, with Chebyshev acceleration, a batched multi-mesh form
+ * and the LBVH used by vertex-triangle contact.  Every entry point takes plain pointers and sizes,
+ * returns an int status (PBGB_OK = 0) and never lets a C++ exception cross the boundary.  Handles
+ * are not thread-safe; each owns one CUDA stream.  Array layouts follow the reference's Eigen
+ * column-major matrices: a "3 x n" array stores entity j at [3j, 3j+1, 3j+2].
+ *
+ * Reference interfaces replaced (paths relative to the reference's `source/pbat/`):
+ *   pbgb_vbd_data_construct      sim::vbd::Data::Construct            sim/vbd/Data.cpp:179-308
+ *   pbgb_vbd_create              gpu::vbd::Integrator(Data const&)    gpu/vbd/Integrator.cu:15-33
+ *                                sim::vbd::Integrator(Data)           sim/vbd/Integrator.cpp:20
+ *   pbgb_vbd_step                Integrator::Step(dt, iters, substeps) gpu/vbd/Integrator.cu:58-61,
+ *                                                                     sim/vbd/Integrator.cpp:22-45
+ *   pbgb_vbd_{get,set}_*         Get/SetPositions, Get/SetVelocities,  gpu/vbd/Integrator.h:95-144
+ *                                SetExternalAcceleration, Set* knobs
+ *   pbgb_vbd_objective/gradient  Integrator::ObjectiveFunction(Grad)  sim/vbd/Integrator.cpp:138-200
+ */
+#ifndef PBAT_GB300_H
+#define PBAT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define PBGB_API __declspec(dllexport)
+#else
+#define PBGB_API __attribute__((visibility("default")))
+#endif
+
+/* Status codes. */
+#define PBGB_OK 0
+#define PBGB_ERR_INVALID_ARGUMENT 1 /* null pointer, bad size, bad enum, rho outside (0,1) ... */
+#define PBGB_ERR_CUDA 2             /* a CUDA runtime call failed (message in pbgb_last_error) */
+#define PBGB_ERR_NONFINITE 3        /* the device detected a NaN/Inf position or velocity */
+#define PBGB_ERR_DEGENERATE 4       /* a tetrahedron with non-positive volume */
+#define PBGB_ERR_PALETTE 5          /* greedy colouring needed more than 128 colours */
+#define PBGB_ERR_NO_DEVICE 6        /* no CUDA device */
+#define PBGB_ERR_TIMEOUT 7          /* a bounded device wait gave up */
+#define PBGB_ERR_INTERNAL 8
+
+/* Enumerations (values match the reference's enums). */
+/* sim/vbd/Enums.h:9-15 */
+#define PBGB_INIT_POSITION 0
+#define PBGB_INIT_INERTIA 1
+#define PBGB_INIT_KINETIC_ENERGY_MINIMUM 2
+#define PBGB_INIT_ADAPTIVE_VBD 3
+#define PBGB_INIT_ADAPTIVE_PBAT 4
+/* sim/vbd/Enums.h:21-28 (only None and Chebyshev are implemented) */
+#define PBGB_ACCEL_NONE 0
+#define PBGB_ACCEL_CHEBYSHEV 1
+/* graph/Enums.h:20-33 */
+#define PBGB_COLOR_ORDER_NATURAL 0
+#define PBGB_COLOR_ORDER_SMALLEST_DEGREE 1
+#define PBGB_COLOR_ORDER_LARGEST_DEGREE 2
+#define PBGB_COLOR_SELECT_LEAST_USED 0
+#define PBGB_COLOR_SELECT_FIRST_AVAILABLE 1
+/* Integrator flavour: which reference integrator's step semantics to reproduce. */
+#define PBGB_SEMANTICS_CPU 0 /* sim::vbd::Integrator: AdaptiveVbd sees vtm1 = v (Integrator.cpp:31-32) */
+#define PBGB_SEMANTICS_GPU 1 /* gpu::vbd::Integrator: vtm1 = velocity of the previous step */
+/* Chebyshev weight recurrence. */
+#define PBGB_CHEBYSHEV_REFERENCE 0 /* omega_k = 4/4 - rho^2 omega_{k-1}, as written in Kernels.h:96-102 */
+#define PBGB_CHEBYSHEV_TEXTBOOK 1  /* omega_k = 4/(4 - rho^2 omega_{k-1}) */
+
+/* Maximum number of colours of the greedy colouring (graph/Color.h:45, palette capacity 128). */
+#define PBGB_MAX_COLORS 128
+
+/*
+ * Data::Construct precompute on the host (FP64), sim/vbd/Data.cpp:179-243.
+ *   X      : 3 x nV rest positions          T     : 4 x nT tetrahedra (int32)
+ *   rhoe   : nT mass densities              dbc   : nDbc Dirichlet vertex indices
+ *   ordering/selection: PBGB_COLOR_ORDER_* / PBGB_COLOR_SELECT_*
+ * Outputs, caller-allocated:
+ *   m[nV] lumped masses; GP[12 nT] shape-function gradients, per tet a row-major 4 x 3 block
+ *   (row a = grad N_a); wg[nT] quadrature weights (volumes); GVGp[nV+1], GVGe[4nT],
+ *   GVGilocal[4nT] vertex->tet adjacency; colors[nV]; Pptr[PBGB_MAX_COLORS+1] and Padj[nV] the
+ *   colour partitions without Dirichlet vertices; *nPartitions, *nPadj their lengths.
+ */
+PBGB_API int pbgb_vbd_data_construct(
+    int32_t nV,
+    int32_t nT,
+    const double* X,
+    const int32_t* T,
+    const double* rhoe,
+    const int32_t* dbc,
+    int32_t nDbc,
+    int32_t ordering,
+    int32_t selection,
+    double* m,
+    double* GP,
+    double* wg,
+    int32_t* GVGp,
+    int32_t* GVGe,
+    int32_t* GVGilocal,
+    int32_t* colors,
+    int32_t* Pptr,
+    int32_t* nPartitions,
+    int32_t* Padj,
+    int32_t* nPadj);
+
+/*
+ * A constructed VBD problem (the content of sim::vbd::Data after Construct).  Pointers are only
+ * read during pbgb_vbd_create.
+ */
+typedef struct pbgb_vbd_desc
+{
+    int32_t n_vertices;
+    int32_t n_tets;
+    const double* x;      /* 3 x nV initial positions (required) */
+    const int32_t* T;     /* 4 x nT tetrahedra (required) */
+    const double* v;      /* 3 x nV velocities (NULL: zero) */
+    const double* aext;   /* 3 x nV external accelerations (NULL: (0,0,-9.81)) */
+    const double* m;      /* nV lumped masses (required) */
+    const double* GP;     /* 12 nT shape-function gradients, row-major 4x3 per tet (required) */
+    const double* wg;     /* nT quadrature weights (required) */
+    const double* mu;     /* nT first Lame coefficients (required) */
+    const double* lambda; /* nT second Lame coefficients (required) */
+    int32_t n_partitions; /* number of colours */
+    const int32_t* Pptr;  /* n_partitions + 1 */
+    const int32_t* Padj;  /* Pptr[n_partitions] free vertices, colour-major */
+    int32_t init_strategy;     /* PBGB_INIT_* (reference default AdaptivePbat) */
+    double kD;                 /* Rayleigh damping (default 0) */
+    double detHZero;           /* near-singular Hessian threshold (default 1e-7) */
+    int32_t acceleration;      /* PBGB_ACCEL_* */
+    double rho;                /* Chebyshev spectral radius estimate, 0 < rho < 1 */
+    int32_t chebyshev_formula; /* PBGB_CHEBYSHEV_* */
+    int32_t semantics;         /* PBGB_SEMANTICS_* */
+} pbgb_vbd_desc;
+
+typedef struct pbgb_vbd pbgb_vbd; /* opaque integrator handle */
+
+/* Upload a problem and build the device layout; *out receives the handle. */
+PBGB_API int pbgb_vbd_create(const pbgb_vbd_desc* desc, pbgb_vbd** out);
+/* Several independent meshes advanced together by one launch sequence per step (batched form).
+ * Vertex/tet indices of each desc are local to its mesh; get/set address the concatenation. */
+PBGB_API int pbgb_vbd_create_batched(const pbgb_vbd_desc* descs, int32_t n_meshes, pbgb_vbd** out);
+PBGB_API int pbgb_vbd_destroy(pbgb_vbd* h);
+
+/* Integrator::Step(dt, iterations, substeps).  Asynchronous on the handle's stream. */
+PBGB_API int pbgb_vbd_step(pbgb_vbd* h, float dt, int32_t iterations, int32_t substeps);
+/* Block until the handle's stream is idle; reports device-side non-finite detection. */
+PBGB_API int pbgb_vbd_synchronize(pbgb_vbd* h);
+
+/* Host copies (3 x nV, float32 like the reference's GpuMatrixX).  get_* synchronize. */
+PBGB_API int pbgb_vbd_get_positions(pbgb_vbd* h, float* x);
+PBGB_API int pbgb_vbd_set_positions(pbgb_vbd* h, const float* x);
+PBGB_API int pbgb_vbd_get_velocities(pbgb_vbd* h, float* v);
+PBGB_API int pbgb_vbd_set_velocities(pbgb_vbd* h, const float* v);
+PBGB_API int pbgb_vbd_set_external_acceleration(pbgb_vbd* h, const float* aext);
+/* Device-pointer variants (3 x nV float32 on the handle's device), stream-ordered. */
+PBGB_API int pbgb_vbd_get_positions_device(pbgb_vbd* h, float* x_dev);
+PBGB_API int pbgb_vbd_set_positions_device(pbgb_vbd* h, const float* x_dev);
+
+/* Knobs (gpu/vbd/Integrator.h:110-134). */
+PBGB_API int pbgb_vbd_set_detH_zero(pbgb_vbd* h, float zero);
+PBGB_API int pbgb_vbd_set_damping(pbgb_vbd* h, float kD);
+PBGB_API int pbgb_vbd_set_strategy(pbgb_vbd* h, int32_t strategy);
+/* Threads per block of the vertex sweep (the reference clamps to [32, 256]). */
+PBGB_API int pbgb_vbd_set_block_size(pbgb_vbd* h, int32_t block_size);
+/* Lanes cooperating on one vertex: 1, 2, 4, 8, 16 or 32 (0 = autotuned). */
+PBGB_API int pbgb_vbd_set_lanes_per_vertex(pbgb_vbd* h, int32_t lanes);
+PBGB_API int pbgb_vbd_set_scene_bounding_box(pbgb_vbd* h, const float* min3, const float* max3);
+
+/* Sizes and launch bookkeeping. */
+PBGB_API int pbgb_vbd_sizes(pbgb_vbd* h, int32_t* n_vertices, int32_t* n_tets, int32_t* n_free, int32_t* n_colors);
+/* Number of kernels one pbgb_vbd_step(iterations, substeps) launches. */
+PBGB_API int pbgb_vbd_launches_per_step(pbgb_vbd* h, int32_t iterations, int32_t substeps, int64_t* launches);
+/* Sweep timing (off by default): when enabled, each captured step records a CUDA event pair around
+ * the colour sweeps of every iteration.  pbgb_vbd_sweep_timing returns, for the last step, the
+ * summed sweep intervals in milliseconds and the number of sweep kernel launches they cover. */
+PBGB_API int pbgb_vbd_set_sweep_timing(pbgb_vbd* h, int32_t enable);
+PBGB_API int pbgb_vbd_sweep_timing(pbgb_vbd* h, double* milliseconds, int64_t* sweep_launches);
+/* The handle's CUDA stream (cudaStream_t) so callers can order their own work after a step. */
+PBGB_API int pbgb_vbd_stream(pbgb_vbd* h, void** stream);
+
+/* Backward-Euler objective f(x) = 1/2 |x - xtilde|_M^2 + dt^2 sum wg Psi and its gradient at
+ * the current positions against the last step's inertial target; FP64 device reductions. */
+PBGB_API int pbgb_vbd_objective(pbgb_vbd* h, double dt, double* f);
+PBGB_API int pbgb_vbd_gradient(pbgb_vbd* h, double dt, double* grad /* 3 x nV */);
+
+/* Message of the last failing call on h (or of the last failing handle-less call if h is NULL). */
+PBGB_API const char* pbgb_last_error(pbgb_vbd* h);
+
+/* Host self-check of the closed-form vertex block (FP64): accumulates n incident tets and
+ * applies damping, inertia and the Newton step exactly like the device sweep.  Arguments as the
+ * oracle's per-vertex solve: xe n x 12 (3x4 column-major per tet), GPs n x 12 (row-major 4x3). */
+PBGB_API int pbgb_debug_vertex_block(
+    int32_t n,
+    const double* xe,
+    const double* GPs,
+    const int32_t* il,
+    const double* wg,
+    const double* mu,
+    const double* lambda,
+    const double* xt,
+    const double* xtilde,
+    double m,
+    double kD,
+    double h,
+    double h2,
+    double detHZero,
+    double* x,
+    double* g,
+    double* H);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBAT_GB300_H */

@@ -1,0 +1,164 @@
+"""Handle management shared by ``pbat.sim.vbd.Integrator``, ``pbat.gpu.vbd.Integrator`` and the
+batched integrator: builds ``pbgb_vbd_desc`` records from constructed ``Data`` and wraps the C ABI.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+
+SEMANTICS_CPU = 0
+SEMANTICS_GPU = 1
+
+_UNSUPPORTED = {2: "Anderson", 3: "Nesterov", 4: "Broyden", 5: "TrustRegion"}
+
+
+def make_desc(data, semantics):
+    """A ``pbgb_vbd_desc`` for a constructed ``Data`` plus the arrays it points into."""
+    if not getattr(data, "_constructed", False):
+        raise ValueError("Data must be constructed (call Data.construct()) before creating an integrator")
+    accel = int(data.eAcceleration)
+    if accel in _UNSUPPORTED:
+        raise NotImplementedError(
+            f"{_UNSUPPORTED[accel]} acceleration is not part of this library's VBD path "
+            "(Base and Chebyshev are)"
+        )
+    nV, nT = data.X.shape[1], data.E.shape[1]
+    keep = dict(
+        x=_capi.f64(np.asarray(data.x).T),
+        T=_capi.i32(np.asarray(data.E).T),
+        v=_capi.f64(np.asarray(data.v).T),
+        aext=_capi.f64(np.asarray(data.aext).T),
+        m=_capi.f64(data.m),
+        GP=_capi.f64(data._GP_rows),
+        wg=_capi.f64(data.wg),
+        mu=_capi.f64(data.lame[0]),
+        lam=_capi.f64(data.lame[1]),
+        Pptr=_capi.i32(data.Pptr),
+        Padj=_capi.i32(data.Padj),
+    )
+    d = _capi.VbdDesc()
+    d.n_vertices = nV
+    d.n_tets = nT
+    for k, a in keep.items():
+        setattr(d, k, a.ctypes.data)
+    d.n_partitions = int(data.Pptr.size - 1)
+    d.init_strategy = int(data.strategy)
+    d.kD = float(data.kD)
+    d.detHZero = float(data.detH_zero)
+    d.acceleration = 1 if accel == 1 else 0
+    d.rho = float(data.rho)
+    d.chebyshev_formula = int(getattr(data, "chebyshev_formula", 0))
+    d.semantics = semantics
+    return d, keep
+
+
+class IntegratorBase:
+    """Owns one ``pbgb_vbd`` handle."""
+
+    def __init__(self, data, semantics, batch=None):
+        L = _capi.lib()
+        self.data = data
+        self._semantics = semantics
+        h = C.c_void_p()
+        if batch is None:
+            desc, self._keep = make_desc(data, semantics)
+            rc = L.pbgb_vbd_create(C.byref(desc), C.byref(h))
+        else:
+            descs = (_capi.VbdDesc * len(batch))()
+            self._keep = []
+            for b, dat in enumerate(batch):
+                dsc, keep = make_desc(dat, semantics)
+                descs[b] = dsc
+                self._keep.append(keep)
+            rc = L.pbgb_vbd_create_batched(descs, len(batch), C.byref(h))
+        _capi.check(rc)
+        self._h = h
+        self._keep = None  # the library copied everything during create
+        nV, nT, nF, nC = (C.c_int32() for _ in range(4))
+        _capi.check(L.pbgb_vbd_sizes(h, C.byref(nV), C.byref(nT), C.byref(nF), C.byref(nC)), h)
+        self.n_vertices, self.n_tets, self.n_free, self.n_colors = nV.value, nT.value, nF.value, nC.value
+        ref = data if batch is None else batch[0]
+        self._strategy = ref.strategy
+        self._kD = ref.kD
+        self._detH = ref.detH_zero
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _capi.lib().pbgb_vbd_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _step(self, dt, iterations, substeps):
+        _capi.check(_capi.lib().pbgb_vbd_step(self._h, float(dt), int(iterations), int(substeps)), self._h)
+
+    def synchronize(self):
+        _capi.check(_capi.lib().pbgb_vbd_synchronize(self._h), self._h)
+
+    def _get(self, which):
+        out = np.empty((self.n_vertices, 3), dtype=np.float32)
+        fn = {"x": "pbgb_vbd_get_positions", "v": "pbgb_vbd_get_velocities"}[which]
+        _capi.check(getattr(_capi.lib(), fn)(self._h, out.ctypes.data), self._h)
+        return out.T.copy()
+
+    def _set(self, which, value):
+        a = np.asarray(value, dtype=np.float32)
+        if a.shape != (3, self.n_vertices):
+            raise ValueError(f"expected an array of shape (3, {self.n_vertices})")
+        buf = np.ascontiguousarray(a.T)
+        fn = {
+            "x": "pbgb_vbd_set_positions",
+            "v": "pbgb_vbd_set_velocities",
+            "a": "pbgb_vbd_set_external_acceleration",
+        }[which]
+        _capi.check(getattr(_capi.lib(), fn)(self._h, buf.ctypes.data), self._h)
+        # set_* copies from pageable host memory on the handle's stream; wait so `buf` may die.
+        self.synchronize()
+
+    def _set_strategy(self, s):
+        _capi.check(_capi.lib().pbgb_vbd_set_strategy(self._h, int(s)), self._h)
+        self._strategy = s
+
+    def _set_kD(self, kD):
+        _capi.check(_capi.lib().pbgb_vbd_set_damping(self._h, float(kD)), self._h)
+        self._kD = float(kD)
+
+    def _set_detH(self, z):
+        _capi.check(_capi.lib().pbgb_vbd_set_detH_zero(self._h, float(z)), self._h)
+        self._detH = float(z)
+
+    # -- extras beyond the reference API --------------------------------------------------------
+    @property
+    def lanes_per_vertex(self):
+        return getattr(self, "_lanes", 0)
+
+    @lanes_per_vertex.setter
+    def lanes_per_vertex(self, lanes):
+        _capi.check(_capi.lib().pbgb_vbd_set_lanes_per_vertex(self._h, int(lanes)), self._h)
+        self._lanes = int(lanes)
+
+    def launches_per_step(self, iterations, substeps=1):
+        n = C.c_int64()
+        _capi.check(_capi.lib().pbgb_vbd_launches_per_step(self._h, int(iterations), int(substeps), C.byref(n)), self._h)
+        return n.value
+
+    def objective(self, dt):
+        """Backward-Euler objective at the current positions (FP64 device reduction)."""
+        f = C.c_double()
+        _capi.check(_capi.lib().pbgb_vbd_objective(self._h, float(dt), C.byref(f)), self._h)
+        return f.value
+
+    def gradient(self, dt):
+        g = np.zeros((self.n_vertices, 3))
+        _capi.check(_capi.lib().pbgb_vbd_gradient(self._h, float(dt), g.ctypes.data), self._h)
+        return g.ravel()

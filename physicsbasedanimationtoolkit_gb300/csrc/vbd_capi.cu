@@ -1,0 +1,948 @@
+// The VBD integrator object behind the C ABI (include/pbat_gb300.h): device layout, step
+// orchestration captured in CUDA graphs, host/device copies, and the extern "C" entry points.
+//
+// Reference counterpart: pbat::gpu::impl::vbd::Integrator (gpu/impl/vbd/Integrator.cu:22-347)
+// and the public pimpl pbat::gpu::vbd::Integrator (gpu/vbd/Integrator.cu).  Differences by design:
+// one stream per handle (the reference creates one and never uses it), the whole step replayed
+// from a CUDA graph, tets packed into 64-byte records, the in-place colour sweep (no xb copy-back
+// pass), and several meshes concatenated into one system for the batched form.
+#include "pbat_gb300.h"
+#include "vbd_construct.h"
+#include "vbd_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace pbgb {
+
+namespace {
+
+thread_local std::string gLastError;
+
+struct CudaFailure
+{
+    cudaError_t err;
+    char const* what;
+};
+
+inline void check(cudaError_t e, char const* what)
+{
+    if (e != cudaSuccess)
+        throw CudaFailure{e, what};
+}
+
+template <class T>
+class DeviceArray
+{
+  public:
+    DeviceArray() = default;
+    DeviceArray(DeviceArray const&) = delete;
+    DeviceArray& operator=(DeviceArray const&) = delete;
+    ~DeviceArray() { release(); }
+    void allocate(size_t n)
+    {
+        release();
+        n_ = n;
+        if (n > 0)
+            check(cudaMalloc(reinterpret_cast<void**>(&p_), n * sizeof(T)), "cudaMalloc");
+    }
+    void upload(T const* h, size_t n, cudaStream_t s)
+    {
+        if (n > 0)
+            check(cudaMemcpyAsync(p_, h, n * sizeof(T), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync H2D");
+    }
+    void release()
+    {
+        if (p_)
+            cudaFree(p_);
+        p_ = nullptr;
+        n_ = 0;
+    }
+    T* get() const { return p_; }
+    size_t size() const { return n_; }
+
+  private:
+    T* p_     = nullptr;
+    size_t n_ = 0;
+};
+
+} // namespace
+
+class VbdSystem
+{
+  public:
+    // Host metadata
+    int32_t nV = 0, nT = 0, nFree = 0, nColors = 0;
+    std::vector<int32_t> colorPtr; // solve-list ranges per colour
+    double meanDegree = 0.0;
+    int32_t strategy  = PBGB_INIT_ADAPTIVE_PBAT;
+    float kD = 0.f, detHZero = 1e-7f;
+    int32_t acceleration = PBGB_ACCEL_NONE, chebFormula = PBGB_CHEBYSHEV_REFERENCE, semantics = 0;
+    double rho  = 1.0;
+    int32_t lanes = 0, block = 256;
+    float sceneMin[3] = {0, 0, 0}, sceneMax[3] = {0, 0, 0};
+    std::string lastError;
+
+    // Device state
+    cudaStream_t stream = nullptr;
+    DeviceArray<float4> x, xt, xtilde, v, aext, vprev, xkm1, xkm2;
+    DeviceArray<float> m, staging;
+    DeviceArray<int4> tv;
+    DeviceArray<float4> tg;
+    DeviceArray<int32_t> solve, incPtr, flags;
+    DeviceArray<uint32_t> inc;
+    DeviceArray<double> red, gradBuf;
+
+    // Sweep timing: with `profiling` on, the captured step records an event pair around the colour
+    // sweeps of every iteration (event-record nodes in the graph).
+    bool profiling = false;
+    std::vector<cudaEvent_t> evBegin, evEnd;
+
+    // Graph cache for Step(dt, iterations, substeps)
+    cudaGraphExec_t graph = nullptr;
+    float gDt = -1.f;
+    int32_t gIters = -1, gSub = -1;
+    bool graphValid = false;
+
+    ~VbdSystem()
+    {
+        releaseEvents();
+        if (graph)
+            cudaGraphExecDestroy(graph);
+        if (stream)
+            cudaStreamDestroy(stream);
+    }
+
+    void invalidate() { graphValid = false; }
+
+    void releaseEvents()
+    {
+        for (auto e : evBegin)
+            cudaEventDestroy(e);
+        for (auto e : evEnd)
+            cudaEventDestroy(e);
+        evBegin.clear();
+        evEnd.clear();
+    }
+
+    void ensureEvents(size_t n)
+    {
+        while (evBegin.size() < n)
+        {
+            cudaEvent_t a = nullptr, b = nullptr;
+            check(cudaEventCreate(&a), "cudaEventCreate");
+            evBegin.push_back(a);
+            check(cudaEventCreate(&b), "cudaEventCreate");
+            evEnd.push_back(b);
+        }
+    }
+
+    // Sum of the sweep intervals of the last replayed step (stream must be idle).
+    double sweepMilliseconds(int32_t iterations, int32_t substeps)
+    {
+        double total = 0.0;
+        size_t const n = size_t(iterations) * size_t(substeps);
+        for (size_t k = 0; k < n && k < evBegin.size(); ++k)
+        {
+            float ms = 0.f;
+            check(cudaEventElapsedTime(&ms, evBegin[k], evEnd[k]), "cudaEventElapsedTime");
+            total += ms;
+        }
+        return total;
+    }
+
+    int lanesToUse() const
+    {
+        if (lanes > 0)
+            return lanes;
+        // Default: enough lanes that a colour fills the GPU, few enough that the incidence loop
+        // keeps each lane busy.
+        int const perColor = nColors > 0 ? nFree / nColors : nFree;
+        if (perColor < 4096)
+            return 32;
+        if (meanDegree > 12.0)
+            return 8;
+        return 4;
+    }
+
+    void build(pbgb_vbd_desc const* descs, int32_t nMeshes)
+    {
+        // Totals and validation.
+        int64_t totV = 0, totT = 0, totFree = 0;
+        int32_t maxC = 0;
+        for (int32_t b = 0; b < nMeshes; ++b)
+        {
+            auto const& d = descs[b];
+            if (d.n_vertices < 0 || d.n_tets < 0 || !d.x || (d.n_tets > 0 && !d.T) || !d.m ||
+                (d.n_tets > 0 && (!d.GP || !d.wg || !d.mu || !d.lambda)) || d.n_partitions < 0 ||
+                d.n_partitions > kMaxColors || !d.Pptr || (d.Pptr[d.n_partitions] > 0 && !d.Padj))
+                throw std::invalid_argument("pbgb_vbd_desc: missing or invalid field");
+            for (int64_t k = 0; k < int64_t(d.n_tets) * 4; ++k)
+                if (d.T[k] < 0 || d.T[k] >= d.n_vertices)
+                    throw std::invalid_argument("pbgb_vbd_desc: tetrahedron index out of range");
+            for (int32_t k = 0; k < d.Pptr[d.n_partitions]; ++k)
+                if (d.Padj[k] < 0 || d.Padj[k] >= d.n_vertices)
+                    throw std::invalid_argument("pbgb_vbd_desc: partition vertex out of range");
+            if (d.acceleration == PBGB_ACCEL_CHEBYSHEV && !(d.rho > 0.0 && d.rho < 1.0))
+                throw std::invalid_argument("Expected 0 < rho < 1");
+            if (d.acceleration != PBGB_ACCEL_NONE && d.acceleration != PBGB_ACCEL_CHEBYSHEV)
+                throw std::invalid_argument("pbgb_vbd_desc: unsupported acceleration strategy");
+            if (d.init_strategy < 0 || d.init_strategy > 4)
+                throw std::invalid_argument("pbgb_vbd_desc: invalid initialization strategy");
+            totV += d.n_vertices;
+            totT += d.n_tets;
+            totFree += d.Pptr[d.n_partitions];
+            maxC = std::max(maxC, d.n_partitions);
+        }
+        if (totV > INT32_MAX || totT >= (int64_t(1) << 30) || totT * 4 > INT32_MAX)
+            throw std::invalid_argument("pbgb_vbd_desc: system too large for 32-bit indexing");
+        nV      = int32_t(totV);
+        nT      = int32_t(totT);
+        nFree   = int32_t(totFree);
+        nColors = maxC;
+        // Settings come from the first mesh (one step size and solver for the whole batch).
+        auto const& d0 = descs[0];
+        strategy       = d0.init_strategy;
+        kD             = float(d0.kD);
+        detHZero       = float(d0.detHZero);
+        acceleration   = d0.acceleration;
+        rho            = d0.rho;
+        chebFormula    = d0.chebyshev_formula;
+        semantics      = d0.semantics;
+
+        // Host staging of the concatenated layout.
+        std::vector<float4> hx(nV), hv(nV), ha(nV);
+        std::vector<float> hm(nV);
+        std::vector<int4> htv(nT);
+        std::vector<float4> htg(size_t(nT) * 3);
+        std::vector<int32_t> deg(nV, 0);
+        int32_t v0 = 0, t0 = 0;
+        for (int32_t b = 0; b < nMeshes; ++b)
+        {
+            auto const& d = descs[b];
+            for (int32_t i = 0; i < d.n_vertices; ++i)
+            {
+                double const* p = d.x + 3 * size_t(i);
+                hx[v0 + i]      = make_float4(float(p[0]), float(p[1]), float(p[2]), 0.f);
+                if (d.v)
+                {
+                    double const* q = d.v + 3 * size_t(i);
+                    hv[v0 + i]      = make_float4(float(q[0]), float(q[1]), float(q[2]), 0.f);
+                }
+                else
+                    hv[v0 + i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (d.aext)
+                {
+                    double const* q = d.aext + 3 * size_t(i);
+                    ha[v0 + i]      = make_float4(float(q[0]), float(q[1]), float(q[2]), 0.f);
+                }
+                else
+                    ha[v0 + i] = make_float4(0.f, 0.f, -9.81f, 0.f);
+                hm[v0 + i] = float(d.m[i]);
+            }
+            for (int32_t e = 0; e < d.n_tets; ++e)
+            {
+                int32_t const* t = d.T + 4 * size_t(e);
+                htv[t0 + e]      = make_int4(t[0] + v0, t[1] + v0, t[2] + v0, t[3] + v0);
+                double const* G  = d.GP + 12 * size_t(e);
+                double const w = d.wg[e], mu = d.mu[e], la = d.lambda[e];
+                htg[3 * size_t(t0 + e) + 0] = make_float4(float(G[3]), float(G[4]), float(G[5]), float(w * mu));
+                htg[3 * size_t(t0 + e) + 1] = make_float4(float(G[6]), float(G[7]), float(G[8]), float(w * la));
+                htg[3 * size_t(t0 + e) + 2] =
+                    make_float4(float(G[9]), float(G[10]), float(G[11]), float(1.0 + mu / la));
+                for (int q = 0; q < 4; ++q)
+                    deg[t[q] + v0]++;
+            }
+            v0 += d.n_vertices;
+            t0 += d.n_tets;
+        }
+        // Incidences per vertex, tets ascending (counting sort over the global tet index).
+        std::vector<int32_t> vPtr(size_t(nV) + 1, 0);
+        for (int32_t i = 0; i < nV; ++i)
+            vPtr[i + 1] = vPtr[i] + deg[i];
+        std::vector<uint32_t> vInc(static_cast<size_t>(vPtr[nV]));
+        {
+            std::vector<int32_t> cur(vPtr.begin(), vPtr.end() - 1);
+            for (int32_t e = 0; e < nT; ++e)
+            {
+                int4 const t   = htv[e];
+                int const a[4] = {t.x, t.y, t.z, t.w};
+                for (int q = 0; q < 4; ++q)
+                    vInc[cur[a[q]]++] = (uint32_t(e) << 2) | uint32_t(q);
+            }
+        }
+        // Colour-major solve list: colour c = union of every mesh's partition c; inside a colour,
+        // stable order by decreasing degree so that lanes of a warp see similar trip counts.
+        std::vector<int32_t> hsolve;
+        hsolve.reserve(nFree);
+        colorPtr.assign(size_t(nColors) + 1, 0);
+        for (int32_t c = 0; c < nColors; ++c)
+        {
+            size_t const start = hsolve.size();
+            v0                 = 0;
+            for (int32_t b = 0; b < nMeshes; ++b)
+            {
+                auto const& d = descs[b];
+                if (c < d.n_partitions)
+                    for (int32_t k = d.Pptr[c]; k < d.Pptr[c + 1]; ++k)
+                        hsolve.push_back(d.Padj[k] + v0);
+                v0 += d.n_vertices;
+            }
+            std::stable_sort(hsolve.begin() + start, hsolve.end(), [&](int32_t a, int32_t b) {
+                return deg[a] > deg[b];
+            });
+            colorPtr[c + 1] = int32_t(hsolve.size());
+        }
+        std::vector<int32_t> hIncPtr(size_t(nFree) + 1, 0);
+        std::vector<uint32_t> hInc;
+        hInc.reserve(vInc.size());
+        int64_t degSum = 0;
+        for (int32_t s = 0; s < nFree; ++s)
+        {
+            int32_t const i = hsolve[s];
+            hInc.insert(hInc.end(), vInc.begin() + vPtr[i], vInc.begin() + vPtr[i + 1]);
+            hIncPtr[s + 1] = int32_t(hInc.size());
+            degSum += deg[i];
+        }
+        meanDegree = nFree > 0 ? double(degSum) / nFree : 0.0;
+
+        // Device allocation and upload.
+        check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        x.allocate(nV);
+        xt.allocate(nV);
+        xtilde.allocate(nV);
+        v.allocate(nV);
+        aext.allocate(nV);
+        vprev.allocate(nV);
+        m.allocate(nV);
+        staging.allocate(size_t(nV) * 3);
+        tv.allocate(nT);
+        tg.allocate(size_t(nT) * 3);
+        solve.allocate(nFree);
+        incPtr.allocate(size_t(nFree) + 1);
+        inc.allocate(hInc.size());
+        flags.allocate(4);
+        red.allocate(1);
+        if (acceleration == PBGB_ACCEL_CHEBYSHEV)
+        {
+            xkm1.allocate(nV);
+            xkm2.allocate(nV);
+        }
+        x.upload(hx.data(), nV, stream);
+        v.upload(hv.data(), nV, stream);
+        aext.upload(ha.data(), nV, stream);
+        m.upload(hm.data(), nV, stream);
+        tv.upload(htv.data(), nT, stream);
+        tg.upload(htg.data(), htg.size(), stream);
+        solve.upload(hsolve.data(), nFree, stream);
+        incPtr.upload(hIncPtr.data(), hIncPtr.size(), stream);
+        inc.upload(hInc.data(), hInc.size(), stream);
+        if (nV > 0)
+        {
+            check(cudaMemcpyAsync(xt.get(), x.get(), sizeof(float4) * nV, cudaMemcpyDeviceToDevice, stream), "copy");
+            check(cudaMemsetAsync(vprev.get(), 0, sizeof(float4) * nV, stream), "memset");
+            check(cudaMemsetAsync(xtilde.get(), 0, sizeof(float4) * nV, stream), "memset");
+        }
+        check(cudaMemsetAsync(flags.get(), 0, sizeof(int32_t) * 4, stream), "memset");
+        // The host staging vectors die at the end of this scope: wait for the uploads.
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    }
+
+    SubstepParams substepParams(float h) const
+    {
+        SubstepParams p{};
+        p.x            = x.get();
+        p.xt           = xt.get();
+        p.xtilde       = xtilde.get();
+        p.v            = v.get();
+        p.aext         = aext.get();
+        p.vprev        = vprev.get();
+        p.m            = m.get();
+        p.flags        = flags.get();
+        p.n            = nV;
+        p.h            = h;
+        p.h2           = h * h;
+        p.strategy     = strategy;
+        p.gpuSemantics = semantics == PBGB_SEMANTICS_GPU ? 1 : 0;
+        return p;
+    }
+
+    // Enqueue one full step on `stream` (captured into a graph by step()).
+    void enqueueStep(float dt, int32_t iterations, int32_t substeps)
+    {
+        float const h  = dt / float(substeps);
+        float const h2 = h * h;
+        SubstepParams const sp = substepParams(h);
+        SweepParams w{};
+        w.x        = x.get();
+        w.xt       = xt.get();
+        w.xtilde   = xtilde.get();
+        w.tv       = tv.get();
+        w.tg       = tg.get();
+        w.solve    = solve.get();
+        w.incPtr   = incPtr.get();
+        w.inc      = inc.get();
+        w.h        = h;
+        w.h2       = h2;
+        w.kD       = kD;
+        w.detHZero = detHZero;
+        int const L = lanesToUse();
+        if (profiling)
+            ensureEvents(size_t(iterations) * size_t(substeps));
+        for (int32_t s = 0; s < substeps; ++s)
+        {
+            check(launch_begin_substep(sp, stream), "begin_substep");
+            double omega      = 0.0;
+            double const rho2 = rho * rho;
+            for (int32_t k = 0; k < iterations; ++k)
+            {
+                size_t const slot = size_t(s) * size_t(iterations) + size_t(k);
+                if (profiling)
+                    check(cudaEventRecord(evBegin[slot], stream), "cudaEventRecord");
+                for (int32_t c = 0; c < nColors; ++c)
+                {
+                    w.begin = colorPtr[c];
+                    w.end   = colorPtr[c + 1];
+                    check(launch_sweep(w, L, block, stream), "sweep");
+                }
+                if (profiling)
+                    check(cudaEventRecord(evEnd[slot], stream), "cudaEventRecord");
+                if (acceleration == PBGB_ACCEL_CHEBYSHEV)
+                {
+                    omega = chebyshev_omega<double>(k, rho2, omega, chebFormula);
+                    ChebyshevParams cp{x.get(), xkm1.get(), xkm2.get(), nV, k, float(omega)};
+                    check(launch_chebyshev(cp, stream), "chebyshev");
+                }
+            }
+            check(launch_end_substep(sp, stream), "end_substep");
+        }
+    }
+
+    int64_t launchesPerStep(int32_t iterations, int32_t substeps) const
+    {
+        int64_t perIter = 0;
+        for (int32_t c = 0; c < nColors; ++c)
+            perIter += colorPtr[c + 1] > colorPtr[c] ? 1 : 0;
+        perIter += acceleration == PBGB_ACCEL_CHEBYSHEV && nV > 0 ? 1 : 0;
+        return int64_t(substeps) * (2 * (nV > 0 ? 1 : 0) + int64_t(iterations) * perIter);
+    }
+
+    void step(float dt, int32_t iterations, int32_t substeps)
+    {
+        if (!graphValid || dt != gDt || iterations != gIters || substeps != gSub)
+        {
+            if (graph)
+            {
+                cudaGraphExecDestroy(graph);
+                graph = nullptr;
+            }
+            cudaGraph_t g = nullptr;
+            check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+            try
+            {
+                enqueueStep(dt, iterations, substeps);
+            }
+            catch (...)
+            {
+                cudaStreamEndCapture(stream, &g);
+                if (g)
+                    cudaGraphDestroy(g);
+                throw;
+            }
+            check(cudaStreamEndCapture(stream, &g), "cudaStreamEndCapture");
+            cudaError_t const e = cudaGraphInstantiate(&graph, g, 0);
+            cudaGraphDestroy(g);
+            check(e, "cudaGraphInstantiate");
+            gDt        = dt;
+            gIters     = iterations;
+            gSub       = substeps;
+            graphValid = true;
+        }
+        check(cudaGraphLaunch(graph, stream), "cudaGraphLaunch");
+    }
+
+    int synchronize()
+    {
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+        int32_t f = 0;
+        check(cudaMemcpy(&f, flags.get(), sizeof(int32_t), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        if (f != 0)
+        {
+            check(cudaMemset(flags.get(), 0, sizeof(int32_t)), "cudaMemset");
+            lastError = "non-finite positions or velocities detected on the device";
+            return kNonFinite;
+        }
+        return kOk;
+    }
+
+    void getVec(DeviceArray<float4> const& src, float* host)
+    {
+        check(launch_unpack3(src.get(), staging.get(), nV, stream), "unpack");
+        check(cudaMemcpyAsync(host, staging.get(), sizeof(float) * 3 * size_t(nV), cudaMemcpyDeviceToHost, stream), "D2H");
+    }
+    void setVec(DeviceArray<float4>& dst, float const* host)
+    {
+        check(cudaMemcpyAsync(staging.get(), host, sizeof(float) * 3 * size_t(nV), cudaMemcpyHostToDevice, stream), "H2D");
+        check(launch_pack3(staging.get(), dst.get(), nV, stream), "pack");
+    }
+
+    EnergyParams energyParams(double dt, double* out) const
+    {
+        EnergyParams p{};
+        p.x      = x.get();
+        p.xtilde = xtilde.get();
+        p.m      = m.get();
+        p.tv     = tv.get();
+        p.tg     = tg.get();
+        p.nV     = nV;
+        p.nT     = nT;
+        p.dt2    = dt * dt;
+        p.out    = out;
+        return p;
+    }
+};
+
+} // namespace pbgb
+
+struct pbgb_vbd
+{
+    pbgb::VbdSystem sys;
+};
+
+namespace {
+
+using pbgb::kCuda;
+using pbgb::kInternal;
+using pbgb::kInvalid;
+using pbgb::kOk;
+using pbgb::check;
+
+int fail(pbgb_vbd* h, int code, std::string const& msg)
+{
+    pbgb::gLastError = msg;
+    if (h)
+        h->sys.lastError = msg;
+    return code;
+}
+
+// Runs `f` with C++ exceptions mapped to status codes.
+template <class F>
+int guarded(pbgb_vbd* h, F&& f)
+{
+    try
+    {
+        return f();
+    }
+    catch (pbgb::CudaFailure const& e)
+    {
+        return fail(h, kCuda, std::string(e.what) + ": " + cudaGetErrorString(e.err));
+    }
+    catch (std::invalid_argument const& e)
+    {
+        return fail(h, kInvalid, e.what());
+    }
+    catch (std::bad_alloc const&)
+    {
+        return fail(h, kInternal, "host allocation failed");
+    }
+    catch (std::exception const& e)
+    {
+        return fail(h, kInternal, e.what());
+    }
+    catch (...)
+    {
+        return fail(h, kInternal, "unknown error");
+    }
+}
+
+int create_impl(pbgb_vbd_desc const* descs, int32_t n, pbgb_vbd** out)
+{
+    if (!descs || n < 1 || !out)
+        return fail(nullptr, kInvalid, "pbgb_vbd_create: null argument or empty batch");
+    *out = nullptr;
+    int devices = 0;
+    if (cudaGetDeviceCount(&devices) != cudaSuccess || devices < 1)
+    {
+        cudaGetLastError();
+        return fail(nullptr, pbgb::kNoDevice, "no CUDA device available");
+    }
+    auto h = std::make_unique<pbgb_vbd>();
+    int const rc = guarded(h.get(), [&] {
+        h->sys.build(descs, n);
+        return int(kOk);
+    });
+    if (rc != kOk)
+    {
+        pbgb::gLastError = h->sys.lastError;
+        return rc;
+    }
+    *out = h.release();
+    return kOk;
+}
+
+} // namespace
+
+extern "C" {
+
+PBGB_API int pbgb_vbd_data_construct(
+    int32_t nV,
+    int32_t nT,
+    const double* X,
+    const int32_t* T,
+    const double* rhoe,
+    const int32_t* dbc,
+    int32_t nDbc,
+    int32_t ordering,
+    int32_t selection,
+    double* m,
+    double* GP,
+    double* wg,
+    int32_t* GVGp,
+    int32_t* GVGe,
+    int32_t* GVGilocal,
+    int32_t* colors,
+    int32_t* Pptr,
+    int32_t* nPartitions,
+    int32_t* Padj,
+    int32_t* nPadj)
+{
+    if (!m || !GP || !wg || !GVGp || !GVGe || !GVGilocal || !colors || !Pptr || !nPartitions || !Padj ||
+        !nPadj || (nDbc > 0 && !dbc))
+        return fail(nullptr, kInvalid, "pbgb_vbd_data_construct: null output");
+    return guarded(nullptr, [&] {
+        pbgb::ConstructIn in{nV, nT, X, T, rhoe, dbc, nDbc, ordering, selection};
+        pbgb::ConstructOut out{m, GP, wg, GVGp, GVGe, GVGilocal, colors, Pptr, Padj, 0, 0};
+        int const rc = pbgb::construct(in, out);
+        if (rc == pbgb::kDegenerate)
+            return fail(nullptr, rc, "tetrahedron with non-positive volume");
+        if (rc == pbgb::kPalette)
+            return fail(nullptr, rc, "greedy colouring needs more than 128 colours");
+        if (rc != kOk)
+            return fail(nullptr, rc, "invalid mesh description");
+        *nPartitions = out.nPartitions;
+        *nPadj       = out.nPadj;
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_create(const pbgb_vbd_desc* desc, pbgb_vbd** out)
+{
+    return create_impl(desc, 1, out);
+}
+
+PBGB_API int pbgb_vbd_create_batched(const pbgb_vbd_desc* descs, int32_t n_meshes, pbgb_vbd** out)
+{
+    return create_impl(descs, n_meshes, out);
+}
+
+PBGB_API int pbgb_vbd_destroy(pbgb_vbd* h)
+{
+    if (!h)
+        return kOk;
+    if (h->sys.stream)
+        cudaStreamSynchronize(h->sys.stream);
+    delete h;
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_step(pbgb_vbd* h, float dt, int32_t iterations, int32_t substeps)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (!(dt > 0.f) || !std::isfinite(dt) || iterations < 0 || substeps < 1)
+        return fail(h, kInvalid, "pbgb_vbd_step: expected dt > 0, iterations >= 0, substeps >= 1");
+    return guarded(h, [&] {
+        h->sys.step(dt, iterations, substeps);
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_synchronize(pbgb_vbd* h)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    return guarded(h, [&] {
+        int const rc = h->sys.synchronize();
+        if (rc != kOk)
+            pbgb::gLastError = h->sys.lastError;
+        return rc;
+    });
+}
+
+#define PBGB_CHECK_HANDLE_PTR(h, p)                                                                \
+    if (!(h))                                                                                      \
+        return fail(nullptr, kInvalid, "null handle");                                             \
+    if (!(p) && (h)->sys.nV > 0)                                                                   \
+        return fail((h), kInvalid, "null buffer");
+
+PBGB_API int pbgb_vbd_get_positions(pbgb_vbd* h, float* x)
+{
+    PBGB_CHECK_HANDLE_PTR(h, x)
+    return guarded(h, [&] {
+        h->sys.getVec(h->sys.x, x);
+        return h->sys.synchronize();
+    });
+}
+
+PBGB_API int pbgb_vbd_set_positions(pbgb_vbd* h, const float* x)
+{
+    PBGB_CHECK_HANDLE_PTR(h, x)
+    return guarded(h, [&] {
+        h->sys.setVec(h->sys.x, x);
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_get_velocities(pbgb_vbd* h, float* v)
+{
+    PBGB_CHECK_HANDLE_PTR(h, v)
+    return guarded(h, [&] {
+        h->sys.getVec(h->sys.v, v);
+        return h->sys.synchronize();
+    });
+}
+
+PBGB_API int pbgb_vbd_set_velocities(pbgb_vbd* h, const float* v)
+{
+    PBGB_CHECK_HANDLE_PTR(h, v)
+    return guarded(h, [&] {
+        h->sys.setVec(h->sys.v, v);
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_set_external_acceleration(pbgb_vbd* h, const float* a)
+{
+    PBGB_CHECK_HANDLE_PTR(h, a)
+    return guarded(h, [&] {
+        h->sys.setVec(h->sys.aext, a);
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_get_positions_device(pbgb_vbd* h, float* x_dev)
+{
+    PBGB_CHECK_HANDLE_PTR(h, x_dev)
+    return guarded(h, [&] {
+        pbgb::check(pbgb::launch_unpack3(h->sys.x.get(), x_dev, h->sys.nV, h->sys.stream), "unpack");
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_set_positions_device(pbgb_vbd* h, const float* x_dev)
+{
+    PBGB_CHECK_HANDLE_PTR(h, x_dev)
+    return guarded(h, [&] {
+        pbgb::check(pbgb::launch_pack3(x_dev, h->sys.x.get(), h->sys.nV, h->sys.stream), "pack");
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_set_detH_zero(pbgb_vbd* h, float zero)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    h->sys.detHZero = zero;
+    h->sys.invalidate();
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_set_damping(pbgb_vbd* h, float kD)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    h->sys.kD = kD;
+    h->sys.invalidate();
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_set_strategy(pbgb_vbd* h, int32_t strategy)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (strategy < 0 || strategy > 4)
+        return fail(h, kInvalid, "invalid initialization strategy");
+    h->sys.strategy = strategy;
+    h->sys.invalidate();
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_set_block_size(pbgb_vbd* h, int32_t block_size)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    // Clamp like the reference (gpu/impl/vbd/Integrator.cu:158-161), rounded to a warp multiple.
+    int32_t b = std::clamp(block_size, int32_t(32), int32_t(256));
+    h->sys.block = (b + 31) / 32 * 32;
+    h->sys.invalidate();
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_set_lanes_per_vertex(pbgb_vbd* h, int32_t lanes)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+        return fail(h, kInvalid, "lanes per vertex must be 0, 1, 2, 4, 8, 16 or 32");
+    h->sys.lanes = lanes;
+    h->sys.invalidate();
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_set_scene_bounding_box(pbgb_vbd* h, const float* min3, const float* max3)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (!min3 || !max3)
+        return fail(h, kInvalid, "null bounding box");
+    for (int k = 0; k < 3; ++k)
+    {
+        h->sys.sceneMin[k] = min3[k];
+        h->sys.sceneMax[k] = max3[k];
+    }
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_set_sweep_timing(pbgb_vbd* h, int32_t enable)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    h->sys.profiling = enable != 0;
+    h->sys.invalidate();
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_sweep_timing(pbgb_vbd* h, double* milliseconds, int64_t* sweep_launches)
+{
+    if (!h || !milliseconds || !sweep_launches)
+        return fail(h, kInvalid, "null argument");
+    if (!h->sys.profiling || !h->sys.graphValid)
+        return fail(h, kInvalid, "sweep timing is off or no step was taken since it was enabled");
+    return guarded(h, [&] {
+        auto& s = h->sys;
+        check(cudaStreamSynchronize(s.stream), "cudaStreamSynchronize");
+        *milliseconds = s.sweepMilliseconds(s.gIters, s.gSub);
+        int64_t nonEmpty = 0;
+        for (int32_t c = 0; c < s.nColors; ++c)
+            nonEmpty += s.colorPtr[c + 1] > s.colorPtr[c] ? 1 : 0;
+        *sweep_launches = nonEmpty * int64_t(s.gIters) * int64_t(s.gSub);
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_sizes(pbgb_vbd* h, int32_t* n_vertices, int32_t* n_tets, int32_t* n_free, int32_t* n_colors)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (n_vertices)
+        *n_vertices = h->sys.nV;
+    if (n_tets)
+        *n_tets = h->sys.nT;
+    if (n_free)
+        *n_free = h->sys.nFree;
+    if (n_colors)
+        *n_colors = h->sys.nColors;
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_launches_per_step(pbgb_vbd* h, int32_t iterations, int32_t substeps, int64_t* launches)
+{
+    if (!h || !launches)
+        return fail(h, kInvalid, "null argument");
+    *launches = h->sys.launchesPerStep(iterations, substeps);
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_stream(pbgb_vbd* h, void** stream)
+{
+    if (!h || !stream)
+        return fail(h, kInvalid, "null argument");
+    *stream = static_cast<void*>(h->sys.stream);
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_objective(pbgb_vbd* h, double dt, double* f)
+{
+    if (!h || !f)
+        return fail(h, kInvalid, "null argument");
+    return guarded(h, [&] {
+        auto& s = h->sys;
+        pbgb::check(cudaMemsetAsync(s.red.get(), 0, sizeof(double), s.stream), "memset");
+        pbgb::check(pbgb::launch_objective(s.energyParams(dt, s.red.get()), s.stream), "objective");
+        pbgb::check(cudaMemcpyAsync(f, s.red.get(), sizeof(double), cudaMemcpyDeviceToHost, s.stream), "D2H");
+        pbgb::check(cudaStreamSynchronize(s.stream), "sync");
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_gradient(pbgb_vbd* h, double dt, double* grad)
+{
+    if (!h || !grad)
+        return fail(h, kInvalid, "null argument");
+    return guarded(h, [&] {
+        auto& s = h->sys;
+        if (s.gradBuf.size() < size_t(s.nV) * 3)
+            s.gradBuf.allocate(size_t(s.nV) * 3);
+        double* d = s.gradBuf.get();
+        pbgb::check(cudaMemsetAsync(d, 0, sizeof(double) * 3 * size_t(s.nV), s.stream), "memset");
+        pbgb::check(pbgb::launch_gradient(s.energyParams(dt, d), s.stream), "gradient");
+        pbgb::check(cudaMemcpyAsync(grad, d, sizeof(double) * 3 * size_t(s.nV), cudaMemcpyDeviceToHost, s.stream), "D2H");
+        pbgb::check(cudaStreamSynchronize(s.stream), "sync");
+        return int(kOk);
+    });
+}
+
+PBGB_API const char* pbgb_last_error(pbgb_vbd* h)
+{
+    if (h)
+        return h->sys.lastError.c_str();
+    return pbgb::gLastError.c_str();
+}
+
+PBGB_API int pbgb_debug_vertex_block(
+    int32_t n,
+    const double* xe,
+    const double* GPs,
+    const int32_t* il,
+    const double* wg,
+    const double* mu,
+    const double* lambda,
+    const double* xt,
+    const double* xtilde,
+    double m,
+    double kD,
+    double h,
+    double h2,
+    double detHZero,
+    double* x,
+    double* g,
+    double* H)
+{
+    if (n < 0 || (n > 0 && (!xe || !GPs || !il || !wg || !mu || !lambda)) || !xt || !xtilde || !x)
+        return fail(nullptr, kInvalid, "pbgb_debug_vertex_block: null argument");
+    pbgb::VertexBlock<double> b;
+    pbgb::zero(b);
+    for (int32_t q = 0; q < n; ++q)
+    {
+        double const* xq = xe + 12 * size_t(q);
+        double const* G  = GPs + 12 * size_t(q);
+        if (il[q] < 0 || il[q] > 3)
+            return fail(nullptr, kInvalid, "local index out of range");
+        pbgb::accumulate_tet(
+            b, xq, xq + 3, xq + 6, xq + 9, G + 3, G + 6, G + 9, il[q], wg[q] * mu[q], wg[q] * lambda[q],
+            1.0 + mu[q] / lambda[q]);
+    }
+    pbgb::newton_update(b, xt, xtilde, m, h, h2, kD, detHZero, x, g, H);
+    return kOk;
+}
+
+} // extern "C"

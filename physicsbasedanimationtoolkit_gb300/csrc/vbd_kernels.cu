@@ -1,0 +1,386 @@
+// CUDA kernels of the VBD step (sm_103a).  See vbd_kernels.cuh for the data layout.
+#include "vbd_kernels.cuh"
+
+#include <cfloat>
+
+namespace pbgb {
+
+namespace {
+
+__device__ __forceinline__ void load3(float4 const v, float* o)
+{
+    o[0] = v.x;
+    o[1] = v.y;
+    o[2] = v.z;
+}
+
+// Per-colour Gauss-Seidel sweep (reference: VbdIteration, gpu/impl/vbd/Kernels.cuh:148-233, and
+// Integrator::SolveVertex, sim/vbd/Integrator.cpp:98-136).  L lanes cooperate on one vertex: lane
+// l takes incidences l, l+L, ...; the 10 accumulated floats are then reduced with xor shuffles
+// and lane 0 applies damping, inertia and the 3x3 Newton step, writing x in place.  Vertices of a
+// colour share no tet, so the in-place write races with no reader of this launch.
+template <int L>
+__global__ void __launch_bounds__(256) sweep_kernel(SweepParams p)
+{
+    int const tid   = blockIdx.x * blockDim.x + threadIdx.x;
+    int const s     = p.begin + tid / L;
+    int const lane  = tid & (L - 1);
+    bool const valid = s < p.end;
+
+    VertexBlock<float> b;
+    zero(b);
+    int i = 0;
+    float xi[3] = {0.f, 0.f, 0.f};
+    if (valid)
+    {
+        i = __ldg(p.solve + s);
+        load3(p.x[i], xi);
+        int const k1 = __ldg(p.incPtr + s + 1);
+        for (int k = __ldg(p.incPtr + s) + lane; k < k1; k += L)
+        {
+            uint32_t const q = __ldg(p.inc + k);
+            int const e      = int(q >> 2);
+            int const il     = int(q & 3u);
+            int4 const t     = __ldg(p.tv + e);
+            float4 const g1  = __ldg(p.tg + 3 * e + 0);
+            float4 const g2  = __ldg(p.tg + 3 * e + 1);
+            float4 const g3  = __ldg(p.tg + 3 * e + 2);
+            float xa[4][3];
+            int const vid[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+            {
+                if (a == il)
+                {
+                    xa[a][0] = xi[0];
+                    xa[a][1] = xi[1];
+                    xa[a][2] = xi[2];
+                }
+                else
+                    load3(__ldg(p.x + vid[a]), xa[a]);
+            }
+            float const G1[3] = {g1.x, g1.y, g1.z};
+            float const G2[3] = {g2.x, g2.y, g2.z};
+            float const G3[3] = {g3.x, g3.y, g3.z};
+            accumulate_tet(b, xa[0], xa[1], xa[2], xa[3], G1, G2, G3, il, g1.w, g2.w, g3.w);
+        }
+    }
+#pragma unroll
+    for (int off = L / 2; off > 0; off >>= 1)
+    {
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            b.g[r] += __shfl_xor_sync(0xffffffffu, b.g[r], off);
+        b.s += __shfl_xor_sync(0xffffffffu, b.s, off);
+#pragma unroll
+        for (int r = 0; r < 6; ++r)
+            b.C[r] += __shfl_xor_sync(0xffffffffu, b.C[r], off);
+    }
+    if (!valid || lane != 0)
+        return;
+    float4 const xt4 = p.xt[i];
+    float4 const xl4 = p.xtilde[i];
+    float const xt[3] = {xt4.x, xt4.y, xt4.z};
+    float const xl[3] = {xl4.x, xl4.y, xl4.z};
+    if (newton_update(b, xt, xl, xt4.w, p.h, p.h2, p.kD, p.detHZero, xi))
+        p.x[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
+}
+
+// Start of a substep (sim/vbd/Integrator.cpp:31-34,54-71; gpu/impl/vbd/Integrator.cu:190-248):
+// xt <- x, xtilde = xt + h v + h^2 aext, x <- initial guess.
+__global__ void begin_substep_kernel(SubstepParams p)
+{
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n)
+        return;
+    float4 const x4 = p.x[i];
+    float4 const v4 = p.v[i];
+    float4 const a4 = p.aext[i];
+    float const xt[3] = {x4.x, x4.y, x4.z};
+    float const vt[3] = {v4.x, v4.y, v4.z};
+    float const a[3]  = {a4.x, a4.y, a4.z};
+    float vm[3]       = {vt[0], vt[1], vt[2]};
+    if (p.gpuSemantics)
+    {
+        float4 const w = p.vprev[i];
+        vm[0] = w.x, vm[1] = w.y, vm[2] = w.z;
+    }
+    p.xt[i]     = make_float4(xt[0], xt[1], xt[2], p.m[i]);
+    p.xtilde[i] = make_float4(
+        xt[0] + p.h * vt[0] + p.h2 * a[0],
+        xt[1] + p.h * vt[1] + p.h2 * a[1],
+        xt[2] + p.h * vt[2] + p.h2 * a[2],
+        0.f);
+    float x0[3];
+    initial_position(xt, vm, vt, a, p.h, p.h2, p.strategy, FLT_MIN, x0);
+    p.x[i] = make_float4(x0[0], x0[1], x0[2], 0.f);
+}
+
+// End of a substep: v = (x - xt)/h (sim/vbd/Kernels.h:121-129); the previous velocity is kept
+// for the GPU integrator's AdaptiveVbd (gpu/impl/vbd/Integrator.cu:329-347).  Non-finite state
+// raises flags[0].
+__global__ void end_substep_kernel(SubstepParams p)
+{
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n)
+        return;
+    float4 const x4  = p.x[i];
+    float4 const xt4 = p.xt[i];
+    float4 const vo  = p.v[i];
+    float const inv  = 1.f / p.h;
+    float4 const vn  = make_float4((x4.x - xt4.x) * inv, (x4.y - xt4.y) * inv, (x4.z - xt4.z) * inv, 0.f);
+    if (p.gpuSemantics)
+        p.vprev[i] = vo;
+    p.v[i] = vn;
+    bool const finite = isfinite(x4.x) && isfinite(x4.y) && isfinite(x4.z) && isfinite(vn.x) &&
+                        isfinite(vn.y) && isfinite(vn.z);
+    if (!finite)
+        atomicOr(p.flags, 1);
+}
+
+// Chebyshev semi-iterative update after each sweep (sim/vbd/ChebyshevIntegrator.cpp:15-32,
+// gpu/impl/vbd/ChebyshevIntegrator.cu:38-59).
+__global__ void chebyshev_kernel(ChebyshevParams p)
+{
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n)
+        return;
+    float4 xk        = p.x[i];
+    float4 const km1 = p.xkm1[i];
+    if (p.k > 1)
+    {
+        float4 const km2 = p.xkm2[i];
+        xk.x             = p.omega * (xk.x - km2.x) + km2.x;
+        xk.y             = p.omega * (xk.y - km2.y) + km2.y;
+        xk.z             = p.omega * (xk.z - km2.z) + km2.z;
+        p.x[i]           = xk;
+    }
+    p.xkm2[i] = km1;
+    p.xkm1[i] = xk;
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int off = 16; off > 0; off >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// Tet geometry helper: F (columns f[c]) of tet e at positions x.
+__device__ __forceinline__ void tet_F(EnergyParams const& p, int e, float f[3][3], int4& t, float4& g1, float4& g2, float4& g3)
+{
+    t  = p.tv[e];
+    g1 = p.tg[3 * e + 0];
+    g2 = p.tg[3 * e + 1];
+    g3 = p.tg[3 * e + 2];
+    float4 const x0 = p.x[t.x], x1 = p.x[t.y], x2 = p.x[t.z], x3 = p.x[t.w];
+    float const d1[3] = {x1.x - x0.x, x1.y - x0.y, x1.z - x0.z};
+    float const d2[3] = {x2.x - x0.x, x2.y - x0.y, x2.z - x0.z};
+    float const d3[3] = {x3.x - x0.x, x3.y - x0.y, x3.z - x0.z};
+    float const G1[3] = {g1.x, g1.y, g1.z}, G2[3] = {g2.x, g2.y, g2.z}, G3[3] = {g3.x, g3.y, g3.z};
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r)
+            f[c][r] = d1[r] * G1[c] + d2[r] * G2[c] + d3[r] * G3[c];
+}
+
+// Objective of the backward-Euler step (sim/vbd/Integrator.cpp:138-165): per-entity terms in FP32,
+// the global sum in FP64.
+__global__ void objective_kernel(EnergyParams p)
+{
+    double acc  = 0.0;
+    int const n = p.nV > p.nT ? p.nV : p.nT;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    {
+        if (j < p.nV)
+        {
+            float4 const x = p.x[j], y = p.xtilde[j];
+            double const dx = double(x.x) - y.x, dy = double(x.y) - y.y, dz = double(x.z) - y.z;
+            acc += 0.5 * double(p.m[j]) * (dx * dx + dy * dy + dz * dz);
+        }
+        if (j < p.nT)
+        {
+            float f[3][3];
+            int4 t;
+            float4 g1, g2, g3;
+            tet_F(p, j, f, t, g1, g2, g3);
+            double I2 = 0.0;
+            for (int c = 0; c < 3; ++c)
+                for (int r = 0; r < 3; ++r)
+                    I2 += double(f[c][r]) * f[c][r];
+            double const J = double(f[0][0]) * (double(f[1][1]) * f[2][2] - double(f[1][2]) * f[2][1]) -
+                             double(f[1][0]) * (double(f[0][1]) * f[2][2] - double(f[0][2]) * f[2][1]) +
+                             double(f[2][0]) * (double(f[0][1]) * f[1][2] - double(f[0][2]) * f[1][1]);
+            double const a = J - double(g3.w);
+            acc += p.dt2 * (0.5 * double(g2.w) * a * a + 0.5 * double(g1.w) * (I2 - 3.0));
+        }
+    }
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0)
+        atomicAdd(p.out, acc);
+}
+
+// Gradient of the objective (sim/vbd/Integrator.cpp:167-200): inertial part per vertex, elastic
+// part per tet scattered with FP64 atomics.
+__global__ void gradient_kernel(EnergyParams p)
+{
+    int const n = p.nV > p.nT ? p.nV : p.nT;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    {
+        if (j < p.nV)
+        {
+            float4 const x = p.x[j], y = p.xtilde[j];
+            double const mj = p.m[j];
+            atomicAdd(p.out + 3 * j + 0, mj * (double(x.x) - y.x));
+            atomicAdd(p.out + 3 * j + 1, mj * (double(x.y) - y.y));
+            atomicAdd(p.out + 3 * j + 2, mj * (double(x.z) - y.z));
+        }
+        if (j < p.nT)
+        {
+            float f[3][3];
+            int4 t;
+            float4 g1, g2, g3;
+            tet_F(p, j, f, t, g1, g2, g3);
+            float k[3][3];
+            k[0][0] = f[1][1] * f[2][2] - f[1][2] * f[2][1];
+            k[0][1] = f[1][2] * f[2][0] - f[1][0] * f[2][2];
+            k[0][2] = f[1][0] * f[2][1] - f[1][1] * f[2][0];
+            k[1][0] = f[2][1] * f[0][2] - f[2][2] * f[0][1];
+            k[1][1] = f[2][2] * f[0][0] - f[2][0] * f[0][2];
+            k[1][2] = f[2][0] * f[0][1] - f[2][1] * f[0][0];
+            k[2][0] = f[0][1] * f[1][2] - f[0][2] * f[1][1];
+            k[2][1] = f[0][2] * f[1][0] - f[0][0] * f[1][2];
+            k[2][2] = f[0][0] * f[1][1] - f[0][1] * f[1][0];
+            float const J  = f[0][0] * k[0][0] + f[0][1] * k[0][1] + f[0][2] * k[0][2];
+            float const sl = g2.w * (J - g3.w);
+            // P = mu' F + lambda' (J - alpha) cof F ; dE/dx_a = P w_a
+            float P[3][3];
+            for (int c = 0; c < 3; ++c)
+                for (int r = 0; r < 3; ++r)
+                    P[c][r] = g1.w * f[c][r] + sl * k[c][r];
+            float const G[4][3] = {
+                {-(g1.x + g2.x + g3.x), -(g1.y + g2.y + g3.y), -(g1.z + g2.z + g3.z)},
+                {g1.x, g1.y, g1.z},
+                {g2.x, g2.y, g2.z},
+                {g3.x, g3.y, g3.z}};
+            int const vid[4] = {t.x, t.y, t.z, t.w};
+            for (int a = 0; a < 4; ++a)
+                for (int r = 0; r < 3; ++r)
+                {
+                    double const s = double(P[0][r]) * G[a][0] + double(P[1][r]) * G[a][1] +
+                                     double(P[2][r]) * G[a][2];
+                    atomicAdd(p.out + 3 * vid[a] + r, p.dt2 * s);
+                }
+        }
+    }
+}
+
+__global__ void pack3_kernel(float const* __restrict__ in3, float4* __restrict__ out4, int32_t n)
+{
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        out4[i] = make_float4(in3[3 * i], in3[3 * i + 1], in3[3 * i + 2], 0.f);
+}
+
+__global__ void unpack3_kernel(float4 const* __restrict__ in4, float* __restrict__ out3, int32_t n)
+{
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        float4 const v = in4[i];
+        out3[3 * i]     = v.x;
+        out3[3 * i + 1] = v.y;
+        out3[3 * i + 2] = v.z;
+    }
+}
+
+inline int blocks_for(int64_t n, int block)
+{
+    return int((n + block - 1) / block);
+}
+
+} // namespace
+
+cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, cudaStream_t s)
+{
+    int64_t const n = int64_t(p.end - p.begin) * lanes;
+    if (n <= 0)
+        return cudaSuccess;
+    int const g = blocks_for(n, block);
+    switch (lanes)
+    {
+        case 1: sweep_kernel<1><<<g, block, 0, s>>>(p); break;
+        case 2: sweep_kernel<2><<<g, block, 0, s>>>(p); break;
+        case 4: sweep_kernel<4><<<g, block, 0, s>>>(p); break;
+        case 8: sweep_kernel<8><<<g, block, 0, s>>>(p); break;
+        case 16: sweep_kernel<16><<<g, block, 0, s>>>(p); break;
+        case 32: sweep_kernel<32><<<g, block, 0, s>>>(p); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_begin_substep(SubstepParams const& p, cudaStream_t s)
+{
+    if (p.n <= 0)
+        return cudaSuccess;
+    begin_substep_kernel<<<blocks_for(p.n, 256), 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_end_substep(SubstepParams const& p, cudaStream_t s)
+{
+    if (p.n <= 0)
+        return cudaSuccess;
+    end_substep_kernel<<<blocks_for(p.n, 256), 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chebyshev(ChebyshevParams const& p, cudaStream_t s)
+{
+    if (p.n <= 0)
+        return cudaSuccess;
+    chebyshev_kernel<<<blocks_for(p.n, 256), 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_objective(EnergyParams const& p, cudaStream_t s)
+{
+    int const n = p.nV > p.nT ? p.nV : p.nT;
+    int g       = blocks_for(n, 256);
+    if (g > 4096)
+        g = 4096;
+    if (g < 1)
+        g = 1;
+    objective_kernel<<<g, 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gradient(EnergyParams const& p, cudaStream_t s)
+{
+    int const n = p.nV > p.nT ? p.nV : p.nT;
+    int g       = blocks_for(n, 256);
+    if (g > 4096)
+        g = 4096;
+    if (g < 1)
+        g = 1;
+    gradient_kernel<<<g, 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack3(float const* in3, float4* out4, int32_t n, cudaStream_t s)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    pack3_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in3, out4, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack3(float4 const* in4, float* out3, int32_t n, cudaStream_t s)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    unpack3_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in4, out3, n);
+    return cudaGetLastError();
+}
+
+} // namespace pbgb

@@ -1,0 +1,1 @@
+from . import vbd  # noqa: F401

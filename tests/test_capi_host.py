@@ -1,0 +1,150 @@
+"""C-ABI surface and host-side logic of the product library (no GPU needed)."""
+
+import ctypes as C
+import pathlib
+import re
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from physicsbasedanimationtoolkit_gb300 import _capi, meshgen, pbat
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        names |= set(re.findall(r"PBGB_API\s+[\w\s\*]+?\b(pbgb_\w+)\s*\(", h.read_text()))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    L = _capi.lib()
+    declared = declared_symbols()
+    assert len(declared) >= 20
+    for name in declared:
+        assert hasattr(L, name), name
+    # The Python binding covers the whole header.
+    assert declared == set(_capi.SYMBOLS)
+
+
+def test_library_has_no_cpu_fallback_symbols():
+    # The only compute entry point usable without a device is the documented host self-check.
+    L = _capi.lib()
+    h = C.c_void_p()
+    d = _capi.VbdDesc()
+    rc = L.pbgb_vbd_create(C.byref(d), C.byref(h))
+    assert rc != 0
+
+
+def _construct_product(X, T, rho, dbc, o=2, s=0):
+    d = (pbat.sim.vbd.Data().with_volume_mesh(X.T, T.T).with_material(rho, np.ones_like(rho), np.ones_like(rho))
+         .with_dirichlet_vertices(dbc).with_vertex_coloring_strategy(o, s).construct())
+    return d
+
+
+@pytest.mark.parametrize("n", [1, 3, 10])
+def test_product_construct_matches_oracle(n):
+    w = meshgen.unit_cube_workload(n=n, seed=n)
+    for o in range(3):
+        for s in range(2):
+            d = _construct_product(w["X"], w["T"], w["rho"], w["dbc"], o, s)
+            r = O.construct(w["X"], w["T"], w["rho"], w["dbc"], o, s)
+            np.testing.assert_array_equal(d.colors, r["colors"])
+            np.testing.assert_array_equal(d.Pptr, r["Pptr"])
+            np.testing.assert_array_equal(d.Padj, r["Padj"])
+            np.testing.assert_array_equal(d.GVGp, r["GVGp"])
+            np.testing.assert_array_equal(d.GVGe, r["GVGe"])
+            np.testing.assert_array_equal(d.GVGilocal, r["GVGilocal"])
+            np.testing.assert_allclose(d.m, r["m"], rtol=1e-13)
+            np.testing.assert_allclose(d.wg, r["wg"], rtol=1e-13)
+            np.testing.assert_allclose(d._GP_rows.reshape(-1, 4, 3), r["GP"], rtol=1e-12, atol=1e-9)
+
+
+def test_product_construct_reference_gp_layout():
+    P, T, V, F = meshgen.cube5()
+    d = pbat.sim.vbd.Data().with_volume_mesh(P, T).with_surface_mesh(V, F).construct()
+    assert d.GP.shape == (4, 15)
+    # Column 3e+k of GP holds d/dX_k of the 4 shape functions of element e.
+    r = O.construct(P.T, T.T, np.full(5, 1000.0), np.zeros(0, np.int32))
+    for e in range(5):
+        np.testing.assert_allclose(d.GP[:, 3 * e: 3 * e + 3], r["GP"][e], atol=1e-14)
+    assert d.XVA.shape == (8,) and d.FA.shape == (12,)
+    assert abs(d.FA.sum() - 6.0) < 1e-12
+
+
+def test_product_coloring_matches_reference_fixture():
+    g = np.load(ROOT / "tests" / "golden" / "coloring.npz")
+    X = meshgen.hex_grid(10, 10, 10)[0]
+    T = g["cube10_T"]
+    for o in range(3):
+        for s in range(2):
+            d = _construct_product(X, T, np.full(T.shape[0], 1000.0), np.zeros(0, np.int64), o, s)
+            np.testing.assert_array_equal(d.colors, g[f"cube10_{o}_{s}"])
+
+
+def test_construct_rejects_bad_meshes():
+    X, T = meshgen.hex_grid(2, 2, 2)
+    bad = T.copy()
+    bad[0, [1, 2]] = bad[0, [2, 1]]  # inverted tet
+    with pytest.raises(_capi.PbgbError) as e:
+        _construct_product(X, bad, np.full(T.shape[0], 1000.0), np.zeros(0, np.int64))
+    assert e.value.code == 4
+    oob = T.copy()
+    oob[3, 0] = X.shape[0] + 5
+    with pytest.raises(_capi.PbgbError) as e:
+        _construct_product(X, oob, np.full(T.shape[0], 1000.0), np.zeros(0, np.int64))
+    assert e.value.code == 1
+    with pytest.raises(_capi.PbgbError):
+        _construct_product(X, T, np.full(T.shape[0], 1000.0), np.array([X.shape[0] + 1]))
+
+
+def test_chebyshev_rho_validation():
+    P, T, _, _ = meshgen.cube5()
+    with pytest.raises(ValueError):
+        pbat.sim.vbd.Data().with_volume_mesh(P, T).with_chebyshev_acceleration(1.0).construct()
+
+
+def test_closed_form_vertex_block_matches_reference_fixture():
+    """The device sweep's closed-form 3x3 block (host FP64 build of the same code) against the
+    reference's full 9x9 SNH contraction."""
+    g = np.load(ROOT / "tests" / "golden" / "vertex_solve.npz")
+    L = _capi.lib()
+    for c in range(int(g["count"])):
+        a = {k.split("_", 1)[1]: g[k] for k in g.files if k.startswith(f"c{c}_")}
+        x = a["x"].astype(np.float64).copy()
+        gg = np.zeros(3)
+        H = np.zeros(9)
+        arrs = [np.ascontiguousarray(a[k]) for k in ("xe", "GPs")]
+        il = np.ascontiguousarray(a["il"], dtype=np.int32)
+        rc = L.pbgb_debug_vertex_block(int(a["n"]), arrs[0].ctypes.data, arrs[1].ctypes.data, il.ctypes.data,
+                                       a["wg"].ctypes.data, a["mu"].ctypes.data, a["lam"].ctypes.data,
+                                       a["xt"].ctypes.data, a["xtilde"].ctypes.data, float(a["m"]),
+                                       float(a["kD"]), float(a["h"]), float(a["h"]) ** 2, 1e-7,
+                                       x.ctypes.data, gg.ctypes.data, H.ctypes.data)
+        assert rc == 0
+        scale = np.abs(a["H"]).max()
+        np.testing.assert_allclose(H.reshape(3, 3).T.ravel(), a["H"], rtol=1e-10, atol=1e-10 * scale)
+        np.testing.assert_allclose(gg, a["g"], rtol=1e-8, atol=1e-9 * scale)
+        np.testing.assert_allclose(x, a["x_out"], rtol=0, atol=1e-11)
+
+
+def test_integrator_creation_without_device_fails_loudly():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    P, T, _, _ = meshgen.cube5()
+    d = pbat.sim.vbd.Data().with_volume_mesh(P, T).construct()
+    with pytest.raises(_capi.PbgbError) as e:
+        pbat.gpu.vbd.Integrator(d)
+    assert e.value.code == 6
+
+
+def test_unsupported_accelerations_are_rejected():
+    P, T, _, _ = meshgen.cube5()
+    d = pbat.sim.vbd.Data().with_volume_mesh(P, T).with_anderson_acceleration(5).construct()
+    with pytest.raises(NotImplementedError):
+        pbat.gpu.vbd.Integrator(d)

@@ -1,0 +1,227 @@
+"""Pins the FP64 oracle against the reference: golden fixtures produced by the reference's own
+kernels (tests/golden/make_golden.py), the reference doctests' known answers, and, where the
+reference harness was built here, direct comparison with it."""
+
+import json
+import pathlib
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from physicsbasedanimationtoolkit_gb300 import meshgen
+
+GOLD = pathlib.Path(__file__).resolve().parent / "golden"
+
+
+def test_snh_matches_reference_fixture():
+    g = np.load(GOLD / "snh.npz")
+    L = O.lib()
+    for k in range(g["F"].shape[0]):
+        f = np.ascontiguousarray(g["F"][k].ravel(order="F"))
+        e = L.orc_snh_eval(f, g["mu"][k], g["lam"][k])
+        gr = np.zeros(9)
+        H = np.zeros(81)
+        L.orc_snh_grad_hessian(f, g["mu"][k], g["lam"][k], gr, H)
+        assert abs(e - g["E"][k]) <= 1e-12 * max(1.0, abs(g["E"][k]))
+        np.testing.assert_allclose(gr, g["G"][k], rtol=1e-11, atol=1e-9 * np.abs(g["G"][k]).max())
+        np.testing.assert_allclose(H, g["H"][k], rtol=1e-11, atol=1e-11 * np.abs(g["H"][k]).max())
+
+
+def test_snh_known_answer_at_identity():
+    kat = json.loads((GOLD / "kat.json").read_text())["snh_identity"]
+    mu, lam = meshgen.lame(kat["E"], kat["nu"])
+    gamma = 1.0 + mu / lam
+    expected = 0.5 * mu * (3 - 3) + 0.5 * lam * (1.0 - gamma) ** 2
+    F = np.ascontiguousarray(np.eye(3).ravel(order="F"))
+    assert abs(O.lib().orc_snh_eval(F, mu, lam) - expected) <= kat["tolerance"]
+    assert O.lib().orc_snh_eval(F, mu, lam) >= 0.0
+
+
+def test_lame_known_answer():
+    kat = json.loads((GOLD / "kat.json").read_text())["lame"]
+    import ctypes as C
+
+    mu, lam = C.c_double(), C.c_double()
+    O.lib().orc_lame(C.c_double(kat["E"]), C.c_double(kat["nu"]), C.byref(mu), C.byref(lam))
+    assert mu.value == kat["E"] / (2 * (1 + kat["nu"]))
+    assert lam.value == kat["E"] * kat["nu"] / ((1 + kat["nu"]) * (1 - 2 * kat["nu"]))
+
+
+def test_snh_hessian_is_derivative_of_gradient():
+    rng = np.random.default_rng(3)
+    L = O.lib()
+    for _ in range(10):
+        F = np.ascontiguousarray((np.eye(3) + 0.3 * rng.standard_normal((3, 3))).ravel(order="F"))
+        g = np.zeros(9)
+        H = np.zeros(81)
+        L.orc_snh_grad_hessian(F, 3e5, 2e6, g, H)
+        Hfd = np.zeros((9, 9))
+        for j in range(9):
+            e = np.zeros(9)
+            e[j] = 1e-6
+            gp = np.zeros(9)
+            gm = np.zeros(9)
+            L.orc_snh_grad(np.ascontiguousarray(F + e), 3e5, 2e6, gp)
+            L.orc_snh_grad(np.ascontiguousarray(F - e), 3e5, 2e6, gm)
+            Hfd[:, j] = (gp - gm) / 2e-6
+        np.testing.assert_allclose(H.reshape(9, 9), Hfd, rtol=1e-5, atol=1e-4 * np.abs(Hfd).max())
+
+
+def test_vertex_solve_matches_reference_fixture():
+    g = np.load(GOLD / "vertex_solve.npz")
+    L = O.lib()
+    for c in range(int(g["count"])):
+        a = {k.split("_", 1)[1]: g[k] for k in g.files if k.startswith(f"c{c}_")}
+        x = a["x"].astype(np.float64).copy()
+        gg = np.zeros(3)
+        H = np.zeros(9)
+        L.orc_vertex_solve(int(a["n"]), np.ascontiguousarray(a["xe"]), np.ascontiguousarray(a["GPs"]),
+                           a["il"].astype(np.int32), a["wg"], a["mu"], a["lam"], a["xt"], a["xtilde"],
+                           float(a["m"]), float(a["kD"]), float(a["h"]), float(a["h"]) ** 2, 1e-7, x, gg, H)
+        np.testing.assert_allclose(H, a["H"], rtol=1e-11, atol=1e-11 * np.abs(a["H"]).max())
+        np.testing.assert_allclose(gg, a["g"], rtol=1e-9, atol=1e-10 * np.abs(a["H"]).max())
+        np.testing.assert_allclose(x, a["x_out"], rtol=0, atol=1e-12)
+
+
+def test_initial_positions_match_reference_fixture():
+    g = np.load(GOLD / "init_strategies.npz")
+    L = O.lib()
+    for s in range(5):
+        for k in range(g["xt"].shape[0]):
+            r = np.zeros(3)
+            L.orc_initial_positions(g["xt"][k].copy(), g["vtm1"][k].copy(), g["vt"][k].copy(),
+                                    g["a"][k].copy(), 1 / 60, 1 / 3600, s, r)
+            np.testing.assert_allclose(r, g["out"][s, k], rtol=0, atol=1e-14)
+
+
+def test_chebyshev_weights_match_reference_fixture():
+    g = np.load(GOLD / "chebyshev.npz")
+    for r, rho in enumerate(g["rho"]):
+        w = 0.0
+        for k in range(g["omega"].shape[1]):
+            w = O.lib().orc_chebyshev_omega(k, rho * rho, w, 0)
+            assert w == g["omega"][r, k]
+
+
+@pytest.mark.parametrize("name", ["cube5", "cube10", "beam"])
+def test_coloring_matches_reference_fixture(name):
+    g = np.load(GOLD / "coloring.npz")
+    T = g[f"{name}_T"]
+    nV = int(T.max()) + 1
+    X = np.zeros((nV, 3))
+    # Geometry does not matter for the colouring; use a valid embedding for the mass pass.
+    if name == "cube5":
+        X = meshgen.cube5()[0].T.copy()
+    elif name == "cube10":
+        X = meshgen.hex_grid(10, 10, 10)[0]
+    else:
+        X = meshgen.hex_grid(12, 3, 3, hi=(4.0, 1.0, 1.0))[0]
+    for o in range(3):
+        for s in range(2):
+            d = O.construct(X, T, np.full(T.shape[0], 1000.0), np.zeros(0, np.int32), o, s)
+            np.testing.assert_array_equal(d["colors"], g[f"{name}_{o}_{s}"])
+
+
+def test_coloring_is_valid_and_partitions_drop_dirichlet():
+    w = meshgen.unit_cube_workload()
+    d = O.construct(w["X"], w["T"], w["rho"], w["dbc"])
+    c = d["colors"]
+    for t in w["T"]:
+        assert len(set(c[t])) == 4
+    assert set(d["Padj"]).isdisjoint(set(w["dbc"]))
+    assert d["Padj"].size == w["X"].shape[0] - w["dbc"].size
+    for p in range(d["Pptr"].size - 1):
+        part = d["Padj"][d["Pptr"][p]: d["Pptr"][p + 1]]
+        assert np.all(c[part] == p)
+        assert np.all(np.diff(part) > 0)
+
+
+def test_mass_and_gradients_of_linear_tets():
+    w = meshgen.unit_cube_workload()
+    d = O.construct(w["X"], w["T"], w["rho"], w["dbc"])
+    # Total mass = rho * volume; GP rows sum to zero; GP reproduces linear fields exactly.
+    vol = d["wg"].sum()
+    assert abs(d["m"].sum() - 1000.0 * vol) < 1e-9
+    assert np.abs(d["GP"].sum(axis=1)).max() < 1e-12
+    A = np.array([[1.0, 2.0, 3.0], [0.5, -1.0, 0.25], [2.0, 0.0, 1.0]])
+    for e in range(0, w["T"].shape[0], 97):
+        Xe = w["X"][w["T"][e]]
+        F = (A @ Xe.T) @ d["GP"][e]
+        np.testing.assert_allclose(F, A, atol=1e-10)
+
+
+def test_cube_trajectories_match_reference_fixture():
+    g = np.load(GOLD / "trajectories.npz")
+    P, T, _, _ = meshgen.cube5()
+    for tag, cheb in (("base", None), ("cheb", 0.9)):
+        I = O.OracleVbd(P.T.copy(), T.T.copy(), np.full(5, 1000.0),
+                        *meshgen.lame(np.full(5, 1e6), np.full(5, 0.45)), dbc=np.zeros(0, np.int32),
+                        rho_chebyshev=cheb)
+        I.step(1e-2, 10, 1, 1)
+        np.testing.assert_allclose(I.x, g[f"cube5_{tag}_x"], rtol=0, atol=1e-12)
+
+
+def test_unit_cube_trajectory_matches_reference_fixture():
+    g = np.load(GOLD / "trajectories.npz")
+    w = meshgen.unit_cube_workload()
+    I = O.OracleVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"])
+    I.step(1 / 60, 20, 1, 30)
+    np.testing.assert_allclose(I.x, g["cube10_x"], rtol=0, atol=1e-11)
+    np.testing.assert_allclose(I.v, g["cube10_v"], rtol=0, atol=1e-9)
+
+
+def test_beam_trajectory_with_chebyshev_damping_substeps_matches_reference_fixture():
+    g = np.load(GOLD / "trajectories.npz")
+    X, T = meshgen.hex_grid(12, 3, 3, hi=(4.0, 1.0, 1.0))
+    dbc = meshgen.face_vertices(X, 0, 0.0)
+    mu, lam = meshgen.lame(np.full(T.shape[0], 5e5), np.full(T.shape[0], 0.48))
+    I = O.OracleVbd(X, T, np.full(T.shape[0], 1000.0), mu, lam, dbc, v=g["beam_v0"], rho_chebyshev=0.95,
+                    kD=1e-3, strategy=3)
+    I.step(1 / 60, 15, 2, 6)
+    np.testing.assert_allclose(I.x, g["beam_x"], rtol=0, atol=1e-10)
+
+
+def test_reference_cube_properties():
+    """The reference doctest's assertions on the 5-tet cube (sim/vbd/Integrator.cpp:245-293)."""
+    kat = json.loads((GOLD / "kat.json").read_text())["vbd_cube"]
+    P, T, _, _ = meshgen.cube5()
+    I = O.OracleVbd(P.T.copy(), T.T.copy(), np.full(5, 1000.0), *meshgen.lame(np.full(5, 1e6), np.full(5, 0.45)),
+                    dbc=np.zeros(0, np.int32))
+    dt = kat["dt"]
+    xtilde = I.x + dt * I.v + dt * dt * I.aext
+    f0 = I.objective(I.x, xtilde, dt)
+    I.step(dt, kat["iterations"], kat["substeps"])
+    dx = I.x - P.T
+    assert np.all(dx[:, 2] < 0)
+    assert np.all(np.abs(dx[:, :2]) < kat["zero"])
+    assert np.linalg.norm(I.gradient(I.x, xtilde, dt)) < kat["zero"]
+    assert I.objective(I.x, xtilde, dt) < f0
+
+
+def test_thread_count_does_not_change_results():
+    w = meshgen.unit_cube_workload(n=6)
+    A = O.OracleVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], nthreads=1)
+    B = O.OracleVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], nthreads=4)
+    A.step(1 / 60, 10, 1, 5)
+    B.step(1 / 60, 10, 1, 5)
+    np.testing.assert_array_equal(A.x, B.x)
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference harness not built (no reference sources)")
+def test_oracle_matches_reference_harness_directly():
+    R = O.ref()
+    w = meshgen.unit_cube_workload(n=5, seed=7)
+    for strategy in range(5):
+        for semantics in (0, 1):
+            A = O.OracleVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], strategy=strategy,
+                            semantics=semantics, kD=1e-3 * strategy)
+            B = O.OracleVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], strategy=strategy,
+                            semantics=semantics, kD=1e-3 * strategy)
+            A.step(1 / 60, 8, 2, 4)
+            B.step(1 / 60, 8, 2, 4, use_ref=True)
+            np.testing.assert_allclose(A.x, B.x, rtol=0, atol=1e-12)
+    rng = np.random.default_rng(0)
+    for _ in range(50):
+        x = rng.uniform(-0.2, 1.2, 3).astype(np.float32)
+        assert R.ref_morton3d(*x) == R.ref_morton3d(*x)
