@@ -407,7 +407,7 @@ class VbdSystem
             {
                 size_t const slot = size_t(s) * size_t(iterations) + size_t(k);
                 if (profiling)
-                    check(cudaEventRecord(evBegin[slot], stream), "cudaEventRecord");
+                    check(cudaEventRecordWithFlags(evBegin[slot], stream, cudaEventRecordExternal), "cudaEventRecord");
                 for (int32_t c = 0; c < nColors; ++c)
                 {
                     w.begin = colorPtr[c];
@@ -415,7 +415,7 @@ class VbdSystem
                     check(launch_sweep(w, L, block, stream), "sweep");
                 }
                 if (profiling)
-                    check(cudaEventRecord(evEnd[slot], stream), "cudaEventRecord");
+                    check(cudaEventRecordWithFlags(evEnd[slot], stream, cudaEventRecordExternal), "cudaEventRecord");
                 if (acceleration == PBGB_ACCEL_CHEBYSHEV)
                 {
                     omega = chebyshev_omega<double>(k, rho2, omega, chebFormula);
