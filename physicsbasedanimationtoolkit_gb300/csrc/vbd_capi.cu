@@ -94,10 +94,9 @@ class VbdSystem
 
     // Device state
     cudaStream_t stream = nullptr;
-    DeviceArray<float4> x, xt, xtilde, v, aext, vprev, xkm1, xkm2;
+    DeviceArray<float4> x, xt, xtilde, v, aext, vprev, h0, h1;
     DeviceArray<float> m, staging;
-    DeviceArray<int4> tv;
-    DeviceArray<float4> tg;
+    DeviceArray<TetRecord> tets;
     DeviceArray<int32_t> solve, incPtr, flags;
     DeviceArray<uint32_t> inc;
     DeviceArray<double> red, gradBuf;
@@ -169,8 +168,6 @@ class VbdSystem
         int const perColor = nColors > 0 ? nFree / nColors : nFree;
         if (perColor < 4096)
             return 32;
-        if (meanDegree > 12.0)
-            return 8;
         return 4;
     }
 
@@ -222,9 +219,22 @@ class VbdSystem
         // Host staging of the concatenated layout.
         std::vector<float4> hx(nV), hv(nV), ha(nV);
         std::vector<float> hm(nV);
-        std::vector<int4> htv(nT);
-        std::vector<float4> htg(size_t(nT) * 3);
+        std::vector<TetRecord> hrec(nT);
         std::vector<int32_t> deg(nV, 0);
+        // Colour of every vertex (free vertices from the partitions; pinned ones are never solved
+        // and hold the same value in every position buffer, so any colour works: -1).
+        std::vector<int32_t> color(nV, -1);
+        {
+            int32_t vb = 0;
+            for (int32_t b = 0; b < nMeshes; ++b)
+            {
+                auto const& d = descs[b];
+                for (int32_t c = 0; c < d.n_partitions; ++c)
+                    for (int32_t k = d.Pptr[c]; k < d.Pptr[c + 1]; ++k)
+                        color[d.Padj[k] + vb] = c;
+                vb += d.n_vertices;
+            }
+        }
         int32_t v0 = 0, t0 = 0;
         for (int32_t b = 0; b < nMeshes; ++b)
         {
@@ -252,15 +262,29 @@ class VbdSystem
             for (int32_t e = 0; e < d.n_tets; ++e)
             {
                 int32_t const* t = d.T + 4 * size_t(e);
-                htv[t0 + e]      = make_int4(t[0] + v0, t[1] + v0, t[2] + v0, t[3] + v0);
-                double const* G  = d.GP + 12 * size_t(e);
-                double const w = d.wg[e], mu = d.mu[e], la = d.lambda[e];
-                htg[3 * size_t(t0 + e) + 0] = make_float4(float(G[3]), float(G[4]), float(G[5]), float(w * mu));
-                htg[3 * size_t(t0 + e) + 1] = make_float4(float(G[6]), float(G[7]), float(G[8]), float(w * la));
-                htg[3 * size_t(t0 + e) + 2] =
-                    make_float4(float(G[9]), float(G[10]), float(G[11]), float(1.0 + mu / la));
+                uint32_t gv[4];
                 for (int q = 0; q < 4; ++q)
-                    deg[t[q] + v0]++;
+                {
+                    gv[q] = uint32_t(t[q] + v0);
+                    deg[gv[q]]++;
+                }
+                // Rank of each vertex by colour inside the tet (ties broken by position).
+                uint32_t packed[4];
+                for (int q = 0; q < 4; ++q)
+                {
+                    uint32_t rank = 0;
+                    for (int o = 0; o < 4; ++o)
+                        if (color[gv[o]] < color[gv[q]] || (color[gv[o]] == color[gv[q]] && o < q))
+                            ++rank;
+                    packed[q] = gv[q] | (rank << 30);
+                }
+                double const* G = d.GP + 12 * size_t(e);
+                double const w = d.wg[e], mu = d.mu[e], la = d.lambda[e];
+                TetRecord& r    = hrec[t0 + e];
+                r.v             = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                r.g1            = make_float4(float(G[3]), float(G[4]), float(G[5]), float(w * mu));
+                r.g2            = make_float4(float(G[6]), float(G[7]), float(G[8]), float(w * la));
+                r.g3            = make_float4(float(G[9]), float(G[10]), float(G[11]), float(1.0 + mu / la));
             }
             v0 += d.n_vertices;
             t0 += d.n_tets;
@@ -274,8 +298,8 @@ class VbdSystem
             std::vector<int32_t> cur(vPtr.begin(), vPtr.end() - 1);
             for (int32_t e = 0; e < nT; ++e)
             {
-                int4 const t   = htv[e];
-                int const a[4] = {t.x, t.y, t.z, t.w};
+                uint4 const t       = hrec[e].v;
+                uint32_t const a[4] = {t.x & kIndexMask, t.y & kIndexMask, t.z & kIndexMask, t.w & kIndexMask};
                 for (int q = 0; q < 4; ++q)
                     vInc[cur[a[q]]++] = (uint32_t(e) << 2) | uint32_t(q);
             }
@@ -325,8 +349,7 @@ class VbdSystem
         vprev.allocate(nV);
         m.allocate(nV);
         staging.allocate(size_t(nV) * 3);
-        tv.allocate(nT);
-        tg.allocate(size_t(nT) * 3);
+        tets.allocate(nT);
         solve.allocate(nFree);
         incPtr.allocate(size_t(nFree) + 1);
         inc.allocate(hInc.size());
@@ -334,15 +357,14 @@ class VbdSystem
         red.allocate(1);
         if (acceleration == PBGB_ACCEL_CHEBYSHEV)
         {
-            xkm1.allocate(nV);
-            xkm2.allocate(nV);
+            h0.allocate(nV);
+            h1.allocate(nV);
         }
         x.upload(hx.data(), nV, stream);
         v.upload(hv.data(), nV, stream);
         aext.upload(ha.data(), nV, stream);
         m.upload(hm.data(), nV, stream);
-        tv.upload(htv.data(), nT, stream);
-        tg.upload(htg.data(), htg.size(), stream);
+        tets.upload(hrec.data(), nT, stream);
         solve.upload(hsolve.data(), nFree, stream);
         incPtr.upload(hIncPtr.data(), hIncPtr.size(), stream);
         inc.upload(hInc.data(), hInc.size(), stream);
@@ -366,6 +388,9 @@ class VbdSystem
         p.v            = v.get();
         p.aext         = aext.get();
         p.vprev        = vprev.get();
+        p.h0           = h0.get();
+        p.h1           = h1.get();
+        p.result       = x.get();
         p.m            = m.get();
         p.flags        = flags.get();
         p.n            = nV;
@@ -379,15 +404,19 @@ class VbdSystem
     // Enqueue one full step on `stream` (captured into a graph by step()).
     void enqueueStep(float dt, int32_t iterations, int32_t substeps)
     {
-        float const h  = dt / float(substeps);
-        float const h2 = h * h;
-        SubstepParams const sp = substepParams(h);
+        float const h   = dt / float(substeps);
+        float const h2  = h * h;
+        bool const cheb = acceleration == PBGB_ACCEL_CHEBYSHEV;
+        SubstepParams sp = substepParams(h);
+        if (!cheb)
+            sp.h0 = sp.h1 = nullptr;
+        else if (iterations > 0)
+            sp.result = ((iterations - 1) % 2 == 0) ? h0.get() : h1.get();
         SweepParams w{};
         w.x        = x.get();
         w.xt       = xt.get();
         w.xtilde   = xtilde.get();
-        w.tv       = tv.get();
-        w.tg       = tg.get();
+        w.tets     = tets.get();
         w.solve    = solve.get();
         w.incPtr   = incPtr.get();
         w.inc      = inc.get();
@@ -398,6 +427,7 @@ class VbdSystem
         int const L = lanesToUse();
         if (profiling)
             ensureEvents(size_t(iterations) * size_t(substeps));
+        float4* H[2] = {h0.get(), h1.get()};
         for (int32_t s = 0; s < substeps; ++s)
         {
             check(launch_begin_substep(sp, stream), "begin_substep");
@@ -405,6 +435,14 @@ class VbdSystem
             double const rho2 = rho * rho;
             for (int32_t k = 0; k < iterations; ++k)
             {
+                if (cheb)
+                {
+                    omega   = chebyshev_omega<double>(k, rho2, omega, chebFormula);
+                    w.omega = float(omega);
+                    w.k     = k;
+                    w.hprev = H[(k + 1) % 2];
+                    w.hcur  = H[k % 2];
+                }
                 size_t const slot = size_t(s) * size_t(iterations) + size_t(k);
                 if (profiling)
                     check(cudaEventRecordWithFlags(evBegin[slot], stream, cudaEventRecordExternal), "cudaEventRecord");
@@ -412,16 +450,10 @@ class VbdSystem
                 {
                     w.begin = colorPtr[c];
                     w.end   = colorPtr[c + 1];
-                    check(launch_sweep(w, L, block, stream), "sweep");
+                    check(launch_sweep(w, L, block, cheb, stream), "sweep");
                 }
                 if (profiling)
                     check(cudaEventRecordWithFlags(evEnd[slot], stream, cudaEventRecordExternal), "cudaEventRecord");
-                if (acceleration == PBGB_ACCEL_CHEBYSHEV)
-                {
-                    omega = chebyshev_omega<double>(k, rho2, omega, chebFormula);
-                    ChebyshevParams cp{x.get(), xkm1.get(), xkm2.get(), nV, k, float(omega)};
-                    check(launch_chebyshev(cp, stream), "chebyshev");
-                }
             }
             check(launch_end_substep(sp, stream), "end_substep");
         }
@@ -432,7 +464,6 @@ class VbdSystem
         int64_t perIter = 0;
         for (int32_t c = 0; c < nColors; ++c)
             perIter += colorPtr[c + 1] > colorPtr[c] ? 1 : 0;
-        perIter += acceleration == PBGB_ACCEL_CHEBYSHEV && nV > 0 ? 1 : 0;
         return int64_t(substeps) * (2 * (nV > 0 ? 1 : 0) + int64_t(iterations) * perIter);
     }
 
@@ -501,8 +532,7 @@ class VbdSystem
         p.x      = x.get();
         p.xtilde = xtilde.get();
         p.m      = m.get();
-        p.tv     = tv.get();
-        p.tg     = tg.get();
+        p.tets   = tets.get();
         p.nV     = nV;
         p.nT     = nT;
         p.dt2    = dt * dt;

@@ -19,34 +19,42 @@ __device__ __forceinline__ void load3(float4 const v, float* o)
 // l takes incidences l, l+L, ...; the 10 accumulated floats are then reduced with xor shuffles
 // and lane 0 applies damping, inertia and the 3x3 Newton step, writing x in place.  Vertices of a
 // colour share no tet, so the in-place write races with no reader of this launch.
-template <int L>
+//
+// CHEB: the Chebyshev update of the reference (applied to all vertices after each full sweep,
+// sim/vbd/ChebyshevIntegrator.cpp:15-32) is fused in.  Only vertex i's own values enter its
+// update, so it is applied right after i's solve, with two position buffers keeping the
+// reference's ordering: a neighbour of lower colour rank (already solved in iteration k) is read
+// from x (raw iterate k), one of higher rank from hprev (accelerated iterate k-1).  hcur holds
+// iterate k-2 on entry and receives the accelerated iterate k.
+template <int L, bool CHEB>
 __global__ void __launch_bounds__(256) sweep_kernel(SweepParams p)
 {
-    int const tid   = blockIdx.x * blockDim.x + threadIdx.x;
-    int const s     = p.begin + tid / L;
-    int const lane  = tid & (L - 1);
+    int const tid    = blockIdx.x * blockDim.x + threadIdx.x;
+    int const s      = p.begin + tid / L;
+    int const lane   = tid & (L - 1);
     bool const valid = s < p.end;
 
     VertexBlock<float> b;
     zero(b);
-    int i = 0;
+    int i       = 0;
     float xi[3] = {0.f, 0.f, 0.f};
     if (valid)
     {
         i = __ldg(p.solve + s);
-        load3(p.x[i], xi);
+        load3(CHEB ? p.hprev[i] : p.x[i], xi);
         int const k1 = __ldg(p.incPtr + s + 1);
         for (int k = __ldg(p.incPtr + s) + lane; k < k1; k += L)
         {
-            uint32_t const q = __ldg(p.inc + k);
-            int const e      = int(q >> 2);
-            int const il     = int(q & 3u);
-            int4 const t     = __ldg(p.tv + e);
-            float4 const g1  = __ldg(p.tg + 3 * e + 0);
-            float4 const g2  = __ldg(p.tg + 3 * e + 1);
-            float4 const g3  = __ldg(p.tg + 3 * e + 2);
+            uint32_t const q   = __ldg(p.inc + k);
+            TetRecord const* r = p.tets + (q >> 2);
+            int const il       = int(q & 3u);
+            uint4 const t      = __ldg(&r->v);
+            float4 const g1    = __ldg(&r->g1);
+            float4 const g2    = __ldg(&r->g2);
+            float4 const g3    = __ldg(&r->g3);
+            uint32_t const tv[4] = {t.x, t.y, t.z, t.w};
+            uint32_t const own   = tv[il] >> 30;
             float xa[4][3];
-            int const vid[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
             for (int a = 0; a < 4; ++a)
             {
@@ -57,7 +65,12 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepParams p)
                     xa[a][2] = xi[2];
                 }
                 else
-                    load3(__ldg(p.x + vid[a]), xa[a]);
+                {
+                    float4 const* src = p.x;
+                    if (CHEB && (tv[a] >> 30) > own)
+                        src = p.hprev;
+                    load3(__ldg(src + (tv[a] & kIndexMask)), xa[a]);
+                }
             }
             float const G1[3] = {g1.x, g1.y, g1.z};
             float const G2[3] = {g2.x, g2.y, g2.z};
@@ -78,11 +91,25 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepParams p)
     }
     if (!valid || lane != 0)
         return;
-    float4 const xt4 = p.xt[i];
-    float4 const xl4 = p.xtilde[i];
+    float4 const xt4  = p.xt[i];
+    float4 const xl4  = p.xtilde[i];
     float const xt[3] = {xt4.x, xt4.y, xt4.z};
     float const xl[3] = {xl4.x, xl4.y, xl4.z};
-    if (newton_update(b, xt, xl, xt4.w, p.h, p.h2, p.kD, p.detHZero, xi))
+    bool const moved  = newton_update(b, xt, xl, xt4.w, p.h, p.h2, p.kD, p.detHZero, xi);
+    if (CHEB)
+    {
+        // Raw iterate k (even when the Newton step was skipped: later colours read it).
+        p.x[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
+        if (p.k > 1)
+        {
+            float4 const km2 = p.hcur[i];
+            xi[0]            = p.omega * (xi[0] - km2.x) + km2.x;
+            xi[1]            = p.omega * (xi[1] - km2.y) + km2.y;
+            xi[2]            = p.omega * (xi[2] - km2.z) + km2.z;
+        }
+        p.hcur[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
+    }
+    else if (moved)
         p.x[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
 }
 
@@ -113,7 +140,13 @@ __global__ void begin_substep_kernel(SubstepParams p)
         0.f);
     float x0[3];
     initial_position(xt, vm, vt, a, p.h, p.h2, p.strategy, FLT_MIN, x0);
-    p.x[i] = make_float4(x0[0], x0[1], x0[2], 0.f);
+    float4 const x04 = make_float4(x0[0], x0[1], x0[2], 0.f);
+    p.x[i]           = x04;
+    if (p.h0)
+    {
+        p.h0[i] = x04;
+        p.h1[i] = x04;
+    }
 }
 
 // End of a substep: v = (x - xt)/h (sim/vbd/Kernels.h:121-129); the previous velocity is kept
@@ -124,9 +157,11 @@ __global__ void end_substep_kernel(SubstepParams p)
     int const i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n)
         return;
-    float4 const x4  = p.x[i];
+    float4 const x4  = p.result[i];
     float4 const xt4 = p.xt[i];
     float4 const vo  = p.v[i];
+    if (p.result != p.x)
+        p.x[i] = x4;
     float const inv  = 1.f / p.h;
     float4 const vn  = make_float4((x4.x - xt4.x) * inv, (x4.y - xt4.y) * inv, (x4.z - xt4.z) * inv, 0.f);
     if (p.gpuSemantics)
@@ -136,27 +171,6 @@ __global__ void end_substep_kernel(SubstepParams p)
                         isfinite(vn.y) && isfinite(vn.z);
     if (!finite)
         atomicOr(p.flags, 1);
-}
-
-// Chebyshev semi-iterative update after each sweep (sim/vbd/ChebyshevIntegrator.cpp:15-32,
-// gpu/impl/vbd/ChebyshevIntegrator.cu:38-59).
-__global__ void chebyshev_kernel(ChebyshevParams p)
-{
-    int const i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n)
-        return;
-    float4 xk        = p.x[i];
-    float4 const km1 = p.xkm1[i];
-    if (p.k > 1)
-    {
-        float4 const km2 = p.xkm2[i];
-        xk.x             = p.omega * (xk.x - km2.x) + km2.x;
-        xk.y             = p.omega * (xk.y - km2.y) + km2.y;
-        xk.z             = p.omega * (xk.z - km2.z) + km2.z;
-        p.x[i]           = xk;
-    }
-    p.xkm2[i] = km1;
-    p.xkm1[i] = xk;
 }
 
 __device__ __forceinline__ double warp_sum(double v)
@@ -169,10 +183,12 @@ __device__ __forceinline__ double warp_sum(double v)
 // Tet geometry helper: F (columns f[c]) of tet e at positions x.
 __device__ __forceinline__ void tet_F(EnergyParams const& p, int e, float f[3][3], int4& t, float4& g1, float4& g2, float4& g3)
 {
-    t  = p.tv[e];
-    g1 = p.tg[3 * e + 0];
-    g2 = p.tg[3 * e + 1];
-    g3 = p.tg[3 * e + 2];
+    TetRecord const& r = p.tets[e];
+    uint4 const tu     = r.v;
+    t  = make_int4(int(tu.x & kIndexMask), int(tu.y & kIndexMask), int(tu.z & kIndexMask), int(tu.w & kIndexMask));
+    g1 = r.g1;
+    g2 = r.g2;
+    g3 = r.g3;
     float4 const x0 = p.x[t.x], x1 = p.x[t.y], x2 = p.x[t.z], x3 = p.x[t.w];
     float const d1[3] = {x1.x - x0.x, x1.y - x0.y, x1.z - x0.z};
     float const d2[3] = {x2.x - x0.x, x2.y - x0.y, x2.z - x0.z};
@@ -300,23 +316,29 @@ inline int blocks_for(int64_t n, int block)
 
 } // namespace
 
-cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, cudaStream_t s)
+template <bool CHEB>
+cudaError_t launch_sweep_t(SweepParams const& p, int lanes, int g, int block, cudaStream_t s)
+{
+    switch (lanes)
+    {
+        case 1: sweep_kernel<1, CHEB><<<g, block, 0, s>>>(p); break;
+        case 2: sweep_kernel<2, CHEB><<<g, block, 0, s>>>(p); break;
+        case 4: sweep_kernel<4, CHEB><<<g, block, 0, s>>>(p); break;
+        case 8: sweep_kernel<8, CHEB><<<g, block, 0, s>>>(p); break;
+        case 16: sweep_kernel<16, CHEB><<<g, block, 0, s>>>(p); break;
+        case 32: sweep_kernel<32, CHEB><<<g, block, 0, s>>>(p); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, cudaStream_t s)
 {
     int64_t const n = int64_t(p.end - p.begin) * lanes;
     if (n <= 0)
         return cudaSuccess;
     int const g = blocks_for(n, block);
-    switch (lanes)
-    {
-        case 1: sweep_kernel<1><<<g, block, 0, s>>>(p); break;
-        case 2: sweep_kernel<2><<<g, block, 0, s>>>(p); break;
-        case 4: sweep_kernel<4><<<g, block, 0, s>>>(p); break;
-        case 8: sweep_kernel<8><<<g, block, 0, s>>>(p); break;
-        case 16: sweep_kernel<16><<<g, block, 0, s>>>(p); break;
-        case 32: sweep_kernel<32><<<g, block, 0, s>>>(p); break;
-        default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
+    return chebyshev ? launch_sweep_t<true>(p, lanes, g, block, s) : launch_sweep_t<false>(p, lanes, g, block, s);
 }
 
 cudaError_t launch_begin_substep(SubstepParams const& p, cudaStream_t s)
@@ -332,14 +354,6 @@ cudaError_t launch_end_substep(SubstepParams const& p, cudaStream_t s)
     if (p.n <= 0)
         return cudaSuccess;
     end_substep_kernel<<<blocks_for(p.n, 256), 256, 0, s>>>(p);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_chebyshev(ChebyshevParams const& p, cudaStream_t s)
-{
-    if (p.n <= 0)
-        return cudaSuccess;
-    chebyshev_kernel<<<blocks_for(p.n, 256), 256, 0, s>>>(p);
     return cudaGetLastError();
 }
 

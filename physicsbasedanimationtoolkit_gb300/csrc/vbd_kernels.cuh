@@ -2,15 +2,14 @@
 // system; indices global):
 //
 //   x, xt, xtilde, v, aext, vprev : float4 per vertex (xyz, w unused except xt.w = lumped mass)
-//   tv    : int4   per tet   — the 4 vertex indices
-//   tg    : 3 float4 per tet — (GP row 1, wg*mu), (GP row 2, wg*lambda), (GP row 3, alpha)
-//           where GP row 0 = -(rows 1+2+3) and alpha = 1 + mu/lambda
+//   h0, h1: float4 per vertex, the Chebyshev iterate history (allocated with acceleration only)
+//   tets  : one 64-byte TetRecord per tet (below)
 //   solve : free vertices, colour-major; inside a colour sorted by decreasing degree
 //   incPtr: offsets of each solved vertex's incidences; inc: (tet << 2 | local index), tets
 //           ascending
 //
-// A tet record is 64 B and is read by each of its 4 vertices in 4 different colour passes of an
-// iteration; the record table stays L2-resident for meshes whose table fits in L2.
+// A tet record is read by each of its 4 vertices in 4 different colour passes of an iteration;
+// being 64-byte aligned it costs exactly two 32-byte sectors per visit.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -20,13 +19,29 @@
 
 namespace pbgb {
 
+// One tetrahedron.  v.{x,y,z,w}: vertex indices in bits 0-29; bits 30-31 hold the vertex's rank
+// (0..3) by colour inside the tet, which tells a vertex solve whether a neighbour was already
+// updated in the current iteration (lower rank) or not (higher rank).
+//   g1 = (GP row 1, wg*mu), g2 = (GP row 2, wg*lambda), g3 = (GP row 3, alpha = 1 + mu/lambda),
+// with GP row 0 = -(rows 1 + 2 + 3).
+struct __align__(64) TetRecord
+{
+    uint4 v;
+    float4 g1;
+    float4 g2;
+    float4 g3;
+};
+
+uint32_t constexpr kIndexMask = 0x3FFFFFFFu;
+
 struct SweepParams
 {
-    float4* __restrict__ x;
+    float4* __restrict__ x;            // positions (with Chebyshev: raw sweep results)
+    float4 const* __restrict__ hprev;  // Chebyshev: accelerated iterate k-1 (read)
+    float4* __restrict__ hcur;         // Chebyshev: iterate k-2 in, accelerated iterate k out
     float4 const* __restrict__ xt;     // .w = lumped mass
     float4 const* __restrict__ xtilde; // inertial target
-    int4 const* __restrict__ tv;
-    float4 const* __restrict__ tg;
+    TetRecord const* __restrict__ tets;
     int32_t const* __restrict__ solve;
     int32_t const* __restrict__ incPtr;
     uint32_t const* __restrict__ inc;
@@ -36,6 +51,8 @@ struct SweepParams
     float h2;
     float kD;
     float detHZero;
+    int32_t k;   // iteration index (Chebyshev)
+    float omega; // Chebyshev weight of iteration k
 };
 
 struct SubstepParams
@@ -46,6 +63,9 @@ struct SubstepParams
     float4* __restrict__ v;
     float4 const* __restrict__ aext;
     float4* __restrict__ vprev;
+    float4* __restrict__ h0; // Chebyshev history (nullptr without acceleration)
+    float4* __restrict__ h1;
+    float4 const* __restrict__ result; // buffer holding the final iterate at end of substep
     float const* __restrict__ m;
     int32_t* __restrict__ flags;
     int32_t n;
@@ -55,23 +75,12 @@ struct SubstepParams
     int32_t gpuSemantics;
 };
 
-struct ChebyshevParams
-{
-    float4* __restrict__ x;
-    float4* __restrict__ xkm1;
-    float4* __restrict__ xkm2;
-    int32_t n;
-    int32_t k;
-    float omega;
-};
-
 struct EnergyParams
 {
     float4 const* __restrict__ x;
     float4 const* __restrict__ xtilde;
     float const* __restrict__ m;
-    int4 const* __restrict__ tv;
-    float4 const* __restrict__ tg;
+    TetRecord const* __restrict__ tets;
     int32_t nV;
     int32_t nT;
     double dt2;
@@ -79,10 +88,9 @@ struct EnergyParams
 };
 
 // Launchers (defined in vbd_kernels.cu).  Each returns the launch status.
-cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, cudaStream_t s);
+cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, cudaStream_t s);
 cudaError_t launch_begin_substep(SubstepParams const& p, cudaStream_t s);
 cudaError_t launch_end_substep(SubstepParams const& p, cudaStream_t s);
-cudaError_t launch_chebyshev(ChebyshevParams const& p, cudaStream_t s);
 cudaError_t launch_objective(EnergyParams const& p, cudaStream_t s);
 cudaError_t launch_gradient(EnergyParams const& p, cudaStream_t s);
 cudaError_t launch_pack3(float const* in3, float4* out4, int32_t n, cudaStream_t s);
