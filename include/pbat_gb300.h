@@ -117,7 +117,8 @@ typedef struct pbgb_vbd_desc
     const double* v;      /* 3 x nV velocities (NULL: zero) */
     const double* aext;   /* 3 x nV external accelerations (NULL: (0,0,-9.81)) */
     const double* m;      /* nV lumped masses (required) */
-    const double* GP;     /* 12 nT shape-function gradients, row-major 4x3 per tet (required) */
+    const double* GP;     /* 12 nT shape-function gradients, row-major 4x3 per tet (optional: the
+                             device recomputes them from the rest positions X) */
     const double* wg;     /* nT quadrature weights (required) */
     const double* mu;     /* nT first Lame coefficients (required) */
     const double* lambda; /* nT second Lame coefficients (required) */
@@ -131,6 +132,7 @@ typedef struct pbgb_vbd_desc
     double rho;                /* Chebyshev spectral radius estimate, 0 < rho < 1 */
     int32_t chebyshev_formula; /* PBGB_CHEBYSHEV_* */
     int32_t semantics;         /* PBGB_SEMANTICS_* */
+    const double* X;           /* 3 x nV rest positions (NULL: x) */
 } pbgb_vbd_desc;
 
 typedef struct pbgb_vbd pbgb_vbd; /* opaque integrator handle */

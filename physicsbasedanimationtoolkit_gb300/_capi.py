@@ -63,6 +63,7 @@ class VbdDesc(C.Structure):
         ("rho", C.c_double),
         ("chebyshev_formula", C.c_int32),
         ("semantics", C.c_int32),
+        ("X", C.c_void_p),
     ]
 
 

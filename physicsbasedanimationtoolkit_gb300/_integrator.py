@@ -29,6 +29,7 @@ def make_desc(data, semantics):
     nV, nT = data.X.shape[1], data.E.shape[1]
     keep = dict(
         x=_capi.f64(np.asarray(data.x).T),
+        X=_capi.f64(np.asarray(data.X).T),
         T=_capi.i32(np.asarray(data.E).T),
         v=_capi.f64(np.asarray(data.v).T),
         aext=_capi.f64(np.asarray(data.aext).T),

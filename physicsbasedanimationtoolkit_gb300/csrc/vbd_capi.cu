@@ -94,7 +94,7 @@ class VbdSystem
 
     // Device state
     cudaStream_t stream = nullptr;
-    DeviceArray<float4> x, xt, xtilde, v, aext, vprev, h0, h1;
+    DeviceArray<float4> x, xt, xtilde, v, aext, vprev, h0, h1, X;
     DeviceArray<float> m, staging;
     DeviceArray<TetRecord> tets;
     DeviceArray<int32_t> solve, incPtr, flags;
@@ -180,7 +180,7 @@ class VbdSystem
         {
             auto const& d = descs[b];
             if (d.n_vertices < 0 || d.n_tets < 0 || !d.x || (d.n_tets > 0 && !d.T) || !d.m ||
-                (d.n_tets > 0 && (!d.GP || !d.wg || !d.mu || !d.lambda)) || d.n_partitions < 0 ||
+                (d.n_tets > 0 && (!d.wg || !d.mu || !d.lambda)) || d.n_partitions < 0 ||
                 d.n_partitions > kMaxColors || !d.Pptr || (d.Pptr[d.n_partitions] > 0 && !d.Padj))
                 throw std::invalid_argument("pbgb_vbd_desc: missing or invalid field");
             for (int64_t k = 0; k < int64_t(d.n_tets) * 4; ++k)
@@ -217,7 +217,7 @@ class VbdSystem
         semantics      = d0.semantics;
 
         // Host staging of the concatenated layout.
-        std::vector<float4> hx(nV), hv(nV), ha(nV);
+        std::vector<float4> hx(nV), hv(nV), ha(nV), hX(nV);
         std::vector<float> hm(nV);
         std::vector<TetRecord> hrec(nT);
         std::vector<int32_t> deg(nV, 0);
@@ -258,6 +258,8 @@ class VbdSystem
                 else
                     ha[v0 + i] = make_float4(0.f, 0.f, -9.81f, 0.f);
                 hm[v0 + i] = float(d.m[i]);
+                double const* R = (d.X ? d.X : d.x) + 3 * size_t(i);
+                hX[v0 + i]      = make_float4(float(R[0]), float(R[1]), float(R[2]), 0.f);
             }
             for (int32_t e = 0; e < d.n_tets; ++e)
             {
@@ -278,13 +280,10 @@ class VbdSystem
                             ++rank;
                     packed[q] = gv[q] | (rank << 30);
                 }
-                double const* G = d.GP + 12 * size_t(e);
                 double const w = d.wg[e], mu = d.mu[e], la = d.lambda[e];
-                TetRecord& r    = hrec[t0 + e];
-                r.v             = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                r.g1            = make_float4(float(G[3]), float(G[4]), float(G[5]), float(w * mu));
-                r.g2            = make_float4(float(G[6]), float(G[7]), float(G[8]), float(w * la));
-                r.g3            = make_float4(float(G[9]), float(G[10]), float(G[11]), float(1.0 + mu / la));
+                TetRecord& r   = hrec[t0 + e];
+                r.v            = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                r.mat          = make_float4(float(w * mu), float(w * la), float(1.0 + mu / la), 0.f);
             }
             v0 += d.n_vertices;
             t0 += d.n_tets;
@@ -350,6 +349,7 @@ class VbdSystem
         m.allocate(nV);
         staging.allocate(size_t(nV) * 3);
         tets.allocate(nT);
+        X.allocate(nV);
         solve.allocate(nFree);
         incPtr.allocate(size_t(nFree) + 1);
         inc.allocate(hInc.size());
@@ -365,6 +365,7 @@ class VbdSystem
         aext.upload(ha.data(), nV, stream);
         m.upload(hm.data(), nV, stream);
         tets.upload(hrec.data(), nT, stream);
+        X.upload(hX.data(), nV, stream);
         solve.upload(hsolve.data(), nFree, stream);
         incPtr.upload(hIncPtr.data(), hIncPtr.size(), stream);
         inc.upload(hInc.data(), hInc.size(), stream);
@@ -417,6 +418,7 @@ class VbdSystem
         w.xt       = xt.get();
         w.xtilde   = xtilde.get();
         w.tets     = tets.get();
+        w.X        = X.get();
         w.solve    = solve.get();
         w.incPtr   = incPtr.get();
         w.inc      = inc.get();
@@ -533,6 +535,7 @@ class VbdSystem
         p.xtilde = xtilde.get();
         p.m      = m.get();
         p.tets   = tets.get();
+        p.X      = X.get();
         p.nV     = nV;
         p.nT     = nT;
         p.dt2    = dt * dt;
@@ -964,12 +967,21 @@ PBGB_API int pbgb_debug_vertex_block(
     for (int32_t q = 0; q < n; ++q)
     {
         double const* xq = xe + 12 * size_t(q);
-        double const* G  = GPs + 12 * size_t(q);
+        double const* G4 = GPs + 12 * size_t(q);
         if (il[q] < 0 || il[q] > 3)
             return fail(nullptr, kInvalid, "local index out of range");
-        pbgb::accumulate_tet(
-            b, xq, xq + 3, xq + 6, xq + 9, G + 3, G + 6, G + 9, il[q], wg[q] * mu[q], wg[q] * lambda[q],
-            1.0 + mu[q] / lambda[q]);
+        // Same own-corner-relative form as the device sweep.
+        double d[3][3], G[3][3];
+        for (int m = 0; m < 3; ++m)
+        {
+            int const a = (il[q] + 1 + m) & 3;
+            for (int r = 0; r < 3; ++r)
+            {
+                d[m][r] = xq[3 * a + r] - xq[3 * il[q] + r];
+                G[m][r] = G4[3 * a + r];
+            }
+        }
+        pbgb::accumulate_tet(b, d, G, wg[q] * mu[q], wg[q] * lambda[q], 1.0 + mu[q] / lambda[q]);
     }
     pbgb::newton_update(b, xt, xtilde, m, h, h2, kD, detHZero, x, g, H);
     return kOk;

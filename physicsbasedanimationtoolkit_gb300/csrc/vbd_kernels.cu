@@ -14,6 +14,11 @@ __device__ __forceinline__ void load3(float4 const v, float* o)
     o[2] = v.z;
 }
 
+__device__ __forceinline__ uint32_t corner(uint4 const& t, int a)
+{
+    return a == 0 ? t.x : (a == 1 ? t.y : (a == 2 ? t.z : t.w));
+}
+
 // Per-colour Gauss-Seidel sweep (reference: VbdIteration, gpu/impl/vbd/Kernels.cuh:148-233, and
 // Integrator::SolveVertex, sim/vbd/Integrator.cpp:98-136).  L lanes cooperate on one vertex: lane
 // l takes incidences l, l+L, ...; the 10 accumulated floats are then reduced with xor shuffles
@@ -27,7 +32,7 @@ __device__ __forceinline__ void load3(float4 const v, float* o)
 // from x (raw iterate k), one of higher rank from hprev (accelerated iterate k-1).  hcur holds
 // iterate k-2 on entry and receives the accelerated iterate k.
 template <int L, bool CHEB>
-__global__ void __launch_bounds__(256) sweep_kernel(SweepParams p)
+__global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
 {
     int const tid    = blockIdx.x * blockDim.x + threadIdx.x;
     int const s      = p.begin + tid / L;
@@ -42,6 +47,8 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepParams p)
     {
         i = __ldg(p.solve + s);
         load3(CHEB ? p.hprev[i] : p.x[i], xi);
+        float Xi[3];
+        load3(__ldg(p.X + i), Xi);
         int const k1 = __ldg(p.incPtr + s + 1);
         for (int k = __ldg(p.incPtr + s) + lane; k < k1; k += L)
         {
@@ -49,33 +56,29 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepParams p)
             TetRecord const* r = p.tets + (q >> 2);
             int const il       = int(q & 3u);
             uint4 const t      = __ldg(&r->v);
-            float4 const g1    = __ldg(&r->g1);
-            float4 const g2    = __ldg(&r->g2);
-            float4 const g3    = __ldg(&r->g3);
-            uint32_t const tv[4] = {t.x, t.y, t.z, t.w};
-            uint32_t const own   = tv[il] >> 30;
-            float xa[4][3];
+            float4 const mat   = __ldg(&r->mat);
+            uint32_t const own = corner(t, il) >> 30;
+            float d[3][3], e[3][3];
 #pragma unroll
-            for (int a = 0; a < 4; ++a)
+            for (int m = 0; m < 3; ++m)
             {
-                if (a == il)
-                {
-                    xa[a][0] = xi[0];
-                    xa[a][1] = xi[1];
-                    xa[a][2] = xi[2];
-                }
-                else
-                {
-                    float4 const* src = p.x;
-                    if (CHEB && (tv[a] >> 30) > own)
-                        src = p.hprev;
-                    load3(__ldg(src + (tv[a] & kIndexMask)), xa[a]);
-                }
+                uint32_t const ta = corner(t, (il + 1 + m) & 3);
+                uint32_t const j  = ta & kIndexMask;
+                float4 const* src = p.x;
+                if (CHEB && (ta >> 30) > own)
+                    src = p.hprev;
+                float4 const xa = __ldg(src + j);
+                float4 const Xa = __ldg(p.X + j);
+                d[m][0] = xa.x - xi[0];
+                d[m][1] = xa.y - xi[1];
+                d[m][2] = xa.z - xi[2];
+                e[m][0] = Xa.x - Xi[0];
+                e[m][1] = Xa.y - Xi[1];
+                e[m][2] = Xa.z - Xi[2];
             }
-            float const G1[3] = {g1.x, g1.y, g1.z};
-            float const G2[3] = {g2.x, g2.y, g2.z};
-            float const G3[3] = {g3.x, g3.y, g3.z};
-            accumulate_tet(b, xa[0], xa[1], xa[2], xa[3], G1, G2, G3, il, g1.w, g2.w, g3.w);
+            float G[3][3];
+            rest_gradients(e, G);
+            accumulate_tet(b, d, G, mat.x, mat.y, mat.z);
         }
     }
 #pragma unroll
@@ -180,23 +183,33 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
-// Tet geometry helper: F (columns f[c]) of tet e at positions x.
-__device__ __forceinline__ void tet_F(EnergyParams const& p, int e, float f[3][3], int4& t, float4& g1, float4& g2, float4& g3)
+// Tet geometry helper: deformation gradient F (columns f[c]) of tet e, the shape-function
+// gradients of its 4 corners (G4[a]) and its material scalars.
+__device__ __forceinline__ void tet_F(EnergyParams const& p, int e, float f[3][3], int4& t, float G4[4][3], float4& mat)
 {
     TetRecord const& r = p.tets[e];
     uint4 const tu     = r.v;
-    t  = make_int4(int(tu.x & kIndexMask), int(tu.y & kIndexMask), int(tu.z & kIndexMask), int(tu.w & kIndexMask));
-    g1 = r.g1;
-    g2 = r.g2;
-    g3 = r.g3;
-    float4 const x0 = p.x[t.x], x1 = p.x[t.y], x2 = p.x[t.z], x3 = p.x[t.w];
-    float const d1[3] = {x1.x - x0.x, x1.y - x0.y, x1.z - x0.z};
-    float const d2[3] = {x2.x - x0.x, x2.y - x0.y, x2.z - x0.z};
-    float const d3[3] = {x3.x - x0.x, x3.y - x0.y, x3.z - x0.z};
-    float const G1[3] = {g1.x, g1.y, g1.z}, G2[3] = {g2.x, g2.y, g2.z}, G3[3] = {g3.x, g3.y, g3.z};
+    t   = make_int4(int(tu.x & kIndexMask), int(tu.y & kIndexMask), int(tu.z & kIndexMask), int(tu.w & kIndexMask));
+    mat = r.mat;
+    int const vid[4] = {t.x, t.y, t.z, t.w};
+    float4 const X0 = p.X[vid[0]], x0 = p.x[vid[0]];
+    float d[3][3], E[3][3], G[3][3];
+    for (int m = 0; m < 3; ++m)
+    {
+        float4 const Xa = p.X[vid[m + 1]], xa = p.x[vid[m + 1]];
+        d[m][0] = xa.x - x0.x, d[m][1] = xa.y - x0.y, d[m][2] = xa.z - x0.z;
+        E[m][0] = Xa.x - X0.x, E[m][1] = Xa.y - X0.y, E[m][2] = Xa.z - X0.z;
+    }
+    rest_gradients(E, G);
     for (int c = 0; c < 3; ++c)
-        for (int r = 0; r < 3; ++r)
-            f[c][r] = d1[r] * G1[c] + d2[r] * G2[c] + d3[r] * G3[c];
+    {
+        for (int rr = 0; rr < 3; ++rr)
+            f[c][rr] = d[0][rr] * G[0][c] + d[1][rr] * G[1][c] + d[2][rr] * G[2][c];
+        G4[0][c] = -(G[0][c] + G[1][c] + G[2][c]);
+        G4[1][c] = G[0][c];
+        G4[2][c] = G[1][c];
+        G4[3][c] = G[2][c];
+    }
 }
 
 // Objective of the backward-Euler step (sim/vbd/Integrator.cpp:138-165): per-entity terms in FP32,
@@ -215,10 +228,10 @@ __global__ void objective_kernel(EnergyParams p)
         }
         if (j < p.nT)
         {
-            float f[3][3];
+            float f[3][3], G4[4][3];
             int4 t;
-            float4 g1, g2, g3;
-            tet_F(p, j, f, t, g1, g2, g3);
+            float4 mat;
+            tet_F(p, j, f, t, G4, mat);
             double I2 = 0.0;
             for (int c = 0; c < 3; ++c)
                 for (int r = 0; r < 3; ++r)
@@ -226,8 +239,8 @@ __global__ void objective_kernel(EnergyParams p)
             double const J = double(f[0][0]) * (double(f[1][1]) * f[2][2] - double(f[1][2]) * f[2][1]) -
                              double(f[1][0]) * (double(f[0][1]) * f[2][2] - double(f[0][2]) * f[2][1]) +
                              double(f[2][0]) * (double(f[0][1]) * f[1][2] - double(f[0][2]) * f[1][1]);
-            double const a = J - double(g3.w);
-            acc += p.dt2 * (0.5 * double(g2.w) * a * a + 0.5 * double(g1.w) * (I2 - 3.0));
+            double const a = J - double(mat.z);
+            acc += p.dt2 * (0.5 * double(mat.y) * a * a + 0.5 * double(mat.x) * (I2 - 3.0));
         }
     }
     acc = warp_sum(acc);
@@ -252,10 +265,10 @@ __global__ void gradient_kernel(EnergyParams p)
         }
         if (j < p.nT)
         {
-            float f[3][3];
+            float f[3][3], G[4][3];
             int4 t;
-            float4 g1, g2, g3;
-            tet_F(p, j, f, t, g1, g2, g3);
+            float4 mat;
+            tet_F(p, j, f, t, G, mat);
             float k[3][3];
             k[0][0] = f[1][1] * f[2][2] - f[1][2] * f[2][1];
             k[0][1] = f[1][2] * f[2][0] - f[1][0] * f[2][2];
@@ -267,17 +280,12 @@ __global__ void gradient_kernel(EnergyParams p)
             k[2][1] = f[0][2] * f[1][0] - f[0][0] * f[1][2];
             k[2][2] = f[0][0] * f[1][1] - f[0][1] * f[1][0];
             float const J  = f[0][0] * k[0][0] + f[0][1] * k[0][1] + f[0][2] * k[0][2];
-            float const sl = g2.w * (J - g3.w);
+            float const sl = mat.y * (J - mat.z);
             // P = mu' F + lambda' (J - alpha) cof F ; dE/dx_a = P w_a
             float P[3][3];
             for (int c = 0; c < 3; ++c)
                 for (int r = 0; r < 3; ++r)
-                    P[c][r] = g1.w * f[c][r] + sl * k[c][r];
-            float const G[4][3] = {
-                {-(g1.x + g2.x + g3.x), -(g1.y + g2.y + g3.y), -(g1.z + g2.z + g3.z)},
-                {g1.x, g1.y, g1.z},
-                {g2.x, g2.y, g2.z},
-                {g3.x, g3.y, g3.z}};
+                    P[c][r] = mat.x * f[c][r] + sl * k[c][r];
             int const vid[4] = {t.x, t.y, t.z, t.w};
             for (int a = 0; a < 4; ++a)
                 for (int r = 0; r < 3; ++r)

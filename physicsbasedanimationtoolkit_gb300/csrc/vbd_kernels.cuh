@@ -3,13 +3,16 @@
 //
 //   x, xt, xtilde, v, aext, vprev : float4 per vertex (xyz, w unused except xt.w = lumped mass)
 //   h0, h1: float4 per vertex, the Chebyshev iterate history (allocated with acceleration only)
-//   tets  : one 64-byte TetRecord per tet (below)
+//   X     : float4 per vertex, rest positions (the shape-function gradients are recomputed from
+//           them, which keeps a tet record at 32 bytes)
+//   tets  : one 32-byte TetRecord per tet (below)
 //   solve : free vertices, colour-major; inside a colour sorted by decreasing degree
 //   incPtr: offsets of each solved vertex's incidences; inc: (tet << 2 | local index), tets
 //           ascending
 //
 // A tet record is read by each of its 4 vertices in 4 different colour passes of an iteration;
-// being 64-byte aligned it costs exactly two 32-byte sectors per visit.
+// being 32-byte aligned it costs exactly one sector per visit, and the records, incidences and
+// position tables of a ~1.5M-tet mesh fit in the 129 MB L2 together.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -22,14 +25,11 @@ namespace pbgb {
 // One tetrahedron.  v.{x,y,z,w}: vertex indices in bits 0-29; bits 30-31 hold the vertex's rank
 // (0..3) by colour inside the tet, which tells a vertex solve whether a neighbour was already
 // updated in the current iteration (lower rank) or not (higher rank).
-//   g1 = (GP row 1, wg*mu), g2 = (GP row 2, wg*lambda), g3 = (GP row 3, alpha = 1 + mu/lambda),
-// with GP row 0 = -(rows 1 + 2 + 3).
-struct __align__(64) TetRecord
+//   mat = (wg*mu, wg*lambda, alpha = 1 + mu/lambda, unused)
+struct __align__(32) TetRecord
 {
     uint4 v;
-    float4 g1;
-    float4 g2;
-    float4 g3;
+    float4 mat;
 };
 
 uint32_t constexpr kIndexMask = 0x3FFFFFFFu;
@@ -41,6 +41,7 @@ struct SweepParams
     float4* __restrict__ hcur;         // Chebyshev: iterate k-2 in, accelerated iterate k out
     float4 const* __restrict__ xt;     // .w = lumped mass
     float4 const* __restrict__ xtilde; // inertial target
+    float4 const* __restrict__ X;      // rest positions
     TetRecord const* __restrict__ tets;
     int32_t const* __restrict__ solve;
     int32_t const* __restrict__ incPtr;
@@ -80,6 +81,7 @@ struct EnergyParams
     float4 const* __restrict__ x;
     float4 const* __restrict__ xtilde;
     float const* __restrict__ m;
+    float4 const* __restrict__ X;
     TetRecord const* __restrict__ tets;
     int32_t nV;
     int32_t nT;

@@ -41,50 +41,42 @@ PBGB_HD void zero(VertexBlock<T>& b)
         b.C[k] = T(0);
 }
 
-// Adds one tetrahedron's contribution to vertex `il` (local index 0..3) of the tet.
-//   x0..x3 : the tet's vertex positions
-//   G1..G3 : rows 1..3 of the tet's shape-function gradients (row 0 = -(G1+G2+G3))
-//   muw, law: wg*mu and wg*lambda; alpha = 1 + mu/lambda
+// Shape-function gradients of the three corners a_0, a_1, a_2 of a linear tet other than the
+// solved corner o, from the rest edge vectors e[k] = X_{a_k} - X_o: they are the rows of
+// [e0 e1 e2]^-1 (the reference solves the same system by LU, fem/ShapeFunctions.h:267-296), and
+// grad N_o = -(G0 + G1 + G2).
 template <class T>
-PBGB_HD void accumulate_tet(
-    VertexBlock<T>& b,
-    T const* x0,
-    T const* x1,
-    T const* x2,
-    T const* x3,
-    T const* G1,
-    T const* G2,
-    T const* G3,
-    int il,
-    T muw,
-    T law,
-    T alpha)
+PBGB_HD void rest_gradients(T const (&e)[3][3], T (&G)[3][3])
 {
-    // Edge vectors d_a = x_a - x_0 and F = sum_a d_a G_a^T (columns f_c = F(:, c)).
-    T d1[3], d2[3], d3[3];
-    for (int r = 0; r < 3; ++r)
-    {
-        d1[r] = x1[r] - x0[r];
-        d2[r] = x2[r] - x0[r];
-        d3[r] = x3[r] - x0[r];
-    }
+    G[0][0] = e[1][1] * e[2][2] - e[1][2] * e[2][1];
+    G[0][1] = e[1][2] * e[2][0] - e[1][0] * e[2][2];
+    G[0][2] = e[1][0] * e[2][1] - e[1][1] * e[2][0];
+    G[1][0] = e[2][1] * e[0][2] - e[2][2] * e[0][1];
+    G[1][1] = e[2][2] * e[0][0] - e[2][0] * e[0][2];
+    G[1][2] = e[2][0] * e[0][1] - e[2][1] * e[0][0];
+    G[2][0] = e[0][1] * e[1][2] - e[0][2] * e[1][1];
+    G[2][1] = e[0][2] * e[1][0] - e[0][0] * e[1][2];
+    G[2][2] = e[0][0] * e[1][1] - e[0][1] * e[1][0];
+    T const inv = T(1) / (e[0][0] * G[0][0] + e[0][1] * G[0][1] + e[0][2] * G[0][2]);
+    for (int k = 0; k < 3; ++k)
+        for (int c = 0; c < 3; ++c)
+            G[k][c] *= inv;
+}
+
+// Adds one tetrahedron's contribution to its solved corner o.
+//   d[k] = x_{a_k} - x_o and G[k] = grad N_{a_k} for the three other corners (any order);
+//   muw, law: wg*mu and wg*lambda; alpha = 1 + mu/lambda.
+// F = sum_a x_a grad N_a^T = sum_k d[k] G[k]^T because the gradients sum to zero.
+template <class T>
+PBGB_HD void accumulate_tet(VertexBlock<T>& b, T const (&d)[3][3], T const (&G)[3][3], T muw, T law, T alpha)
+{
     T f[3][3]; // f[c][r] = F(r, c)
     for (int c = 0; c < 3; ++c)
         for (int r = 0; r < 3; ++r)
-            f[c][r] = d1[r] * G1[c] + d2[r] * G2[c] + d3[r] * G3[c];
-    // Gradient row of the solved vertex.
+            f[c][r] = d[0][r] * G[0][c] + d[1][r] * G[1][c] + d[2][r] * G[2][c];
     T w[3];
-    if (il == 0)
-    {
-        for (int c = 0; c < 3; ++c)
-            w[c] = -(G1[c] + G2[c] + G3[c]);
-    }
-    else
-    {
-        T const* G = il == 1 ? G1 : (il == 2 ? G2 : G3);
-        for (int c = 0; c < 3; ++c)
-            w[c] = G[c];
-    }
+    for (int c = 0; c < 3; ++c)
+        w[c] = -(G[0][c] + G[1][c] + G[2][c]);
     // Cofactor columns k0 = f1 x f2, k1 = f2 x f0, k2 = f0 x f1;  J = f0 . k0.
     T k[3][3];
     k[0][0] = f[1][1] * f[2][2] - f[1][2] * f[2][1];
