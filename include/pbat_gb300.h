@@ -186,6 +186,26 @@ PBGB_API int pbgb_vbd_stream(pbgb_vbd* h, void** stream);
 PBGB_API int pbgb_vbd_objective(pbgb_vbd* h, double dt, double* f);
 PBGB_API int pbgb_vbd_gradient(pbgb_vbd* h, double dt, double* grad /* 3 x nV */);
 
+/*
+ * pbgb_vbd_gradient without any device allocation.  This entry point has no counterpart in the
+ * reference; it exists for callers that must not call cudaMalloc once their set-up is done, such
+ * as applications whose device memory is owned and budgeted by another runtime or engine, or
+ * frame loops that forbid allocation after start-up.  pbgb_vbd_gradient allocates its FP64
+ * accumulation buffer on its first call; this variant accumulates in a fixed device array built
+ * into the library instead (PBGB_NOALLOC_MAX_VERTICES x 3 doubles, 6 MiB, held by every device
+ * that loads the library until the process exits).
+ *   - Meshes (or batches) with more than PBGB_NOALLOC_MAX_VERTICES vertices are rejected with
+ *     PBGB_ERR_INVALID_ARGUMENT.
+ *   - The first call on a device looks up that array's device address (cudaGetSymbolAddress,
+ *     with the handle's device made current); make that first call before any stream capture.
+ *   - All calls share the one array: the used part is cleared at the start of every call, and
+ *     calls whose work overlaps on the GPU (different handles or streams at the same time) race.
+ *   - Output and blocking behaviour are those of pbgb_vbd_gradient: grad (3 x nV, host) is
+ *     written and the call returns once the handle's stream is idle.
+ */
+#define PBGB_NOALLOC_MAX_VERTICES 262144
+PBGB_API int pbgb_vbd_gradient_noalloc(pbgb_vbd* h, double dt, double* grad /* 3 x nV */);
+
 /* Message of the last failing call on h (or of the last failing handle-less call if h is NULL). */
 PBGB_API const char* pbgb_last_error(pbgb_vbd* h);
 

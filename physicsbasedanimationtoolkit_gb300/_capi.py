@@ -100,6 +100,7 @@ _SIGNATURES = [
     ("pbgb_vbd_sweep_timing", C.c_int, [_vp, C.POINTER(_f64), C.POINTER(C.c_int64)]),
     ("pbgb_vbd_objective", C.c_int, [_vp, _f64, C.POINTER(_f64)]),
     ("pbgb_vbd_gradient", C.c_int, [_vp, _f64, _vp]),
+    ("pbgb_vbd_gradient_noalloc", C.c_int, [_vp, _f64, _vp]),
     ("pbgb_last_error", C.c_char_p, [_vp]),
     ("pbgb_debug_vertex_block", C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _f64, _f64,
                                          _f64, _f64, _f64, _vp, _vp, _vp]),

@@ -17,6 +17,7 @@
 #include <cstring>
 #include <exception>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -89,6 +90,7 @@ class VbdSystem
     int32_t acceleration = PBGB_ACCEL_NONE, chebFormula = PBGB_CHEBYSHEV_REFERENCE, semantics = 0;
     double rho  = 1.0;
     int32_t lanes = 0, block = 256;
+    int device = 0;
     float sceneMin[3] = {0, 0, 0}, sceneMax[3] = {0, 0, 0};
     std::string lastError;
 
@@ -339,6 +341,7 @@ class VbdSystem
         meanDegree = nFree > 0 ? double(degSum) / nFree : 0.0;
 
         // Device allocation and upload.
+        check(cudaGetDevice(&device), "cudaGetDevice");
         check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
         x.allocate(nV);
         xt.allocate(nV);
@@ -931,6 +934,73 @@ PBGB_API int pbgb_vbd_gradient(pbgb_vbd* h, double dt, double* grad)
         pbgb::check(cudaMemcpyAsync(grad, d, sizeof(double) * 3 * size_t(s.nV), cudaMemcpyDeviceToHost, s.stream), "D2H");
         pbgb::check(cudaStreamSynchronize(s.stream), "sync");
         return int(kOk);
+    });
+}
+
+} // extern "C"
+
+namespace {
+
+// Fixed device scratch of pbgb_vbd_gradient_noalloc: one FP64 accumulator per vertex coordinate.
+__device__ __align__(256) double gNoAllocGradient[3 * PBGB_NOALLOC_MAX_VERTICES];
+
+// Device address of gNoAllocGradient per device, looked up on the first call on that device (the
+// host-side name is only a stand-in for the symbol, not an address the GPU can use).
+std::mutex gNoAllocMutex;
+double* gNoAllocAddress[256] = {};
+
+double* noalloc_scratch(int device)
+{
+    if (device < 0 || device >= 256)
+        throw std::invalid_argument("device ordinal out of range");
+    std::lock_guard<std::mutex> lock(gNoAllocMutex);
+    if (!gNoAllocAddress[device])
+    {
+        void* p = nullptr;
+        check(cudaGetSymbolAddress(&p, gNoAllocGradient), "cudaGetSymbolAddress");
+        gNoAllocAddress[device] = static_cast<double*>(p);
+    }
+    return gNoAllocAddress[device];
+}
+
+} // namespace
+
+extern "C" {
+
+PBGB_API int pbgb_vbd_gradient_noalloc(pbgb_vbd* h, double dt, double* grad)
+{
+    if (!h || !grad)
+        return fail(h, kInvalid, "null argument");
+    if (h->sys.nV > PBGB_NOALLOC_MAX_VERTICES)
+        return fail(
+            h,
+            kInvalid,
+            "pbgb_vbd_gradient_noalloc: " + std::to_string(h->sys.nV) + " vertices exceed the fixed scratch of " +
+                std::to_string(PBGB_NOALLOC_MAX_VERTICES) + " vertices; use pbgb_vbd_gradient");
+    return guarded(h, [&] {
+        auto& s  = h->sys;
+        int prev = 0;
+        check(cudaGetDevice(&prev), "cudaGetDevice");
+        if (prev != s.device)
+            check(cudaSetDevice(s.device), "cudaSetDevice");
+        int rc = kOk;
+        try
+        {
+            double* d = noalloc_scratch(s.device);
+            check(cudaMemsetAsync(d, 0, sizeof(double) * 3 * size_t(s.nV), s.stream), "cudaMemsetAsync");
+            check(pbgb::launch_gradient(s.energyParams(dt, d), s.stream), "gradient");
+            check(cudaMemcpyAsync(grad, d, sizeof(double) * 3 * size_t(s.nV), cudaMemcpyDeviceToHost, s.stream), "D2H");
+            check(cudaStreamSynchronize(s.stream), "cudaStreamSynchronize");
+        }
+        catch (...)
+        {
+            if (prev != s.device)
+                cudaSetDevice(prev);
+            throw;
+        }
+        if (prev != s.device)
+            check(cudaSetDevice(prev), "cudaSetDevice");
+        return rc;
     });
 }
 
