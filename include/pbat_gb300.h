@@ -167,6 +167,9 @@ PBGB_API int pbgb_vbd_set_strategy(pbgb_vbd* h, int32_t strategy);
 PBGB_API int pbgb_vbd_set_block_size(pbgb_vbd* h, int32_t block_size);
 /* Lanes cooperating on one vertex: 1, 2, 4, 8, 16 or 32 (0 = autotuned). */
 PBGB_API int pbgb_vbd_set_lanes_per_vertex(pbgb_vbd* h, int32_t lanes);
+/* Programmatic dependent launch of the colour sweeps (default on): each colour's kernel loads its
+ * mesh tables while the previous colour drains, then waits before reading positions. */
+PBGB_API int pbgb_vbd_set_programmatic_launch(pbgb_vbd* h, int32_t enable);
 PBGB_API int pbgb_vbd_set_scene_bounding_box(pbgb_vbd* h, const float* min3, const float* max3);
 
 /* Sizes and launch bookkeeping. */

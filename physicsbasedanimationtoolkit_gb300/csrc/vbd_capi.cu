@@ -90,6 +90,7 @@ class VbdSystem
     int32_t acceleration = PBGB_ACCEL_NONE, chebFormula = PBGB_CHEBYSHEV_REFERENCE, semantics = 0;
     double rho  = 1.0;
     int32_t lanes = 0, block = 256;
+    bool pdl   = true;
     int device = 0;
     float sceneMin[3] = {0, 0, 0}, sceneMax[3] = {0, 0, 0};
     std::string lastError;
@@ -455,7 +456,7 @@ class VbdSystem
                 {
                     w.begin = colorPtr[c];
                     w.end   = colorPtr[c + 1];
-                    check(launch_sweep(w, L, block, cheb, stream), "sweep");
+                    check(launch_sweep(w, L, block, cheb, pdl, stream), "sweep");
                 }
                 if (profiling)
                     check(cudaEventRecordWithFlags(evEnd[slot], stream, cudaEventRecordExternal), "cudaEventRecord");
@@ -830,6 +831,15 @@ PBGB_API int pbgb_vbd_set_lanes_per_vertex(pbgb_vbd* h, int32_t lanes)
     if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
         return fail(h, kInvalid, "lanes per vertex must be 0, 1, 2, 4, 8, 16 or 32");
     h->sys.lanes = lanes;
+    h->sys.invalidate();
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_set_programmatic_launch(pbgb_vbd* h, int32_t enable)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    h->sys.pdl = enable != 0;
     h->sys.invalidate();
     return kOk;
 }

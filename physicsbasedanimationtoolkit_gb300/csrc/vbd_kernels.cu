@@ -43,20 +43,47 @@ __global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
     zero(b);
     int i       = 0;
     float xi[3] = {0.f, 0.f, 0.f};
+    float Xi[3] = {0.f, 0.f, 0.f};
+    int k = 0, k1 = 0;
+    uint32_t q0 = 0u, q1 = 0u;
+    uint4 t     = make_uint4(0u, 0u, 0u, 0u);
+    float4 mat  = make_float4(0.f, 0.f, 0.f, 0.f);
+    // Prologue on data no earlier launch writes (mesh tables): with programmatic dependent launch
+    // it overlaps the previous colour's tail.
     if (valid)
     {
-        i = __ldg(p.solve + s);
-        load3(CHEB ? p.hprev[i] : p.x[i], xi);
-        float Xi[3];
+        i  = __ldg(p.solve + s);
         load3(__ldg(p.X + i), Xi);
-        int const k1 = __ldg(p.incPtr + s + 1);
-        for (int k = __ldg(p.incPtr + s) + lane; k < k1; k += L)
+        k1 = __ldg(p.incPtr + s + 1);
+        k  = __ldg(p.incPtr + s) + lane;
+        // Software pipeline: the record of incidence k+L and the incidence word of k+2L are in
+        // flight while incidence k's corners are gathered and its block accumulated.
+        q0 = k < k1 ? __ldg(p.inc + k) : 0u;
+        q1 = k + L < k1 ? __ldg(p.inc + k + L) : 0u;
+        if (k < k1)
         {
-            uint32_t const q   = __ldg(p.inc + k);
-            TetRecord const* r = p.tets + (q >> 2);
-            int const il       = int(q & 3u);
-            uint4 const t      = __ldg(&r->v);
-            float4 const mat   = __ldg(&r->mat);
+            t   = __ldg(&p.tets[q0 >> 2].v);
+            mat = __ldg(&p.tets[q0 >> 2].mat);
+        }
+    }
+    // Positions are written by the previous launches: wait for them (no-op without PDL), then let
+    // the next colour's grid start its own prologue.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    if (valid)
+    {
+        load3(CHEB ? p.hprev[i] : p.x[i], xi);
+        for (; k < k1; k += L)
+        {
+            int const il = int(q0 & 3u);
+            uint4 tn     = make_uint4(0u, 0u, 0u, 0u);
+            float4 matn  = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k + L < k1)
+            {
+                tn   = __ldg(&p.tets[q1 >> 2].v);
+                matn = __ldg(&p.tets[q1 >> 2].mat);
+            }
+            uint32_t const q2 = k + 2 * L < k1 ? __ldg(p.inc + k + 2 * L) : 0u;
             uint32_t const own = corner(t, il) >> 30;
             float d[3][3], e[3][3];
 #pragma unroll
@@ -79,6 +106,10 @@ __global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
             float G[3][3];
             rest_gradients(e, G);
             accumulate_tet(b, d, G, mat.x, mat.y, mat.z);
+            q0  = q1;
+            q1  = q2;
+            t   = tn;
+            mat = matn;
         }
     }
 #pragma unroll
@@ -324,29 +355,45 @@ inline int blocks_for(int64_t n, int block)
 
 } // namespace
 
+template <int L, bool CHEB>
+cudaError_t launch_sweep_l(SweepParams const& p, int g, int block, bool pdl, cudaStream_t s)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim            = dim3(unsigned(g));
+    cfg.blockDim           = dim3(unsigned(block));
+    cfg.dynamicSmemBytes   = 0;
+    cfg.stream             = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs                                          = attr;
+    cfg.numAttrs                                       = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, sweep_kernel<L, CHEB>, p);
+}
+
 template <bool CHEB>
-cudaError_t launch_sweep_t(SweepParams const& p, int lanes, int g, int block, cudaStream_t s)
+cudaError_t launch_sweep_t(SweepParams const& p, int lanes, int g, int block, bool pdl, cudaStream_t s)
 {
     switch (lanes)
     {
-        case 1: sweep_kernel<1, CHEB><<<g, block, 0, s>>>(p); break;
-        case 2: sweep_kernel<2, CHEB><<<g, block, 0, s>>>(p); break;
-        case 4: sweep_kernel<4, CHEB><<<g, block, 0, s>>>(p); break;
-        case 8: sweep_kernel<8, CHEB><<<g, block, 0, s>>>(p); break;
-        case 16: sweep_kernel<16, CHEB><<<g, block, 0, s>>>(p); break;
-        case 32: sweep_kernel<32, CHEB><<<g, block, 0, s>>>(p); break;
+        case 1: return launch_sweep_l<1, CHEB>(p, g, block, pdl, s);
+        case 2: return launch_sweep_l<2, CHEB>(p, g, block, pdl, s);
+        case 4: return launch_sweep_l<4, CHEB>(p, g, block, pdl, s);
+        case 8: return launch_sweep_l<8, CHEB>(p, g, block, pdl, s);
+        case 16: return launch_sweep_l<16, CHEB>(p, g, block, pdl, s);
+        case 32: return launch_sweep_l<32, CHEB>(p, g, block, pdl, s);
         default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
 }
 
-cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, cudaStream_t s)
+cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, bool pdl, cudaStream_t s)
 {
     int64_t const n = int64_t(p.end - p.begin) * lanes;
     if (n <= 0)
         return cudaSuccess;
     int const g = blocks_for(n, block);
-    return chebyshev ? launch_sweep_t<true>(p, lanes, g, block, s) : launch_sweep_t<false>(p, lanes, g, block, s);
+    return chebyshev ? launch_sweep_t<true>(p, lanes, g, block, pdl, s)
+                     : launch_sweep_t<false>(p, lanes, g, block, pdl, s);
 }
 
 cudaError_t launch_begin_substep(SubstepParams const& p, cudaStream_t s)

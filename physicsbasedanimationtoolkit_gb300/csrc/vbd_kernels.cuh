@@ -90,7 +90,10 @@ struct EnergyParams
 };
 
 // Launchers (defined in vbd_kernels.cu).  Each returns the launch status.
-cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, cudaStream_t s);
+// pdl: launch with programmatic stream serialization, so that the kernel's mesh-table prologue
+// overlaps the tail of the previous launch on the stream (the kernel waits before reading
+// positions).
+cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, bool pdl, cudaStream_t s);
 cudaError_t launch_begin_substep(SubstepParams const& p, cudaStream_t s);
 cudaError_t launch_end_substep(SubstepParams const& p, cudaStream_t s);
 cudaError_t launch_objective(EnergyParams const& p, cudaStream_t s);
