@@ -134,7 +134,8 @@ def peak_hbm():
 
 
 def traffic_from_profiles():
-    """DRAM bytes per sweep launch from the committed ncu summary (None if absent)."""
+    """DRAM bytes per sweep launch from the committed ncu summary (warm-L2 capture; None if
+    absent)."""
     f = ROOT / "profiles" / "vbd_sweep_beam160x40x40.md"
     try:
         for line in f.read_text().splitlines():
