@@ -225,6 +225,82 @@ def run_reference(args):
     return 0
 
 
+def run_batch(args, pbat, _capi, torch):
+    """Batched uneven meshes: 256 cube grids with side n ~ U{6..32} hexes (6 tets per hex),
+    E log-uniform in [1e5, 1e7], nu ~ U(0.30, 0.48), density 1000, one face pinned, gravity,
+    20 iterations per step, dt = 1/60.  One captured launch sequence steps the whole batch; the
+    comparison steps one integrator per mesh (each on its own stream, all launched before one
+    wait).  Returns the batch figures and the agreement between the two."""
+    from physicsbasedanimationtoolkit_gb300 import meshgen
+
+    meshes = meshgen.batch_workload(n_meshes=args.batch_meshes, nmin=6, nmax=32, seed=0)
+    datas = [
+        pbat.sim.vbd.Data().with_volume_mesh(m["X"].T, m["T"].T).with_material(m["rho"], m["mu"], m["lam"])
+        .with_dirichlet_vertices(m["dbc"]).construct()
+        for m in meshes
+    ]
+    dt, iters = 1 / 60, args.batch_iterations
+    B = pbat.gpu.vbd.BatchedIntegrator(datas)
+    lanes, block, tuned_ms = B.autotune(dt, iters, 1)
+    singles = []
+    for d in datas:
+        s = pbat.gpu.vbd.Integrator(d)
+        s.lanes_per_vertex = lanes
+        _capi.check(_capi.lib().pbgb_vbd_set_block_size(s.handle, block), s.handle)
+        singles.append(s)
+    n_free = B.n_free
+    for _ in range(args.warmup):
+        B.step(dt, iters, 1)
+        for s in singles:
+            s.step(dt, iters, 1)
+    B.synchronize()
+    for s in singles:
+        s.synchronize()
+    sp = C.c_void_p()
+    _capi.check(_capi.lib().pbgb_vbd_stream(B.handle, C.byref(sp)), B.handle)
+    stream = torch.cuda.ExternalStream(sp.value)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        B.step(dt, iters, 1)
+    e1.record(stream)
+    B.synchronize()
+    t_batched = e0.elapsed_time(e1) * 1e-3
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for s in singles:
+            s.step(dt, iters, 1)
+    for s in singles:
+        s.synchronize()
+    t_single = time.perf_counter() - t0
+    # Agreement between the two forms (same lanes and block size: same arithmetic per vertex).
+    xb = B.x
+    off = B.vertex_offsets
+    worst = 0.0
+    for b, s in enumerate(singles):
+        X = meshes[b]["X"]
+        diag = np.linalg.norm(X.max(0) - X.min(0))
+        worst = max(worst, float(np.abs(xb[:, off[b]: off[b + 1]] - s.x).max() / diag))
+    launches = B.launches_per_step(iters, 1)
+    return {
+        "workload": f"{len(meshes)} cube grids, side U{{6..32}} hexes x 6 tets, {iters} iterations, no acceleration",
+        "n_meshes": len(meshes),
+        "n_vertices": int(B.n_vertices),
+        "n_tets": int(B.n_tets),
+        "batched_value": n_free * iters * args.steps / t_batched,
+        "single_launch_value": n_free * iters * args.steps / t_single,
+        "speedup": t_single / t_batched,
+        "batched_ms_per_step": 1e3 * t_batched / args.steps,
+        "single_launch_ms_per_step": 1e3 * t_single / args.steps,
+        "max_rel_diff_batched_vs_single": worst,
+        "autotuned": {"lanes": lanes, "block": block, "ms_per_step": tuned_ms},
+        "batched_launches_per_step": int(launches),
+        "single_launches_per_step": int(sum(s.launches_per_step(iters, 1) for s in singles)),
+        "unit": UNIT,
+    }
+
+
 def config_of(args, w):
     return {
         "workload": f"beam [0,4]x[0,1]^2 {args.nx}x{args.ny}x{args.nz} hexes x 6 tets, Chebyshev rho=0.95",
@@ -251,6 +327,11 @@ def main():
     ap.add_argument("--nz", type=int, default=40)
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch", dest="batch", action="store_true", default=True,
+                    help="also measure the batched multi-mesh form against one launch per mesh")
+    ap.add_argument("--no-batch", dest="batch", action="store_false")
+    ap.add_argument("--batch-meshes", type=int, default=256)
+    ap.add_argument("--batch-iterations", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -323,6 +404,8 @@ def main():
     updates_per_step = n_free * iters
     value = world * updates_per_step * args.steps / (t_total * 1e-3)
 
+    launches_per_step = vbd.launches_per_step(iters, 1)
+    n_colors = vbd.n_colors
     # ---- end to end through the C ABI with host buffers -----------------------------------------
     _capi.check(L.pbgb_vbd_set_sweep_timing(h, 0), h)
     nV = vbd.n_vertices
@@ -359,7 +442,12 @@ def main():
         achieved = bytes_per_launch / (avg_launch_ms * 1e-3) / 1e9
         traffic = traffic_from_profiles()
         cpu = None if args.no_cpu_baseline else cpu_baseline(w, iters)
-        launches = vbd.launches_per_step(iters, 1) * args.steps
+        batched = None
+        if args.batch:
+            del vbd
+            torch.cuda.empty_cache()
+            batched = run_batch(args, pbat, _capi, torch)
+        launches = launches_per_step * args.steps
         line = {
             "metric": METRIC,
             "value": value,
@@ -387,7 +475,8 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clocks.summary(),
             "n_free_vertices": n_free,
-            "n_colors": vbd.n_colors,
+            "n_colors": n_colors,
+            "batched": batched,
         }
         print(json.dumps(line))
     if dist:

@@ -167,6 +167,18 @@ PBGB_API int pbgb_vbd_set_strategy(pbgb_vbd* h, int32_t strategy);
 PBGB_API int pbgb_vbd_set_block_size(pbgb_vbd* h, int32_t block_size);
 /* Lanes cooperating on one vertex: 1, 2, 4, 8, 16 or 32 (0 = autotuned). */
 PBGB_API int pbgb_vbd_set_lanes_per_vertex(pbgb_vbd* h, int32_t lanes);
+/* Autotuner: times one step of (dt, iterations, substeps) for every lanes-per-vertex in
+ * {1,2,4,8,16,32} x block size in {64,128,256}, keeps the fastest for this handle and caches it per
+ * size bucket (vertex and tet counts rounded up to powers of two, colours, iterations).  The
+ * handle's positions and velocities are restored after each trial.  Outputs may be NULL. */
+PBGB_API int pbgb_vbd_autotune(
+    pbgb_vbd* h,
+    float dt,
+    int32_t iterations,
+    int32_t substeps,
+    int32_t* lanes,
+    int32_t* block_size,
+    float* ms_per_step);
 /* Programmatic dependent launch of the colour sweeps (default on): each colour's kernel loads its
  * mesh tables while the previous colour drains, then waits before reading positions. */
 PBGB_API int pbgb_vbd_set_programmatic_launch(pbgb_vbd* h, int32_t enable);

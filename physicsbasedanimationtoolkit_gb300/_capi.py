@@ -92,6 +92,7 @@ _SIGNATURES = [
     ("pbgb_vbd_set_strategy", C.c_int, [_vp, _i32]),
     ("pbgb_vbd_set_block_size", C.c_int, [_vp, _i32]),
     ("pbgb_vbd_set_lanes_per_vertex", C.c_int, [_vp, _i32]),
+    ("pbgb_vbd_autotune", C.c_int, [_vp, _f32, _i32, _i32, _vp, _vp, _vp]),
     ("pbgb_vbd_set_programmatic_launch", C.c_int, [_vp, _i32]),
     ("pbgb_vbd_set_scene_bounding_box", C.c_int, [_vp, _vp, _vp]),
     ("pbgb_vbd_sizes", C.c_int, [_vp, _vp, _vp, _vp, _vp]),

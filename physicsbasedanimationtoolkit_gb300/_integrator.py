@@ -148,6 +148,15 @@ class IntegratorBase:
         _capi.check(_capi.lib().pbgb_vbd_set_lanes_per_vertex(self._h, int(lanes)), self._h)
         self._lanes = int(lanes)
 
+    def autotune(self, dt, iterations, substeps=1):
+        """Pick lanes per vertex and block size by timing one step of each candidate (state is
+        restored); returns (lanes, block_size, ms_per_step)."""
+        lanes, block, ms = C.c_int32(), C.c_int32(), C.c_float()
+        _capi.check(_capi.lib().pbgb_vbd_autotune(self._h, float(dt), int(iterations), int(substeps),
+                                                 C.byref(lanes), C.byref(block), C.byref(ms)), self._h)
+        self._lanes = lanes.value
+        return lanes.value, block.value, ms.value
+
     def launches_per_step(self, iterations, substeps=1):
         n = C.c_int64()
         _capi.check(_capi.lib().pbgb_vbd_launches_per_step(self._h, int(iterations), int(substeps), C.byref(n)), self._h)

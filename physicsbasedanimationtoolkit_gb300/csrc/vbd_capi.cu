@@ -507,6 +507,132 @@ class VbdSystem
         check(cudaGraphLaunch(graph, stream), "cudaGraphLaunch");
     }
 
+    // Project-written autotuner: times one replayed step per candidate (lanes per vertex x block
+    // size) with CUDA events on the handle's stream, restoring the state after each candidate, and
+    // keeps the fastest.  Results are cached per (vertices, tets, colours) bucket.
+    struct TuneKey
+    {
+        int64_t nV, nT, nC, iters, sub;
+        bool cheb;
+        bool operator==(TuneKey const& o) const
+        {
+            return nV == o.nV && nT == o.nT && nC == o.nC && iters == o.iters && sub == o.sub && cheb == o.cheb;
+        }
+    };
+    struct TuneEntry
+    {
+        TuneKey key;
+        int32_t lanes, block;
+        float ms;
+    };
+    static std::vector<TuneEntry>& tuneCache()
+    {
+        static std::vector<TuneEntry> cache;
+        return cache;
+    }
+
+    void autotune(float dt, int32_t iterations, int32_t substeps, int32_t* bestLanes, int32_t* bestBlock, float* bestMs)
+    {
+        static std::mutex cacheMutex;
+        // Size buckets: powers of two of the vertex and tet counts.
+        auto bucket = [](int64_t n) {
+            int64_t b = 1;
+            while (b < n)
+                b <<= 1;
+            return b;
+        };
+        TuneKey const key{bucket(nV), bucket(nT), nColors, iterations, substeps, acceleration == PBGB_ACCEL_CHEBYSHEV};
+        {
+            std::lock_guard<std::mutex> lock(cacheMutex);
+            for (auto const& e : tuneCache())
+                if (e.key == key)
+                {
+                    lanes = e.lanes;
+                    block = e.block;
+                    invalidate();
+                    *bestLanes = e.lanes;
+                    *bestBlock = e.block;
+                    *bestMs    = e.ms;
+                    return;
+                }
+        }
+        // Snapshot the state the steps modify.
+        DeviceArray<float4> sx, sv, svp;
+        sx.allocate(nV);
+        sv.allocate(nV);
+        svp.allocate(nV);
+        size_t const bytes = sizeof(float4) * size_t(nV);
+        check(cudaMemcpyAsync(sx.get(), x.get(), bytes, cudaMemcpyDeviceToDevice, stream), "snapshot");
+        check(cudaMemcpyAsync(sv.get(), v.get(), bytes, cudaMemcpyDeviceToDevice, stream), "snapshot");
+        check(cudaMemcpyAsync(svp.get(), vprev.get(), bytes, cudaMemcpyDeviceToDevice, stream), "snapshot");
+        auto restore = [&] {
+            check(cudaMemcpyAsync(x.get(), sx.get(), bytes, cudaMemcpyDeviceToDevice, stream), "restore");
+            check(cudaMemcpyAsync(v.get(), sv.get(), bytes, cudaMemcpyDeviceToDevice, stream), "restore");
+            check(cudaMemcpyAsync(vprev.get(), svp.get(), bytes, cudaMemcpyDeviceToDevice, stream), "restore");
+        };
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        check(cudaEventCreate(&e0), "cudaEventCreate");
+        check(cudaEventCreate(&e1), "cudaEventCreate");
+        int32_t const savedLanes = lanes, savedBlock = block;
+        bool const savedProfiling = profiling;
+        profiling = false;
+        float best = -1.f;
+        int32_t bl = lanesToUse(), bb = block;
+        try
+        {
+            int32_t const laneSet[]  = {1, 2, 4, 8, 16, 32};
+            int32_t const blockSet[] = {64, 128, 256};
+            for (int32_t L : laneSet)
+                for (int32_t B : blockSet)
+                {
+                    lanes = L;
+                    block = B;
+                    invalidate();
+                    step(dt, iterations, substeps); // capture + warm-up
+                    restore();
+                    check(cudaEventRecord(e0, stream), "cudaEventRecord");
+                    step(dt, iterations, substeps);
+                    check(cudaEventRecord(e1, stream), "cudaEventRecord");
+                    restore();
+                    check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+                    float ms = 0.f;
+                    check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+                    if (best < 0.f || ms < best)
+                    {
+                        best = ms;
+                        bl   = L;
+                        bb   = B;
+                    }
+                }
+        }
+        catch (...)
+        {
+            lanes     = savedLanes;
+            block     = savedBlock;
+            profiling = savedProfiling;
+            invalidate();
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            cudaStreamSynchronize(stream);
+            throw;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+        check(cudaMemsetAsync(flags.get(), 0, sizeof(int32_t), stream), "cudaMemsetAsync");
+        lanes     = bl;
+        block     = bb;
+        profiling = savedProfiling;
+        invalidate();
+        {
+            std::lock_guard<std::mutex> lock(cacheMutex);
+            tuneCache().push_back(TuneEntry{key, bl, bb, best});
+        }
+        *bestLanes = bl;
+        *bestBlock = bb;
+        *bestMs    = best;
+    }
+
     int synchronize()
     {
         check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
@@ -833,6 +959,33 @@ PBGB_API int pbgb_vbd_set_lanes_per_vertex(pbgb_vbd* h, int32_t lanes)
     h->sys.lanes = lanes;
     h->sys.invalidate();
     return kOk;
+}
+
+PBGB_API int pbgb_vbd_autotune(
+    pbgb_vbd* h,
+    float dt,
+    int32_t iterations,
+    int32_t substeps,
+    int32_t* lanes,
+    int32_t* block_size,
+    float* ms_per_step)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (!(dt > 0.f) || iterations < 0 || substeps < 1)
+        return fail(h, kInvalid, "pbgb_vbd_autotune: expected dt > 0, iterations >= 0, substeps >= 1");
+    return guarded(h, [&] {
+        int32_t l = 0, b = 0;
+        float ms  = 0.f;
+        h->sys.autotune(dt, iterations, substeps, &l, &b, &ms);
+        if (lanes)
+            *lanes = l;
+        if (block_size)
+            *block_size = b;
+        if (ms_per_step)
+            *ms_per_step = ms;
+        return int(kOk);
+    });
 }
 
 PBGB_API int pbgb_vbd_set_programmatic_launch(pbgb_vbd* h, int32_t enable)

@@ -221,3 +221,32 @@ def test_invalid_step_arguments():
         I.step(0.01, 10, 0)
     with pytest.raises(ValueError):
         I.x = np.zeros((3, 2))
+
+
+def test_autotuner_restores_state_and_keeps_parity():
+    w = meshgen.unit_cube_workload(n=5, seed=21)
+    I = pbat.sim.vbd.Integrator(make_data(w, rho=0.9))
+    I.step(1 / 60, 10, 1)
+    x_before = I.x.copy()
+    v_before = I.v.copy()
+    lanes, block, ms = I.autotune(1 / 60, 10, 1)
+    assert lanes in (1, 2, 4, 8, 16, 32) and block in (64, 128, 256) and ms > 0
+    np.testing.assert_array_equal(I.x, x_before)
+    np.testing.assert_array_equal(I.v, v_before)
+    for _ in range(4):
+        I.step(1 / 60, 10, 1)
+    R = oracle_for(w, rho=0.9)
+    R.step(1 / 60, 10, 1, 5)
+    assert rel_err(I.x.T, R.x, w["X"]) <= TOL
+
+
+@pytest.mark.parametrize("pdl", [0, 1])
+def test_programmatic_launch_does_not_change_results(pdl):
+    w = meshgen.unit_cube_workload(n=6, seed=5)
+    I = pbat.sim.vbd.Integrator(make_data(w, rho=0.9))
+    _capi.check(_capi.lib().pbgb_vbd_set_programmatic_launch(I.handle, pdl), I.handle)
+    for _ in range(5):
+        I.step(1 / 60, 10, 1)
+    R = oracle_for(w, rho=0.9)
+    R.step(1 / 60, 10, 1, 5)
+    assert rel_err(I.x.T, R.x, w["X"]) <= TOL
