@@ -221,6 +221,44 @@ PBGB_API int pbgb_vbd_gradient(pbgb_vbd* h, double dt, double* grad /* 3 x nV */
 #define PBGB_NOALLOC_MAX_VERTICES 262144
 PBGB_API int pbgb_vbd_gradient_noalloc(pbgb_vbd* h, double dt, double* grad /* 3 x nV */);
 
+/*
+ * Linear BVH over axis-aligned boxes (reference: gpu::geometry::Bvh, gpu/geometry/Bvh.cu, and its
+ * implementation gpu/impl/geometry/Bvh.cu:24-229, Bvh.cuh:205-588, Morton.cu:23-44).
+ * Boxes are host arrays, 3 x n (box i at [3i, 3i+2]).  Node numbering as in the reference:
+ * internal nodes 0..n-2 (root 0), leaves n-1..2n-2 in Morton order.
+ */
+typedef struct pbgb_bvh pbgb_bvh;
+PBGB_API int pbgb_bvh_create(int32_t capacity, pbgb_bvh** out);
+PBGB_API int pbgb_bvh_destroy(pbgb_bvh* b);
+/* Morton codes of box centres normalised by the scene box [wmin, wmax] (30 bits), stable radix
+ * sort of (code, box index), Karras hierarchy, bottom-up internal boxes.  Bvh::Build. */
+PBGB_API int pbgb_bvh_build(pbgb_bvh* b, int32_t n, const float* lower, const float* upper, const float* wmin3, const float* wmax3);
+/* New boxes for the same n boxes, topology kept (Bvh::ConstructBoxes after a box update). */
+PBGB_API int pbgb_bvh_refit(pbgb_bvh* b, const float* lower, const float* upper);
+/* Read-back: sorted codes[n], inds[n] (original box of each sorted leaf), child[2(n-1)]
+ * (child[2i], child[2i+1]), parent[2n-1] (-1 at the root), rightmost[2(n-1)], internal boxes
+ * 3 x (n-1).  Any output may be NULL. */
+PBGB_API int pbgb_bvh_topology(
+    pbgb_bvh* b,
+    uint32_t* codes,
+    int32_t* inds,
+    int32_t* child,
+    int32_t* parent,
+    int32_t* rightmost,
+    float* internal_lower,
+    float* internal_upper);
+/* All (query, box) pairs whose closed boxes overlap (Bvh::DetectOverlaps(leafAabbs, queryAabbs)):
+ * pairs[2k] = query, pairs[2k+1] = box for k < min(*count, capacity); *count = pairs found. */
+PBGB_API int pbgb_bvh_overlaps(
+    pbgb_bvh* b,
+    int32_t nq,
+    const float* qlower,
+    const float* qupper,
+    int32_t* pairs,
+    int64_t capacity,
+    int64_t* count);
+PBGB_API const char* pbgb_bvh_last_error(pbgb_bvh* b);
+
 /* Message of the last failing call on h (or of the last failing handle-less call if h is NULL). */
 PBGB_API const char* pbgb_last_error(pbgb_vbd* h);
 

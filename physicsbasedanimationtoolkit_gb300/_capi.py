@@ -104,6 +104,13 @@ _SIGNATURES = [
     ("pbgb_vbd_gradient", C.c_int, [_vp, _f64, _vp]),
     ("pbgb_vbd_gradient_noalloc", C.c_int, [_vp, _f64, _vp]),
     ("pbgb_last_error", C.c_char_p, [_vp]),
+    ("pbgb_bvh_create", C.c_int, [_i32, C.POINTER(_vp)]),
+    ("pbgb_bvh_destroy", C.c_int, [_vp]),
+    ("pbgb_bvh_build", C.c_int, [_vp, _i32, _vp, _vp, _vp, _vp]),
+    ("pbgb_bvh_refit", C.c_int, [_vp, _vp, _vp]),
+    ("pbgb_bvh_topology", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("pbgb_bvh_overlaps", C.c_int, [_vp, _i32, _vp, _vp, _vp, C.c_int64, C.POINTER(C.c_int64)]),
+    ("pbgb_bvh_last_error", C.c_char_p, [_vp]),
     ("pbgb_debug_vertex_block", C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _f64, _f64,
                                          _f64, _f64, _f64, _vp, _vp, _vp]),
 ]
@@ -129,6 +136,12 @@ def lib():
 def check(rc, handle=None):
     if rc != PBGB_OK:
         msg = lib().pbgb_last_error(handle)
+        raise PbgbError(rc, msg.decode() if msg else "")
+
+
+def check_bvh(rc, bvh=None):
+    if rc != PBGB_OK:
+        msg = lib().pbgb_bvh_last_error(bvh)
         raise PbgbError(rc, msg.decode() if msg else "")
 
 

@@ -1,0 +1,428 @@
+// LBVH kernels (sm_103a).  See lbvh.cuh.
+#include "lbvh.cuh"
+
+namespace pbgb {
+
+namespace {
+
+int constexpr kSortThreads = 256;
+int constexpr kSortRounds  = 16; // a tile is kSortRounds * kSortThreads consecutive keys
+int constexpr kTile        = kSortThreads * kSortRounds;
+int constexpr kBuckets     = 256;
+int constexpr kWarps       = kSortThreads / 32;
+
+inline int tiles_for(int32_t n)
+{
+    return (n + kTile - 1) / kTile;
+}
+
+// Morton code of box i's centre normalised by the scene box.  The arithmetic order of the
+// reference (gpu/impl/geometry/Morton.cu:40: (0.5*(b+e) - wmin)/(wmax - wmin)) is kept with
+// explicitly rounded operations so that no multiply-add is contracted.
+__device__ __forceinline__ float normalised(float b, float e, float lo, float ext)
+{
+    return __fdiv_rn(__fsub_rn(__fmul_rn(0.5f, __fadd_rn(b, e)), lo), ext);
+}
+
+__device__ __forceinline__ uint32_t quantise(float c)
+{
+    // min(max(c * 1024, 0), 1023), truncated (geometry/Morton.h:73-79).
+    float q = __fmul_rn(c, 1024.f);
+    q       = fminf(fmaxf(q, 0.f), 1023.f);
+    return static_cast<uint32_t>(q);
+}
+
+__global__ void morton_kernel(int32_t n, float4 const* __restrict__ lo, float4 const* __restrict__ hi, float3 wmin, float3 ext, uint32_t* __restrict__ codes, int32_t* __restrict__ inds)
+{
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    float4 const b = lo[i], e = hi[i];
+    uint32_t const x = quantise(normalised(b.x, e.x, wmin.x, ext.x));
+    uint32_t const y = quantise(normalised(b.y, e.y, wmin.y, ext.y));
+    uint32_t const z = quantise(normalised(b.z, e.z, wmin.z, ext.z));
+    codes[i]         = expand_bits(x) * 4u + expand_bits(y) * 2u + expand_bits(z);
+    inds[i]          = i;
+}
+
+// --- stable LSD radix sort, 8-bit digits ------------------------------------------------------
+// Pass = count digits per tile -> exclusive scan (digit-major, so tiles keep their order inside a
+// digit) -> scatter with each key's rank inside its tile.  The rank inside a tile is built round by
+// round (kSortThreads consecutive keys per round): warp-level peers from __match_any_sync, then the
+// earlier warps' counts of the same digit, then the running count of earlier rounds, so equal
+// digits keep their input order and every pass is stable.
+
+__global__ void radix_count_kernel(uint32_t const* __restrict__ keys, int32_t n, int shift, uint32_t* __restrict__ counts, int tiles)
+{
+    __shared__ uint32_t hist[kBuckets];
+    int const tile = blockIdx.x;
+    for (int d = threadIdx.x; d < kBuckets; d += blockDim.x)
+        hist[d] = 0;
+    __syncthreads();
+    int const base = tile * kTile;
+    for (int r = 0; r < kSortRounds; ++r)
+    {
+        int const i = base + r * kSortThreads + threadIdx.x;
+        if (i < n)
+            atomicAdd(&hist[(keys[i] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kBuckets; d += blockDim.x)
+        counts[size_t(d) * tiles + tile] = hist[d];
+}
+
+// Exclusive scan of `total` counters in place by one block of 1024 threads.
+__global__ void exclusive_scan_kernel(uint32_t* __restrict__ a, int64_t total)
+{
+    __shared__ uint32_t sums[1024];
+    int64_t const chunk = (total + blockDim.x - 1) / blockDim.x;
+    int64_t const b     = threadIdx.x * chunk;
+    int64_t const e     = b + chunk < total ? b + chunk : total;
+    uint32_t local      = 0;
+    for (int64_t k = b; k < e; ++k)
+        local += a[k];
+    sums[threadIdx.x] = local;
+    __syncthreads();
+    // Hillis-Steele inclusive scan of the per-thread sums.
+    for (int off = 1; off < int(blockDim.x); off <<= 1)
+    {
+        uint32_t const v = threadIdx.x >= unsigned(off) ? sums[threadIdx.x - off] : 0u;
+        __syncthreads();
+        sums[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = threadIdx.x > 0 ? sums[threadIdx.x - 1] : 0u;
+    for (int64_t k = b; k < e; ++k)
+    {
+        uint32_t const v = a[k];
+        a[k]             = run;
+        run += v;
+    }
+}
+
+__global__ void radix_scatter_kernel(
+    uint32_t const* __restrict__ kin,
+    int32_t const* __restrict__ vin,
+    uint32_t* __restrict__ kout,
+    int32_t* __restrict__ vout,
+    int32_t n,
+    int shift,
+    uint32_t const* __restrict__ offsets,
+    int tiles)
+{
+    __shared__ uint32_t run[kBuckets];
+    __shared__ uint32_t warpCount[kWarps][kBuckets];
+    int const tile = blockIdx.x;
+    int const lane = threadIdx.x & 31;
+    int const warp = threadIdx.x >> 5;
+    for (int d = threadIdx.x; d < kBuckets; d += blockDim.x)
+        run[d] = offsets[size_t(d) * tiles + tile];
+    unsigned const lanesBelow = (1u << lane) - 1u;
+    int const base            = tile * kTile;
+    for (int r = 0; r < kSortRounds; ++r)
+    {
+        for (int q = threadIdx.x; q < kWarps * kBuckets; q += blockDim.x)
+            (&warpCount[0][0])[q] = 0;
+        __syncthreads();
+        int const i       = base + r * kSortThreads + threadIdx.x;
+        bool const valid  = i < n;
+        uint32_t const k  = valid ? kin[i] : 0u;
+        int32_t const v   = valid ? vin[i] : 0;
+        uint32_t const d  = valid ? ((k >> shift) & 0xFFu) : uint32_t(kBuckets);
+        unsigned const peers = __match_any_sync(0xffffffffu, d);
+        unsigned const rank  = __popc(peers & lanesBelow);
+        if (valid && rank == 0)
+            warpCount[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid)
+        {
+            uint32_t pos = run[d] + rank;
+            for (int w = 0; w < warp; ++w)
+                pos += warpCount[w][d];
+            kout[pos] = k;
+            vout[pos] = v;
+        }
+        __syncthreads();
+        for (int dd = threadIdx.x; dd < kBuckets; dd += blockDim.x)
+        {
+            uint32_t add = 0;
+            for (int w = 0; w < kWarps; ++w)
+                add += warpCount[w][dd];
+            run[dd] += add;
+        }
+        __syncthreads();
+    }
+}
+
+// --- Karras hierarchy (gpu/impl/geometry/Bvh.cu:24-114) -------------------------------------------
+
+struct Karras
+{
+    uint32_t const* __restrict__ code;
+    int32_t n;
+
+    // Length of the common prefix of keys i and j (index bits break ties of equal codes); -1
+    // outside [0, n).
+    __device__ int delta(int32_t i, int32_t j) const
+    {
+        if (j < 0 || j >= n)
+            return -1;
+        uint32_t const a = code[i], b = code[j];
+        if (a == b)
+            return 32 + __clz(uint32_t(i) ^ uint32_t(j));
+        return __clz(a ^ b);
+    }
+};
+
+__global__ void karras_kernel(Karras K, int32_t* __restrict__ child, int32_t* __restrict__ parent, int32_t* __restrict__ rightmost)
+{
+    int32_t const i = blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t const n = K.n;
+    if (i >= n - 1)
+        return;
+    int32_t const leafBegin = n - 1;
+    // Direction of the range and a lower bound on its common prefix.
+    int32_t const d    = (K.delta(i, i + 1) - K.delta(i, i - 1)) > 0 ? 1 : -1;
+    int const dmin     = K.delta(i, i - d);
+    int32_t lmax       = 2;
+    while (K.delta(i, i + lmax * d) > dmin)
+        lmax <<= 1;
+    int32_t l = 0;
+    do
+    {
+        lmax >>= 1;
+        if (K.delta(i, i + (l + lmax) * d) > dmin)
+            l += lmax;
+    } while (lmax > 1);
+    int32_t const j   = i + l * d;
+    int const dnode   = K.delta(i, j);
+    int32_t s         = 0;
+    int32_t t         = l;
+    do
+    {
+        t = (t + 1) >> 1;
+        if (K.delta(i, i + (s + t) * d) > dnode)
+            s += t;
+    } while (t > 1);
+    int32_t const gamma = i + s * d + (d < 0 ? d : 0);
+    int32_t const lo    = i < j ? i : j;
+    int32_t const hi    = i < j ? j : i;
+    int32_t const lc    = lo == gamma ? leafBegin + gamma : gamma;
+    int32_t const rc    = hi == gamma + 1 ? leafBegin + gamma + 1 : gamma + 1;
+    child[2 * i]         = lc;
+    child[2 * i + 1]     = rc;
+    parent[lc]           = i;
+    parent[rc]           = i;
+    rightmost[2 * i]     = leafBegin + gamma;
+    rightmost[2 * i + 1] = leafBegin + hi;
+}
+
+__global__ void gather_leaves_kernel(int32_t n, int32_t const* __restrict__ inds, float4 const* __restrict__ lo, float4 const* __restrict__ hi, float4* __restrict__ llo, float4* __restrict__ lhi)
+{
+    int const s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n)
+        return;
+    int const i = inds[s];
+    llo[s]      = lo[i];
+    lhi[s]      = hi[i];
+}
+
+__device__ __forceinline__ float4 fmin4(float4 a, float4 b)
+{
+    return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.f);
+}
+__device__ __forceinline__ float4 fmax4(float4 a, float4 b)
+{
+    return make_float4(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), 0.f);
+}
+
+// Bottom-up internal boxes (gpu/impl/geometry/Bvh.cu:175-229): the second thread to reach a node
+// computes its box from both children and continues upward; at most 64 levels, deeper trees raise
+// kBvhErrDepth instead of looping on.
+__global__ void boxes_kernel(int32_t n, BvhBuffers B)
+{
+    int const s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n)
+        return;
+    int32_t const leafBegin = n - 1;
+    int32_t p               = B.parent[leafBegin + s];
+    int k                   = 0;
+    for (; k < 64 && p >= 0; ++k)
+    {
+        __threadfence();
+        if (atomicAdd(&B.visits[p], 1) == 0)
+            return;
+        __threadfence();
+        int32_t const lc = __ldcg(&B.child[2 * p]);
+        int32_t const rc = __ldcg(&B.child[2 * p + 1]);
+        float4 const llo = lc >= leafBegin ? __ldcg(&B.llo[lc - leafBegin]) : __ldcg(&B.ilo[lc]);
+        float4 const lhi = lc >= leafBegin ? __ldcg(&B.lhi[lc - leafBegin]) : __ldcg(&B.ihi[lc]);
+        float4 const rlo = rc >= leafBegin ? __ldcg(&B.llo[rc - leafBegin]) : __ldcg(&B.ilo[rc]);
+        float4 const rhi = rc >= leafBegin ? __ldcg(&B.lhi[rc - leafBegin]) : __ldcg(&B.ihi[rc]);
+        __stcg(&B.ilo[p], fmin4(llo, rlo));
+        __stcg(&B.ihi[p], fmax4(lhi, rhi));
+        p = __ldcg(&B.parent[p]);
+    }
+    if (k == 64 && p >= 0)
+        atomicOr(B.flags, kBvhErrDepth);
+}
+
+__device__ __forceinline__ bool boxes_overlap(float4 const& l1, float4 const& u1, float4 const& l2, float4 const& u2)
+{
+    // Closed intervals on every axis (geometry/OverlapQueries.h:608-616).
+    return l1.x <= u2.x && l1.y <= u2.y && l1.z <= u2.z && l2.x <= u1.x && l2.y <= u1.y && l2.z <= u1.z;
+}
+
+// Query boxes against the tree (gpu/impl/geometry/Bvh.cuh:282-345 with the overlap predicate of
+// Bvh.cuh:476-588): depth-first from the root with a bounded stack.
+__global__ void overlaps_kernel(BvhView V, int32_t nq, float4 const* __restrict__ qlo, float4 const* __restrict__ qhi, int32_t* __restrict__ pairs, int64_t capacity, unsigned long long* __restrict__ count, int32_t* __restrict__ flags)
+{
+    int const q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq || V.n < 1)
+        return;
+    float4 const L = qlo[q], U = qhi[q];
+    int32_t const leafBegin = V.n - 1;
+    int32_t stack[kBvhStack];
+    int top      = 0;
+    stack[top++] = 0;
+    while (top > 0)
+    {
+        int32_t const node = stack[--top];
+        if (node >= leafBegin)
+        {
+            int32_t const s = node - leafBegin;
+            if (boxes_overlap(L, U, V.llo[s], V.lhi[s]))
+            {
+                unsigned long long const slot = atomicAdd(count, 1ull);
+                if (slot < (unsigned long long)capacity)
+                {
+                    pairs[2 * slot]     = q;
+                    pairs[2 * slot + 1] = V.inds[s];
+                }
+            }
+        }
+        else if (boxes_overlap(L, U, V.ilo[node], V.ihi[node]))
+        {
+            if (top + 2 > kBvhStack)
+            {
+                atomicOr(flags, kBvhErrStackOverflow);
+                return;
+            }
+            stack[top++] = V.child[2 * node];
+            stack[top++] = V.child[2 * node + 1];
+        }
+    }
+}
+
+inline int blocks(int64_t n, int b)
+{
+    return int((n + b - 1) / b);
+}
+
+cudaError_t sort_impl(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, float3 wmin, float3 wmax, cudaStream_t s)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    float3 const ext = make_float3(wmax.x - wmin.x, wmax.y - wmin.y, wmax.z - wmin.z);
+    morton_kernel<<<blocks(n, 256), 256, 0, s>>>(n, lo, hi, wmin, ext, B.codes, B.inds);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    int const tiles     = tiles_for(n);
+    int64_t const total = int64_t(kBuckets) * tiles;
+    uint32_t* kin       = B.codes;
+    uint32_t* kout      = B.codesAlt;
+    int32_t* vin        = B.inds;
+    int32_t* vout       = B.indsAlt;
+    for (int shift = 0; shift < 32; shift += 8)
+    {
+        radix_count_kernel<<<tiles, kSortThreads, 0, s>>>(kin, n, shift, B.counts, tiles);
+        exclusive_scan_kernel<<<1, 1024, 0, s>>>(B.counts, total);
+        radix_scatter_kernel<<<tiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift, B.counts, tiles);
+        if ((e = cudaGetLastError()) != cudaSuccess)
+            return e;
+        uint32_t* tk = kin;
+        kin          = kout;
+        kout         = tk;
+        int32_t* tv  = vin;
+        vin          = vout;
+        vout         = tv;
+    }
+    // Four passes: the sorted keys end in B.codes / B.inds again.
+    return cudaSuccess;
+}
+
+cudaError_t boxes_impl(BvhBuffers const& B, int32_t n, cudaStream_t s)
+{
+    if (n < 2)
+        return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(B.visits, 0, sizeof(int32_t) * size_t(n - 1), s);
+    if (e != cudaSuccess)
+        return e;
+    boxes_kernel<<<blocks(n, 256), 256, 0, s>>>(n, B);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+int64_t radix_counts_size(int32_t n)
+{
+    return int64_t(kBuckets) * tiles_for(n > 0 ? n : 1);
+}
+
+cudaError_t bvh_sort(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, float3 wmin, float3 wmax, cudaStream_t s)
+{
+    return sort_impl(B, n, lo, hi, wmin, wmax, s);
+}
+
+cudaError_t bvh_build(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, float3 wmin, float3 wmax, cudaStream_t s)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    cudaError_t e = sort_impl(B, n, lo, hi, wmin, wmax, s);
+    if (e != cudaSuccess)
+        return e;
+    if ((e = cudaMemsetAsync(B.parent, 0xFF, sizeof(int32_t) * size_t(2 * n - 1), s)) != cudaSuccess)
+        return e;
+    if (n > 1)
+    {
+        karras_kernel<<<blocks(n - 1, 256), 256, 0, s>>>(Karras{B.codes, n}, B.child, B.parent, B.rightmost);
+        if ((e = cudaGetLastError()) != cudaSuccess)
+            return e;
+    }
+    gather_leaves_kernel<<<blocks(n, 256), 256, 0, s>>>(n, B.inds, lo, hi, B.llo, B.lhi);
+    if ((e = cudaGetLastError()) != cudaSuccess)
+        return e;
+    return boxes_impl(B, n, s);
+}
+
+cudaError_t bvh_refit(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, cudaStream_t s)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    gather_leaves_kernel<<<blocks(n, 256), 256, 0, s>>>(n, B.inds, lo, hi, B.llo, B.lhi);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    return boxes_impl(B, n, s);
+}
+
+cudaError_t bvh_overlaps(
+    BvhView const& V,
+    int32_t nq,
+    float4 const* qlo,
+    float4 const* qhi,
+    int32_t* pairs,
+    int64_t capacity,
+    unsigned long long* count,
+    int32_t* flags,
+    cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess || nq <= 0)
+        return e;
+    overlaps_kernel<<<blocks(nq, 128), 128, 0, s>>>(V, nq, qlo, qhi, pairs, capacity, count, flags);
+    return cudaGetLastError();
+}
+
+} // namespace pbgb

@@ -1,0 +1,95 @@
+// Linear BVH over axis-aligned boxes (reference: pbat::gpu::impl::geometry::Bvh,
+// gpu/impl/geometry/Bvh.cu:24-229 and Bvh.cuh:205-588; Morton codes gpu/impl/geometry/Morton.cu:23-44
+// and geometry/Morton.h:35-80).
+//
+// Build = Morton codes of the box centres normalised by the scene box, a stable LSD radix sort of
+// (code, box index), Karras' radix-tree hierarchy, and bottom-up internal boxes.  Node numbering
+// follows the reference: internal nodes 0..n-2 (0 is the root), leaves n-1..2n-2 in sorted order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pbgb {
+
+int constexpr kBvhStack = 64;       // traversal stack capacity (reference kStackSize)
+int constexpr kBvhMaxNeighbours = 8; // nearest-neighbour ties kept per query (reference kQueueSize)
+
+// Error bits raised on the device (read back by the host after a query or build).
+int constexpr kBvhErrStackOverflow = 1;
+int constexpr kBvhErrDepth        = 2;
+
+struct BvhView
+{
+    int32_t n;                       // leaves
+    int32_t const* __restrict__ inds; // n: original box index of sorted leaf s
+    int32_t const* __restrict__ child;     // 2(n-1): child[2i], child[2i+1]
+    int32_t const* __restrict__ rightmost; // 2(n-1)
+    float4 const* __restrict__ ilo;  // n-1 internal boxes
+    float4 const* __restrict__ ihi;
+    float4 const* __restrict__ llo;  // n leaf boxes in sorted order
+    float4 const* __restrict__ lhi;
+};
+
+// Work arrays of one BVH (allocated by the owner, sized for `capacity` boxes).
+struct BvhBuffers
+{
+    int32_t capacity;
+    uint32_t* codes;    // n   sorted Morton codes
+    uint32_t* codesAlt; // n   radix-sort ping-pong
+    int32_t* inds;      // n   sorted original indices
+    int32_t* indsAlt;   // n
+    uint32_t* counts;   // 256 * tiles (radix digit counts / offsets)
+    int32_t* child;     // 2(n-1)
+    int32_t* parent;    // 2n-1
+    int32_t* rightmost; // 2(n-1)
+    int32_t* visits;    // n-1
+    float4* ilo;        // n-1
+    float4* ihi;
+    float4* llo;        // n
+    float4* lhi;
+    int32_t* flags;     // device error bits
+};
+
+// Number of uint32 digit counters the radix sort needs for n keys.
+int64_t radix_counts_size(int32_t n);
+
+// Full build from unsorted boxes lo/hi (n each) and the scene box (wmin, wmax).
+cudaError_t bvh_build(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, float3 wmin, float3 wmax, cudaStream_t s);
+// Only the Morton codes + stable sort (codes, inds ascending) — exposed for tests.
+cudaError_t bvh_sort(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, float3 wmin, float3 wmax, cudaStream_t s);
+// Recompute leaf boxes (gathered through inds) and internal boxes, topology unchanged
+// (reference: VertexTriangleMixedCcdDcd::UpdateBvh + Bvh::ConstructBoxes).
+cudaError_t bvh_refit(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, cudaStream_t s);
+
+// Overlapping (query, original box index) pairs, appended at pairs[2k], pairs[2k+1] for k < capacity;
+// *count (device) receives the total number found (may exceed capacity).
+cudaError_t bvh_overlaps(
+    BvhView const& V,
+    int32_t nq,
+    float4 const* qlo,
+    float4 const* qhi,
+    int32_t* pairs,
+    int64_t capacity,
+    unsigned long long* count,
+    int32_t* flags,
+    cudaStream_t s);
+
+inline BvhView view_of(BvhBuffers const& B, int32_t n)
+{
+    return BvhView{n, B.inds, B.child, B.rightmost, B.ilo, B.ihi, B.llo, B.lhi};
+}
+
+// Spreads the 10 low bits of v so that bit k lands on bit 3k (shift-or form).  A 30-bit Morton
+// code is expand(x) * 4 + expand(y) * 2 + expand(z) (geometry/Morton.h:35-80 of the reference).
+__host__ __device__ inline uint32_t expand_bits(uint32_t v)
+{
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+} // namespace pbgb

@@ -1,0 +1,327 @@
+// C ABI of the LBVH (include/pbat_gb300.h, pbgb_bvh_*): a BVH object that owns its device arrays
+// and a stream, built from host boxes; topology read-back and box-overlap queries for tests and
+// for callers of the reference's gpu::geometry::Bvh (gpu/geometry/Bvh.cu).
+#include "lbvh.cuh"
+#include "pbat_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <exception>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string gBvhError;
+
+struct CudaError
+{
+    cudaError_t e;
+    char const* what;
+};
+
+void ck(cudaError_t e, char const* what)
+{
+    if (e != cudaSuccess)
+        throw CudaError{e, what};
+}
+
+template <class T>
+T* dalloc(size_t n)
+{
+    T* p = nullptr;
+    if (n > 0)
+        ck(cudaMalloc(reinterpret_cast<void**>(&p), n * sizeof(T)), "cudaMalloc");
+    return p;
+}
+
+} // namespace
+
+struct pbgb_bvh
+{
+    pbgb::BvhBuffers B{};
+    int32_t n        = 0;
+    int32_t capacity = 0;
+    float4* lo       = nullptr; // unsorted input boxes
+    float4* hi       = nullptr;
+    float4* qlo      = nullptr; // query staging
+    float4* qhi      = nullptr;
+    int32_t qcap     = 0;
+    int32_t* pairs   = nullptr;
+    int64_t pcap     = 0;
+    unsigned long long* count = nullptr;
+    cudaStream_t stream       = nullptr;
+    std::string error;
+
+    ~pbgb_bvh()
+    {
+        if (stream)
+            cudaStreamSynchronize(stream);
+        void* ptrs[] = {B.codes, B.codesAlt, B.inds, B.indsAlt, B.counts, B.child, B.parent, B.rightmost,
+                        B.visits, B.ilo, B.ihi, B.llo, B.lhi, B.flags, lo, hi, qlo, qhi, pairs, count};
+        for (void* p : ptrs)
+            if (p)
+                cudaFree(p);
+        if (stream)
+            cudaStreamDestroy(stream);
+    }
+
+    void allocate(int32_t cap)
+    {
+        capacity   = cap;
+        size_t n   = size_t(cap);
+        size_t ni  = n > 1 ? n - 1 : 1;
+        B.capacity = cap;
+        B.codes    = dalloc<uint32_t>(n);
+        B.codesAlt = dalloc<uint32_t>(n);
+        B.inds     = dalloc<int32_t>(n);
+        B.indsAlt  = dalloc<int32_t>(n);
+        B.counts   = dalloc<uint32_t>(size_t(pbgb::radix_counts_size(cap)));
+        B.child    = dalloc<int32_t>(2 * ni);
+        B.parent   = dalloc<int32_t>(2 * n);
+        B.rightmost = dalloc<int32_t>(2 * ni);
+        B.visits   = dalloc<int32_t>(ni);
+        B.ilo      = dalloc<float4>(ni);
+        B.ihi      = dalloc<float4>(ni);
+        B.llo      = dalloc<float4>(n);
+        B.lhi      = dalloc<float4>(n);
+        B.flags    = dalloc<int32_t>(1);
+        lo         = dalloc<float4>(n);
+        hi         = dalloc<float4>(n);
+        count      = dalloc<unsigned long long>(1);
+        ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        ck(cudaMemsetAsync(B.flags, 0, sizeof(int32_t), stream), "cudaMemsetAsync");
+    }
+
+    void upload_boxes(int32_t m, float const* l3, float const* u3, float4*& dl, float4*& du)
+    {
+        std::vector<float4> hl(static_cast<size_t>(m)), hu(static_cast<size_t>(m));
+        for (int32_t i = 0; i < m; ++i)
+        {
+            hl[i] = make_float4(l3[3 * size_t(i)], l3[3 * size_t(i) + 1], l3[3 * size_t(i) + 2], 0.f);
+            hu[i] = make_float4(u3[3 * size_t(i)], u3[3 * size_t(i) + 1], u3[3 * size_t(i) + 2], 0.f);
+        }
+        ck(cudaMemcpyAsync(dl, hl.data(), sizeof(float4) * size_t(m), cudaMemcpyHostToDevice, stream), "H2D");
+        ck(cudaMemcpyAsync(du, hu.data(), sizeof(float4) * size_t(m), cudaMemcpyHostToDevice, stream), "H2D");
+        ck(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    }
+
+    int check_flags()
+    {
+        int32_t f = 0;
+        ck(cudaMemcpyAsync(&f, B.flags, sizeof(int32_t), cudaMemcpyDeviceToHost, stream), "D2H");
+        ck(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+        if (f)
+        {
+            ck(cudaMemsetAsync(B.flags, 0, sizeof(int32_t), stream), "cudaMemsetAsync");
+            error = (f & pbgb::kBvhErrStackOverflow) ? "BVH traversal stack (64) overflowed"
+                                                      : "BVH deeper than 64 levels";
+            return PBGB_ERR_INTERNAL;
+        }
+        return PBGB_OK;
+    }
+};
+
+namespace {
+
+int bvh_fail(pbgb_bvh* b, int code, std::string const& msg)
+{
+    gBvhError = msg;
+    if (b)
+        b->error = msg;
+    return code;
+}
+
+template <class F>
+int bvh_guard(pbgb_bvh* b, F&& f)
+{
+    try
+    {
+        return f();
+    }
+    catch (CudaError const& e)
+    {
+        return bvh_fail(b, PBGB_ERR_CUDA, std::string(e.what) + ": " + cudaGetErrorString(e.e));
+    }
+    catch (std::bad_alloc const&)
+    {
+        return bvh_fail(b, PBGB_ERR_INTERNAL, "host allocation failed");
+    }
+    catch (std::exception const& e)
+    {
+        return bvh_fail(b, PBGB_ERR_INTERNAL, e.what());
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+PBGB_API int pbgb_bvh_create(int32_t capacity, pbgb_bvh** out)
+{
+    if (!out || capacity < 1 || capacity >= (1 << 30))
+        return bvh_fail(nullptr, PBGB_ERR_INVALID_ARGUMENT, "pbgb_bvh_create: expected 1 <= capacity < 2^30");
+    *out = nullptr;
+    int devices = 0;
+    if (cudaGetDeviceCount(&devices) != cudaSuccess || devices < 1)
+    {
+        cudaGetLastError();
+        return bvh_fail(nullptr, PBGB_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    pbgb_bvh* b = new (std::nothrow) pbgb_bvh();
+    if (!b)
+        return bvh_fail(nullptr, PBGB_ERR_INTERNAL, "host allocation failed");
+    int const rc = bvh_guard(b, [&] {
+        b->allocate(capacity);
+        return int(PBGB_OK);
+    });
+    if (rc != PBGB_OK)
+    {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return PBGB_OK;
+}
+
+PBGB_API int pbgb_bvh_destroy(pbgb_bvh* b)
+{
+    delete b;
+    return PBGB_OK;
+}
+
+PBGB_API int pbgb_bvh_build(pbgb_bvh* b, int32_t n, const float* lower, const float* upper, const float* wmin, const float* wmax)
+{
+    if (!b)
+        return bvh_fail(nullptr, PBGB_ERR_INVALID_ARGUMENT, "null BVH");
+    if (n < 1 || n > b->capacity || !lower || !upper || !wmin || !wmax)
+        return bvh_fail(b, PBGB_ERR_INVALID_ARGUMENT, "pbgb_bvh_build: expected 1 <= n <= capacity and non-null boxes");
+    return bvh_guard(b, [&] {
+        b->upload_boxes(n, lower, upper, b->lo, b->hi);
+        b->n = n;
+        ck(pbgb::bvh_build(b->B, n, b->lo, b->hi, make_float3(wmin[0], wmin[1], wmin[2]),
+                           make_float3(wmax[0], wmax[1], wmax[2]), b->stream),
+           "bvh_build");
+        return b->check_flags();
+    });
+}
+
+PBGB_API int pbgb_bvh_refit(pbgb_bvh* b, const float* lower, const float* upper)
+{
+    if (!b)
+        return bvh_fail(nullptr, PBGB_ERR_INVALID_ARGUMENT, "null BVH");
+    if (b->n < 1 || !lower || !upper)
+        return bvh_fail(b, PBGB_ERR_INVALID_ARGUMENT, "pbgb_bvh_refit: build first; non-null boxes");
+    return bvh_guard(b, [&] {
+        b->upload_boxes(b->n, lower, upper, b->lo, b->hi);
+        ck(pbgb::bvh_refit(b->B, b->n, b->lo, b->hi, b->stream), "bvh_refit");
+        return b->check_flags();
+    });
+}
+
+PBGB_API int pbgb_bvh_topology(
+    pbgb_bvh* b,
+    uint32_t* codes,
+    int32_t* inds,
+    int32_t* child,
+    int32_t* parent,
+    int32_t* rightmost,
+    float* internal_lower,
+    float* internal_upper)
+{
+    if (!b)
+        return bvh_fail(nullptr, PBGB_ERR_INVALID_ARGUMENT, "null BVH");
+    if (b->n < 1)
+        return bvh_fail(b, PBGB_ERR_INVALID_ARGUMENT, "pbgb_bvh_topology: build first");
+    return bvh_guard(b, [&] {
+        size_t const n = size_t(b->n), ni = n - 1;
+        auto get = [&](void* dst, void const* src, size_t bytes) {
+            if (dst && bytes)
+                ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, b->stream), "D2H");
+        };
+        get(codes, b->B.codes, sizeof(uint32_t) * n);
+        get(inds, b->B.inds, sizeof(int32_t) * n);
+        get(child, b->B.child, sizeof(int32_t) * 2 * ni);
+        get(parent, b->B.parent, sizeof(int32_t) * (2 * n - 1));
+        get(rightmost, b->B.rightmost, sizeof(int32_t) * 2 * ni);
+        std::vector<float4> lo(ni), hi(ni);
+        if (ni && (internal_lower || internal_upper))
+        {
+            get(lo.data(), b->B.ilo, sizeof(float4) * ni);
+            get(hi.data(), b->B.ihi, sizeof(float4) * ni);
+        }
+        ck(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+        for (size_t i = 0; i < ni; ++i)
+        {
+            if (internal_lower)
+            {
+                internal_lower[3 * i]     = lo[i].x;
+                internal_lower[3 * i + 1] = lo[i].y;
+                internal_lower[3 * i + 2] = lo[i].z;
+            }
+            if (internal_upper)
+            {
+                internal_upper[3 * i]     = hi[i].x;
+                internal_upper[3 * i + 1] = hi[i].y;
+                internal_upper[3 * i + 2] = hi[i].z;
+            }
+        }
+        return int(PBGB_OK);
+    });
+}
+
+PBGB_API int pbgb_bvh_overlaps(
+    pbgb_bvh* b,
+    int32_t nq,
+    const float* qlower,
+    const float* qupper,
+    int32_t* pairs,
+    int64_t capacity,
+    int64_t* count)
+{
+    if (!b)
+        return bvh_fail(nullptr, PBGB_ERR_INVALID_ARGUMENT, "null BVH");
+    if (b->n < 1 || nq < 0 || (nq > 0 && (!qlower || !qupper)) || !count || capacity < 0 || (capacity > 0 && !pairs))
+        return bvh_fail(b, PBGB_ERR_INVALID_ARGUMENT, "pbgb_bvh_overlaps: invalid argument");
+    return bvh_guard(b, [&] {
+        if (nq > b->qcap)
+        {
+            if (b->qlo)
+                cudaFree(b->qlo);
+            if (b->qhi)
+                cudaFree(b->qhi);
+            b->qlo  = dalloc<float4>(size_t(nq));
+            b->qhi  = dalloc<float4>(size_t(nq));
+            b->qcap = nq;
+        }
+        if (capacity > b->pcap)
+        {
+            if (b->pairs)
+                cudaFree(b->pairs);
+            b->pairs = dalloc<int32_t>(2 * size_t(capacity));
+            b->pcap  = capacity;
+        }
+        if (nq > 0)
+            b->upload_boxes(nq, qlower, qupper, b->qlo, b->qhi);
+        ck(pbgb::bvh_overlaps(pbgb::view_of(b->B, b->n), nq, b->qlo, b->qhi, b->pairs, capacity, b->count,
+                              b->B.flags, b->stream),
+           "bvh_overlaps");
+        unsigned long long c = 0;
+        ck(cudaMemcpyAsync(&c, b->count, sizeof(c), cudaMemcpyDeviceToHost, b->stream), "D2H");
+        ck(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+        int64_t const m = int64_t(c) < capacity ? int64_t(c) : capacity;
+        if (m > 0)
+            ck(cudaMemcpy(pairs, b->pairs, sizeof(int32_t) * 2 * size_t(m), cudaMemcpyDeviceToHost), "D2H");
+        *count = int64_t(c);
+        return b->check_flags();
+    });
+}
+
+PBGB_API const char* pbgb_bvh_last_error(pbgb_bvh* b)
+{
+    return b ? b->error.c_str() : gBvhError.c_str();
+}
+
+} // extern "C"

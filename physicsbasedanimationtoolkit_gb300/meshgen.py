@@ -200,3 +200,53 @@ def batch_workload(n_meshes=256, nmin=6, nmax=32, seed=0, spacing=1.5):
             )
         )
     return meshes
+
+
+def contact_scene_workload(n_cubes_side=4, cube_hexes=16, slab_hexes=(64, 64, 2), cube_size=0.6,
+                           cell=1.0, gap=0.05, seed=0, E=1e6, nu=0.45, rho=1000.0):
+    """Cubes dropped on a fixed slab: an ``n x n`` arrangement of ``cube_hexes^3``-hex cubes (6 tets
+    per hex) with a seeded random yaw in [0, 2 pi), each centred in a ``cell`` x ``cell`` square,
+    their bottoms ``gap`` above a ``slab_hexes`` slab whose top face is z = 0 and whose vertices are
+    all pinned.  Body 0 is the slab, bodies 1.. the cubes.  With the defaults: 91,283 vertices,
+    442,368 tets and 66,560 surface triangles.
+
+    Returns X (nV x 3), T (nT x 4), F (surface triangles, nF x 3, outward), V (surface vertices),
+    B (body of each vertex), dbc (pinned vertices) and materials.
+    """
+    rng = np.random.default_rng(seed)
+    sx, sy, sz = slab_hexes
+    hxy = cell * n_cubes_side / sx
+    Xs, Ts = hex_grid(sx, sy, sz, lo=(0.0, 0.0, -hxy * sz), hi=(cell * n_cubes_side, cell * n_cubes_side, 0.0))
+    Xs = Xs.copy()
+    Xs[:, 2] = np.linspace(-hxy * sz, 0.0, sz + 1)[np.arange(Xs.shape[0]) // ((sx + 1) * (sy + 1))]
+    parts_X, parts_T, parts_B = [Xs], [Ts], [np.zeros(Xs.shape[0], np.int32)]
+    offset = Xs.shape[0]
+    yaws = rng.uniform(0.0, 2.0 * np.pi, n_cubes_side * n_cubes_side)
+    Xc, Tc = hex_grid(cube_hexes, cube_hexes, cube_hexes, lo=(-0.5, -0.5, 0.0), hi=(0.5, 0.5, 1.0))
+    Xc = Xc * cube_size
+    for k in range(n_cubes_side * n_cubes_side):
+        i, j = k % n_cubes_side, k // n_cubes_side
+        c, s = np.cos(yaws[k]), np.sin(yaws[k])
+        R = np.array([[c, -s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]])
+        Xk = Xc @ R.T + np.array([(i + 0.5) * cell, (j + 0.5) * cell, gap])
+        parts_X.append(Xk)
+        parts_T.append(Tc + offset)
+        parts_B.append(np.full(Xk.shape[0], k + 1, np.int32))
+        offset += Xk.shape[0]
+    X = np.vstack(parts_X)
+    T = np.vstack(parts_T).astype(np.int32)
+    B = np.concatenate(parts_B)
+    F = boundary_faces(T)
+    V = np.unique(F).astype(np.int32)
+    dbc = np.arange(Xs.shape[0], dtype=np.int32)
+    mu, lam = lame(np.full(T.shape[0], E), np.full(T.shape[0], nu))
+    return dict(X=X, T=T, F=F, V=V, B=B, dbc=dbc, rho=np.full(T.shape[0], rho), mu=mu, lam=lam,
+                v=np.zeros_like(X), yaws=yaws)
+
+
+def triangle_boxes(X, F, Xnext=None):
+    """Axis-aligned boxes of triangles (swept between X and Xnext when given): lower, upper (n x 3)."""
+    P = X[F]
+    if Xnext is not None:
+        P = np.concatenate([P, Xnext[F]], axis=1)
+    return P.min(axis=1), P.max(axis=1)

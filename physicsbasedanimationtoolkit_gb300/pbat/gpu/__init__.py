@@ -1,1 +1,1 @@
-from . import vbd  # noqa: F401
+from . import geometry, vbd  # noqa: F401

@@ -170,6 +170,23 @@ def trajectories(R):
     np.savez_compressed(HERE / "trajectories.npz", **out)
 
 
+def morton_codes(R, rng):
+    """Boxes in a scene box, their centres normalised in FP32 with the reference's operation order
+    ((0.5*(b+e) - wmin)/(wmax - wmin), each step rounded), then the reference's Morton3D."""
+    n = 4096
+    wmin = np.array([-1.0, 0.5, -2.0], np.float32)
+    wmax = np.array([3.0, 1.5, 6.0], np.float32)
+    c = rng.uniform(-0.05, 1.05, (n, 3)).astype(np.float32)
+    lo = (wmin + c * (wmax - wmin) - rng.uniform(0, 0.01, (n, 3))).astype(np.float32)
+    hi = (lo + rng.uniform(0, 0.02, (n, 3))).astype(np.float32)
+    lo[:64] = lo[64:128]  # duplicate boxes -> equal codes
+    hi[:64] = hi[64:128]
+    ext = (wmax - wmin).astype(np.float32)
+    cn = ((np.float32(0.5) * (lo + hi)).astype(np.float32) - wmin).astype(np.float32) / ext
+    codes = np.array([R.ref_morton3d(*map(float, p)) for p in cn.astype(np.float32)], np.uint32)
+    np.savez_compressed(HERE / "morton.npz", lo=lo, hi=hi, wmin=wmin, wmax=wmax, codes=codes)
+
+
 def main():
     O.build_oracle(ref=True)
     R = O.ref()
@@ -182,6 +199,7 @@ def main():
     chebyshev(R)
     coloring(R)
     trajectories(R)
+    morton_codes(R, rng)
     print("fixtures written to", HERE)
 
 

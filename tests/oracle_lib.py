@@ -101,6 +101,14 @@ def lib():
             C.c_double, C.c_double, C.c_double, C.c_double, _f64p, _f64p, _f64p,
         ]
         L.orc_num_threads.restype = C.c_int32
+        _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        _u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+        L.orc_morton.argtypes = [C.c_int32, _f32p, _f32p, _f32p, _f32p, _u32p]
+        L.orc_bvh_build.argtypes = [C.c_int32, _f32p, _f32p, _f32p, _f32p, _u32p, _i32p, _i32p, _i32p,
+                                    _i32p, _f32p, _f32p]
+        L.orc_bvh_boxes.argtypes = [C.c_int32, _i32p, _i32p, _f32p, _f32p, _f32p, _f32p]
+        L.orc_overlaps.restype = C.c_int64
+        L.orc_overlaps.argtypes = [C.c_int32, _f32p, _f32p, C.c_int32, _f32p, _f32p, _i32p, C.c_int64]
         _lib = L
     return _lib
 
@@ -230,6 +238,56 @@ class OracleVbd:
         g = np.zeros(self.X.shape[0] * 3)
         lib().orc_gradient(C.byref(self.P), np.ascontiguousarray(x), np.ascontiguousarray(xtilde), dt, g)
         return g
+
+
+def bvh_build(lo, hi, wmin, wmax):
+    """Oracle LBVH build; lo, hi: n x 3 float32.  Returns a dict of the sorted codes, leaf order,
+    child (n-1 x 2), parent (2n-1), rightmost (n-1 x 2) and internal boxes."""
+    lo = np.ascontiguousarray(lo, dtype=np.float32)
+    hi = np.ascontiguousarray(hi, dtype=np.float32)
+    n = lo.shape[0]
+    out = dict(codes=np.zeros(n, np.uint32), inds=np.zeros(n, np.int32),
+               child=np.zeros(max(2 * (n - 1), 1), np.int32), parent=np.zeros(2 * n - 1, np.int32),
+               rightmost=np.zeros(max(2 * (n - 1), 1), np.int32), ilo=np.zeros((max(n - 1, 1), 3), np.float32),
+               ihi=np.zeros((max(n - 1, 1), 3), np.float32))
+    lib().orc_bvh_build(n, lo, hi, np.asarray(wmin, np.float32), np.asarray(wmax, np.float32), out["codes"],
+                        out["inds"], out["child"], out["parent"], out["rightmost"], out["ilo"], out["ihi"])
+    out["child"] = out["child"][: 2 * (n - 1)].reshape(-1, 2)
+    out["rightmost"] = out["rightmost"][: 2 * (n - 1)].reshape(-1, 2)
+    out["ilo"], out["ihi"] = out["ilo"][: n - 1], out["ihi"][: n - 1]
+    return out
+
+
+def bvh_boxes(child, inds, lo, hi):
+    n = inds.size
+    ilo = np.zeros((max(n - 1, 1), 3), np.float32)
+    ihi = np.zeros((max(n - 1, 1), 3), np.float32)
+    lib().orc_bvh_boxes(n, np.ascontiguousarray(child, np.int32).ravel(), np.ascontiguousarray(inds, np.int32),
+                        np.ascontiguousarray(lo, np.float32), np.ascontiguousarray(hi, np.float32), ilo, ihi)
+    return ilo[: n - 1], ihi[: n - 1]
+
+
+def morton(lo, hi, wmin, wmax):
+    lo = np.ascontiguousarray(lo, dtype=np.float32)
+    codes = np.zeros(lo.shape[0], np.uint32)
+    lib().orc_morton(lo.shape[0], lo, np.ascontiguousarray(hi, np.float32), np.asarray(wmin, np.float32),
+                     np.asarray(wmax, np.float32), codes)
+    return codes
+
+
+def overlaps(lo, hi, qlo, qhi):
+    """Brute-force overlapping (query, box) pairs as a set of tuples."""
+    lo = np.ascontiguousarray(lo, np.float32)
+    hi = np.ascontiguousarray(hi, np.float32)
+    qlo = np.ascontiguousarray(qlo, np.float32)
+    qhi = np.ascontiguousarray(qhi, np.float32)
+    cap = 1 << 20
+    while True:
+        pairs = np.zeros(2 * cap, np.int32)
+        c = lib().orc_overlaps(lo.shape[0], lo, hi, qlo.shape[0], qlo, qhi, pairs, cap)
+        if c <= cap:
+            return pairs[: 2 * c].reshape(-1, 2)
+        cap = int(c)
 
 
 def primal_graph(T, nV):
