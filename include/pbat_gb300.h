@@ -133,6 +133,20 @@ typedef struct pbgb_vbd_desc
     int32_t chebyshev_formula; /* PBGB_CHEBYSHEV_* */
     int32_t semantics;         /* PBGB_SEMANTICS_* */
     const double* X;           /* 3 x nV rest positions (NULL: x) */
+    /* Vertex-triangle contact (gpu/impl/vbd/Kernels.cuh:80-114,203-223; active set
+     * gpu/impl/contact/VertexTriangleMixedCcdDcd.cu).  n_collision_triangles = 0 disables it; only
+     * a single (non-batched) mesh may carry contact.  Bodies separate self-contact. */
+    int32_t n_collision_vertices;  /* |V| */
+    const int32_t* V;              /* collision vertices */
+    int32_t n_collision_triangles; /* |F| */
+    const int32_t* F;              /* 3 x |F| collision triangles */
+    const int32_t* B;              /* nV body of each vertex (NULL: one body) */
+    const double* XVA;             /* nV vertex areas (Data::XVA) */
+    const double* FA;              /* |F| triangle areas (Data::FA) */
+    double muC;                    /* contact penalty (default 1e6) */
+    double muF;                    /* friction coefficient (default 0.3) */
+    double epsv;                   /* IPC smooth friction velocity threshold (default 1e-3) */
+    int32_t active_set_update_frequency; /* update the contact list every k substeps (default 1) */
 } pbgb_vbd_desc;
 
 typedef struct pbgb_vbd pbgb_vbd; /* opaque integrator handle */
@@ -195,6 +209,10 @@ PBGB_API int pbgb_vbd_set_sweep_timing(pbgb_vbd* h, int32_t enable);
 PBGB_API int pbgb_vbd_sweep_timing(pbgb_vbd* h, double* milliseconds, int64_t* sweep_launches);
 /* The handle's CUDA stream (cudaStream_t) so callers can order their own work after a step. */
 PBGB_API int pbgb_vbd_stream(pbgb_vbd* h, void** stream);
+
+/* Contact lists after the last step: fc[8 nV] contact triangles per vertex (-1 = none) and
+ * active[|V|] (1 if the collision vertex is in the active set).  Either may be NULL. */
+PBGB_API int pbgb_vbd_get_contacts(pbgb_vbd* h, int32_t* fc, uint8_t* active);
 
 /* Backward-Euler objective f(x) = 1/2 |x - xtilde|_M^2 + dt^2 sum wg Psi and its gradient at
  * the current positions against the last step's inertial target; FP64 device reductions. */
@@ -259,6 +277,25 @@ PBGB_API int pbgb_bvh_overlaps(
     int64_t* count);
 PBGB_API const char* pbgb_bvh_last_error(pbgb_bvh* b);
 
+/*
+ * Vertex-triangle contact detector (reference: gpu::impl::contact::VertexTriangleMixedCcdDcd,
+ * gpu/impl/contact/VertexTriangleMixedCcdDcd.cu:17-223).  V: collision vertices, F: 3 x |F|
+ * triangles, B: nV bodies (NULL: one body; same-body pairs never collide).  Positions are host
+ * arrays 3 x nV.
+ */
+typedef struct pbgb_ccd pbgb_ccd;
+PBGB_API int pbgb_ccd_create(int32_t nV, int32_t nSurfV, const int32_t* V, int32_t nF, const int32_t* F, const int32_t* B, pbgb_ccd** out);
+PBGB_API int pbgb_ccd_destroy(pbgb_ccd* c);
+/* InitializeActiveSet(xt, x, wmin, wmax): swept vertices vs swept triangles. */
+PBGB_API int pbgb_ccd_initialize(pbgb_ccd* c, const float* xt, const float* x, const float* wmin3, const float* wmax3);
+/* UpdateActiveSet(x): nearest triangles (<= 8, ties within FLT_EPSILON) of active vertices. */
+PBGB_API int pbgb_ccd_update(pbgb_ccd* c, const float* x);
+/* FinalizeActiveSet(x): keep the vertices that lie behind their nearest triangle's plane. */
+PBGB_API int pbgb_ccd_finalize(pbgb_ccd* c, const float* x);
+/* active[|V|], nn[8 |V|] (-1 = none), dupper[|V|] (squared search radius), *n_active. */
+PBGB_API int pbgb_ccd_get(pbgb_ccd* c, uint8_t* active, int32_t* nn, float* dupper, int32_t* n_active);
+PBGB_API const char* pbgb_ccd_last_error(pbgb_ccd* c);
+
 /* Message of the last failing call on h (or of the last failing handle-less call if h is NULL). */
 PBGB_API const char* pbgb_last_error(pbgb_vbd* h);
 
@@ -283,6 +320,22 @@ PBGB_API int pbgb_debug_vertex_block(
     double* x,
     double* g,
     double* H);
+
+/* Host self-check of one vertex-triangle contact term (FP32), the arithmetic of the device sweep
+ * (sim/vbd/Kernels.h:215-302).  xtf, xf: 3 x 3 corners (corner-major); adds to g[3] and to the
+ * symmetric H[9] (column-major); *energy (may be NULL) receives the contact energy. */
+PBGB_API int pbgb_debug_vertex_triangle_contact(
+    const float* xtv,
+    const float* xv,
+    const float* xtf,
+    const float* xf,
+    float dt,
+    float muC,
+    float muF,
+    float epsv,
+    float* g,
+    float* H,
+    float* energy);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,447 @@
+// FP64 restatement of the reference GPU integrator's contact-enabled VBD step (TEST
+// INFRASTRUCTURE ONLY; see vbd_oracle.cpp).
+//
+//   Step order          gpu/impl/vbd/Integrator.cu:82-103 (active set on the full-step prediction,
+//                       per substep: inertial target, initial guess, contact list, sweeps,
+//                       velocity; finalise at the end), GPU velocity semantics
+//   active set          gpu/impl/contact/VertexTriangleMixedCcdDcd.cu:51-223, with brute-force
+//                       overlaps and nearest triangles instead of the BVH (the same sets: every
+//                       box pair is tested); the search radius of a vertex overlapping several
+//                       triangles is the largest joint-box diagonal
+//   contact energy      gpu/impl/vbd/Kernels.cuh:80-114,203-223 and sim/vbd/Kernels.h:215-302
+//   colour pass reads   the reference writes every vertex of a colour to a buffer and copies it
+//                       back after the pass, so a contact triangle's corners are read as they were
+//                       at the start of the pass; this oracle reads them from a snapshot
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "orc_problem.h"
+
+namespace {
+
+using Real = double;
+
+struct V3
+{
+    Real x, y, z;
+};
+inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 add(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 mul(Real s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline Real dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline V3 at(Real const* x, int32_t i) { return {x[3 * size_t(i)], x[3 * size_t(i) + 1], x[3 * size_t(i) + 2]}; }
+
+// Closest point on a triangle by Voronoi regions (Ericson, section 5.1.5); squared distance.
+Real point_triangle_sqdist(V3 p, V3 a, V3 b, V3 c)
+{
+    V3 ab = sub(b, a), ac = sub(c, a), ap = sub(p, a);
+    Real d1 = dot(ab, ap), d2 = dot(ac, ap);
+    V3 q;
+    if (d1 <= 0 && d2 <= 0)
+        q = a;
+    else
+    {
+        V3 bp   = sub(p, b);
+        Real d3 = dot(ab, bp), d4 = dot(ac, bp);
+        Real vc = d1 * d4 - d3 * d2;
+        V3 cp   = sub(p, c);
+        Real d5 = dot(ab, cp), d6 = dot(ac, cp);
+        Real vb = d5 * d2 - d1 * d6;
+        Real va = d3 * d6 - d5 * d4;
+        if (d3 >= 0 && d4 <= d3)
+            q = b;
+        else if (vc <= 0 && d1 >= 0 && d3 <= 0)
+            q = add(a, mul(d1 / (d1 - d3), ab));
+        else if (d6 >= 0 && d5 <= d6)
+            q = c;
+        else if (vb <= 0 && d2 >= 0 && d6 <= 0)
+            q = add(a, mul(d2 / (d2 - d6), ac));
+        else if (va <= 0 && (d4 - d3) >= 0 && (d5 - d6) >= 0)
+            q = add(b, mul((d4 - d3) / ((d4 - d3) + (d5 - d6)), sub(c, b)));
+        else
+        {
+            Real den = 1 / (va + vb + vc);
+            q        = add(a, add(mul(vb * den, ab), mul(vc * den, ac)));
+        }
+    }
+    V3 d = sub(p, q);
+    return dot(d, d);
+}
+
+// sim/vbd/Kernels.h:215-302 (energy not needed): adds to g and H (column-major 3x3).
+void vertex_triangle_contact(V3 xtv, V3 xv, V3 const* xtf, V3 const* xf, Real dt, Real muC, Real muF, Real epsv, Real* g, Real* H, Real epsilon = Real(FLT_EPSILON))
+{
+    V3 e0 = sub(xf[1], xf[0]), e1 = sub(xf[2], xf[0]);
+    V3 n  = cross(e0, e1);
+    Real const dbl = std::sqrt(dot(n, n));
+    if (dbl <= 1e-8)
+        return;
+    n           = mul(1 / dbl, n);
+    Real const t = dot(n, sub(xv, xf[0]));
+    V3 ap        = sub(sub(xv, mul(t, n)), xf[0]);
+    Real d00 = dot(e0, e0), d01 = dot(e0, e1), d11 = dot(e1, e1), d20 = dot(ap, e0), d21 = dot(ap, e1);
+    Real denom = d00 * d11 - d01 * d01;
+    Real bv = (d11 * d20 - d01 * d21) / denom, bw = (d00 * d21 - d01 * d20) / denom, bu = 1 - bv - bw;
+    if (!(bu >= 0 && bu <= 1 && bv >= 0 && bv <= 1 && bw >= 0 && bw <= 1))
+        return;
+    V3 xb  = add(add(mul(bu, xf[0]), mul(bv, xf[1])), mul(bw, xf[2]));
+    V3 xtb = add(add(mul(bu, xtf[0]), mul(bv, xtf[1])), mul(bw, xtf[2]));
+    Real const dn     = dot(sub(xv, xb), n);
+    Real const d      = std::min(Real(0), dn);
+    Real const lambda = muC * d;
+    Real const nn[3]  = {n.x, n.y, n.z};
+    g[0] += lambda * n.x;
+    g[1] += lambda * n.y;
+    g[2] += lambda * n.z;
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r)
+            H[3 * c + r] += muC * nn[r] * nn[c];
+    V3 b1      = cross(n, e0);
+    V3 dx      = sub(sub(xv, xtv), sub(xb, xtb));
+    Real u0    = dot(e0, dx), u1 = dot(b1, dx);
+    // The reference adds numeric_limits<Scalar>::epsilon(); its contact runs in FP32 on the GPU.
+    Real unorm = std::sqrt(u0 * u0 + u1 * u1) + epsilon;
+    Real epsvh = epsv * dt;
+    Real y     = unorm / epsvh;
+    Real f1    = y < 1 ? 2 * y - y * y : Real(1);
+    Real s     = muF * std::abs(lambda) * f1 / unorm;
+    V3 gt      = add(mul(u0, e0), mul(u1, b1));
+    g[0] += s * gt.x;
+    g[1] += s * gt.y;
+    g[2] += s * gt.z;
+    Real const E0[3] = {e0.x, e0.y, e0.z}, E1[3] = {b1.x, b1.y, b1.z};
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r)
+            H[3 * c + r] += s * (E0[r] * E0[c] + E1[r] * E1[c]);
+}
+
+// SNH closed-form vertex block in FP64 (same contraction the full 9x9 reference Hessian reduces
+// to; the CPU oracle without contact uses the full form, this one is checked against it).
+void elastic_block(orc_problem const& P, int32_t i, Real const* x, Real* H, Real* g)
+{
+    for (int k = 0; k < 9; ++k)
+        H[k] = 0;
+    g[0] = g[1] = g[2] = 0;
+    Real s = 0;
+    for (int32_t n = P.GVGp[i]; n < P.GVGp[i + 1]; ++n)
+    {
+        int32_t const e   = P.GVGe[n];
+        int32_t const il  = P.GVGilocal[n];
+        int32_t const* t  = P.T + 4 * e;
+        double const* GPe = P.GP + 12 * e;
+        Real F[9]         = {0};
+        for (int a = 0; a < 4; ++a)
+            for (int d = 0; d < 3; ++d)
+                for (int r = 0; r < 3; ++r)
+                    F[3 * d + r] += x[3 * t[a] + r] * GPe[3 * a + d];
+        Real const* w = GPe + 3 * il;
+        V3 f0{F[0], F[1], F[2]}, f1{F[3], F[4], F[5]}, f2{F[6], F[7], F[8]};
+        V3 k0 = cross(f1, f2), k1 = cross(f2, f0), k2 = cross(f0, f1);
+        Real J = dot(f0, k0);
+        V3 c   = add(add(mul(w[0], k0), mul(w[1], k1)), mul(w[2], k2));
+        V3 Fw  = add(add(mul(w[0], f0), mul(w[1], f1)), mul(w[2], f2));
+        Real const mu = P.mu[e] * P.wg[e], la = P.lambda[e] * P.wg[e];
+        Real const sl = la * (J - 1 - P.mu[e] / P.lambda[e]);
+        g[0] += mu * Fw.x + sl * c.x;
+        g[1] += mu * Fw.y + sl * c.y;
+        g[2] += mu * Fw.z + sl * c.z;
+        s += mu * (w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        Real const cc[3] = {c.x, c.y, c.z};
+        for (int cc_ = 0; cc_ < 3; ++cc_)
+            for (int r = 0; r < 3; ++r)
+                H[3 * cc_ + r] += la * cc[r] * cc[cc_];
+    }
+    H[0] += s;
+    H[4] += s;
+    H[8] += s;
+}
+
+} // namespace
+
+extern "C" {
+
+struct orc_contact
+{
+    int32_t nSurfV;
+    int32_t const* V;
+    int32_t nF;
+    int32_t const* F; // 3 x nF
+    int32_t const* B; // nV
+    double const* XVA;
+    double const* FA;
+    double muC, muF, epsv;
+    int32_t freq;
+    // persistent state (caller-owned)
+    uint8_t* active;  // nSurfV
+    double* dupper;   // nSurfV
+    int32_t* fc;      // nV * 8
+};
+
+namespace {
+
+void nearest(orc_contact const& C, Real const* x, int32_t q, std::vector<int32_t>& list)
+{
+    int32_t const i = C.V[q];
+    V3 const p      = at(x, i);
+    list.clear();
+    Real dmin = std::numeric_limits<Real>::max();
+    std::vector<std::pair<Real, int32_t>> d;
+    d.reserve(64);
+    for (int32_t f = 0; f < C.nF; ++f)
+    {
+        int32_t const* t = C.F + 3 * size_t(f);
+        if (C.B[t[0]] == C.B[i])
+            continue;
+        Real const dd = point_triangle_sqdist(p, at(x, t[0]), at(x, t[1]), at(x, t[2]));
+        d.push_back({dd, f});
+        dmin = std::min(dmin, dd);
+    }
+    if (dmin > C.dupper[q] + Real(FLT_EPSILON))
+        return; // outside the search radius: the branch and bound finds nothing
+    for (auto const& [dd, f] : d)
+        if (dd <= dmin + Real(FLT_EPSILON) && list.size() < 8)
+            list.push_back(f);
+}
+
+} // namespace
+
+// Advance nsteps contact-enabled steps (GPU integrator semantics).  x, v, vprev: nV x 3.
+int orc_run_contact(orc_problem const* Pp, orc_contact const* Cp, double* x, double* v, double* vprev, double dt, int32_t iterations, int32_t substeps, int32_t nsteps)
+{
+    orc_problem const& P = *Pp;
+    orc_contact const& C = *Cp;
+    int32_t const nV     = P.nV;
+    size_t const n3      = size_t(nV) * 3;
+    std::vector<Real> xt(n3), xtilde(n3), xpred(n3), snap(n3), vtm1(n3);
+    Real const sdt = dt / Real(substeps), sdt2 = sdt * sdt;
+    std::vector<int32_t> list;
+    for (int32_t step = 0; step < nsteps; ++step)
+    {
+        // InitializeActiveSet on the full-step prediction.
+        for (size_t k = 0; k < n3; ++k)
+            xpred[k] = x[k] + dt * v[k] + dt * dt * P.aext[k];
+        std::vector<V3> flo(size_t(C.nF)), fhi(size_t(C.nF));
+        for (int32_t f = 0; f < C.nF; ++f)
+        {
+            int32_t const* t = C.F + 3 * size_t(f);
+            V3 lo = at(x, t[0]), hi = lo;
+            for (int k = 0; k < 3; ++k)
+                for (Real const* src : {x, xpred.data()})
+                {
+                    V3 p = at(src, t[k]);
+                    lo   = {std::min(lo.x, p.x), std::min(lo.y, p.y), std::min(lo.z, p.z)};
+                    hi   = {std::max(hi.x, p.x), std::max(hi.y, p.y), std::max(hi.z, p.z)};
+                }
+            flo[f] = lo;
+            fhi[f] = hi;
+        }
+#pragma omp parallel for schedule(dynamic, 16)
+        for (int32_t q = 0; q < C.nSurfV; ++q)
+        {
+            int32_t const i = C.V[q];
+            V3 a = at(x, i), b = at(xpred.data(), i);
+            V3 lo{std::min(a.x, b.x), std::min(a.y, b.y), std::min(a.z, b.z)};
+            V3 hi{std::max(a.x, b.x), std::max(a.y, b.y), std::max(a.z, b.z)};
+            Real best = 0;
+            bool hit  = false;
+            for (int32_t f = 0; f < C.nF; ++f)
+            {
+                bool const ov = lo.x <= fhi[f].x && lo.y <= fhi[f].y && lo.z <= fhi[f].z && flo[f].x <= hi.x &&
+                                flo[f].y <= hi.y && flo[f].z <= hi.z;
+                if (!ov)
+                    continue;
+                int32_t const* t = C.F + 3 * size_t(f);
+                if (C.B[i] == C.B[t[0]])
+                    continue;
+                V3 jl = a, jh = a;
+                for (Real const* src : {x, xpred.data()})
+                {
+                    for (int k = 0; k < 4; ++k)
+                    {
+                        V3 p = at(src, k < 3 ? t[k] : i);
+                        jl   = {std::min(jl.x, p.x), std::min(jl.y, p.y), std::min(jl.z, p.z)};
+                        jh   = {std::max(jh.x, p.x), std::max(jh.y, p.y), std::max(jh.z, p.z)};
+                    }
+                }
+                V3 dg = sub(jh, jl);
+                best  = std::max(best, dot(dg, dg));
+                hit   = true;
+            }
+            if (hit)
+            {
+                C.dupper[q] = best;
+                C.active[q] = 1;
+            }
+        }
+        for (int32_t s = 0; s < substeps; ++s)
+        {
+            std::memcpy(xt.data(), x, sizeof(Real) * n3);
+            std::memcpy(vtm1.data(), vprev, sizeof(Real) * n3);
+            for (int32_t i = 0; i < nV; ++i)
+            {
+                Real const* vv = v + 3 * size_t(i);
+                Real const* aa = P.aext + 3 * size_t(i);
+                Real const* tt = xt.data() + 3 * size_t(i);
+                Real* xo       = x + 3 * size_t(i);
+                for (int d = 0; d < 3; ++d)
+                    xtilde[3 * size_t(i) + d] = tt[d] + sdt * vv[d] + sdt2 * aa[d];
+                // InitialPositionsForSolve (sim/vbd/Kernels.h:39-94)
+                Real an2 = aa[0] * aa[0] + aa[1] * aa[1] + aa[2] * aa[2];
+                Real atl = 1;
+                if (P.strategy == 0)
+                {
+                    for (int d = 0; d < 3; ++d)
+                        xo[d] = tt[d];
+                    continue;
+                }
+                if (P.strategy == 1)
+                    atl = 0;
+                else if (P.strategy >= 3)
+                {
+                    atl = 0;
+                    if (an2 != 0)
+                    {
+                        Real const* vm = vtm1.data() + 3 * size_t(i);
+                        if (P.strategy == 3)
+                        {
+                            Real dd = 0;
+                            for (int d = 0; d < 3; ++d)
+                                dd += ((vv[d] - vm[d]) / sdt) * aa[d];
+                            atl = std::min(std::max(dd / an2, Real(0)), Real(1));
+                        }
+                        else
+                        {
+                            Real vn = std::sqrt(vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]) + std::numeric_limits<Real>::min();
+                            Real dd = 0;
+                            for (int d = 0; d < 3; ++d)
+                                dd += (vv[d] / vn) * aa[d];
+                            atl = std::min(std::abs(dd / an2), Real(1));
+                        }
+                    }
+                }
+                for (int d = 0; d < 3; ++d)
+                    xo[d] = tt[d] + sdt * vv[d] + sdt2 * atl * aa[d];
+            }
+            if (s % C.freq == 0)
+            {
+                for (int32_t q = 0; q < C.nSurfV; ++q)
+                {
+                    if (!C.active[q])
+                        continue;
+                    nearest(C, x, q, list);
+                    int32_t const i = C.V[q];
+                    for (int c = 0; c < 8; ++c)
+                        C.fc[8 * size_t(i) + c] = c < int(list.size()) ? list[c] : -1;
+                }
+            }
+            for (int32_t k = 0; k < iterations; ++k)
+                for (int32_t p = 0; p < P.nPartitions; ++p)
+                {
+                    std::memcpy(snap.data(), x, sizeof(Real) * n3);
+#pragma omp parallel for schedule(dynamic, 32)
+                    for (int32_t kk = P.Pptr[p]; kk < P.Pptr[p + 1]; ++kk)
+                    {
+                        int32_t const i = P.Padj[kk];
+                        Real H[9], g[3];
+                        elastic_block(P, i, snap.data(), H, g);
+                        Real* xi        = x + 3 * size_t(i);
+                        Real const* xti = xt.data() + 3 * size_t(i);
+                        Real const D    = P.kD / sdt;
+                        Real hx[3]      = {0, 0, 0};
+                        for (int r = 0; r < 3; ++r)
+                            for (int c = 0; c < 3; ++c)
+                                hx[r] += H[3 * c + r] * (xi[c] - xti[c]);
+                        for (int r = 0; r < 3; ++r)
+                            g[r] += D * hx[r];
+                        for (int q = 0; q < 9; ++q)
+                            H[q] *= 1 + D;
+                        // Contacts: corners as at the start of the pass.
+                        int32_t const* f = C.fc + 8 * size_t(i);
+                        int nc           = 0;
+                        for (int c = 0; c < 8; ++c)
+                            nc += f[c] >= 0 ? 1 : 0;
+                        if (nc > 0)
+                        {
+                            Real sumfa = 0;
+                            for (int c = 0; c < nc; ++c)
+                                sumfa += C.FA[f[c]];
+                            Real const kC = C.XVA[i] * C.muC / sumfa;
+                            for (int c = 0; c < nc; ++c)
+                            {
+                                int32_t const* t = C.F + 3 * size_t(f[c]);
+                                V3 xtf[3], xf[3];
+                                for (int m = 0; m < 3; ++m)
+                                {
+                                    xtf[m] = at(xt.data(), t[m]);
+                                    xf[m]  = at(snap.data(), t[m]);
+                                }
+                                vertex_triangle_contact(at(xt.data(), i), at(snap.data(), i), xtf, xf, sdt, kC * C.FA[f[c]], C.muF, C.epsv, g, H);
+                            }
+                        }
+                        Real const K = P.m[i] / sdt2;
+                        for (int r = 0; r < 3; ++r)
+                        {
+                            H[4 * r] += K;
+                            g[r] += K * (xi[r] - xtilde[3 * size_t(i) + r]);
+                        }
+                        Real a00 = H[4] * H[8] - H[5] * H[7], a01 = H[7] * H[2] - H[1] * H[8], a02 = H[1] * H[5] - H[4] * H[2];
+                        Real a11 = H[0] * H[8] - H[2] * H[6], a12 = H[2] * H[3] - H[0] * H[5], a22 = H[0] * H[4] - H[1] * H[3];
+                        Real det = H[0] * a00 + H[3] * a01 + H[6] * a02;
+                        if (!(std::abs(det) > P.detHZero))
+                            continue;
+                        Real const inv = 1 / det;
+                        Real const dx0 = inv * (a00 * g[0] + a01 * g[1] + a02 * g[2]);
+                        Real const dx1 = inv * (a01 * g[0] + a11 * g[1] + a12 * g[2]);
+                        Real const dx2 = inv * (a02 * g[0] + a12 * g[1] + a22 * g[2]);
+                        xi[0] -= dx0;
+                        xi[1] -= dx1;
+                        xi[2] -= dx2;
+                    }
+                }
+            for (size_t k = 0; k < n3; ++k)
+            {
+                vprev[k] = v[k];
+                v[k]     = (x[k] - xt[k]) / sdt;
+            }
+        }
+        // FinalizeActiveSet: a vertex stays active while behind its nearest triangle's plane.
+        for (int32_t q = 0; q < C.nSurfV; ++q)
+        {
+            if (!C.active[q])
+                continue;
+            nearest(C, x, q, list);
+            if (list.empty())
+                continue;
+            int32_t const* t = C.F + 3 * size_t(list.back());
+            V3 a = at(x, t[0]);
+            V3 nrm = cross(sub(at(x, t[1]), a), sub(at(x, t[2]), a));
+            C.active[q] = dot(sub(at(x, C.V[q]), a), nrm) < 0 ? 1 : 0;
+        }
+    }
+    return 0;
+}
+
+// FP64 evaluation of one vertex-triangle contact (for comparison with the reference's kernel);
+// epsilon regularises |u| (FLT_EPSILON for the GPU path, DBL_EPSILON for an FP64 instantiation).
+void orc_vertex_triangle_contact(double const* xtv, double const* xv, double const* xtf, double const* xf, double dt, double muC, double muF, double epsv, double epsilon, double* g, double* H)
+{
+    V3 tf[3], f[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        tf[k] = at(xtf, k);
+        f[k]  = at(xf, k);
+    }
+    vertex_triangle_contact(at(xtv, 0), at(xv, 0), tf, f, dt, muC, muF, epsv, g, H, epsilon);
+}
+
+} // extern "C"

@@ -260,6 +260,33 @@ float ref_vertex_triangle_contact(
     return E;
 }
 
+// The same kernel instantiated in FP64.
+double ref_vertex_triangle_contact_d(
+    double const* xtv,
+    double const* xv,
+    double const* xtf,
+    double const* xf,
+    double dt,
+    double muC,
+    double muF,
+    double epsv,
+    double* g,
+    double* H)
+{
+    mini::SVector<double, 3> xtv_ = load<3, 1>(xtv), xv_ = load<3, 1>(xv);
+    mini::SMatrix<double, 3, 3> xtf_ = load<3, 3>(xtf), xf_ = load<3, 3>(xf);
+    mini::SVector<double, 3> gi      = load<3, 1>(g);
+    mini::SMatrix<double, 3, 3> Hi   = load<3, 3>(H);
+    double E = pbat::sim::vbd::kernels::AccumulateVertexTriangleContact(xtv_, xv_, xtf_, xf_, dt, muC, muF, epsv, &gi, &Hi);
+    for (int r = 0; r < 3; ++r)
+    {
+        g[r] = gi(r);
+        for (int c = 0; c < 3; ++c)
+            H[3 * c + r] = Hi(r, c);
+    }
+    return E;
+}
+
 // A full step loop (sim/vbd/Integrator.cpp:22-96, ChebyshevIntegrator.cpp:15-32) whose
 // per-vertex work is the reference's own kernels.  Same argument meaning as orc_run.
 int ref_run(orc_problem const* Pp, double* x, double* v, double* vprev, double dt, int32_t iterations, int32_t substeps, int32_t nsteps)

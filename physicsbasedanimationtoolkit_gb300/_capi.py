@@ -64,6 +64,17 @@ class VbdDesc(C.Structure):
         ("chebyshev_formula", C.c_int32),
         ("semantics", C.c_int32),
         ("X", C.c_void_p),
+        ("n_collision_vertices", C.c_int32),
+        ("V", C.c_void_p),
+        ("n_collision_triangles", C.c_int32),
+        ("F", C.c_void_p),
+        ("B", C.c_void_p),
+        ("XVA", C.c_void_p),
+        ("FA", C.c_void_p),
+        ("muC", C.c_double),
+        ("muF", C.c_double),
+        ("epsv", C.c_double),
+        ("active_set_update_frequency", C.c_int32),
     ]
 
 
@@ -100,6 +111,7 @@ _SIGNATURES = [
     ("pbgb_vbd_stream", C.c_int, [_vp, C.POINTER(_vp)]),
     ("pbgb_vbd_set_sweep_timing", C.c_int, [_vp, _i32]),
     ("pbgb_vbd_sweep_timing", C.c_int, [_vp, C.POINTER(_f64), C.POINTER(C.c_int64)]),
+    ("pbgb_vbd_get_contacts", C.c_int, [_vp, _vp, _vp]),
     ("pbgb_vbd_objective", C.c_int, [_vp, _f64, C.POINTER(_f64)]),
     ("pbgb_vbd_gradient", C.c_int, [_vp, _f64, _vp]),
     ("pbgb_vbd_gradient_noalloc", C.c_int, [_vp, _f64, _vp]),
@@ -111,6 +123,14 @@ _SIGNATURES = [
     ("pbgb_bvh_topology", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("pbgb_bvh_overlaps", C.c_int, [_vp, _i32, _vp, _vp, _vp, C.c_int64, C.POINTER(C.c_int64)]),
     ("pbgb_bvh_last_error", C.c_char_p, [_vp]),
+    ("pbgb_ccd_create", C.c_int, [_i32, _i32, _vp, _i32, _vp, _vp, C.POINTER(_vp)]),
+    ("pbgb_ccd_destroy", C.c_int, [_vp]),
+    ("pbgb_ccd_initialize", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    ("pbgb_ccd_update", C.c_int, [_vp, _vp]),
+    ("pbgb_ccd_finalize", C.c_int, [_vp, _vp]),
+    ("pbgb_ccd_get", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    ("pbgb_ccd_last_error", C.c_char_p, [_vp]),
+    ("pbgb_debug_vertex_triangle_contact", C.c_int, [_vp, _vp, _vp, _vp, _f32, _f32, _f32, _f32, _vp, _vp, _vp]),
     ("pbgb_debug_vertex_block", C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _f64, _f64,
                                          _f64, _f64, _f64, _vp, _vp, _vp]),
 ]
@@ -136,6 +156,12 @@ def lib():
 def check(rc, handle=None):
     if rc != PBGB_OK:
         msg = lib().pbgb_last_error(handle)
+        raise PbgbError(rc, msg.decode() if msg else "")
+
+
+def check_ccd(rc, ccd=None):
+    if rc != PBGB_OK:
+        msg = lib().pbgb_ccd_last_error(ccd)
         raise PbgbError(rc, msg.decode() if msg else "")
 
 

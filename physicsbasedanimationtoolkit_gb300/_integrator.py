@@ -44,6 +44,20 @@ def make_desc(data, semantics):
     d = _capi.VbdDesc()
     d.n_vertices = nV
     d.n_tets = nT
+    if getattr(data, "F", None) is not None and np.asarray(data.F).size > 0:
+        keep.update(
+            V=_capi.i32(data.V),
+            F=_capi.i32(np.asarray(data.F).T),
+            B=_capi.i32(data.B),
+            XVA=_capi.f64(data.XVA),
+            FA=_capi.f64(data.FA),
+        )
+        d.n_collision_vertices = int(np.asarray(data.V).size)
+        d.n_collision_triangles = int(np.asarray(data.F).shape[1])
+    d.muC = float(data.muC)
+    d.muF = float(data.muF)
+    d.epsv = float(data.epsv)
+    d.active_set_update_frequency = int(data.active_set_update_frequency)
     for k, a in keep.items():
         setattr(d, k, a.ctypes.data)
     d.n_partitions = int(data.Pptr.size - 1)
@@ -161,6 +175,16 @@ class IntegratorBase:
         n = C.c_int64()
         _capi.check(_capi.lib().pbgb_vbd_launches_per_step(self._h, int(iterations), int(substeps), C.byref(n)), self._h)
         return n.value
+
+    def contacts(self):
+        """(fc, active): contact triangles per vertex (|#vertices| x 8, -1 = none) and the active
+        flags of the collision vertices after the last step."""
+        nV = self.n_vertices
+        fc = np.full((nV, 8), -1, np.int32)
+        nS = int(np.asarray(getattr(self.data, "V", np.zeros(0))).size)
+        active = np.zeros(max(nS, 1), np.uint8)
+        _capi.check(_capi.lib().pbgb_vbd_get_contacts(self._h, fc.ctypes.data, active.ctypes.data), self._h)
+        return fc, active[:nS]
 
     def objective(self, dt):
         """Backward-Euler objective at the current positions (FP64 device reduction)."""

@@ -370,6 +370,46 @@ int64_t radix_counts_size(int32_t n)
     return int64_t(kBuckets) * tiles_for(n > 0 ? n : 1);
 }
 
+cudaError_t bvh_allocate(BvhBuffers& B, int32_t capacity)
+{
+    B          = BvhBuffers{};
+    B.capacity = capacity;
+    size_t const n  = size_t(capacity > 0 ? capacity : 1);
+    size_t const ni = n > 1 ? n - 1 : 1;
+    cudaError_t e   = cudaSuccess;
+    auto get = [&](auto*& p, size_t count) {
+        if (e == cudaSuccess)
+            e = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(*p));
+    };
+    get(B.codes, n);
+    get(B.codesAlt, n);
+    get(B.inds, n);
+    get(B.indsAlt, n);
+    get(B.counts, size_t(radix_counts_size(capacity)));
+    get(B.child, 2 * ni);
+    get(B.parent, 2 * n);
+    get(B.rightmost, 2 * ni);
+    get(B.visits, ni);
+    get(B.ilo, ni);
+    get(B.ihi, ni);
+    get(B.llo, n);
+    get(B.lhi, n);
+    get(B.flags, 1);
+    if (e == cudaSuccess)
+        e = cudaMemset(B.flags, 0, sizeof(int32_t));
+    return e;
+}
+
+void bvh_release(BvhBuffers& B)
+{
+    void* ptrs[] = {B.codes, B.codesAlt, B.inds, B.indsAlt, B.counts, B.child, B.parent, B.rightmost,
+                    B.visits, B.ilo, B.ihi, B.llo, B.lhi, B.flags};
+    for (void* p : ptrs)
+        if (p)
+            cudaFree(p);
+    B = BvhBuffers{};
+}
+
 cudaError_t bvh_sort(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, float3 wmin, float3 wmax, cudaStream_t s)
 {
     return sort_impl(B, n, lo, hi, wmin, wmax, s);

@@ -54,6 +54,11 @@ struct BvhBuffers
 // Number of uint32 digit counters the radix sort needs for n keys.
 int64_t radix_counts_size(int32_t n);
 
+// Device arrays of a BVH for up to `capacity` boxes (bvh_release frees them; safe on partial
+// allocation).
+cudaError_t bvh_allocate(BvhBuffers& B, int32_t capacity);
+void bvh_release(BvhBuffers& B);
+
 // Full build from unsorted boxes lo/hi (n each) and the scene box (wmin, wmax).
 cudaError_t bvh_build(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, float3 wmin, float3 wmax, cudaStream_t s);
 // Only the Morton codes + stable sort (codes, inds ascending) — exposed for tests.

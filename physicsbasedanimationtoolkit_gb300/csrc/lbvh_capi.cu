@@ -59,8 +59,8 @@ struct pbgb_bvh
     {
         if (stream)
             cudaStreamSynchronize(stream);
-        void* ptrs[] = {B.codes, B.codesAlt, B.inds, B.indsAlt, B.counts, B.child, B.parent, B.rightmost,
-                        B.visits, B.ilo, B.ihi, B.llo, B.lhi, B.flags, lo, hi, qlo, qhi, pairs, count};
+        pbgb::bvh_release(B);
+        void* ptrs[] = {lo, hi, qlo, qhi, pairs, count};
         for (void* p : ptrs)
             if (p)
                 cudaFree(p);
@@ -70,25 +70,10 @@ struct pbgb_bvh
 
     void allocate(int32_t cap)
     {
-        capacity   = cap;
-        size_t n   = size_t(cap);
-        size_t ni  = n > 1 ? n - 1 : 1;
-        B.capacity = cap;
-        B.codes    = dalloc<uint32_t>(n);
-        B.codesAlt = dalloc<uint32_t>(n);
-        B.inds     = dalloc<int32_t>(n);
-        B.indsAlt  = dalloc<int32_t>(n);
-        B.counts   = dalloc<uint32_t>(size_t(pbgb::radix_counts_size(cap)));
-        B.child    = dalloc<int32_t>(2 * ni);
-        B.parent   = dalloc<int32_t>(2 * n);
-        B.rightmost = dalloc<int32_t>(2 * ni);
-        B.visits   = dalloc<int32_t>(ni);
-        B.ilo      = dalloc<float4>(ni);
-        B.ihi      = dalloc<float4>(ni);
-        B.llo      = dalloc<float4>(n);
-        B.lhi      = dalloc<float4>(n);
-        B.flags    = dalloc<int32_t>(1);
-        lo         = dalloc<float4>(n);
+        capacity = cap;
+        size_t n = size_t(cap);
+        ck(pbgb::bvh_allocate(B, cap), "cudaMalloc");
+        lo       = dalloc<float4>(n);
         hi         = dalloc<float4>(n);
         count      = dalloc<unsigned long long>(1);
         ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");

@@ -6,9 +6,12 @@
 // one stream per handle (the reference creates one and never uses it), the whole step replayed
 // from a CUDA graph, tets packed into 64-byte records, the in-place colour sweep (no xb copy-back
 // pass), and several meshes concatenated into one system for the batched form.
+#include "contact.cuh"
 #include "pbat_gb300.h"
 #include "vbd_construct.h"
 #include "vbd_kernels.cuh"
+
+#include <cfloat>
 
 #include <cuda_runtime.h>
 
@@ -109,6 +112,18 @@ class VbdSystem
     bool profiling = false;
     std::vector<cudaEvent_t> evBegin, evEnd;
 
+    // Vertex-triangle contact (single mesh with a collision surface).
+    bool contact = false;
+    float muC = 1e6f, muF = 0.3f, epsv = 1e-3f;
+    int32_t activeSetFreq = 1;
+    ContactMesh cmesh{};
+    ContactState cstate{};
+    DeviceArray<int32_t> cV, cB, vcolorD, cAv, cNActive, cNn, cFc, cFlags;
+    DeviceArray<int4> cF;
+    DeviceArray<float> cXVA, cFA, cDupper;
+    DeviceArray<float4> cTlo, cThi, cVlo, cVhi, xpred;
+    DeviceArray<uint8_t> cActive;
+
     // Graph cache for Step(dt, iterations, substeps)
     cudaGraphExec_t graph = nullptr;
     float gDt = -1.f;
@@ -117,6 +132,9 @@ class VbdSystem
 
     ~VbdSystem()
     {
+        if (stream)
+            cudaStreamSynchronize(stream);
+        bvh_release(cstate.bvh);
         releaseEvents();
         if (graph)
             cudaGraphExecDestroy(graph);
@@ -380,6 +398,109 @@ class VbdSystem
             check(cudaMemsetAsync(xtilde.get(), 0, sizeof(float4) * nV, stream), "memset");
         }
         check(cudaMemsetAsync(flags.get(), 0, sizeof(int32_t) * 4, stream), "memset");
+        vcolorD.allocate(nV);
+        vcolorD.upload(color.data(), nV, stream);
+        std::vector<int32_t> hV, hB;
+        std::vector<int4> hF;
+        std::vector<float> hXVA, hFA;
+        std::vector<float> hDupper;
+        if (d0.n_collision_triangles > 0)
+        {
+            if (nMeshes != 1)
+                throw std::invalid_argument("contact is supported on a single (non-batched) mesh");
+            if (!d0.V || !d0.F || !d0.XVA || !d0.FA || d0.n_collision_vertices <= 0)
+                throw std::invalid_argument("pbgb_vbd_desc: contact needs V, F, XVA and FA");
+            if (d0.active_set_update_frequency < 1)
+                throw std::invalid_argument("pbgb_vbd_desc: active set update frequency must be >= 1");
+            contact       = true;
+            muC           = float(d0.muC);
+            muF           = float(d0.muF);
+            epsv          = float(d0.epsv);
+            activeSetFreq = d0.active_set_update_frequency;
+            int32_t const nS = d0.n_collision_vertices, nF = d0.n_collision_triangles;
+            hV.assign(d0.V, d0.V + nS);
+            for (int32_t q : hV)
+                if (q < 0 || q >= nV)
+                    throw std::invalid_argument("pbgb_vbd_desc: collision vertex out of range");
+            hF.resize(size_t(nF));
+            for (int32_t f = 0; f < nF; ++f)
+            {
+                int32_t const* t = d0.F + 3 * size_t(f);
+                for (int k = 0; k < 3; ++k)
+                    if (t[k] < 0 || t[k] >= nV)
+                        throw std::invalid_argument("pbgb_vbd_desc: collision triangle index out of range");
+                hF[f] = make_int4(t[0], t[1], t[2], 0);
+            }
+            hB.resize(size_t(nV));
+            for (int32_t i = 0; i < nV; ++i)
+                hB[i] = d0.B ? d0.B[i] : 1;
+            hXVA.resize(size_t(nV));
+            for (int32_t i = 0; i < nV; ++i)
+                hXVA[i] = float(d0.XVA[i]);
+            hFA.resize(size_t(nF));
+            for (int32_t f = 0; f < nF; ++f)
+                hFA[f] = float(d0.FA[f]);
+            hDupper.assign(size_t(nS), FLT_MAX);
+            cV.allocate(nS);
+            cF.allocate(nF);
+            cB.allocate(nV);
+            cXVA.allocate(nV);
+            cFA.allocate(nF);
+            cDupper.allocate(nS);
+            cTlo.allocate(nF);
+            cThi.allocate(nF);
+            cVlo.allocate(nS);
+            cVhi.allocate(nS);
+            xpred.allocate(nV);
+            cActive.allocate(nS);
+            cAv.allocate(nS);
+            cNActive.allocate(1);
+            cNn.allocate(size_t(nS) * kMaxContacts);
+            cFc.allocate(size_t(nV) * kMaxContacts);
+            check(bvh_allocate(cstate.bvh, nF), "cudaMalloc");
+            cV.upload(hV.data(), nS, stream);
+            cF.upload(hF.data(), nF, stream);
+            cB.upload(hB.data(), nV, stream);
+            cXVA.upload(hXVA.data(), nV, stream);
+            cFA.upload(hFA.data(), nF, stream);
+            cDupper.upload(hDupper.data(), nS, stream);
+            check(cudaMemsetAsync(cActive.get(), 0, size_t(nS), stream), "memset");
+            check(cudaMemsetAsync(cNActive.get(), 0, sizeof(int32_t), stream), "memset");
+            check(cudaMemsetAsync(cNn.get(), 0xFF, sizeof(int32_t) * size_t(nS) * kMaxContacts, stream), "memset");
+            check(cudaMemsetAsync(cFc.get(), 0xFF, sizeof(int32_t) * size_t(nV) * kMaxContacts, stream), "memset");
+            cmesh  = ContactMesh{nV, nS, nF, cV.get(), cF.get(), cB.get()};
+            cstate.tlo     = cTlo.get();
+            cstate.thi     = cThi.get();
+            cstate.vlo     = cVlo.get();
+            cstate.vhi     = cVhi.get();
+            cstate.active  = cActive.get();
+            cstate.dupper  = cDupper.get();
+            cstate.av      = cAv.get();
+            cstate.nActive = cNActive.get();
+            cstate.nn      = cNn.get();
+            cstate.fc      = cFc.get();
+            cstate.flags   = cstate.bvh.flags;
+            // Default scene box: the rest positions' box (pbgb_vbd_set_scene_bounding_box overrides).
+            for (int k = 0; k < 3; ++k)
+            {
+                sceneMin[k] = FLT_MAX;
+                sceneMax[k] = -FLT_MAX;
+            }
+            for (int32_t i = 0; i < nV; ++i)
+            {
+                float const p[3] = {hX[i].x, hX[i].y, hX[i].z};
+                for (int k = 0; k < 3; ++k)
+                {
+                    sceneMin[k] = std::min(sceneMin[k], p[k]);
+                    sceneMax[k] = std::max(sceneMax[k], p[k]);
+                }
+            }
+            if (!h0.get())
+            {
+                h0.allocate(nV);
+                h1.allocate(nV);
+            }
+        }
         // The host staging vectors die at the end of this scope: wait for the uploads.
         check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
     }
@@ -406,14 +527,20 @@ class VbdSystem
         return p;
     }
 
-    // Enqueue one full step on `stream` (captured into a graph by step()).
+    // Enqueue one full step on `stream` (captured into a graph by step()).  Order of the
+    // reference GPU integrator (gpu/impl/vbd/Integrator.cu:82-103): contact active set initialised
+    // on the full-step prediction, per substep inertial target + initial guess, contact list update,
+    // colour sweeps, velocity update; contact active set finalised at the end.
     void enqueueStep(float dt, int32_t iterations, int32_t substeps)
     {
-        float const h   = dt / float(substeps);
-        float const h2  = h * h;
-        bool const cheb = acceleration == PBGB_ACCEL_CHEBYSHEV;
-        SubstepParams sp = substepParams(h);
-        if (!cheb)
+        float const h    = dt / float(substeps);
+        float const h2   = h * h;
+        bool const cheb  = acceleration == PBGB_ACCEL_CHEBYSHEV;
+        // Contact reads same-colour partners too, so it always uses the two-buffer sweep (with
+        // omega = 1 when there is no acceleration).
+        bool const twoBuffer = cheb || contact;
+        SubstepParams sp     = substepParams(h);
+        if (!twoBuffer)
             sp.h0 = sp.h1 = nullptr;
         else if (iterations > 0)
             sp.result = ((iterations - 1) % 2 == 0) ? h0.get() : h1.get();
@@ -430,22 +557,47 @@ class VbdSystem
         w.h2       = h2;
         w.kD       = kD;
         w.detHZero = detHZero;
+        w.omega    = 1.f;
+        w.k        = 0;
+        if (contact)
+        {
+            w.fc     = cFc.get();
+            w.F      = cF.get();
+            w.XVA    = cXVA.get();
+            w.FA     = cFA.get();
+            w.vcolor = vcolorD.get();
+            w.muC    = muC;
+            w.muF    = muF;
+            w.epsv   = epsv;
+        }
         int const L = lanesToUse();
         if (profiling)
             ensureEvents(size_t(iterations) * size_t(substeps));
         float4* H[2] = {h0.get(), h1.get()};
+        float3 const wmin = make_float3(sceneMin[0], sceneMin[1], sceneMin[2]);
+        float3 const wmax = make_float3(sceneMax[0], sceneMax[1], sceneMax[2]);
+        if (contact)
+        {
+            check(contact_predict(nV, x.get(), v.get(), aext.get(), dt, xpred.get(), stream), "contact_predict");
+            check(contact_initialize(cmesh, cstate, x.get(), xpred.get(), wmin, wmax, stream), "contact_initialize");
+        }
         for (int32_t s = 0; s < substeps; ++s)
         {
             check(launch_begin_substep(sp, stream), "begin_substep");
+            if (contact && s % activeSetFreq == 0)
+                check(contact_update(cmesh, cstate, x.get(), stream), "contact_update");
             double omega      = 0.0;
             double const rho2 = rho * rho;
             for (int32_t k = 0; k < iterations; ++k)
             {
-                if (cheb)
+                if (twoBuffer)
                 {
-                    omega   = chebyshev_omega<double>(k, rho2, omega, chebFormula);
-                    w.omega = float(omega);
-                    w.k     = k;
+                    if (cheb)
+                    {
+                        omega   = chebyshev_omega<double>(k, rho2, omega, chebFormula);
+                        w.omega = float(omega);
+                        w.k     = k;
+                    }
                     w.hprev = H[(k + 1) % 2];
                     w.hcur  = H[k % 2];
                 }
@@ -456,13 +608,16 @@ class VbdSystem
                 {
                     w.begin = colorPtr[c];
                     w.end   = colorPtr[c + 1];
-                    check(launch_sweep(w, L, block, cheb, pdl, stream), "sweep");
+                    w.color = c;
+                    check(launch_sweep(w, L, block, twoBuffer, pdl, stream), "sweep");
                 }
                 if (profiling)
                     check(cudaEventRecordWithFlags(evEnd[slot], stream, cudaEventRecordExternal), "cudaEventRecord");
             }
             check(launch_end_substep(sp, stream), "end_substep");
         }
+        if (contact)
+            check(contact_finalize(cmesh, cstate, x.get(), stream), "contact_finalize");
     }
 
     int64_t launchesPerStep(int32_t iterations, int32_t substeps) const
@@ -470,7 +625,15 @@ class VbdSystem
         int64_t perIter = 0;
         for (int32_t c = 0; c < nColors; ++c)
             perIter += colorPtr[c + 1] > colorPtr[c] ? 1 : 0;
-        return int64_t(substeps) * (2 * (nV > 0 ? 1 : 0) + int64_t(iterations) * perIter);
+        int64_t n = int64_t(substeps) * (2 * (nV > 0 ? 1 : 0) + int64_t(iterations) * perIter);
+        if (contact)
+        {
+            // predict, vertex and triangle boxes, Morton, 4 x (count, scan, scatter), Karras, leaf
+            // gather, internal boxes, overlaps, compaction; then 4 per update and 4 at finalize.
+            int64_t const updates = (substeps + activeSetFreq - 1) / activeSetFreq;
+            n += 21 + 4 * updates + 4;
+        }
+        return n;
     }
 
     void step(float dt, int32_t iterations, int32_t substeps)
@@ -1069,6 +1232,27 @@ PBGB_API int pbgb_vbd_stream(pbgb_vbd* h, void** stream)
     return kOk;
 }
 
+PBGB_API int pbgb_vbd_get_contacts(pbgb_vbd* h, int32_t* fc, uint8_t* active)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    return guarded(h, [&] {
+        auto& s = h->sys;
+        check(cudaStreamSynchronize(s.stream), "cudaStreamSynchronize");
+        if (!s.contact)
+        {
+            if (fc)
+                std::fill(fc, fc + size_t(s.nV) * pbgb::kMaxContacts, -1);
+            return int(kOk);
+        }
+        if (fc)
+            check(cudaMemcpy(fc, s.cFc.get(), sizeof(int32_t) * size_t(s.nV) * pbgb::kMaxContacts, cudaMemcpyDeviceToHost), "D2H");
+        if (active)
+            check(cudaMemcpy(active, s.cActive.get(), size_t(s.cmesh.nSurfV), cudaMemcpyDeviceToHost), "D2H");
+        return int(kOk);
+    });
+}
+
 PBGB_API int pbgb_vbd_objective(pbgb_vbd* h, double dt, double* f)
 {
     if (!h || !f)
@@ -1172,6 +1356,38 @@ PBGB_API const char* pbgb_last_error(pbgb_vbd* h)
     if (h)
         return h->sys.lastError.c_str();
     return pbgb::gLastError.c_str();
+}
+
+PBGB_API int pbgb_debug_vertex_triangle_contact(
+    const float* xtv,
+    const float* xv,
+    const float* xtf,
+    const float* xf,
+    float dt,
+    float muC,
+    float muF,
+    float epsv,
+    float* g,
+    float* H,
+    float* energy)
+{
+    if (!xtv || !xv || !xtf || !xf || !g || !H)
+        return fail(nullptr, kInvalid, "pbgb_debug_vertex_triangle_contact: null argument");
+    float tf[3][3], f[3][3];
+    for (int k = 0; k < 3; ++k)
+        for (int r = 0; r < 3; ++r)
+        {
+            tf[k][r] = xtf[3 * k + r];
+            f[k][r]  = xf[3 * k + r];
+        }
+    float Hs[6] = {H[0], H[3], H[6], H[4], H[7], H[8]};
+    float const E = pbgb::vertex_triangle_contact(xtv, xv, tf, f, dt, muC, muF, epsv, FLT_EPSILON, g, Hs);
+    H[0] = Hs[0], H[1] = Hs[1], H[2] = Hs[2];
+    H[3] = Hs[1], H[4] = Hs[3], H[5] = Hs[4];
+    H[6] = Hs[2], H[7] = Hs[4], H[8] = Hs[5];
+    if (energy)
+        *energy = E;
+    return kOk;
 }
 
 PBGB_API int pbgb_debug_vertex_block(

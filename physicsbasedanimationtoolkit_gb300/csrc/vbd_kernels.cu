@@ -5,6 +5,8 @@
 
 namespace pbgb {
 
+int constexpr kMaxContactsPerVertex = 8;
+
 namespace {
 
 __device__ __forceinline__ void load3(float4 const v, float* o)
@@ -17,6 +19,41 @@ __device__ __forceinline__ void load3(float4 const v, float* o)
 __device__ __forceinline__ uint32_t corner(uint4 const& t, int a)
 {
     return a == 0 ? t.x : (a == 1 ? t.y : (a == 2 ? t.z : t.w));
+}
+
+// Contact energy of vertex i (gpu/impl/vbd/Kernels.cuh:80-114,203-223): the contact penalty is
+// scaled by the vertex area over the summed areas of the vertex's contact triangles, and every
+// listed triangle adds its normal penalty and friction (vertex_triangle_contact).
+__device__ __noinline__ void add_contacts(SweepParams const& p, int i, float const* xt, float const* xi, float* H, float* g)
+{
+    int32_t f[kMaxContactsPerVertex];
+    int n = 0;
+#pragma unroll
+    for (int c = 0; c < kMaxContactsPerVertex; ++c)
+    {
+        f[c] = p.fc[i * kMaxContactsPerVertex + c];
+        n += f[c] >= 0 ? 1 : 0;
+    }
+    if (n == 0)
+        return;
+    float sumfa = 0.f;
+    for (int c = 0; c < n; ++c)
+        sumfa += p.FA[f[c]];
+    float const kC = (p.XVA[i] * p.muC) / sumfa;
+    for (int c = 0; c < n; ++c)
+    {
+        int4 const t   = p.F[f[c]];
+        int const v[3] = {t.x, t.y, t.z};
+        float xtf[3][3], xf[3][3];
+        for (int k = 0; k < 3; ++k)
+        {
+            float4 const a = p.xt[v[k]];
+            float4 const b = __ldcg((p.vcolor[v[k]] < p.color ? p.x : p.hprev) + v[k]);
+            xtf[k][0] = a.x, xtf[k][1] = a.y, xtf[k][2] = a.z;
+            xf[k][0] = b.x, xf[k][1] = b.y, xf[k][2] = b.z;
+        }
+        vertex_triangle_contact(xt, xi, xtf, xf, p.h, kC * p.FA[f[c]], p.muF, p.epsv, FLT_EPSILON, g, H);
+    }
 }
 
 // Per-colour Gauss-Seidel sweep (reference: VbdIteration, gpu/impl/vbd/Kernels.cuh:148-233, and
@@ -129,7 +166,11 @@ __global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
     float4 const xl4  = p.xtilde[i];
     float const xt[3] = {xt4.x, xt4.y, xt4.z};
     float const xl[3] = {xl4.x, xl4.y, xl4.z};
-    bool const moved  = newton_update(b, xt, xl, xt4.w, p.h, p.h2, p.kD, p.detHZero, xi);
+    float H[6], g[3];
+    elastic_system(b, xt, xi, p.h, p.kD, H, g);
+    if (CHEB && p.fc)
+        add_contacts(p, i, xt, xi, H, g);
+    bool const moved = inertia_solve(H, g, xl, xt4.w, p.h2, p.detHZero, xi);
     if (CHEB)
     {
         // Raw iterate k (even when the Newton step was skipped: later colours read it).

@@ -54,6 +54,17 @@ struct SweepParams
     float detHZero;
     int32_t k;   // iteration index (Chebyshev)
     float omega; // Chebyshev weight of iteration k
+    // Vertex-triangle contact (fc == nullptr: none).  Contact triangles' corners are read with
+    // the same colour rule as mesh neighbours: colour < `color` from x, otherwise from hprev.
+    int32_t const* __restrict__ fc;     // nV x 8 contact triangles, -1 = none
+    int4 const* __restrict__ F;         // collision triangles
+    float const* __restrict__ XVA;      // nV vertex areas
+    float const* __restrict__ FA;       // triangle areas
+    int32_t const* __restrict__ vcolor; // nV colour of each vertex (-1 for pinned ones)
+    int32_t color;                      // colour of this launch
+    float muC;
+    float muF;
+    float epsv;
 };
 
 struct SubstepParams

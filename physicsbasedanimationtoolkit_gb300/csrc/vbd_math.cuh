@@ -107,26 +107,15 @@ PBGB_HD void accumulate_tet(VertexBlock<T>& b, T const (&d)[3][3], T const (&G)[
     b.C[5] += law * c[2] * c[2];
 }
 
-// Finishes the vertex: Rayleigh damping (sim/vbd/Kernels.h:179-191), inertia (:310-322) and the
-// 3x3 Newton step with the near-singular skip (:329-339).  Updates x in place; returns false when
-// the step was skipped.
+// Elastic block with Rayleigh damping (sim/vbd/Kernels.h:179-191): H = s I + C, g from the
+// accumulated block; damping adds (kD/h) H (x - xt) to g and scales H by 1 + kD/h.
+// H is symmetric (xx xy xz yy yz zz).
 template <class T>
-PBGB_HD bool newton_update(
-    VertexBlock<T> const& b,
-    T const* xt,
-    T const* xtilde,
-    T m,
-    T h,
-    T h2,
-    T kD,
-    T detHZero,
-    T* x,
-    T* gout = nullptr,
-    T* Hout = nullptr)
+PBGB_HD void elastic_system(VertexBlock<T> const& b, T const* xt, T const* x, T h, T kD, T* H, T* g)
 {
-    // H = s I + C (symmetric; xx xy xz yy yz zz)
-    T H[6] = {b.C[0] + b.s, b.C[1], b.C[2], b.C[3] + b.s, b.C[4], b.C[5] + b.s};
-    T g[3] = {b.g[0], b.g[1], b.g[2]};
+    H[0] = b.C[0] + b.s, H[1] = b.C[1], H[2] = b.C[2];
+    H[3] = b.C[3] + b.s, H[4] = b.C[4], H[5] = b.C[5] + b.s;
+    g[0] = b.g[0], g[1] = b.g[1], g[2] = b.g[2];
     if (kD != T(0))
     {
         T const D  = kD / h;
@@ -138,6 +127,13 @@ PBGB_HD bool newton_update(
         for (int q = 0; q < 6; ++q)
             H[q] *= s;
     }
+}
+
+// Inertia (sim/vbd/Kernels.h:310-322) and the 3x3 Newton step with the near-singular skip
+// (:329-339).  Updates x in place; returns false when the step was skipped.
+template <class T>
+PBGB_HD bool inertia_solve(T* H, T* g, T const* xtilde, T m, T h2, T detHZero, T* x, T* gout = nullptr, T* Hout = nullptr)
+{
     T const K = m / h2;
     H[0] += K;
     H[3] += K;
@@ -169,6 +165,124 @@ PBGB_HD bool newton_update(
     x[1] -= inv * (a01 * g[0] + a11 * g[1] + a12 * g[2]);
     x[2] -= inv * (a02 * g[0] + a12 * g[1] + a22 * g[2]);
     return true;
+}
+
+// Finishes a vertex without contact: damping, inertia and the Newton step.
+template <class T>
+PBGB_HD bool newton_update(
+    VertexBlock<T> const& b,
+    T const* xt,
+    T const* xtilde,
+    T m,
+    T h,
+    T h2,
+    T kD,
+    T detHZero,
+    T* x,
+    T* gout = nullptr,
+    T* Hout = nullptr)
+{
+    T H[6], g[3];
+    elastic_system(b, xt, x, h, kD, H, g);
+    return inertia_solve(H, g, xtilde, m, h2, detHZero, x, gout, Hout);
+}
+
+// Vertex-triangle contact (sim/vbd/Kernels.h:215-302 of the reference): penalty 1/2 muC d^2 on the
+// signed distance d = min(0, (xv - xb) . n) to the triangle's plane when xv projects inside the
+// triangle, plus IPC's smoothed friction (epsv * dt) in the tangent basis (xf1 - xf0, n x (xf1 -
+// xf0)).  The basis vectors are not normalised, as in the reference.  Adds to g and H
+// (symmetric, xx xy xz yy yz zz); returns the energy.
+//   xtv, xv: vertex at t and now; xtf, xf: triangle corners at t and now (3 x 3, corner-major).
+template <class T>
+PBGB_HD T vertex_triangle_contact(
+    T const* xtv,
+    T const* xv,
+    T const (&xtf)[3][3],
+    T const (&xf)[3][3],
+    T dt,
+    T muC,
+    T muF,
+    T epsv,
+    T epsilon,
+    T* g,
+    T* H)
+{
+    T e0[3], e1[3], n[3];
+    for (int r = 0; r < 3; ++r)
+    {
+        e0[r] = xf[1][r] - xf[0][r];
+        e1[r] = xf[2][r] - xf[0][r];
+    }
+    n[0]            = e0[1] * e1[2] - e0[2] * e1[1];
+    n[1]            = e0[2] * e1[0] - e0[0] * e1[2];
+    n[2]            = e0[0] * e1[1] - e0[1] * e1[0];
+    T const dblArea = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (dblArea <= T(1e-8))
+        return T(0);
+    for (int r = 0; r < 3; ++r)
+        n[r] /= dblArea;
+    // Projection of xv on the triangle's plane, and its barycentric coordinates.
+    T const t = n[0] * (xv[0] - xf[0][0]) + n[1] * (xv[1] - xf[0][1]) + n[2] * (xv[2] - xf[0][2]);
+    T ap[3];
+    for (int r = 0; r < 3; ++r)
+        ap[r] = (xv[r] - t * n[r]) - xf[0][r];
+    T const d00   = e0[0] * e0[0] + e0[1] * e0[1] + e0[2] * e0[2];
+    T const d01   = e0[0] * e1[0] + e0[1] * e1[1] + e0[2] * e1[2];
+    T const d11   = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+    T const d20   = ap[0] * e0[0] + ap[1] * e0[1] + ap[2] * e0[2];
+    T const d21   = ap[0] * e1[0] + ap[1] * e1[1] + ap[2] * e1[2];
+    T const denom = d00 * d11 - d01 * d01;
+    T const bv    = (d11 * d20 - d01 * d21) / denom;
+    T const bw    = (d00 * d21 - d01 * d20) / denom;
+    T const bu    = T(1) - bv - bw;
+    bool const inside = bu >= T(0) && bu <= T(1) && bv >= T(0) && bv <= T(1) && bw >= T(0) && bw <= T(1);
+    if (!inside)
+        return T(0);
+    T xb[3], xtb[3];
+    for (int r = 0; r < 3; ++r)
+    {
+        xb[r]  = xf[0][r] * bu + xf[1][r] * bv + xf[2][r] * bw;
+        xtb[r] = xtf[0][r] * bu + xtf[1][r] * bv + xtf[2][r] * bw;
+    }
+    T dn = (xv[0] - xb[0]) * n[0] + (xv[1] - xb[1]) * n[1] + (xv[2] - xb[2]) * n[2];
+    T const d      = dn < T(0) ? dn : T(0);
+    T const lambda = muC * d;
+    T E            = T(0.5) * lambda * d;
+    for (int r = 0; r < 3; ++r)
+        g[r] += lambda * n[r];
+    H[0] += muC * n[0] * n[0];
+    H[1] += muC * n[0] * n[1];
+    H[2] += muC * n[0] * n[2];
+    H[3] += muC * n[1] * n[1];
+    H[4] += muC * n[1] * n[2];
+    H[5] += muC * n[2] * n[2];
+    // Friction in the (e0, n x e0) basis on the relative tangential displacement.
+    T b1[3];
+    b1[0] = n[1] * e0[2] - n[2] * e0[1];
+    b1[1] = n[2] * e0[0] - n[0] * e0[2];
+    b1[2] = n[0] * e0[1] - n[1] * e0[0];
+    T dx[3];
+    for (int r = 0; r < 3; ++r)
+        dx[r] = (xv[r] - xtv[r]) - (xb[r] - xtb[r]);
+    T const u0      = e0[0] * dx[0] + e0[1] * dx[1] + e0[2] * dx[2];
+    T const u1      = b1[0] * dx[0] + b1[1] * dx[1] + b1[2] * dx[2];
+    T const unorm   = sqrt(u0 * u0 + u1 * u1) + epsilon;
+    T const epsvh   = epsv * dt;
+    T const muFlam  = muF * fabs(lambda);
+    T const y       = unorm / epsvh;
+    T const f1      = y < T(1) ? T(2) * y - y * y : T(1);
+    T const s       = muFlam * f1 / unorm;
+    for (int r = 0; r < 3; ++r)
+        g[r] += s * (e0[r] * u0 + b1[r] * u1);
+    H[0] += s * (e0[0] * e0[0] + b1[0] * b1[0]);
+    H[1] += s * (e0[0] * e0[1] + b1[0] * b1[1]);
+    H[2] += s * (e0[0] * e0[2] + b1[0] * b1[2]);
+    H[3] += s * (e0[1] * e0[1] + b1[1] * b1[1]);
+    H[4] += s * (e0[1] * e0[2] + b1[1] * b1[2]);
+    H[5] += s * (e0[2] * e0[2] + b1[2] * b1[2]);
+    T const un2 = unorm * unorm;
+    E += muFlam * (T(1) / T(3) * epsvh + un2 / epsvh - un2 * unorm / (T(3) * epsvh * epsvh));
+    return E;
 }
 
 // Initial guess of the block-coordinate solve (sim/vbd/Kernels.h:39-94).  `tiny` is the smallest

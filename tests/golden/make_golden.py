@@ -187,6 +187,39 @@ def morton_codes(R, rng):
     np.savez_compressed(HERE / "morton.npz", lo=lo, hi=hi, wmin=wmin, wmax=wmax, codes=codes)
 
 
+def contact_cases(R, rng):
+    """The reference's vertex-triangle contact kernel in FP64 on seeded configurations: vertices
+    slightly behind or in front of a triangle's plane, inside and outside its projection."""
+    n = 96
+    out = {k: [] for k in ("xtv", "xv", "xtf", "xf", "dt", "muC", "muF", "epsv", "g", "H", "E")}
+    for c in range(n):
+        xf = rng.uniform(-0.5, 0.5, (3, 3))
+        xf[:, 2] = rng.uniform(-0.05, 0.05, 3)
+        xtf = xf + rng.uniform(-0.01, 0.01, (3, 3))
+        bary = rng.dirichlet([1, 1, 1]) if c % 4 else rng.uniform(-0.5, 1.5, 3)
+        p = bary @ xf
+        nrm = np.cross(xf[1] - xf[0], xf[2] - xf[0])
+        nrm /= np.linalg.norm(nrm)
+        xv = p + nrm * rng.uniform(-0.02, 0.01)
+        xtv = xv + rng.uniform(-0.01, 0.01, 3)
+        g = rng.standard_normal(3)
+        H = rng.standard_normal((3, 3))
+        H = H + H.T
+        args = dict(xtv=xtv, xv=xv, xtf=np.ascontiguousarray(xtf.ravel()), xf=np.ascontiguousarray(xf.ravel()),
+                    dt=1 / 60, muC=rng.uniform(1e4, 1e7), muF=rng.uniform(0.0, 0.6),
+                    epsv=[1e-3, 1e-1, 10.0][c % 3])
+        g_out = g.copy()
+        H_out = np.ascontiguousarray(H.ravel(order="F"))
+        E = R.ref_vertex_triangle_contact_d(args["xtv"], args["xv"], args["xtf"], args["xf"], args["dt"],
+                                            args["muC"], args["muF"], args["epsv"], g_out, H_out)
+        for k, v in args.items():
+            out[k].append(v)
+        out["g"].append(np.stack([g, g_out]))
+        out["H"].append(np.stack([H.ravel(order="F"), H_out]))
+        out["E"].append(E)
+    np.savez_compressed(HERE / "contact.npz", **{k: np.array(v) for k, v in out.items()})
+
+
 def main():
     O.build_oracle(ref=True)
     R = O.ref()
@@ -200,6 +233,7 @@ def main():
     coloring(R)
     trajectories(R)
     morton_codes(R, rng)
+    contact_cases(R, rng)
     print("fixtures written to", HERE)
 
 

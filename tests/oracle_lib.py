@@ -107,6 +107,10 @@ def lib():
         L.orc_bvh_build.argtypes = [C.c_int32, _f32p, _f32p, _f32p, _f32p, _u32p, _i32p, _i32p, _i32p,
                                     _i32p, _f32p, _f32p]
         L.orc_bvh_boxes.argtypes = [C.c_int32, _i32p, _i32p, _f32p, _f32p, _f32p, _f32p]
+        L.orc_vertex_triangle_contact.argtypes = [_f64p] * 4 + [C.c_double] * 5 + [_f64p, _f64p]
+        L.orc_run_contact.restype = C.c_int
+        L.orc_run_contact.argtypes = [C.POINTER(OrcProblem), C.c_void_p, _f64p, _f64p, _f64p, C.c_double,
+                                      C.c_int32, C.c_int32, C.c_int32]
         L.orc_overlaps.restype = C.c_int64
         L.orc_overlaps.argtypes = [C.c_int32, _f32p, _f32p, C.c_int32, _f32p, _f32p, _i32p, C.c_int64]
         _lib = L
@@ -140,6 +144,8 @@ def ref():
         L.ref_run.restype = C.c_int
         L.ref_run.argtypes = lib().orc_run.argtypes
         fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        L.ref_vertex_triangle_contact_d.restype = C.c_double
+        L.ref_vertex_triangle_contact_d.argtypes = [_f64p] * 4 + [C.c_double] * 4 + [_f64p, _f64p]
         L.ref_vertex_triangle_contact.restype = C.c_float
         L.ref_vertex_triangle_contact.argtypes = [
             fp, fp, fp, fp, C.c_float, C.c_float, C.c_float, C.c_float, fp, fp,
@@ -238,6 +244,52 @@ class OracleVbd:
         g = np.zeros(self.X.shape[0] * 3)
         lib().orc_gradient(C.byref(self.P), np.ascontiguousarray(x), np.ascontiguousarray(xtilde), dt, g)
         return g
+
+
+class OrcContact(C.Structure):
+    """Mirror of ``orc_contact`` (oracle/contact_oracle.cpp)."""
+
+    _fields_ = [
+        ("nSurfV", C.c_int32), ("V", C.c_void_p), ("nF", C.c_int32), ("F", C.c_void_p), ("B", C.c_void_p),
+        ("XVA", C.c_void_p), ("FA", C.c_void_p), ("muC", C.c_double), ("muF", C.c_double),
+        ("epsv", C.c_double), ("freq", C.c_int32), ("active", C.c_void_p), ("dupper", C.c_void_p),
+        ("fc", C.c_void_p),
+    ]
+
+
+class OracleContactVbd(OracleVbd):
+    """FP64 oracle of the contact-enabled step (GPU integrator semantics)."""
+
+    def __init__(self, X, T, rho, mu, lam, dbc, V, F, B, muC=1e6, muF=0.3, epsv=1e-3, freq=1, **kw):
+        kw.setdefault("semantics", 1)
+        super().__init__(X, T, rho, mu, lam, dbc, **kw)
+        X = self.X
+        Fv = np.ascontiguousarray(F, dtype=np.int32)
+        dbl = np.linalg.norm(np.cross(X[Fv[:, 1]] - X[Fv[:, 0]], X[Fv[:, 2]] - X[Fv[:, 0]]), axis=1)
+        XVA = np.zeros(X.shape[0])
+        for r in range(3):
+            np.add.at(XVA, Fv[:, r], dbl / 6.0)
+        self.cV = np.ascontiguousarray(V, dtype=np.int32)
+        self.cF = Fv
+        self.cB = np.ascontiguousarray(B, dtype=np.int32)
+        self.XVA = XVA
+        self.FA = dbl / 2.0
+        self.active = np.zeros(self.cV.size, np.uint8)
+        self.dupper = np.full(self.cV.size, float(np.finfo(np.float32).max))
+        self.fc = np.full(X.shape[0] * 8, -1, np.int32)
+        Cc = OrcContact()
+        Cc.nSurfV, Cc.nF = self.cV.size, Fv.shape[0]
+        Cc.V, Cc.F, Cc.B = self.cV.ctypes.data, Fv.ctypes.data, self.cB.ctypes.data
+        Cc.XVA, Cc.FA = self.XVA.ctypes.data, self.FA.ctypes.data
+        Cc.muC, Cc.muF, Cc.epsv, Cc.freq = muC, muF, epsv, freq
+        Cc.active, Cc.dupper, Cc.fc = self.active.ctypes.data, self.dupper.ctypes.data, self.fc.ctypes.data
+        self.C = Cc
+
+    def step(self, dt, iterations, substeps=1, nsteps=1, use_ref=False):
+        rc = lib().orc_run_contact(C.byref(self.P), C.addressof(self.C), self.x, self.v, self.vprev, dt,
+                                   iterations, substeps, nsteps)
+        if rc != 0:
+            raise RuntimeError(f"oracle run failed: {rc}")
 
 
 def bvh_build(lo, hi, wmin, wmax):

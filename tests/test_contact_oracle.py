@@ -1,0 +1,85 @@
+"""Contact term of the oracle and of the device arithmetic, pinned to the reference's
+AccumulateVertexTriangleContact (fixture made from its FP64 instantiation)."""
+
+import ctypes as C
+import pathlib
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from physicsbasedanimationtoolkit_gb300 import _capi, meshgen
+
+GOLD = pathlib.Path(__file__).resolve().parent / "golden"
+
+
+def test_oracle_contact_matches_reference_fixture():
+    g = np.load(GOLD / "contact.npz")
+    hit = 0
+    for k in range(g["dt"].size):
+        gg = g["g"][k, 0].copy()
+        H = g["H"][k, 0].copy()
+        O.lib().orc_vertex_triangle_contact(g["xtv"][k], g["xv"][k], g["xtf"][k], g["xf"][k], g["dt"][k], g["muC"][k],
+                                           g["muF"][k], g["epsv"][k], float(np.finfo(np.float64).eps), gg, H)
+        scale = max(1.0, np.abs(g["H"][k, 1]).max())
+        np.testing.assert_allclose(H, g["H"][k, 1], rtol=1e-9, atol=1e-9 * scale)
+        np.testing.assert_allclose(gg, g["g"][k, 1], rtol=1e-9, atol=1e-9 * max(1.0, np.abs(g["g"][k, 1]).max()))
+        hit += int(not np.allclose(g["g"][k, 0], g["g"][k, 1]))
+    assert hit > 20  # both contact and no-contact cases are covered
+
+
+def test_device_contact_arithmetic_matches_reference_fixture():
+    g = np.load(GOLD / "contact.npz")
+    L = _capi.lib()
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    for k in range(g["dt"].size):
+        gg = f(g["g"][k, 0])
+        H = f(g["H"][k, 0])
+        E = C.c_float()
+        args = [f(g["xtv"][k]), f(g["xv"][k]), f(g["xtf"][k]), f(g["xf"][k])]  # kept alive for the call
+        rc = L.pbgb_debug_vertex_triangle_contact(*[a.ctypes.data for a in args],
+                                                  g["dt"][k], g["muC"][k], g["muF"][k], g["epsv"][k],
+                                                  gg.ctypes.data, H.ctypes.data, C.byref(E))
+        assert rc == 0
+        ref_g, ref_H = g["g"][k, 1], g["H"][k, 1]
+        np.testing.assert_allclose(H, ref_H, rtol=2e-3, atol=2e-4 * max(1.0, np.abs(ref_H).max()))
+        np.testing.assert_allclose(gg, ref_g, rtol=2e-3, atol=2e-4 * max(1.0, np.abs(ref_g).max()))
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference harness not built")
+def test_oracle_contact_matches_reference_directly():
+    R = O.ref()
+    rng = np.random.default_rng(11)
+    for _ in range(200):
+        xf = rng.uniform(-1, 1, (3, 3))
+        p = rng.dirichlet([1, 1, 1]) @ xf
+        n = np.cross(xf[1] - xf[0], xf[2] - xf[0])
+        xv = p - 0.01 * n / np.linalg.norm(n)
+        xtv = xv + rng.uniform(-0.02, 0.02, 3)
+        xtf = (xf + rng.uniform(-0.02, 0.02, (3, 3))).ravel()
+        g1, H1, g2, H2 = np.zeros(3), np.zeros(9), np.zeros(3), np.zeros(9)
+        R.ref_vertex_triangle_contact_d(xtv, xv, xtf, np.ascontiguousarray(xf.ravel()), 1 / 60, 1e6, 0.3, 1e-2, g1, H1)
+        O.lib().orc_vertex_triangle_contact(xtv, xv, xtf, np.ascontiguousarray(xf.ravel()), 1 / 60, 1e6, 0.3, 1e-2,
+                                           float(np.finfo(np.float64).eps), g2, H2)
+        np.testing.assert_allclose(g2, g1, rtol=1e-10, atol=1e-9)
+        np.testing.assert_allclose(H2, H1, rtol=1e-10, atol=1e-9)
+
+
+def small_scene(n_cubes=2, hexes=3, slab=(8, 8, 1)):
+    return meshgen.contact_scene_workload(n_cubes_side=n_cubes, cube_hexes=hexes, slab_hexes=slab, gap=0.01)
+
+
+def test_oracle_contact_step_keeps_cubes_above_slab():
+    w = small_scene()
+    O_ = O.OracleContactVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], w["V"], w["F"], w["B"],
+                            muC=1e7, strategy=2)
+    z0 = w["X"][w["B"] > 0, 2].min()
+    zs = []
+    for _ in range(20):
+        O_.step(1 / 60, 20, 1, 1)
+        zs.append(O_.x[w["B"] > 0, 2].min())
+    assert np.isfinite(O_.x).all()
+    assert zs[-1] < z0  # fell onto the slab (top face at z = 0)
+    assert min(zs) > -0.02  # and was stopped by it
+    assert abs(zs[-1] - zs[-2]) < 2e-3  # coming to rest
+    assert O_.active.sum() > 0

@@ -1,0 +1,109 @@
+"""Vertex-triangle contact on the device: the reference doctest's active-set scenario, and
+contact-enabled steps against the FP64 oracle."""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from physicsbasedanimationtoolkit_gb300 import _capi, meshgen, pbat
+
+pytestmark = pytest.mark.gpu
+
+
+class Ccd:
+    def __init__(self, nV, V, F, B):
+        self.V = np.ascontiguousarray(V, np.int32)
+        self.F = np.ascontiguousarray(F, np.int32)
+        self.B = np.ascontiguousarray(B, np.int32)
+        h = C.c_void_p()
+        _capi.check_ccd(_capi.lib().pbgb_ccd_create(nV, self.V.size, self.V.ctypes.data, self.F.shape[0],
+                                                    self.F.ctypes.data, self.B.ctypes.data, C.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        _capi.lib().pbgb_ccd_destroy(self.h)
+
+    def call(self, name, *arrays):
+        arrays = [np.ascontiguousarray(a, np.float32) for a in arrays]
+        _capi.check_ccd(getattr(_capi.lib(), name)(self.h, *[a.ctypes.data for a in arrays]), self.h)
+
+    def get(self):
+        n = self.V.size
+        active = np.zeros(n, np.uint8)
+        nn = np.zeros(8 * n, np.int32)
+        dup = np.zeros(n, np.float32)
+        na = C.c_int32()
+        _capi.check_ccd(_capi.lib().pbgb_ccd_get(self.h, active.ctypes.data, nn.ctypes.data, dup.ctypes.data,
+                                                 C.byref(na)), self.h)
+        return active, nn.reshape(n, 8), dup, na.value
+
+
+def test_two_tets_active_set_reference_scenario():
+    """gpu/impl/contact/VertexTriangleMixedCcdDcd.cu:232-328: the bottom tet's top vertex passes
+    through the top tet's bottom face."""
+    XT = np.array([[0, 1, 0, 0.1, 0, 1, 0, 0.1],
+                   [0, 0, 1, 0.1, 0, 0, 1, 0.1],
+                   [0, 0, 0, 1, 1.01, 1.01, 1.01, 2.01]], np.float32)
+    F = np.array([[0, 1, 2, 0, 4, 5, 6, 4], [1, 2, 0, 2, 5, 6, 4, 6], [3, 3, 3, 1, 7, 7, 7, 5]]).T
+    V = np.arange(8)
+    B = np.array([0, 0, 0, 0, 1, 1, 1, 1])
+    X = XT.copy()
+    X[2, :4] += 0.01
+    X[2, 4:] -= 0.01
+    c = Ccd(8, V, F, B)
+    c.call("pbgb_ccd_initialize", XT.T, X.T, np.array([0, 0, 0]), np.array([1, 1, 2.01]))
+    active, nn, dup, na = c.get()
+    assert na == 4
+    assert active.sum() == 4
+    assert active[3] == 1
+    c.call("pbgb_ccd_update", X.T)
+    active, nn, dup, na = c.get()
+    for v in range(8):
+        assert (nn[v] >= 0).any() == bool(active[v])
+    c.call("pbgb_ccd_finalize", X.T)
+
+
+def small_scene():
+    return meshgen.contact_scene_workload(n_cubes_side=2, cube_hexes=3, slab_hexes=(8, 8, 1), gap=0.01)
+
+
+def contact_data(w, muC=1e7, strategy=2):
+    return (pbat.sim.vbd.Data().with_volume_mesh(w["X"].T, w["T"].T).with_surface_mesh(w["V"], w["F"].T)
+            .with_bodies(w["B"]).with_material(w["rho"], w["mu"], w["lam"]).with_dirichlet_vertices(w["dbc"])
+            .with_contact_parameters(muC, 0.3, 1e-3).with_initialization_strategy(strategy).construct())
+
+
+def test_contact_steps_match_oracle():
+    w = small_scene()
+    I = pbat.gpu.vbd.Integrator(contact_data(w))
+    R = O.OracleContactVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], w["V"], w["F"], w["B"],
+                           muC=1e7, strategy=2)
+    diag = np.linalg.norm(w["X"].max(0) - w["X"].min(0))
+    errs = []
+    for _ in range(20):
+        I.step(1 / 60, 20, 1)
+        R.step(1 / 60, 20, 1, 1)
+        errs.append(np.abs(I.x.T - R.x).max() / diag)
+    fc, active = I.contacts()
+    assert active.sum() > 0
+    assert max(errs) <= 1e-4, errs
+    # Same active collision vertices as the oracle.
+    np.testing.assert_array_equal(active.astype(bool), R.active.astype(bool))
+
+
+def test_contact_scene_of_sixteen_cubes_runs():
+    """16 cubes of 16^3 hexes on a 64x64x2 slab (91,283 vertices, 66,560 surface triangles)."""
+    w = meshgen.contact_scene_workload()
+    I = pbat.gpu.vbd.Integrator(contact_data(w))
+    z0 = w["X"][w["B"] > 0, 2].min()
+    for _ in range(8):
+        I.step(1 / 60, 30, 1)
+    x = I.x.T
+    assert np.isfinite(x).all()
+    zc = x[w["B"] > 0, 2]
+    assert zc.min() < z0 and zc.min() > -0.02
+    fc, active = I.contacts()
+    assert active.sum() > 100
+    assert (fc >= 0).any()
