@@ -5,9 +5,16 @@
 //                       per substep: inertial target, initial guess, contact list, sweeps,
 //                       velocity; finalise at the end), GPU velocity semantics
 //   active set          gpu/impl/contact/VertexTriangleMixedCcdDcd.cu:51-223, with brute-force
-//                       overlaps and nearest triangles instead of the BVH (the same sets: every
-//                       box pair is tested); the search radius of a vertex overlapping several
-//                       triangles is the largest joint-box diagonal
+//                       overlaps instead of the BVH (the same sets: every box pair is tested); the
+//                       search radius of a vertex overlapping several triangles is the largest
+//                       joint-box diagonal
+//   nearest triangles   gpu/impl/geometry/Bvh.cuh:347-474: the branch and bound visits the leaves
+//                       of the LBVH in descending Morton order (the right child is popped first)
+//                       and keeps a FIFO list that restarts on a strictly nearer triangle.  Pruning
+//                       never drops a triangle within the current radius, so visiting every
+//                       triangle in that leaf order gives the same list; the order is taken from
+//                       FP32 Morton codes of the swept triangle boxes at each step's initialise,
+//                       stably sorted (the LBVH restatement in lbvh_oracle.cpp)
 //   contact energy      gpu/impl/vbd/Kernels.cuh:80-114,203-223 and sim/vbd/Kernels.h:215-302
 //   colour pass reads   the reference writes every vertex of a colour to a buffer and copies it
 //                       back after the pass, so a contact triangle's corners are read as they were
@@ -181,6 +188,7 @@ struct orc_contact
     double const* FA;
     double muC, muF, epsv;
     int32_t freq;
+    float wmin[3], wmax[3]; // scene box the Morton codes are normalised by
     // persistent state (caller-owned)
     uint8_t* active;  // nSurfV
     double* dupper;   // nSurfV
@@ -189,28 +197,55 @@ struct orc_contact
 
 namespace {
 
-void nearest(orc_contact const& C, Real const* x, int32_t q, std::vector<int32_t>& list)
+// Nearest triangles of collision vertex q (gpu/impl/geometry/Bvh.cuh:408-466 with the callbacks of
+// gpu/impl/contact/VertexTriangleMixedCcdDcd.cuh:109-162).  order: triangles in the order the
+// depth-first traversal reaches their leaves.  Triangles of the vertex's own body are skipped.
+void nearest(orc_contact const& C, Real const* x, int32_t q, std::vector<int32_t> const& order, std::vector<int32_t>& list)
 {
     int32_t const i = C.V[q];
     V3 const p      = at(x, i);
+    Real const eps  = Real(FLT_EPSILON);
+    Real dmin       = C.dupper[q];
     list.clear();
-    Real dmin = std::numeric_limits<Real>::max();
-    std::vector<std::pair<Real, int32_t>> d;
-    d.reserve(64);
-    for (int32_t f = 0; f < C.nF; ++f)
+    for (int32_t f : order)
     {
         int32_t const* t = C.F + 3 * size_t(f);
         if (C.B[t[0]] == C.B[i])
             continue;
-        Real const dd = point_triangle_sqdist(p, at(x, t[0]), at(x, t[1]), at(x, t[2]));
-        d.push_back({dd, f});
-        dmin = std::min(dmin, dd);
-    }
-    if (dmin > C.dupper[q] + Real(FLT_EPSILON))
-        return; // outside the search radius: the branch and bound finds nothing
-    for (auto const& [dd, f] : d)
-        if (dd <= dmin + Real(FLT_EPSILON) && list.size() < 8)
+        Real const d = point_triangle_sqdist(p, at(x, t[0]), at(x, t[1]), at(x, t[2]));
+        if (d < dmin - eps)
+        {
+            list.assign(1, f);
+            dmin = d;
+        }
+        else if (d <= dmin + eps && list.size() < 8)
             list.push_back(f);
+    }
+}
+
+// Leaf order of the LBVH over the FP32 swept triangle boxes, reversed: the depth-first visit order.
+extern "C" void orc_morton(int32_t n, float const* lo, float const* hi, float const* wmin, float const* wmax, uint32_t* codes);
+
+void visit_order(orc_contact const& C, std::vector<V3> const& flo, std::vector<V3> const& fhi, std::vector<int32_t>& order)
+{
+    size_t const n = size_t(C.nF);
+    std::vector<float> lo(3 * n), hi(3 * n);
+    for (size_t f = 0; f < n; ++f)
+    {
+        lo[3 * f + 0] = float(flo[f].x);
+        lo[3 * f + 1] = float(flo[f].y);
+        lo[3 * f + 2] = float(flo[f].z);
+        hi[3 * f + 0] = float(fhi[f].x);
+        hi[3 * f + 1] = float(fhi[f].y);
+        hi[3 * f + 2] = float(fhi[f].z);
+    }
+    std::vector<uint32_t> codes(n);
+    orc_morton(C.nF, lo.data(), hi.data(), C.wmin, C.wmax, codes.data());
+    order.resize(n);
+    for (size_t f = 0; f < n; ++f)
+        order[f] = int32_t(f);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return codes[a] < codes[b]; });
+    std::reverse(order.begin(), order.end());
 }
 
 } // namespace
@@ -224,7 +259,7 @@ int orc_run_contact(orc_problem const* Pp, orc_contact const* Cp, double* x, dou
     size_t const n3      = size_t(nV) * 3;
     std::vector<Real> xt(n3), xtilde(n3), xpred(n3), snap(n3), vtm1(n3);
     Real const sdt = dt / Real(substeps), sdt2 = sdt * sdt;
-    std::vector<int32_t> list;
+    std::vector<int32_t> list, order;
     for (int32_t step = 0; step < nsteps; ++step)
     {
         // InitializeActiveSet on the full-step prediction.
@@ -245,6 +280,7 @@ int orc_run_contact(orc_problem const* Pp, orc_contact const* Cp, double* x, dou
             flo[f] = lo;
             fhi[f] = hi;
         }
+        visit_order(C, flo, fhi, order);
 #pragma omp parallel for schedule(dynamic, 16)
         for (int32_t q = 0; q < C.nSurfV; ++q)
         {
@@ -338,7 +374,7 @@ int orc_run_contact(orc_problem const* Pp, orc_contact const* Cp, double* x, dou
                 {
                     if (!C.active[q])
                         continue;
-                    nearest(C, x, q, list);
+                    nearest(C, x, q, order, list);
                     int32_t const i = C.V[q];
                     for (int c = 0; c < 8; ++c)
                         C.fc[8 * size_t(i) + c] = c < int(list.size()) ? list[c] : -1;
@@ -419,7 +455,7 @@ int orc_run_contact(orc_problem const* Pp, orc_contact const* Cp, double* x, dou
         {
             if (!C.active[q])
                 continue;
-            nearest(C, x, q, list);
+            nearest(C, x, q, order, list);
             if (list.empty())
                 continue;
             int32_t const* t = C.F + 3 * size_t(list.back());

@@ -252,8 +252,8 @@ class OrcContact(C.Structure):
     _fields_ = [
         ("nSurfV", C.c_int32), ("V", C.c_void_p), ("nF", C.c_int32), ("F", C.c_void_p), ("B", C.c_void_p),
         ("XVA", C.c_void_p), ("FA", C.c_void_p), ("muC", C.c_double), ("muF", C.c_double),
-        ("epsv", C.c_double), ("freq", C.c_int32), ("active", C.c_void_p), ("dupper", C.c_void_p),
-        ("fc", C.c_void_p),
+        ("epsv", C.c_double), ("freq", C.c_int32), ("wmin", C.c_float * 3), ("wmax", C.c_float * 3),
+        ("active", C.c_void_p), ("dupper", C.c_void_p), ("fc", C.c_void_p),
     ]
 
 
@@ -283,6 +283,9 @@ class OracleContactVbd(OracleVbd):
         Cc.XVA, Cc.FA = self.XVA.ctypes.data, self.FA.ctypes.data
         Cc.muC, Cc.muF, Cc.epsv, Cc.freq = muC, muF, epsv, freq
         Cc.active, Cc.dupper, Cc.fc = self.active.ctypes.data, self.dupper.ctypes.data, self.fc.ctypes.data
+        # Scene box of the Morton codes: the rest-state bounding box, as on the device by default.
+        Cc.wmin[:] = [float(c) for c in X.min(axis=0).astype(np.float32)]
+        Cc.wmax[:] = [float(c) for c in X.max(axis=0).astype(np.float32)]
         self.C = Cc
 
     def step(self, dt, iterations, substeps=1, nsteps=1, use_ref=False):
