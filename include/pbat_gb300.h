@@ -172,6 +172,11 @@ PBGB_API int pbgb_vbd_set_external_acceleration(pbgb_vbd* h, const float* aext);
 /* Device-pointer variants (3 x nV float32 on the handle's device), stream-ordered. */
 PBGB_API int pbgb_vbd_get_positions_device(pbgb_vbd* h, float* x_dev);
 PBGB_API int pbgb_vbd_set_positions_device(pbgb_vbd* h, const float* x_dev);
+PBGB_API int pbgb_vbd_get_velocities_device(pbgb_vbd* h, float* v_dev);
+PBGB_API int pbgb_vbd_set_velocities_device(pbgb_vbd* h, const float* v_dev);
+/* Per-tet Lame coefficients (host, nT each, system order), as Data::WithMaterial sets them
+ * (sim/vbd/Data.cpp:60-75); masses and quadrature weights are kept.  Synchronizes. */
+PBGB_API int pbgb_vbd_set_material(pbgb_vbd* h, const double* mu, const double* lambda);
 
 /* Knobs (gpu/vbd/Integrator.h:110-134). */
 PBGB_API int pbgb_vbd_set_detH_zero(pbgb_vbd* h, float zero);
@@ -240,6 +245,42 @@ PBGB_API int pbgb_vbd_gradient(pbgb_vbd* h, double dt, double* grad /* 3 x nV */
 PBGB_API int pbgb_vbd_gradient_noalloc(pbgb_vbd* h, double dt, double* grad /* 3 x nV */);
 
 /*
+ * Adjoint of the step (no counterpart in the reference, which has no differentiation).  The
+ * adjoint is the exact derivative of the computed iterations: each colour sweep is reversed by the
+ * same coloured block sweep on the transposed system (colours in reverse order), with the
+ * curvature terms of the Stable Neo-Hookean energy that make it exact for the nonlinear update.
+ * When the forward iterations converge it becomes the adjoint of the converged step,
+ * (M/h^2 + d2E/dx2) lambda = dL/dx.
+ *
+ * Supported forward settings: no acceleration, kD = 0, no contact, initial guess Position, Inertia
+ * or KineticEnergyMinimum; other settings return PBGB_ERR_INVALID_ARGUMENT.
+ *
+ *   pbgb_vbd_adjoint_reserve: device tape for `slots` recorded substeps of `iterations` iterations:
+ *     (iterations + 1) x nV iterates and iterations x n_free inverse 3x3 Newton matrices per slot
+ *     (16 (iterations + 1) nV + 32 iterations n_free bytes).
+ *   pbgb_vbd_step_record: one pbgb_vbd_step(dt, iterations, substeps) (the same positions) that
+ *     records substep s into slot `slot` + s.  Launched directly, not from the step's graph.
+ *   pbgb_vbd_step_adjoint: reverses the substeps in slots slot + substeps - 1 down to slot.
+ *     xbar_dev, vbar_dev (device, 3 x nV): on entry the adjoints dL/dx, dL/dv of the state after
+ *     the recorded step, on return those of the state before it.  dlogmu_dev, dloglambda_dev
+ *     (device, nT, FP64): dL/dlog(mu), dL/dlog(lambda) of every tet, added to what they hold
+ *     (with a fixed Poisson ratio, dL/dlog(E) is their sum).  Each is a sum over every iteration
+ *     of terms that largely cancel, so it is accumulated in FP64; the terms are FP32.
+ * All three are asynchronous on the handle's stream; the tape is overwritten by the next record
+ * into the same slot.
+ */
+PBGB_API int pbgb_vbd_adjoint_reserve(pbgb_vbd* h, int32_t slots, int32_t iterations);
+PBGB_API int pbgb_vbd_step_record(pbgb_vbd* h, float dt, int32_t iterations, int32_t substeps, int32_t slot);
+PBGB_API int pbgb_vbd_step_adjoint(
+    pbgb_vbd* h,
+    int32_t slot,
+    int32_t substeps,
+    float* xbar_dev,
+    float* vbar_dev,
+    double* dlogmu_dev,
+    double* dloglambda_dev);
+
+/*
  * Linear BVH over axis-aligned boxes (reference: gpu::geometry::Bvh, gpu/geometry/Bvh.cu, and its
  * implementation gpu/impl/geometry/Bvh.cu:24-229, Bvh.cuh:205-588, Morton.cu:23-44).
  * Boxes are host arrays, 3 x n (box i at [3i, 3i+2]).  Node numbering as in the reference:
@@ -298,6 +339,24 @@ PBGB_API const char* pbgb_ccd_last_error(pbgb_ccd* c);
 
 /* Message of the last failing call on h (or of the last failing handle-less call if h is NULL). */
 PBGB_API const char* pbgb_last_error(pbgb_vbd* h);
+
+/* Host self-check of the per-tet adjoint term of the device's adjoint sweep (adjoint_tet): for one
+ * tet with solved corner o, xe (4 x 3 current positions, row a = corner a), Xe (4 x 3 rest
+ * positions), il = o's local index, w and delta (3 each), muw = wg mu, law = wg lambda, writes
+ * dphi (4 x 3, row a = d(phi_e)/d(x_a), o's row included) and d(phi_e)/dlog(mu),
+ * d(phi_e)/dlog(lambda).  precision 64 evaluates in double, 32 in float like the device. */
+PBGB_API int pbgb_debug_adjoint_tet(
+    int32_t precision,
+    const double* xe,
+    const double* Xe,
+    int32_t il,
+    const double* w,
+    const double* delta,
+    double muw,
+    double law,
+    double* dphi,
+    double* dlogmu,
+    double* dloglambda);
 
 /* Host self-check of the closed-form vertex block (FP64): accumulates n incident tets and
  * applies damping, inertia and the Newton step exactly like the device sweep.  Arguments as the

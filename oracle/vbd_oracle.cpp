@@ -410,8 +410,9 @@ void orc_initial_positions(
 
 // Accumulate the elastic gradient and 3x3 Hessian of vertex i (sim/vbd/Integrator.cpp:102-121,
 // sim/vbd/Kernels.h:131-171), then damping, inertia and the Newton step (Kernels.h:179-191,
-// 310-339).  x is updated in place.
-static void solve_vertex(orc_problem const& P, int32_t i, Real const* xt, Real const* xtilde, Real* x, Real sdt, Real sdt2)
+// 310-339).  x is updated in place.  HinvOut (optional): the inverse of the 3x3 Newton matrix,
+// zero when the step is skipped.
+static void solve_vertex(orc_problem const& P, int32_t i, Real const* xt, Real const* xtilde, Real* x, Real sdt, Real sdt2, Real* HinvOut = nullptr)
 {
     Real H[9] = {0}, g[3] = {0};
     for (int32_t n = P.GVGp[i]; n < P.GVGp[i + 1]; ++n)
@@ -465,9 +466,15 @@ static void solve_vertex(orc_problem const& P, int32_t i, Real const* xt, Real c
     }
     // IntegratePositions (Kernels.h:329-339)
     if (std::abs(det3(H)) <= P.detHZero)
+    {
+        if (HinvOut)
+            std::fill(HinvOut, HinvOut + 9, Real(0));
         return;
+    }
     Real Hi[9];
     inv3(H, Hi);
+    if (HinvOut)
+        std::copy(Hi, Hi + 9, HinvOut);
     for (int r = 0; r < 3; ++r)
     {
         Real dx = 0;
@@ -706,6 +713,232 @@ void orc_vertex_solve(
             dx += Hi[3 * c + r] * gd[c];
         xi[r] -= dx;
     }
+}
+
+// ---- Adjoint (no reference counterpart) ----------------------------------------------------
+//
+// Reverse-mode derivative of orc_run for strategies Position, Inertia and KineticEnergyMinimum,
+// without acceleration or damping.  Every vertex update x_o' = x_o - H^-1 g (g, H at the state
+// before the update) is reversed with w = H^-1 u (u: adjoint of x_o') and the applied step
+// delta = x_o - x_o': the adjoints of the inputs are u e_o - grad phi with phi = w.(g - H delta),
+// w and delta held fixed.  Per tet, grad_F phi_e = wg [d2Psi:A - lambda ((cof:B) D_A + (cof:A) D_B)]
+// with A = w g_o^T, B = delta g_o^T, d2Psi the 9x9 Stable Neo-Hookean Hessian above and
+// D_A = d(cof F : A)/dF = J (tr(F^-1 A) F^-T - (F^-1 A F^-1)^T).  Sweeps are reversed colour by
+// colour; the state each update saw is rebuilt from the iterates recorded per iteration.
+//
+// x0, v0: the start state (nV x 3); xbar, vbar (nV x 3): on entry dL/dx, dL/dv of the state after
+// nsteps, on return of the start state.  dlogmu, dloglambda (nT): dL/dlog(mu), dL/dlog(lambda)
+// added to.  Returns 0, or 2 for unsupported settings.
+int orc_adjoint(
+    orc_problem const* Pp,
+    double const* x0,
+    double const* v0,
+    double dt,
+    int32_t iterations,
+    int32_t substeps,
+    int32_t nsteps,
+    double* xbar,
+    double* vbar,
+    double* dlogmu,
+    double* dloglambda)
+{
+    orc_problem const& P = *Pp;
+    if (P.acceleration != 0 || P.kD != 0.0 || P.strategy > 2 || substeps < 1 || iterations < 0 || nsteps < 0)
+        return 2;
+    int32_t const nV = P.nV;
+    size_t const n3  = size_t(nV) * 3;
+    int32_t const N  = nsteps * substeps;
+    Real const h = dt / Real(substeps), h2 = h * h;
+    int32_t const K = iterations;
+    // Colour of every vertex (-1: pinned, never solved).
+    std::vector<int32_t> colour(size_t(nV), -1);
+    for (int32_t p = 0; p < P.nPartitions; ++p)
+        for (int32_t kk = P.Pptr[p]; kk < P.Pptr[p + 1]; ++kk)
+            colour[P.Padj[kk]] = p;
+    // Forward: the state at the start of every substep.
+    std::vector<Real> xs(size_t(N + 1) * n3), vs(size_t(N + 1) * n3);
+    std::copy(x0, x0 + n3, xs.begin());
+    std::copy(v0, v0 + n3, vs.begin());
+    std::vector<Real> xt(n3), xtilde(n3), snaps(size_t(K + 1) * n3), hinv(size_t(K) * size_t(nV) * 9);
+    auto substep = [&](int32_t t, bool record) {
+        Real const* xa = xs.data() + size_t(t) * n3;
+        Real const* va = vs.data() + size_t(t) * n3;
+        std::vector<Real> x(xa, xa + n3);
+        std::copy(xa, xa + n3, xt.begin());
+        for (int32_t i = 0; i < nV; ++i)
+        {
+            for (int d = 0; d < 3; ++d)
+                xtilde[3 * i + d] = xt[3 * i + d] + h * va[3 * i + d] + h2 * P.aext[3 * i + d];
+            initial_positions(&xt[3 * size_t(i)], va + 3 * size_t(i), va + 3 * size_t(i), P.aext + 3 * size_t(i), h, h2, P.strategy, &x[3 * size_t(i)]);
+        }
+        if (record)
+            std::copy(x.begin(), x.end(), snaps.begin());
+        for (int32_t k = 0; k < K; ++k)
+        {
+            for (int32_t p = 0; p < P.nPartitions; ++p)
+            {
+#pragma omp parallel for schedule(dynamic, 64)
+                for (int32_t kk = P.Pptr[p]; kk < P.Pptr[p + 1]; ++kk)
+                {
+                    int32_t const i = P.Padj[kk];
+                    solve_vertex(P, i, xt.data(), xtilde.data(), x.data(), h, h2,
+                                 record ? &hinv[(size_t(k) * nV + i) * 9] : nullptr);
+                }
+            }
+            if (record)
+                std::copy(x.begin(), x.end(), snaps.begin() + size_t(k + 1) * n3);
+        }
+        if (!record)
+        {
+            Real* xn = xs.data() + size_t(t + 1) * n3;
+            Real* vn = vs.data() + size_t(t + 1) * n3;
+            for (size_t q = 0; q < n3; ++q)
+            {
+                xn[q] = x[q];
+                vn[q] = (x[q] - xt[q]) / h;
+            }
+        }
+    };
+    for (int32_t t = 0; t < N; ++t)
+        substep(t, false);
+    // Reverse.
+    std::vector<Real> ubar(n3), xtbar(n3);
+    Real const s1 = P.strategy == 0 ? Real(0) : Real(1);
+    for (int32_t t = N - 1; t >= 0; --t)
+    {
+        substep(t, true);
+        for (size_t q = 0; q < n3; ++q)
+        {
+            ubar[q]  = xbar[q] + vbar[q] / h;
+            xtbar[q] = 0;
+        }
+        for (int32_t k = K; k >= 1; --k)
+        {
+            Real const* Xk   = snaps.data() + size_t(k) * n3;
+            Real const* Xkm1 = snaps.data() + size_t(k - 1) * n3;
+            for (int32_t p = P.nPartitions - 1; p >= 0; --p)
+            {
+#pragma omp parallel for schedule(dynamic, 32)
+                for (int32_t kk = P.Pptr[p]; kk < P.Pptr[p + 1]; ++kk)
+                {
+                    int32_t const o = P.Padj[kk];
+                    Real const* Hi  = &hinv[(size_t(k - 1) * nV + o) * 9];
+                    Real w[3], delta[3];
+                    for (int r = 0; r < 3; ++r)
+                    {
+                        w[r]     = Hi[r] * ubar[3 * o] + Hi[3 + r] * ubar[3 * o + 1] + Hi[6 + r] * ubar[3 * o + 2];
+                        delta[r] = Xkm1[3 * o + r] - Xk[3 * o + r];
+                    }
+                    Real own[3] = {0, 0, 0};
+                    for (int32_t n = P.GVGp[o]; n < P.GVGp[o + 1]; ++n)
+                    {
+                        int32_t const e   = P.GVGe[n];
+                        int32_t const il  = P.GVGilocal[n];
+                        int32_t const* tv = P.T + 4 * e;
+                        double const* GPe = P.GP + 12 * e;
+                        Real F[9] = {0};
+                        for (int a = 0; a < 4; ++a)
+                        {
+                            int32_t const va = tv[a];
+                            Real const* src  = (a == il) ? Xkm1 : (colour[va] < p ? Xk : Xkm1);
+                            for (int d = 0; d < 3; ++d)
+                                for (int r = 0; r < 3; ++r)
+                                    F[3 * d + r] += src[3 * va + r] * GPe[3 * a + d];
+                        }
+                        Real const mu = P.mu[e], la = P.lambda[e], wg = P.wg[e];
+                        Real gF[9], HF[81];
+                        snh_grad_hessian(F, mu, la, gF, HF);
+                        Real const* go = GPe + 3 * il;
+                        Real A[9], B[9];
+                        for (int c = 0; c < 3; ++c)
+                            for (int r = 0; r < 3; ++r)
+                            {
+                                A[3 * c + r] = go[c] * w[r];
+                                B[3 * c + r] = go[c] * delta[r];
+                            }
+                        Real C[9];
+                        cofactor(F, C);
+                        Real const J = det3(F);
+                        Real cA = 0, cB = 0, FA = 0;
+                        for (int q = 0; q < 9; ++q)
+                        {
+                            cA += C[q] * A[q];
+                            cB += C[q] * B[q];
+                            FA += F[q] * A[q];
+                        }
+                        Real Fi[9];
+                        inv3(F, Fi);
+                        // D_X = J (tr(F^-1 X) F^-T - (F^-1 X F^-1)^T)
+                        auto dJ2 = [&](Real const* Xm, Real* D) {
+                            Real FX[9] = {0}, FXF[9] = {0};
+                            for (int c = 0; c < 3; ++c)
+                                for (int r = 0; r < 3; ++r)
+                                    for (int q = 0; q < 3; ++q)
+                                        FX[3 * c + r] += Fi[3 * q + r] * Xm[3 * c + q];
+                            for (int c = 0; c < 3; ++c)
+                                for (int r = 0; r < 3; ++r)
+                                    for (int q = 0; q < 3; ++q)
+                                        FXF[3 * c + r] += FX[3 * q + r] * Fi[3 * c + q];
+                            Real const tr = FX[0] + FX[4] + FX[8];
+                            for (int c = 0; c < 3; ++c)
+                                for (int r = 0; r < 3; ++r)
+                                    D[3 * c + r] = J * (tr * Fi[3 * r + c] - FXF[3 * r + c]);
+                        };
+                        Real DA[9], DB[9];
+                        dJ2(A, DA);
+                        dJ2(B, DB);
+                        Real M[9];
+                        for (int i9 = 0; i9 < 9; ++i9)
+                        {
+                            Real HA = 0;
+                            for (int j9 = 0; j9 < 9; ++j9)
+                                HA += HF[i9 * 9 + j9] * A[j9];
+                            M[i9] = wg * (HA - la * (cB * DA[i9] + cA * DB[i9]));
+                        }
+                        Real wd = 0, gg = 0;
+                        for (int r = 0; r < 3; ++r)
+                        {
+                            wd += w[r] * delta[r];
+                            gg += go[r] * go[r];
+                        }
+                        dlogmu[e] -= wg * mu * (FA - cA - gg * wd);
+                        dloglambda[e] -= wg * la * ((J - 1) * cA - cA * cB);
+                        for (int a = 0; a < 4; ++a)
+                        {
+                            Real gphi[3];
+                            for (int r = 0; r < 3; ++r)
+                                gphi[r] = M[r] * GPe[3 * a] + M[3 + r] * GPe[3 * a + 1] + M[6 + r] * GPe[3 * a + 2];
+                            if (a == il)
+                            {
+                                for (int r = 0; r < 3; ++r)
+                                    own[r] += gphi[r];
+                                continue;
+                            }
+                            int32_t const va = tv[a];
+                            for (int r = 0; r < 3; ++r)
+                            {
+#pragma omp atomic
+                                ubar[3 * va + r] -= gphi[r];
+                            }
+                        }
+                    }
+                    Real const Km = P.m[o] / h2;
+                    for (int r = 0; r < 3; ++r)
+                    {
+                        ubar[3 * o + r] -= Km * w[r] + own[r];
+                        xtbar[3 * o + r] += Km * w[r];
+                    }
+                }
+            }
+        }
+        for (size_t q = 0; q < n3; ++q)
+        {
+            Real const vb = vbar[q];
+            xbar[q]       = -vb / h + ubar[q] + xtbar[q];
+            vbar[q]       = s1 * h * ubar[q] + h * xtbar[q];
+        }
+    }
+    return 0;
 }
 
 int32_t orc_num_threads()

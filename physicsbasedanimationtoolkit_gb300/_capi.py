@@ -98,6 +98,12 @@ _SIGNATURES = [
     ("pbgb_vbd_set_external_acceleration", C.c_int, [_vp, _vp]),
     ("pbgb_vbd_get_positions_device", C.c_int, [_vp, _vp]),
     ("pbgb_vbd_set_positions_device", C.c_int, [_vp, _vp]),
+    ("pbgb_vbd_get_velocities_device", C.c_int, [_vp, _vp]),
+    ("pbgb_vbd_set_velocities_device", C.c_int, [_vp, _vp]),
+    ("pbgb_vbd_set_material", C.c_int, [_vp, _vp, _vp]),
+    ("pbgb_vbd_adjoint_reserve", C.c_int, [_vp, _i32, _i32]),
+    ("pbgb_vbd_step_record", C.c_int, [_vp, _f32, _i32, _i32, _i32]),
+    ("pbgb_vbd_step_adjoint", C.c_int, [_vp, _i32, _i32, _vp, _vp, _vp, _vp]),
     ("pbgb_vbd_set_detH_zero", C.c_int, [_vp, _f32]),
     ("pbgb_vbd_set_damping", C.c_int, [_vp, _f32]),
     ("pbgb_vbd_set_strategy", C.c_int, [_vp, _i32]),
@@ -116,6 +122,7 @@ _SIGNATURES = [
     ("pbgb_vbd_gradient", C.c_int, [_vp, _f64, _vp]),
     ("pbgb_vbd_gradient_noalloc", C.c_int, [_vp, _f64, _vp]),
     ("pbgb_last_error", C.c_char_p, [_vp]),
+    ("pbgb_debug_adjoint_tet", C.c_int, [_i32, _vp, _vp, _i32, _vp, _vp, _f64, _f64, _vp, _vp, _vp]),
     ("pbgb_bvh_create", C.c_int, [_i32, C.POINTER(_vp)]),
     ("pbgb_bvh_destroy", C.c_int, [_vp]),
     ("pbgb_bvh_build", C.c_int, [_vp, _i32, _vp, _vp, _vp, _vp]),

@@ -186,6 +186,36 @@ class IntegratorBase:
         _capi.check(_capi.lib().pbgb_vbd_get_contacts(self._h, fc.ctypes.data, active.ctypes.data), self._h)
         return fc, active[:nS]
 
+    def set_material(self, mu, lam):
+        """Per-tet Lame coefficients (|#tets| each, system order); masses are kept."""
+        mu = np.ascontiguousarray(mu, dtype=np.float64).ravel()
+        lam = np.ascontiguousarray(lam, dtype=np.float64).ravel()
+        if mu.size != self.n_tets or lam.size != self.n_tets:
+            raise ValueError(f"expected {self.n_tets} Lame coefficients")
+        _capi.check(_capi.lib().pbgb_vbd_set_material(self._h, mu.ctypes.data, lam.ctypes.data), self._h)
+
+    # Device-pointer state access (|#vertices| x 3 float32 on the handle's device).  Stream-ordered
+    # on the handle's stream: callers order their own work around them (synchronize()).
+    def _get_device(self, which, ptr):
+        fn = {"x": "pbgb_vbd_get_positions_device", "v": "pbgb_vbd_get_velocities_device"}[which]
+        _capi.check(getattr(_capi.lib(), fn)(self._h, C.c_void_p(ptr)), self._h)
+
+    def _set_device(self, which, ptr):
+        fn = {"x": "pbgb_vbd_set_positions_device", "v": "pbgb_vbd_set_velocities_device"}[which]
+        _capi.check(getattr(_capi.lib(), fn)(self._h, C.c_void_p(ptr)), self._h)
+
+    def adjoint_reserve(self, slots, iterations):
+        _capi.check(_capi.lib().pbgb_vbd_adjoint_reserve(self._h, int(slots), int(iterations)), self._h)
+
+    def step_record(self, dt, iterations, substeps, slot):
+        _capi.check(_capi.lib().pbgb_vbd_step_record(self._h, float(dt), int(iterations), int(substeps), int(slot)),
+                    self._h)
+
+    def step_adjoint(self, slot, substeps, xbar_ptr, vbar_ptr, dlogmu_ptr, dloglambda_ptr):
+        _capi.check(_capi.lib().pbgb_vbd_step_adjoint(self._h, int(slot), int(substeps), C.c_void_p(xbar_ptr),
+                                                     C.c_void_p(vbar_ptr), C.c_void_p(dlogmu_ptr),
+                                                     C.c_void_p(dloglambda_ptr)), self._h)
+
     def objective(self, dt):
         """Backward-Euler objective at the current positions (FP64 device reduction)."""
         f = C.c_double()

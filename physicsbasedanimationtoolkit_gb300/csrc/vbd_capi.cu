@@ -6,6 +6,7 @@
 // one stream per handle (the reference creates one and never uses it), the whole step replayed
 // from a CUDA graph, tets packed into 64-byte records, the in-place colour sweep (no xb copy-back
 // pass), and several meshes concatenated into one system for the batched form.
+#include "adjoint.cuh"
 #include "contact.cuh"
 #include "pbat_gb300.h"
 #include "vbd_construct.h"
@@ -124,6 +125,22 @@ class VbdSystem
     DeviceArray<float4> cTlo, cThi, cVlo, cVhi, xpred;
     DeviceArray<uint8_t> cActive;
 
+    // Host copies of the tet records and quadrature weights (pbgb_vbd_set_material rewrites the
+    // material words).
+    std::vector<TetRecord> hostRecords;
+    std::vector<double> hostWg;
+
+    // Adjoint tape (pbgb_vbd_adjoint_reserve): one slot per recorded substep, holding the iterates
+    // X_0..X_K (nV float4 each) and K x nFree inverse Newton matrices (2 float4 each).
+    int32_t tapeSlots = 0, tapeIters = 0;
+    std::vector<float> slotH;
+    std::vector<int32_t> slotStrategy;
+    DeviceArray<float4> tapeX, tapeH, ubar, xtbar;
+    // Reversed steps run on these (the caller's arrays are copied in and out), so that their graphs
+    // do not depend on the caller's pointers.
+    DeviceArray<float> adjX, adjV;
+    DeviceArray<double> adjMu, adjLa;
+
     // Graph cache for Step(dt, iterations, substeps)
     cudaGraphExec_t graph = nullptr;
     float gDt = -1.f;
@@ -136,13 +153,65 @@ class VbdSystem
             cudaStreamSynchronize(stream);
         bvh_release(cstate.bvh);
         releaseEvents();
+        dropSlotGraphs();
         if (graph)
             cudaGraphExecDestroy(graph);
         if (stream)
             cudaStreamDestroy(stream);
     }
 
-    void invalidate() { graphValid = false; }
+    void invalidate()
+    {
+        graphValid = false;
+        dropSlotGraphs();
+    }
+
+    // Graphs of recorded and reversed steps, one per first slot (captured on first use).
+    struct SlotGraph
+    {
+        cudaGraphExec_t exec = nullptr;
+        float dt             = 0.f;
+        int32_t iters = -1, sub = -1;
+        std::vector<float> h; // reversed steps: the step size of every covered slot
+        std::vector<int32_t> strategy;
+    };
+    std::vector<SlotGraph> recGraphs, adjGraphs;
+
+    void dropSlotGraphs()
+    {
+        for (auto* v : {&recGraphs, &adjGraphs})
+        {
+            for (auto& g : *v)
+                if (g.exec)
+                    cudaGraphExecDestroy(g.exec);
+            v->clear();
+        }
+    }
+
+    // Captures what `enqueue` puts on the stream into an executable graph.
+    template <class F>
+    cudaGraphExec_t capture(F&& enqueue)
+    {
+        cudaGraph_t g = nullptr;
+        check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+        try
+        {
+            enqueue();
+        }
+        catch (...)
+        {
+            cudaStreamEndCapture(stream, &g);
+            if (g)
+                cudaGraphDestroy(g);
+            throw;
+        }
+        check(cudaStreamEndCapture(stream, &g), "cudaStreamEndCapture");
+        cudaGraphExec_t exec = nullptr;
+        cudaError_t const e  = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        check(e, "cudaGraphInstantiate");
+        return exec;
+    }
 
     void releaseEvents()
     {
@@ -241,6 +310,7 @@ class VbdSystem
         std::vector<float4> hx(nV), hv(nV), ha(nV), hX(nV);
         std::vector<float> hm(nV);
         std::vector<TetRecord> hrec(nT);
+        hostWg.assign(size_t(nT), 0.0);
         std::vector<int32_t> deg(nV, 0);
         // Colour of every vertex (free vertices from the partitions; pinned ones are never solved
         // and hold the same value in every position buffer, so any colour works: -1).
@@ -302,6 +372,7 @@ class VbdSystem
                     packed[q] = gv[q] | (rank << 30);
                 }
                 double const w = d.wg[e], mu = d.mu[e], la = d.lambda[e];
+                hostWg[t0 + e] = w;
                 TetRecord& r   = hrec[t0 + e];
                 r.v            = make_uint4(packed[0], packed[1], packed[2], packed[3]);
                 r.mat          = make_float4(float(w * mu), float(w * la), float(1.0 + mu / la), 0.f);
@@ -503,6 +574,222 @@ class VbdSystem
         }
         // The host staging vectors die at the end of this scope: wait for the uploads.
         check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+        hostRecords = std::move(hrec);
+    }
+
+    // Per-tet Lame coefficients (system order); the records keep (wg mu, wg lambda, 1 + mu/lambda).
+    void setMaterial(double const* mu, double const* lambda)
+    {
+        for (int32_t e = 0; e < nT; ++e)
+            if (!(mu[e] > 0.0) || !(lambda[e] > 0.0) || !std::isfinite(mu[e]) || !std::isfinite(lambda[e]))
+                throw std::invalid_argument("pbgb_vbd_set_material: expected finite mu > 0 and lambda > 0");
+        for (int32_t e = 0; e < nT; ++e)
+        {
+            double const w     = hostWg[e];
+            hostRecords[e].mat = make_float4(float(w * mu[e]), float(w * lambda[e]), float(1.0 + mu[e] / lambda[e]), 0.f);
+        }
+        tets.upload(hostRecords.data(), size_t(nT), stream);
+        // The upload reads hostRecords asynchronously.
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    }
+
+    void adjointReserve(int32_t slots, int32_t iterations)
+    {
+        if (slots < 0 || iterations < 0)
+            throw std::invalid_argument("pbgb_vbd_adjoint_reserve: expected slots >= 0, iterations >= 0");
+        checkDifferentiable();
+        if (slots == tapeSlots && iterations == tapeIters && ubar.size() == size_t(nV))
+            return;
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+        dropSlotGraphs();
+        adjX.allocate(size_t(nV) * 3);
+        adjV.allocate(size_t(nV) * 3);
+        adjMu.allocate(size_t(nT));
+        adjLa.allocate(size_t(nT));
+        tapeX.allocate(size_t(slots) * size_t(iterations + 1) * size_t(nV));
+        tapeH.allocate(size_t(slots) * size_t(iterations) * size_t(nFree) * 2);
+        ubar.allocate(size_t(nV));
+        xtbar.allocate(size_t(nV));
+        tapeSlots = slots;
+        tapeIters = iterations;
+        slotH.assign(size_t(slots), 0.f);
+        slotStrategy.assign(size_t(slots), -1);
+    }
+
+    void checkDifferentiable() const
+    {
+        if (contact)
+            throw std::invalid_argument("the adjoint does not support contact");
+        if (acceleration != PBGB_ACCEL_NONE)
+            throw std::invalid_argument("the adjoint does not support Chebyshev acceleration");
+        if (kD != 0.f)
+            throw std::invalid_argument("the adjoint does not support damping (kD != 0)");
+        if (strategy > PBGB_INIT_KINETIC_ENERGY_MINIMUM)
+            throw std::invalid_argument("the adjoint supports the Position, Inertia and KineticEnergyMinimum initial guesses");
+    }
+
+    float4* slotX(int32_t slot, int32_t k) const
+    {
+        return tapeX.get() + (size_t(slot) * size_t(tapeIters + 1) + size_t(k)) * size_t(nV);
+    }
+    float4* slotTape(int32_t slot, int32_t k) const
+    {
+        return tapeH.get() + (size_t(slot) * size_t(tapeIters) + size_t(k)) * size_t(nFree) * 2;
+    }
+
+    // One step like step(), with every substep recorded into slots slot0, slot0 + 1, ...  Launched
+    // directly (not from the graph) with the same kernels' recording variant, so the positions
+    // match an unrecorded step.
+    void recordStep(float dt, int32_t iterations, int32_t substeps, int32_t slot0)
+    {
+        checkDifferentiable();
+        if (iterations != tapeIters || slot0 < 0 || int64_t(slot0) + substeps > tapeSlots)
+            throw std::invalid_argument("pbgb_vbd_step_record: slots or iteration count differ from pbgb_vbd_adjoint_reserve");
+        if (recGraphs.size() < size_t(tapeSlots))
+            recGraphs.resize(size_t(tapeSlots));
+        SlotGraph& g = recGraphs[slot0];
+        if (!g.exec || g.dt != dt || g.iters != iterations || g.sub != substeps)
+        {
+            if (g.exec)
+                cudaGraphExecDestroy(g.exec);
+            g.exec  = nullptr;
+            g.exec  = capture([&] { enqueueRecord(dt, iterations, substeps, slot0); });
+            g.dt    = dt;
+            g.iters = iterations;
+            g.sub   = substeps;
+        }
+        check(cudaGraphLaunch(g.exec, stream), "cudaGraphLaunch");
+        float const h = dt / float(substeps);
+        for (int32_t s = 0; s < substeps; ++s)
+        {
+            slotH[slot0 + s]        = h;
+            slotStrategy[slot0 + s] = strategy;
+        }
+    }
+
+    void enqueueRecord(float dt, int32_t iterations, int32_t substeps, int32_t slot0)
+    {
+        float const h   = dt / float(substeps);
+        SubstepParams sp = substepParams(h);
+        sp.h0 = sp.h1 = nullptr;
+        SweepParams w{};
+        w.x        = x.get();
+        w.xt       = xt.get();
+        w.xtilde   = xtilde.get();
+        w.tets     = tets.get();
+        w.X        = X.get();
+        w.solve    = solve.get();
+        w.incPtr   = incPtr.get();
+        w.inc      = inc.get();
+        w.h        = h;
+        w.h2       = h * h;
+        w.kD       = kD;
+        w.detHZero = detHZero;
+        w.omega    = 1.f;
+        int const L = lanesToUse();
+        size_t const bytes = sizeof(float4) * size_t(nV);
+        for (int32_t s = 0; s < substeps; ++s)
+        {
+            int32_t const slot = slot0 + s;
+            check(launch_begin_substep(sp, stream), "begin_substep");
+            if (nV > 0)
+                check(cudaMemcpyAsync(slotX(slot, 0), x.get(), bytes, cudaMemcpyDeviceToDevice, stream), "tape copy");
+            for (int32_t k = 0; k < iterations; ++k)
+            {
+                w.tape = slotTape(slot, k);
+                for (int32_t c = 0; c < nColors; ++c)
+                {
+                    w.begin = colorPtr[c];
+                    w.end   = colorPtr[c + 1];
+                    w.color = c;
+                    // The first colour follows the copy of x into the tape (not a kernel): no programmatic
+                    // launch there, so that it cannot overwrite x while the copy reads it.
+                    check(launch_sweep_record(w, L, block, pdl && c > 0, stream), "sweep_record");
+                }
+                if (nV > 0)
+                    check(cudaMemcpyAsync(slotX(slot, k + 1), x.get(), bytes, cudaMemcpyDeviceToDevice, stream), "tape copy");
+            }
+            check(launch_end_substep(sp, stream), "end_substep");
+        }
+    }
+
+    // Reverses the substeps recorded in slots slot0 + substeps - 1, ..., slot0.  xbar, vbar
+    // (device, nV x 3): adjoints of the positions and velocities after the last substep on entry,
+    // before the first on return.  dlogmu, dloglambda (device, nT, FP64): accumulated.
+    void adjointStep(int32_t slot0, int32_t substeps, float* xbar, float* vbar, double* dlogmu, double* dloglambda)
+    {
+        checkDifferentiable();
+        if (slot0 < 0 || substeps < 1 || int64_t(slot0) + substeps > tapeSlots)
+            throw std::invalid_argument("pbgb_vbd_step_adjoint: slot range outside the reserved tape");
+        std::vector<float> hs(slotH.begin() + slot0, slotH.begin() + slot0 + substeps);
+        std::vector<int32_t> st(slotStrategy.begin() + slot0, slotStrategy.begin() + slot0 + substeps);
+        for (int32_t v : st)
+            if (v < 0)
+                throw std::invalid_argument("pbgb_vbd_step_adjoint: slot was not recorded");
+        if (adjGraphs.size() < size_t(tapeSlots))
+            adjGraphs.resize(size_t(tapeSlots));
+        SlotGraph& g = adjGraphs[slot0];
+        if (!g.exec || g.sub != substeps || g.h != hs || g.strategy != st)
+        {
+            if (g.exec)
+                cudaGraphExecDestroy(g.exec);
+            g.exec     = nullptr;
+            g.exec     = capture([&] { enqueueAdjoint(slot0, substeps, adjX.get(), adjV.get(), adjMu.get(), adjLa.get()); });
+            g.sub      = substeps;
+            g.h        = hs;
+            g.strategy = st;
+        }
+        size_t const b3 = sizeof(float) * 3 * size_t(nV), bt = sizeof(double) * size_t(nT);
+        auto copy = [&](void* dst, void const* src, size_t n) {
+            if (n > 0)
+                check(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToDevice, stream), "adjoint copy");
+        };
+        copy(adjX.get(), xbar, b3);
+        copy(adjV.get(), vbar, b3);
+        copy(adjMu.get(), dlogmu, bt);
+        copy(adjLa.get(), dloglambda, bt);
+        check(cudaGraphLaunch(g.exec, stream), "cudaGraphLaunch");
+        copy(xbar, adjX.get(), b3);
+        copy(vbar, adjV.get(), b3);
+        copy(dlogmu, adjMu.get(), bt);
+        copy(dloglambda, adjLa.get(), bt);
+    }
+
+    void enqueueAdjoint(int32_t slot0, int32_t substeps, float* xbar, float* vbar, double* dlogmu, double* dloglambda)
+    {
+        int const L = lanesToUse();
+        for (int32_t s = substeps - 1; s >= 0; --s)
+        {
+            int32_t const slot = slot0 + s;
+            float const h      = slotH[slot];
+            check(launch_adjoint_begin(nV, xbar, vbar, ubar.get(), xtbar.get(), h, stream), "adjoint_begin");
+            AdjointSweepParams a{};
+            a.X          = X.get();
+            a.tets       = tets.get();
+            a.solve      = solve.get();
+            a.incPtr     = incPtr.get();
+            a.inc        = inc.get();
+            a.m          = m.get();
+            a.ubar       = ubar.get();
+            a.xtbar      = xtbar.get();
+            a.dlogmu     = dlogmu;
+            a.dloglambda = dloglambda;
+            a.h2         = h * h;
+            for (int32_t k = tapeIters; k >= 1; --k)
+            {
+                a.xk   = slotX(slot, k);
+                a.xkm1 = slotX(slot, k - 1);
+                a.tape = slotTape(slot, k - 1);
+                for (int32_t c = nColors - 1; c >= 0; --c)
+                {
+                    a.begin = colorPtr[c];
+                    a.end   = colorPtr[c + 1];
+                    check(launch_adjoint_sweep(a, L, std::min(block, 256), pdl, stream), "adjoint_sweep");
+                }
+            }
+            float const s1 = slotStrategy[slot] == PBGB_INIT_POSITION ? 0.f : 1.f;
+            check(launch_adjoint_end(nV, xbar, vbar, ubar.get(), xtbar.get(), h, s1, stream), "adjoint_end");
+        }
     }
 
     SubstepParams substepParams(float h) const
@@ -1073,6 +1360,77 @@ PBGB_API int pbgb_vbd_set_positions_device(pbgb_vbd* h, const float* x_dev)
     });
 }
 
+PBGB_API int pbgb_vbd_get_velocities_device(pbgb_vbd* h, float* v_dev)
+{
+    PBGB_CHECK_HANDLE_PTR(h, v_dev)
+    return guarded(h, [&] {
+        pbgb::check(pbgb::launch_unpack3(h->sys.v.get(), v_dev, h->sys.nV, h->sys.stream), "unpack");
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_set_velocities_device(pbgb_vbd* h, const float* v_dev)
+{
+    PBGB_CHECK_HANDLE_PTR(h, v_dev)
+    return guarded(h, [&] {
+        pbgb::check(pbgb::launch_pack3(v_dev, h->sys.v.get(), h->sys.nV, h->sys.stream), "pack");
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_set_material(pbgb_vbd* h, const double* mu, const double* lambda)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (h->sys.nT > 0 && (!mu || !lambda))
+        return fail(h, kInvalid, "null argument");
+    return guarded(h, [&] {
+        h->sys.setMaterial(mu, lambda);
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_adjoint_reserve(pbgb_vbd* h, int32_t slots, int32_t iterations)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    return guarded(h, [&] {
+        h->sys.adjointReserve(slots, iterations);
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_step_record(pbgb_vbd* h, float dt, int32_t iterations, int32_t substeps, int32_t slot)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (!(dt > 0.f) || !std::isfinite(dt) || iterations < 0 || substeps < 1)
+        return fail(h, kInvalid, "pbgb_vbd_step_record: expected dt > 0, iterations >= 0, substeps >= 1");
+    return guarded(h, [&] {
+        h->sys.recordStep(dt, iterations, substeps, slot);
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_step_adjoint(
+    pbgb_vbd* h,
+    int32_t slot,
+    int32_t substeps,
+    float* xbar_dev,
+    float* vbar_dev,
+    double* dlogmu_dev,
+    double* dloglambda_dev)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (!xbar_dev || !vbar_dev || (h->sys.nT > 0 && (!dlogmu_dev || !dloglambda_dev)))
+        return fail(h, kInvalid, "null argument");
+    return guarded(h, [&] {
+        h->sys.adjointStep(slot, substeps, xbar_dev, vbar_dev, dlogmu_dev, dloglambda_dev);
+        return int(kOk);
+    });
+}
+
 PBGB_API int pbgb_vbd_set_detH_zero(pbgb_vbd* h, float zero)
 {
     if (!h)
@@ -1387,6 +1745,60 @@ PBGB_API int pbgb_debug_vertex_triangle_contact(
     H[6] = Hs[2], H[7] = Hs[4], H[8] = Hs[5];
     if (energy)
         *energy = E;
+    return kOk;
+}
+
+PBGB_API int pbgb_debug_adjoint_tet(
+    int32_t precision,
+    const double* xe,
+    const double* Xe,
+    int32_t il,
+    const double* w,
+    const double* delta,
+    double muw,
+    double law,
+    double* dphi,
+    double* dlogmu,
+    double* dloglambda)
+{
+    if (!xe || !Xe || !w || !delta || !dphi || !dlogmu || !dloglambda || il < 0 || il > 3 ||
+        (precision != 32 && precision != 64))
+        return fail(nullptr, kInvalid, "pbgb_debug_adjoint_tet: invalid argument");
+    auto run = [&](auto zero) {
+        using T = decltype(zero);
+        T d[3][3], e[3][3], G[3][3], c[3][3];
+        T const tw[3] = {T(w[0]), T(w[1]), T(w[2])};
+        T const td[3] = {T(delta[0]), T(delta[1]), T(delta[2])};
+        for (int m = 0; m < 3; ++m)
+        {
+            int const a = (il + 1 + m) & 3;
+            for (int r = 0; r < 3; ++r)
+            {
+                d[m][r] = T(xe[3 * a + r]) - T(xe[3 * il + r]);
+                e[m][r] = T(Xe[3 * a + r]) - T(Xe[3 * il + r]);
+            }
+        }
+        pbgb::rest_gradients(e, G);
+        T dm = T(0), dl = T(0);
+        pbgb::adjoint_tet(d, e, G, tw, td, T(muw), T(law), c, dm, dl);
+        for (int r = 0; r < 3; ++r)
+            dphi[3 * il + r] = 0.0;
+        for (int m = 0; m < 3; ++m)
+        {
+            int const a = (il + 1 + m) & 3;
+            for (int r = 0; r < 3; ++r)
+            {
+                dphi[3 * a + r] = double(c[m][r]);
+                dphi[3 * il + r] -= double(c[m][r]);
+            }
+        }
+        *dlogmu     = double(dm);
+        *dloglambda = double(dl);
+    };
+    if (precision == 64)
+        run(0.0);
+    else
+        run(0.0f);
     return kOk;
 }
 

@@ -68,7 +68,10 @@ __device__ __noinline__ void add_contacts(SweepParams const& p, int i, float con
 // reference's ordering: a neighbour of lower colour rank (already solved in iteration k) is read
 // from x (raw iterate k), one of higher rank from hprev (accelerated iterate k-1).  hcur holds
 // iterate k-2 on entry and receives the accelerated iterate k.
-template <int L, bool CHEB>
+//
+// REC (without CHEB): also writes the inverse Newton matrix of every solved vertex to p.tape for
+// the adjoint sweep.
+template <int L, bool CHEB, bool REC = false>
 __global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
 {
     int const tid    = blockIdx.x * blockDim.x + threadIdx.x;
@@ -171,6 +174,25 @@ __global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
     if (CHEB && p.fc)
         add_contacts(p, i, xt, xi, H, g);
     bool const moved = inertia_solve(H, g, xl, xt4.w, p.h2, p.detHZero, xi);
+    if (REC)
+    {
+        // H now includes the inertia term; its inverse by the adjugate, as in inertia_solve.
+        float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
+        if (moved)
+        {
+            float const a00 = H[3] * H[5] - H[4] * H[4];
+            float const a01 = H[2] * H[4] - H[1] * H[5];
+            float const a02 = H[1] * H[4] - H[2] * H[3];
+            float const a11 = H[0] * H[5] - H[2] * H[2];
+            float const a12 = H[1] * H[2] - H[0] * H[4];
+            float const a22 = H[0] * H[3] - H[1] * H[1];
+            float const inv = 1.f / (H[0] * a00 + H[1] * a01 + H[2] * a02);
+            r0 = make_float4(inv * a00, inv * a01, inv * a02, inv * a11);
+            r1 = make_float4(inv * a12, inv * a22, 0.f, 0.f);
+        }
+        p.tape[2 * s]     = r0;
+        p.tape[2 * s + 1] = r1;
+    }
     if (CHEB)
     {
         // Raw iterate k (even when the Newton step was skipped: later colours read it).
@@ -396,7 +418,7 @@ inline int blocks_for(int64_t n, int block)
 
 } // namespace
 
-template <int L, bool CHEB>
+template <int L, bool CHEB, bool REC = false>
 cudaError_t launch_sweep_l(SweepParams const& p, int g, int block, bool pdl, cudaStream_t s)
 {
     cudaLaunchConfig_t cfg = {};
@@ -409,7 +431,7 @@ cudaError_t launch_sweep_l(SweepParams const& p, int g, int block, bool pdl, cud
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs                                          = attr;
     cfg.numAttrs                                       = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, sweep_kernel<L, CHEB>, p);
+    return cudaLaunchKernelEx(&cfg, sweep_kernel<L, CHEB, REC>, p);
 }
 
 template <bool CHEB>
@@ -435,6 +457,26 @@ cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebys
     int const g = blocks_for(n, block);
     return chebyshev ? launch_sweep_t<true>(p, lanes, g, block, pdl, s)
                      : launch_sweep_t<false>(p, lanes, g, block, pdl, s);
+}
+
+cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool pdl, cudaStream_t s)
+{
+    int64_t const n = int64_t(p.end - p.begin) * lanes;
+    if (n <= 0)
+        return cudaSuccess;
+    if (!p.tape)
+        return cudaErrorInvalidValue;
+    int const g = blocks_for(n, block);
+    switch (lanes)
+    {
+        case 1: return launch_sweep_l<1, false, true>(p, g, block, pdl, s);
+        case 2: return launch_sweep_l<2, false, true>(p, g, block, pdl, s);
+        case 4: return launch_sweep_l<4, false, true>(p, g, block, pdl, s);
+        case 8: return launch_sweep_l<8, false, true>(p, g, block, pdl, s);
+        case 16: return launch_sweep_l<16, false, true>(p, g, block, pdl, s);
+        case 32: return launch_sweep_l<32, false, true>(p, g, block, pdl, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_begin_substep(SubstepParams const& p, cudaStream_t s)

@@ -65,6 +65,10 @@ struct SweepParams
     float muC;
     float muF;
     float epsv;
+    // Adjoint tape of this iteration (recording sweeps only): for solve-list entry s, the inverse
+    // of the vertex's 3x3 Newton matrix (xx xy xz yy | yz zz 0 0) in tape[2s], tape[2s+1]; zero
+    // when the Newton step was skipped.
+    float4* __restrict__ tape;
 };
 
 struct SubstepParams
@@ -105,6 +109,9 @@ struct EnergyParams
 // overlaps the tail of the previous launch on the stream (the kernel waits before reading
 // positions).
 cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, bool pdl, cudaStream_t s);
+// The plain (one-buffer) sweep that also writes p.tape; the same arithmetic as launch_sweep with
+// chebyshev = false, so a recorded step reproduces an unrecorded one.
+cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool pdl, cudaStream_t s);
 cudaError_t launch_begin_substep(SubstepParams const& p, cudaStream_t s);
 cudaError_t launch_end_substep(SubstepParams const& p, cudaStream_t s);
 cudaError_t launch_objective(EnergyParams const& p, cudaStream_t s);

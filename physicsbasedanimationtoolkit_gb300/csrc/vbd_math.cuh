@@ -342,4 +342,131 @@ PBGB_HD T chebyshev_omega(int k, T rho2, T omega, int formula)
     return formula == 0 ? T(1) - rho2 * omega : T(4) / (T(4) - rho2 * omega);
 }
 
+// Reverse of one vertex's Newton update, restricted to one incident tetrahedron.
+//
+// The forward update of vertex o is x_o' = x_o - H^-1 g with g, H the vertex's gradient and 3x3
+// block at the state before the update.  With w = H^-1 u (u: adjoint of x_o') and the applied step
+// delta = x_o - x_o', the adjoint of every input of the update is minus the gradient of
+//   phi = w . (g - H delta)        (w and delta held fixed),
+// plus u itself for x_o.  One tetrahedron contributes
+//   phi_e = wg [P(F):A - mu |g_o|^2 (w.delta) - lambda (cof F : A)(cof F : B)],
+//   A = w g_o^T, B = delta g_o^T, P = mu F + lambda (J - alpha) cof F,
+// and its gradient with respect to F is
+//   M = wg [mu A + lambda (cof:A)(cof - D_B) + lambda (J - alpha - cof:B) D_A],
+// where D_A = d(cof F : A)/dF.  For a rank-one A = a g^T the columns of D_A are
+//   g1 (a x f2) + g2 (f1 x a),  g0 (f2 x a) + g2 (a x f0),  g0 (a x f1) + g1 (f0 x a).
+// The third derivative of det F contracted with A and B vanishes because A and B share the row
+// vector g_o, so no other term appears.  The gradient of phi_e with respect to corner a_k is M G[k];
+// for o it is M g_o = -(sum of the three), which the caller accumulates.
+//
+// The material sensitivities are proportional to the stress, a small difference of O(1) terms at
+// small strain: with the displacement gradient D = F - I = sum_k (d[k] - e[k]) G[k]^T (the edge
+// differences are exact in floating point for nearby points), they are formed from
+//   J - 1 = tr D + (sum of the principal 2x2 minors of D) + det D,
+//   F - cof F = D + D^T - tr(D) I - cof D,
+// and lambda (J - alpha) = lambda (J - 1) - mu, so nothing cancels.
+//
+//   d[k] = x_{a_k} - x_o, e[k] = X_{a_k} - X_o (rest), G[k] = grad N_{a_k} (as in accumulate_tet),
+//   evaluated before the update;
+//   w, delta: see above; muw, law: wg*mu, wg*lambda (alpha = 1 + mu/lambda is implied).
+//   c[k]: d(phi_e)/d(x_{a_k}).
+//   dlogmu, dloglambda: d(phi_e)/d(log mu), d(phi_e)/d(log lambda), with alpha = 1 + mu/lambda
+//   varying with both.
+template <class T>
+PBGB_HD void adjoint_tet(
+    T const (&d)[3][3],
+    T const (&e)[3][3],
+    T const (&G)[3][3],
+    T const* w,
+    T const* delta,
+    T muw,
+    T law,
+    T (&c)[3][3],
+    T& dlogmu,
+    T& dloglambda)
+{
+    T f[3][3]; // f[col][row] = F(row, col)
+    for (int q = 0; q < 3; ++q)
+        for (int r = 0; r < 3; ++r)
+            f[q][r] = d[0][r] * G[0][q] + d[1][r] * G[1][q] + d[2][r] * G[2][q];
+    T go[3];
+    for (int q = 0; q < 3; ++q)
+        go[q] = -(G[0][q] + G[1][q] + G[2][q]);
+    T k[3][3]; // cofactor columns
+    k[0][0] = f[1][1] * f[2][2] - f[1][2] * f[2][1];
+    k[0][1] = f[1][2] * f[2][0] - f[1][0] * f[2][2];
+    k[0][2] = f[1][0] * f[2][1] - f[1][1] * f[2][0];
+    k[1][0] = f[2][1] * f[0][2] - f[2][2] * f[0][1];
+    k[1][1] = f[2][2] * f[0][0] - f[2][0] * f[0][2];
+    k[1][2] = f[2][0] * f[0][1] - f[2][1] * f[0][0];
+    k[2][0] = f[0][1] * f[1][2] - f[0][2] * f[1][1];
+    k[2][1] = f[0][2] * f[1][0] - f[0][0] * f[1][2];
+    k[2][2] = f[0][0] * f[1][1] - f[0][1] * f[1][0];
+    // Displacement gradient D[col][row].
+    T D[3][3];
+    for (int q = 0; q < 3; ++q)
+        for (int r = 0; r < 3; ++r)
+            D[q][r] = (d[0][r] - e[0][r]) * G[0][q] + (d[1][r] - e[1][r]) * G[1][q] + (d[2][r] - e[2][r]) * G[2][q];
+    // cof D (columns D1 x D2, D2 x D0, D0 x D1), J - 1 and F - cof F.
+    T cd[3][3];
+    for (int q = 0; q < 3; ++q)
+    {
+        T const* u = D[(q + 1) % 3];
+        T const* v = D[(q + 2) % 3];
+        cd[q][0] = u[1] * v[2] - u[2] * v[1];
+        cd[q][1] = u[2] * v[0] - u[0] * v[2];
+        cd[q][2] = u[0] * v[1] - u[1] * v[0];
+    }
+    T const trD  = D[0][0] + D[1][1] + D[2][2];
+    T const min2 = (D[0][0] * D[1][1] - D[1][0] * D[0][1]) + (D[0][0] * D[2][2] - D[2][0] * D[0][2]) +
+                   (D[1][1] * D[2][2] - D[2][1] * D[1][2]);
+    T const detD = D[0][0] * cd[0][0] + D[0][1] * cd[0][1] + D[0][2] * cd[0][2];
+    T const Jm1  = trD + min2 + detD;
+    // cof:A = w . (cof g_o), cof:B = delta . (cof g_o), (F - cof):A = w . ((F - cof) g_o)
+    T cg[3], sg[3];
+    for (int r = 0; r < 3; ++r)
+    {
+        cg[r] = go[0] * k[0][r] + go[1] * k[1][r] + go[2] * k[2][r];
+        T acc = T(0);
+        for (int q = 0; q < 3; ++q)
+            acc += go[q] * (D[q][r] + D[r][q] - cd[q][r] - (q == r ? trD : T(0)));
+        sg[r] = acc;
+    }
+    T const cA  = w[0] * cg[0] + w[1] * cg[1] + w[2] * cg[2];
+    T const cB  = delta[0] * cg[0] + delta[1] * cg[1] + delta[2] * cg[2];
+    T const FmC = w[0] * sg[0] + w[1] * sg[1] + w[2] * sg[2];
+    T const wd  = w[0] * delta[0] + w[1] * delta[1] + w[2] * delta[2];
+    T const gg  = go[0] * go[0] + go[1] * go[1] + go[2] * go[2];
+    dlogmu      = muw * (FmC - gg * wd);
+    dloglambda  = law * (Jm1 * cA - cA * cB);
+    // Columns of D_a for a rank-one direction a g_o^T.
+    auto dcol = [&](T const* a, int q, T* out) {
+        auto cross = [](T const* u, T const* v, T* o) {
+            o[0] = u[1] * v[2] - u[2] * v[1];
+            o[1] = u[2] * v[0] - u[0] * v[2];
+            o[2] = u[0] * v[1] - u[1] * v[0];
+        };
+        int const q1 = (q + 1) % 3, q2 = (q + 2) % 3;
+        T u[3], v[3];
+        cross(a, f[q2], u); // a x f_{q+2}
+        cross(f[q1], a, v); // f_{q+1} x a
+        for (int r = 0; r < 3; ++r)
+            out[r] = go[q1] * u[r] + go[q2] * v[r];
+    };
+    T const sA = law * (Jm1 - cB) - muw;
+    T const sC = law * cA;
+    T M[3][3]; // M[col][row]
+    for (int q = 0; q < 3; ++q)
+    {
+        T dA[3], dB[3];
+        dcol(w, q, dA);
+        dcol(delta, q, dB);
+        for (int r = 0; r < 3; ++r)
+            M[q][r] = muw * go[q] * w[r] + sC * (k[q][r] - dB[r]) + sA * dA[r];
+    }
+    for (int m = 0; m < 3; ++m)
+        for (int r = 0; r < 3; ++r)
+            c[m][r] = M[0][r] * G[m][0] + M[1][r] * G[m][1] + M[2][r] * G[m][2];
+}
+
 } // namespace pbgb

@@ -202,6 +202,20 @@ def batch_workload(n_meshes=256, nmin=6, nmax=32, seed=0, spacing=1.5):
     return meshes
 
 
+def adjoint_beam_workload(nx=40, ny=10, nz=10, seed=0, nu=0.45, rho=1000.0, offset=(0.0, 0.0, -0.3)):
+    """Differentiation workload: beam ``[0,4]x[0,1]x[0,1]`` as an ``nx x ny x nz`` hex grid, per-tet
+    log Young's modulus ~ N(log 1e6, 0.3^2) from ``seed``, the x=0 face pinned, starting at rest.
+    The loss is the sum over the x=4 tip-face vertices of |x - (X + offset)|^2.  With 40x10x10:
+    4,961 vertices, 24,000 tets, 121 tip vertices.
+    """
+    X, T = hex_grid(nx, ny, nz, hi=(4.0, 1.0, 1.0))
+    rng = np.random.default_rng(seed)
+    logE = rng.normal(np.log(1e6), 0.3, size=T.shape[0])
+    tip = face_vertices(X, 0, 4.0)
+    return dict(X=X, T=T, dbc=face_vertices(X, 0, 0.0), logE=logE, nu=nu, rho=np.full(T.shape[0], rho),
+                tip=tip, target=X[tip] + np.asarray(offset, dtype=np.float64))
+
+
 def contact_scene_workload(n_cubes_side=4, cube_hexes=16, slab_hexes=(64, 64, 2), cube_size=0.6,
                            cell=1.0, gap=0.05, seed=0, E=1e6, nu=0.45, rho=1000.0):
     """Cubes dropped on a fixed slab: an ``n x n`` arrangement of ``cube_hexes^3``-hex cubes (6 tets

@@ -104,3 +104,104 @@ class BatchedIntegrator(IntegratorBase):
     @v.setter
     def v(self, value):
         self._set("v", value)
+
+
+class _Rollout:
+    """torch.autograd.Function over ``steps`` GPU VBD steps (built on first use so that importing
+    this module does not import torch)."""
+
+    fn = None
+
+    @classmethod
+    def get(cls):
+        if cls.fn is not None:
+            return cls.fn
+        import torch
+
+        class Rollout(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, mu, lam, x0, v0, integ, dt, iterations, substeps, steps, every):
+                dev = x0.device
+                nV = integ.n_vertices
+                # The tape is reserved up front so that unsupported settings fail here.
+                integ.adjoint_reserve(min(every, steps) * substeps, iterations)
+                integ.set_material(mu.detach().cpu().numpy(), lam.detach().cpu().numpy())
+                x = x0.detach().to(torch.float32).contiguous()
+                v = v0.detach().to(torch.float32).contiguous()
+                torch.cuda.synchronize(dev)
+                integ._set_device("x", x.data_ptr())
+                integ._set_device("v", v.data_ptr())
+                checkpoints = []
+                for t in range(steps):
+                    if t % every == 0:
+                        cx = torch.empty((nV, 3), dtype=torch.float32, device=dev)
+                        cv = torch.empty_like(cx)
+                        integ._get_device("x", cx.data_ptr())
+                        integ._get_device("v", cv.data_ptr())
+                        checkpoints.append((cx, cv))
+                    integ.step(dt, iterations, substeps)
+                xT = torch.empty((nV, 3), dtype=torch.float32, device=dev)
+                vT = torch.empty_like(xT)
+                integ._get_device("x", xT.data_ptr())
+                integ._get_device("v", vT.data_ptr())
+                integ.synchronize()
+                ctx.integ = integ
+                ctx.args = (dt, iterations, substeps, steps, every)
+                ctx.checkpoints = checkpoints
+                ctx.final = (xT.clone(), vT.clone())
+                ctx.save_for_backward(mu, lam)
+                return xT, vT
+
+            @staticmethod
+            def backward(ctx, gx, gv):
+                mu, lam = ctx.saved_tensors
+                integ = ctx.integ
+                dt, iterations, substeps, steps, every = ctx.args
+                dev = ctx.final[0].device
+                nV, nT = integ.n_vertices, integ.n_tets
+                xbar = (torch.zeros((nV, 3), device=dev) if gx is None else gx.detach().to(dev, torch.float32)).contiguous().clone()
+                vbar = (torch.zeros((nV, 3), device=dev) if gv is None else gv.detach().to(dev, torch.float32)).contiguous().clone()
+                dlogmu = torch.zeros(nT, dtype=torch.float64, device=dev)
+                dloglambda = torch.zeros_like(dlogmu)
+                integ.adjoint_reserve(min(every, steps) * substeps, iterations)
+                torch.cuda.synchronize(dev)
+                for seg in reversed(range(len(ctx.checkpoints))):
+                    start = seg * every
+                    end = min(start + every, steps)
+                    cx, cv = ctx.checkpoints[seg]
+                    integ._set_device("x", cx.data_ptr())
+                    integ._set_device("v", cv.data_ptr())
+                    for t in range(start, end):
+                        integ.step_record(dt, iterations, substeps, (t - start) * substeps)
+                    for t in reversed(range(start, end)):
+                        integ.step_adjoint((t - start) * substeps, substeps, xbar.data_ptr(), vbar.data_ptr(),
+                                           dlogmu.data_ptr(), dloglambda.data_ptr())
+                # Leave the integrator at the end of the forward rollout.
+                integ._set_device("x", ctx.final[0].data_ptr())
+                integ._set_device("v", ctx.final[1].data_ptr())
+                integ.synchronize()
+                dmu = dlogmu.to(mu.dtype).to(mu.device) / mu.detach()
+                dlam = dloglambda.to(lam.dtype).to(lam.device) / lam.detach()
+                return dmu, dlam, xbar, vbar, None, None, None, None, None, None
+
+        cls.fn = Rollout
+        return Rollout
+
+
+def rollout(integrator, mu, lam, x0, v0, dt=0.01, iterations=20, steps=1, substeps=1, checkpoint_every=5):
+    """Differentiable rollout of ``steps`` steps of ``integrator`` (an addition: the reference has
+    no differentiation).
+
+    mu, lam: per-tet Lame coefficients (|#tets|, torch tensors; set on the integrator);
+    x0, v0: |#vertices| x 3 start positions and velocities (CUDA tensors).  Returns the positions
+    and velocities after the last step.  Backward runs the adjoint kernels: the positions are
+    checkpointed every ``checkpoint_every`` steps in the forward pass, and each checkpoint segment
+    is re-run with recording before it is reversed.  The gradient is the exact derivative of the
+    computed iterations (FP32).  Supported: no acceleration, kD = 0, no contact, initial guess
+    Position, Inertia or KineticEnergyMinimum.  Backward leaves the integrator at the rollout's
+    end state.
+    """
+    if checkpoint_every < 1:
+        raise ValueError("checkpoint_every must be >= 1")
+    return _Rollout.get().apply(mu, lam, x0, v0, integrator, float(dt), int(iterations), int(substeps), int(steps),
+                                int(checkpoint_every))

@@ -84,6 +84,9 @@ def lib():
             C.c_int32,
         ]
         L.orc_objective.restype = C.c_double
+        L.orc_adjoint.restype = C.c_int
+        L.orc_adjoint.argtypes = [C.POINTER(OrcProblem), _f64p, _f64p, C.c_double, C.c_int32, C.c_int32,
+                                  C.c_int32, _f64p, _f64p, _f64p, _f64p]
         L.orc_objective.argtypes = [C.POINTER(OrcProblem), _f64p, _f64p, C.c_double]
         L.orc_gradient.restype = None
         L.orc_gradient.argtypes = [C.POINTER(OrcProblem), _f64p, _f64p, C.c_double, _f64p]
@@ -236,6 +239,20 @@ class OracleVbd:
             nsteps)
         if rc != 0:
             raise RuntimeError(f"oracle run failed: {rc}")
+
+    def adjoint(self, dt, iterations, substeps, nsteps, xbar, vbar):
+        """Reverse-mode derivative of ``nsteps`` steps from the current state (not advanced).
+        xbar, vbar (nV x 3): dL/dx, dL/dv of the final state.  Returns dL/dx0, dL/dv0 and
+        dL/dlog(mu), dL/dlog(lambda) per tet."""
+        xb = np.array(xbar, dtype=np.float64, order="C")
+        vb = np.array(vbar, dtype=np.float64, order="C")
+        dmu = np.zeros(self.T.shape[0])
+        dla = np.zeros(self.T.shape[0])
+        rc = lib().orc_adjoint(C.byref(self.P), np.ascontiguousarray(self.x), np.ascontiguousarray(self.v), dt,
+                               iterations, substeps, nsteps, xb, vb, dmu, dla)
+        if rc != 0:
+            raise RuntimeError(f"oracle adjoint failed: {rc}")
+        return xb, vb, dmu, dla
 
     def objective(self, x, xtilde, dt):
         return lib().orc_objective(C.byref(self.P), np.ascontiguousarray(x), np.ascontiguousarray(xtilde), dt)
