@@ -282,6 +282,15 @@ def run_batch(args, pbat, _capi, torch):
         X = meshes[b]["X"]
         diag = np.linalg.norm(X.max(0) - X.min(0))
         worst = max(worst, float(np.abs(xb[:, off[b]: off[b + 1]] - s.x).max() / diag))
+    # One mesh at a time (each step waited for before the next mesh's), as separate integrators
+    # run by a caller that does not overlap them.  After the agreement check: it advances the
+    # single integrators further.
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for s in singles:
+            s.step(dt, iters, 1)
+            s.synchronize()
+    t_serial = time.perf_counter() - t0
     launches = B.launches_per_step(iters, 1)
     return {
         "workload": f"{len(meshes)} cube grids, side U{{6..32}} hexes x 6 tets, {iters} iterations, no acceleration",
@@ -291,6 +300,8 @@ def run_batch(args, pbat, _capi, torch):
         "batched_value": n_free * iters * args.steps / t_batched,
         "single_launch_value": n_free * iters * args.steps / t_single,
         "speedup": t_single / t_batched,
+        "single_launch_serial_value": n_free * iters * args.steps / t_serial,
+        "speedup_vs_serial": t_serial / t_batched,
         "batched_ms_per_step": 1e3 * t_batched / args.steps,
         "single_launch_ms_per_step": 1e3 * t_single / args.steps,
         "max_rel_diff_batched_vs_single": worst,
@@ -298,6 +309,102 @@ def run_batch(args, pbat, _capi, torch):
         "batched_launches_per_step": int(launches),
         "single_launches_per_step": int(sum(s.launches_per_step(iters, 1) for s in singles)),
         "unit": UNIT,
+    }
+
+
+def run_adjoint(args, pbat, torch):
+    """Differentiation workload: beam [0,4]x[0,1]^2 at 40x10x10 hexes (4,961 vertices, 24,000
+    tets), per-tet log E ~ N(log 1e6, 0.3^2), nu 0.45, 30 steps of 20 iterations at dt = 1/60, loss
+    on the 121 tip vertices; checkpoints every 5 steps.  Forward = the rollout (graph-replayed steps
+    plus checkpoint copies), backward = re-recording each segment and reversing it; both timed on
+    the host around a device synchronize."""
+    from physicsbasedanimationtoolkit_gb300 import meshgen
+
+    w = meshgen.adjoint_beam_workload()
+    nT = w["T"].shape[0]
+    nu = w["nu"]
+    mu0, lam0 = meshgen.lame(np.exp(w["logE"]), np.full(nT, nu))
+    data = (pbat.sim.vbd.Data().with_volume_mesh(w["X"].T, w["T"].T).with_material(w["rho"], mu0, lam0)
+            .with_dirichlet_vertices(w["dbc"]).with_initialization_strategy(2).construct())
+    I = pbat.gpu.vbd.Integrator(data)
+    dt, iters, steps, every = 1 / 60, 20, 30, 5
+    logE = torch.tensor(w["logE"], dtype=torch.float64, requires_grad=True)
+    x0 = torch.tensor(w["X"], dtype=torch.float32, device="cuda", requires_grad=True)
+    v0 = torch.zeros_like(x0, requires_grad=True)
+    tip = torch.tensor(w["tip"], device="cuda")
+    target = torch.tensor(w["target"], dtype=torch.float32, device="cuda")
+    fwd, bwd = [], []
+    for k in range(args.warmup + args.steps):
+        logE.grad = None
+        x0.grad = None
+        v0.grad = None
+        E = torch.exp(logE)
+        mu = E / (2 * (1 + nu))
+        lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xT, _ = pbat.gpu.vbd.rollout(I, mu, lam, x0, v0, dt=dt, iterations=iters, steps=steps, checkpoint_every=every)
+        loss = ((xT[tip] - target) ** 2).sum()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        loss.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        if k >= args.warmup:
+            fwd.append(t1 - t0)
+            bwd.append(t2 - t1)
+    f, b = float(np.median(fwd)), float(np.median(bwd))
+    return {
+        "workload": "beam [0,4]x[0,1]^2 40x10x10 hexes x 6 tets, log E ~ N(log 1e6, 0.3^2), nu 0.45, "
+                    "30 steps x 20 iterations, dt 1/60, tip-face loss, checkpoints every 5 steps",
+        "fwd_ms": 1e3 * f,
+        "bwd_ms": 1e3 * b,
+        "bwd_over_fwd": b / f,
+        "loss": float(loss.detach()),
+        "grad_norms": {"log_E": float(logE.grad.norm()), "v0": float(v0.grad.norm()), "x0": float(x0.grad.norm())},
+        "timing": "host clock around torch.cuda.synchronize, median of the timed repetitions",
+    }
+
+
+def run_contact(args, pbat, torch):
+    """Contact scene: 16 cubes (16^3 hexes, 0.6 m) above a pinned 64x64x2 slab, 91,283 vertices,
+    442,368 tets, 66,560 collision triangles; 30 iterations per step, dt = 1/60, muC = 1e7.  Each
+    step rebuilds the active set (LBVH over swept triangle boxes), refreshes the contact lists and
+    runs the contact-aware colour sweeps; timed with CUDA events on the integrator's stream."""
+    from physicsbasedanimationtoolkit_gb300 import meshgen
+
+    w = meshgen.contact_scene_workload()
+    d = (pbat.sim.vbd.Data().with_volume_mesh(w["X"].T, w["T"].T).with_surface_mesh(w["V"], w["F"].T)
+         .with_bodies(w["B"]).with_material(w["rho"], w["mu"], w["lam"]).with_dirichlet_vertices(w["dbc"])
+         .with_contact_parameters(1e7, 0.3, 1e-3).with_initialization_strategy(2).construct())
+    I = pbat.gpu.vbd.Integrator(d)
+    dt, iters = 1 / 60, 30
+    for _ in range(args.warmup):
+        I.step(dt, iters, 1)
+    I.synchronize()
+    sp = C.c_void_p()
+    from physicsbasedanimationtoolkit_gb300 import _capi
+    _capi.check(_capi.lib().pbgb_vbd_stream(I.handle, C.byref(sp)), I.handle)
+    stream = torch.cuda.ExternalStream(sp.value)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        I.step(dt, iters, 1)
+    e1.record(stream)
+    I.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3
+    fc, active = I.contacts()
+    return {
+        "workload": "16 cubes of 16^3 hexes on a pinned 64x64x2 slab, vertex-triangle contact, 30 iterations",
+        "n_vertices": int(I.n_vertices),
+        "n_tets": int(I.n_tets),
+        "value": I.n_free * iters * args.steps / t,
+        "unit": UNIT,
+        "ms_per_step": 1e3 * t / args.steps,
+        "launches_per_step": int(I.launches_per_step(iters, 1)),
+        "active_vertices": int(active.sum()),
+        "vertices_with_contacts": int((fc >= 0).any(axis=1).sum()),
     }
 
 
@@ -332,6 +439,10 @@ def main():
     ap.add_argument("--no-batch", dest="batch", action="store_false")
     ap.add_argument("--batch-meshes", type=int, default=256)
     ap.add_argument("--batch-iterations", type=int, default=20)
+    ap.add_argument("--no-adjoint", dest="adjoint", action="store_false", default=True,
+                    help="skip the adjoint (bwd/fwd) measurement on the differentiation beam")
+    ap.add_argument("--no-contact", dest="contact", action="store_false", default=True,
+                    help="skip the contact-scene step measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -447,6 +558,8 @@ def main():
             del vbd
             torch.cuda.empty_cache()
             batched = run_batch(args, pbat, _capi, torch)
+        adjoint = run_adjoint(args, pbat, torch) if args.adjoint else None
+        contact = run_contact(args, pbat, torch) if args.contact else None
         launches = launches_per_step * args.steps
         line = {
             "metric": METRIC,
@@ -477,6 +590,8 @@ def main():
             "n_free_vertices": n_free,
             "n_colors": n_colors,
             "batched": batched,
+            "adjoint": adjoint,
+            "contact": contact,
         }
         print(json.dumps(line))
     if dist:
