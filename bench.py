@@ -408,6 +408,71 @@ def run_contact(args, pbat, torch):
     }
 
 
+LBVH_BYTES_PER_BOX = 343  # Morton 40, 4 radix passes 83, Karras 36, leaf gather 68, boxes 116
+
+
+def run_lbvh(args, _capi, torch):
+    """LBVH build over 4,194,304 seeded boxes (centres U[0,1)^3, half-extents U[0, 1e-3)) from
+    device arrays: Morton codes, the stable 4-pass radix sort, the Karras hierarchy, the leaf gather
+    and the bottom-up boxes; CUDA events on the BVH's stream.  Algorithmic bytes per box: Morton 40
+    (two boxes read, code and index written), radix 4 x 20 + digit counts 3, Karras 36, leaf gather
+    68, bottom-up boxes 116."""
+    n = 1 << 22
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    c = torch.rand((n, 3), device="cuda", generator=g)
+    e = torch.rand((n, 3), device="cuda", generator=g) * 1e-3
+    lo = torch.zeros((n, 4), device="cuda")
+    hi = torch.zeros((n, 4), device="cuda")
+    lo[:, :3] = c - e
+    hi[:, :3] = c + e
+    wmin = np.zeros(3, np.float32)
+    wmax = np.ones(3, np.float32)
+    L = _capi.lib()
+    b = C.c_void_p()
+    _capi.check_bvh(L.pbgb_bvh_create(n, C.byref(b)), b)
+    try:
+        sp = C.c_void_p()
+        _capi.check_bvh(L.pbgb_bvh_stream(b, C.byref(sp)), b)
+        stream = torch.cuda.ExternalStream(sp.value)
+        torch.cuda.synchronize()
+
+        def build():
+            _capi.check_bvh(L.pbgb_bvh_build_device(b, n, C.c_void_p(lo.data_ptr()), C.c_void_p(hi.data_ptr()),
+                                                     wmin.ctypes.data, wmax.ctypes.data), b)
+
+        for _ in range(args.warmup):
+            build()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stream.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            build()
+        e1.record(stream)
+        stream.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        # A host-buffer call surfaces the device-side error flags of the builds.
+        nq = 1
+        cnt = C.c_int64()
+        q = np.array([[0.5, 0.5, 0.5]], np.float32)
+        _capi.check_bvh(L.pbgb_bvh_overlaps(b, nq, q.ctypes.data, q.ctypes.data, None, 0, C.byref(cnt)), b)
+    finally:
+        L.pbgb_bvh_destroy(b)
+    peak, peak_kind = peak_hbm()
+    achieved = n * LBVH_BYTES_PER_BOX / (ms * 1e-3) / 1e9
+    return {
+        "workload": "LBVH build of 4,194,304 seeded boxes from device arrays (Morton, 4-pass radix sort, "
+                    "Karras, leaf gather, bottom-up boxes)",
+        "n_boxes": n,
+        "ms_per_build": ms,
+        "boxes_per_s": n / (ms * 1e-3),
+        "algorithmic_bytes_per_box": LBVH_BYTES_PER_BOX,
+        "achieved_GBs": achieved,
+        "frac_of_hbm_peak": achieved / peak,
+        "peak_kind": peak_kind,
+    }
+
+
 def config_of(args, w):
     return {
         "workload": f"beam [0,4]x[0,1]^2 {args.nx}x{args.ny}x{args.nz} hexes x 6 tets, Chebyshev rho=0.95",
@@ -443,6 +508,10 @@ def main():
                     help="skip the adjoint (bwd/fwd) measurement on the differentiation beam")
     ap.add_argument("--no-contact", dest="contact", action="store_false", default=True,
                     help="skip the contact-scene step measurement")
+    ap.add_argument("--no-lbvh", dest="lbvh", action="store_false", default=True,
+                    help="skip the LBVH build measurement")
+    ap.add_argument("--only", choices=["batch", "adjoint", "contact", "lbvh"], default=None,
+                    help="run only this secondary measurement and print its figures (no benchmark line)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -462,6 +531,17 @@ def main():
         dist.init_process_group("nccl")
 
     from physicsbasedanimationtoolkit_gb300 import _capi, pbat
+
+    if args.only:
+        legs = {
+            "batch": lambda: run_batch(args, pbat, _capi, torch),
+            "adjoint": lambda: run_adjoint(args, pbat, torch),
+            "contact": lambda: run_contact(args, pbat, torch),
+            "lbvh": lambda: run_lbvh(args, _capi, torch),
+        }
+        if rank == 0:
+            print(json.dumps({"only": args.only, args.only: legs[args.only]()}))
+        return 0
 
     w = workload_beam(args)
     data = make_data(pbat, w)
@@ -560,6 +640,7 @@ def main():
             batched = run_batch(args, pbat, _capi, torch)
         adjoint = run_adjoint(args, pbat, torch) if args.adjoint else None
         contact = run_contact(args, pbat, torch) if args.contact else None
+        lbvh = run_lbvh(args, _capi, torch) if args.lbvh else None
         launches = launches_per_step * args.steps
         line = {
             "metric": METRIC,
@@ -592,6 +673,7 @@ def main():
             "batched": batched,
             "adjoint": adjoint,
             "contact": contact,
+            "lbvh": lbvh,
         }
         print(json.dumps(line))
     if dist:

@@ -294,6 +294,13 @@ PBGB_API int pbgb_bvh_destroy(pbgb_bvh* b);
 PBGB_API int pbgb_bvh_build(pbgb_bvh* b, int32_t n, const float* lower, const float* upper, const float* wmin3, const float* wmax3);
 /* New boxes for the same n boxes, topology kept (Bvh::ConstructBoxes after a box update). */
 PBGB_API int pbgb_bvh_refit(pbgb_bvh* b, const float* lower, const float* upper);
+/* Bvh::Build from device boxes (the reference builds from device Aabb buffers,
+ * gpu/impl/geometry/Bvh.cu:116-137): lower4_dev, upper4_dev are n x 4 floats (x, y, z, unused),
+ * 16-byte aligned, on the BVH's device; read during the call only.  Asynchronous on the BVH's
+ * stream (pbgb_bvh_stream); errors of the device-side checks surface at the next host-buffer
+ * call. */
+PBGB_API int pbgb_bvh_build_device(pbgb_bvh* b, int32_t n, const float* lower4_dev, const float* upper4_dev, const float* wmin3, const float* wmax3);
+PBGB_API int pbgb_bvh_stream(pbgb_bvh* b, void** stream);
 /* Read-back: sorted codes[n], inds[n] (original box of each sorted leaf), child[2(n-1)]
  * (child[2i], child[2i+1]), parent[2n-1] (-1 at the root), rightmost[2(n-1)], internal boxes
  * 3 x (n-1).  Any output may be NULL. */

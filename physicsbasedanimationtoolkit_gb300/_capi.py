@@ -127,6 +127,8 @@ _SIGNATURES = [
     ("pbgb_bvh_destroy", C.c_int, [_vp]),
     ("pbgb_bvh_build", C.c_int, [_vp, _i32, _vp, _vp, _vp, _vp]),
     ("pbgb_bvh_refit", C.c_int, [_vp, _vp, _vp]),
+    ("pbgb_bvh_build_device", C.c_int, [_vp, _i32, _vp, _vp, _vp, _vp]),
+    ("pbgb_bvh_stream", C.c_int, [_vp, C.POINTER(_vp)]),
     ("pbgb_bvh_topology", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("pbgb_bvh_overlaps", C.c_int, [_vp, _i32, _vp, _vp, _vp, C.c_int64, C.POINTER(C.c_int64)]),
     ("pbgb_bvh_last_error", C.c_char_p, [_vp]),

@@ -71,33 +71,114 @@ __global__ void radix_count_kernel(uint32_t const* __restrict__ keys, int32_t n,
         counts[size_t(d) * tiles + tile] = hist[d];
 }
 
-// Exclusive scan of `total` counters in place by one block of 1024 threads.
-__global__ void exclusive_scan_kernel(uint32_t* __restrict__ a, int64_t total)
+// Exclusive scan of the digit counters, in place.  Each block scans kScanItems consecutive
+// counters: loaded coalesced into shared memory (padded one word per 32 so that both the strided
+// and the contiguous accesses are free of bank conflicts), kScanPer consecutive counters per
+// thread, thread totals scanned with warp shuffles, stored back coalesced; the block's total goes
+// to `sums`.  The block totals are scanned the same way (recursively) and added back.
+int constexpr kScanThreads = 256;
+int constexpr kScanPer     = 8;
+int constexpr kScanItems   = kScanThreads * kScanPer;
+
+__device__ __forceinline__ int scan_pad(int i)
 {
-    __shared__ uint32_t sums[1024];
-    int64_t const chunk = (total + blockDim.x - 1) / blockDim.x;
-    int64_t const b     = threadIdx.x * chunk;
-    int64_t const e     = b + chunk < total ? b + chunk : total;
-    uint32_t local      = 0;
-    for (int64_t k = b; k < e; ++k)
-        local += a[k];
-    sums[threadIdx.x] = local;
+    return i + (i >> 5);
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_blocks_kernel(uint32_t* __restrict__ a, int64_t total, uint32_t* __restrict__ sums)
+{
+    __shared__ uint32_t sh[kScanItems + kScanItems / 32];
+    __shared__ uint32_t warpTotal[kScanThreads / 32];
+    int64_t const base = int64_t(blockIdx.x) * kScanItems;
+    int const t        = threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j)
+    {
+        int const i      = t + j * kScanThreads;
+        int64_t const g  = base + i;
+        sh[scan_pad(i)] = g < total ? a[g] : 0u;
+    }
     __syncthreads();
-    // Hillis-Steele inclusive scan of the per-thread sums.
-    for (int off = 1; off < int(blockDim.x); off <<= 1)
+    uint32_t v[kScanPer];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j)
     {
-        uint32_t const v = threadIdx.x >= unsigned(off) ? sums[threadIdx.x - off] : 0u;
-        __syncthreads();
-        sums[threadIdx.x] += v;
-        __syncthreads();
+        v[j] = sh[scan_pad(t * kScanPer + j)];
+        sum += v[j];
     }
-    uint32_t run = threadIdx.x > 0 ? sums[threadIdx.x - 1] : 0u;
-    for (int64_t k = b; k < e; ++k)
+    int const lane = t & 31, warp = t >> 5;
+    uint32_t inc   = sum;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1)
     {
-        uint32_t const v = a[k];
-        a[k]             = run;
-        run += v;
+        uint32_t const y = __shfl_up_sync(0xffffffffu, inc, off);
+        if (lane >= off)
+            inc += y;
     }
+    if (lane == 31)
+        warpTotal[warp] = inc;
+    __syncthreads();
+    uint32_t run = inc - sum;
+    for (int w = 0; w < warp; ++w)
+        run += warpTotal[w];
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j)
+    {
+        sh[scan_pad(t * kScanPer + j)] = run;
+        run += v[j];
+    }
+    if (t == kScanThreads - 1)
+        sums[blockIdx.x] = run;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j)
+    {
+        int const i     = t + j * kScanThreads;
+        int64_t const g = base + i;
+        if (g < total)
+            a[g] = sh[scan_pad(i)];
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_add_kernel(uint32_t* __restrict__ a, int64_t total, uint32_t const* __restrict__ sums)
+{
+    int64_t const base = int64_t(blockIdx.x) * kScanItems;
+    uint32_t const off = sums[blockIdx.x];
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j)
+    {
+        int64_t const g = base + threadIdx.x + j * kScanThreads;
+        if (g < total)
+            a[g] += off;
+    }
+}
+
+// Scratch words the scan of `total` counters needs for its block totals (all levels).
+int64_t scan_tmp_size(int64_t total)
+{
+    int64_t words = 0;
+    while (total > 1)
+    {
+        total = (total + kScanItems - 1) / kScanItems;
+        words += total;
+    }
+    return words + 1;
+}
+
+cudaError_t exclusive_scan(uint32_t* a, int64_t total, uint32_t* tmp, cudaStream_t s)
+{
+    int64_t const nb = (total + kScanItems - 1) / kScanItems;
+    if (nb <= 0)
+        return cudaSuccess;
+    scan_blocks_kernel<<<unsigned(nb), kScanThreads, 0, s>>>(a, total, tmp);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || nb == 1)
+        return e;
+    if ((e = exclusive_scan(tmp, nb, tmp + nb, s)) != cudaSuccess)
+        return e;
+    scan_add_kernel<<<unsigned(nb), kScanThreads, 0, s>>>(a, total, tmp);
+    return cudaGetLastError();
 }
 
 __global__ void radix_scatter_kernel(
@@ -337,7 +418,10 @@ cudaError_t sort_impl(BvhBuffers const& B, int32_t n, float4 const* lo, float4 c
     for (int shift = 0; shift < 32; shift += 8)
     {
         radix_count_kernel<<<tiles, kSortThreads, 0, s>>>(kin, n, shift, B.counts, tiles);
-        exclusive_scan_kernel<<<1, 1024, 0, s>>>(B.counts, total);
+        if ((e = cudaGetLastError()) != cudaSuccess)
+            return e;
+        if ((e = exclusive_scan(B.counts, total, B.scanTmp, s)) != cudaSuccess)
+            return e;
         radix_scatter_kernel<<<tiles, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift, B.counts, tiles);
         if ((e = cudaGetLastError()) != cudaSuccess)
             return e;
@@ -386,6 +470,7 @@ cudaError_t bvh_allocate(BvhBuffers& B, int32_t capacity)
     get(B.inds, n);
     get(B.indsAlt, n);
     get(B.counts, size_t(radix_counts_size(capacity)));
+    get(B.scanTmp, size_t(scan_tmp_size(radix_counts_size(capacity))));
     get(B.child, 2 * ni);
     get(B.parent, 2 * n);
     get(B.rightmost, 2 * ni);
@@ -402,8 +487,8 @@ cudaError_t bvh_allocate(BvhBuffers& B, int32_t capacity)
 
 void bvh_release(BvhBuffers& B)
 {
-    void* ptrs[] = {B.codes, B.codesAlt, B.inds, B.indsAlt, B.counts, B.child, B.parent, B.rightmost,
-                    B.visits, B.ilo, B.ihi, B.llo, B.lhi, B.flags};
+    void* ptrs[] = {B.codes, B.codesAlt, B.inds, B.indsAlt, B.counts, B.scanTmp, B.child, B.parent,
+                    B.rightmost, B.visits, B.ilo, B.ihi, B.llo, B.lhi, B.flags};
     for (void* p : ptrs)
         if (p)
             cudaFree(p);

@@ -40,6 +40,7 @@ struct BvhBuffers
     int32_t* inds;      // n   sorted original indices
     int32_t* indsAlt;   // n
     uint32_t* counts;   // 256 * tiles (radix digit counts / offsets)
+    uint32_t* scanTmp;  // block totals of the counter scan (all levels)
     int32_t* child;     // 2(n-1)
     int32_t* parent;    // 2n-1
     int32_t* rightmost; // 2(n-1)

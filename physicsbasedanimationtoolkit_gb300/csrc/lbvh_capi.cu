@@ -6,6 +6,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 #include <exception>
 #include <new>
 #include <stdexcept>
@@ -191,6 +193,31 @@ PBGB_API int pbgb_bvh_build(pbgb_bvh* b, int32_t n, const float* lower, const fl
            "bvh_build");
         return b->check_flags();
     });
+}
+
+PBGB_API int pbgb_bvh_build_device(pbgb_bvh* b, int32_t n, const float* lower4, const float* upper4, const float* wmin, const float* wmax)
+{
+    if (!b)
+        return bvh_fail(nullptr, PBGB_ERR_INVALID_ARGUMENT, "null BVH");
+    if (n < 1 || n > b->capacity || !lower4 || !upper4 || !wmin || !wmax ||
+        (reinterpret_cast<uintptr_t>(lower4) & 15u) || (reinterpret_cast<uintptr_t>(upper4) & 15u))
+        return bvh_fail(b, PBGB_ERR_INVALID_ARGUMENT,
+                        "pbgb_bvh_build_device: expected 1 <= n <= capacity and 16-byte aligned device boxes");
+    return bvh_guard(b, [&] {
+        b->n = n;
+        ck(pbgb::bvh_build(b->B, n, reinterpret_cast<float4 const*>(lower4), reinterpret_cast<float4 const*>(upper4),
+                           make_float3(wmin[0], wmin[1], wmin[2]), make_float3(wmax[0], wmax[1], wmax[2]), b->stream),
+           "bvh_build");
+        return int(PBGB_OK);
+    });
+}
+
+PBGB_API int pbgb_bvh_stream(pbgb_bvh* b, void** stream)
+{
+    if (!b || !stream)
+        return bvh_fail(b, PBGB_ERR_INVALID_ARGUMENT, "null argument");
+    *stream = b->stream;
+    return PBGB_OK;
 }
 
 PBGB_API int pbgb_bvh_refit(pbgb_bvh* b, const float* lower, const float* upper)

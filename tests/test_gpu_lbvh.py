@@ -112,3 +112,32 @@ def test_refit_matches_oracle_boxes_for_same_topology():
     ilo, ihi = O.bvh_boxes(g["child"], g["inds"], lo2, hi2)
     np.testing.assert_array_equal(g["ilo"], ilo)
     np.testing.assert_array_equal(g["ihi"], ihi)
+
+
+def test_build_from_device_boxes_equals_host_build():
+    """pbgb_bvh_build_device (boxes already on the device) gives the same codes, order, topology
+    and boxes as the host-buffer build, and both equal the oracle."""
+    import ctypes as C
+
+    import torch
+
+    from physicsbasedanimationtoolkit_gb300 import _capi
+
+    rng = np.random.default_rng(21)
+    n = 20000
+    c = rng.uniform(0, 1, (n, 3)).astype(np.float32)
+    e = rng.uniform(0, 0.01, (n, 3)).astype(np.float32)
+    lo, hi = (c - e).astype(np.float32), (c + e).astype(np.float32)
+    wmin, wmax = np.zeros(3, np.float32), np.ones(3, np.float32)
+    bvh, host = gpu_build(lo, hi, wmin, wmax)
+    lo4 = torch.zeros((n, 4), device="cuda")
+    hi4 = torch.zeros((n, 4), device="cuda")
+    lo4[:, :3] = torch.from_numpy(lo).cuda()
+    hi4[:, :3] = torch.from_numpy(hi).cuda()
+    torch.cuda.synchronize()
+    L = _capi.lib()
+    _capi.check_bvh(L.pbgb_bvh_build_device(bvh._h, n, C.c_void_p(lo4.data_ptr()), C.c_void_p(hi4.data_ptr()),
+                                            wmin.ctypes.data, wmax.ctypes.data), bvh._h)
+    dev = bvh._topology()
+    assert_same(dev, host)
+    assert_same(dev, O.bvh_build(lo, hi, wmin, wmax))
