@@ -408,15 +408,18 @@ def run_contact(args, pbat, torch):
     }
 
 
-LBVH_BYTES_PER_BOX = 343  # Morton 40, 4 radix passes 83, Karras 36, leaf gather 68, boxes 116
+LBVH_BYTES_PER_BOX = 312  # Morton 40, 4 radix passes 84, Karras 36, leaf 68, internal node 84
 
 
 def run_lbvh(args, _capi, torch):
     """LBVH build over 4,194,304 seeded boxes (centres U[0,1)^3, half-extents U[0, 1e-3)) from
-    device arrays: Morton codes, the stable 4-pass radix sort, the Karras hierarchy, the leaf gather
-    and the bottom-up boxes; CUDA events on the BVH's stream.  Algorithmic bytes per box: Morton 40
-    (two boxes read, code and index written), radix 4 x 20 + digit counts 3, Karras 36, leaf gather
-    68, bottom-up boxes 116."""
+    device arrays: Morton codes, the stable 4-pass radix sort, the Karras hierarchy and the bottom-up
+    boxes (leaf gather fused in); CUDA events on the BVH's stream.  Algorithmic bytes per box:
+    Morton 40 (two boxes read, code and index written); radix 4 x (key read by the count, key and
+    index read and written by the scatter) = 80, plus ~4 of digit counters; Karras 36 (codes read,
+    children, parents and rightmost leaves written); leaf 68 (index, gathered box, leaf box
+    written); internal node 84 (visit counter cleared and added 8, children 8, sibling box 32, box
+    written 32, parent 4)."""
     n = 1 << 22
     g = torch.Generator(device="cuda")
     g.manual_seed(0)

@@ -10,6 +10,7 @@ int constexpr kSortRounds  = 16; // a tile is kSortRounds * kSortThreads consecu
 int constexpr kTile        = kSortThreads * kSortRounds;
 int constexpr kBuckets     = 256;
 int constexpr kWarps       = kSortThreads / 32;
+static_assert(kBuckets == kSortThreads, "the scatter scans the tile's digit counts one digit per thread");
 
 inline int tiles_for(int32_t n)
 {
@@ -181,7 +182,7 @@ cudaError_t exclusive_scan(uint32_t* a, int64_t total, uint32_t* tmp, cudaStream
     return cudaGetLastError();
 }
 
-__global__ void radix_scatter_kernel(
+__global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     uint32_t const* __restrict__ kin,
     int32_t const* __restrict__ vin,
     uint32_t* __restrict__ kout,
@@ -191,25 +192,64 @@ __global__ void radix_scatter_kernel(
     uint32_t const* __restrict__ offsets,
     int tiles)
 {
+    // The tile is first sorted by digit in shared memory (stable), then each digit's run is
+    // written to its global range, so consecutive threads write consecutive addresses.
+    __shared__ uint32_t skey[kTile];
+    __shared__ int32_t sval[kTile];
     __shared__ uint32_t run[kBuckets];
+    __shared__ uint32_t localStart[kBuckets];
     __shared__ uint32_t warpCount[kWarps][kBuckets];
     int const tile = blockIdx.x;
-    int const lane = threadIdx.x & 31;
-    int const warp = threadIdx.x >> 5;
-    for (int d = threadIdx.x; d < kBuckets; d += blockDim.x)
-        run[d] = offsets[size_t(d) * tiles + tile];
-    unsigned const lanesBelow = (1u << lane) - 1u;
-    int const base            = tile * kTile;
+    int const t    = threadIdx.x;
+    int const lane = t & 31;
+    int const warp = t >> 5;
+    int const base = tile * kTile;
+    uint32_t key[kSortRounds];
+    int32_t val[kSortRounds];
+    for (int d = t; d < kBuckets; d += blockDim.x)
+        run[d] = 0;
+    __syncthreads();
+#pragma unroll
     for (int r = 0; r < kSortRounds; ++r)
     {
-        for (int q = threadIdx.x; q < kWarps * kBuckets; q += blockDim.x)
+        int const i = base + r * kSortThreads + t;
+        key[r]      = i < n ? kin[i] : 0u;
+        val[r]      = i < n ? vin[i] : 0;
+        if (i < n)
+            atomicAdd(&run[(key[r] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    // Exclusive scan of the tile's digit counts (kBuckets == kSortThreads: one digit per thread).
+    {
+        uint32_t const c = run[t];
+        uint32_t inc     = c;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1)
+        {
+            uint32_t const y = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off)
+                inc += y;
+        }
+        if (lane == 31)
+            warpCount[0][warp] = inc;
+        __syncthreads();
+        uint32_t start = inc - c;
+        for (int w = 0; w < warp; ++w)
+            start += warpCount[0][w];
+        __syncthreads();
+        localStart[t] = start;
+        run[t]        = start;
+    }
+    unsigned const lanesBelow = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r)
+    {
+        for (int q = t; q < kWarps * kBuckets; q += blockDim.x)
             (&warpCount[0][0])[q] = 0;
         __syncthreads();
-        int const i       = base + r * kSortThreads + threadIdx.x;
-        bool const valid  = i < n;
-        uint32_t const k  = valid ? kin[i] : 0u;
-        int32_t const v   = valid ? vin[i] : 0;
-        uint32_t const d  = valid ? ((k >> shift) & 0xFFu) : uint32_t(kBuckets);
+        int const i          = base + r * kSortThreads + t;
+        bool const valid     = i < n;
+        uint32_t const d     = valid ? ((key[r] >> shift) & 0xFFu) : uint32_t(kBuckets);
         unsigned const peers = __match_any_sync(0xffffffffu, d);
         unsigned const rank  = __popc(peers & lanesBelow);
         if (valid && rank == 0)
@@ -220,11 +260,11 @@ __global__ void radix_scatter_kernel(
             uint32_t pos = run[d] + rank;
             for (int w = 0; w < warp; ++w)
                 pos += warpCount[w][d];
-            kout[pos] = k;
-            vout[pos] = v;
+            skey[pos] = key[r];
+            sval[pos] = val[r];
         }
         __syncthreads();
-        for (int dd = threadIdx.x; dd < kBuckets; dd += blockDim.x)
+        for (int dd = t; dd < kBuckets; dd += blockDim.x)
         {
             uint32_t add = 0;
             for (int w = 0; w < kWarps; ++w)
@@ -232,6 +272,15 @@ __global__ void radix_scatter_kernel(
             run[dd] += add;
         }
         __syncthreads();
+    }
+    int const count = n - base < kTile ? n - base : kTile;
+    for (int j = t; j < count; j += kSortThreads)
+    {
+        uint32_t const k = skey[j];
+        uint32_t const d = (k >> shift) & 0xFFu;
+        uint32_t const g = offsets[size_t(d) * tiles + tile] + (uint32_t(j) - localStart[d]);
+        kout[g]          = k;
+        vout[g]          = sval[j];
     }
 }
 
@@ -298,16 +347,6 @@ __global__ void karras_kernel(Karras K, int32_t* __restrict__ child, int32_t* __
     rightmost[2 * i + 1] = leafBegin + hi;
 }
 
-__global__ void gather_leaves_kernel(int32_t n, int32_t const* __restrict__ inds, float4 const* __restrict__ lo, float4 const* __restrict__ hi, float4* __restrict__ llo, float4* __restrict__ lhi)
-{
-    int const s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n)
-        return;
-    int const i = inds[s];
-    llo[s]      = lo[i];
-    lhi[s]      = hi[i];
-}
-
 __device__ __forceinline__ float4 fmin4(float4 a, float4 b)
 {
     return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.f);
@@ -317,32 +356,51 @@ __device__ __forceinline__ float4 fmax4(float4 a, float4 b)
     return make_float4(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), 0.f);
 }
 
-// Bottom-up internal boxes (gpu/impl/geometry/Bvh.cu:175-229): the second thread to reach a node
-// computes its box from both children and continues upward; at most 64 levels, deeper trees raise
-// kBvhErrDepth instead of looping on.
-__global__ void boxes_kernel(int32_t n, BvhBuffers B)
+// Atomic add with release and acquire semantics at device scope: the caller's earlier stores are
+// visible to the thread that later reads the counter's new value, and the caller sees the stores
+// of the threads whose additions it reads.
+__device__ __forceinline__ int atomic_add_acq_rel(int32_t* p, int v)
+{
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+// Leaf boxes in sorted order and the bottom-up internal boxes (gpu/impl/geometry/Bvh.cu:175-229).
+// Thread s gathers leaf s's box, then climbs: the first thread to reach a node stops; the second
+// unites the box it carries in registers with its sibling's (stored by the first thread before
+// that thread's counter update) and continues.  At most 64 levels; deeper trees raise
+// kBvhErrDepth instead of looping on.  Min and max are exact and commutative, so the boxes do not
+// depend on which child's thread goes on.
+__global__ void boxes_kernel(int32_t n, BvhBuffers B, float4 const* __restrict__ lo, float4 const* __restrict__ hi)
 {
     int const s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n)
         return;
     int32_t const leafBegin = n - 1;
-    int32_t p               = B.parent[leafBegin + s];
-    int k                   = 0;
+    int32_t const i         = B.inds[s];
+    float4 bl               = lo[i];
+    float4 bh               = hi[i];
+    __stcg(&B.llo[s], bl);
+    __stcg(&B.lhi[s], bh);
+    int32_t node = leafBegin + s;
+    int32_t p    = B.parent[node];
+    int k        = 0;
     for (; k < 64 && p >= 0; ++k)
     {
-        __threadfence();
-        if (atomicAdd(&B.visits[p], 1) == 0)
+        if (atomic_add_acq_rel(&B.visits[p], 1) == 0)
             return;
-        __threadfence();
-        int32_t const lc = __ldcg(&B.child[2 * p]);
-        int32_t const rc = __ldcg(&B.child[2 * p + 1]);
-        float4 const llo = lc >= leafBegin ? __ldcg(&B.llo[lc - leafBegin]) : __ldcg(&B.ilo[lc]);
-        float4 const lhi = lc >= leafBegin ? __ldcg(&B.lhi[lc - leafBegin]) : __ldcg(&B.ihi[lc]);
-        float4 const rlo = rc >= leafBegin ? __ldcg(&B.llo[rc - leafBegin]) : __ldcg(&B.ilo[rc]);
-        float4 const rhi = rc >= leafBegin ? __ldcg(&B.lhi[rc - leafBegin]) : __ldcg(&B.ihi[rc]);
-        __stcg(&B.ilo[p], fmin4(llo, rlo));
-        __stcg(&B.ihi[p], fmax4(lhi, rhi));
-        p = __ldcg(&B.parent[p]);
+        int32_t const lc  = B.child[2 * p];
+        int32_t const rc  = B.child[2 * p + 1];
+        int32_t const sib = lc == node ? rc : lc;
+        float4 const sl   = sib >= leafBegin ? __ldcg(&B.llo[sib - leafBegin]) : __ldcg(&B.ilo[sib]);
+        float4 const sh   = sib >= leafBegin ? __ldcg(&B.lhi[sib - leafBegin]) : __ldcg(&B.ihi[sib]);
+        bl                = fmin4(bl, sl);
+        bh                = fmax4(bh, sh);
+        __stcg(&B.ilo[p], bl);
+        __stcg(&B.ihi[p], bh);
+        node = p;
+        p    = B.parent[p];
     }
     if (k == 64 && p >= 0)
         atomicOr(B.flags, kBvhErrDepth);
@@ -436,14 +494,17 @@ cudaError_t sort_impl(BvhBuffers const& B, int32_t n, float4 const* lo, float4 c
     return cudaSuccess;
 }
 
-cudaError_t boxes_impl(BvhBuffers const& B, int32_t n, cudaStream_t s)
+cudaError_t boxes_impl(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, cudaStream_t s)
 {
-    if (n < 2)
+    if (n < 1)
         return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(B.visits, 0, sizeof(int32_t) * size_t(n - 1), s);
-    if (e != cudaSuccess)
-        return e;
-    boxes_kernel<<<blocks(n, 256), 256, 0, s>>>(n, B);
+    if (n > 1)
+    {
+        cudaError_t const e = cudaMemsetAsync(B.visits, 0, sizeof(int32_t) * size_t(n - 1), s);
+        if (e != cudaSuccess)
+            return e;
+    }
+    boxes_kernel<<<blocks(n, 256), 256, 0, s>>>(n, B, lo, hi);
     return cudaGetLastError();
 }
 
@@ -507,7 +568,9 @@ cudaError_t bvh_build(BvhBuffers const& B, int32_t n, float4 const* lo, float4 c
     cudaError_t e = sort_impl(B, n, lo, hi, wmin, wmax, s);
     if (e != cudaSuccess)
         return e;
-    if ((e = cudaMemsetAsync(B.parent, 0xFF, sizeof(int32_t) * size_t(2 * n - 1), s)) != cudaSuccess)
+    // The root has no parent; every other node is the child of exactly one internal node, whose
+    // Karras thread writes its parent.
+    if ((e = cudaMemsetAsync(B.parent, 0xFF, sizeof(int32_t), s)) != cudaSuccess)
         return e;
     if (n > 1)
     {
@@ -515,21 +578,14 @@ cudaError_t bvh_build(BvhBuffers const& B, int32_t n, float4 const* lo, float4 c
         if ((e = cudaGetLastError()) != cudaSuccess)
             return e;
     }
-    gather_leaves_kernel<<<blocks(n, 256), 256, 0, s>>>(n, B.inds, lo, hi, B.llo, B.lhi);
-    if ((e = cudaGetLastError()) != cudaSuccess)
-        return e;
-    return boxes_impl(B, n, s);
+    return boxes_impl(B, n, lo, hi, s);
 }
 
 cudaError_t bvh_refit(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, cudaStream_t s)
 {
     if (n <= 0)
         return cudaSuccess;
-    gather_leaves_kernel<<<blocks(n, 256), 256, 0, s>>>(n, B.inds, lo, hi, B.llo, B.lhi);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess)
-        return e;
-    return boxes_impl(B, n, s);
+    return boxes_impl(B, n, lo, hi, s);
 }
 
 cudaError_t bvh_overlaps(
