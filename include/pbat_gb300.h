@@ -201,6 +201,12 @@ PBGB_API int pbgb_vbd_autotune(
 /* Programmatic dependent launch of the colour sweeps (default on): each colour's kernel loads its
  * mesh tables while the previous colour drains, then waits before reading positions. */
 PBGB_API int pbgb_vbd_set_programmatic_launch(pbgb_vbd* h, int32_t enable);
+/* Staged colour sweep (default on): each vertex's distinct neighbours are loaded once into shared
+ * memory instead of three corners per incident tet; same arithmetic, same results.  Unavailable
+ * (the gathering sweep runs) when a vertex has more than 256 neighbours; a colour whose blocks
+ * would need more than 200 KB of shared memory also runs the gathering sweep. */
+PBGB_API int pbgb_vbd_set_staged_sweep(pbgb_vbd* h, int32_t enable);
+PBGB_API int pbgb_vbd_staged_sweep(pbgb_vbd* h, int32_t* available, int32_t* enabled);
 PBGB_API int pbgb_vbd_set_scene_bounding_box(pbgb_vbd* h, const float* min3, const float* max3);
 
 /* Sizes and launch bookkeeping. */

@@ -111,6 +111,8 @@ _SIGNATURES = [
     ("pbgb_vbd_set_lanes_per_vertex", C.c_int, [_vp, _i32]),
     ("pbgb_vbd_autotune", C.c_int, [_vp, _f32, _i32, _i32, _vp, _vp, _vp]),
     ("pbgb_vbd_set_programmatic_launch", C.c_int, [_vp, _i32]),
+    ("pbgb_vbd_set_staged_sweep", C.c_int, [_vp, _i32]),
+    ("pbgb_vbd_staged_sweep", C.c_int, [_vp, C.POINTER(_i32), C.POINTER(_i32)]),
     ("pbgb_vbd_set_scene_bounding_box", C.c_int, [_vp, _vp, _vp]),
     ("pbgb_vbd_sizes", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     ("pbgb_vbd_launches_per_step", C.c_int, [_vp, _i32, _i32, C.POINTER(C.c_int64)]),

@@ -162,6 +162,17 @@ class IntegratorBase:
         _capi.check(_capi.lib().pbgb_vbd_set_lanes_per_vertex(self._h, int(lanes)), self._h)
         self._lanes = int(lanes)
 
+    @property
+    def staged_sweep(self):
+        """(available, enabled) of the staged colour sweep (neighbours in shared memory)."""
+        av, en = C.c_int32(), C.c_int32()
+        _capi.check(_capi.lib().pbgb_vbd_staged_sweep(self._h, C.byref(av), C.byref(en)), self._h)
+        return bool(av.value), bool(en.value)
+
+    @staged_sweep.setter
+    def staged_sweep(self, enable):
+        _capi.check(_capi.lib().pbgb_vbd_set_staged_sweep(self._h, int(bool(enable))), self._h)
+
     def autotune(self, dt, iterations, substeps=1):
         """Pick lanes per vertex and block size by timing one step of each candidate (state is
         restored); returns (lanes, block_size, ms_per_step)."""

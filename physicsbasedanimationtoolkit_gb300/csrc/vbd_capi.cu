@@ -106,6 +106,15 @@ class VbdSystem
     DeviceArray<TetRecord> tets;
     DeviceArray<int32_t> solve, incPtr, flags;
     DeviceArray<uint32_t> inc;
+    // Staged sweep: per free vertex its distinct neighbours, per incidence (tet, neighbour slots),
+    // per tet its material words.  stagedOk is false when some vertex has more than 256
+    // neighbours (slots are bytes); `staged` is the user's choice.
+    bool stagedOk = false, staged = true;
+    std::vector<int32_t> hostNbrPtr;
+    DeviceArray<int32_t> nbrPtr;
+    DeviceArray<uint32_t> nbr;
+    DeviceArray<uint2> incPack;
+    DeviceArray<float4> mats;
     DeviceArray<double> red, gradBuf;
 
     // Sweep timing: with `profiling` on, the captured step records an event pair around the colour
@@ -247,6 +256,22 @@ class VbdSystem
             total += ms;
         }
         return total;
+    }
+
+    // Staged-sweep fields of a SweepParams, and the shared memory of colour c's launch (0: gather).
+    void stagedFields(SweepParams& w) const
+    {
+        w.nbrPtr  = nbrPtr.get();
+        w.nbr     = nbr.get();
+        w.incPack = incPack.get();
+        w.mats    = mats.get();
+    }
+    size_t stagedBytes(int32_t c, int L) const
+    {
+        if (!stagedOk || !staged)
+            return 0;
+        size_t const bytes = staged_sweep_bytes(hostNbrPtr.data(), colorPtr[c], colorPtr[c + 1], L, block);
+        return bytes <= kStagedMaxBytes ? bytes : 0;
     }
 
     int lanesToUse() const
@@ -430,6 +455,48 @@ class VbdSystem
         }
         meanDegree = nFree > 0 ? double(degSum) / nFree : 0.0;
 
+        // Neighbour lists of the staged sweep, in first-use order over the vertex's incidences and
+        // corners ((local + 1 + m) & 3, the order the sweep visits them).
+        std::vector<uint32_t> hNbr;
+        std::vector<uint2> hPack(hInc.size());
+        hostNbrPtr.assign(size_t(nFree) + 1, 0);
+        stagedOk = true;
+        {
+            std::vector<uint32_t> list;
+            for (int32_t s = 0; s < nFree && stagedOk; ++s)
+            {
+                list.clear();
+                for (int32_t k = hIncPtr[s]; k < hIncPtr[s + 1]; ++k)
+                {
+                    uint32_t const q  = hInc[k];
+                    uint4 const t     = hrec[q >> 2].v;
+                    int const il      = int(q & 3u);
+                    uint32_t const c4[4] = {t.x, t.y, t.z, t.w};
+                    uint32_t const own = c4[il] >> 30;
+                    uint32_t slots     = 0;
+                    for (int m = 0; m < 3; ++m)
+                    {
+                        uint32_t const ca = c4[(il + 1 + m) & 3];
+                        uint32_t const a  = (ca & kIndexMask) | ((ca >> 30) < own ? 0x80000000u : 0u);
+                        size_t idx        = 0;
+                        while (idx < list.size() && list[idx] != a)
+                            ++idx;
+                        if (idx == list.size())
+                            list.push_back(a);
+                        slots |= uint32_t(idx) << (8 * m);
+                    }
+                    hPack[k] = make_uint2(q >> 2, slots);
+                }
+                if (list.size() > 256)
+                    stagedOk = false;
+                hNbr.insert(hNbr.end(), list.begin(), list.end());
+                hostNbrPtr[s + 1] = int32_t(hNbr.size());
+            }
+        }
+        std::vector<float4> hMats(hrec.size());
+        for (size_t e = 0; e < hrec.size(); ++e)
+            hMats[e] = hrec[e].mat;
+
         // Device allocation and upload.
         check(cudaGetDevice(&device), "cudaGetDevice");
         check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -462,6 +529,20 @@ class VbdSystem
         solve.upload(hsolve.data(), nFree, stream);
         incPtr.upload(hIncPtr.data(), hIncPtr.size(), stream);
         inc.upload(hInc.data(), hInc.size(), stream);
+        if (stagedOk)
+        {
+            nbrPtr.allocate(hostNbrPtr.size());
+            nbr.allocate(hNbr.size());
+            incPack.allocate(hPack.size());
+            mats.allocate(hMats.size());
+            nbrPtr.upload(hostNbrPtr.data(), hostNbrPtr.size(), stream);
+            nbr.upload(hNbr.data(), hNbr.size(), stream);
+            incPack.upload(hPack.data(), hPack.size(), stream);
+            mats.upload(hMats.data(), hMats.size(), stream);
+            check(prepare_staged_sweeps(), "cudaFuncSetAttribute");
+        }
+        else
+            hostNbrPtr.clear();
         if (nV > 0)
         {
             check(cudaMemcpyAsync(xt.get(), x.get(), sizeof(float4) * nV, cudaMemcpyDeviceToDevice, stream), "copy");
@@ -589,7 +670,14 @@ class VbdSystem
             hostRecords[e].mat = make_float4(float(w * mu[e]), float(w * lambda[e]), float(1.0 + mu[e] / lambda[e]), 0.f);
         }
         tets.upload(hostRecords.data(), size_t(nT), stream);
-        // The upload reads hostRecords asynchronously.
+        std::vector<float4> hMats(static_cast<size_t>(nT));
+        if (stagedOk)
+        {
+            for (int32_t e = 0; e < nT; ++e)
+                hMats[e] = hostRecords[e].mat;
+            mats.upload(hMats.data(), size_t(nT), stream);
+        }
+        // The uploads read the host arrays asynchronously.
         check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
     }
 
@@ -681,6 +769,7 @@ class VbdSystem
         w.solve    = solve.get();
         w.incPtr   = incPtr.get();
         w.inc      = inc.get();
+        stagedFields(w);
         w.h        = h;
         w.h2       = h * h;
         w.kD       = kD;
@@ -704,7 +793,7 @@ class VbdSystem
                     w.color = c;
                     // The first colour follows the copy of x into the tape (not a kernel): no programmatic
                     // launch there, so that it cannot overwrite x while the copy reads it.
-                    check(launch_sweep_record(w, L, block, pdl && c > 0, stream), "sweep_record");
+                    check(launch_sweep_record(w, L, block, pdl && c > 0, stream, stagedBytes(c, L)), "sweep_record");
                 }
                 if (nV > 0)
                     check(cudaMemcpyAsync(slotX(slot, k + 1), x.get(), bytes, cudaMemcpyDeviceToDevice, stream), "tape copy");
@@ -840,6 +929,7 @@ class VbdSystem
         w.solve    = solve.get();
         w.incPtr   = incPtr.get();
         w.inc      = inc.get();
+        stagedFields(w);
         w.h        = h;
         w.h2       = h2;
         w.kD       = kD;
@@ -896,7 +986,7 @@ class VbdSystem
                     w.begin = colorPtr[c];
                     w.end   = colorPtr[c + 1];
                     w.color = c;
-                    check(launch_sweep(w, L, block, twoBuffer, pdl, stream), "sweep");
+                    check(launch_sweep(w, L, block, twoBuffer, pdl, stream, stagedBytes(c, L)), "sweep");
                 }
                 if (profiling)
                     check(cudaEventRecordWithFlags(evEnd[slot], stream, cudaEventRecordExternal), "cudaEventRecord");
@@ -1507,6 +1597,26 @@ PBGB_API int pbgb_vbd_autotune(
             *ms_per_step = ms;
         return int(kOk);
     });
+}
+
+PBGB_API int pbgb_vbd_set_staged_sweep(pbgb_vbd* h, int32_t enable)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    h->sys.staged = enable != 0;
+    h->sys.invalidate();
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_staged_sweep(pbgb_vbd* h, int32_t* available, int32_t* enabled)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (available)
+        *available = h->sys.stagedOk ? 1 : 0;
+    if (enabled)
+        *enabled = h->sys.staged ? 1 : 0;
+    return kOk;
 }
 
 PBGB_API int pbgb_vbd_set_programmatic_launch(pbgb_vbd* h, int32_t enable)

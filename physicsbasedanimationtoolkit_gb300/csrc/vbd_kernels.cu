@@ -1,6 +1,7 @@
 // CUDA kernels of the VBD step (sm_103a).  See vbd_kernels.cuh for the data layout.
 #include "vbd_kernels.cuh"
 
+#include <algorithm>
 #include <cfloat>
 
 namespace pbgb {
@@ -54,6 +55,70 @@ __device__ __noinline__ void add_contacts(SweepParams const& p, int i, float con
         }
         vertex_triangle_contact(xt, xi, xtf, xf, p.h, kC * p.FA[f[c]], p.muF, p.epsv, FLT_EPSILON, g, H);
     }
+}
+
+// The end of a vertex solve, shared by both sweep kernels: xor-shuffle reduction of the lanes'
+// 10 accumulated floats, then lane 0 applies damping, contact, inertia and the 3x3 Newton step and
+// writes the iterate(s).
+template <int L, bool CHEB, bool REC>
+__device__ __forceinline__ void finish_vertex(SweepParams const& p, VertexBlock<float>& b, bool valid, int lane, int i, int s, float* xi)
+{
+#pragma unroll
+    for (int off = L / 2; off > 0; off >>= 1)
+    {
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            b.g[r] += __shfl_xor_sync(0xffffffffu, b.g[r], off);
+        b.s += __shfl_xor_sync(0xffffffffu, b.s, off);
+#pragma unroll
+        for (int r = 0; r < 6; ++r)
+            b.C[r] += __shfl_xor_sync(0xffffffffu, b.C[r], off);
+    }
+    if (!valid || lane != 0)
+        return;
+    float4 const xt4  = p.xt[i];
+    float4 const xl4  = p.xtilde[i];
+    float const xt[3] = {xt4.x, xt4.y, xt4.z};
+    float const xl[3] = {xl4.x, xl4.y, xl4.z};
+    float H[6], g[3];
+    elastic_system(b, xt, xi, p.h, p.kD, H, g);
+    if (CHEB && p.fc)
+        add_contacts(p, i, xt, xi, H, g);
+    bool const moved = inertia_solve(H, g, xl, xt4.w, p.h2, p.detHZero, xi);
+    if (REC)
+    {
+        // H now includes the inertia term; its inverse by the adjugate, as in inertia_solve.
+        float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
+        if (moved)
+        {
+            float const a00 = H[3] * H[5] - H[4] * H[4];
+            float const a01 = H[2] * H[4] - H[1] * H[5];
+            float const a02 = H[1] * H[4] - H[2] * H[3];
+            float const a11 = H[0] * H[5] - H[2] * H[2];
+            float const a12 = H[1] * H[2] - H[0] * H[4];
+            float const a22 = H[0] * H[3] - H[1] * H[1];
+            float const inv = 1.f / (H[0] * a00 + H[1] * a01 + H[2] * a02);
+            r0 = make_float4(inv * a00, inv * a01, inv * a02, inv * a11);
+            r1 = make_float4(inv * a12, inv * a22, 0.f, 0.f);
+        }
+        p.tape[2 * s]     = r0;
+        p.tape[2 * s + 1] = r1;
+    }
+    if (CHEB)
+    {
+        // Raw iterate k (even when the Newton step was skipped: later colours read it).
+        p.x[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
+        if (p.k > 1)
+        {
+            float4 const km2 = p.hcur[i];
+            xi[0]            = p.omega * (xi[0] - km2.x) + km2.x;
+            xi[1]            = p.omega * (xi[1] - km2.y) + km2.y;
+            xi[2]            = p.omega * (xi[2] - km2.z) + km2.z;
+        }
+        p.hcur[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
+    }
+    else if (moved)
+        p.x[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
 }
 
 // Per-colour Gauss-Seidel sweep (reference: VbdIteration, gpu/impl/vbd/Kernels.cuh:148-233, and
@@ -152,62 +217,101 @@ __global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
             mat = matn;
         }
     }
-#pragma unroll
-    for (int off = L / 2; off > 0; off >>= 1)
+    finish_vertex<L, CHEB, REC>(p, b, valid, lane, i, s, xi);
+}
+
+// The same sweep with each vertex's neighbours staged in shared memory.  A vertex's ~23 incident
+// tets reference only ~14 distinct neighbours, so instead of gathering three corners' current
+// and rest positions per incidence, the vertex's lanes load each neighbour once into its slice of
+// the block's slab (rest positions before griddepcontrol.wait: no launch writes them; current
+// positions after it), and the incidence loop reads them back through the three slot bytes of its
+// packed incidence word.  The slab slice of solve entry s starts at nbrPtr[s] - nbrPtr[first
+// entry of the block]; the lanes of a vertex share a warp, so __syncwarp orders the staging.
+template <int L, bool CHEB, bool REC = false>
+__global__ void __launch_bounds__(256, 4) staged_sweep_kernel(SweepParams p)
+{
+    extern __shared__ float4 slab[]; // per staged neighbour: position, rest position
+    int const tid    = blockIdx.x * blockDim.x + threadIdx.x;
+    int const s      = p.begin + tid / L;
+    int const lane   = tid & (L - 1);
+    bool const valid = s < p.end;
+    // The block's first entry is valid: the grid covers exactly (end - begin) * L threads.
+    int const first = p.begin + int(blockIdx.x) * (int(blockDim.x) / L);
+    int const nb0   = __ldg(p.nbrPtr + first);
+
+    VertexBlock<float> b;
+    zero(b);
+    int i       = 0;
+    float xi[3] = {0.f, 0.f, 0.f};
+    float Xi[3] = {0.f, 0.f, 0.f};
+    int k = 0, k1 = 0, n0 = 0, n1 = 0, base = 0;
+    uint2 q     = make_uint2(0u, 0u);
+    float4 mat  = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid)
     {
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-            b.g[r] += __shfl_xor_sync(0xffffffffu, b.g[r], off);
-        b.s += __shfl_xor_sync(0xffffffffu, b.s, off);
-#pragma unroll
-        for (int r = 0; r < 6; ++r)
-            b.C[r] += __shfl_xor_sync(0xffffffffu, b.C[r], off);
-    }
-    if (!valid || lane != 0)
-        return;
-    float4 const xt4  = p.xt[i];
-    float4 const xl4  = p.xtilde[i];
-    float const xt[3] = {xt4.x, xt4.y, xt4.z};
-    float const xl[3] = {xl4.x, xl4.y, xl4.z};
-    float H[6], g[3];
-    elastic_system(b, xt, xi, p.h, p.kD, H, g);
-    if (CHEB && p.fc)
-        add_contacts(p, i, xt, xi, H, g);
-    bool const moved = inertia_solve(H, g, xl, xt4.w, p.h2, p.detHZero, xi);
-    if (REC)
-    {
-        // H now includes the inertia term; its inverse by the adjugate, as in inertia_solve.
-        float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
-        if (moved)
+        i  = __ldg(p.solve + s);
+        load3(__ldg(p.X + i), Xi);
+        n0   = __ldg(p.nbrPtr + s);
+        n1   = __ldg(p.nbrPtr + s + 1);
+        base = n0 - nb0;
+        for (int j = n0 + lane; j < n1; j += L)
+            slab[2 * (base + j - n0) + 1] = __ldg(p.X + (__ldg(p.nbr + j) & kIndexMask));
+        k1 = __ldg(p.incPtr + s + 1);
+        k  = __ldg(p.incPtr + s) + lane;
+        if (k < k1)
         {
-            float const a00 = H[3] * H[5] - H[4] * H[4];
-            float const a01 = H[2] * H[4] - H[1] * H[5];
-            float const a02 = H[1] * H[4] - H[2] * H[3];
-            float const a11 = H[0] * H[5] - H[2] * H[2];
-            float const a12 = H[1] * H[2] - H[0] * H[4];
-            float const a22 = H[0] * H[3] - H[1] * H[1];
-            float const inv = 1.f / (H[0] * a00 + H[1] * a01 + H[2] * a02);
-            r0 = make_float4(inv * a00, inv * a01, inv * a02, inv * a11);
-            r1 = make_float4(inv * a12, inv * a22, 0.f, 0.f);
+            q   = __ldg(p.incPack + k);
+            mat = __ldg(p.mats + q.x);
         }
-        p.tape[2 * s]     = r0;
-        p.tape[2 * s + 1] = r1;
     }
-    if (CHEB)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    if (valid)
     {
-        // Raw iterate k (even when the Newton step was skipped: later colours read it).
-        p.x[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
-        if (p.k > 1)
+        load3(CHEB ? p.hprev[i] : p.x[i], xi);
+        for (int j = n0 + lane; j < n1; j += L)
         {
-            float4 const km2 = p.hcur[i];
-            xi[0]            = p.omega * (xi[0] - km2.x) + km2.x;
-            xi[1]            = p.omega * (xi[1] - km2.y) + km2.y;
-            xi[2]            = p.omega * (xi[2] - km2.z) + km2.z;
+            uint32_t const a  = __ldg(p.nbr + j);
+            float4 const* src = p.x;
+            if (CHEB && !(a >> 31))
+                src = p.hprev;
+            slab[2 * (base + j - n0)] = __ldg(src + (a & kIndexMask));
         }
-        p.hcur[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
     }
-    else if (moved)
-        p.x[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
+    __syncwarp();
+    if (valid)
+    {
+        for (; k < k1; k += L)
+        {
+            uint2 qn     = make_uint2(0u, 0u);
+            float4 matn  = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k + L < k1)
+            {
+                qn   = __ldg(p.incPack + k + L);
+                matn = __ldg(p.mats + qn.x);
+            }
+            float d[3][3], e[3][3];
+#pragma unroll
+            for (int m = 0; m < 3; ++m)
+            {
+                int const slot   = base + int((q.y >> (8 * m)) & 0xFFu);
+                float4 const xa  = slab[2 * slot];
+                float4 const Xa  = slab[2 * slot + 1];
+                d[m][0] = xa.x - xi[0];
+                d[m][1] = xa.y - xi[1];
+                d[m][2] = xa.z - xi[2];
+                e[m][0] = Xa.x - Xi[0];
+                e[m][1] = Xa.y - Xi[1];
+                e[m][2] = Xa.z - Xi[2];
+            }
+            float G[3][3];
+            rest_gradients(e, G);
+            accumulate_tet(b, d, G, mat.x, mat.y, mat.z);
+            q   = qn;
+            mat = matn;
+        }
+    }
+    finish_vertex<L, CHEB, REC>(p, b, valid, lane, i, s, xi);
 }
 
 // Start of a substep (sim/vbd/Integrator.cpp:31-34,54-71; gpu/impl/vbd/Integrator.cu:190-248):
@@ -419,64 +523,103 @@ inline int blocks_for(int64_t n, int block)
 } // namespace
 
 template <int L, bool CHEB, bool REC = false>
-cudaError_t launch_sweep_l(SweepParams const& p, int g, int block, bool pdl, cudaStream_t s)
+cudaError_t launch_sweep_l(SweepParams const& p, int g, int block, bool pdl, cudaStream_t s, size_t stagedBytes)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim            = dim3(unsigned(g));
     cfg.blockDim           = dim3(unsigned(block));
-    cfg.dynamicSmemBytes   = 0;
+    cfg.dynamicSmemBytes   = stagedBytes;
     cfg.stream             = s;
     cudaLaunchAttribute attr[1];
     attr[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs                                          = attr;
     cfg.numAttrs                                       = pdl ? 1 : 0;
+    if (stagedBytes > 0)
+        return cudaLaunchKernelEx(&cfg, staged_sweep_kernel<L, CHEB, REC>, p);
     return cudaLaunchKernelEx(&cfg, sweep_kernel<L, CHEB, REC>, p);
 }
 
-template <bool CHEB>
-cudaError_t launch_sweep_t(SweepParams const& p, int lanes, int g, int block, bool pdl, cudaStream_t s)
+template <bool CHEB, bool REC>
+cudaError_t launch_sweep_t(SweepParams const& p, int lanes, int g, int block, bool pdl, cudaStream_t s, size_t stagedBytes)
 {
     switch (lanes)
     {
-        case 1: return launch_sweep_l<1, CHEB>(p, g, block, pdl, s);
-        case 2: return launch_sweep_l<2, CHEB>(p, g, block, pdl, s);
-        case 4: return launch_sweep_l<4, CHEB>(p, g, block, pdl, s);
-        case 8: return launch_sweep_l<8, CHEB>(p, g, block, pdl, s);
-        case 16: return launch_sweep_l<16, CHEB>(p, g, block, pdl, s);
-        case 32: return launch_sweep_l<32, CHEB>(p, g, block, pdl, s);
+        case 1: return launch_sweep_l<1, CHEB, REC>(p, g, block, pdl, s, stagedBytes);
+        case 2: return launch_sweep_l<2, CHEB, REC>(p, g, block, pdl, s, stagedBytes);
+        case 4: return launch_sweep_l<4, CHEB, REC>(p, g, block, pdl, s, stagedBytes);
+        case 8: return launch_sweep_l<8, CHEB, REC>(p, g, block, pdl, s, stagedBytes);
+        case 16: return launch_sweep_l<16, CHEB, REC>(p, g, block, pdl, s, stagedBytes);
+        case 32: return launch_sweep_l<32, CHEB, REC>(p, g, block, pdl, s, stagedBytes);
         default: return cudaErrorInvalidValue;
     }
 }
 
-cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, bool pdl, cudaStream_t s)
+cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, bool pdl, cudaStream_t s, size_t stagedBytes)
 {
     int64_t const n = int64_t(p.end - p.begin) * lanes;
     if (n <= 0)
         return cudaSuccess;
-    int const g = blocks_for(n, block);
-    return chebyshev ? launch_sweep_t<true>(p, lanes, g, block, pdl, s)
-                     : launch_sweep_t<false>(p, lanes, g, block, pdl, s);
-}
-
-cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool pdl, cudaStream_t s)
-{
-    int64_t const n = int64_t(p.end - p.begin) * lanes;
-    if (n <= 0)
-        return cudaSuccess;
-    if (!p.tape)
+    if (stagedBytes > kStagedMaxBytes || (stagedBytes > 0 && (!p.nbrPtr || !p.nbr || !p.incPack || !p.mats)))
         return cudaErrorInvalidValue;
     int const g = blocks_for(n, block);
-    switch (lanes)
+    return chebyshev ? launch_sweep_t<true, false>(p, lanes, g, block, pdl, s, stagedBytes)
+                     : launch_sweep_t<false, false>(p, lanes, g, block, pdl, s, stagedBytes);
+}
+
+cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool pdl, cudaStream_t s, size_t stagedBytes)
+{
+    int64_t const n = int64_t(p.end - p.begin) * lanes;
+    if (n <= 0)
+        return cudaSuccess;
+    if (!p.tape || stagedBytes > kStagedMaxBytes || (stagedBytes > 0 && (!p.nbrPtr || !p.nbr || !p.incPack || !p.mats)))
+        return cudaErrorInvalidValue;
+    return launch_sweep_t<false, true>(p, lanes, blocks_for(n, block), block, pdl, s, stagedBytes);
+}
+
+size_t staged_sweep_bytes(int32_t const* nbrPtr, int32_t begin, int32_t end, int lanes, int block)
+{
+    int const per = block / lanes;
+    if (per <= 0)
+        return 0;
+    int64_t most = 0;
+    for (int32_t b0 = begin; b0 < end; b0 += per)
     {
-        case 1: return launch_sweep_l<1, false, true>(p, g, block, pdl, s);
-        case 2: return launch_sweep_l<2, false, true>(p, g, block, pdl, s);
-        case 4: return launch_sweep_l<4, false, true>(p, g, block, pdl, s);
-        case 8: return launch_sweep_l<8, false, true>(p, g, block, pdl, s);
-        case 16: return launch_sweep_l<16, false, true>(p, g, block, pdl, s);
-        case 32: return launch_sweep_l<32, false, true>(p, g, block, pdl, s);
-        default: return cudaErrorInvalidValue;
+        int32_t const b1 = b0 + per < end ? b0 + per : end;
+        most             = std::max<int64_t>(most, int64_t(nbrPtr[b1]) - nbrPtr[b0]);
     }
+    return size_t(most) * 2 * sizeof(float4);
+}
+
+namespace {
+
+template <bool CHEB, bool REC>
+cudaError_t allow_staged_smem()
+{
+    cudaError_t e = cudaSuccess;
+    auto set      = [&](auto kernel) {
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kStagedMaxBytes));
+    };
+    set(staged_sweep_kernel<1, CHEB, REC>);
+    set(staged_sweep_kernel<2, CHEB, REC>);
+    set(staged_sweep_kernel<4, CHEB, REC>);
+    set(staged_sweep_kernel<8, CHEB, REC>);
+    set(staged_sweep_kernel<16, CHEB, REC>);
+    set(staged_sweep_kernel<32, CHEB, REC>);
+    return e;
+}
+
+} // namespace
+
+cudaError_t prepare_staged_sweeps()
+{
+    cudaError_t e = allow_staged_smem<false, false>();
+    if (e == cudaSuccess)
+        e = allow_staged_smem<true, false>();
+    if (e == cudaSuccess)
+        e = allow_staged_smem<false, true>();
+    return e;
 }
 
 cudaError_t launch_begin_substep(SubstepParams const& p, cudaStream_t s)

@@ -65,6 +65,15 @@ struct SweepParams
     float muC;
     float muF;
     float epsv;
+    // Neighbour staging (staged sweep only): for solve-list entry s, its distinct neighbours
+    // nbr[nbrPtr[s] .. nbrPtr[s+1]) (vertex index in bits 0-29, bit 31 set when the neighbour has a
+    // lower colour, so that the two-buffer sweep reads it from x rather than hprev); per incidence
+    // k, incPack[k] = (tet, slots) with the three other corners' positions in that list in bytes
+    // 0-2 (corner order (local + 1 + m) & 3); mats[tet] = the record's material words.
+    int32_t const* __restrict__ nbrPtr;
+    uint32_t const* __restrict__ nbr;
+    uint2 const* __restrict__ incPack;
+    float4 const* __restrict__ mats;
     // Adjoint tape of this iteration (recording sweeps only): for solve-list entry s, the inverse
     // of the vertex's 3x3 Newton matrix (xx xy xz yy | yz zz 0 0) in tape[2s], tape[2s+1]; zero
     // when the Newton step was skipped.
@@ -108,10 +117,21 @@ struct EnergyParams
 // pdl: launch with programmatic stream serialization, so that the kernel's mesh-table prologue
 // overlaps the tail of the previous launch on the stream (the kernel waits before reading
 // positions).
-cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, bool pdl, cudaStream_t s);
+// stagedBytes > 0: the staged sweep (neighbours in shared memory), with that much dynamic shared
+// memory per block (staged_sweep_bytes); 0: the sweep that gathers every incidence's corners.  Both
+// compute the same arithmetic in the same order.
+cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, bool pdl, cudaStream_t s, size_t stagedBytes = 0);
 // The plain (one-buffer) sweep that also writes p.tape; the same arithmetic as launch_sweep with
 // chebyshev = false, so a recorded step reproduces an unrecorded one.
-cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool pdl, cudaStream_t s);
+cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool pdl, cudaStream_t s, size_t stagedBytes = 0);
+// Dynamic shared memory of the staged sweep over solve entries [begin, end) with `lanes` lanes per
+// vertex and `block` threads per block: 32 bytes per staged neighbour of the block that stages the
+// most (nbrPtr on the host).
+size_t staged_sweep_bytes(int32_t const* nbrPtr, int32_t begin, int32_t end, int lanes, int block);
+// Largest dynamic shared memory a staged sweep may use (set on the current device by
+// prepare_staged_sweeps); larger launches fall back to the gathering sweep.
+size_t constexpr kStagedMaxBytes = 200 * 1024;
+cudaError_t prepare_staged_sweeps();
 cudaError_t launch_begin_substep(SubstepParams const& p, cudaStream_t s);
 cudaError_t launch_end_substep(SubstepParams const& p, cudaStream_t s);
 cudaError_t launch_objective(EnergyParams const& p, cudaStream_t s);

@@ -139,3 +139,18 @@ def test_contact_scene_of_sixteen_cubes_runs():
     fc, active = I.contacts()
     assert active.sum() > 100
     assert (fc >= 0).any()
+
+
+def test_staged_sweep_equals_gathering_sweep_with_contact():
+    w = small_scene()
+    A = pbat.gpu.vbd.Integrator(contact_data(w))
+    B = pbat.gpu.vbd.Integrator(contact_data(w))
+    B.staged_sweep = False
+    for _ in range(6):
+        A.step(1 / 60, 15, 1)
+        B.step(1 / 60, 15, 1)
+    np.testing.assert_array_equal(A.x, B.x)
+    fa, aa = A.contacts()
+    fb, ab = B.contacts()
+    np.testing.assert_array_equal(fa, fb)
+    np.testing.assert_array_equal(aa, ab)
