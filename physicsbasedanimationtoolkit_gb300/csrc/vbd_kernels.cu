@@ -226,11 +226,14 @@ __global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
 // the block's slab (rest positions before griddepcontrol.wait: no launch writes them; current
 // positions after it), and the incidence loop reads them back through the three slot bytes of its
 // packed incidence word.  The slab slice of solve entry s starts at nbrPtr[s] - nbrPtr[first
-// entry of the block]; the lanes of a vertex share a warp, so __syncwarp orders the staging.
+// entry of the block]; positions and rest positions are two arrays of p.slab float4 each (a 16-byte
+// stride spreads random slots over all shared-memory banks); the lanes of a vertex share a warp,
+// so __syncwarp orders the staging.
 template <int L, bool CHEB, bool REC = false>
 __global__ void __launch_bounds__(256, 4) staged_sweep_kernel(SweepParams p)
 {
-    extern __shared__ float4 slab[]; // per staged neighbour: position, rest position
+    extern __shared__ float4 slab[]; // positions [0, p.slab), rest positions [p.slab, 2 p.slab)
+    float4* const rest = slab + p.slab;
     int const tid    = blockIdx.x * blockDim.x + threadIdx.x;
     int const s      = p.begin + tid / L;
     int const lane   = tid & (L - 1);
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(256, 4) staged_sweep_kernel(SweepParams p)
         n1   = __ldg(p.nbrPtr + s + 1);
         base = n0 - nb0;
         for (int j = n0 + lane; j < n1; j += L)
-            slab[2 * (base + j - n0) + 1] = __ldg(p.X + (__ldg(p.nbr + j) & kIndexMask));
+            rest[base + j - n0] = __ldg(p.X + (__ldg(p.nbr + j) & kIndexMask));
         k1 = __ldg(p.incPtr + s + 1);
         k  = __ldg(p.incPtr + s) + lane;
         if (k < k1)
@@ -275,7 +278,7 @@ __global__ void __launch_bounds__(256, 4) staged_sweep_kernel(SweepParams p)
             float4 const* src = p.x;
             if (CHEB && !(a >> 31))
                 src = p.hprev;
-            slab[2 * (base + j - n0)] = __ldg(src + (a & kIndexMask));
+            slab[base + j - n0] = __ldg(src + (a & kIndexMask));
         }
     }
     __syncwarp();
@@ -295,8 +298,8 @@ __global__ void __launch_bounds__(256, 4) staged_sweep_kernel(SweepParams p)
             for (int m = 0; m < 3; ++m)
             {
                 int const slot   = base + int((q.y >> (8 * m)) & 0xFFu);
-                float4 const xa  = slab[2 * slot];
-                float4 const Xa  = slab[2 * slot + 1];
+                float4 const xa  = slab[slot];
+                float4 const Xa  = rest[slot];
                 d[m][0] = xa.x - xi[0];
                 d[m][1] = xa.y - xi[1];
                 d[m][2] = xa.z - xi[2];
@@ -562,9 +565,11 @@ cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebys
         return cudaSuccess;
     if (stagedBytes > kStagedMaxBytes || (stagedBytes > 0 && (!p.nbrPtr || !p.nbr || !p.incPack || !p.mats)))
         return cudaErrorInvalidValue;
-    int const g = blocks_for(n, block);
-    return chebyshev ? launch_sweep_t<true, false>(p, lanes, g, block, pdl, s, stagedBytes)
-                     : launch_sweep_t<false, false>(p, lanes, g, block, pdl, s, stagedBytes);
+    int const g   = blocks_for(n, block);
+    SweepParams q = p;
+    q.slab        = int32_t(stagedBytes / (2 * sizeof(float4)));
+    return chebyshev ? launch_sweep_t<true, false>(q, lanes, g, block, pdl, s, stagedBytes)
+                     : launch_sweep_t<false, false>(q, lanes, g, block, pdl, s, stagedBytes);
 }
 
 cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool pdl, cudaStream_t s, size_t stagedBytes)
@@ -574,7 +579,9 @@ cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool
         return cudaSuccess;
     if (!p.tape || stagedBytes > kStagedMaxBytes || (stagedBytes > 0 && (!p.nbrPtr || !p.nbr || !p.incPack || !p.mats)))
         return cudaErrorInvalidValue;
-    return launch_sweep_t<false, true>(p, lanes, blocks_for(n, block), block, pdl, s, stagedBytes);
+    SweepParams q = p;
+    q.slab        = int32_t(stagedBytes / (2 * sizeof(float4)));
+    return launch_sweep_t<false, true>(q, lanes, blocks_for(n, block), block, pdl, s, stagedBytes);
 }
 
 size_t staged_sweep_bytes(int32_t const* nbrPtr, int32_t begin, int32_t end, int lanes, int block)
