@@ -55,6 +55,7 @@ extern "C" {
 /* sim/vbd/Enums.h:21-28 (only None and Chebyshev are implemented) */
 #define PBGB_ACCEL_NONE 0
 #define PBGB_ACCEL_CHEBYSHEV 1
+#define PBGB_ACCEL_ANDERSON 2 /* single mesh without contact; window_size columns */
 /* graph/Enums.h:20-33 */
 #define PBGB_COLOR_ORDER_NATURAL 0
 #define PBGB_COLOR_ORDER_SMALLEST_DEGREE 1
@@ -147,6 +148,7 @@ typedef struct pbgb_vbd_desc
     double muF;                    /* friction coefficient (default 0.3) */
     double epsv;                   /* IPC smooth friction velocity threshold (default 1e-3) */
     int32_t active_set_update_frequency; /* update the contact list every k substeps (default 1) */
+    int32_t window_size; /* Anderson window m, 1..16 (PBGB_ACCEL_ANDERSON; Data::mWindowSize, default 5) */
 } pbgb_vbd_desc;
 
 typedef struct pbgb_vbd pbgb_vbd; /* opaque integrator handle */

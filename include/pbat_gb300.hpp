@@ -8,7 +8,7 @@
  * Header-only, C++17, no Eigen dependency:
  *   - the constructor takes the reference's own pbat::sim::vbd::Data after Construct() (or any
  *     object with the same member names: x, X, E, v, aext, m, wg, lame, Pptr, Padj, strategy, kD,
- *     detHZero, eAcceleration, rho, and for contact V, F, B, XVA, FA, muC, muF, epsv,
+ *     detHZero, eAcceleration, rho, mWindowSize, and for contact V, F, B, XVA, FA, muC, muF, epsv,
  *     mActiveSetUpdateFrequency), reading each member through data()/size()/cols();
  *   - matrices passed in are any column-major 3 x n float matrix with data() and cols() (Eigen's
  *     GpuMatrixX, Eigen::Ref<GpuMatrixX const>, or pbgb::Matrix3X);
@@ -137,6 +137,7 @@ class Integrator
         d.detHZero          = static_cast<double>(data.detHZero);
         d.acceleration      = static_cast<std::int32_t>(data.eAcceleration);
         d.rho               = static_cast<double>(data.rho);
+        d.window_size       = static_cast<std::int32_t>(data.mWindowSize);
         d.chebyshev_formula = PBGB_CHEBYSHEV_REFERENCE;
         d.semantics         = PBGB_SEMANTICS_GPU;
         std::vector<std::int32_t> V, F, B;

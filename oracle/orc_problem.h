@@ -25,10 +25,11 @@ struct orc_problem
     int32_t strategy;    // EInitializationStrategy (sim/vbd/Enums.h:9-15)
     double kD;
     double detHZero;
-    int32_t acceleration;      // 0 none, 1 Chebyshev
+    int32_t acceleration;      // 0 none, 1 Chebyshev, 2 Anderson
     double rho;                // Chebyshev spectral radius estimate
     int32_t chebyshev_formula; // 0: reference weights (sim/vbd/Kernels.h:96-102), 1: textbook
     int32_t semantics;         // 0: CPU integrator (vtm1 = v), 1: GPU integrator (vtm1 = v(t-1))
     int32_t nthreads;          // <= 0: OpenMP default
+    int32_t window;            // Anderson window (acceleration 2)
 };
 }

@@ -495,6 +495,84 @@ double orc_chebyshev_omega(int32_t k, double rho2, double omega, int32_t formula
     return formula == 0 ? (4.0 / 4.0 - rho2 * omega) : 4.0 / (4.0 - rho2 * omega);
 }
 
+// Minimum-norm least-squares solution of min |A alpha - f| for the n x m window A (columns A[j]),
+// from the Gram matrix A^T A and A^T f in FP64 and a Jacobi eigen-decomposition of the Gram
+// matrix: alpha = V diag(1/l) V^T A^T f over the eigenvalues l above 1e-14 of the largest.  This is
+// the solution the reference's complete orthogonal decomposition gives
+// (sim/vbd/AndersonIntegrator.cpp:26-27,49-55), the rank decided on the Gram matrix.
+static void anderson_lsq(std::vector<std::vector<Real>> const& A, int m, Real const* f, size_t n, Real* alpha)
+{
+    Real G[16][16] = {}, b[16] = {}, V[16][16] = {};
+    for (int i = 0; i < m; ++i)
+    {
+        for (int j = 0; j <= i; ++j)
+        {
+            Real d = 0;
+            for (size_t q = 0; q < n; ++q)
+                d += A[i][q] * A[j][q];
+            G[i][j] = G[j][i] = d;
+        }
+        Real d = 0;
+        for (size_t q = 0; q < n; ++q)
+            d += A[i][q] * f[q];
+        b[i] = d;
+        V[i][i] = 1;
+    }
+    // Cyclic Jacobi rotations until the off-diagonal part vanishes.
+    for (int sweep = 0; sweep < 64; ++sweep)
+    {
+        Real off = 0, diag = 0;
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < m; ++j)
+                (i == j ? diag : off) += G[i][j] * G[i][j];
+        if (off <= 1e-30 * diag || off == 0)
+            break;
+        for (int p = 0; p < m; ++p)
+            for (int q = p + 1; q < m; ++q)
+            {
+                if (G[p][q] == 0)
+                    continue;
+                Real const theta = (G[q][q] - G[p][p]) / (2 * G[p][q]);
+                Real const t     = (theta >= 0 ? 1 : -1) / (std::abs(theta) + std::sqrt(theta * theta + 1));
+                Real const c     = 1 / std::sqrt(t * t + 1), sn = t * c;
+                for (int k = 0; k < m; ++k)
+                {
+                    Real const gkp = G[k][p], gkq = G[k][q];
+                    G[k][p]        = c * gkp - sn * gkq;
+                    G[k][q]        = sn * gkp + c * gkq;
+                }
+                for (int k = 0; k < m; ++k)
+                {
+                    Real const gpk = G[p][k], gqk = G[q][k];
+                    G[p][k]        = c * gpk - sn * gqk;
+                    G[q][k]        = sn * gpk + c * gqk;
+                }
+                for (int k = 0; k < m; ++k)
+                {
+                    Real const vkp = V[k][p], vkq = V[k][q];
+                    V[k][p]        = c * vkp - sn * vkq;
+                    V[k][q]        = sn * vkp + c * vkq;
+                }
+            }
+    }
+    Real lmax = 0;
+    for (int i = 0; i < m; ++i)
+        lmax = std::max(lmax, G[i][i]);
+    for (int j = 0; j < m; ++j)
+        alpha[j] = 0;
+    for (int e = 0; e < m; ++e)
+    {
+        Real const l = G[e][e];
+        if (!(l > 1e-14 * lmax))
+            continue;
+        Real proj = 0;
+        for (int i = 0; i < m; ++i)
+            proj += V[i][e] * b[i];
+        for (int j = 0; j < m; ++j)
+            alpha[j] += V[j][e] * proj / l;
+    }
+}
+
 // Advance `nsteps` time steps in place: x, v (nV x 3), vprev (nV x 3, GPU semantics only: the
 // velocity of the previous step, initially zero).  sim/vbd/Integrator.cpp:22-96 and
 // ChebyshevIntegrator.cpp:15-32.
@@ -544,7 +622,61 @@ int orc_run(orc_problem const* Pp, double* x, double* v, double* vprev, double d
             }
             Real const rho2 = P.rho * P.rho;
             Real omega      = 0;
-            for (int32_t k = 0; k < iterations; ++k)
+            if (P.acceleration == 2)
+            {
+                // AndersonIntegrator::Solve (sim/vbd/AndersonIntegrator.cpp:24-57): after each VBD
+                // iteration k >= 1, G_k = x, F_k = G_k - x_{k-1}; column (k-1) mod m of the window
+                // gets G_k - G_{k-1} and F_k - F_{k-1}; x = G_k - DG alpha with
+                // alpha = argmin |DF alpha - F_k| over the min(m, k) filled columns.
+                size_t const n3 = size_t(nV) * 3;
+                int const m     = P.window;
+                std::vector<std::vector<Real>> DF(static_cast<size_t>(m), std::vector<Real>(n3));
+                std::vector<std::vector<Real>> DG(static_cast<size_t>(m), std::vector<Real>(n3));
+                std::vector<Real> xkm1(x, x + n3), Gkm1(n3), Fkm1(n3), Fk(n3);
+                auto sweep = [&] {
+                    for (int32_t p = 0; p < P.nPartitions; ++p)
+                    {
+                        int32_t const b = P.Pptr[p], e = P.Pptr[p + 1];
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+                        for (int32_t kk = b; kk < e; ++kk)
+                            solve_vertex(P, P.Padj[kk], xt.data(), xtilde.data(), x, sdt, sdt2);
+                    }
+                };
+                if (iterations > 0)
+                {
+                    sweep();
+                    for (size_t q = 0; q < n3; ++q)
+                    {
+                        Gkm1[q] = x[q];
+                        Fkm1[q] = x[q] - xkm1[q];
+                    }
+                }
+                for (int32_t k = 1; k < iterations; ++k)
+                {
+                    std::copy(x, x + n3, xkm1.begin());
+                    sweep();
+                    int const dkl = (k - 1) % m;
+                    for (size_t q = 0; q < n3; ++q)
+                    {
+                        Fk[q]      = x[q] - xkm1[q];
+                        DG[dkl][q] = x[q] - Gkm1[q];
+                        DF[dkl][q] = Fk[q] - Fkm1[q];
+                        Gkm1[q]    = x[q];
+                        Fkm1[q]    = Fk[q];
+                    }
+                    int const mk = std::min(m, int(k));
+                    Real alpha[16];
+                    anderson_lsq(DF, mk, Fk.data(), n3, alpha);
+                    for (size_t q = 0; q < n3; ++q)
+                    {
+                        Real u = x[q];
+                        for (int j = 0; j < mk; ++j)
+                            u -= DG[j][q] * alpha[j];
+                        x[q] = u;
+                    }
+                }
+            }
+            for (int32_t k = 0; k < (P.acceleration == 2 ? 0 : iterations); ++k)
             {
                 // RunVbdIteration (Integrator.cpp:73-87): colours in sequence, vertices of a
                 // colour in parallel.

@@ -74,7 +74,7 @@ class VbdDesc(C.Structure):
         ("muC", C.c_double),
         ("muF", C.c_double),
         ("epsv", C.c_double),
-        ("active_set_update_frequency", C.c_int32),
+        ("active_set_update_frequency", C.c_int32), ("window_size", C.c_int32),
     ]
 
 

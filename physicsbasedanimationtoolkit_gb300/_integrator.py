@@ -13,7 +13,7 @@ from . import _capi
 SEMANTICS_CPU = 0
 SEMANTICS_GPU = 1
 
-_UNSUPPORTED = {2: "Anderson", 3: "Nesterov", 4: "Broyden", 5: "TrustRegion"}
+_UNSUPPORTED = {3: "Nesterov", 4: "Broyden", 5: "TrustRegion"}
 
 
 def make_desc(data, semantics):
@@ -24,7 +24,7 @@ def make_desc(data, semantics):
     if accel in _UNSUPPORTED:
         raise NotImplementedError(
             f"{_UNSUPPORTED[accel]} acceleration is not part of this library's VBD path "
-            "(Base and Chebyshev are)"
+            "(Base, Chebyshev and Anderson are)"
         )
     nV, nT = data.X.shape[1], data.E.shape[1]
     keep = dict(
@@ -64,8 +64,9 @@ def make_desc(data, semantics):
     d.init_strategy = int(data.strategy)
     d.kD = float(data.kD)
     d.detHZero = float(data.detH_zero)
-    d.acceleration = 1 if accel == 1 else 0
+    d.acceleration = accel if accel in (1, 2) else 0
     d.rho = float(data.rho)
+    d.window_size = int(getattr(data, "window_size", 5))
     d.chebyshev_formula = int(getattr(data, "chebyshev_formula", 0))
     d.semantics = semantics
     return d, keep

@@ -7,6 +7,7 @@
 // from a CUDA graph, tets packed into 64-byte records, the in-place colour sweep (no xb copy-back
 // pass), and several meshes concatenated into one system for the batched form.
 #include "adjoint.cuh"
+#include "anderson.cuh"
 #include "contact.cuh"
 #include "pbat_gb300.h"
 #include "vbd_construct.h"
@@ -92,6 +93,7 @@ class VbdSystem
     int32_t strategy  = PBGB_INIT_ADAPTIVE_PBAT;
     float kD = 0.f, detHZero = 1e-7f;
     int32_t acceleration = PBGB_ACCEL_NONE, chebFormula = PBGB_CHEBYSHEV_REFERENCE, semantics = 0;
+    int32_t window = 0; // Anderson window
     double rho  = 1.0;
     int32_t lanes = 0, block = 256;
     bool pdl   = true;
@@ -102,6 +104,10 @@ class VbdSystem
     // Device state
     cudaStream_t stream = nullptr;
     DeviceArray<float4> x, xt, xtilde, v, aext, vprev, h0, h1, X;
+    // Anderson acceleration: the sweep's increments (zero for pinned vertices), last un-accelerated
+    // iterate and residual, the window columns, FP64 block partials, Gram matrix and coefficients.
+    DeviceArray<float4> anStep, anGkm1, anFkm1, anDF, anDG;
+    DeviceArray<double> anPartials, anGram, anAlpha;
     DeviceArray<float> m, staging;
     DeviceArray<TetRecord> tets;
     DeviceArray<int32_t> solve, incPtr, flags;
@@ -306,8 +312,16 @@ class VbdSystem
                     throw std::invalid_argument("pbgb_vbd_desc: partition vertex out of range");
             if (d.acceleration == PBGB_ACCEL_CHEBYSHEV && !(d.rho > 0.0 && d.rho < 1.0))
                 throw std::invalid_argument("Expected 0 < rho < 1");
-            if (d.acceleration != PBGB_ACCEL_NONE && d.acceleration != PBGB_ACCEL_CHEBYSHEV)
+            if (d.acceleration != PBGB_ACCEL_NONE && d.acceleration != PBGB_ACCEL_CHEBYSHEV &&
+                d.acceleration != PBGB_ACCEL_ANDERSON)
                 throw std::invalid_argument("pbgb_vbd_desc: unsupported acceleration strategy");
+            if (d.acceleration == PBGB_ACCEL_ANDERSON)
+            {
+                if (d.window_size < 1 || d.window_size > kAndersonMaxWindow)
+                    throw std::invalid_argument("pbgb_vbd_desc: Anderson window must be in [1, 16]");
+                if (nMeshes != 1 || d.n_collision_triangles > 0)
+                    throw std::invalid_argument("Anderson acceleration needs a single mesh without contact");
+            }
             if (d.init_strategy < 0 || d.init_strategy > 4)
                 throw std::invalid_argument("pbgb_vbd_desc: invalid initialization strategy");
             totV += d.n_vertices;
@@ -330,6 +344,7 @@ class VbdSystem
         rho            = d0.rho;
         chebFormula    = d0.chebyshev_formula;
         semantics      = d0.semantics;
+        window         = acceleration == PBGB_ACCEL_ANDERSON ? d0.window_size : 0;
 
         // Host staging of the concatenated layout.
         std::vector<float4> hx(nV), hv(nV), ha(nV), hX(nV);
@@ -519,6 +534,20 @@ class VbdSystem
         {
             h0.allocate(nV);
             h1.allocate(nV);
+        }
+        if (acceleration == PBGB_ACCEL_ANDERSON)
+        {
+            anStep.allocate(nV);
+            anGkm1.allocate(nV);
+            anFkm1.allocate(nV);
+            anDF.allocate(size_t(window) * size_t(nV));
+            anDG.allocate(size_t(window) * size_t(nV));
+            anPartials.allocate(size_t(anderson_window_blocks(nV)) * 2 * size_t(window));
+            anGram.allocate(size_t(window) * size_t(window));
+            anAlpha.allocate(size_t(window));
+            // Pinned vertices are never solved: their increment stays zero.
+            check(cudaMemsetAsync(anStep.get(), 0, sizeof(float4) * size_t(nV), stream), "memset");
+            check(cudaMemsetAsync(anGram.get(), 0, sizeof(double) * size_t(window) * size_t(window), stream), "memset");
         }
         x.upload(hx.data(), nV, stream);
         v.upload(hv.data(), nV, stream);
@@ -965,6 +994,23 @@ class VbdSystem
                 check(contact_update(cmesh, cstate, x.get(), stream), "contact_update");
             double omega      = 0.0;
             double const rho2 = rho * rho;
+            bool const anderson = acceleration == PBGB_ACCEL_ANDERSON;
+            AndersonParams ap{};
+            if (anderson)
+            {
+                ap.x        = x.get();
+                ap.step     = anStep.get();
+                ap.Gkm1     = anGkm1.get();
+                ap.Fkm1     = anFkm1.get();
+                ap.DF       = anDF.get();
+                ap.DG       = anDG.get();
+                ap.partials = anPartials.get();
+                ap.gram     = anGram.get();
+                ap.alpha    = anAlpha.get();
+                ap.n        = nV;
+                ap.m        = window;
+                w.step = anStep.get();
+            }
             for (int32_t k = 0; k < iterations; ++k)
             {
                 if (twoBuffer)
@@ -990,6 +1036,20 @@ class VbdSystem
                 }
                 if (profiling)
                     check(cudaEventRecordWithFlags(evEnd[slot], stream, cudaEventRecordExternal), "cudaEventRecord");
+                if (anderson)
+                {
+                    // AndersonIntegrator::Solve (sim/vbd/AndersonIntegrator.cpp:31-56).
+                    if (k == 0)
+                        check(launch_anderson_start(ap, stream), "anderson_start");
+                    else
+                    {
+                        ap.dkl = (k - 1) % window;
+                        ap.mk  = std::min(window, k);
+                        check(launch_anderson_window(ap, stream), "anderson_window");
+                        check(launch_anderson_solve(ap, stream), "anderson_solve");
+                        check(launch_anderson_update(ap, stream), "anderson_update");
+                    }
+                }
             }
             check(launch_end_substep(sp, stream), "end_substep");
         }
@@ -1003,6 +1063,8 @@ class VbdSystem
         for (int32_t c = 0; c < nColors; ++c)
             perIter += colorPtr[c + 1] > colorPtr[c] ? 1 : 0;
         int64_t n = int64_t(substeps) * (2 * (nV > 0 ? 1 : 0) + int64_t(iterations) * perIter);
+        if (acceleration == PBGB_ACCEL_ANDERSON && iterations > 0)
+            n += int64_t(substeps) * (1 + 3 * int64_t(iterations - 1));
         if (contact)
         {
             // predict, vertex and triangle boxes, Morton, 4 x (count, scan, scatter), Karras, leaf

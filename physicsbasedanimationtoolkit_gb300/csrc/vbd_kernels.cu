@@ -84,7 +84,11 @@ __device__ __forceinline__ void finish_vertex(SweepParams const& p, VertexBlock<
     elastic_system(b, xt, xi, p.h, p.kD, H, g);
     if (CHEB && p.fc)
         add_contacts(p, i, xt, xi, H, g);
-    bool const moved = inertia_solve(H, g, xl, xt4.w, p.h2, p.detHZero, xi);
+    float dx[3];
+    bool const moved = inertia_solve(H, g, xl, xt4.w, p.h2, p.detHZero, xi, static_cast<float*>(nullptr),
+                                     static_cast<float*>(nullptr), dx);
+    if (!CHEB && p.step)
+        p.step[i] = make_float4(dx[0], dx[1], dx[2], 0.f);
     if (REC)
     {
         // H now includes the inertia term; its inverse by the adjugate, as in inertia_solve.

@@ -75,6 +75,10 @@ struct SweepParams
     uint2 const* __restrict__ incPack;
     float4 const* __restrict__ mats;
     int32_t slab; // staged entries per block (set by launch_sweep): positions [0, slab), rest positions [slab, 2 slab)
+    // Applied Newton increments (one-buffer sweeps only, nullptr: not written): step[i] = x_new -
+    // x_old for every solved vertex, the residual Anderson acceleration mixes (exact to FP32
+    // relative precision, unlike the difference of two rounded positions).
+    float4* __restrict__ step;
     // Adjoint tape of this iteration (recording sweeps only): for solve-list entry s, the inverse
     // of the vertex's 3x3 Newton matrix (xx xy xz yy | yz zz 0 0) in tape[2s], tape[2s+1]; zero
     // when the Newton step was skipped.

@@ -130,9 +130,20 @@ PBGB_HD void elastic_system(VertexBlock<T> const& b, T const* xt, T const* x, T 
 }
 
 // Inertia (sim/vbd/Kernels.h:310-322) and the 3x3 Newton step with the near-singular skip
-// (:329-339).  Updates x in place; returns false when the step was skipped.
+// (:329-339).  Updates x in place; returns false when the step was skipped.  dxOut (optional): the
+// applied increment -H^-1 g (zero when skipped).
 template <class T>
-PBGB_HD bool inertia_solve(T* H, T* g, T const* xtilde, T m, T h2, T detHZero, T* x, T* gout = nullptr, T* Hout = nullptr)
+PBGB_HD bool inertia_solve(
+    T* H,
+    T* g,
+    T const* xtilde,
+    T m,
+    T h2,
+    T detHZero,
+    T* x,
+    T* gout  = nullptr,
+    T* Hout  = nullptr,
+    T* dxOut = nullptr)
 {
     T const K = m / h2;
     H[0] += K;
@@ -159,11 +170,24 @@ PBGB_HD bool inertia_solve(T* H, T* g, T const* xtilde, T m, T h2, T detHZero, T
     T const a22 = H[0] * H[3] - H[1] * H[1];
     T const det = H[0] * a00 + H[1] * a01 + H[2] * a02;
     if (!(fabs(det) > detHZero))
+    {
+        if (dxOut)
+            dxOut[0] = dxOut[1] = dxOut[2] = T(0);
         return false;
+    }
     T const inv = T(1) / det;
-    x[0] -= inv * (a00 * g[0] + a01 * g[1] + a02 * g[2]);
-    x[1] -= inv * (a01 * g[0] + a11 * g[1] + a12 * g[2]);
-    x[2] -= inv * (a02 * g[0] + a12 * g[1] + a22 * g[2]);
+    T const d0  = inv * (a00 * g[0] + a01 * g[1] + a02 * g[2]);
+    T const d1  = inv * (a01 * g[0] + a11 * g[1] + a12 * g[2]);
+    T const d2  = inv * (a02 * g[0] + a12 * g[1] + a22 * g[2]);
+    x[0] -= d0;
+    x[1] -= d1;
+    x[2] -= d2;
+    if (dxOut)
+    {
+        dxOut[0] = -d0;
+        dxOut[1] = -d1;
+        dxOut[2] = -d2;
+    }
     return true;
 }
 

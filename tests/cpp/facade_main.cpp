@@ -41,6 +41,7 @@ struct Data
     EInitializationStrategy strategy{EInitializationStrategy::KineticEnergyMinimum};
     double kD{0}, detHZero{1e-7}, rho{1}, muC{1e6}, muF{0.3}, epsv{1e-3};
     std::ptrdiff_t mActiveSetUpdateFrequency{1};
+    std::ptrdiff_t mWindowSize{5};
     EAccelerationStrategy eAcceleration{EAccelerationStrategy::None};
 };
 

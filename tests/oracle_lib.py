@@ -50,7 +50,7 @@ class OrcProblem(C.Structure):
         ("rho", C.c_double),
         ("chebyshev_formula", C.c_int32),
         ("semantics", C.c_int32),
-        ("nthreads", C.c_int32),
+        ("nthreads", C.c_int32), ("window", C.c_int32),
     ]
 
 
@@ -195,7 +195,7 @@ class OracleVbd:
 
     def __init__(self, X, T, rho, mu, lam, dbc, v=None, aext=None, strategy=4, kD=0.0,
                  detHZero=1e-7, rho_chebyshev=None, chebyshev_formula=0, semantics=0,
-                 nthreads=0, ordering=2, selection=0, data=None):
+                 nthreads=0, ordering=2, selection=0, data=None, anderson_window=None):
         self.X = np.ascontiguousarray(X, dtype=np.float64)
         self.T = np.ascontiguousarray(T, dtype=np.int32)
         nV = self.X.shape[0]
@@ -226,6 +226,11 @@ class OracleVbd:
         P.detHZero = detHZero
         P.acceleration = 0 if rho_chebyshev is None else 1
         P.rho = 1.0 if rho_chebyshev is None else rho_chebyshev
+        if anderson_window is not None:
+            if not 1 <= anderson_window <= 16:
+                raise ValueError("Anderson window must be in [1, 16]")
+            P.acceleration = 2
+            P.window = int(anderson_window)
         P.chebyshev_formula = chebyshev_formula
         P.semantics = semantics
         P.nthreads = nthreads

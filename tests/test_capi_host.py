@@ -143,8 +143,11 @@ def test_integrator_creation_without_device_fails_loudly():
     assert e.value.code == 6
 
 
-def test_unsupported_accelerations_are_rejected():
+@pytest.mark.parametrize("accel", ["broyden", "nesterov", "trust_region"])
+def test_unsupported_accelerations_are_rejected(accel):
     P, T, _, _ = meshgen.cube5()
-    d = pbat.sim.vbd.Data().with_volume_mesh(P, T).with_anderson_acceleration(5).construct()
+    d = pbat.sim.vbd.Data().with_volume_mesh(P, T)
+    d = {"broyden": lambda: d.with_broyden_acceleration(5), "nesterov": lambda: d.with_nesterov_acceleration(1.0, 3),
+         "trust_region": lambda: d.with_trust_region_acceleration(0.2, 2.0, True)}[accel]().construct()
     with pytest.raises(NotImplementedError):
         pbat.gpu.vbd.Integrator(d)
