@@ -366,6 +366,58 @@ def run_adjoint(args, pbat, torch):
     }
 
 
+def run_anderson(args, pbat, torch):
+    """Anderson acceleration (window 5) on the benchmark beam [0,4]x[0,1]^2 at 160x40x40 hexes
+    (270,641 vertices, 1,536,000 tets), 50 iterations per step, dt = 1/60, against plain VBD with
+    the same iterations from the same state: step time (CUDA events on the integrator's stream)
+    and the norm of the FP64 objective gradient over the free vertices after one step."""
+    import ctypes as C
+
+    from physicsbasedanimationtoolkit_gb300 import _capi
+
+    w = workload_beam(args)
+    dt, iters = 1 / 60, 50
+
+    def measure(window):
+        d = (pbat.sim.vbd.Data().with_volume_mesh(w["X"].T, w["T"].T).with_material(w["rho"], w["mu"], w["lam"])
+             .with_dirichlet_vertices(w["dbc"]).with_velocity(w["v"].T).with_initialization_strategy(2))
+        if window:
+            d = d.with_anderson_acceleration(window)
+        I = pbat.gpu.vbd.Integrator(d.construct())
+        x0, v0 = I.x.copy(), I.v.copy()
+        I.step(dt, iters, 1)
+        g = I.gradient(dt).reshape(-1, 3)
+        g[w["dbc"]] = 0.0
+        gnorm = float(np.linalg.norm(g))
+        for _ in range(args.warmup):
+            I.step(dt, iters, 1)
+        I.x, I.v = x0, v0
+        sp = C.c_void_p()
+        _capi.check(_capi.lib().pbgb_vbd_stream(I.handle, C.byref(sp)), I.handle)
+        stream = torch.cuda.ExternalStream(sp.value)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        I.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            I.step(dt, iters, 1)
+        e1.record(stream)
+        I.synchronize()
+        return e0.elapsed_time(e1) / args.steps, gnorm, I.n_free
+
+    ms_a, g_a, n_free = measure(5)
+    ms_p, g_p, _ = measure(0)
+    return {
+        "workload": "beam 160x40x40 hexes x 6 tets, 50 iterations, dt 1/60, KineticEnergyMinimum initial guess",
+        "window": 5,
+        "ms_per_step": ms_a,
+        "value": n_free * iters / (ms_a * 1e-3),
+        "unit": UNIT,
+        "grad_norm_after_one_step": g_a,
+        "plain_ms_per_step": ms_p,
+        "plain_grad_norm_after_one_step": g_p,
+    }
+
+
 def run_contact(args, pbat, torch):
     """Contact scene: 16 cubes (16^3 hexes, 0.6 m) above a pinned 64x64x2 slab, 91,283 vertices,
     442,368 tets, 66,560 collision triangles; 30 iterations per step, dt = 1/60, muC = 1e7.  Each
@@ -513,7 +565,9 @@ def main():
                     help="skip the contact-scene step measurement")
     ap.add_argument("--no-lbvh", dest="lbvh", action="store_false", default=True,
                     help="skip the LBVH build measurement")
-    ap.add_argument("--only", choices=["batch", "adjoint", "contact", "lbvh"], default=None,
+    ap.add_argument("--no-anderson", dest="anderson", action="store_false", default=True,
+                    help="skip the Anderson-acceleration measurement")
+    ap.add_argument("--only", choices=["batch", "adjoint", "contact", "lbvh", "anderson"], default=None,
                     help="run only this secondary measurement and print its figures (no benchmark line)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -541,6 +595,7 @@ def main():
             "adjoint": lambda: run_adjoint(args, pbat, torch),
             "contact": lambda: run_contact(args, pbat, torch),
             "lbvh": lambda: run_lbvh(args, _capi, torch),
+            "anderson": lambda: run_anderson(args, pbat, torch),
         }
         if rank == 0:
             print(json.dumps({"only": args.only, args.only: legs[args.only]()}))
@@ -644,6 +699,7 @@ def main():
         adjoint = run_adjoint(args, pbat, torch) if args.adjoint else None
         contact = run_contact(args, pbat, torch) if args.contact else None
         lbvh = run_lbvh(args, _capi, torch) if args.lbvh else None
+        anderson = run_anderson(args, pbat, torch) if args.anderson else None
         launches = launches_per_step * args.steps
         line = {
             "metric": METRIC,
@@ -677,6 +733,7 @@ def main():
             "adjoint": adjoint,
             "contact": contact,
             "lbvh": lbvh,
+            "anderson": anderson,
         }
         print(json.dumps(line))
     if dist:

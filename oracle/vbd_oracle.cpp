@@ -495,14 +495,14 @@ double orc_chebyshev_omega(int32_t k, double rho2, double omega, int32_t formula
     return formula == 0 ? (4.0 / 4.0 - rho2 * omega) : 4.0 / (4.0 - rho2 * omega);
 }
 
-// Minimum-norm least-squares solution of min |A alpha - f| for the n x m window A (columns A[j]),
-// from the Gram matrix A^T A and A^T f in FP64 and a Jacobi eigen-decomposition of the Gram
-// matrix: alpha = V diag(1/l) V^T A^T f over the eigenvalues l above 1e-14 of the largest.  This is
-// the solution the reference's complete orthogonal decomposition gives
-// (sim/vbd/AndersonIntegrator.cpp:26-27,49-55), the rank decided on the Gram matrix.
+// Least-squares coefficients of min |A alpha - f| for the n x m window A (columns A[j]), from the
+// Gram matrix A^T A and A^T f in FP64: (A^T A + eps I) alpha = A^T f by Cholesky, eps = 1e-10 of
+// the largest diagonal entry.  Where A is well conditioned this is the reference's complete
+// orthogonal decomposition solution (sim/vbd/AndersonIntegrator.cpp:26-27,49-55); directions far
+// below eps are damped to zero, as in its minimum-norm solution.
 static void anderson_lsq(std::vector<std::vector<Real>> const& A, int m, Real const* f, size_t n, Real* alpha)
 {
-    Real G[16][16] = {}, b[16] = {}, V[16][16] = {};
+    Real G[16][16] = {}, b[16] = {};
     for (int i = 0; i < m; ++i)
     {
         for (int j = 0; j <= i; ++j)
@@ -516,60 +516,41 @@ static void anderson_lsq(std::vector<std::vector<Real>> const& A, int m, Real co
         for (size_t q = 0; q < n; ++q)
             d += A[i][q] * f[q];
         b[i] = d;
-        V[i][i] = 1;
     }
-    // Cyclic Jacobi rotations until the off-diagonal part vanishes.
-    for (int sweep = 0; sweep < 64; ++sweep)
-    {
-        Real off = 0, diag = 0;
-        for (int i = 0; i < m; ++i)
-            for (int j = 0; j < m; ++j)
-                (i == j ? diag : off) += G[i][j] * G[i][j];
-        if (off <= 1e-30 * diag || off == 0)
-            break;
-        for (int p = 0; p < m; ++p)
-            for (int q = p + 1; q < m; ++q)
-            {
-                if (G[p][q] == 0)
-                    continue;
-                Real const theta = (G[q][q] - G[p][p]) / (2 * G[p][q]);
-                Real const t     = (theta >= 0 ? 1 : -1) / (std::abs(theta) + std::sqrt(theta * theta + 1));
-                Real const c     = 1 / std::sqrt(t * t + 1), sn = t * c;
-                for (int k = 0; k < m; ++k)
-                {
-                    Real const gkp = G[k][p], gkq = G[k][q];
-                    G[k][p]        = c * gkp - sn * gkq;
-                    G[k][q]        = sn * gkp + c * gkq;
-                }
-                for (int k = 0; k < m; ++k)
-                {
-                    Real const gpk = G[p][k], gqk = G[q][k];
-                    G[p][k]        = c * gpk - sn * gqk;
-                    G[q][k]        = sn * gpk + c * gqk;
-                }
-                for (int k = 0; k < m; ++k)
-                {
-                    Real const vkp = V[k][p], vkq = V[k][q];
-                    V[k][p]        = c * vkp - sn * vkq;
-                    V[k][q]        = sn * vkp + c * vkq;
-                }
-            }
-    }
-    Real lmax = 0;
+    Real dmax = 0;
     for (int i = 0; i < m; ++i)
-        lmax = std::max(lmax, G[i][i]);
+        dmax = std::max(dmax, G[i][i]);
+    Real const eps = 1e-10 * dmax + 1e-300;
+    for (int i = 0; i < m; ++i)
+        G[i][i] += eps;
+    Real L[16][16] = {}, y[16];
     for (int j = 0; j < m; ++j)
-        alpha[j] = 0;
-    for (int e = 0; e < m; ++e)
     {
-        Real const l = G[e][e];
-        if (!(l > 1e-14 * lmax))
-            continue;
-        Real proj = 0;
-        for (int i = 0; i < m; ++i)
-            proj += V[i][e] * b[i];
-        for (int j = 0; j < m; ++j)
-            alpha[j] += V[j][e] * proj / l;
+        Real d = G[j][j];
+        for (int k = 0; k < j; ++k)
+            d -= L[j][k] * L[j][k];
+        L[j][j] = std::sqrt(std::max(d, eps));
+        for (int i = j + 1; i < m; ++i)
+        {
+            Real v = G[i][j];
+            for (int k = 0; k < j; ++k)
+                v -= L[i][k] * L[j][k];
+            L[i][j] = v / L[j][j];
+        }
+    }
+    for (int i = 0; i < m; ++i)
+    {
+        Real v = b[i];
+        for (int k = 0; k < i; ++k)
+            v -= L[i][k] * y[k];
+        y[i] = v / L[i][i];
+    }
+    for (int i = m - 1; i >= 0; --i)
+    {
+        Real v = y[i];
+        for (int k = i + 1; k < m; ++k)
+            v -= L[k][i] * alpha[k];
+        alpha[i] = v / L[i][i];
     }
 }
 

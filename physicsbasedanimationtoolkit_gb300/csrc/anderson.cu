@@ -28,12 +28,12 @@ __global__ void __launch_bounds__(kWindowThreads) anderson_window_kernel(Anderso
     __shared__ double warpSums[kWindowThreads / 32][2 * kAndersonMaxWindow];
     int const i  = blockIdx.x * blockDim.x + threadIdx.x;
     int const mk = p.mk;
-    // Dots with the new column (accA) and with F_k (accB); indices known at compile time so that
-    // the accumulators stay in registers.
-    double accA[kAndersonMaxWindow], accB[kAndersonMaxWindow];
+    // Dots with the new column (accA, indices known at compile time so that the accumulators stay
+    // in registers) and the new column's dot with F_k (accF).
+    double accA[kAndersonMaxWindow], accF = 0.0;
 #pragma unroll
     for (int t = 0; t < kAndersonMaxWindow; ++t)
-        accA[t] = accB[t] = 0.0;
+        accA[t] = 0.0;
     if (i < p.n)
     {
         float4 const g  = p.x[i];
@@ -50,32 +50,28 @@ __global__ void __launch_bounds__(kWindowThreads) anderson_window_kernel(Anderso
 #pragma unroll
         for (int j = 0; j < kAndersonMaxWindow; ++j)
             if (j < mk)
-            {
-                float4 const c = j == p.dkl ? df : p.DF[size_t(j) * n + i];
-                accA[j]        = dot3(c, df);
-                accB[j]        = dot3(c, f);
-            }
+                accA[j] = dot3(j == p.dkl ? df : p.DF[size_t(j) * n + i], df);
+        accF = dot3(df, f);
     }
     int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int t = 0; t < kAndersonMaxWindow; ++t)
         if (t < mk)
         {
-            double a = accA[t], c = accB[t];
+            double a = accA[t];
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1)
-            {
                 a += __shfl_xor_sync(0xffffffffu, a, off);
-                c += __shfl_xor_sync(0xffffffffu, c, off);
-            }
             if (lane == 0)
-            {
-                warpSums[warp][t]      = a;
-                warpSums[warp][mk + t] = c;
-            }
+                warpSums[warp][t] = a;
         }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+        accF += __shfl_xor_sync(0xffffffffu, accF, off);
+    if (lane == 0)
+        warpSums[warp][mk] = accF;
     __syncthreads();
-    if (threadIdx.x < 2 * mk)
+    if (threadIdx.x < mk + 1)
     {
         double v = 0.0;
         for (int w = 0; w < kWindowThreads / 32; ++w)
@@ -84,92 +80,107 @@ __global__ void __launch_bounds__(kWindowThreads) anderson_window_kernel(Anderso
     }
 }
 
-// One block: the 2 mk sums over the window blocks in order, the Gram row/column update and the
-// mk x mk minimum-norm least-squares solve by cyclic Jacobi rotations (thread 0).
-__global__ void anderson_solve_kernel(AndersonParams p, int nblocks)
+int constexpr kSolveThreads = 256;
+
+// One block: the 2 mk sums over the window blocks (each thread a strided set of blocks, then a
+// fixed reduction tree: deterministic), the Gram row/column update and the mk x mk ridge-
+// regularised solve by Cholesky (thread 0, matrices in shared memory; the few FP64 divisions and
+// square roots of a Cholesky keep this latency-bound single thread short).
+__global__ void __launch_bounds__(kSolveThreads) anderson_solve_kernel(AndersonParams p, int nblocks)
 {
+    __shared__ double warpSums[kSolveThreads / 32][2 * kAndersonMaxWindow];
     __shared__ double sums[2 * kAndersonMaxWindow];
+    __shared__ double G[kAndersonMaxWindow][kAndersonMaxWindow];
+    __shared__ double V[kAndersonMaxWindow][kAndersonMaxWindow];
     int const mk = p.mk, m = p.m, t = threadIdx.x;
-    if (t < 2 * mk)
+    double acc[kAndersonMaxWindow + 1];
+#pragma unroll
+    for (int j = 0; j <= kAndersonMaxWindow; ++j)
+        acc[j] = 0.0;
+    for (int b = t; b < nblocks; b += kSolveThreads)
+    {
+        double const* row = p.partials + size_t(b) * 2 * m;
+#pragma unroll
+        for (int j = 0; j <= kAndersonMaxWindow; ++j)
+            if (j <= mk)
+                acc[j] += row[j];
+    }
+    int const lane = t & 31, warp = t >> 5;
+#pragma unroll
+    for (int j = 0; j <= kAndersonMaxWindow; ++j)
+        if (j <= mk)
+        {
+            double a = acc[j];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1)
+                a += __shfl_xor_sync(0xffffffffu, a, off);
+            if (lane == 0)
+                warpSums[warp][j] = a;
+        }
+    __syncthreads();
+    if (t <= mk)
     {
         double v = 0.0;
-        for (int b = 0; b < nblocks; ++b)
-            v += p.partials[size_t(b) * 2 * m + t];
+        for (int w = 0; w < kSolveThreads / 32; ++w)
+            v += warpSums[w][t];
         sums[t] = v;
     }
     __syncthreads();
     if (t != 0)
         return;
+    // Gram row/column dkl; right-hand side: the new column's product directly, the others updated.
+    double const fnew = sums[mk];
     for (int j = 0; j < mk; ++j)
     {
         p.gram[j * m + p.dkl] = sums[j];
         p.gram[p.dkl * m + j] = sums[j];
+        p.rhs[j]              = j == p.dkl ? fnew : p.rhs[j] + sums[j];
     }
-    double G[kAndersonMaxWindow][kAndersonMaxWindow], V[kAndersonMaxWindow][kAndersonMaxWindow];
+    for (int j = 0; j < mk; ++j)
+        sums[mk + j] = p.rhs[j];
+    // (G + eps I) alpha = b by Cholesky, eps = 1e-10 of the largest diagonal entry: the exact
+    // least-squares solution where DF is well conditioned, directions far below eps damped to zero.
+    double dmax = 0.0;
     for (int i = 0; i < mk; ++i)
-        for (int j = 0; j < mk; ++j)
+        dmax = fmax(dmax, p.gram[i * m + i]);
+    double const eps = 1e-10 * dmax + 1e-300;
+    for (int i = 0; i < mk; ++i)
+        for (int j = 0; j <= i; ++j)
+            G[i][j] = p.gram[i * m + j] + (i == j ? eps : 0.0);
+    for (int j = 0; j < mk; ++j)
+    {
+        double d = G[j][j];
+        for (int k = 0; k < j; ++k)
+            d -= G[j][k] * G[j][k];
+        d          = d > eps ? d : eps;
+        double const r = sqrt(d);
+        G[j][j]        = r;
+        V[0][j]        = 1.0 / r; // reciprocal pivots
+        for (int i = j + 1; i < mk; ++i)
         {
-            G[i][j] = p.gram[i * m + j];
-            V[i][j] = i == j ? 1.0 : 0.0;
+            double v = G[i][j];
+            for (int k = 0; k < j; ++k)
+                v -= G[i][k] * G[j][k];
+            G[i][j] = v * V[0][j];
         }
-    for (int sweep = 0; sweep < 64; ++sweep)
-    {
-        double off = 0.0, diag = 0.0;
-        for (int i = 0; i < mk; ++i)
-            for (int j = 0; j < mk; ++j)
-                if (i == j)
-                    diag += G[i][j] * G[i][j];
-                else
-                    off += G[i][j] * G[i][j];
-        if (off <= 1e-30 * diag || off == 0.0)
-            break;
-        for (int a = 0; a < mk; ++a)
-            for (int b = a + 1; b < mk; ++b)
-            {
-                if (G[a][b] == 0.0)
-                    continue;
-                double const theta = (G[b][b] - G[a][a]) / (2.0 * G[a][b]);
-                double const tn    = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                double const c     = 1.0 / sqrt(tn * tn + 1.0), sn = tn * c;
-                for (int k = 0; k < mk; ++k)
-                {
-                    double const gka = G[k][a], gkb = G[k][b];
-                    G[k][a]          = c * gka - sn * gkb;
-                    G[k][b]          = sn * gka + c * gkb;
-                }
-                for (int k = 0; k < mk; ++k)
-                {
-                    double const gak = G[a][k], gbk = G[b][k];
-                    G[a][k]          = c * gak - sn * gbk;
-                    G[b][k]          = sn * gak + c * gbk;
-                }
-                for (int k = 0; k < mk; ++k)
-                {
-                    double const vka = V[k][a], vkb = V[k][b];
-                    V[k][a]          = c * vka - sn * vkb;
-                    V[k][b]          = sn * vka + c * vkb;
-                }
-            }
     }
-    double lmax = 0.0;
+    // L y = b, then L^T alpha = y (alpha into sums[0..mk)).
     for (int i = 0; i < mk; ++i)
-        lmax = fmax(lmax, G[i][i]);
-    double al[kAndersonMaxWindow];
-    for (int j = 0; j < mk; ++j)
-        al[j] = 0.0;
-    for (int e = 0; e < mk; ++e)
     {
-        double const l = G[e][e];
-        if (!(l > 1e-14 * lmax))
-            continue;
-        double proj = 0.0;
-        for (int i = 0; i < mk; ++i)
-            proj += V[i][e] * sums[mk + i];
-        for (int j = 0; j < mk; ++j)
-            al[j] += V[j][e] * proj / l;
+        double v = sums[mk + i];
+        for (int k = 0; k < i; ++k)
+            v -= G[i][k] * sums[k];
+        sums[i] = v * V[0][i];
+    }
+    for (int i = mk - 1; i >= 0; --i)
+    {
+        double v = sums[i];
+        for (int k = i + 1; k < mk; ++k)
+            v -= G[k][i] * sums[k];
+        sums[i] = v * V[0][i];
     }
     for (int j = 0; j < mk; ++j)
-        p.alpha[j] = al[j];
+        p.alpha[j] = sums[j];
 }
 
 __global__ void anderson_update_kernel(AndersonParams p)
@@ -221,7 +232,7 @@ cudaError_t launch_anderson_window(AndersonParams const& p, cudaStream_t s)
 
 cudaError_t launch_anderson_solve(AndersonParams const& p, cudaStream_t s)
 {
-    anderson_solve_kernel<<<1, 64, 0, s>>>(p, anderson_window_blocks(p.n));
+    anderson_solve_kernel<<<1, kSolveThreads, 0, s>>>(p, anderson_window_blocks(p.n));
     return cudaGetLastError();
 }
 

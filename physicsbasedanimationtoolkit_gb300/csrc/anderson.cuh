@@ -6,18 +6,21 @@
 // x = G_k - DG alpha with alpha the minimum-norm minimiser of |DF alpha - F_k| over the
 // mk = min(m, k) filled columns.  Layout and kernels:
 //   window kernel: one streaming pass that forms the new column and, per block, the FP64 partial
-//       dot products DF_j . DF_new and DF_j . F_k (j < mk) in a fixed reduction order;
+//       dot products DF_j . DF_new (j < mk) and DF_new . F_k in a fixed reduction order (since
+//       F_k = F_{k-1} + DF_new, DF_j . F_k = DF_j . F_{k-1} + DF_j . DF_new for the unchanged
+//       columns, so only the new column needs its own product with F_k);
 //   solve kernel (one block): sums the block partials in order, refreshes row and column
-//       (k-1) mod m of the persistent FP64 Gram matrix DF^T DF, and solves the mk x mk system by a
-//       Jacobi eigen-decomposition (pseudo-inverse over eigenvalues above 1e-14 of the largest);
+//       (k-1) mod m of the persistent FP64 Gram matrix DF^T DF, and solves
+//       (DF^T DF + eps I) alpha = DF^T F_k by Cholesky, eps = 1e-10 of the largest diagonal entry;
 //   update kernel: x = G_k - DG alpha.
 // F_k is taken from the increments the sweep applied (x_k - x_{k-1} vertex by vertex, each free
 // vertex moving once per iteration), so it keeps FP32 relative precision when it is far smaller than
 // the positions.
 // The reference's CPU integrator uses a complete orthogonal decomposition with threshold 1e-10 and
-// its GPU integrator a Householder QR whose zero pivots are replaced by a tiny value; both give the
-// same alpha when DF has full rank, and the pseudo-inverse gives the CPU's minimum-norm solution
-// when it does not.
+// its GPU integrator a Householder QR whose zero pivots are replaced by a tiny value; all give the
+// same alpha when DF is well conditioned.  When it is not, the ridge damps the directions below eps
+// towards zero as the CPU's minimum-norm solution does, where a QR with patched pivots can return
+// arbitrarily large coefficients.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -35,8 +38,9 @@ struct AndersonParams
     float4* __restrict__ Fkm1; // last residual F_{k-1}
     float4* __restrict__ DF;   // m columns of n float4 (column j at j * n)
     float4* __restrict__ DG;
-    double* __restrict__ partials; // per window block: mk dots with DF_new, then mk dots with F_k
+    double* __restrict__ partials; // per window block: mk dots DF_j . DF_new, then DF_new . F_k
     double* __restrict__ gram;     // m x m, row-major
+    double* __restrict__ rhs;      // m: DF_j . F_k
     double* __restrict__ alpha;    // m
     int32_t n;
     int32_t m;

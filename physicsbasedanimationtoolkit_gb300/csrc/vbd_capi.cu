@@ -107,7 +107,7 @@ class VbdSystem
     // Anderson acceleration: the sweep's increments (zero for pinned vertices), last un-accelerated
     // iterate and residual, the window columns, FP64 block partials, Gram matrix and coefficients.
     DeviceArray<float4> anStep, anGkm1, anFkm1, anDF, anDG;
-    DeviceArray<double> anPartials, anGram, anAlpha;
+    DeviceArray<double> anPartials, anGram, anRhs, anAlpha;
     DeviceArray<float> m, staging;
     DeviceArray<TetRecord> tets;
     DeviceArray<int32_t> solve, incPtr, flags;
@@ -545,6 +545,7 @@ class VbdSystem
             anPartials.allocate(size_t(anderson_window_blocks(nV)) * 2 * size_t(window));
             anGram.allocate(size_t(window) * size_t(window));
             anAlpha.allocate(size_t(window));
+            anRhs.allocate(size_t(window));
             // Pinned vertices are never solved: their increment stays zero.
             check(cudaMemsetAsync(anStep.get(), 0, sizeof(float4) * size_t(nV), stream), "memset");
             check(cudaMemsetAsync(anGram.get(), 0, sizeof(double) * size_t(window) * size_t(window), stream), "memset");
@@ -1007,6 +1008,7 @@ class VbdSystem
                 ap.partials = anPartials.get();
                 ap.gram     = anGram.get();
                 ap.alpha    = anAlpha.get();
+                ap.rhs      = anRhs.get();
                 ap.n        = nV;
                 ap.m        = window;
                 w.step = anStep.get();
