@@ -162,6 +162,17 @@ PBGB_API int pbgb_vbd_destroy(pbgb_vbd* h);
 
 /* Integrator::Step(dt, iterations, substeps).  Asynchronous on the handle's stream. */
 PBGB_API int pbgb_vbd_step(pbgb_vbd* h, float dt, int32_t iterations, int32_t substeps);
+/* Integrator::TracedStep (gpu/vbd/Integrator.h:79-93, gpu/impl/vbd/Integrator.cu:105-148): one
+ * step of plain VBD iterations (whatever the acceleration, as the reference's TracedSolve) written
+ * to `dir` as Matrix Market files: on t == 0 T.mtx (nT x 4), M.mtx, wg.mtx, GP.mtx (4 x 3 nT),
+ * lame.mtx (nT x 2); per substep xtilde.t.{t}.s.{s}.mtx (nV x 3) and x.t.{t}.s.{s}.k.{k}.mtx for
+ * k = 0 .. iterations.  Synchronous. */
+PBGB_API int pbgb_vbd_traced_step(pbgb_vbd* h, float dt, int32_t iterations, int32_t substeps, int32_t t, const char* dir);
+/* Integrator::TraceNextStep of the CPU integrator (sim/vbd/Integrator.cpp:47-52,202-235): the next
+ * pbgb_vbd_step writes, per substep, {path}/{t}.{s}.f.mtx (objective at the iterates k = 0 ..
+ * iterations), {t}.{s}.grad.mtx and {t}.{s}.x.mtx (3 nV x iterations+1, FP64 gradient and
+ * positions), with the configured acceleration.  That step runs outside the step graph. */
+PBGB_API int pbgb_vbd_trace_next_step(pbgb_vbd* h, const char* path, int32_t t);
 /* Block until the handle's stream is idle; reports device-side non-finite detection. */
 PBGB_API int pbgb_vbd_synchronize(pbgb_vbd* h);
 

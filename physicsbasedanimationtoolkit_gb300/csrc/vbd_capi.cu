@@ -19,7 +19,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <functional>
 #include <exception>
 #include <memory>
 #include <mutex>
@@ -144,6 +146,15 @@ class VbdSystem
     // material words).
     std::vector<TetRecord> hostRecords;
     std::vector<double> hostWg;
+    // Host copies for the descent-path traces: lumped masses, Lame coefficients and the
+    // shape-function gradients (row-major 4x3 per tet; from the descriptor's GP when given, else
+    // from the rest positions).
+    std::vector<double> hostM, hostMu, hostLambda, hostGP;
+
+    // The next step is traced in the CPU integrator's format (pbgb_vbd_trace_next_step).
+    bool traceNext = false;
+    std::string tracePath;
+    int32_t traceStep = -1;
 
     // Adjoint tape (pbgb_vbd_adjoint_reserve): one slot per recorded substep, holding the iterates
     // X_0..X_K (nV float4 each) and K x nFree inverse Newton matrices (2 float4 each).
@@ -351,6 +362,10 @@ class VbdSystem
         std::vector<float> hm(nV);
         std::vector<TetRecord> hrec(nT);
         hostWg.assign(size_t(nT), 0.0);
+        hostM.assign(size_t(nV), 0.0);
+        hostMu.assign(size_t(nT), 0.0);
+        hostLambda.assign(size_t(nT), 0.0);
+        hostGP.assign(size_t(nT) * 12, 0.0);
         std::vector<int32_t> deg(nV, 0);
         // Colour of every vertex (free vertices from the partitions; pinned ones are never solved
         // and hold the same value in every position buffer, so any colour works: -1).
@@ -388,7 +403,8 @@ class VbdSystem
                 }
                 else
                     ha[v0 + i] = make_float4(0.f, 0.f, -9.81f, 0.f);
-                hm[v0 + i] = float(d.m[i]);
+                hm[v0 + i]    = float(d.m[i]);
+                hostM[v0 + i] = d.m[i];
                 double const* R = (d.X ? d.X : d.x) + 3 * size_t(i);
                 hX[v0 + i]      = make_float4(float(R[0]), float(R[1]), float(R[2]), 0.f);
             }
@@ -412,7 +428,29 @@ class VbdSystem
                     packed[q] = gv[q] | (rank << 30);
                 }
                 double const w = d.wg[e], mu = d.mu[e], la = d.lambda[e];
-                hostWg[t0 + e] = w;
+                hostWg[t0 + e]     = w;
+                hostMu[t0 + e]     = mu;
+                hostLambda[t0 + e] = la;
+                if (d.GP)
+                    std::copy(d.GP + 12 * size_t(e), d.GP + 12 * size_t(e + 1), hostGP.begin() + 12 * size_t(t0 + e));
+                else
+                {
+                    // Gradients of the linear shape functions from the rest positions (FP64).
+                    double const* R  = d.X ? d.X : d.x;
+                    int32_t const* q = d.T + 4 * size_t(e);
+                    double ed[3][3], Gd[3][3];
+                    for (int mm = 0; mm < 3; ++mm)
+                        for (int r = 0; r < 3; ++r)
+                            ed[mm][r] = R[3 * size_t(q[mm + 1]) + r] - R[3 * size_t(q[0]) + r];
+                    rest_gradients(ed, Gd);
+                    double* out = hostGP.data() + 12 * size_t(t0 + e);
+                    for (int c = 0; c < 3; ++c)
+                    {
+                        out[c] = -(Gd[0][c] + Gd[1][c] + Gd[2][c]);
+                        for (int mm = 0; mm < 3; ++mm)
+                            out[3 * (mm + 1) + c] = Gd[mm][c];
+                    }
+                }
                 TetRecord& r   = hrec[t0 + e];
                 r.v            = make_uint4(packed[0], packed[1], packed[2], packed[3]);
                 r.mat          = make_float4(float(w * mu), float(w * la), float(1.0 + mu / la), 0.f);
@@ -698,6 +736,8 @@ class VbdSystem
         {
             double const w     = hostWg[e];
             hostRecords[e].mat = make_float4(float(w * mu[e]), float(w * lambda[e]), float(1.0 + mu[e] / lambda[e]), 0.f);
+            hostMu[e]          = mu[e];
+            hostLambda[e]      = lambda[e];
         }
         tets.upload(hostRecords.data(), size_t(nT), stream);
         std::vector<float4> hMats(static_cast<size_t>(nT));
@@ -937,11 +977,24 @@ class VbdSystem
     // reference GPU integrator (gpu/impl/vbd/Integrator.cu:82-103): contact active set initialised
     // on the full-step prediction, per substep inertial target + initial guess, contact list update,
     // colour sweeps, velocity update; contact active set finalised at the end.
-    void enqueueStep(float dt, int32_t iterations, int32_t substeps)
+    // Host callbacks of a step run outside a graph (the descent-path traces): after the substep's
+    // inertial target and initial guess, at every iterate (k = 0 .. iterations; `current` holds it)
+    // and after the velocity update.  plain: plain VBD iterations whatever the acceleration, as the
+    // reference's GPU TracedSolve runs them.
+    struct StepHooks
+    {
+        bool plain = false;
+        std::function<void(int32_t s)> substepBegin;
+        std::function<void(int32_t s, int32_t k, float4 const* current)> iterate;
+        std::function<void(int32_t s)> substepEnd;
+    };
+
+    void enqueueStep(float dt, int32_t iterations, int32_t substeps, StepHooks const* hooks = nullptr)
     {
         float const h    = dt / float(substeps);
         float const h2   = h * h;
-        bool const cheb  = acceleration == PBGB_ACCEL_CHEBYSHEV;
+        bool const plainOnly = hooks && hooks->plain;
+        bool const cheb  = !plainOnly && acceleration == PBGB_ACCEL_CHEBYSHEV;
         // Contact reads same-colour partners too, so it always uses the two-buffer sweep (with
         // omega = 1 when there is no acceleration).
         bool const twoBuffer = cheb || contact;
@@ -993,9 +1046,11 @@ class VbdSystem
             check(launch_begin_substep(sp, stream), "begin_substep");
             if (contact && s % activeSetFreq == 0)
                 check(contact_update(cmesh, cstate, x.get(), stream), "contact_update");
+            if (hooks && hooks->substepBegin)
+                hooks->substepBegin(s);
             double omega      = 0.0;
             double const rho2 = rho * rho;
-            bool const anderson = acceleration == PBGB_ACCEL_ANDERSON;
+            bool const anderson = !plainOnly && acceleration == PBGB_ACCEL_ANDERSON;
             AndersonParams ap{};
             if (anderson)
             {
@@ -1015,6 +1070,8 @@ class VbdSystem
             }
             for (int32_t k = 0; k < iterations; ++k)
             {
+                if (hooks && hooks->iterate)
+                    hooks->iterate(s, k, twoBuffer ? H[(k + 1) % 2] : x.get());
                 if (twoBuffer)
                 {
                     if (cheb)
@@ -1053,10 +1110,131 @@ class VbdSystem
                     }
                 }
             }
+            if (hooks && hooks->iterate)
+                hooks->iterate(s, iterations, twoBuffer && iterations > 0 ? sp.result : x.get());
             check(launch_end_substep(sp, stream), "end_substep");
+            if (hooks && hooks->substepEnd)
+                hooks->substepEnd(s);
         }
         if (contact)
             check(contact_finalize(cmesh, cstate, x.get(), stream), "contact_finalize");
+    }
+
+    // Dense Matrix Market ("array" format, column-major) of a rows x cols matrix; value(r, c).
+    template <class F>
+    static void writeMarket(std::string const& path, int64_t rows, int64_t cols, bool integer, F&& value)
+    {
+        std::FILE* f = std::fopen(path.c_str(), "w");
+        if (!f)
+            throw std::invalid_argument("cannot write " + path);
+        std::fprintf(f, "%%%%MatrixMarket matrix array %s general\n%lld %lld\n", integer ? "integer" : "real",
+                     static_cast<long long>(rows), static_cast<long long>(cols));
+        for (int64_t c = 0; c < cols; ++c)
+            for (int64_t r = 0; r < rows; ++r)
+            {
+                if (integer)
+                    std::fprintf(f, "%lld\n", static_cast<long long>(value(r, c)));
+                else
+                    std::fprintf(f, "%.17g\n", static_cast<double>(value(r, c)));
+            }
+        bool const ok = std::fclose(f) == 0;
+        if (!ok)
+            throw std::invalid_argument("cannot write " + path);
+    }
+
+    std::vector<float4> deviceToHost(float4 const* src)
+    {
+        std::vector<float4> out(static_cast<size_t>(nV));
+        if (nV > 0)
+            check(cudaMemcpyAsync(out.data(), src, sizeof(float4) * size_t(nV), cudaMemcpyDeviceToHost, stream), "D2H");
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+        return out;
+    }
+
+    // Integrator::TracedStep of the reference GPU integrator (gpu/impl/vbd/Integrator.cu:105-148,
+    // 284-301): on frame 0 the mesh and material (T, M, wg, GP, lame), then per substep the
+    // inertial target xtilde.t.{t}.s.{s}.mtx and every iterate x.t.{t}.s.{s}.k.{k}.mtx of plain VBD
+    // iterations (k = 0 .. iterations).
+    void tracedStep(float dt, int32_t iterations, int32_t substeps, int32_t t, std::string const& dir)
+    {
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+        auto at = [&](std::string const& name) { return dir + "/" + name; };
+        if (t == 0)
+        {
+            writeMarket(at("T.mtx"), nT, 4, true, [&](int64_t e, int64_t q) {
+                uint4 const v = hostRecords[size_t(e)].v;
+                uint32_t const c4[4] = {v.x, v.y, v.z, v.w};
+                return int64_t(c4[q] & kIndexMask);
+            });
+            writeMarket(at("M.mtx"), nV, 1, false, [&](int64_t i, int64_t) { return hostM[size_t(i)]; });
+            writeMarket(at("wg.mtx"), nT, 1, false, [&](int64_t e, int64_t) { return hostWg[size_t(e)]; });
+            // GP: 4 x 3 nT, column 3e + d holding d/dX_d of the 4 shape functions of tet e.
+            writeMarket(at("GP.mtx"), 4, 3 * int64_t(nT), false, [&](int64_t a, int64_t c) {
+                return hostGP[12 * size_t(c / 3) + 3 * size_t(a) + size_t(c % 3)];
+            });
+            writeMarket(at("lame.mtx"), nT, 2, false, [&](int64_t e, int64_t q) {
+                return q == 0 ? hostMu[size_t(e)] : hostLambda[size_t(e)];
+            });
+        }
+        StepHooks hooks;
+        hooks.plain        = true;
+        hooks.substepBegin = [&](int32_t s) {
+            std::vector<float4> const xt4 = deviceToHost(xtilde.get());
+            writeMarket(at("xtilde.t." + std::to_string(t) + ".s." + std::to_string(s) + ".mtx"), nV, 3, false,
+                        [&](int64_t i, int64_t c) { return (&xt4[size_t(i)].x)[c]; });
+        };
+        hooks.iterate = [&](int32_t s, int32_t k, float4 const* current) {
+            std::vector<float4> const x4 = deviceToHost(current);
+            writeMarket(at("x.t." + std::to_string(t) + ".s." + std::to_string(s) + ".k." + std::to_string(k) + ".mtx"),
+                        nV, 3, false, [&](int64_t i, int64_t c) { return (&x4[size_t(i)].x)[c]; });
+        };
+        enqueueStep(dt, iterations, substeps, &hooks);
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    }
+
+    // The reference CPU integrator's trace of one step (sim/vbd/Integrator.cpp:22-45,202-235): per
+    // substep, the FP64 objective, its gradient and the positions at every iterate k = 0 ..
+    // iterations (before each VBD iteration, then the result), written as {t}.{s}.f.mtx
+    // (iterations+1 x 1), {t}.{s}.grad.mtx and {t}.{s}.x.mtx (3 nV x iterations+1).
+    void tracedStepCpuFormat(float dt, int32_t iterations, int32_t substeps)
+    {
+        double const h = double(dt) / double(substeps);
+        if (gradBuf.size() < size_t(nV) * 3)
+            gradBuf.allocate(size_t(nV) * 3);
+        std::vector<double> fs, gs, xs;
+        StepHooks hooks;
+        hooks.iterate = [&](int32_t, int32_t, float4 const* current) {
+            check(cudaMemsetAsync(red.get(), 0, sizeof(double), stream), "memset");
+            check(launch_objective(energyParams(h, red.get(), current), stream), "objective");
+            check(cudaMemsetAsync(gradBuf.get(), 0, sizeof(double) * 3 * size_t(nV), stream), "memset");
+            check(launch_gradient(energyParams(h, gradBuf.get(), current), stream), "gradient");
+            double f = 0.0;
+            std::vector<double> g(3 * size_t(nV));
+            check(cudaMemcpyAsync(&f, red.get(), sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H");
+            if (nV > 0)
+                check(cudaMemcpyAsync(g.data(), gradBuf.get(), sizeof(double) * g.size(), cudaMemcpyDeviceToHost, stream), "D2H");
+            std::vector<float4> const x4 = deviceToHost(current);
+            fs.push_back(f);
+            gs.insert(gs.end(), g.begin(), g.end());
+            for (auto const& q : x4)
+            {
+                xs.push_back(q.x);
+                xs.push_back(q.y);
+                xs.push_back(q.z);
+            }
+        };
+        hooks.substepEnd = [&](int32_t s) {
+            std::string const base = tracePath + "/" + std::to_string(traceStep) + "." + std::to_string(s);
+            int64_t const n = int64_t(fs.size()), rows = 3 * int64_t(nV);
+            writeMarket(base + ".f.mtx", n, 1, false, [&](int64_t r, int64_t) { return fs[size_t(r)]; });
+            writeMarket(base + ".grad.mtx", rows, n, false, [&](int64_t r, int64_t c) { return gs[size_t(c * rows + r)]; });
+            writeMarket(base + ".x.mtx", rows, n, false, [&](int64_t r, int64_t c) { return xs[size_t(c * rows + r)]; });
+            fs.clear();
+            gs.clear();
+            xs.clear();
+        };
+        enqueueStep(dt, iterations, substeps, &hooks);
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
     }
 
     int64_t launchesPerStep(int32_t iterations, int32_t substeps) const
@@ -1079,6 +1257,12 @@ class VbdSystem
 
     void step(float dt, int32_t iterations, int32_t substeps)
     {
+        if (traceNext)
+        {
+            traceNext = false;
+            tracedStepCpuFormat(dt, iterations, substeps);
+            return;
+        }
         if (!graphValid || dt != gDt || iterations != gIters || substeps != gSub)
         {
             if (graph)
@@ -1262,10 +1446,10 @@ class VbdSystem
         check(launch_pack3(staging.get(), dst.get(), nV, stream), "pack");
     }
 
-    EnergyParams energyParams(double dt, double* out) const
+    EnergyParams energyParams(double dt, double* out, float4 const* at = nullptr) const
     {
         EnergyParams p{};
-        p.x      = x.get();
+        p.x      = at ? at : x.get();
         p.xtilde = xtilde.get();
         p.m      = m.get();
         p.tets   = tets.get();
@@ -1431,6 +1615,28 @@ PBGB_API int pbgb_vbd_step(pbgb_vbd* h, float dt, int32_t iterations, int32_t su
         h->sys.step(dt, iterations, substeps);
         return int(kOk);
     });
+}
+
+PBGB_API int pbgb_vbd_traced_step(pbgb_vbd* h, float dt, int32_t iterations, int32_t substeps, int32_t t, const char* dir)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (!dir || !(dt > 0.f) || !std::isfinite(dt) || iterations < 0 || substeps < 1)
+        return fail(h, kInvalid, "pbgb_vbd_traced_step: expected a directory, dt > 0, iterations >= 0, substeps >= 1");
+    return guarded(h, [&] {
+        h->sys.tracedStep(dt, iterations, substeps, t, std::string(dir));
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_trace_next_step(pbgb_vbd* h, const char* path, int32_t t)
+{
+    if (!h || !path)
+        return fail(h, kInvalid, "null argument");
+    h->sys.traceNext = true;
+    h->sys.tracePath = path;
+    h->sys.traceStep = t;
+    return kOk;
 }
 
 PBGB_API int pbgb_vbd_synchronize(pbgb_vbd* h)

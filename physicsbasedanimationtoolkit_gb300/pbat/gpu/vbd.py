@@ -24,6 +24,12 @@ class Integrator(IntegratorBase):
         """Integrate 1 time step (dt, iterations per substep, substeps)."""
         self._step(dt, iterations, substeps)
 
+    def traced_step(self, dt=0.01, iterations=20, substeps=1, t=0, dir="."):
+        """Integrate 1 time step and trace the result to disk as Matrix Market files named
+        {variable}.t.{timestep}.s.{substep}[.k.{iteration}].mtx (plain VBD iterations)."""
+        _capi.check(_capi.lib().pbgb_vbd_traced_step(self._h, float(dt), int(iterations), int(substeps), int(t),
+                                                    str(dir).encode()), self._h)
+
     @property
     def x(self):
         """3 x |#vertices| vertex positions (float32)."""

@@ -286,6 +286,11 @@ class Integrator(IntegratorBase):
     def step(self, dt, iterations, substeps=1):
         self._step(dt, iterations, substeps)
 
+    def trace_next_step(self, path=".", t=-1):
+        """Trace the next step: per substep, {path}/{t}.{s}.f.mtx, .grad.mtx and .x.mtx hold the
+        objective, its gradient and the positions at every iterate (Matrix Market)."""
+        _capi.check(_capi.lib().pbgb_vbd_trace_next_step(self._h, str(path).encode(), int(t)), self._h)
+
     @property
     def x(self):
         return self._get("x").astype(np.float64)
