@@ -577,17 +577,13 @@ def main():
 
     import torch
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+    from physicsbasedanimationtoolkit_gb300 import _capi, pbat
+    from physicsbasedanimationtoolkit_gb300.replicas import Replicas
+
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
-
-    from physicsbasedanimationtoolkit_gb300 import _capi, pbat
+    group = Replicas("nccl", device=torch.device("cuda", local))
+    rank, world = group.rank, group.world
 
     if args.only:
         legs = {
@@ -599,6 +595,7 @@ def main():
         }
         if rank == 0:
             print(json.dumps({"only": args.only, args.only: legs[args.only]()}))
+        group.close()
         return 0
 
     w = workload_beam(args)
@@ -626,8 +623,7 @@ def main():
     sweep_launches = 0
     ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    if dist:
-        dist.barrier()
+    group.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         for k in range(args.steps):
@@ -644,14 +640,11 @@ def main():
             sweep_ms += ms.value
             sweep_launches += nl.value
         torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-        t = torch.tensor([t_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_total = float(t.item())
+    group.barrier()
+    t_total = group.max(t_total)
     ms_per_step = t_total / args.steps
     updates_per_step = n_free * iters
-    value = world * updates_per_step * args.steps / (t_total * 1e-3)
+    value = group.sum(updates_per_step * args.steps) / (t_total * 1e-3)
 
     launches_per_step = vbd.launches_per_step(iters, 1)
     n_colors = vbd.n_colors
@@ -665,8 +658,7 @@ def main():
     vbd.step(dt, iters, 1)  # re-capture the graph without timing events
     vbd.synchronize()
     e2e_steps = max(3, args.steps // 2)
-    if dist:
-        dist.barrier()
+    group.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         _capi.check(L.pbgb_vbd_set_positions(h, xh.data_ptr()), h)
@@ -674,12 +666,8 @@ def main():
         _capi.check(L.pbgb_vbd_step(h, dt, iters, 1), h)
         _capi.check(L.pbgb_vbd_get_positions(h, xh.data_ptr()), h)
         _capi.check(L.pbgb_vbd_get_velocities(h, vh.data_ptr()), h)
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * updates_per_step * e2e_steps / e2e_s
+    e2e_s = group.max(time.perf_counter() - t0)
+    e2e_value = group.sum(updates_per_step * e2e_steps) / e2e_s
     io_bytes = nV * 3 * 4 * 2
 
     if rank == 0:
@@ -736,8 +724,7 @@ def main():
             "anderson": anderson,
         }
         print(json.dumps(line))
-    if dist:
-        dist.destroy_process_group()
+    group.close()
     return 0
 
 
