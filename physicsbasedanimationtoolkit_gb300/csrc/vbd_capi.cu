@@ -85,6 +85,116 @@ class DeviceArray
 
 } // namespace
 
+// Host checks of a batch of descriptors, before any device work (the reference validates in
+// Data::Construct, sim/vbd/Data.cpp:259-305): present and in-range fields, finite and positive
+// physical inputs, and a valid colouring -- every free vertex in exactly one partition, and no two
+// free vertices of one colour in the same tet (the sweep updates a colour's vertices in place and
+// relies on it).
+inline void validate_descs(pbgb_vbd_desc const* descs, int32_t nMeshes)
+{
+    auto bad = [](char const* what) { throw std::invalid_argument(std::string("pbgb_vbd_desc: ") + what); };
+    auto finite = [](double const* a, int64_t n) {
+        for (int64_t k = 0; k < n; ++k)
+            if (!std::isfinite(a[k]))
+                return false;
+        return true;
+    };
+    int64_t totV = 0, totT = 0;
+    for (int32_t b = 0; b < nMeshes; ++b)
+    {
+        auto const& d = descs[b];
+        if (d.n_vertices < 0 || d.n_tets < 0 || !d.x || (d.n_tets > 0 && !d.T) || !d.m ||
+            (d.n_tets > 0 && (!d.wg || !d.mu || !d.lambda)) || d.n_partitions < 0 ||
+            d.n_partitions > kMaxColors || !d.Pptr || (d.Pptr[d.n_partitions] > 0 && !d.Padj))
+            bad("missing or invalid field");
+        int64_t const n3 = 3 * int64_t(d.n_vertices);
+        if (!finite(d.x, n3) || (d.X && !finite(d.X, n3)) || (d.v && !finite(d.v, n3)) ||
+            (d.aext && !finite(d.aext, n3)))
+            bad("non-finite positions, velocities or accelerations");
+        for (int32_t i = 0; i < d.n_vertices; ++i)
+            if (!(d.m[i] >= 0.0) || !std::isfinite(d.m[i]))
+                bad("masses must be finite and non-negative");
+        for (int32_t e = 0; e < d.n_tets; ++e)
+            if (!(d.wg[e] > 0.0) || !(d.mu[e] > 0.0) || !(d.lambda[e] > 0.0) || !std::isfinite(d.wg[e]) ||
+                !std::isfinite(d.mu[e]) || !std::isfinite(d.lambda[e]))
+                bad("quadrature weights and Lame coefficients must be finite and positive");
+        if (!std::isfinite(d.kD) || d.kD < 0.0 || !std::isfinite(d.detHZero) || d.detHZero < 0.0)
+            bad("damping and the Hessian determinant threshold must be finite and non-negative");
+        for (int64_t k = 0; k < int64_t(d.n_tets) * 4; ++k)
+            if (d.T[k] < 0 || d.T[k] >= d.n_vertices)
+                bad("tetrahedron index out of range");
+        if (d.Pptr[0] != 0)
+            bad("partition pointers must start at 0");
+        for (int32_t c = 0; c < d.n_partitions; ++c)
+            if (d.Pptr[c + 1] < d.Pptr[c])
+                bad("partition pointers must not decrease");
+        std::vector<int32_t> colour(static_cast<size_t>(d.n_vertices), -1);
+        for (int32_t c = 0; c < d.n_partitions; ++c)
+            for (int32_t k = d.Pptr[c]; k < d.Pptr[c + 1]; ++k)
+            {
+                int32_t const v = d.Padj[k];
+                if (v < 0 || v >= d.n_vertices)
+                    bad("partition vertex out of range");
+                if (colour[v] >= 0)
+                    bad("a vertex appears in more than one partition");
+                colour[v] = c;
+            }
+        for (int32_t e = 0; e < d.n_tets; ++e)
+        {
+            int32_t const* t = d.T + 4 * size_t(e);
+            for (int a = 0; a < 4; ++a)
+                for (int q = a + 1; q < 4; ++q)
+                {
+                    if (t[a] == t[q])
+                        bad("a tetrahedron repeats a vertex");
+                    if (colour[t[a]] >= 0 && colour[t[a]] == colour[t[q]])
+                        bad("invalid colouring: two vertices of one colour share a tetrahedron");
+                }
+        }
+        if (d.acceleration == PBGB_ACCEL_CHEBYSHEV && !(d.rho > 0.0 && d.rho < 1.0))
+            throw std::invalid_argument("Expected 0 < rho < 1");
+        if (d.acceleration != PBGB_ACCEL_NONE && d.acceleration != PBGB_ACCEL_CHEBYSHEV &&
+            d.acceleration != PBGB_ACCEL_ANDERSON)
+            bad("unsupported acceleration strategy");
+        if (d.acceleration == PBGB_ACCEL_ANDERSON)
+        {
+            if (d.window_size < 1 || d.window_size > kAndersonMaxWindow)
+                bad("Anderson window must be in [1, 16]");
+            if (nMeshes != 1 || d.n_collision_triangles > 0)
+                bad("Anderson acceleration needs a single mesh without contact");
+        }
+        if (d.init_strategy < 0 || d.init_strategy > 4)
+            bad("invalid initialization strategy");
+        if (d.n_collision_triangles > 0)
+        {
+            if (d.n_collision_vertices <= 0 || !d.V || !d.F || !d.XVA || !d.FA)
+                bad("contact needs V, F, XVA and FA");
+            for (int32_t k = 0; k < d.n_collision_vertices; ++k)
+                if (d.V[k] < 0 || d.V[k] >= d.n_vertices)
+                    bad("collision vertex out of range");
+            for (int64_t k = 0; k < 3 * int64_t(d.n_collision_triangles); ++k)
+                if (d.F[k] < 0 || d.F[k] >= d.n_vertices)
+                    bad("collision triangle index out of range");
+            for (int32_t i = 0; i < d.n_vertices; ++i)
+                if (!(d.XVA[i] >= 0.0) || !std::isfinite(d.XVA[i]))
+                    bad("vertex areas must be finite and non-negative");
+            for (int32_t f = 0; f < d.n_collision_triangles; ++f)
+                if (!(d.FA[f] >= 0.0) || !std::isfinite(d.FA[f]))
+                    bad("triangle areas must be finite and non-negative");
+            if (!(d.muC >= 0.0) || !(d.muF >= 0.0) || !(d.epsv > 0.0))
+                bad("contact parameters must satisfy muC >= 0, muF >= 0, epsv > 0");
+            if (d.active_set_update_frequency < 1)
+                bad("active set update frequency must be >= 1");
+            if (nMeshes != 1)
+                bad("contact is supported on a single (non-batched) mesh");
+        }
+        totV += d.n_vertices;
+        totT += d.n_tets;
+    }
+    if (totV > INT32_MAX || totT >= (int64_t(1) << 30) || totT * 4 > INT32_MAX)
+        bad("system too large for 32-bit indexing");
+}
+
 class VbdSystem
 {
   public:
@@ -305,36 +415,12 @@ class VbdSystem
 
     void build(pbgb_vbd_desc const* descs, int32_t nMeshes)
     {
-        // Totals and validation.
+        validate_descs(descs, nMeshes);
         int64_t totV = 0, totT = 0, totFree = 0;
         int32_t maxC = 0;
         for (int32_t b = 0; b < nMeshes; ++b)
         {
             auto const& d = descs[b];
-            if (d.n_vertices < 0 || d.n_tets < 0 || !d.x || (d.n_tets > 0 && !d.T) || !d.m ||
-                (d.n_tets > 0 && (!d.wg || !d.mu || !d.lambda)) || d.n_partitions < 0 ||
-                d.n_partitions > kMaxColors || !d.Pptr || (d.Pptr[d.n_partitions] > 0 && !d.Padj))
-                throw std::invalid_argument("pbgb_vbd_desc: missing or invalid field");
-            for (int64_t k = 0; k < int64_t(d.n_tets) * 4; ++k)
-                if (d.T[k] < 0 || d.T[k] >= d.n_vertices)
-                    throw std::invalid_argument("pbgb_vbd_desc: tetrahedron index out of range");
-            for (int32_t k = 0; k < d.Pptr[d.n_partitions]; ++k)
-                if (d.Padj[k] < 0 || d.Padj[k] >= d.n_vertices)
-                    throw std::invalid_argument("pbgb_vbd_desc: partition vertex out of range");
-            if (d.acceleration == PBGB_ACCEL_CHEBYSHEV && !(d.rho > 0.0 && d.rho < 1.0))
-                throw std::invalid_argument("Expected 0 < rho < 1");
-            if (d.acceleration != PBGB_ACCEL_NONE && d.acceleration != PBGB_ACCEL_CHEBYSHEV &&
-                d.acceleration != PBGB_ACCEL_ANDERSON)
-                throw std::invalid_argument("pbgb_vbd_desc: unsupported acceleration strategy");
-            if (d.acceleration == PBGB_ACCEL_ANDERSON)
-            {
-                if (d.window_size < 1 || d.window_size > kAndersonMaxWindow)
-                    throw std::invalid_argument("pbgb_vbd_desc: Anderson window must be in [1, 16]");
-                if (nMeshes != 1 || d.n_collision_triangles > 0)
-                    throw std::invalid_argument("Anderson acceleration needs a single mesh without contact");
-            }
-            if (d.init_strategy < 0 || d.init_strategy > 4)
-                throw std::invalid_argument("pbgb_vbd_desc: invalid initialization strategy");
             totV += d.n_vertices;
             totT += d.n_tets;
             totFree += d.Pptr[d.n_partitions];
@@ -1520,6 +1606,13 @@ int create_impl(pbgb_vbd_desc const* descs, int32_t n, pbgb_vbd** out)
     if (!descs || n < 1 || !out)
         return fail(nullptr, kInvalid, "pbgb_vbd_create: null argument or empty batch");
     *out = nullptr;
+    // Descriptor errors are reported whether or not a device is present.
+    int const rc0 = guarded(nullptr, [&] {
+        pbgb::validate_descs(descs, n);
+        return int(kOk);
+    });
+    if (rc0 != kOk)
+        return rc0;
     int devices = 0;
     if (cudaGetDeviceCount(&devices) != cudaSuccess || devices < 1)
     {

@@ -151,3 +151,51 @@ def test_unsupported_accelerations_are_rejected(accel):
          "trust_region": lambda: d.with_trust_region_acceleration(0.2, 2.0, True)}[accel]().construct()
     with pytest.raises(NotImplementedError):
         pbat.gpu.vbd.Integrator(d)
+
+
+def _cube_data():
+    w = meshgen.unit_cube_workload(n=3, seed=1)
+    return (pbat.sim.vbd.Data().with_volume_mesh(w["X"].T, w["T"].T).with_material(w["rho"], w["mu"], w["lam"])
+            .with_dirichlet_vertices(w["dbc"]).construct())
+
+
+@pytest.mark.parametrize("defect", ["colouring", "duplicate", "nan_x", "zero_wg", "negative_lambda"])
+def test_descriptor_errors_are_reported_without_a_device(defect):
+    """Host validation runs before the device query, so a bad descriptor is an invalid argument
+    (with its message) whether or not a GPU is present."""
+    d = _cube_data()
+    if defect == "colouring":
+        # Move a vertex into the colour of one of its neighbours.
+        ptr, adj = d.Pptr.copy(), d.Padj.copy()
+        T = np.asarray(d.E).T
+        v = int(adj[ptr[0]])
+        nb = next(int(u) for t in T if v in t for u in t if u != v and u in adj[ptr[1]:ptr[2]])
+        k = int(np.nonzero(adj == nb)[0][0])
+        adj[k] = v
+        adj[ptr[0]] = nb
+        d.Padj = adj
+        expect = "invalid colouring"
+    elif defect == "duplicate":
+        adj = d.Padj.copy()
+        adj[1] = adj[0]
+        d.Padj = adj
+        expect = "more than one partition"
+    elif defect == "nan_x":
+        x = np.array(d.x, dtype=np.float64)
+        x[0, 3] = np.nan
+        d.x = x
+        expect = "non-finite"
+    elif defect == "zero_wg":
+        wg = d.wg.copy()
+        wg[2] = 0.0
+        d.wg = wg
+        expect = "quadrature weights"
+    else:
+        lame = np.array(d.lame, dtype=np.float64)
+        lame[1, 0] = -1.0
+        d.lame = lame
+        expect = "Lame"
+    with pytest.raises(_capi.PbgbError) as e:
+        pbat.gpu.vbd.Integrator(d)
+    assert e.value.code == 1, e.value
+    assert expect in str(e.value)
