@@ -182,6 +182,14 @@ PBGB_API int pbgb_vbd_set_positions(pbgb_vbd* h, const float* x);
 PBGB_API int pbgb_vbd_get_velocities(pbgb_vbd* h, float* v);
 PBGB_API int pbgb_vbd_set_velocities(pbgb_vbd* h, const float* v);
 PBGB_API int pbgb_vbd_set_external_acceleration(pbgb_vbd* h, const float* aext);
+/* Checkpoint / resume: the whole state a step reads (positions, velocities, the previous step's
+ * velocities, external accelerations, and with contact the persistent active set, search radii and
+ * contact lists) as one host blob with a header.  A handle built from the same descriptors that
+ * loads the blob continues bit for bit.  pbgb_vbd_state_size gives the blob's size; save and load
+ * synchronize; loading a blob of another system size is PBGB_ERR_INVALID_ARGUMENT. */
+PBGB_API int pbgb_vbd_state_size(pbgb_vbd* h, size_t* bytes);
+PBGB_API int pbgb_vbd_save_state(pbgb_vbd* h, void* blob, size_t bytes);
+PBGB_API int pbgb_vbd_load_state(pbgb_vbd* h, const void* blob, size_t bytes);
 /* Device-pointer variants (3 x nV float32 on the handle's device), stream-ordered. */
 PBGB_API int pbgb_vbd_get_positions_device(pbgb_vbd* h, float* x_dev);
 PBGB_API int pbgb_vbd_set_positions_device(pbgb_vbd* h, const float* x_dev);

@@ -99,6 +99,9 @@ _SIGNATURES = [
     ("pbgb_vbd_get_positions_device", C.c_int, [_vp, _vp]),
     ("pbgb_vbd_set_positions_device", C.c_int, [_vp, _vp]),
     ("pbgb_vbd_traced_step", C.c_int, [_vp, _f32, _i32, _i32, _i32, C.c_char_p]),
+    ("pbgb_vbd_state_size", C.c_int, [_vp, C.POINTER(C.c_size_t)]),
+    ("pbgb_vbd_save_state", C.c_int, [_vp, _vp, C.c_size_t]),
+    ("pbgb_vbd_load_state", C.c_int, [_vp, _vp, C.c_size_t]),
     ("pbgb_vbd_trace_next_step", C.c_int, [_vp, C.c_char_p, _i32]),
     ("pbgb_vbd_get_velocities_device", C.c_int, [_vp, _vp]),
     ("pbgb_vbd_set_velocities_device", C.c_int, [_vp, _vp]),

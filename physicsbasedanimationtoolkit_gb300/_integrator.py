@@ -198,6 +198,20 @@ class IntegratorBase:
         _capi.check(_capi.lib().pbgb_vbd_get_contacts(self._h, fc.ctypes.data, active.ctypes.data), self._h)
         return fc, active[:nS]
 
+    def save_state(self):
+        """Checkpoint of the step state (positions, velocities, previous velocities, external
+        accelerations, contact active set and lists) as bytes."""
+        n = C.c_size_t()
+        _capi.check(_capi.lib().pbgb_vbd_state_size(self._h, C.byref(n)), self._h)
+        buf = (C.c_ubyte * n.value)()
+        _capi.check(_capi.lib().pbgb_vbd_save_state(self._h, buf, n.value), self._h)
+        return bytes(buf)
+
+    def load_state(self, blob):
+        """Resume from save_state's bytes (a handle built from the same data)."""
+        buf = (C.c_ubyte * len(blob)).from_buffer_copy(blob)
+        _capi.check(_capi.lib().pbgb_vbd_load_state(self._h, buf, len(blob)), self._h)
+
     def set_material(self, mu, lam):
         """Per-tet Lame coefficients (|#tets| each, system order); masses are kept."""
         mu = np.ascontiguousarray(mu, dtype=np.float64).ravel()

@@ -1228,6 +1228,85 @@ class VbdSystem
             throw std::invalid_argument("cannot write " + path);
     }
 
+    // Checkpoint blob: header, x, v, vprev, aext (nV float4 each), then with contact the active
+    // flags (nSurfV bytes, padded to 4), search radii (nSurfV float) and contact lists (8 nV int32).
+    struct StateHeader
+    {
+        uint32_t magic;
+        uint32_t version;
+        int32_t nV;
+        int32_t nSurfV;
+        int32_t contact;
+        int32_t reserved;
+    };
+    static uint32_t constexpr kStateMagic = 0x53474250u; // "PBGS"
+
+    size_t stateBytes() const
+    {
+        size_t b = sizeof(StateHeader) + 4 * sizeof(float4) * size_t(nV);
+        if (contact)
+            b += ((size_t(cmesh.nSurfV) + 3) & ~size_t(3)) + sizeof(float) * size_t(cmesh.nSurfV) +
+                 sizeof(int32_t) * 8 * size_t(nV);
+        return b;
+    }
+
+    template <class F>
+    void stateParts(F&& part)
+    {
+        size_t const v4 = sizeof(float4) * size_t(nV);
+        part(static_cast<void*>(x.get()), v4);
+        part(static_cast<void*>(v.get()), v4);
+        part(static_cast<void*>(vprev.get()), v4);
+        part(static_cast<void*>(aext.get()), v4);
+        if (contact)
+        {
+            part(static_cast<void*>(cActive.get()), size_t(cmesh.nSurfV));
+            part(nullptr, ((size_t(cmesh.nSurfV) + 3) & ~size_t(3)) - size_t(cmesh.nSurfV)); // padding
+            part(static_cast<void*>(cDupper.get()), sizeof(float) * size_t(cmesh.nSurfV));
+            part(static_cast<void*>(cFc.get()), sizeof(int32_t) * 8 * size_t(nV));
+        }
+    }
+
+    void saveState(void* blob, size_t bytes)
+    {
+        if (bytes < stateBytes())
+            throw std::invalid_argument("pbgb_vbd_save_state: buffer smaller than pbgb_vbd_state_size");
+        StateHeader hd{kStateMagic, 1u, nV, contact ? cmesh.nSurfV : 0, contact ? 1 : 0, 0};
+        auto* out = static_cast<unsigned char*>(blob);
+        std::memcpy(out, &hd, sizeof(hd));
+        size_t off = sizeof(hd);
+        stateParts([&](void* dev, size_t n) {
+            if (n == 0)
+                return;
+            if (dev)
+                check(cudaMemcpyAsync(out + off, dev, n, cudaMemcpyDeviceToHost, stream), "D2H");
+            else
+                std::memset(out + off, 0, n);
+            off += n;
+        });
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    }
+
+    void loadState(void const* blob, size_t bytes)
+    {
+        StateHeader hd{};
+        if (bytes < sizeof(hd))
+            throw std::invalid_argument("pbgb_vbd_load_state: blob too small");
+        std::memcpy(&hd, blob, sizeof(hd));
+        if (hd.magic != kStateMagic || hd.version != 1u || hd.nV != nV || hd.contact != (contact ? 1 : 0) ||
+            hd.nSurfV != (contact ? cmesh.nSurfV : 0) || bytes < stateBytes())
+            throw std::invalid_argument("pbgb_vbd_load_state: the blob belongs to another system");
+        auto const* in = static_cast<unsigned char const*>(blob);
+        size_t off     = sizeof(hd);
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+        stateParts([&](void* dev, size_t n) {
+            if (dev && n)
+                check(cudaMemcpyAsync(dev, in + off, n, cudaMemcpyHostToDevice, stream), "H2D");
+            off += n;
+        });
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    }
+
     std::vector<float4> deviceToHost(float4 const* src)
     {
         std::vector<float4> out(static_cast<size_t>(nV));
@@ -1827,6 +1906,34 @@ PBGB_API int pbgb_vbd_set_velocities_device(pbgb_vbd* h, const float* v_dev)
     PBGB_CHECK_HANDLE_PTR(h, v_dev)
     return guarded(h, [&] {
         pbgb::check(pbgb::launch_pack3(v_dev, h->sys.v.get(), h->sys.nV, h->sys.stream), "pack");
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_state_size(pbgb_vbd* h, size_t* bytes)
+{
+    if (!h || !bytes)
+        return fail(h, kInvalid, "null argument");
+    *bytes = h->sys.stateBytes();
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_save_state(pbgb_vbd* h, void* blob, size_t bytes)
+{
+    if (!h || !blob)
+        return fail(h, kInvalid, "null argument");
+    return guarded(h, [&] {
+        h->sys.saveState(blob, bytes);
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_load_state(pbgb_vbd* h, const void* blob, size_t bytes)
+{
+    if (!h || !blob)
+        return fail(h, kInvalid, "null argument");
+    return guarded(h, [&] {
+        h->sys.loadState(blob, bytes);
         return int(kOk);
     });
 }
