@@ -87,6 +87,11 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
+            # nvidia-smi takes a moment to start: wait for its first sample so that the timed
+            # region is sampled from its beginning.
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -285,12 +290,13 @@ def run_batch(args, pbat, _capi, torch):
     # One mesh at a time (each step waited for before the next mesh's), as separate integrators
     # run by a caller that does not overlap them.  After the agreement check: it advances the
     # single integrators further.
+    serial_steps = min(args.steps, 10)  # ~0.25 s per step: bounded so the leg stays short
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(serial_steps):
         for s in singles:
             s.step(dt, iters, 1)
             s.synchronize()
-    t_serial = time.perf_counter() - t0
+    t_serial = (time.perf_counter() - t0) * args.steps / serial_steps
     launches = B.launches_per_step(iters, 1)
     return {
         "workload": f"{len(meshes)} cube grids, side U{{6..32}} hexes x 6 tets, {iters} iterations, no acceleration",
@@ -366,11 +372,12 @@ def run_adjoint(args, pbat, torch):
     }
 
 
-def run_anderson(args, pbat, torch):
-    """Anderson acceleration (window 5) on the benchmark beam [0,4]x[0,1]^2 at 160x40x40 hexes
-    (270,641 vertices, 1,536,000 tets), 50 iterations per step, dt = 1/60, against plain VBD with
-    the same iterations from the same state: step time (CUDA events on the integrator's stream)
-    and the norm of the FP64 objective gradient over the free vertices after one step."""
+def run_accelerated(args, pbat, torch, kind):
+    """An accelerated solve on the benchmark beam [0,4]x[0,1]^2 at 160x40x40 hexes (270,641
+    vertices, 1,536,000 tets), 50 iterations per step, dt = 1/60, against plain VBD with the same
+    iterations from the same state: step time (CUDA events on the integrator's stream) and the norm
+    of the FP64 objective gradient over the free vertices after one step.  kind: "anderson"
+    (window 5) or "trust_region" (linear path, eta 0.2, tau 2)."""
     import ctypes as C
 
     from physicsbasedanimationtoolkit_gb300 import _capi
@@ -378,11 +385,13 @@ def run_anderson(args, pbat, torch):
     w = workload_beam(args)
     dt, iters = 1 / 60, 50
 
-    def measure(window):
+    def measure(accel):
         d = (pbat.sim.vbd.Data().with_volume_mesh(w["X"].T, w["T"].T).with_material(w["rho"], w["mu"], w["lam"])
              .with_dirichlet_vertices(w["dbc"]).with_velocity(w["v"].T).with_initialization_strategy(2))
-        if window:
-            d = d.with_anderson_acceleration(window)
+        if accel == "anderson":
+            d = d.with_anderson_acceleration(5)
+        elif accel == "trust_region":
+            d = d.with_trust_region_acceleration(0.2, 2.0, False)
         I = pbat.gpu.vbd.Integrator(d.construct())
         x0, v0 = I.x.copy(), I.v.copy()
         I.step(dt, iters, 1)
@@ -404,11 +413,10 @@ def run_anderson(args, pbat, torch):
         I.synchronize()
         return e0.elapsed_time(e1) / args.steps, gnorm, I.n_free
 
-    ms_a, g_a, n_free = measure(5)
-    ms_p, g_p, _ = measure(0)
-    return {
+    ms_a, g_a, n_free = measure(kind)
+    ms_p, g_p, _ = measure(None)
+    out = {
         "workload": "beam 160x40x40 hexes x 6 tets, 50 iterations, dt 1/60, KineticEnergyMinimum initial guess",
-        "window": 5,
         "ms_per_step": ms_a,
         "value": n_free * iters / (ms_a * 1e-3),
         "unit": UNIT,
@@ -416,6 +424,8 @@ def run_anderson(args, pbat, torch):
         "plain_ms_per_step": ms_p,
         "plain_grad_norm_after_one_step": g_p,
     }
+    out.update({"window": 5} if kind == "anderson" else {"path": "linear", "eta": 0.2, "tau": 2.0})
+    return out
 
 
 def run_contact(args, pbat, torch):
@@ -545,7 +555,7 @@ def config_of(args, w):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--iterations", type=int, default=50)
@@ -567,7 +577,10 @@ def main():
                     help="skip the LBVH build measurement")
     ap.add_argument("--no-anderson", dest="anderson", action="store_false", default=True,
                     help="skip the Anderson-acceleration measurement")
-    ap.add_argument("--only", choices=["batch", "adjoint", "contact", "lbvh", "anderson"], default=None,
+    ap.add_argument("--no-trust-region", dest="trust_region", action="store_false", default=True,
+                    help="skip the trust-region-acceleration measurement")
+    ap.add_argument("--only", choices=["batch", "adjoint", "contact", "lbvh", "anderson", "trust_region"],
+                    default=None,
                     help="run only this secondary measurement and print its figures (no benchmark line)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -591,7 +604,8 @@ def main():
             "adjoint": lambda: run_adjoint(args, pbat, torch),
             "contact": lambda: run_contact(args, pbat, torch),
             "lbvh": lambda: run_lbvh(args, _capi, torch),
-            "anderson": lambda: run_anderson(args, pbat, torch),
+            "anderson": lambda: run_accelerated(args, pbat, torch, "anderson"),
+            "trust_region": lambda: run_accelerated(args, pbat, torch, "trust_region"),
         }
         if rank == 0:
             print(json.dumps({"only": args.only, args.only: legs[args.only]()}))
@@ -687,7 +701,8 @@ def main():
         adjoint = run_adjoint(args, pbat, torch) if args.adjoint else None
         contact = run_contact(args, pbat, torch) if args.contact else None
         lbvh = run_lbvh(args, _capi, torch) if args.lbvh else None
-        anderson = run_anderson(args, pbat, torch) if args.anderson else None
+        anderson = run_accelerated(args, pbat, torch, "anderson") if args.anderson else None
+        trust_region = run_accelerated(args, pbat, torch, "trust_region") if args.trust_region else None
         launches = launches_per_step * args.steps
         line = {
             "metric": METRIC,
@@ -722,6 +737,7 @@ def main():
             "contact": contact,
             "lbvh": lbvh,
             "anderson": anderson,
+            "trust_region": trust_region,
         }
         print(json.dumps(line))
     group.close()

@@ -56,6 +56,8 @@ extern "C" {
 #define PBGB_ACCEL_NONE 0
 #define PBGB_ACCEL_CHEBYSHEV 1
 #define PBGB_ACCEL_ANDERSON 2 /* single mesh without contact; window_size columns */
+#define PBGB_ACCEL_NESTEROV 3 /* nesterov_lipschitz, nesterov_start */
+#define PBGB_ACCEL_TRUST_REGION 5 /* tr_eta, tr_tau, tr_curved; single mesh without contact */
 /* graph/Enums.h:20-33 */
 #define PBGB_COLOR_ORDER_NATURAL 0
 #define PBGB_COLOR_ORDER_SMALLEST_DEGREE 1
@@ -149,6 +151,12 @@ typedef struct pbgb_vbd_desc
     double epsv;                   /* IPC smooth friction velocity threshold (default 1e-3) */
     int32_t active_set_update_frequency; /* update the contact list every k substeps (default 1) */
     int32_t window_size; /* Anderson window m, 1..16 (PBGB_ACCEL_ANDERSON; Data::mWindowSize, default 5) */
+    double nesterov_lipschitz; /* L > 0 (Data::mNesterovLipschitzConstant, default 1) */
+    int32_t nesterov_start;    /* accelerate iterations k > start >= 0 (default 3) */
+    /* Trust-region acceleration (gpu/impl/vbd/TrustRegionIntegrator.cu; Data::eta, tau, bCurved). */
+    double tr_eta;     /* energy-reduction ratio threshold, >= 0 (default 0.2) */
+    double tr_tau;     /* radius growth factor, > 1 (default 2) */
+    int32_t tr_curved; /* 1: curved path (its steps are plain VBD iterations), 0: linear path */
 } pbgb_vbd_desc;
 
 typedef struct pbgb_vbd pbgb_vbd; /* opaque integrator handle */
@@ -250,6 +258,14 @@ PBGB_API int pbgb_vbd_get_contacts(pbgb_vbd* h, int32_t* fc, uint8_t* active);
  * the current positions against the last step's inertial target; FP64 device reductions. */
 PBGB_API int pbgb_vbd_objective(pbgb_vbd* h, double dt, double* f);
 PBGB_API int pbgb_vbd_gradient(pbgb_vbd* h, double dt, double* grad /* 3 x nV */);
+
+/* Trust-region decisions of the last step (PBGB_ACCEL_TRUST_REGION, linear path): 4 doubles per
+ * (substep, iteration) entry, substep-major -- the step length t, the actual/predicted decrease
+ * ratio rho (NaN when no stretched step was tried), the squared radius after the iteration and
+ * flags (1: tried, 2: accepted); iterations 0 and 1 are plain.  These are the quantities the
+ * reference's integrator logs through its profiler (gpu/impl/vbd/TrustRegionIntegrator.cu:71-160).
+ * *count receives the number of entries; at most `capacity` are written to out (may be NULL). */
+PBGB_API int pbgb_vbd_trust_region_log(pbgb_vbd* h, double* out, int32_t capacity, int32_t* count);
 
 /*
  * pbgb_vbd_gradient without any device allocation.  This entry point has no counterpart in the

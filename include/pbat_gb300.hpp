@@ -8,7 +8,8 @@
  * Header-only, C++17, no Eigen dependency:
  *   - the constructor takes the reference's own pbat::sim::vbd::Data after Construct() (or any
  *     object with the same member names: x, X, E, v, aext, m, wg, lame, Pptr, Padj, strategy, kD,
- *     detHZero, eAcceleration, rho, mWindowSize, and for contact V, F, B, XVA, FA, muC, muF, epsv,
+ *     detHZero, eAcceleration, rho, mWindowSize, mNesterovLipschitzConstant,
+ *     mNesterovAccelerationStart, eta, tau, bCurved, and for contact V, F, B, XVA, FA, muC, muF, epsv,
  *     mActiveSetUpdateFrequency), reading each member through data()/size()/cols();
  *   - matrices passed in are any column-major 3 x n float matrix with data() and cols() (Eigen's
  *     GpuMatrixX, Eigen::Ref<GpuMatrixX const>, or pbgb::Matrix3X);
@@ -135,9 +136,18 @@ class Integrator
         d.init_strategy     = static_cast<std::int32_t>(data.strategy);
         d.kD                = static_cast<double>(data.kD);
         d.detHZero          = static_cast<double>(data.detHZero);
-        d.acceleration      = static_cast<std::int32_t>(data.eAcceleration);
+        // gpu/vbd/Integrator.cu:15-33 builds Anderson, Chebyshev and trust-region integrators and
+        // the base integrator for every other strategy (Nesterov and Broyden included).
+        std::int32_t const accel = static_cast<std::int32_t>(data.eAcceleration);
+        d.acceleration = (accel == PBGB_ACCEL_CHEBYSHEV || accel == PBGB_ACCEL_ANDERSON ||
+                          accel == PBGB_ACCEL_TRUST_REGION) ? accel : PBGB_ACCEL_NONE;
         d.rho               = static_cast<double>(data.rho);
         d.window_size       = static_cast<std::int32_t>(data.mWindowSize);
+        d.nesterov_lipschitz = static_cast<double>(data.mNesterovLipschitzConstant);
+        d.nesterov_start     = static_cast<std::int32_t>(data.mNesterovAccelerationStart);
+        d.tr_eta             = static_cast<double>(data.eta);
+        d.tr_tau             = static_cast<double>(data.tau);
+        d.tr_curved          = data.bCurved ? 1 : 0;
         d.chebyshev_formula = PBGB_CHEBYSHEV_REFERENCE;
         d.semantics         = PBGB_SEMANTICS_GPU;
         std::vector<std::int32_t> V, F, B;

@@ -14,6 +14,7 @@
 // doctest known-answer values committed under tests/golden/.
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -557,6 +558,133 @@ static void anderson_lsq(std::vector<std::vector<Real>> const& A, int m, Real co
 // Advance `nsteps` time steps in place: x, v (nV x 3), vprev (nV x 3, GPU semantics only: the
 // velocity of the previous step, initially zero).  sim/vbd/Integrator.cpp:22-96 and
 // ChebyshevIntegrator.cpp:15-32.
+double orc_objective(orc_problem const* Pp, double const* x, double const* xtilde, double dt);
+
+// Minimiser of the quadratic model a t^2 + b t + c (TrustRegionIntegrator.cu:400-430), with the
+// reference's float thresholds: FLT_MIN as zero and FLT_MAX as infinity.
+static Real tr_model_optimal_step(Real const aQ[3])
+{
+    Real const zero = Real(FLT_MIN), inf = Real(FLT_MAX);
+    if (std::abs(aQ[0]) > zero)
+        return aQ[0] > zero ? -aQ[1] / (Real(2) * aQ[0]) : inf;
+    if (std::abs(aQ[1]) > zero)
+        return aQ[1] > 0 ? -inf : inf;
+    return Real(0);
+}
+
+// std::clamp as min(max(v, lo), hi) (the comparisons decide NaN bounds: a NaN upper bound leaves
+// max(v, lo)).
+static Real tr_clamp(Real v, Real lo, Real hi)
+{
+    Real const m = (v < lo) ? lo : v;
+    return (hi < m) ? hi : m;
+}
+
+// TrustRegionIntegrator::SolveWithLinearAcceleratedPath (gpu/impl/vbd/TrustRegionIntegrator.cu:
+// 48-165).  The first two iterations are plain VBD sweeps that record f and t; from k = 2 on, a
+// quadratic model m(t) through (t_{k-2}, f_{k-2}), (t_{k-1}, f_{k-1}), (t_k = 0, f_k) is built,
+// the VBD step x_{k-1} -> x is taken and then stretched to x_{k-1} + t (x - x_{k-1}), t the model's
+// minimiser clamped to [1, R / |dx|]; the stretched step is kept when the actual decrease is more
+// than eta of the predicted one, else rolled back to the VBD step, with the radius R grown or
+// shrunk by tau.
+static void trust_region_linear(orc_problem const& P, Real const* xt, Real const* xtilde, Real* x, Real sdt, Real sdt2, int32_t iterations, int nthreads, double const* forced, double* log)
+{
+    (void)nthreads;
+    size_t const n3 = size_t(P.nV) * 3;
+    std::vector<Real> xkm1(x, x + n3);
+    auto objective = [&] { return orc_objective(&P, x, xtilde, sdt); };
+    auto sweep     = [&] {
+        for (int32_t p = 0; p < P.nPartitions; ++p)
+        {
+            int32_t const b = P.Pptr[p], e = P.Pptr[p + 1];
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+            for (int32_t kk = b; kk < e; ++kk)
+                solve_vertex(P, P.Padj[kk], xt, xtilde, x, sdt, sdt2);
+        }
+    };
+    Real const eta = P.tr_eta, tau = P.tr_tau, zero = 1e-6;
+    Real fk = objective(), fkm1 = 0, fkm2 = 0, tk = -1, tkm1 = 0, tkm2 = 0, R2 = 0;
+    for (int32_t k = 0; k < iterations; ++k)
+    {
+        if (k >= 2)
+        {
+            // ConstructModel: translate so that t_k = 0, then solve Q aQ = f.
+            tkm2 -= tk;
+            tkm1 -= tk;
+            tk = 0;
+            Real const Q[9] = {tkm2 * tkm2, tkm1 * tkm1, tk * tk, tkm2, tkm1, tk, 1, 1, 1}; // column-major
+            Real Qi[9];
+            inv3(Q, Qi);
+            Real const fv[3] = {fkm2, fkm1, fk};
+            Real aQ[3];
+            for (int r = 0; r < 3; ++r)
+                aQ[r] = Qi[r] * fv[0] + Qi[3 + r] * fv[1] + Qi[6 + r] * fv[2];
+            // UpdateIterates
+            fkm2 = fkm1, fkm1 = fk, tkm2 = tkm1, tkm1 = tk;
+            std::copy(x, x + n3, xkm1.begin());
+            sweep();
+            Real dx2 = 0;
+            for (size_t q = 0; q < n3; ++q)
+                dx2 += (x[q] - xkm1[q]) * (x[q] - xkm1[q]);
+            if (R2 < dx2 + zero)
+                R2 = tau * tau * dx2;
+            Real const lower = 1, upper = std::sqrt(R2 / dx2);
+            Real t            = tr_clamp(tr_model_optimal_step(aQ), lower, upper);
+            bool tryAcc       = !(std::abs(t - lower) < zero);
+            double const* F   = forced ? forced + 4 * size_t(k) : nullptr;
+            if (F)
+            {
+                t      = F[0];
+                tryAcc = (int(F[3]) & 1) != 0;
+            }
+            bool accepted = false;
+            Real rhoTR    = std::numeric_limits<Real>::quiet_NaN();
+            if (tryAcc)
+            {
+                for (size_t q = 0; q < n3; ++q)
+                    x[q] = xkm1[q] + t * (x[q] - xkm1[q]);
+                fk               = objective();
+                Real const mNext = aQ[0] * t * t + aQ[1] * t + aQ[2];
+                rhoTR            = (fkm1 - fk) / (fkm1 - mNext);
+                accepted         = F ? (int(F[3]) & 2) != 0 : rhoTR > eta;
+            }
+            if (accepted)
+            {
+                if ((upper - t) < zero)
+                    R2 *= tau * tau;
+                tk = t;
+            }
+            else
+            {
+                R2 /= tau * tau;
+                if (tryAcc)
+                    for (size_t q = 0; q < n3; ++q)
+                        x[q] = xkm1[q] + (x[q] - xkm1[q]) / t;
+                fk = objective();
+                tk = tkm1 + 1;
+            }
+            if (log)
+            {
+                double* L = log + 4 * size_t(k);
+                L[0] = t, L[1] = rhoTR, L[2] = R2, L[3] = tryAcc ? (accepted ? 3.0 : 1.0) : 0.0;
+            }
+        }
+        else
+        {
+            fkm2 = fkm1, fkm1 = fk, tkm2 = tkm1, tkm1 = tk;
+            std::copy(x, x + n3, xkm1.begin());
+            sweep();
+            fk = objective();
+            tk = Real(k);
+            if (log)
+            {
+                double* L = log + 4 * size_t(k);
+                L[0] = 0.0, L[1] = std::numeric_limits<double>::quiet_NaN(), L[2] = R2, L[3] = 0.0;
+            }
+        }
+    }
+}
+
 int orc_run(orc_problem const* Pp, double* x, double* v, double* vprev, double dt, int32_t iterations, int32_t substeps, int32_t nsteps)
 {
     orc_problem const& P = *Pp;
@@ -657,8 +785,32 @@ int orc_run(orc_problem const* Pp, double* x, double* v, double* vprev, double d
                     }
                 }
             }
-            for (int32_t k = 0; k < (P.acceleration == 2 ? 0 : iterations); ++k)
+            // NesterovIntegrator::Solve (sim/vbd/NesterovIntegrator.cpp:16-43): x_0 is the solve's
+            // start (never updated); for k > start, y = x + beta (x - x_0) before the sweep and
+            // x = y - (x - x_0)/L after it, then lambda and beta advance.
+            std::vector<Real> neX0, neY;
+            Real neLambda = 0, neBeta = 0;
+            if (P.acceleration == 3)
             {
+                neX0.assign(x, x + size_t(nV) * 3);
+                neY.assign(size_t(nV) * 3, 0);
+            }
+            if (P.acceleration == 5 && !P.tr_curved)
+                trust_region_linear(P, xt.data(), xtilde.data(), x, sdt, sdt2, iterations, nthreads,
+                                    P.tr_forced ? P.tr_forced + 4 * (size_t(step) * size_t(substeps) + size_t(s)) * size_t(iterations)
+                                                : nullptr,
+                                    P.tr_log ? P.tr_log + 4 * (size_t(step) * size_t(substeps) + size_t(s)) * size_t(iterations)
+                                             : nullptr);
+            // The curved trust-region path (TrustRegionIntegrator.cu:167-263) never moves x off the
+            // VBD iterates: its constraint solve returns 0, so t = clamp(t*, FLT_MIN, 0) is at the
+            // lower bound, no accelerated step is tried and every iteration is a plain VBD sweep.
+            bool const plainLoop = !(P.acceleration == 2 || (P.acceleration == 5 && !P.tr_curved));
+            for (int32_t k = 0; k < (plainLoop ? iterations : 0); ++k)
+            {
+                bool const neActive = P.acceleration == 3 && P.nesterov_start < k;
+                if (neActive)
+                    for (size_t q = 0; q < size_t(nV) * 3; ++q)
+                        neY[q] = x[q] + neBeta * (x[q] - neX0[q]);
                 // RunVbdIteration (Integrator.cpp:73-87): colours in sequence, vertices of a
                 // colour in parallel.
                 for (int32_t p = 0; p < P.nPartitions; ++p)
@@ -667,6 +819,15 @@ int orc_run(orc_problem const* Pp, double* x, double* v, double* vprev, double d
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
                     for (int32_t kk = b; kk < e; ++kk)
                         solve_vertex(P, P.Padj[kk], xt.data(), xtilde.data(), x, sdt, sdt2);
+                }
+                if (neActive)
+                {
+                    Real const alpha = Real(1) / P.nesterov_L;
+                    for (size_t q = 0; q < size_t(nV) * 3; ++q)
+                        x[q] = neY[q] - alpha * (x[q] - neX0[q]);
+                    Real const lk = neLambda;
+                    neLambda      = (1 + std::sqrt(1 + 4 * neLambda * neLambda)) / 2;
+                    neBeta        = (lk - 1) / neLambda;
                 }
                 if (P.acceleration == 1)
                 {

@@ -75,6 +75,8 @@ class VbdDesc(C.Structure):
         ("muF", C.c_double),
         ("epsv", C.c_double),
         ("active_set_update_frequency", C.c_int32), ("window_size", C.c_int32),
+        ("nesterov_lipschitz", C.c_double), ("nesterov_start", C.c_int32),
+        ("tr_eta", C.c_double), ("tr_tau", C.c_double), ("tr_curved", C.c_int32),
     ]
 
 
@@ -126,6 +128,7 @@ _SIGNATURES = [
     ("pbgb_vbd_sweep_timing", C.c_int, [_vp, C.POINTER(_f64), C.POINTER(C.c_int64)]),
     ("pbgb_vbd_get_contacts", C.c_int, [_vp, _vp, _vp]),
     ("pbgb_vbd_objective", C.c_int, [_vp, _f64, C.POINTER(_f64)]),
+    ("pbgb_vbd_trust_region_log", C.c_int, [_vp, _vp, _i32, C.POINTER(_i32)]),
     ("pbgb_vbd_gradient", C.c_int, [_vp, _f64, _vp]),
     ("pbgb_vbd_gradient_noalloc", C.c_int, [_vp, _f64, _vp]),
     ("pbgb_last_error", C.c_char_p, [_vp]),

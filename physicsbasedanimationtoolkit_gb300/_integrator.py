@@ -13,18 +13,27 @@ from . import _capi
 SEMANTICS_CPU = 0
 SEMANTICS_GPU = 1
 
-_UNSUPPORTED = {3: "Nesterov", 4: "Broyden", 5: "TrustRegion"}
+# Acceleration strategy each integrator runs, as the reference dispatches them: the CPU integrator
+# (bindings/pypbat/sim/vbd/Integrator.cpp:31-45) builds Chebyshev, Anderson, Broyden and Nesterov
+# integrators and the base integrator otherwise (trust region included); the GPU integrator
+# (gpu/vbd/Integrator.cu:15-33) builds Anderson, Chebyshev and trust-region integrators and the base
+# integrator otherwise (Nesterov and Broyden included).  None marks what this library lacks.
+_DISPATCH = {
+    SEMANTICS_CPU: {0: 0, 1: 1, 2: 2, 3: 3, 4: None, 5: 0},
+    SEMANTICS_GPU: {0: 0, 1: 1, 2: 2, 3: 0, 4: 0, 5: 5},
+}
+_NAMES = {4: "Broyden"}
 
 
 def make_desc(data, semantics):
     """A ``pbgb_vbd_desc`` for a constructed ``Data`` plus the arrays it points into."""
     if not getattr(data, "_constructed", False):
         raise ValueError("Data must be constructed (call Data.construct()) before creating an integrator")
-    accel = int(data.eAcceleration)
-    if accel in _UNSUPPORTED:
+    accel = _DISPATCH[semantics].get(int(data.eAcceleration), 0)
+    if accel is None:
         raise NotImplementedError(
-            f"{_UNSUPPORTED[accel]} acceleration is not part of this library's VBD path "
-            "(Base, Chebyshev and Anderson are)"
+            f"{_NAMES[int(data.eAcceleration)]} acceleration is not part of this library's VBD path "
+            "(Base, Chebyshev, Anderson, Nesterov and trust region are)"
         )
     nV, nT = data.X.shape[1], data.E.shape[1]
     keep = dict(
@@ -64,9 +73,14 @@ def make_desc(data, semantics):
     d.init_strategy = int(data.strategy)
     d.kD = float(data.kD)
     d.detHZero = float(data.detH_zero)
-    d.acceleration = accel if accel in (1, 2) else 0
+    d.acceleration = accel
     d.rho = float(data.rho)
     d.window_size = int(getattr(data, "window_size", 5))
+    d.nesterov_lipschitz = float(getattr(data, "nesterov_L", 1.0))
+    d.nesterov_start = int(getattr(data, "nesterov_start", 3))
+    d.tr_eta = float(getattr(data, "eta", 0.2))
+    d.tr_tau = float(getattr(data, "tau", 2.0))
+    d.tr_curved = int(bool(getattr(data, "curved", True)))
     d.chebyshev_formula = int(getattr(data, "chebyshev_formula", 0))
     d.semantics = semantics
     return d, keep
@@ -241,6 +255,17 @@ class IntegratorBase:
         _capi.check(_capi.lib().pbgb_vbd_step_adjoint(self._h, int(slot), int(substeps), C.c_void_p(xbar_ptr),
                                                      C.c_void_p(vbar_ptr), C.c_void_p(dlogmu_ptr),
                                                      C.c_void_p(dloglambda_ptr)), self._h)
+
+    def trust_region_log(self):
+        """Trust-region decisions of the last step: an (entries, 4) array, one row per (substep,
+        iteration) -- t, rho (NaN when no stretched step was tried), squared radius after the
+        iteration, flags (1 tried, 2 accepted)."""
+        L, n = _capi.lib(), C.c_int32(0)
+        _capi.check(L.pbgb_vbd_trust_region_log(self._h, None, 0, C.byref(n)), self._h)
+        out = np.zeros((n.value, 4), dtype=np.float64)
+        if n.value:
+            _capi.check(L.pbgb_vbd_trust_region_log(self._h, out.ctypes.data, n.value, C.byref(n)), self._h)
+        return out
 
     def objective(self, dt):
         """Backward-Euler objective at the current positions (FP64 device reduction)."""

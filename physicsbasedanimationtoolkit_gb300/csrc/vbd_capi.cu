@@ -8,6 +8,8 @@
 // pass), and several meshes concatenated into one system for the batched form.
 #include "adjoint.cuh"
 #include "anderson.cuh"
+#include "nesterov.cuh"
+#include "trust_region.cuh"
 #include "contact.cuh"
 #include "pbat_gb300.h"
 #include "vbd_construct.h"
@@ -154,8 +156,21 @@ inline void validate_descs(pbgb_vbd_desc const* descs, int32_t nMeshes)
         if (d.acceleration == PBGB_ACCEL_CHEBYSHEV && !(d.rho > 0.0 && d.rho < 1.0))
             throw std::invalid_argument("Expected 0 < rho < 1");
         if (d.acceleration != PBGB_ACCEL_NONE && d.acceleration != PBGB_ACCEL_CHEBYSHEV &&
-            d.acceleration != PBGB_ACCEL_ANDERSON)
+            d.acceleration != PBGB_ACCEL_ANDERSON && d.acceleration != PBGB_ACCEL_NESTEROV &&
+            d.acceleration != PBGB_ACCEL_TRUST_REGION)
             bad("unsupported acceleration strategy");
+        if (d.acceleration == PBGB_ACCEL_TRUST_REGION)
+        {
+            if (!(d.tr_eta >= 0.0) || !std::isfinite(d.tr_eta) || !(d.tr_tau > 1.0) || !std::isfinite(d.tr_tau))
+                bad("trust-region acceleration expects eta >= 0 and tau > 1");
+            if (nMeshes != 1 || d.n_collision_triangles > 0)
+                bad("trust-region acceleration needs a single mesh without contact");
+        }
+        if (d.acceleration == PBGB_ACCEL_NESTEROV &&
+            (!(d.nesterov_lipschitz > 0.0) || !std::isfinite(d.nesterov_lipschitz) || d.nesterov_start < 0))
+            bad("Nesterov acceleration expects L > 0 and start >= 0");
+        if (d.acceleration == PBGB_ACCEL_NESTEROV && (nMeshes != 1 || d.n_collision_triangles > 0))
+            bad("Nesterov acceleration needs a single mesh without contact");
         if (d.acceleration == PBGB_ACCEL_ANDERSON)
         {
             if (d.window_size < 1 || d.window_size > kAndersonMaxWindow)
@@ -206,6 +221,10 @@ class VbdSystem
     float kD = 0.f, detHZero = 1e-7f;
     int32_t acceleration = PBGB_ACCEL_NONE, chebFormula = PBGB_CHEBYSHEV_REFERENCE, semantics = 0;
     int32_t window = 0; // Anderson window
+    double nesterovL = 1.0;
+    int32_t nesterovStart = 3;
+    double trEta = 0.2, trTau = 2.0;
+    bool trCurved = true;
     double rho  = 1.0;
     int32_t lanes = 0, block = 256;
     bool pdl   = true;
@@ -220,6 +239,14 @@ class VbdSystem
     // iterate and residual, the window columns, FP64 block partials, Gram matrix and coefficients.
     DeviceArray<float4> anStep, anGkm1, anFkm1, anDF, anDG;
     DeviceArray<double> anPartials, anGram, anRhs, anAlpha;
+    // Nesterov acceleration: the solve's start iterate and the extrapolated point.
+    DeviceArray<float4> neX0, neY;
+    // Trust-region acceleration (linear path): x_{k-1}, the device-resident scalars and the
+    // reduction partials.
+    DeviceArray<float4> trXkm1;
+    DeviceArray<TrustState> trState;
+    DeviceArray<double> trPartials, trLog;
+    int32_t trLogEntries = 0; // entries the last enqueued step writes
     DeviceArray<float> m, staging;
     DeviceArray<TetRecord> tets;
     DeviceArray<int32_t> solve, incPtr, flags;
@@ -442,6 +469,11 @@ class VbdSystem
         chebFormula    = d0.chebyshev_formula;
         semantics      = d0.semantics;
         window         = acceleration == PBGB_ACCEL_ANDERSON ? d0.window_size : 0;
+        nesterovL      = d0.nesterov_lipschitz;
+        nesterovStart  = d0.nesterov_start;
+        trEta          = d0.tr_eta;
+        trTau          = d0.tr_tau;
+        trCurved       = d0.tr_curved != 0;
 
         // Host staging of the concatenated layout.
         std::vector<float4> hx(nV), hv(nV), ha(nV), hX(nV);
@@ -659,6 +691,18 @@ class VbdSystem
             h0.allocate(nV);
             h1.allocate(nV);
         }
+        if (acceleration == PBGB_ACCEL_NESTEROV)
+        {
+            neX0.allocate(nV);
+            neY.allocate(nV);
+        }
+        if (trustLinear())
+        {
+            trXkm1.allocate(nV);
+            trState.allocate(1);
+            trPartials.allocate(size_t(kTrustMaxBlocks));
+            check(cudaMemsetAsync(trState.get(), 0, sizeof(TrustState), stream), "memset");
+        }
         if (acceleration == PBGB_ACCEL_ANDERSON)
         {
             anStep.allocate(nV);
@@ -815,6 +859,7 @@ class VbdSystem
     // Per-tet Lame coefficients (system order); the records keep (wg mu, wg lambda, 1 + mu/lambda).
     void setMaterial(double const* mu, double const* lambda)
     {
+        restEnergyValid = false;
         for (int32_t e = 0; e < nT; ++e)
             if (!(mu[e] > 0.0) || !(lambda[e] > 0.0) || !std::isfinite(mu[e]) || !std::isfinite(lambda[e]))
                 throw std::invalid_argument("pbgb_vbd_set_material: expected finite mu > 0 and lambda > 0");
@@ -865,7 +910,7 @@ class VbdSystem
         if (contact)
             throw std::invalid_argument("the adjoint does not support contact");
         if (acceleration != PBGB_ACCEL_NONE)
-            throw std::invalid_argument("the adjoint does not support Chebyshev acceleration");
+            throw std::invalid_argument("the adjoint does not support acceleration strategies");
         if (kD != 0.f)
             throw std::invalid_argument("the adjoint does not support damping (kD != 0)");
         if (strategy > PBGB_INIT_KINETIC_ENERGY_MINIMUM)
@@ -1137,6 +1182,32 @@ class VbdSystem
             double omega      = 0.0;
             double const rho2 = rho * rho;
             bool const anderson = !plainOnly && acceleration == PBGB_ACCEL_ANDERSON;
+            bool const nesterov = !plainOnly && acceleration == PBGB_ACCEL_NESTEROV;
+            bool const trust    = !plainOnly && trustLinear();
+            TrustParams tp{};
+            if (trust)
+            {
+                if (trLog.size() < size_t(kTrustLogFields) * size_t(iterations) * size_t(substeps))
+                    throw std::logic_error("trust-region log not reserved for this step");
+                tp.log       = trLog.get();
+                trLogEntries = iterations * substeps;
+                tp.x        = x.get();
+                tp.xkm1     = trXkm1.get();
+                tp.energy   = energyParams(h, nullptr);
+                tp.state    = trState.get();
+                tp.partials = trPartials.get();
+                tp.nV       = nV;
+                tp.eta      = trEta;
+                tp.tau      = trTau;
+                // TrustRegionIntegrator::SolveWithLinearAcceleratedPath (:48-170): f at the initial guess.
+                check(launch_trust_objective(tp, kTrustInitial, 0, 0, stream), "trust_objective");
+            }
+            // NesterovIntegrator::Solve (sim/vbd/NesterovIntegrator.cpp:16-43).
+            double const neAlpha = 1.0 / nesterovL;
+            double neLambda = 0.0, neBeta = 0.0;
+            if (nesterov && iterations > 0 && nV > 0)
+                check(cudaMemcpyAsync(neX0.get(), x.get(), sizeof(float4) * size_t(nV), cudaMemcpyDeviceToDevice, stream),
+                      "nesterov copy");
             AndersonParams ap{};
             if (anderson)
             {
@@ -1169,6 +1240,12 @@ class VbdSystem
                     w.hprev = H[(k + 1) % 2];
                     w.hcur  = H[k % 2];
                 }
+                if (trust)
+                    check(launch_trust_begin(tp, k, stream), "trust_begin");
+                bool const neActive = nesterov && nesterovStart < k;
+                if (neActive)
+                    check(launch_nesterov_extrapolate(nV, x.get(), neX0.get(), neY.get(), float(neBeta), stream),
+                          "nesterov_extrapolate");
                 size_t const slot = size_t(s) * size_t(iterations) + size_t(k);
                 if (profiling)
                     check(cudaEventRecordWithFlags(evBegin[slot], stream, cudaEventRecordExternal), "cudaEventRecord");
@@ -1181,6 +1258,25 @@ class VbdSystem
                 }
                 if (profiling)
                     check(cudaEventRecordWithFlags(evEnd[slot], stream, cudaEventRecordExternal), "cudaEventRecord");
+                int32_t const entry = s * iterations + k;
+                if (trust && k < 2)
+                    check(launch_trust_objective(tp, kTrustPlain, k, entry, stream), "trust_objective");
+                else if (trust)
+                {
+                    check(launch_trust_step_size(tp, entry, stream), "trust_step_size");
+                    check(launch_trust_apply(tp, false, stream), "trust_apply");
+                    check(launch_trust_objective(tp, kTrustTrial, k, entry, stream), "trust_objective");
+                    check(launch_trust_apply(tp, true, stream), "trust_apply");
+                    check(launch_trust_objective(tp, kTrustFinal, k, entry, stream), "trust_objective");
+                }
+                if (neActive)
+                {
+                    check(launch_nesterov_update(nV, x.get(), neX0.get(), neY.get(), float(neAlpha), stream),
+                          "nesterov_update");
+                    double const lk = neLambda;
+                    neLambda        = (1.0 + std::sqrt(1.0 + 4.0 * neLambda * neLambda)) / 2.0;
+                    neBeta          = (lk - 1.0) / neLambda;
+                }
                 if (anderson)
                 {
                     // AndersonIntegrator::Solve (sim/vbd/AndersonIntegrator.cpp:31-56).
@@ -1363,6 +1459,7 @@ class VbdSystem
     // (iterations+1 x 1), {t}.{s}.grad.mtx and {t}.{s}.x.mtx (3 nV x iterations+1).
     void tracedStepCpuFormat(float dt, int32_t iterations, int32_t substeps)
     {
+        reserveTrustLog(iterations, substeps);
         double const h = double(dt) / double(substeps);
         if (gradBuf.size() < size_t(nV) * 3)
             gradBuf.allocate(size_t(nV) * 3);
@@ -1402,6 +1499,10 @@ class VbdSystem
         check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
     }
 
+    // The curved trust-region path moves x exactly as plain VBD does (its constraint solve
+    // returns 0, so no accelerated step is ever tried): only the linear path has device work.
+    bool trustLinear() const { return acceleration == PBGB_ACCEL_TRUST_REGION && !trCurved; }
+
     int64_t launchesPerStep(int32_t iterations, int32_t substeps) const
     {
         int64_t perIter = 0;
@@ -1410,6 +1511,11 @@ class VbdSystem
         int64_t n = int64_t(substeps) * (2 * (nV > 0 ? 1 : 0) + int64_t(iterations) * perIter);
         if (acceleration == PBGB_ACCEL_ANDERSON && iterations > 0)
             n += int64_t(substeps) * (1 + 3 * int64_t(iterations - 1));
+        if (acceleration == PBGB_ACCEL_NESTEROV)
+            n += int64_t(substeps) * 2 * std::max<int64_t>(0, int64_t(iterations) - 1 - nesterovStart);
+        if (trustLinear())
+            n += int64_t(substeps) * (1 + 2 * std::min<int64_t>(iterations, 2) +
+                                      6 * std::max<int64_t>(0, int64_t(iterations) - 2));
         if (contact)
         {
             // predict, vertex and triangle boxes, Morton, 4 x (count, scan, scatter), Karras, leaf
@@ -1420,8 +1526,23 @@ class VbdSystem
         return n;
     }
 
+    // The trust-region decision log holds one entry per (substep, iteration) of a step; it is
+    // grown here, outside any stream capture.
+    void reserveTrustLog(int32_t iterations, int32_t substeps)
+    {
+        size_t const need = size_t(kTrustLogFields) * size_t(std::max(iterations, 1)) * size_t(std::max(substeps, 1));
+        if (!trustLinear() || trLog.size() >= need)
+            return;
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+        graphValid = false;
+        dropSlotGraphs();
+        trLog.allocate(need);
+        check(cudaMemsetAsync(trLog.get(), 0, sizeof(double) * need, stream), "memset");
+    }
+
     void step(float dt, int32_t iterations, int32_t substeps)
     {
+        reserveTrustLog(iterations, substeps);
         if (traceNext)
         {
             traceNext = false;
@@ -1458,6 +1579,7 @@ class VbdSystem
             graphValid = true;
         }
         check(cudaGraphLaunch(graph, stream), "cudaGraphLaunch");
+        trLogEntries = trustLinear() ? iterations * substeps : 0;
     }
 
     // Project-written autotuner: times one replayed step per candidate (lanes per vertex x block
@@ -1623,8 +1745,26 @@ class VbdSystem
         p.nT     = nT;
         p.dt2    = dt * dt;
         p.out    = out;
+        p.restEnergy = restEnergy();
         return p;
     }
+
+    // sum_e wg_e mu_e^2 / (2 lambda_e), the elastic energy of the rest state (cached until the
+    // material changes).
+    double restEnergy() const
+    {
+        if (!restEnergyValid)
+        {
+            double e = 0.0;
+            for (size_t t = 0; t < hostWg.size(); ++t)
+                e += hostWg[t] * hostMu[t] * hostMu[t] / (2.0 * hostLambda[t]);
+            restEnergyCache = e;
+            restEnergyValid = true;
+        }
+        return restEnergyCache;
+    }
+    mutable double restEnergyCache = 0.0;
+    mutable bool restEnergyValid   = false;
 };
 
 } // namespace pbgb
@@ -2201,6 +2341,27 @@ PBGB_API int pbgb_vbd_objective(pbgb_vbd* h, double dt, double* f)
         pbgb::check(pbgb::launch_objective(s.energyParams(dt, s.red.get()), s.stream), "objective");
         pbgb::check(cudaMemcpyAsync(f, s.red.get(), sizeof(double), cudaMemcpyDeviceToHost, s.stream), "D2H");
         pbgb::check(cudaStreamSynchronize(s.stream), "sync");
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_trust_region_log(pbgb_vbd* h, double* out, int32_t capacity, int32_t* count)
+{
+    if (!h || !count || capacity < 0)
+        return fail(h, kInvalid, "null argument or negative capacity");
+    return guarded(h, [&] {
+        auto& s = h->sys;
+        if (!s.trustLinear())
+            throw std::invalid_argument("the integrator does not run the linear trust-region path");
+        *count        = s.trLogEntries;
+        int32_t const n = std::min(capacity, s.trLogEntries);
+        if (out && n > 0)
+        {
+            pbgb::check(cudaMemcpyAsync(out, s.trLog.get(), sizeof(double) * pbgb::kTrustLogFields * size_t(n),
+                                        cudaMemcpyDeviceToHost, s.stream),
+                        "D2H");
+            pbgb::check(cudaStreamSynchronize(s.stream), "sync");
+        }
         return int(kOk);
     });
 }

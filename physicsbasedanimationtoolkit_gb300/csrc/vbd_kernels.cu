@@ -1,5 +1,6 @@
 // CUDA kernels of the VBD step (sm_103a).  See vbd_kernels.cuh for the data layout.
 #include "vbd_kernels.cuh"
+#include "energy.cuh"
 
 #include <algorithm>
 #include <cfloat>
@@ -381,42 +382,6 @@ __global__ void end_substep_kernel(SubstepParams p)
         atomicOr(p.flags, 1);
 }
 
-__device__ __forceinline__ double warp_sum(double v)
-{
-    for (int off = 16; off > 0; off >>= 1)
-        v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
-}
-
-// Tet geometry helper: deformation gradient F (columns f[c]) of tet e, the shape-function
-// gradients of its 4 corners (G4[a]) and its material scalars.
-__device__ __forceinline__ void tet_F(EnergyParams const& p, int e, float f[3][3], int4& t, float G4[4][3], float4& mat)
-{
-    TetRecord const& r = p.tets[e];
-    uint4 const tu     = r.v;
-    t   = make_int4(int(tu.x & kIndexMask), int(tu.y & kIndexMask), int(tu.z & kIndexMask), int(tu.w & kIndexMask));
-    mat = r.mat;
-    int const vid[4] = {t.x, t.y, t.z, t.w};
-    float4 const X0 = p.X[vid[0]], x0 = p.x[vid[0]];
-    float d[3][3], E[3][3], G[3][3];
-    for (int m = 0; m < 3; ++m)
-    {
-        float4 const Xa = p.X[vid[m + 1]], xa = p.x[vid[m + 1]];
-        d[m][0] = xa.x - x0.x, d[m][1] = xa.y - x0.y, d[m][2] = xa.z - x0.z;
-        E[m][0] = Xa.x - X0.x, E[m][1] = Xa.y - X0.y, E[m][2] = Xa.z - X0.z;
-    }
-    rest_gradients(E, G);
-    for (int c = 0; c < 3; ++c)
-    {
-        for (int rr = 0; rr < 3; ++rr)
-            f[c][rr] = d[0][rr] * G[0][c] + d[1][rr] * G[1][c] + d[2][rr] * G[2][c];
-        G4[0][c] = -(G[0][c] + G[1][c] + G[2][c]);
-        G4[1][c] = G[0][c];
-        G4[2][c] = G[1][c];
-        G4[3][c] = G[2][c];
-    }
-}
-
 // Objective of the backward-Euler step (sim/vbd/Integrator.cpp:138-165): per-entity terms in FP32,
 // the global sum in FP64.
 __global__ void objective_kernel(EnergyParams p)
@@ -424,30 +389,9 @@ __global__ void objective_kernel(EnergyParams p)
     double acc  = 0.0;
     int const n = p.nV > p.nT ? p.nV : p.nT;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-    {
-        if (j < p.nV)
-        {
-            float4 const x = p.x[j], y = p.xtilde[j];
-            double const dx = double(x.x) - y.x, dy = double(x.y) - y.y, dz = double(x.z) - y.z;
-            acc += 0.5 * double(p.m[j]) * (dx * dx + dy * dy + dz * dz);
-        }
-        if (j < p.nT)
-        {
-            float f[3][3], G4[4][3];
-            int4 t;
-            float4 mat;
-            tet_F(p, j, f, t, G4, mat);
-            double I2 = 0.0;
-            for (int c = 0; c < 3; ++c)
-                for (int r = 0; r < 3; ++r)
-                    I2 += double(f[c][r]) * f[c][r];
-            double const J = double(f[0][0]) * (double(f[1][1]) * f[2][2] - double(f[1][2]) * f[2][1]) -
-                             double(f[1][0]) * (double(f[0][1]) * f[2][2] - double(f[0][2]) * f[2][1]) +
-                             double(f[2][0]) * (double(f[0][1]) * f[1][2] - double(f[0][2]) * f[1][1]);
-            double const a = J - double(mat.z);
-            acc += p.dt2 * (0.5 * double(mat.y) * a * a + 0.5 * double(mat.x) * (I2 - 3.0));
-        }
-    }
+        acc += objective_term(p, j);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        acc += p.dt2 * p.restEnergy;
     acc = warp_sum(acc);
     if ((threadIdx.x & 31) == 0)
         atomicAdd(p.out, acc);

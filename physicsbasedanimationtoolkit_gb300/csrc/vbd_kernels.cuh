@@ -116,6 +116,9 @@ struct EnergyParams
     int32_t nT;
     double dt2;
     double* __restrict__ out; // objective: out[0]; gradient: 3 x nV
+    // sum_e wg_e mu_e^2 / (2 lambda_e): the elastic energy of the rest state, which the objective
+    // adds once (times dt^2) so that per-tet terms carry only what varies with x.
+    double restEnergy;
 };
 
 // Launchers (defined in vbd_kernels.cu).  Each returns the launch status.

@@ -192,11 +192,20 @@ class Data:
         self.eAcceleration = AccelerationStrategy.Broyden
         return self
 
-    def with_nesterov_acceleration(self, L, start):
+    def with_nesterov_acceleration(self, L, start=3):
+        """Nesterov-accelerated VBD (sim/vbd/NesterovIntegrator.cpp) with Lipschitz constant L,
+        accelerating the iterations after ``start``."""
+        self.nesterov_L = float(L)
+        self.nesterov_start = int(start)
         self.eAcceleration = AccelerationStrategy.Nesterov
         return self
 
     def with_trust_region_acceleration(self, eta, tau, curved):
+        """Trust-region accelerated VBD (gpu/impl/vbd/TrustRegionIntegrator.cu): energy-reduction
+        threshold ``eta``, radius growth factor ``tau`` and the curved or linear accelerated path."""
+        self.eta = float(eta)
+        self.tau = float(tau)
+        self.curved = bool(curved)
         self.eAcceleration = AccelerationStrategy.TrustRegion
         return self
 
@@ -271,6 +280,16 @@ class Data:
                 raise ValueError("Expected 0 < rho < 1")
             if self.eAcceleration in (AccelerationStrategy.Anderson, AccelerationStrategy.Broyden) and self.window_size < 1:
                 raise ValueError("Expected m > 0")
+            if self.eAcceleration == AccelerationStrategy.Nesterov:
+                if not getattr(self, "nesterov_L", 1.0) > 0.0:
+                    raise ValueError("Expected L > 0")
+                if getattr(self, "nesterov_start", 3) < 0:
+                    raise ValueError("Expected start >= 0")
+            if self.eAcceleration == AccelerationStrategy.TrustRegion:
+                if getattr(self, "eta", 0.2) < 0:
+                    raise ValueError("Expected eta >= 0")
+                if getattr(self, "tau", 2.0) <= 1:
+                    raise ValueError("Expected tau > 1")
         self._constructed = True
         return self
 

@@ -42,6 +42,10 @@ struct Data
     double kD{0}, detHZero{1e-7}, rho{1}, muC{1e6}, muF{0.3}, epsv{1e-3};
     std::ptrdiff_t mActiveSetUpdateFrequency{1};
     std::ptrdiff_t mWindowSize{5};
+    double mNesterovLipschitzConstant{1};
+    std::ptrdiff_t mNesterovAccelerationStart{3};
+    double eta{0.2}, tau{2};
+    bool bCurved{true};
     EAccelerationStrategy eAcceleration{EAccelerationStrategy::None};
 };
 

@@ -50,7 +50,9 @@ class OrcProblem(C.Structure):
         ("rho", C.c_double),
         ("chebyshev_formula", C.c_int32),
         ("semantics", C.c_int32),
-        ("nthreads", C.c_int32), ("window", C.c_int32),
+        ("nthreads", C.c_int32), ("window", C.c_int32), ("nesterov_L", C.c_double),
+        ("nesterov_start", C.c_int32), ("tr_eta", C.c_double), ("tr_tau", C.c_double), ("tr_curved", C.c_int32),
+        ("tr_forced", C.c_void_p), ("tr_log", C.c_void_p),
     ]
 
 
@@ -195,7 +197,8 @@ class OracleVbd:
 
     def __init__(self, X, T, rho, mu, lam, dbc, v=None, aext=None, strategy=4, kD=0.0,
                  detHZero=1e-7, rho_chebyshev=None, chebyshev_formula=0, semantics=0,
-                 nthreads=0, ordering=2, selection=0, data=None, anderson_window=None):
+                 nthreads=0, ordering=2, selection=0, data=None, anderson_window=None, nesterov=None,
+                 trust_region=None):
         self.X = np.ascontiguousarray(X, dtype=np.float64)
         self.T = np.ascontiguousarray(T, dtype=np.int32)
         nV = self.X.shape[0]
@@ -231,17 +234,40 @@ class OracleVbd:
                 raise ValueError("Anderson window must be in [1, 16]")
             P.acceleration = 2
             P.window = int(anderson_window)
+        if nesterov is not None:
+            P.acceleration = 3
+            P.nesterov_L, P.nesterov_start = float(nesterov[0]), int(nesterov[1])
+        if trust_region is not None:
+            P.acceleration = 5
+            P.tr_eta, P.tr_tau, P.tr_curved = float(trust_region[0]), float(trust_region[1]), int(bool(trust_region[2]))
         P.chebyshev_formula = chebyshev_formula
         P.semantics = semantics
         P.nthreads = nthreads
         self.P = P
 
-    def step(self, dt, iterations, substeps=1, nsteps=1, use_ref=False):
+    def step(self, dt, iterations, substeps=1, nsteps=1, use_ref=False, trust_region_log=None):
+        """Advance ``nsteps`` steps.  trust_region_log: a logged run's trust-region decisions
+        (nsteps x substeps x iterations rows of t, rho, R^2, flags) to replay instead of the
+        oracle's own.  With the trust-region strategy the oracle's own decisions are kept in
+        ``self.trust_region_log`` afterwards (same layout)."""
         L = ref() if use_ref else lib()
-        rc = L.ref_run(C.byref(self.P), self.x, self.v, self.vprev.ctypes.data, dt, iterations,
-                       substeps, nsteps) if use_ref else L.orc_run(
-            C.byref(self.P), self.x, self.v, self.vprev.ctypes.data, dt, iterations, substeps,
-            nsteps)
+        own = np.zeros((nsteps * substeps * iterations, 4))
+        self.P.tr_log = own.ctypes.data
+        self.trust_region_log = own
+        forced = None
+        if trust_region_log is not None:
+            forced = np.ascontiguousarray(trust_region_log, dtype=np.float64)
+            if forced.shape != (nsteps * substeps * iterations, 4):
+                raise ValueError("trust_region_log must hold nsteps x substeps x iterations rows of 4")
+            self.P.tr_forced = forced.ctypes.data
+        try:
+            rc = L.ref_run(C.byref(self.P), self.x, self.v, self.vprev.ctypes.data, dt, iterations,
+                           substeps, nsteps) if use_ref else L.orc_run(
+                C.byref(self.P), self.x, self.v, self.vprev.ctypes.data, dt, iterations, substeps,
+                nsteps)
+        finally:
+            self.P.tr_forced = None
+            self.P.tr_log = None
         if rc != 0:
             raise RuntimeError(f"oracle run failed: {rc}")
 

@@ -143,14 +143,46 @@ def test_integrator_creation_without_device_fails_loudly():
     assert e.value.code == 6
 
 
-@pytest.mark.parametrize("accel", ["broyden", "nesterov", "trust_region"])
-def test_unsupported_accelerations_are_rejected(accel):
+def test_broyden_is_rejected():
+    P, T, _, _ = meshgen.cube5()
+    d = pbat.sim.vbd.Data().with_volume_mesh(P, T).with_broyden_acceleration(5).construct()
+    with pytest.raises(NotImplementedError):
+        pbat.sim.vbd.Integrator(d)
+
+
+@pytest.mark.parametrize("accel,cpu,gpu", [("none", 0, 0), ("chebyshev", 1, 1), ("anderson", 2, 2),
+                                           ("nesterov", 3, 0), ("broyden", None, 0), ("trust_region", 0, 5)])
+def test_acceleration_dispatch_follows_the_reference(accel, cpu, gpu):
+    """The CPU integrator runs Chebyshev, Anderson, Broyden and Nesterov and the base integrator
+    otherwise; the GPU integrator runs Anderson, Chebyshev and trust region and the base
+    integrator otherwise."""
+    from physicsbasedanimationtoolkit_gb300 import _integrator as I
+
     P, T, _, _ = meshgen.cube5()
     d = pbat.sim.vbd.Data().with_volume_mesh(P, T)
-    d = {"broyden": lambda: d.with_broyden_acceleration(5), "nesterov": lambda: d.with_nesterov_acceleration(1.0, 3),
-         "trust_region": lambda: d.with_trust_region_acceleration(0.2, 2.0, True)}[accel]().construct()
-    with pytest.raises(NotImplementedError):
+    d = {"none": lambda: d, "chebyshev": lambda: d.with_chebyshev_acceleration(0.5),
+         "anderson": lambda: d.with_anderson_acceleration(5), "nesterov": lambda: d.with_nesterov_acceleration(1.0, 3),
+         "broyden": lambda: d.with_broyden_acceleration(5),
+         "trust_region": lambda: d.with_trust_region_acceleration(0.2, 2.0, False)}[accel]().construct()
+    for sem, want in ((I.SEMANTICS_CPU, cpu), (I.SEMANTICS_GPU, gpu)):
+        if want is None:
+            with pytest.raises(NotImplementedError):
+                I.make_desc(d, sem)
+        else:
+            assert I.make_desc(d, sem)[0].acceleration == want
+
+
+def test_trust_region_settings_are_validated():
+    P, T, V, F = meshgen.cube5()
+    with pytest.raises(ValueError):
+        pbat.sim.vbd.Data().with_volume_mesh(P, T).with_trust_region_acceleration(-0.1, 2.0, False).construct()
+    with pytest.raises(ValueError):
+        pbat.sim.vbd.Data().with_volume_mesh(P, T).with_trust_region_acceleration(0.2, 1.0, True).construct()
+    d = (pbat.sim.vbd.Data().with_volume_mesh(P, T).with_surface_mesh(V, F)
+         .with_trust_region_acceleration(0.2, 2.0, False).construct())
+    with pytest.raises(_capi.PbgbError) as e:
         pbat.gpu.vbd.Integrator(d)
+    assert e.value.code == 1 and "trust-region" in str(e.value)
 
 
 def _cube_data():
@@ -199,3 +231,16 @@ def test_descriptor_errors_are_reported_without_a_device(defect):
         pbat.gpu.vbd.Integrator(d)
     assert e.value.code == 1, e.value
     assert expect in str(e.value)
+
+
+def test_nesterov_needs_a_single_mesh_without_contact():
+    P, T, V, F = meshgen.cube5()
+    d = (pbat.sim.vbd.Data().with_volume_mesh(P, T).with_surface_mesh(V, F)
+         .with_nesterov_acceleration(1.0, 3).construct())
+    with pytest.raises(_capi.PbgbError) as e:
+        pbat.sim.vbd.Integrator(d)
+    assert e.value.code == 1 and "Nesterov" in str(e.value)
+    with pytest.raises(ValueError):
+        pbat.sim.vbd.Data().with_volume_mesh(P, T).with_nesterov_acceleration(0.0, 3).construct()
+    with pytest.raises(ValueError):
+        pbat.sim.vbd.Data().with_volume_mesh(P, T).with_nesterov_acceleration(1.0, -1).construct()

@@ -261,3 +261,73 @@ def test_anderson_oracle_converges_faster_than_plain_vbd():
         return np.linalg.norm(g)
 
     assert grad_norm(anderson_window=5) < 0.5 * grad_norm()
+
+
+def test_nesterov_oracle_restates_the_reference_as_written():
+    """sim/vbd/NesterovIntegrator.cpp:16-43 keeps x_{k-1} at the solve's start iterate, so its first
+    accelerated iteration resets x towards that start (x = x_0 - the sweep's step).  Restated as
+    written: with no accelerated iteration (start >= iterations - 1) it is plain VBD bit for bit, and
+    on the reference doctest's 5-tet cube (L = 1, start 3, 10 iterations) it does not converge the
+    way its doctest expects (the objective gradient stays far above 1e-4, where plain VBD reaches
+    2e-6)."""
+    P, T, _, _ = meshgen.cube5()
+    X, Tr = P.T.copy(), T.T.copy()
+    mu, lam = meshgen.lame(np.full(5, 1e6), np.full(5, 0.45))
+    dt = 1e-2
+
+    def run(**kw):
+        I = O.OracleVbd(X, Tr, np.full(5, 1000.0), mu, lam, dbc=np.zeros(0, np.int32), **kw)
+        xtilde = X + dt * I.v + dt * dt * I.aext
+        I.step(dt, 10, 1, 1)
+        return I.x, np.linalg.norm(I.gradient(I.x, xtilde, dt))
+
+    x_plain, g_plain = run()
+    x_idle, _ = run(nesterov=(1.0, 9))
+    np.testing.assert_array_equal(x_idle, x_plain)
+    _, g_nes = run(nesterov=(1.0, 3))
+    assert g_plain < 1e-4 and g_nes > 1e-2
+
+
+def test_trust_region_oracle_properties():
+    """gpu/impl/vbd/TrustRegionIntegrator.cu restated: the curved path never tries an accelerated
+    step (its constraint solve returns 0), so it is plain VBD bit for bit; the linear path lowers
+    the objective gradient of a 40-iteration step well below plain VBD's."""
+    w = meshgen.unit_cube_workload(n=8, seed=1)
+    dt = 1 / 60
+
+    def run(**kw):
+        R = O.OracleVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], strategy=2, semantics=1, **kw)
+        xtilde = R.x + dt * R.v + dt * dt * R.aext
+        R.step(dt, 40, 1, 1)
+        g = R.gradient(R.x, xtilde, dt).reshape(-1, 3)
+        g[w["dbc"]] = 0.0
+        return R.x.copy(), np.linalg.norm(g)
+
+    x_plain, g_plain = run()
+    x_curved, _ = run(trust_region=(0.2, 2.0, True))
+    np.testing.assert_array_equal(x_curved, x_plain)
+    x_lin, g_lin = run(trust_region=(0.2, 2.0, False))
+    assert np.abs(x_lin - x_plain).max() > 1e-6
+    assert g_lin < 0.5 * g_plain
+
+
+def test_trust_region_oracle_replays_forced_decisions():
+    """A log that never tries a stretched step replays plain VBD bit for bit; one that tries and
+    always rejects (stretch, then roll back) stays within rounding of it."""
+    w = meshgen.unit_cube_workload(n=5, seed=2)
+    dt, it = 1 / 60, 10
+
+    def run(log=None, tr=(0.2, 2.0, False)):
+        R = O.OracleVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], strategy=2, semantics=1,
+                        **({"trust_region": tr} if tr else {}))
+        R.step(dt, it, 1, 2, trust_region_log=log)
+        return R.x.copy()
+
+    plain = run(tr=None)
+    never = np.zeros((2 * it, 4))
+    np.testing.assert_array_equal(run(never), plain)
+    reject = np.zeros((2 * it, 4))
+    reject[:, 0], reject[:, 3] = 3.0, 1.0
+    np.testing.assert_allclose(run(reject), plain, rtol=0, atol=1e-12)
+    with pytest.raises(ValueError):
+        run(np.zeros((it, 4)))
