@@ -377,7 +377,7 @@ def run_accelerated(args, pbat, torch, kind):
     vertices, 1,536,000 tets), 50 iterations per step, dt = 1/60, against plain VBD with the same
     iterations from the same state: step time (CUDA events on the integrator's stream) and the norm
     of the FP64 objective gradient over the free vertices after one step.  kind: "anderson"
-    (window 5) or "trust_region" (linear path, eta 0.2, tau 2)."""
+    (window 5), "broyden" (window 5) or "trust_region" (linear path, eta 0.2, tau 2)."""
     import ctypes as C
 
     from physicsbasedanimationtoolkit_gb300 import _capi
@@ -392,7 +392,11 @@ def run_accelerated(args, pbat, torch, kind):
             d = d.with_anderson_acceleration(5)
         elif accel == "trust_region":
             d = d.with_trust_region_acceleration(0.2, 2.0, False)
-        I = pbat.gpu.vbd.Integrator(d.construct())
+        elif accel == "broyden":
+            d = d.with_broyden_acceleration(5)
+        # Broyden is a CPU-integrator strategy in the reference (the GPU integrator runs plain VBD).
+        cls = pbat.sim.vbd.Integrator if accel == "broyden" else pbat.gpu.vbd.Integrator
+        I = cls(d.construct())
         x0, v0 = I.x.copy(), I.v.copy()
         I.step(dt, iters, 1)
         g = I.gradient(dt).reshape(-1, 3)
@@ -424,7 +428,7 @@ def run_accelerated(args, pbat, torch, kind):
         "plain_ms_per_step": ms_p,
         "plain_grad_norm_after_one_step": g_p,
     }
-    out.update({"window": 5} if kind == "anderson" else {"path": "linear", "eta": 0.2, "tau": 2.0})
+    out.update({"path": "linear", "eta": 0.2, "tau": 2.0} if kind == "trust_region" else {"window": 5})
     return out
 
 
@@ -579,7 +583,9 @@ def main():
                     help="skip the Anderson-acceleration measurement")
     ap.add_argument("--no-trust-region", dest="trust_region", action="store_false", default=True,
                     help="skip the trust-region-acceleration measurement")
-    ap.add_argument("--only", choices=["batch", "adjoint", "contact", "lbvh", "anderson", "trust_region"],
+    ap.add_argument("--no-broyden", dest="broyden", action="store_false", default=True,
+                    help="skip the Broyden-acceleration measurement")
+    ap.add_argument("--only", choices=["batch", "adjoint", "contact", "lbvh", "anderson", "broyden", "trust_region"],
                     default=None,
                     help="run only this secondary measurement and print its figures (no benchmark line)")
     args = ap.parse_args()
@@ -606,6 +612,7 @@ def main():
             "lbvh": lambda: run_lbvh(args, _capi, torch),
             "anderson": lambda: run_accelerated(args, pbat, torch, "anderson"),
             "trust_region": lambda: run_accelerated(args, pbat, torch, "trust_region"),
+            "broyden": lambda: run_accelerated(args, pbat, torch, "broyden"),
         }
         if rank == 0:
             print(json.dumps({"only": args.only, args.only: legs[args.only]()}))
@@ -703,6 +710,7 @@ def main():
         lbvh = run_lbvh(args, _capi, torch) if args.lbvh else None
         anderson = run_accelerated(args, pbat, torch, "anderson") if args.anderson else None
         trust_region = run_accelerated(args, pbat, torch, "trust_region") if args.trust_region else None
+        broyden = run_accelerated(args, pbat, torch, "broyden") if args.broyden else None
         launches = launches_per_step * args.steps
         line = {
             "metric": METRIC,
@@ -738,6 +746,7 @@ def main():
             "lbvh": lbvh,
             "anderson": anderson,
             "trust_region": trust_region,
+            "broyden": broyden,
         }
         print(json.dumps(line))
     group.close()

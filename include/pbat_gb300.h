@@ -57,6 +57,7 @@ extern "C" {
 #define PBGB_ACCEL_CHEBYSHEV 1
 #define PBGB_ACCEL_ANDERSON 2 /* single mesh without contact; window_size columns */
 #define PBGB_ACCEL_NESTEROV 3 /* nesterov_lipschitz, nesterov_start */
+#define PBGB_ACCEL_BROYDEN 4 /* single mesh without contact; window_size columns */
 #define PBGB_ACCEL_TRUST_REGION 5 /* tr_eta, tr_tau, tr_curved; single mesh without contact */
 /* graph/Enums.h:20-33 */
 #define PBGB_COLOR_ORDER_NATURAL 0
@@ -150,7 +151,7 @@ typedef struct pbgb_vbd_desc
     double muF;                    /* friction coefficient (default 0.3) */
     double epsv;                   /* IPC smooth friction velocity threshold (default 1e-3) */
     int32_t active_set_update_frequency; /* update the contact list every k substeps (default 1) */
-    int32_t window_size; /* Anderson window m, 1..16 (PBGB_ACCEL_ANDERSON; Data::mWindowSize, default 5) */
+    int32_t window_size; /* Anderson / Broyden window m, 1..16 (Data::mWindowSize, default 5) */
     double nesterov_lipschitz; /* L > 0 (Data::mNesterovLipschitzConstant, default 1) */
     int32_t nesterov_start;    /* accelerate iterations k > start >= 0 (default 3) */
     /* Trust-region acceleration (gpu/impl/vbd/TrustRegionIntegrator.cu; Data::eta, tau, bCurved). */

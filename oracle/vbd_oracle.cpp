@@ -560,6 +560,121 @@ static void anderson_lsq(std::vector<std::vector<Real>> const& A, int m, Real co
 // ChebyshevIntegrator.cpp:15-32.
 double orc_objective(orc_problem const* Pp, double const* x, double const* xtilde, double dt);
 
+// Least-squares conjugate gradient on min |A gamma - b|, A = the first mk of the window columns
+// (Eigen's LeastSquaresConjugateGradient with IdentityPreconditioner and a zero initial guess, the
+// solver BroydenIntegrator.cpp:67-72 calls; Eigen is pinned by the reference at commit
+// 7fd305ecae2410714cde018cb6851f49138568c8 and is not part of its sources).  CGLS: the normal
+// residual A^T r drives the directions; stop after maxIters steps or when |A^T r|^2 < tol^2 |A^T b|^2.
+static void cgls(std::vector<std::vector<Real>> const& A, int mk, Real const* b, size_t n, int maxIters, Real tol, Real* gamma)
+{
+    std::vector<Real> r(b, b + n), tmp(n);
+    Real nr[16], p[16];
+    auto At = [&](Real const* v, Real* out) {
+        for (int j = 0; j < mk; ++j)
+        {
+            Real s = 0;
+            for (size_t q = 0; q < n; ++q)
+                s += A[size_t(j)][q] * v[q];
+            out[j] = s;
+        }
+    };
+    for (int j = 0; j < mk; ++j)
+        gamma[j] = 0;
+    At(b, nr);
+    Real rhsNorm2 = 0;
+    for (int j = 0; j < mk; ++j)
+        rhsNorm2 += nr[j] * nr[j];
+    if (rhsNorm2 == 0)
+        return;
+    Real const threshold = tol * tol * rhsNorm2;
+    Real absNew          = rhsNorm2; // |A^T r|^2 with r = b
+    if (absNew < threshold)
+        return;
+    for (int j = 0; j < mk; ++j)
+        p[j] = nr[j];
+    for (int it = 0; it < maxIters; ++it)
+    {
+        Real tn = 0;
+        for (size_t q = 0; q < n; ++q)
+        {
+            Real v = 0;
+            for (int j = 0; j < mk; ++j)
+                v += A[size_t(j)][q] * p[j];
+            tmp[q] = v;
+            tn += v * v;
+        }
+        Real const alpha = absNew / tn;
+        for (int j = 0; j < mk; ++j)
+            gamma[j] += alpha * p[j];
+        for (size_t q = 0; q < n; ++q)
+            r[q] -= alpha * tmp[q];
+        At(r.data(), nr);
+        Real rn2 = 0;
+        for (int j = 0; j < mk; ++j)
+            rn2 += nr[j] * nr[j];
+        if (rn2 < threshold)
+            break;
+        Real const beta = rn2 / absNew;
+        absNew          = rn2;
+        for (int j = 0; j < mk; ++j)
+            p[j] = nr[j] + beta * p[j];
+    }
+}
+
+// BroydenIntegrator::Solve (sim/vbd/BroydenIntegrator.cpp:41-80): with VBD(f_k) = x_k - x_{k+1}
+// the negated sweep step, after each sweep k >= 1 column (k-1) mod m of X gets x_k - x_{k-1}
+// (pre-sweep iterates) and of G the change of VBD(f); gamma = CGLS(G, VBD(f_k)) with at most
+// max(1, m - k) iterations and tolerance 1e-10, and x <- x - (X - G) gamma.
+static void broyden(orc_problem const& P, Real const* xt, Real const* xtilde, Real* x, Real sdt, Real sdt2, int32_t iterations, int nthreads)
+{
+    (void)nthreads;
+    size_t const n3 = size_t(P.nV) * 3;
+    int const m     = P.window;
+    std::vector<std::vector<Real>> G(static_cast<size_t>(m), std::vector<Real>(n3));
+    std::vector<std::vector<Real>> X(static_cast<size_t>(m), std::vector<Real>(n3));
+    std::vector<Real> xkm1(x, x + n3), fk(n3), fkm1(n3);
+    auto sweep = [&] {
+        for (int32_t p = 0; p < P.nPartitions; ++p)
+        {
+            int32_t const b = P.Pptr[p], e = P.Pptr[p + 1];
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+            for (int32_t kk = b; kk < e; ++kk)
+                solve_vertex(P, P.Padj[kk], xt, xtilde, x, sdt, sdt2);
+        }
+    };
+    if (iterations <= 0)
+        return;
+    sweep();
+    for (size_t q = 0; q < n3; ++q)
+        fkm1[q] = xkm1[q] - x[q];
+    for (int32_t k = 1; k < iterations; ++k)
+    {
+        int const dkl = (k - 1) % m;
+        for (size_t q = 0; q < n3; ++q)
+        {
+            X[size_t(dkl)][q] = x[q] - xkm1[q];
+            xkm1[q]           = x[q];
+        }
+        sweep();
+        for (size_t q = 0; q < n3; ++q)
+        {
+            fk[q]             = xkm1[q] - x[q];
+            G[size_t(dkl)][q] = fk[q] - fkm1[q];
+            fkm1[q]           = fk[q];
+        }
+        int const mk = std::min(m, int(k));
+        Real gamma[16];
+        cgls(G, mk, fk.data(), n3, std::max(1, m - int(k)), Real(1e-10), gamma);
+        for (size_t q = 0; q < n3; ++q)
+        {
+            Real u = 0;
+            for (int j = 0; j < mk; ++j)
+                u += (X[size_t(j)][q] - G[size_t(j)][q]) * gamma[j];
+            x[q] -= u;
+        }
+    }
+}
+
 // Minimiser of the quadratic model a t^2 + b t + c (TrustRegionIntegrator.cu:400-430), with the
 // reference's float thresholds: FLT_MIN as zero and FLT_MAX as infinity.
 static Real tr_model_optimal_step(Real const aQ[3])
@@ -795,6 +910,8 @@ int orc_run(orc_problem const* Pp, double* x, double* v, double* vprev, double d
                 neX0.assign(x, x + size_t(nV) * 3);
                 neY.assign(size_t(nV) * 3, 0);
             }
+            if (P.acceleration == 4)
+                broyden(P, xt.data(), xtilde.data(), x, sdt, sdt2, iterations, nthreads);
             if (P.acceleration == 5 && !P.tr_curved)
                 trust_region_linear(P, xt.data(), xtilde.data(), x, sdt, sdt2, iterations, nthreads,
                                     P.tr_forced ? P.tr_forced + 4 * (size_t(step) * size_t(substeps) + size_t(s)) * size_t(iterations)
@@ -804,7 +921,7 @@ int orc_run(orc_problem const* Pp, double* x, double* v, double* vprev, double d
             // The curved trust-region path (TrustRegionIntegrator.cu:167-263) never moves x off the
             // VBD iterates: its constraint solve returns 0, so t = clamp(t*, FLT_MIN, 0) is at the
             // lower bound, no accelerated step is tried and every iteration is a plain VBD sweep.
-            bool const plainLoop = !(P.acceleration == 2 || (P.acceleration == 5 && !P.tr_curved));
+            bool const plainLoop = !(P.acceleration == 2 || P.acceleration == 4 || (P.acceleration == 5 && !P.tr_curved));
             for (int32_t k = 0; k < (plainLoop ? iterations : 0); ++k)
             {
                 bool const neActive = P.acceleration == 3 && P.nesterov_start < k;

@@ -17,12 +17,11 @@ SEMANTICS_GPU = 1
 # (bindings/pypbat/sim/vbd/Integrator.cpp:31-45) builds Chebyshev, Anderson, Broyden and Nesterov
 # integrators and the base integrator otherwise (trust region included); the GPU integrator
 # (gpu/vbd/Integrator.cu:15-33) builds Anderson, Chebyshev and trust-region integrators and the base
-# integrator otherwise (Nesterov and Broyden included).  None marks what this library lacks.
+# integrator otherwise (Nesterov and Broyden included).
 _DISPATCH = {
-    SEMANTICS_CPU: {0: 0, 1: 1, 2: 2, 3: 3, 4: None, 5: 0},
+    SEMANTICS_CPU: {0: 0, 1: 1, 2: 2, 3: 3, 4: 4, 5: 0},
     SEMANTICS_GPU: {0: 0, 1: 1, 2: 2, 3: 0, 4: 0, 5: 5},
 }
-_NAMES = {4: "Broyden"}
 
 
 def make_desc(data, semantics):
@@ -30,11 +29,6 @@ def make_desc(data, semantics):
     if not getattr(data, "_constructed", False):
         raise ValueError("Data must be constructed (call Data.construct()) before creating an integrator")
     accel = _DISPATCH[semantics].get(int(data.eAcceleration), 0)
-    if accel is None:
-        raise NotImplementedError(
-            f"{_NAMES[int(data.eAcceleration)]} acceleration is not part of this library's VBD path "
-            "(Base, Chebyshev, Anderson, Nesterov and trust region are)"
-        )
     nV, nT = data.X.shape[1], data.E.shape[1]
     keep = dict(
         x=_capi.f64(np.asarray(data.x).T),

@@ -17,7 +17,10 @@ __global__ void anderson_start_kernel(AndersonParams p)
     int const i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n)
         return;
-    p.Gkm1[i] = p.x[i];
+    if (p.broyden)
+        p.DG[i] = p.step[i]; // X_0 = x_1 - x_0: iteration 0 is a plain sweep
+    else
+        p.Gkm1[i] = p.x[i];
     p.Fkm1[i] = p.step[i];
 }
 
@@ -36,16 +39,19 @@ __global__ void __launch_bounds__(kWindowThreads) anderson_window_kernel(Anderso
         accA[t] = 0.0;
     if (i < p.n)
     {
-        float4 const g  = p.x[i];
         float4 const f  = p.step[i];
-        float4 const gp = p.Gkm1[i];
         float4 const fp = p.Fkm1[i];
-        float4 const dg = make_float4(g.x - gp.x, g.y - gp.y, g.z - gp.z, 0.f);
         float4 const df = make_float4(f.x - fp.x, f.y - fp.y, f.z - fp.z, 0.f);
         size_t const n  = size_t(p.n);
-        p.DG[size_t(p.dkl) * n + i] = dg;
+        if (!p.broyden)
+        {
+            // Broyden's X column was written by the previous update.
+            float4 const g              = p.x[i];
+            float4 const gp             = p.Gkm1[i];
+            p.DG[size_t(p.dkl) * n + i] = make_float4(g.x - gp.x, g.y - gp.y, g.z - gp.z, 0.f);
+            p.Gkm1[i]                   = g;
+        }
         p.DF[size_t(p.dkl) * n + i] = df;
-        p.Gkm1[i]                   = g;
         p.Fkm1[i]                   = f;
 #pragma unroll
         for (int j = 0; j < kAndersonMaxWindow; ++j)
@@ -138,6 +144,58 @@ __global__ void __launch_bounds__(kSolveThreads) anderson_solve_kernel(AndersonP
     }
     for (int j = 0; j < mk; ++j)
         sums[mk + j] = p.rhs[j];
+    if (p.broyden)
+    {
+        // Eigen's LeastSquaresConjugateGradient (IdentityPreconditioner, zero initial guess) on
+        // min |DF gamma - F_k|, written on the normal equations: the normal residual
+        // DF^T (F_k - DF gamma) starts at b = DF^T F_k and drops by a (DF^T DF) p per step.
+        double* gam = &V[0][0];
+        double* nr  = &V[1][0];
+        double* pv  = &V[2][0];
+        double* Ap  = &V[3][0];
+        double rhsNorm2 = 0.0;
+        for (int j = 0; j < mk; ++j)
+        {
+            gam[j] = 0.0;
+            nr[j]  = sums[mk + j];
+            pv[j]  = nr[j];
+            rhsNorm2 += nr[j] * nr[j];
+        }
+        double const threshold = 1e-20 * rhsNorm2; // tolerance 1e-10, squared
+        if (rhsNorm2 > 0.0)
+        {
+            double absNew = rhsNorm2;
+            for (int it = 0; it < p.maxIters; ++it)
+            {
+                double pAp = 0.0;
+                for (int i = 0; i < mk; ++i)
+                {
+                    double v = 0.0;
+                    for (int j = 0; j < mk; ++j)
+                        v += p.gram[i * m + j] * pv[j];
+                    Ap[i] = v;
+                    pAp += pv[i] * v;
+                }
+                double const a = absNew / pAp;
+                double rn2     = 0.0;
+                for (int j = 0; j < mk; ++j)
+                {
+                    gam[j] += a * pv[j];
+                    nr[j] -= a * Ap[j];
+                    rn2 += nr[j] * nr[j];
+                }
+                if (rn2 < threshold)
+                    break;
+                double const beta = rn2 / absNew;
+                absNew            = rn2;
+                for (int j = 0; j < mk; ++j)
+                    pv[j] = nr[j] + beta * pv[j];
+            }
+        }
+        for (int j = 0; j < mk; ++j)
+            p.alpha[j] = gam[j];
+        return;
+    }
     // (G + eps I) alpha = b by Cholesky, eps = 1e-10 of the largest diagonal entry: the exact
     // least-squares solution where DF is well conditioned, directions far below eps damped to zero.
     double dmax = 0.0;
@@ -190,6 +248,27 @@ __global__ void anderson_update_kernel(AndersonParams p)
         return;
     float4 u       = p.x[i];
     size_t const n = size_t(p.n);
+    if (p.broyden)
+    {
+        // x <- x - (X + DF) gamma; the next X column is this iteration's total move.
+        float cx = 0.f, cy = 0.f, cz = 0.f;
+        for (int j = 0; j < p.mk; ++j)
+        {
+            float const a   = float(p.alpha[j]);
+            float4 const X  = p.DG[size_t(j) * n + i];
+            float4 const Df = p.DF[size_t(j) * n + i];
+            cx += a * (X.x + Df.x);
+            cy += a * (X.y + Df.y);
+            cz += a * (X.z + Df.z);
+        }
+        p.x[i] = make_float4(u.x - cx, u.y - cy, u.z - cz, 0.f);
+        if (p.next >= 0)
+        {
+            float4 const f               = p.step[i];
+            p.DG[size_t(p.next) * n + i] = make_float4(f.x - cx, f.y - cy, f.z - cz, 0.f);
+        }
+        return;
+    }
     for (int j = 0; j < p.mk; ++j)
     {
         float const a  = float(p.alpha[j]);

@@ -21,6 +21,15 @@
 // same alpha when DF is well conditioned.  When it is not, the ridge damps the directions below eps
 // towards zero as the CPU's minimum-norm solution does, where a QR with patched pivots can return
 // arbitrarily large coefficients.
+//
+// Broyden-accelerated VBD (sim/vbd/BroydenIntegrator.cpp:41-80) runs on the same window: with
+// VBD(f_k) = -(the iteration's increments), its G_{k-m} VBD(Delta f) columns are -DF, and its
+// iterate-difference columns X_j (x_k - x_{k-1}, pre-sweep iterates) are kept in DG.  gamma solves
+// min |DF gamma - F_k| by the reference's least-squares conjugate gradient (Eigen's CGLS, zero
+// initial guess, at most max(1, m - k) iterations, relative tolerance 1e-10), run here on the
+// normal equations with the FP64 Gram matrix (the same iterates in exact arithmetic), and
+// x <- x - (X + DF) gamma.  The update kernel also writes the next X column,
+// x_{k+1} - x_k = F_k - (X + DF) gamma, without cancelling against the positions.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -46,11 +55,15 @@ struct AndersonParams
     int32_t m;
     int32_t dkl; // column written this iteration
     int32_t mk;  // filled columns
+    int32_t broyden;  // 0: Anderson, 1: Broyden
+    int32_t maxIters; // Broyden: conjugate-gradient iterations of this solve
+    int32_t next;     // Broyden: X column the update writes for the next iteration (-1: none)
 };
 
 int anderson_window_blocks(int32_t n);
 
-// After iteration 0: G_{k-1} = x, F_{k-1} = the iteration's increments.
+// After iteration 0: G_{k-1} = x, F_{k-1} = the iteration's increments (Broyden: the first X
+// column = the increments, F_{k-1} = the increments).
 cudaError_t launch_anderson_start(AndersonParams const& p, cudaStream_t s);
 cudaError_t launch_anderson_window(AndersonParams const& p, cudaStream_t s);
 cudaError_t launch_anderson_solve(AndersonParams const& p, cudaStream_t s);

@@ -94,7 +94,7 @@ class DeviceArray
 // relies on it).
 inline void validate_descs(pbgb_vbd_desc const* descs, int32_t nMeshes)
 {
-    auto bad = [](char const* what) { throw std::invalid_argument(std::string("pbgb_vbd_desc: ") + what); };
+    auto bad = [](std::string const& what) { throw std::invalid_argument("pbgb_vbd_desc: " + what); };
     auto finite = [](double const* a, int64_t n) {
         for (int64_t k = 0; k < n; ++k)
             if (!std::isfinite(a[k]))
@@ -157,7 +157,7 @@ inline void validate_descs(pbgb_vbd_desc const* descs, int32_t nMeshes)
             throw std::invalid_argument("Expected 0 < rho < 1");
         if (d.acceleration != PBGB_ACCEL_NONE && d.acceleration != PBGB_ACCEL_CHEBYSHEV &&
             d.acceleration != PBGB_ACCEL_ANDERSON && d.acceleration != PBGB_ACCEL_NESTEROV &&
-            d.acceleration != PBGB_ACCEL_TRUST_REGION)
+            d.acceleration != PBGB_ACCEL_BROYDEN && d.acceleration != PBGB_ACCEL_TRUST_REGION)
             bad("unsupported acceleration strategy");
         if (d.acceleration == PBGB_ACCEL_TRUST_REGION)
         {
@@ -171,12 +171,13 @@ inline void validate_descs(pbgb_vbd_desc const* descs, int32_t nMeshes)
             bad("Nesterov acceleration expects L > 0 and start >= 0");
         if (d.acceleration == PBGB_ACCEL_NESTEROV && (nMeshes != 1 || d.n_collision_triangles > 0))
             bad("Nesterov acceleration needs a single mesh without contact");
-        if (d.acceleration == PBGB_ACCEL_ANDERSON)
+        if (d.acceleration == PBGB_ACCEL_ANDERSON || d.acceleration == PBGB_ACCEL_BROYDEN)
         {
+            char const* name = d.acceleration == PBGB_ACCEL_ANDERSON ? "Anderson" : "Broyden";
             if (d.window_size < 1 || d.window_size > kAndersonMaxWindow)
-                bad("Anderson window must be in [1, 16]");
+                bad(std::string(name) + " window must be in [1, 16]");
             if (nMeshes != 1 || d.n_collision_triangles > 0)
-                bad("Anderson acceleration needs a single mesh without contact");
+                bad(std::string(name) + " acceleration needs a single mesh without contact");
         }
         if (d.init_strategy < 0 || d.init_strategy > 4)
             bad("invalid initialization strategy");
@@ -220,7 +221,7 @@ class VbdSystem
     int32_t strategy  = PBGB_INIT_ADAPTIVE_PBAT;
     float kD = 0.f, detHZero = 1e-7f;
     int32_t acceleration = PBGB_ACCEL_NONE, chebFormula = PBGB_CHEBYSHEV_REFERENCE, semantics = 0;
-    int32_t window = 0; // Anderson window
+    int32_t window = 0; // Anderson / Broyden window
     double nesterovL = 1.0;
     int32_t nesterovStart = 3;
     double trEta = 0.2, trTau = 2.0;
@@ -468,7 +469,7 @@ class VbdSystem
         rho            = d0.rho;
         chebFormula    = d0.chebyshev_formula;
         semantics      = d0.semantics;
-        window         = acceleration == PBGB_ACCEL_ANDERSON ? d0.window_size : 0;
+        window         = windowed() ? d0.window_size : 0;
         nesterovL      = d0.nesterov_lipschitz;
         nesterovStart  = d0.nesterov_start;
         trEta          = d0.tr_eta;
@@ -703,7 +704,7 @@ class VbdSystem
             trPartials.allocate(size_t(kTrustMaxBlocks));
             check(cudaMemsetAsync(trState.get(), 0, sizeof(TrustState), stream), "memset");
         }
-        if (acceleration == PBGB_ACCEL_ANDERSON)
+        if (windowed())
         {
             anStep.allocate(nV);
             anGkm1.allocate(nV);
@@ -1181,7 +1182,7 @@ class VbdSystem
                 hooks->substepBegin(s);
             double omega      = 0.0;
             double const rho2 = rho * rho;
-            bool const anderson = !plainOnly && acceleration == PBGB_ACCEL_ANDERSON;
+            bool const anderson = !plainOnly && windowed();
             bool const nesterov = !plainOnly && acceleration == PBGB_ACCEL_NESTEROV;
             bool const trust    = !plainOnly && trustLinear();
             TrustParams tp{};
@@ -1223,6 +1224,7 @@ class VbdSystem
                 ap.rhs      = anRhs.get();
                 ap.n        = nV;
                 ap.m        = window;
+                ap.broyden  = acceleration == PBGB_ACCEL_BROYDEN;
                 w.step = anStep.get();
             }
             for (int32_t k = 0; k < iterations; ++k)
@@ -1279,13 +1281,16 @@ class VbdSystem
                 }
                 if (anderson)
                 {
-                    // AndersonIntegrator::Solve (sim/vbd/AndersonIntegrator.cpp:31-56).
+                    // AndersonIntegrator::Solve (sim/vbd/AndersonIntegrator.cpp:31-56),
+                    // BroydenIntegrator::Solve (sim/vbd/BroydenIntegrator.cpp:41-80).
                     if (k == 0)
                         check(launch_anderson_start(ap, stream), "anderson_start");
                     else
                     {
-                        ap.dkl = (k - 1) % window;
-                        ap.mk  = std::min(window, k);
+                        ap.dkl      = (k - 1) % window;
+                        ap.mk       = std::min(window, k);
+                        ap.maxIters = std::max(1, window - k);
+                        ap.next     = k + 1 < iterations ? k % window : -1;
                         check(launch_anderson_window(ap, stream), "anderson_window");
                         check(launch_anderson_solve(ap, stream), "anderson_solve");
                         check(launch_anderson_update(ap, stream), "anderson_update");
@@ -1502,6 +1507,8 @@ class VbdSystem
     // The curved trust-region path moves x exactly as plain VBD does (its constraint solve
     // returns 0, so no accelerated step is ever tried): only the linear path has device work.
     bool trustLinear() const { return acceleration == PBGB_ACCEL_TRUST_REGION && !trCurved; }
+    // Anderson and Broyden share the window buffers and kernels.
+    bool windowed() const { return acceleration == PBGB_ACCEL_ANDERSON || acceleration == PBGB_ACCEL_BROYDEN; }
 
     int64_t launchesPerStep(int32_t iterations, int32_t substeps) const
     {
@@ -1509,7 +1516,7 @@ class VbdSystem
         for (int32_t c = 0; c < nColors; ++c)
             perIter += colorPtr[c + 1] > colorPtr[c] ? 1 : 0;
         int64_t n = int64_t(substeps) * (2 * (nV > 0 ? 1 : 0) + int64_t(iterations) * perIter);
-        if (acceleration == PBGB_ACCEL_ANDERSON && iterations > 0)
+        if (windowed() && iterations > 0)
             n += int64_t(substeps) * (1 + 3 * int64_t(iterations - 1));
         if (acceleration == PBGB_ACCEL_NESTEROV)
             n += int64_t(substeps) * 2 * std::max<int64_t>(0, int64_t(iterations) - 1 - nesterovStart);

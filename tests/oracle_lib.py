@@ -198,7 +198,7 @@ class OracleVbd:
     def __init__(self, X, T, rho, mu, lam, dbc, v=None, aext=None, strategy=4, kD=0.0,
                  detHZero=1e-7, rho_chebyshev=None, chebyshev_formula=0, semantics=0,
                  nthreads=0, ordering=2, selection=0, data=None, anderson_window=None, nesterov=None,
-                 trust_region=None):
+                 trust_region=None, broyden_window=None):
         self.X = np.ascontiguousarray(X, dtype=np.float64)
         self.T = np.ascontiguousarray(T, dtype=np.int32)
         nV = self.X.shape[0]
@@ -234,6 +234,11 @@ class OracleVbd:
                 raise ValueError("Anderson window must be in [1, 16]")
             P.acceleration = 2
             P.window = int(anderson_window)
+        if broyden_window is not None:
+            if not 1 <= broyden_window <= 16:
+                raise ValueError("Broyden window must be in [1, 16]")
+            P.acceleration = 4
+            P.window = int(broyden_window)
         if nesterov is not None:
             P.acceleration = 3
             P.nesterov_L, P.nesterov_start = float(nesterov[0]), int(nesterov[1])

@@ -143,15 +143,17 @@ def test_integrator_creation_without_device_fails_loudly():
     assert e.value.code == 6
 
 
-def test_broyden_is_rejected():
-    P, T, _, _ = meshgen.cube5()
-    d = pbat.sim.vbd.Data().with_volume_mesh(P, T).with_broyden_acceleration(5).construct()
-    with pytest.raises(NotImplementedError):
+def test_broyden_needs_a_single_mesh_without_contact():
+    P, T, V, F = meshgen.cube5()
+    d = (pbat.sim.vbd.Data().with_volume_mesh(P, T).with_surface_mesh(V, F)
+         .with_broyden_acceleration(5).construct())
+    with pytest.raises(_capi.PbgbError) as e:
         pbat.sim.vbd.Integrator(d)
+    assert e.value.code == 1 and "Broyden" in str(e.value)
 
 
 @pytest.mark.parametrize("accel,cpu,gpu", [("none", 0, 0), ("chebyshev", 1, 1), ("anderson", 2, 2),
-                                           ("nesterov", 3, 0), ("broyden", None, 0), ("trust_region", 0, 5)])
+                                           ("nesterov", 3, 0), ("broyden", 4, 0), ("trust_region", 0, 5)])
 def test_acceleration_dispatch_follows_the_reference(accel, cpu, gpu):
     """The CPU integrator runs Chebyshev, Anderson, Broyden and Nesterov and the base integrator
     otherwise; the GPU integrator runs Anderson, Chebyshev and trust region and the base
