@@ -215,63 +215,33 @@ __global__ void compact_kernel(int32_t n, uint8_t const* __restrict__ active, in
 }
 
 // Nearest triangles of active vertex av[q] (gpu/impl/geometry/Bvh.cuh:347-474 with the contact
-// callbacks of gpu/impl/contact/VertexTriangleMixedCcdDcd.cuh:109-162): depth-first branch and
-// bound from the warm-start radius; triangles within FLT_EPSILON of the best are kept (at most
-// kMaxContacts), a strictly better one restarts the list.  finalize = false writes the list to nn,
-// finalize = true sets active[v] from the side of the last listed triangle's plane.
-template <bool FINALIZE>
-__global__ void nearest_kernel(ContactMesh M, ContactState S, BvhView T, float4 const* __restrict__ x)
+// callbacks of gpu/impl/contact/VertexTriangleMixedCcdDcd.cuh:109-162): the reference runs a
+// depth-first branch and bound from the warm-start radius (right child first, so leaves are met in
+// decreasing sorted order); triangles within FLT_EPSILON of the best are kept (at most
+// kMaxContacts) and a strictly better one restarts the list.  finalize = false writes the list to
+// nn, finalize = true sets active[v] from the side of the last listed triangle's plane.
+//
+// The list is the result of scanning the leaves in that order with the running minimum: a leaf the
+// branch and bound prunes lies beyond the running bound and would change nothing.  Two passes give
+// the same list with far fewer node visits when the warm-start radius is loose:
+//   1. the exact nearest distance d* (closer child first, pruned by the best distance so far);
+//   2. the reference-order scan, pruned by min(running bound, d* + 8 FLT_EPSILON + 16 ulp).
+// The last restart of the scan has d <= d* + eps (otherwise the d* triangle would restart it
+// again) and every triangle listed after it has d <= d* + 2 eps (FP32 rounding of the bounds
+// widens each eps to at most an ulp of d), so the leaves pass 2 skips can
+// neither restart nor join the final list, and removing them leaves the last restart and
+// everything after it unchanged.
+__device__ __forceinline__ float node_box_sqdist(BvhView const& T, float3 p, int32_t node, int32_t leafBegin)
 {
-    int const q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= *S.nActive || T.n < 1)
-        return;
-    int const v = S.av[q];
-    int const i = M.V[v];
-    float3 const p = f3(x[i]);
-    int const body = M.B[i];
-    float const eps = FLT_EPSILON;
-    float dmin      = S.dupper[v];
-    int32_t list[kMaxContacts];
-    int count = 0;
-    int32_t const leafBegin = T.n - 1;
-    int32_t stack[kBvhStack];
-    int top      = 0;
-    stack[top++] = 0;
-    while (top > 0)
-    {
-        int32_t const node = stack[--top];
-        float const lo     = dmin - eps;
-        float const hi     = dmin + eps;
-        if (node < leafBegin)
-        {
-            if (point_box_sqdist(p, T.ilo[node], T.ihi[node]) <= hi)
-            {
-                if (top + 2 > kBvhStack)
-                {
-                    atomicOr(S.flags, kBvhErrStackOverflow);
-                    return;
-                }
-                stack[top++] = T.child[2 * node];
-                stack[top++] = T.child[2 * node + 1];
-            }
-            continue;
-        }
-        int32_t const s = node - leafBegin;
-        if (point_box_sqdist(p, T.llo[s], T.lhi[s]) > hi)
-            continue;
-        int32_t const f = T.inds[s];
-        int4 const t    = M.F[f];
-        float const d   = M.B[t.x] == body ? FLT_MAX
-                                           : point_triangle_sqdist(p, f3(x[t.x]), f3(x[t.y]), f3(x[t.z]));
-        if (d < lo)
-        {
-            list[0] = f;
-            count   = 1;
-            dmin    = d;
-        }
-        else if (d <= hi && count < kMaxContacts)
-            list[count++] = f;
-    }
+    return node < leafBegin ? point_box_sqdist(p, T.ilo[node], T.ihi[node])
+                            : point_box_sqdist(p, T.llo[node - leafBegin], T.lhi[node - leafBegin]);
+}
+
+// Writes the result of a query (see nearest_kernel).
+template <bool FINALIZE>
+__device__ void nearest_write(ContactMesh const& M, ContactState const& S, float4 const* __restrict__ x, int v, int i,
+                              float3 p, int32_t const* list, int count)
+{
     if (FINALIZE)
     {
         if (count > 0)
@@ -286,11 +256,300 @@ __global__ void nearest_kernel(ContactMesh M, ContactState S, BvhView T, float4 
     {
         for (int k = 0; k < kMaxContacts; ++k)
         {
-            int32_t const f                 = k < count ? list[k] : -1;
-            S.nn[v * kMaxContacts + k]      = f;
-            S.fc[i * kMaxContacts + k]      = f;
+            int32_t const f            = k < count ? list[k] : -1;
+            S.nn[v * kMaxContacts + k] = f;
+            S.fc[i * kMaxContacts + k] = f;
         }
     }
+}
+
+// One thread's query of active vertex av[q]: the two passes described above.
+template <bool FINALIZE>
+__device__ void nearest_serial(ContactMesh const& M, ContactState const& S, BvhView const& T, float4 const* __restrict__ x, int q)
+{
+    int const v = S.av[q];
+    int const i = M.V[v];
+    float3 const p = f3(x[i]);
+    int const body = M.B[i];
+    float const eps = FLT_EPSILON;
+    float const d0  = S.dupper[v];
+    int32_t const leafBegin = T.n - 1;
+    int32_t stack[kBvhStack];
+    float dist[kBvhStack];
+    int top = 0;
+
+    // Pass 1: d* over the triangles of other bodies within the reference's initial bound.
+    float best = d0 + eps;
+    bool found = false;
+    stack[top]  = 0;
+    dist[top++] = node_box_sqdist(T, p, 0, leafBegin);
+    while (top > 0)
+    {
+        --top;
+        int32_t const node = stack[top];
+        if (dist[top] > best)
+            continue;
+        if (node < leafBegin)
+        {
+            int32_t const a = T.child[2 * node], b = T.child[2 * node + 1];
+            float const da = node_box_sqdist(T, p, a, leafBegin), db = node_box_sqdist(T, p, b, leafBegin);
+            if (top + 2 > kBvhStack)
+            {
+                atomicOr(S.flags, kBvhErrStackOverflow);
+                return;
+            }
+            // Farther child first, so the nearer one is expanded next.
+            bool const aFirst = da > db;
+            int32_t const n0 = aFirst ? a : b, n1 = aFirst ? b : a;
+            float const e0 = aFirst ? da : db, e1 = aFirst ? db : da;
+            if (e0 <= best)
+                stack[top] = n0, dist[top++] = e0;
+            if (e1 <= best)
+                stack[top] = n1, dist[top++] = e1;
+            continue;
+        }
+        int4 const t = M.F[T.inds[node - leafBegin]];
+        if (M.B[t.x] == body)
+            continue;
+        float const d = point_triangle_sqdist(p, f3(x[t.x]), f3(x[t.y]), f3(x[t.z]));
+        if (d <= best)
+        {
+            best  = d;
+            found = true;
+        }
+    }
+
+    // Pass 2: the reference-order scan over the leaves that can matter.
+    int32_t list[kMaxContacts];
+    int count = 0;
+    if (found)
+    {
+        // 2 eps suffices in exact arithmetic; FP32 rounding of dmin +- eps can widen each
+        // tolerance to one ulp of dmin, so the cap keeps a relative and an absolute margin.
+        float const cap = best * (1.f + 16.f * eps) + 8.f * eps;
+        float dmin      = d0;
+        top             = 0;
+        stack[top++]    = 0;
+        while (top > 0)
+        {
+            int32_t const node = stack[--top];
+            float const lo     = dmin - eps;
+            float const hi     = dmin + eps;
+            float const bound  = fminf(hi, cap);
+            if (node < leafBegin)
+            {
+                if (point_box_sqdist(p, T.ilo[node], T.ihi[node]) <= bound)
+                {
+                    if (top + 2 > kBvhStack)
+                    {
+                        atomicOr(S.flags, kBvhErrStackOverflow);
+                        return;
+                    }
+                    stack[top++] = T.child[2 * node];
+                    stack[top++] = T.child[2 * node + 1];
+                }
+                continue;
+            }
+            int32_t const s = node - leafBegin;
+            if (point_box_sqdist(p, T.llo[s], T.lhi[s]) > bound)
+                continue;
+            int32_t const f = T.inds[s];
+            int4 const t    = M.F[f];
+            float const d   = M.B[t.x] == body ? FLT_MAX
+                                               : point_triangle_sqdist(p, f3(x[t.x]), f3(x[t.y]), f3(x[t.z]));
+            if (d < lo)
+            {
+                list[0] = f;
+                count   = 1;
+                dmin    = d;
+            }
+            else if (d <= hi && count < kMaxContacts)
+                list[count++] = f;
+        }
+    }
+    nearest_write<FINALIZE>(M, S, x, v, i, p, list, count);
+}
+
+int constexpr kNearestWarps    = 2;    // warps (queries) per block
+int constexpr kNearestFrontier = 1024; // breadth-first frontier capacity per warp
+int constexpr kNearestCand     = 1024; // candidate leaves per warp
+
+struct NearestSmem
+{
+    int32_t frontier[2][kNearestFrontier];
+    int32_t cand[kNearestCand]; // sorted leaf index
+    float candD[kNearestCand];  // its squared distance (FLT_MAX: the vertex's own body)
+};
+
+// Warp-cooperative form of the same query, one warp per active vertex.  The traversal is what
+// bounds the kernel: a query's loads form one dependent chain per thread, so spreading it over 32
+// lanes shortens the longest chain about as many times.
+//   1. breadth first, collect every leaf whose box lies within the reference's initial bound
+//      dupper + eps, with its triangle's squared distance (only these can ever be listed);
+//   2. d* = the warp minimum over other bodies; keep the candidates with d <= d* + margin (see
+//      above: no other leaf can restart the scan's final list or join it);
+//   3. order them by decreasing leaf index (the reference's visit order) and run its scan.
+// A frontier or candidate overflow hands the query to lane 0's serial traversal.
+template <bool FINALIZE>
+__global__ void __launch_bounds__(32 * kNearestWarps) nearest_kernel(ContactMesh M, ContactState S, BvhView T, float4 const* __restrict__ x)
+{
+    extern __shared__ unsigned char nearestSmemRaw[];
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    NearestSmem& sm = reinterpret_cast<NearestSmem*>(nearestSmemRaw)[warp];
+    int const q     = blockIdx.x * kNearestWarps + warp;
+    if (q >= *S.nActive || T.n < 1)
+        return;
+    unsigned const all = 0xffffffffu;
+    int const v        = S.av[q];
+    int const i        = M.V[v];
+    float3 const p     = f3(x[i]);
+    int const body     = M.B[i];
+    float const eps    = FLT_EPSILON;
+    float const d0     = S.dupper[v];
+    float const bound  = d0 + eps;
+    int32_t const leafBegin = T.n - 1;
+
+    // 1. Breadth-first collection.
+    int cur = 0, nf = 1, nc = 0;
+    bool overflow = false;
+    if (lane == 0)
+        sm.frontier[0][0] = 0;
+    __syncwarp();
+    while (nf > 0 && !overflow)
+    {
+        int nn = 0;
+        for (int base = 0; base < nf; base += 32)
+        {
+            int const idx  = base + lane;
+            int32_t node   = idx < nf ? sm.frontier[cur][idx] : -1;
+            bool pushNode  = false, pushLeaf = false;
+            int32_t a = -1, b = -1;
+            float d        = FLT_MAX;
+            if (node >= 0)
+            {
+                if (node < leafBegin)
+                {
+                    if (point_box_sqdist(p, T.ilo[node], T.ihi[node]) <= bound)
+                    {
+                        a        = T.child[2 * node];
+                        b        = T.child[2 * node + 1];
+                        pushNode = true;
+                    }
+                }
+                else
+                {
+                    int32_t const s = node - leafBegin;
+                    if (point_box_sqdist(p, T.llo[s], T.lhi[s]) <= bound)
+                    {
+                        int4 const t = M.F[T.inds[s]];
+                        d            = M.B[t.x] == body ? FLT_MAX
+                                                        : point_triangle_sqdist(p, f3(x[t.x]), f3(x[t.y]), f3(x[t.z]));
+                        pushLeaf = d <= bound;
+                        node     = s;
+                    }
+                }
+            }
+            unsigned const mNode = __ballot_sync(all, pushNode);
+            unsigned const mLeaf = __ballot_sync(all, pushLeaf);
+            unsigned const below = (1u << lane) - 1u;
+            int const slotN      = nn + 2 * __popc(mNode & below);
+            int const slotL      = nc + __popc(mLeaf & below);
+            if (pushNode && slotN + 1 < kNearestFrontier)
+            {
+                sm.frontier[cur ^ 1][slotN]     = a;
+                sm.frontier[cur ^ 1][slotN + 1] = b;
+            }
+            if (pushLeaf && slotL < kNearestCand)
+            {
+                sm.cand[slotL]  = node;
+                sm.candD[slotL] = d;
+            }
+            nn += 2 * __popc(mNode);
+            nc += __popc(mLeaf);
+            if (nn > kNearestFrontier || nc > kNearestCand)
+                overflow = true; // warp-uniform
+        }
+        __syncwarp();
+        cur ^= 1;
+        nf = nn;
+    }
+    if (overflow)
+    {
+        if (lane == 0)
+            nearest_serial<FINALIZE>(M, S, T, x, q);
+        return;
+    }
+
+    // 2. d* and the candidates that can matter.
+    float dstar = FLT_MAX;
+    for (int k = lane; k < nc; k += 32)
+        dstar = fminf(dstar, sm.candD[k]);
+    for (int off = 16; off > 0; off >>= 1)
+        dstar = fminf(dstar, __shfl_xor_sync(all, dstar, off));
+    int32_t list[kMaxContacts];
+    int count = 0;
+    if (dstar <= bound)
+    {
+        float const cap = dstar * (1.f + 16.f * eps) + 8.f * eps;
+        // Compact the kept candidates to the front (order does not matter yet).
+        int kept = 0;
+        for (int base = 0; base < nc; base += 32)
+        {
+            int const k      = base + lane;
+            bool const keep  = k < nc && sm.candD[k] <= cap;
+            int32_t const s  = keep ? sm.cand[k] : 0;
+            float const dk   = keep ? sm.candD[k] : 0.f;
+            unsigned const m = __ballot_sync(all, keep);
+            __syncwarp();
+            if (keep)
+            {
+                int const slot   = kept + __popc(m & ((1u << lane) - 1u));
+                sm.cand[slot]    = s;
+                sm.candD[slot]   = dk;
+            }
+            kept += __popc(m);
+            __syncwarp();
+        }
+        // 3. The reference's scan in decreasing leaf index: repeatedly take the largest remaining.
+        float dmin   = d0;
+        int32_t last = INT32_MAX;
+        for (int r = 0; r < kept; ++r)
+        {
+            int32_t bestS = -1;
+            float bestD   = 0.f;
+            for (int k = lane; k < kept; k += 32)
+            {
+                int32_t const s = sm.cand[k];
+                if (s < last && s > bestS)
+                {
+                    bestS = s;
+                    bestD = sm.candD[k];
+                }
+            }
+            for (int off = 16; off > 0; off >>= 1)
+            {
+                int32_t const os = __shfl_xor_sync(all, bestS, off);
+                float const od   = __shfl_xor_sync(all, bestD, off);
+                if (os > bestS)
+                {
+                    bestS = os;
+                    bestD = od;
+                }
+            }
+            last           = bestS;
+            float const lo = dmin - eps, hi = dmin + eps;
+            if (bestD < lo)
+            {
+                list[0] = T.inds[bestS];
+                count   = 1;
+                dmin    = bestD;
+            }
+            else if (bestD <= hi && count < kMaxContacts)
+                list[count++] = T.inds[bestS];
+        }
+    }
+    if (lane == 0)
+        nearest_write<FINALIZE>(M, S, x, v, i, p, list, count);
 }
 
 inline int blocks(int64_t n, int b)
@@ -346,7 +605,8 @@ cudaError_t contact_update(ContactMesh const& M, ContactState const& S, float4 c
         return e;
     if ((e = cudaMemsetAsync(S.nn, 0xFF, sizeof(int32_t) * size_t(M.nSurfV) * kMaxContacts, s)) != cudaSuccess)
         return e;
-    nearest_kernel<false><<<blocks(M.nSurfV, 128), 128, 0, s>>>(M, S, view_of(S.bvh, M.nF), x);
+    nearest_kernel<false><<<blocks(M.nSurfV, kNearestWarps), 32 * kNearestWarps, sizeof(NearestSmem) * kNearestWarps, s>>>(
+        M, S, view_of(S.bvh, M.nF), x);
     return cudaGetLastError();
 }
 
@@ -357,7 +617,8 @@ cudaError_t contact_finalize(ContactMesh const& M, ContactState const& S, float4
     cudaError_t e = refit(M, S, x, s);
     if (e != cudaSuccess)
         return e;
-    nearest_kernel<true><<<blocks(M.nSurfV, 128), 128, 0, s>>>(M, S, view_of(S.bvh, M.nF), x);
+    nearest_kernel<true><<<blocks(M.nSurfV, kNearestWarps), 32 * kNearestWarps, sizeof(NearestSmem) * kNearestWarps, s>>>(
+        M, S, view_of(S.bvh, M.nF), x);
     return cudaGetLastError();
 }
 

@@ -1595,10 +1595,12 @@ class VbdSystem
     struct TuneKey
     {
         int64_t nV, nT, nC, iters, sub;
-        bool cheb;
+        int32_t accel;
+        bool contact;
         bool operator==(TuneKey const& o) const
         {
-            return nV == o.nV && nT == o.nT && nC == o.nC && iters == o.iters && sub == o.sub && cheb == o.cheb;
+            return nV == o.nV && nT == o.nT && nC == o.nC && iters == o.iters && sub == o.sub && accel == o.accel &&
+                   contact == o.contact;
         }
     };
     struct TuneEntry
@@ -1623,7 +1625,7 @@ class VbdSystem
                 b <<= 1;
             return b;
         };
-        TuneKey const key{bucket(nV), bucket(nT), nColors, iterations, substeps, acceleration == PBGB_ACCEL_CHEBYSHEV};
+        TuneKey const key{bucket(nV), bucket(nT), nColors, iterations, substeps, acceleration, contact};
         {
             std::lock_guard<std::mutex> lock(cacheMutex);
             for (auto const& e : tuneCache())
@@ -1638,19 +1640,25 @@ class VbdSystem
                     return;
                 }
         }
-        // Snapshot the state the steps modify.
-        DeviceArray<float4> sx, sv, svp;
-        sx.allocate(nV);
-        sv.allocate(nV);
-        svp.allocate(nV);
-        size_t const bytes = sizeof(float4) * size_t(nV);
-        check(cudaMemcpyAsync(sx.get(), x.get(), bytes, cudaMemcpyDeviceToDevice, stream), "snapshot");
-        check(cudaMemcpyAsync(sv.get(), v.get(), bytes, cudaMemcpyDeviceToDevice, stream), "snapshot");
-        check(cudaMemcpyAsync(svp.get(), vprev.get(), bytes, cudaMemcpyDeviceToDevice, stream), "snapshot");
+        // Snapshot the state the steps modify (the checkpoint's parts: positions, velocities,
+        // external accelerations and, with contact, the active set and contact lists).
+        DeviceArray<unsigned char> snap;
+        snap.allocate(stateBytes());
+        {
+            size_t off = 0;
+            stateParts([&](void* dev, size_t n) {
+                if (dev && n > 0)
+                    check(cudaMemcpyAsync(snap.get() + off, dev, n, cudaMemcpyDeviceToDevice, stream), "snapshot");
+                off += n;
+            });
+        }
         auto restore = [&] {
-            check(cudaMemcpyAsync(x.get(), sx.get(), bytes, cudaMemcpyDeviceToDevice, stream), "restore");
-            check(cudaMemcpyAsync(v.get(), sv.get(), bytes, cudaMemcpyDeviceToDevice, stream), "restore");
-            check(cudaMemcpyAsync(vprev.get(), svp.get(), bytes, cudaMemcpyDeviceToDevice, stream), "restore");
+            size_t off = 0;
+            stateParts([&](void* dev, size_t n) {
+                if (dev && n > 0)
+                    check(cudaMemcpyAsync(dev, snap.get() + off, n, cudaMemcpyDeviceToDevice, stream), "restore");
+                off += n;
+            });
         };
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         check(cudaEventCreate(&e0), "cudaEventCreate");
