@@ -480,4 +480,117 @@ void orc_vertex_triangle_contact(double const* xtv, double const* xv, double con
     vertex_triangle_contact(at(xtv, 0), at(xv, 0), tf, f, dt, muC, muF, epsv, g, H, epsilon);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Discrete half of the CPU multibody mesh contact detector (sim/contact/MultibodyMeshMixedCcdDcd.h:
+// ForEachBodyPair 733-751, ForEachPenetratingVertex 754-803, HandleDcdPairs 805-845), an
+// independent check on the GPU path's active set and contact lists:
+//   * body pairs: bodies whose collision-vertex boxes overlap, both orders;
+//   * a collision vertex of body oi penetrates body oj when it lies in one of oj's tetrahedra
+//     (geometry/OverlapQueries.h:562-587: outside any face plane, d > 0, means outside; the
+//     boundary counts as inside); the first body found is kept (bodies in increasing order here;
+//     the reference takes its BVH's visit order, which matters only for a vertex inside two bodies);
+//   * each penetrating vertex reports the nearest surface triangles of the body it penetrates
+//     (AabbKdTreeHierarchy::NearestNeighbours with radius = max and eps = 0: exact ties only),
+//     at most 8, in triangle index order.
+// Brute force over tetrahedra and triangles with box prefilters: for test-sized scenes.
+// body[q] = penetrated body or -1; nearest[8 q ..] = triangles (-1 pad); d2[q] = their squared
+// distance (or -1).  The continuous half (vertex-triangle and edge-edge CCD) is not restated.
+int orc_dcd_contacts(
+    int32_t nV,
+    double const* x,
+    int32_t nT,
+    int32_t const* T,
+    int32_t nF,
+    int32_t const* F,
+    int32_t nCV,
+    int32_t const* V,
+    int32_t const* B,
+    int32_t* body,
+    int32_t* nearest,
+    double* d2)
+{
+    (void)nV;
+    int32_t nB = 0;
+    for (int32_t q = 0; q < nCV; ++q)
+        nB = std::max(nB, B[V[q]] + 1);
+    std::vector<V3> blo(static_cast<size_t>(nB), V3{1e300, 1e300, 1e300}), bhi(static_cast<size_t>(nB), V3{-1e300, -1e300, -1e300});
+    for (int32_t q = 0; q < nCV; ++q)
+    {
+        V3 const p = at(x, V[q]);
+        int32_t const b = B[V[q]];
+        blo[size_t(b)] = {std::min(blo[size_t(b)].x, p.x), std::min(blo[size_t(b)].y, p.y), std::min(blo[size_t(b)].z, p.z)};
+        bhi[size_t(b)] = {std::max(bhi[size_t(b)].x, p.x), std::max(bhi[size_t(b)].y, p.y), std::max(bhi[size_t(b)].z, p.z)};
+    }
+    auto overlap = [](V3 l1, V3 u1, V3 l2, V3 u2) {
+        return l1.x <= u2.x && l1.y <= u2.y && l1.z <= u2.z && l2.x <= u1.x && l2.y <= u1.y && l2.z <= u1.z;
+    };
+    // Tetrahedra and triangles per body, with their boxes.
+    std::vector<std::vector<int32_t>> tetsOf(static_cast<size_t>(nB)), trisOf(static_cast<size_t>(nB));
+    std::vector<V3> tlo(static_cast<size_t>(nT)), thi(static_cast<size_t>(nT));
+    for (int32_t e = 0; e < nT; ++e)
+    {
+        int32_t const* t = T + 4 * size_t(e);
+        if (B[t[0]] < nB)
+            tetsOf[size_t(B[t[0]])].push_back(e);
+        V3 l = at(x, t[0]), u = l;
+        for (int a = 1; a < 4; ++a)
+        {
+            V3 const p = at(x, t[a]);
+            l = {std::min(l.x, p.x), std::min(l.y, p.y), std::min(l.z, p.z)};
+            u = {std::max(u.x, p.x), std::max(u.y, p.y), std::max(u.z, p.z)};
+        }
+        tlo[size_t(e)] = l;
+        thi[size_t(e)] = u;
+    }
+    for (int32_t f = 0; f < nF; ++f)
+        if (B[F[3 * size_t(f)]] < nB)
+            trisOf[size_t(B[F[3 * size_t(f)]])].push_back(f);
+    auto outside = [](V3 p, V3 a, V3 b, V3 c) { return dot(sub(p, a), cross(sub(b, a), sub(c, a))) > 0; };
+    for (int32_t q = 0; q < nCV; ++q)
+    {
+        body[q] = -1;
+        d2[q]   = -1;
+        for (int k = 0; k < 8; ++k)
+            nearest[8 * size_t(q) + size_t(k)] = -1;
+        V3 const p     = at(x, V[q]);
+        int32_t const oi = B[V[q]];
+        for (int32_t oj = 0; oj < nB && body[q] < 0; ++oj)
+        {
+            if (oj == oi || !overlap(blo[size_t(oi)], bhi[size_t(oi)], blo[size_t(oj)], bhi[size_t(oj)]))
+                continue;
+            for (int32_t e : tetsOf[size_t(oj)])
+            {
+                if (!overlap(p, p, tlo[size_t(e)], thi[size_t(e)]))
+                    continue;
+                int32_t const* t = T + 4 * size_t(e);
+                V3 const A = at(x, t[0]), Bv = at(x, t[1]), Cv = at(x, t[2]), D = at(x, t[3]);
+                if (outside(p, A, Bv, D) || outside(p, Bv, Cv, D) || outside(p, Cv, A, D) || outside(p, A, Cv, Bv))
+                    continue;
+                body[q] = oj;
+                break;
+            }
+        }
+        if (body[q] < 0)
+            continue;
+        Real best = std::numeric_limits<Real>::max();
+        int count = 0;
+        for (int32_t f : trisOf[size_t(body[q])])
+        {
+            int32_t const* t = F + 3 * size_t(f);
+            Real const d = point_triangle_sqdist(p, at(x, t[0]), at(x, t[1]), at(x, t[2]));
+            if (d < best)
+            {
+                best  = d;
+                count = 0;
+            }
+            if (d == best && count < 8)
+                nearest[8 * size_t(q) + size_t(count++)] = f;
+        }
+        for (int k = count; k < 8; ++k)
+            nearest[8 * size_t(q) + size_t(k)] = -1;
+        d2[q] = best;
+    }
+    return 0;
+}
+
 } // extern "C"

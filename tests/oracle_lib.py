@@ -118,6 +118,9 @@ def lib():
                                       C.c_int32, C.c_int32, C.c_int32]
         L.orc_overlaps.restype = C.c_int64
         L.orc_overlaps.argtypes = [C.c_int32, _f32p, _f32p, C.c_int32, _f32p, _f32p, _i32p, C.c_int64]
+        L.orc_dcd_contacts.restype = C.c_int
+        L.orc_dcd_contacts.argtypes = [C.c_int32, _f64p, C.c_int32, _i32p, C.c_int32, _i32p, C.c_int32, _i32p,
+                                       _i32p, _i32p, _i32p, _f64p]
         _lib = L
     return _lib
 
@@ -408,3 +411,23 @@ def primal_graph(T, nV):
     ptr = np.zeros(nV + 1, np.int32)
     np.add.at(ptr, r + 1, 1)
     return np.cumsum(ptr).astype(np.int32), c.astype(np.int32)
+
+
+def dcd_contacts(x, T, F, V, B):
+    """Discrete half of the CPU multibody mesh detector (oracle/contact_oracle.cpp
+    orc_dcd_contacts): for each collision vertex V[q], the body it penetrates (-1: none), its
+    nearest surface triangles of that body (exact ties, -1 padded, 8 per vertex) and their squared
+    distance.  x (nV x 3), T (nT x 4), F (nF x 3), V (collision vertices), B (body per vertex)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.int32)
+    F = np.ascontiguousarray(F, dtype=np.int32)
+    V = np.ascontiguousarray(V, dtype=np.int32)
+    B = np.ascontiguousarray(B, dtype=np.int32)
+    n = V.size
+    body = np.empty(n, np.int32)
+    nearest = np.empty((n, 8), np.int32)
+    d2 = np.empty(n, np.float64)
+    rc = lib().orc_dcd_contacts(x.shape[0], x, T.shape[0], T, F.shape[0], F, n, V, B, body, nearest, d2)
+    if rc != 0:
+        raise RuntimeError("orc_dcd_contacts failed")
+    return body, nearest, d2

@@ -83,3 +83,62 @@ def test_oracle_contact_step_keeps_cubes_above_slab():
     assert min(zs) > -0.02  # and was stopped by it
     assert abs(zs[-1] - zs[-2]) < 2e-3  # coming to rest
     assert O_.active.sum() > 0
+
+
+def _point_in_tets(p, X, T):
+    """Brute-force PointTetrahedron3D (geometry/OverlapQueries.h:562-587) of points p against every
+    tet: inside unless strictly outside one of the faces (A,B,D), (B,C,D), (C,A,D), (A,C,B)."""
+    A, B, Cc, D = (X[T[:, k]] for k in range(4))
+    inside = np.ones((p.shape[0], T.shape[0]), bool)
+    for a, b, c in ((A, B, D), (B, Cc, D), (Cc, A, D), (A, Cc, B)):
+        nrm = np.cross(b - a, c - a)
+        side = np.einsum("ptk,tk->pt", p[:, None, :] - a[None], nrm)
+        inside &= side <= 0.0
+    return inside
+
+
+def test_multibody_dcd_oracle_matches_brute_force():
+    """The CPU multibody detector's discrete half on a cube sunk 5 cm into a slab: penetrating
+    vertices in both directions, and each one's nearest surface triangles of the body it
+    penetrates, against brute force."""
+    w = meshgen.contact_scene_workload(n_cubes_side=1, cube_hexes=4, slab_hexes=(8, 8, 1), cell=1.0)
+    X, T, F, V, B = w["X"].copy(), w["T"], w["F"], w["V"], w["B"]
+    X[B == 1, 2] -= 0.05 + 0.05  # the cube's bottom 5 cm below the slab's top
+    body, nearest, d2 = O.dcd_contacts(X, T, F, V, B)
+    p = X[V]
+    for q_body in (0, 1):
+        other = 1 - q_body
+        qs = np.nonzero(B[V] == q_body)[0]
+        inside = _point_in_tets(p[qs], X, T[B[T[:, 0]] == other]).any(axis=1)
+        np.testing.assert_array_equal(body[qs] >= 0, inside)
+        assert inside.sum() > 0
+        assert (body[qs][inside] == other).all()
+    # Nearest triangles of the penetrated body: squared distances against brute force.
+    pen = np.nonzero(body >= 0)[0]
+    for q in pen:
+        tris = np.nonzero(B[F[:, 0]] == body[q])[0]
+        a, b, c = (X[F[tris, k]] for k in range(3))
+        dist = np.array([O_point_triangle(p[q], a[j], b[j], c[j]) for j in range(len(tris))])
+        assert abs(d2[q] - dist.min()) <= 1e-12
+        listed = nearest[q][nearest[q] >= 0]
+        assert len(listed) >= 1 and set(listed) <= set(tris[np.abs(dist - dist.min()) <= 0.0])
+
+
+def O_point_triangle(p, a, b, c):
+    """Squared point-triangle distance by dense sampling-free projection (barycentric clamp over the
+    face, then the three edges)."""
+    ab, ac = b - a, c - a
+    M = np.array([[ab @ ab, ab @ ac], [ab @ ac, ac @ ac]])
+    rhs = np.array([ab @ (p - a), ac @ (p - a)])
+    u, v = np.linalg.solve(M, rhs)
+    if u >= 0 and v >= 0 and u + v <= 1:
+        q = a + u * ab + v * ac
+        return float((p - q) @ (p - q))
+
+    def seg(p, s0, s1):
+        d = s1 - s0
+        t = np.clip((p - s0) @ d / (d @ d), 0.0, 1.0)
+        r = p - (s0 + t * d)
+        return float(r @ r)
+
+    return min(seg(p, a, b), seg(p, b, c), seg(p, c, a))

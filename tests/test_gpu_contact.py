@@ -154,3 +154,51 @@ def test_staged_sweep_equals_gathering_sweep_with_contact():
     fb, ab = B.contacts()
     np.testing.assert_array_equal(fa, fb)
     np.testing.assert_array_equal(aa, ab)
+
+
+def test_active_set_agrees_with_cpu_multibody_detector():
+    """The GPU path's active set against the discrete half of the CPU multibody mesh detector
+    (sim/contact/MultibodyMeshMixedCcdDcd.h, restated in oracle/contact_oracle.cpp), an independent
+    algorithm: a 4x4x4-hex cube moved from 5 cm above a slab to 5 cm inside it.  After initialize,
+    update and finalize, a collision vertex is active on the device exactly when the CPU detector
+    finds it inside a tetrahedron of the other body, and the device's nearest listed triangle is at
+    the CPU's nearest squared distance (FP32 tolerance)."""
+    w = meshgen.contact_scene_workload(n_cubes_side=1, cube_hexes=4, slab_hexes=(8, 8, 1), cell=1.0)
+    XT, T, F, V, B = w["X"].copy(), w["T"], w["F"], w["V"], w["B"]
+    X = XT.copy()
+    X[B == 1, 2] -= 0.1  # the cube's bottom from 5 cm above the slab's top to 5 cm below it
+    body, nearest, d2 = O.dcd_contacts(X, T, F, V, B)
+    c = Ccd(X.shape[0], V, F, B)
+    lo, hi = np.minimum(XT.min(0), X.min(0)), np.maximum(XT.max(0), X.max(0))
+    c.call("pbgb_ccd_initialize", XT, X, lo, hi)
+    c.call("pbgb_ccd_update", X)
+    c.call("pbgb_ccd_finalize", X)
+    active, nn, dup, na = c.get()
+    pen = body >= 0
+    assert pen.sum() > 20
+    np.testing.assert_array_equal(active.astype(bool), pen)
+    Xf = X.astype(np.float32).astype(np.float64)
+    for q in np.nonzero(pen)[0]:
+        f = nn[q][nn[q] >= 0]
+        assert len(f) >= 1
+        assert (B[F[f, 0]] == body[q]).all()
+        p = Xf[V[q]]
+        d = min(_sqdist(p, *Xf[F[g]]) for g in f)
+        assert abs(d - d2[q]) <= 1e-6 * max(1.0, d2[q]) + 1e-9
+
+
+def _sqdist(p, a, b, c):
+    ab, ac = b - a, c - a
+    M = np.array([[ab @ ab, ab @ ac], [ab @ ac, ac @ ac]])
+    u, v = np.linalg.solve(M, np.array([ab @ (p - a), ac @ (p - a)]))
+    if u >= 0 and v >= 0 and u + v <= 1:
+        r = p - (a + u * ab + v * ac)
+        return float(r @ r)
+
+    def seg(s0, s1):
+        d = s1 - s0
+        t = np.clip((p - s0) @ d / (d @ d), 0.0, 1.0)
+        r = p - (s0 + t * d)
+        return float(r @ r)
+
+    return min(seg(a, b), seg(b, c), seg(c, a))
