@@ -23,45 +23,74 @@ __device__ __forceinline__ uint32_t corner(uint4 const& t, int a)
     return a == 0 ? t.x : (a == 1 ? t.y : (a == 2 ? t.z : t.w));
 }
 
-// Contact energy of vertex i (gpu/impl/vbd/Kernels.cuh:80-114,203-223): the contact penalty is
-// scaled by the vertex area over the summed areas of the vertex's contact triangles, and every
-// listed triangle adds its normal penalty and friction (vertex_triangle_contact).
-__device__ __noinline__ void add_contacts(SweepParams const& p, int i, float const* xt, float const* xi, float* H, float* g)
+// Contact terms of one vertex-triangle pair (gpu/impl/vbd/Kernels.cuh:80-114,203-223): the
+// triangle's corners at t and now (from x if their colour is solved before this one, else from
+// hprev), then the normal penalty and friction of vertex_triangle_contact with penalty kCf.
+__device__ __noinline__ void contact_pair(SweepParams const& p, int32_t f, float kCf, float const* xt, float const* xi, float* H, float* g)
 {
-    int32_t f[kMaxContactsPerVertex];
-    int n = 0;
-#pragma unroll
-    for (int c = 0; c < kMaxContactsPerVertex; ++c)
+    int4 const t   = p.F[f];
+    int const v[3] = {t.x, t.y, t.z};
+    float xtf[3][3], xf[3][3];
+    for (int k = 0; k < 3; ++k)
     {
-        f[c] = p.fc[i * kMaxContactsPerVertex + c];
-        n += f[c] >= 0 ? 1 : 0;
+        float4 const a = p.xt[v[k]];
+        float4 const b = __ldcg((p.vcolor[v[k]] < p.color ? p.x : p.hprev) + v[k]);
+        xtf[k][0] = a.x, xtf[k][1] = a.y, xtf[k][2] = a.z;
+        xf[k][0] = b.x, xf[k][1] = b.y, xf[k][2] = b.z;
     }
-    if (n == 0)
-        return;
+    vertex_triangle_contact(xt, xi, xtf, xf, p.h, kCf, p.muF, p.epsv, FLT_EPSILON, g, H);
+}
+
+// Contact energy of vertex i, spread over the vertex's L lanes: lane l takes the listed triangles
+// l, l + L, ... (at most kMaxContactsPerVertex), the penalty is scaled by the vertex area over the
+// summed areas of the listed triangles, and the lanes' gradients and Hessians are summed with xor
+// shuffles inside the group (every lane of the warp takes part in the shuffles).  cH, cg: the
+// group's sum, in every lane.
+template <int L>
+__device__ __forceinline__ void contact_terms(SweepParams const& p, bool valid, int lane, int i, float const* xt, float const* xi, float* cH, float* cg)
+{
+    int32_t f[(kMaxContactsPerVertex + L - 1) / L];
+    float fa[(kMaxContactsPerVertex + L - 1) / L];
     float sumfa = 0.f;
-    for (int c = 0; c < n; ++c)
-        sumfa += p.FA[f[c]];
-    float const kC = (p.XVA[i] * p.muC) / sumfa;
-    for (int c = 0; c < n; ++c)
+#pragma unroll
+    for (int c = 0; c < (kMaxContactsPerVertex + L - 1) / L; ++c)
     {
-        int4 const t   = p.F[f[c]];
-        int const v[3] = {t.x, t.y, t.z};
-        float xtf[3][3], xf[3][3];
-        for (int k = 0; k < 3; ++k)
-        {
-            float4 const a = p.xt[v[k]];
-            float4 const b = __ldcg((p.vcolor[v[k]] < p.color ? p.x : p.hprev) + v[k]);
-            xtf[k][0] = a.x, xtf[k][1] = a.y, xtf[k][2] = a.z;
-            xf[k][0] = b.x, xf[k][1] = b.y, xf[k][2] = b.z;
-        }
-        vertex_triangle_contact(xt, xi, xtf, xf, p.h, kC * p.FA[f[c]], p.muF, p.epsv, FLT_EPSILON, g, H);
+        int const k = lane + c * L;
+        f[c]        = valid && k < kMaxContactsPerVertex ? p.fc[i * kMaxContactsPerVertex + k] : -1;
+        fa[c]       = f[c] >= 0 ? p.FA[f[c]] : 0.f;
+        sumfa += fa[c];
+    }
+#pragma unroll
+    for (int off = L / 2; off > 0; off >>= 1)
+        sumfa += __shfl_xor_sync(0xffffffffu, sumfa, off);
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+        cH[r] = 0.f;
+    cg[0] = cg[1] = cg[2] = 0.f;
+    if (sumfa > 0.f)
+    {
+        float const kC = (p.XVA[i] * p.muC) / sumfa;
+#pragma unroll
+        for (int c = 0; c < (kMaxContactsPerVertex + L - 1) / L; ++c)
+            if (f[c] >= 0)
+                contact_pair(p, f[c], kC * fa[c], xt, xi, cH, cg);
+    }
+#pragma unroll
+    for (int off = L / 2; off > 0; off >>= 1)
+    {
+#pragma unroll
+        for (int r = 0; r < 6; ++r)
+            cH[r] += __shfl_xor_sync(0xffffffffu, cH[r], off);
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            cg[r] += __shfl_xor_sync(0xffffffffu, cg[r], off);
     }
 }
 
 // The end of a vertex solve, shared by both sweep kernels: xor-shuffle reduction of the lanes'
 // 10 accumulated floats, then lane 0 applies damping, contact, inertia and the 3x3 Newton step and
 // writes the iterate(s).
-template <int L, bool CHEB, bool REC>
+template <int L, bool CHEB, bool REC, bool CONTACT>
 __device__ __forceinline__ void finish_vertex(SweepParams const& p, VertexBlock<float>& b, bool valid, int lane, int i, int s, float* xi)
 {
 #pragma unroll
@@ -75,16 +104,27 @@ __device__ __forceinline__ void finish_vertex(SweepParams const& p, VertexBlock<
         for (int r = 0; r < 6; ++r)
             b.C[r] += __shfl_xor_sync(0xffffffffu, b.C[r], off);
     }
+    float4 const xt4  = p.xt[i];
+    float const xt[3] = {xt4.x, xt4.y, xt4.z};
+    float cH[6], cg[3];
+    bool constexpr contact = CHEB && CONTACT;
+    if constexpr (contact)
+        contact_terms<L>(p, valid, lane, i, xt, xi, cH, cg);
     if (!valid || lane != 0)
         return;
-    float4 const xt4  = p.xt[i];
     float4 const xl4  = p.xtilde[i];
-    float const xt[3] = {xt4.x, xt4.y, xt4.z};
     float const xl[3] = {xl4.x, xl4.y, xl4.z};
     float H[6], g[3];
     elastic_system(b, xt, xi, p.h, p.kD, H, g);
-    if (CHEB && p.fc)
-        add_contacts(p, i, xt, xi, H, g);
+    if constexpr (contact)
+    {
+#pragma unroll
+        for (int r = 0; r < 6; ++r)
+            H[r] += cH[r];
+        g[0] += cg[0];
+        g[1] += cg[1];
+        g[2] += cg[2];
+    }
     float dx[3];
     bool const moved = inertia_solve(H, g, xl, xt4.w, p.h2, p.detHZero, xi, static_cast<float*>(nullptr),
                                      static_cast<float*>(nullptr), dx);
@@ -141,7 +181,7 @@ __device__ __forceinline__ void finish_vertex(SweepParams const& p, VertexBlock<
 //
 // REC (without CHEB): also writes the inverse Newton matrix of every solved vertex to p.tape for
 // the adjoint sweep.
-template <int L, bool CHEB, bool REC = false>
+template <int L, bool CHEB, bool REC = false, bool CONTACT = false>
 __global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
 {
     int const tid    = blockIdx.x * blockDim.x + threadIdx.x;
@@ -222,7 +262,7 @@ __global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
             mat = matn;
         }
     }
-    finish_vertex<L, CHEB, REC>(p, b, valid, lane, i, s, xi);
+    finish_vertex<L, CHEB, REC, CONTACT>(p, b, valid, lane, i, s, xi);
 }
 
 // The same sweep with each vertex's neighbours staged in shared memory.  A vertex's ~23 incident
@@ -234,7 +274,7 @@ __global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
 // entry of the block]; positions and rest positions are two arrays of p.slab float4 each (a 16-byte
 // stride spreads random slots over all shared-memory banks); the lanes of a vertex share a warp,
 // so __syncwarp orders the staging.
-template <int L, bool CHEB, bool REC = false>
+template <int L, bool CHEB, bool REC = false, bool CONTACT = false>
 __global__ void __launch_bounds__(256, 4) staged_sweep_kernel(SweepParams p)
 {
     extern __shared__ float4 slab[]; // positions [0, p.slab), rest positions [p.slab, 2 p.slab)
@@ -319,7 +359,7 @@ __global__ void __launch_bounds__(256, 4) staged_sweep_kernel(SweepParams p)
             mat = matn;
         }
     }
-    finish_vertex<L, CHEB, REC>(p, b, valid, lane, i, s, xi);
+    finish_vertex<L, CHEB, REC, CONTACT>(p, b, valid, lane, i, s, xi);
 }
 
 // Start of a substep (sim/vbd/Integrator.cpp:31-34,54-71; gpu/impl/vbd/Integrator.cu:190-248):
@@ -473,7 +513,7 @@ inline int blocks_for(int64_t n, int block)
 
 } // namespace
 
-template <int L, bool CHEB, bool REC = false>
+template <int L, bool CHEB, bool REC = false, bool CONTACT = false>
 cudaError_t launch_sweep_l(SweepParams const& p, int g, int block, bool pdl, cudaStream_t s, size_t stagedBytes)
 {
     cudaLaunchConfig_t cfg = {};
@@ -487,21 +527,21 @@ cudaError_t launch_sweep_l(SweepParams const& p, int g, int block, bool pdl, cud
     cfg.attrs                                          = attr;
     cfg.numAttrs                                       = pdl ? 1 : 0;
     if (stagedBytes > 0)
-        return cudaLaunchKernelEx(&cfg, staged_sweep_kernel<L, CHEB, REC>, p);
-    return cudaLaunchKernelEx(&cfg, sweep_kernel<L, CHEB, REC>, p);
+        return cudaLaunchKernelEx(&cfg, staged_sweep_kernel<L, CHEB, REC, CONTACT>, p);
+    return cudaLaunchKernelEx(&cfg, sweep_kernel<L, CHEB, REC, CONTACT>, p);
 }
 
-template <bool CHEB, bool REC>
+template <bool CHEB, bool REC, bool CONTACT = false>
 cudaError_t launch_sweep_t(SweepParams const& p, int lanes, int g, int block, bool pdl, cudaStream_t s, size_t stagedBytes)
 {
     switch (lanes)
     {
-        case 1: return launch_sweep_l<1, CHEB, REC>(p, g, block, pdl, s, stagedBytes);
-        case 2: return launch_sweep_l<2, CHEB, REC>(p, g, block, pdl, s, stagedBytes);
-        case 4: return launch_sweep_l<4, CHEB, REC>(p, g, block, pdl, s, stagedBytes);
-        case 8: return launch_sweep_l<8, CHEB, REC>(p, g, block, pdl, s, stagedBytes);
-        case 16: return launch_sweep_l<16, CHEB, REC>(p, g, block, pdl, s, stagedBytes);
-        case 32: return launch_sweep_l<32, CHEB, REC>(p, g, block, pdl, s, stagedBytes);
+        case 1: return launch_sweep_l<1, CHEB, REC, CONTACT>(p, g, block, pdl, s, stagedBytes);
+        case 2: return launch_sweep_l<2, CHEB, REC, CONTACT>(p, g, block, pdl, s, stagedBytes);
+        case 4: return launch_sweep_l<4, CHEB, REC, CONTACT>(p, g, block, pdl, s, stagedBytes);
+        case 8: return launch_sweep_l<8, CHEB, REC, CONTACT>(p, g, block, pdl, s, stagedBytes);
+        case 16: return launch_sweep_l<16, CHEB, REC, CONTACT>(p, g, block, pdl, s, stagedBytes);
+        case 32: return launch_sweep_l<32, CHEB, REC, CONTACT>(p, g, block, pdl, s, stagedBytes);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -516,6 +556,8 @@ cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebys
     int const g   = blocks_for(n, block);
     SweepParams q = p;
     q.slab        = int32_t(stagedBytes / (2 * sizeof(float4)));
+    if (chebyshev && q.fc)
+        return launch_sweep_t<true, false, true>(q, lanes, g, block, pdl, s, stagedBytes);
     return chebyshev ? launch_sweep_t<true, false>(q, lanes, g, block, pdl, s, stagedBytes)
                      : launch_sweep_t<false, false>(q, lanes, g, block, pdl, s, stagedBytes);
 }
@@ -548,7 +590,7 @@ size_t staged_sweep_bytes(int32_t const* nbrPtr, int32_t begin, int32_t end, int
 
 namespace {
 
-template <bool CHEB, bool REC>
+template <bool CHEB, bool REC, bool CONTACT = false>
 cudaError_t allow_staged_smem()
 {
     cudaError_t e = cudaSuccess;
@@ -556,12 +598,12 @@ cudaError_t allow_staged_smem()
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kStagedMaxBytes));
     };
-    set(staged_sweep_kernel<1, CHEB, REC>);
-    set(staged_sweep_kernel<2, CHEB, REC>);
-    set(staged_sweep_kernel<4, CHEB, REC>);
-    set(staged_sweep_kernel<8, CHEB, REC>);
-    set(staged_sweep_kernel<16, CHEB, REC>);
-    set(staged_sweep_kernel<32, CHEB, REC>);
+    set(staged_sweep_kernel<1, CHEB, REC, CONTACT>);
+    set(staged_sweep_kernel<2, CHEB, REC, CONTACT>);
+    set(staged_sweep_kernel<4, CHEB, REC, CONTACT>);
+    set(staged_sweep_kernel<8, CHEB, REC, CONTACT>);
+    set(staged_sweep_kernel<16, CHEB, REC, CONTACT>);
+    set(staged_sweep_kernel<32, CHEB, REC, CONTACT>);
     return e;
 }
 
@@ -574,6 +616,8 @@ cudaError_t prepare_staged_sweeps()
         e = allow_staged_smem<true, false>();
     if (e == cudaSuccess)
         e = allow_staged_smem<false, true>();
+    if (e == cudaSuccess)
+        e = allow_staged_smem<true, false, true>();
     return e;
 }
 
