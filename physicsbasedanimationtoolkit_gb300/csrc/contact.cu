@@ -141,13 +141,34 @@ __global__ void triangle_boxes_kernel(ContactMesh M, float4 const* __restrict__ 
     hi[f] = make_float4(u.x, u.y, u.z, 0.f);
 }
 
-// Swept vertex box vs the swept-triangle BVH (gpu/impl/contact/VertexTriangleMixedCcdDcd.cu:103-
-// 136): triangles of another body activate the vertex and bound its search radius.
-__global__ void initialize_kernel(ContactMesh M, ContactState S, BvhView T, float4 const* __restrict__ xt, float4 const* __restrict__ xn)
+// Squared diagonal of the joint box of vertex i and triangle t over both position sets (the
+// reference's nearest-neighbour search radius for the pair).
+__device__ __forceinline__ float joint_box_sqdiag(int i, int4 const& t, float4 const* __restrict__ xt, float4 const* __restrict__ xn)
 {
-    int const q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= M.nSurfV || T.n < 1)
-        return;
+    int const c[3] = {t.x, t.y, t.z};
+    float4 lo = xt[i], hi = xt[i];
+    float4 pts[8];
+    pts[0] = xt[i];
+    pts[1] = xn[i];
+    for (int k = 0; k < 3; ++k)
+    {
+        pts[2 + k] = xt[c[k]];
+        pts[5 + k] = xn[c[k]];
+    }
+    for (int k = 0; k < 8; ++k)
+    {
+        lo = make_float4(fminf(lo.x, pts[k].x), fminf(lo.y, pts[k].y), fminf(lo.z, pts[k].z), 0.f);
+        hi = make_float4(fmaxf(hi.x, pts[k].x), fmaxf(hi.y, pts[k].y), fmaxf(hi.z, pts[k].z), 0.f);
+    }
+    float const dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// Swept vertex box vs the swept-triangle BVH (gpu/impl/contact/VertexTriangleMixedCcdDcd.cu:103-
+// 136): triangles of another body activate the vertex and bound its search radius.  One thread's
+// depth-first traversal (the fallback of initialize_kernel).
+__device__ void initialize_serial(ContactMesh const& M, ContactState const& S, BvhView const& T, float4 const* __restrict__ xt, float4 const* __restrict__ xn, int q)
+{
     int const i     = M.V[q];
     float4 const L = S.vlo[q], U = S.vhi[q];
     int32_t const leafBegin = T.n - 1;
@@ -168,25 +189,8 @@ __global__ void initialize_kernel(ContactMesh M, ContactState S, BvhView T, floa
             int4 const t    = M.F[f];
             if (M.B[i] == M.B[t.x])
                 continue;
-            int const c[3] = {t.x, t.y, t.z};
-            float4 lo = xt[i], hi = xt[i];
-            float4 pts[8];
-            pts[0] = xt[i];
-            pts[1] = xn[i];
-            for (int k = 0; k < 3; ++k)
-            {
-                pts[2 + k] = xt[c[k]];
-                pts[5 + k] = xn[c[k]];
-            }
-            for (int k = 0; k < 8; ++k)
-            {
-                lo = make_float4(fminf(lo.x, pts[k].x), fminf(lo.y, pts[k].y), fminf(lo.z, pts[k].z), 0.f);
-                hi = make_float4(fmaxf(hi.x, pts[k].x), fmaxf(hi.y, pts[k].y), fmaxf(hi.z, pts[k].z), 0.f);
-            }
-            float const dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
-            float const d2 = dx * dx + dy * dy + dz * dz;
-            best           = fmaxf(best, d2);
-            hit            = true;
+            best = fmaxf(best, joint_box_sqdiag(i, t, xt, xn));
+            hit  = true;
         }
         else if (boxes_overlap(L, U, T.ilo[node], T.ihi[node]))
         {
@@ -200,6 +204,98 @@ __global__ void initialize_kernel(ContactMesh M, ContactState S, BvhView T, floa
         }
     }
     if (hit)
+    {
+        S.dupper[q] = best;
+        S.active[q] = 1;
+    }
+}
+
+int constexpr kInitWarps    = 4;   // warps (vertices) per block
+int constexpr kInitFrontier = 512; // breadth-first frontier capacity per warp
+
+// Warp-cooperative form of the same overlap query, one warp per collision vertex: the levels of
+// the hierarchy are expanded breadth first across the lanes (the result, a maximum over the
+// overlapping triangles of other bodies, does not depend on the visit order), so a vertex in a
+// dense contact patch costs about the tree's depth in dependent loads instead of one thread's
+// whole traversal.  A frontier overflow hands the vertex to lane 0's depth-first traversal.
+__global__ void __launch_bounds__(32 * kInitWarps) initialize_kernel(ContactMesh M, ContactState S, BvhView T, float4 const* __restrict__ xt, float4 const* __restrict__ xn)
+{
+    __shared__ int32_t frontier[kInitWarps][2][kInitFrontier];
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int const q    = blockIdx.x * kInitWarps + warp;
+    if (q >= M.nSurfV || T.n < 1)
+        return;
+    unsigned const all = 0xffffffffu;
+    int const i        = M.V[q];
+    int const body     = M.B[i];
+    float4 const L = S.vlo[q], U = S.vhi[q];
+    int32_t const leafBegin = T.n - 1;
+    int cur = 0, nf = 1;
+    bool overflow = false;
+    float best    = 0.f;
+    bool hit      = false;
+    if (lane == 0)
+        frontier[warp][0][0] = 0;
+    __syncwarp();
+    while (nf > 0 && !overflow)
+    {
+        int nn = 0;
+        for (int base = 0; base < nf; base += 32)
+        {
+            int const idx = base + lane;
+            int32_t const node = idx < nf ? frontier[warp][cur][idx] : -1;
+            bool push = false;
+            int32_t a = -1, b = -1;
+            if (node >= 0)
+            {
+                if (node < leafBegin)
+                {
+                    if (boxes_overlap(L, U, T.ilo[node], T.ihi[node]))
+                    {
+                        a    = T.child[2 * node];
+                        b    = T.child[2 * node + 1];
+                        push = true;
+                    }
+                }
+                else
+                {
+                    int32_t const s = node - leafBegin;
+                    if (boxes_overlap(L, U, T.llo[s], T.lhi[s]))
+                    {
+                        int4 const t = M.F[T.inds[s]];
+                        if (M.B[t.x] != body)
+                        {
+                            best = fmaxf(best, joint_box_sqdiag(i, t, xt, xn));
+                            hit  = true;
+                        }
+                    }
+                }
+            }
+            unsigned const m = __ballot_sync(all, push);
+            int const slot   = nn + 2 * __popc(m & ((1u << lane) - 1u));
+            if (push && slot + 1 < kInitFrontier)
+            {
+                frontier[warp][cur ^ 1][slot]     = a;
+                frontier[warp][cur ^ 1][slot + 1] = b;
+            }
+            nn += 2 * __popc(m);
+            if (nn > kInitFrontier)
+                overflow = true; // warp-uniform
+        }
+        __syncwarp();
+        cur ^= 1;
+        nf = nn;
+    }
+    if (overflow)
+    {
+        if (lane == 0)
+            initialize_serial(M, S, T, xt, xn, q);
+        return;
+    }
+    for (int off = 16; off > 0; off >>= 1)
+        best = fmaxf(best, __shfl_xor_sync(all, best, off));
+    bool const any = __any_sync(all, hit);
+    if (lane == 0 && any)
     {
         S.dupper[q] = best;
         S.active[q] = 1;
@@ -587,7 +683,7 @@ cudaError_t contact_initialize(ContactMesh const& M, ContactState const& S, floa
         return e;
     if ((e = bvh_build(S.bvh, M.nF, S.tlo, S.thi, wmin, wmax, s)) != cudaSuccess)
         return e;
-    initialize_kernel<<<blocks(M.nSurfV, 128), 128, 0, s>>>(M, S, view_of(S.bvh, M.nF), xt, xnext);
+    initialize_kernel<<<blocks(M.nSurfV, kInitWarps), 32 * kInitWarps, 0, s>>>(M, S, view_of(S.bvh, M.nF), xt, xnext);
     if ((e = cudaGetLastError()) != cudaSuccess)
         return e;
     if ((e = cudaMemsetAsync(S.nActive, 0, sizeof(int32_t), s)) != cudaSuccess)
