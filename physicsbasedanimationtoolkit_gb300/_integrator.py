@@ -47,7 +47,9 @@ def make_desc(data, semantics):
     d = _capi.VbdDesc()
     d.n_vertices = nV
     d.n_tets = nT
-    if getattr(data, "F", None) is not None and np.asarray(data.F).size > 0:
+    # The reference's CPU integrator has no contact terms (sim/vbd/Integrator.cpp:98-136): with its
+    # semantics a surface mesh only describes the boundary; the GPU integrator adds contact.
+    if semantics == SEMANTICS_GPU and getattr(data, "F", None) is not None and np.asarray(data.F).size > 0:
         keep.update(
             V=_capi.i32(data.V),
             F=_capi.i32(np.asarray(data.F).T),

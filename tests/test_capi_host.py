@@ -143,13 +143,39 @@ def test_integrator_creation_without_device_fails_loudly():
     assert e.value.code == 6
 
 
-def test_broyden_needs_a_single_mesh_without_contact():
+def _desc_with_contact(accel):
+    """A GPU-semantics descriptor of the 5-tet cube with its surface mesh, acceleration forced."""
+    from physicsbasedanimationtoolkit_gb300 import _integrator as I
+
     P, T, V, F = meshgen.cube5()
-    d = (pbat.sim.vbd.Data().with_volume_mesh(P, T).with_surface_mesh(V, F)
-         .with_broyden_acceleration(5).construct())
-    with pytest.raises(_capi.PbgbError) as e:
-        pbat.sim.vbd.Integrator(d)
-    assert e.value.code == 1 and "Broyden" in str(e.value)
+    d = pbat.sim.vbd.Data().with_volume_mesh(P, T).with_surface_mesh(V, F).construct()
+    desc, keep = I.make_desc(d, I.SEMANTICS_GPU)
+    assert desc.n_collision_triangles > 0
+    desc.acceleration = accel
+    return desc, keep
+
+
+@pytest.mark.parametrize("accel,name", [(2, "Anderson"), (3, "Nesterov"), (4, "Broyden"), (5, "trust-region")])
+def test_window_and_nesterov_accelerations_need_a_single_mesh_without_contact(accel, name):
+    desc, keep = _desc_with_contact(accel)
+    desc.tr_tau = 2.0
+    desc.nesterov_lipschitz = 1.0
+    desc.window_size = 5
+    h = C.c_void_p()
+    rc = _capi.lib().pbgb_vbd_create(C.byref(desc), C.byref(h))
+    assert rc == 1
+    assert name in _capi.lib().pbgb_last_error(None).decode()
+
+
+def test_cpu_integrator_has_no_contact():
+    """sim/vbd/Integrator.cpp:98-136 has no contact terms: with CPU semantics the surface mesh
+    does not turn contact on; with GPU semantics it does."""
+    from physicsbasedanimationtoolkit_gb300 import _integrator as I
+
+    P, T, V, F = meshgen.cube5()
+    d = pbat.sim.vbd.Data().with_volume_mesh(P, T).with_surface_mesh(V, F).with_broyden_acceleration(5).construct()
+    assert I.make_desc(d, I.SEMANTICS_CPU)[0].n_collision_triangles == 0
+    assert I.make_desc(d, I.SEMANTICS_GPU)[0].n_collision_triangles > 0
 
 
 @pytest.mark.parametrize("accel,cpu,gpu", [("none", 0, 0), ("chebyshev", 1, 1), ("anderson", 2, 2),
@@ -235,13 +261,8 @@ def test_descriptor_errors_are_reported_without_a_device(defect):
     assert expect in str(e.value)
 
 
-def test_nesterov_needs_a_single_mesh_without_contact():
-    P, T, V, F = meshgen.cube5()
-    d = (pbat.sim.vbd.Data().with_volume_mesh(P, T).with_surface_mesh(V, F)
-         .with_nesterov_acceleration(1.0, 3).construct())
-    with pytest.raises(_capi.PbgbError) as e:
-        pbat.sim.vbd.Integrator(d)
-    assert e.value.code == 1 and "Nesterov" in str(e.value)
+def test_nesterov_settings_are_validated():
+    P, T, _, _ = meshgen.cube5()
     with pytest.raises(ValueError):
         pbat.sim.vbd.Data().with_volume_mesh(P, T).with_nesterov_acceleration(0.0, 3).construct()
     with pytest.raises(ValueError):
