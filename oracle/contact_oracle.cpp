@@ -31,6 +31,7 @@
 #include <omp.h>
 #endif
 
+#include "orc_accel.h"
 #include "orc_problem.h"
 
 namespace {
@@ -85,14 +86,15 @@ Real point_triangle_sqdist(V3 p, V3 a, V3 b, V3 c)
     return dot(d, d);
 }
 
-// sim/vbd/Kernels.h:215-302 (energy not needed): adds to g and H (column-major 3x3).
-void vertex_triangle_contact(V3 xtv, V3 xv, V3 const* xtf, V3 const* xf, Real dt, Real muC, Real muF, Real epsv, Real* g, Real* H, Real epsilon = Real(FLT_EPSILON))
+// sim/vbd/Kernels.h:215-302: adds to g and H (column-major 3x3) and returns the energy (normal
+// penalty 1/2 lambda d and IPC friction muF |lambda| f0(|u|), f0 as the reference writes it).
+Real vertex_triangle_contact(V3 xtv, V3 xv, V3 const* xtf, V3 const* xf, Real dt, Real muC, Real muF, Real epsv, Real* g, Real* H, Real epsilon = Real(FLT_EPSILON))
 {
     V3 e0 = sub(xf[1], xf[0]), e1 = sub(xf[2], xf[0]);
     V3 n  = cross(e0, e1);
     Real const dbl = std::sqrt(dot(n, n));
     if (dbl <= 1e-8)
-        return;
+        return 0;
     n           = mul(1 / dbl, n);
     Real const t = dot(n, sub(xv, xf[0]));
     V3 ap        = sub(sub(xv, mul(t, n)), xf[0]);
@@ -100,7 +102,7 @@ void vertex_triangle_contact(V3 xtv, V3 xv, V3 const* xtf, V3 const* xf, Real dt
     Real denom = d00 * d11 - d01 * d01;
     Real bv = (d11 * d20 - d01 * d21) / denom, bw = (d00 * d21 - d01 * d20) / denom, bu = 1 - bv - bw;
     if (!(bu >= 0 && bu <= 1 && bv >= 0 && bv <= 1 && bw >= 0 && bw <= 1))
-        return;
+        return 0;
     V3 xb  = add(add(mul(bu, xf[0]), mul(bv, xf[1])), mul(bw, xf[2]));
     V3 xtb = add(add(mul(bu, xtf[0]), mul(bv, xtf[1])), mul(bw, xtf[2]));
     Real const dn     = dot(sub(xv, xb), n);
@@ -130,6 +132,8 @@ void vertex_triangle_contact(V3 xtv, V3 xv, V3 const* xtf, V3 const* xf, Real dt
     for (int c = 0; c < 3; ++c)
         for (int r = 0; r < 3; ++r)
             H[3 * c + r] += s * (E0[r] * E0[c] + E1[r] * E1[c]);
+    Real const un2 = unorm * unorm;
+    return Real(0.5) * lambda * d + muF * std::abs(lambda) * (epsvh / 3 + un2 / epsvh - un2 * unorm / (3 * epsvh * epsvh));
 }
 
 // SNH closed-form vertex block in FP64 (same contraction the full 9x9 reference Hessian reduces
@@ -176,6 +180,7 @@ void elastic_block(orc_problem const& P, int32_t i, Real const* x, Real* H, Real
 } // namespace
 
 extern "C" {
+double orc_objective(orc_problem const* Pp, double const* x, double const* xtilde, double dt);
 
 struct orc_contact
 {
@@ -380,7 +385,7 @@ int orc_run_contact(orc_problem const* Pp, orc_contact const* Cp, double* x, dou
                         C.fc[8 * size_t(i) + c] = c < int(list.size()) ? list[c] : -1;
                 }
             }
-            for (int32_t k = 0; k < iterations; ++k)
+            auto sweep = [&] {
                 for (int32_t p = 0; p < P.nPartitions; ++p)
                 {
                     std::memcpy(snap.data(), x, sizeof(Real) * n3);
@@ -444,6 +449,55 @@ int orc_run_contact(orc_problem const* Pp, orc_contact const* Cp, double* x, dou
                         xi[2] -= dx2;
                     }
                 }
+            };
+            // The GPU integrator's accelerations with contact (gpu/vbd/Integrator.cu:15-33 builds
+            // Anderson and trust-region integrators whatever the data carries); the objective of
+            // the trust region adds the contact energy of the active vertices
+            // (gpu/impl/vbd/TrustRegionIntegrator.cu:265-360).
+            auto objective = [&] {
+                Real f = orc_objective(&P, x, xtilde.data(), sdt);
+                for (int32_t q = 0; q < C.nSurfV; ++q)
+                {
+                    if (!C.active[q])
+                        continue;
+                    int32_t const i = C.V[q];
+                    int32_t const* fl = C.fc + 8 * size_t(i);
+                    Real sumfa = 0;
+                    int nc     = 0;
+                    for (int c = 0; c < 8; ++c)
+                        if (fl[c] >= 0)
+                            sumfa += C.FA[fl[c]], ++nc;
+                    if (nc == 0)
+                        continue;
+                    Real const kC = C.XVA[i] * C.muC / sumfa;
+                    for (int c = 0; c < 8; ++c)
+                    {
+                        if (fl[c] < 0)
+                            continue;
+                        int32_t const* t = C.F + 3 * size_t(fl[c]);
+                        V3 xtf[3], xf[3];
+                        for (int m = 0; m < 3; ++m)
+                        {
+                            xtf[m] = at(xt.data(), t[m]);
+                            xf[m]  = at(x, t[m]);
+                        }
+                        Real g[3] = {0, 0, 0}, H[9] = {0};
+                        f += vertex_triangle_contact(at(xt.data(), i), at(x, i), xtf, xf, sdt, kC * C.FA[fl[c]], C.muF, C.epsv, g, H);
+                    }
+                }
+                return f;
+            };
+            if (P.acceleration == 2)
+                orc::anderson_solve(P, x, nV, iterations, sweep);
+            else if (P.acceleration == 5 && !P.tr_curved)
+            {
+                size_t const entry = 4 * (size_t(step) * size_t(substeps) + size_t(s)) * size_t(iterations);
+                orc::trust_region_solve(P, x, nV, iterations, sweep, objective, P.tr_forced ? P.tr_forced + entry : nullptr,
+                                        P.tr_log ? P.tr_log + entry : nullptr);
+            }
+            else
+                for (int32_t k = 0; k < iterations; ++k)
+                    sweep();
             for (size_t k = 0; k < n3; ++k)
             {
                 vprev[k] = v[k];

@@ -138,6 +138,7 @@ void snh_grad_hessian(Real const* F, Real mu, Real lambda, Real* g, Real* H)
 
 } // namespace
 
+#include "orc_accel.h"
 #include "orc_problem.h"
 
 extern "C" {
@@ -695,6 +696,8 @@ static Real tr_clamp(Real v, Real lo, Real hi)
     return (hi < m) ? hi : m;
 }
 
+} // extern "C"
+
 // TrustRegionIntegrator::SolveWithLinearAcceleratedPath (gpu/impl/vbd/TrustRegionIntegrator.cu:
 // 48-165).  The first two iterations are plain VBD sweeps that record f and t; from k = 2 on, a
 // quadratic model m(t) through (t_{k-2}, f_{k-2}), (t_{k-1}, f_{k-1}), (t_k = 0, f_k) is built,
@@ -702,21 +705,11 @@ static Real tr_clamp(Real v, Real lo, Real hi)
 // minimiser clamped to [1, R / |dx|]; the stretched step is kept when the actual decrease is more
 // than eta of the predicted one, else rolled back to the VBD step, with the radius R grown or
 // shrunk by tau.
-static void trust_region_linear(orc_problem const& P, Real const* xt, Real const* xtilde, Real* x, Real sdt, Real sdt2, int32_t iterations, int nthreads, double const* forced, double* log)
+void orc::trust_region_solve(orc_problem const& P, double* x, int32_t nV, int32_t iterations, orc::Sweep const& sweep,
+                             orc::Objective const& objective, double const* forced, double* log)
 {
-    (void)nthreads;
-    size_t const n3 = size_t(P.nV) * 3;
+    size_t const n3 = size_t(nV) * 3;
     std::vector<Real> xkm1(x, x + n3);
-    auto objective = [&] { return orc_objective(&P, x, xtilde, sdt); };
-    auto sweep     = [&] {
-        for (int32_t p = 0; p < P.nPartitions; ++p)
-        {
-            int32_t const b = P.Pptr[p], e = P.Pptr[p + 1];
-#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
-            for (int32_t kk = b; kk < e; ++kk)
-                solve_vertex(P, P.Padj[kk], xt, xtilde, x, sdt, sdt2);
-        }
-    };
     Real const eta = P.tr_eta, tau = P.tr_tau, zero = 1e-6;
     Real fk = objective(), fkm1 = 0, fkm2 = 0, tk = -1, tkm1 = 0, tkm2 = 0, R2 = 0;
     for (int32_t k = 0; k < iterations; ++k)
@@ -800,6 +793,54 @@ static void trust_region_linear(orc_problem const& P, Real const* xt, Real const
     }
 }
 
+// AndersonIntegrator::Solve (sim/vbd/AndersonIntegrator.cpp:24-57): after each VBD iteration
+// k >= 1, G_k = x, F_k = G_k - x_{k-1}; column (k-1) mod m of the window gets G_k - G_{k-1} and
+// F_k - F_{k-1}; x = G_k - DG alpha with alpha = argmin |DF alpha - F_k| over the min(m, k) filled
+// columns.
+void orc::anderson_solve(orc_problem const& P, double* x, int32_t nV, int32_t iterations, orc::Sweep const& sweep)
+{
+    size_t const n3 = size_t(nV) * 3;
+    int const m     = P.window;
+    std::vector<std::vector<Real>> DF(static_cast<size_t>(m), std::vector<Real>(n3));
+    std::vector<std::vector<Real>> DG(static_cast<size_t>(m), std::vector<Real>(n3));
+    std::vector<Real> xkm1(x, x + n3), Gkm1(n3), Fkm1(n3), Fk(n3);
+    if (iterations > 0)
+    {
+        sweep();
+        for (size_t q = 0; q < n3; ++q)
+        {
+            Gkm1[q] = x[q];
+            Fkm1[q] = x[q] - xkm1[q];
+        }
+    }
+    for (int32_t k = 1; k < iterations; ++k)
+    {
+        std::copy(x, x + n3, xkm1.begin());
+        sweep();
+        int const dkl = (k - 1) % m;
+        for (size_t q = 0; q < n3; ++q)
+        {
+            Fk[q]      = x[q] - xkm1[q];
+            DG[dkl][q] = x[q] - Gkm1[q];
+            DF[dkl][q] = Fk[q] - Fkm1[q];
+            Gkm1[q]    = x[q];
+            Fkm1[q]    = Fk[q];
+        }
+        int const mk = std::min(m, int(k));
+        Real alpha[16];
+        anderson_lsq(DF, mk, Fk.data(), n3, alpha);
+        for (size_t q = 0; q < n3; ++q)
+        {
+            Real u = x[q];
+            for (int j = 0; j < mk; ++j)
+                u -= DG[j][q] * alpha[j];
+            x[q] = u;
+        }
+    }
+}
+
+extern "C" {
+
 int orc_run(orc_problem const* Pp, double* x, double* v, double* vprev, double dt, int32_t iterations, int32_t substeps, int32_t nsteps)
 {
     orc_problem const& P = *Pp;
@@ -846,60 +887,17 @@ int orc_run(orc_problem const* Pp, double* x, double* v, double* vprev, double d
             }
             Real const rho2 = P.rho * P.rho;
             Real omega      = 0;
-            if (P.acceleration == 2)
-            {
-                // AndersonIntegrator::Solve (sim/vbd/AndersonIntegrator.cpp:24-57): after each VBD
-                // iteration k >= 1, G_k = x, F_k = G_k - x_{k-1}; column (k-1) mod m of the window
-                // gets G_k - G_{k-1} and F_k - F_{k-1}; x = G_k - DG alpha with
-                // alpha = argmin |DF alpha - F_k| over the min(m, k) filled columns.
-                size_t const n3 = size_t(nV) * 3;
-                int const m     = P.window;
-                std::vector<std::vector<Real>> DF(static_cast<size_t>(m), std::vector<Real>(n3));
-                std::vector<std::vector<Real>> DG(static_cast<size_t>(m), std::vector<Real>(n3));
-                std::vector<Real> xkm1(x, x + n3), Gkm1(n3), Fkm1(n3), Fk(n3);
-                auto sweep = [&] {
-                    for (int32_t p = 0; p < P.nPartitions; ++p)
-                    {
-                        int32_t const b = P.Pptr[p], e = P.Pptr[p + 1];
+            auto sweepAll = [&] {
+                for (int32_t p = 0; p < P.nPartitions; ++p)
+                {
+                    int32_t const pb = P.Pptr[p], pe = P.Pptr[p + 1];
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
-                        for (int32_t kk = b; kk < e; ++kk)
-                            solve_vertex(P, P.Padj[kk], xt.data(), xtilde.data(), x, sdt, sdt2);
-                    }
-                };
-                if (iterations > 0)
-                {
-                    sweep();
-                    for (size_t q = 0; q < n3; ++q)
-                    {
-                        Gkm1[q] = x[q];
-                        Fkm1[q] = x[q] - xkm1[q];
-                    }
+                    for (int32_t kk = pb; kk < pe; ++kk)
+                        solve_vertex(P, P.Padj[kk], xt.data(), xtilde.data(), x, sdt, sdt2);
                 }
-                for (int32_t k = 1; k < iterations; ++k)
-                {
-                    std::copy(x, x + n3, xkm1.begin());
-                    sweep();
-                    int const dkl = (k - 1) % m;
-                    for (size_t q = 0; q < n3; ++q)
-                    {
-                        Fk[q]      = x[q] - xkm1[q];
-                        DG[dkl][q] = x[q] - Gkm1[q];
-                        DF[dkl][q] = Fk[q] - Fkm1[q];
-                        Gkm1[q]    = x[q];
-                        Fkm1[q]    = Fk[q];
-                    }
-                    int const mk = std::min(m, int(k));
-                    Real alpha[16];
-                    anderson_lsq(DF, mk, Fk.data(), n3, alpha);
-                    for (size_t q = 0; q < n3; ++q)
-                    {
-                        Real u = x[q];
-                        for (int j = 0; j < mk; ++j)
-                            u -= DG[j][q] * alpha[j];
-                        x[q] = u;
-                    }
-                }
-            }
+            };
+            if (P.acceleration == 2)
+                orc::anderson_solve(P, x, nV, iterations, sweepAll);
             // NesterovIntegrator::Solve (sim/vbd/NesterovIntegrator.cpp:16-43): x_0 is the solve's
             // start (never updated); for k > start, y = x + beta (x - x_0) before the sweep and
             // x = y - (x - x_0)/L after it, then lambda and beta advance.
@@ -913,11 +911,12 @@ int orc_run(orc_problem const* Pp, double* x, double* v, double* vprev, double d
             if (P.acceleration == 4)
                 broyden(P, xt.data(), xtilde.data(), x, sdt, sdt2, iterations, nthreads);
             if (P.acceleration == 5 && !P.tr_curved)
-                trust_region_linear(P, xt.data(), xtilde.data(), x, sdt, sdt2, iterations, nthreads,
-                                    P.tr_forced ? P.tr_forced + 4 * (size_t(step) * size_t(substeps) + size_t(s)) * size_t(iterations)
-                                                : nullptr,
-                                    P.tr_log ? P.tr_log + 4 * (size_t(step) * size_t(substeps) + size_t(s)) * size_t(iterations)
-                                             : nullptr);
+            {
+                size_t const entry = 4 * (size_t(step) * size_t(substeps) + size_t(s)) * size_t(iterations);
+                orc::trust_region_solve(P, x, nV, iterations, sweepAll,
+                                        [&] { return orc_objective(&P, x, xtilde.data(), sdt); },
+                                        P.tr_forced ? P.tr_forced + entry : nullptr, P.tr_log ? P.tr_log + entry : nullptr);
+            }
             // The curved trust-region path (TrustRegionIntegrator.cu:167-263) never moves x off the
             // VBD iterates: its constraint solve returns 0, so t = clamp(t*, FLT_MIN, 0) is at the
             // lower bound, no accelerated step is tried and every iteration is a plain VBD sweep.

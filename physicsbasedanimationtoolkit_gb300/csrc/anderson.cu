@@ -262,6 +262,8 @@ __global__ void anderson_update_kernel(AndersonParams p)
             cz += a * (X.z + Df.z);
         }
         p.x[i] = make_float4(u.x - cx, u.y - cy, u.z - cz, 0.f);
+        if (p.xh)
+            p.xh[i] = p.x[i];
         if (p.next >= 0)
         {
             float4 const f               = p.step[i];
@@ -279,6 +281,8 @@ __global__ void anderson_update_kernel(AndersonParams p)
     }
     u.w    = 0.f;
     p.x[i] = u;
+    if (p.xh)
+        p.xh[i] = u;
 }
 
 inline int blocks_of(int64_t n, int b)

@@ -42,6 +42,7 @@ int constexpr kAndersonMaxWindow = 16;
 struct AndersonParams
 {
     float4* __restrict__ x;
+    float4* xh; // with contact: the two-buffer sweep's copy of the iterate, updated with x (or null)
     float4 const* __restrict__ step; // the last VBD iteration's increments: F_k = step
     float4* __restrict__ Gkm1; // last un-accelerated iterate G_{k-1}
     float4* __restrict__ Fkm1; // last residual F_{k-1}

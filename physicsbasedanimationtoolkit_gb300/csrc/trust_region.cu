@@ -159,8 +159,50 @@ __global__ void trust_apply_kernel(TrustParams p, bool rollback)
         return;
     float4 const a = p.x[i], b = p.xkm1[i];
     double const s = rollback ? 1.0 / t : t;
-    p.x[i] = make_float4(float(double(b.x) + s * (double(a.x) - b.x)), float(double(b.y) + s * (double(a.y) - b.y)),
-                         float(double(b.z) + s * (double(a.z) - b.z)), a.w);
+    float4 const u = make_float4(float(double(b.x) + s * (double(a.x) - b.x)), float(double(b.y) + s * (double(a.y) - b.y)),
+                                 float(double(b.z) + s * (double(a.z) - b.z)), a.w);
+    p.x[i] = u;
+    if (p.xh)
+        p.xh[i] = u;
+}
+
+// Contact energy of active vertex av[q] (TrustRegionIntegrator.cu:310-350): the area-scaled
+// penalty over its listed triangles and vertex_triangle_contact's energy for each, at the current
+// positions against those at t.
+__device__ double contact_energy(TrustParams const& p, int q)
+{
+    int const i = p.cV[p.av[q]];
+    float sumfa = 0.f;
+    int32_t f[8];
+    for (int c = 0; c < 8; ++c)
+    {
+        f[c] = p.fc[i * 8 + c];
+        if (f[c] >= 0)
+            sumfa += p.FA[f[c]];
+    }
+    if (!(sumfa > 0.f))
+        return 0.0;
+    float const kC     = p.XVA[i] * p.muC / sumfa;
+    float4 const xti4  = p.xt[i], xi4 = p.x[i];
+    float const xti[3] = {xti4.x, xti4.y, xti4.z}, xi[3] = {xi4.x, xi4.y, xi4.z};
+    double e = 0.0;
+    for (int c = 0; c < 8; ++c)
+    {
+        if (f[c] < 0)
+            continue;
+        int4 const t   = p.cF[f[c]];
+        int const v[3] = {t.x, t.y, t.z};
+        float xtf[3][3], xf[3][3];
+        for (int k = 0; k < 3; ++k)
+        {
+            float4 const a = p.xt[v[k]], b = p.x[v[k]];
+            xtf[k][0] = a.x, xtf[k][1] = a.y, xtf[k][2] = a.z;
+            xf[k][0] = b.x, xf[k][1] = b.y, xf[k][2] = b.z;
+        }
+        float g[3] = {0.f, 0.f, 0.f}, H[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        e += double(vertex_triangle_contact(xti, xi, xtf, xf, p.h, kC * p.FA[f[c]], p.muF, p.epsv, FLT_EPSILON, g, H));
+    }
+    return e;
 }
 
 __global__ void trust_objective_kernel(TrustParams p, TrustObjectivePhase phase, int32_t k, int32_t entry)
@@ -172,6 +214,12 @@ __global__ void trust_objective_kernel(TrustParams p, TrustObjectivePhase phase,
     int const n = p.energy.nV > p.energy.nT ? p.energy.nV : p.energy.nT;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
         acc += objective_term(p.energy, j);
+    if (p.nActive)
+    {
+        int const na = *p.nActive;
+        for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < na; q += gridDim.x * blockDim.x)
+            acc += contact_energy(p, q);
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0)
         acc += p.energy.dt2 * p.energy.restEnergy;
     double f = 0.0;

@@ -48,6 +48,18 @@ struct TrustParams
     double* partials; // kTrustMaxBlocks
     int32_t nV;
     double eta, tau;
+    float4* xh; // with contact: the two-buffer sweep's copy of the iterate, updated with x (or null)
+    // With contact: the contact energy of the active vertices joins the objective
+    // (gpu/impl/vbd/TrustRegionIntegrator.cu:265-360); nActive = null without contact.
+    int32_t const* nActive;
+    int32_t const* av;  // active collision vertices (indices into cV)
+    int32_t const* cV;  // collision vertex -> system vertex
+    int32_t const* fc;  // 8 contact triangles per system vertex (-1 = none)
+    int4 const* cF;     // triangles
+    float const* FA;    // triangle areas
+    float const* XVA;   // vertex areas
+    float4 const* xt;   // positions at t
+    float muC, muF, epsv, h;
     // Decision log of the step, 4 doubles per (substep, iteration) entry: t, the decrease ratio
     // rho (NaN when no stretched step was tried), the squared radius after the iteration, and
     // flags (1: stretched step tried, 2: accepted).  Iterations 0 and 1 log t = 0, flags 0.

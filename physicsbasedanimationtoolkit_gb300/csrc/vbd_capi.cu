@@ -163,8 +163,8 @@ inline void validate_descs(pbgb_vbd_desc const* descs, int32_t nMeshes)
         {
             if (!(d.tr_eta >= 0.0) || !std::isfinite(d.tr_eta) || !(d.tr_tau > 1.0) || !std::isfinite(d.tr_tau))
                 bad("trust-region acceleration expects eta >= 0 and tau > 1");
-            if (nMeshes != 1 || d.n_collision_triangles > 0)
-                bad("trust-region acceleration needs a single mesh without contact");
+            if (nMeshes != 1)
+                bad("trust-region acceleration needs a single mesh");
         }
         if (d.acceleration == PBGB_ACCEL_NESTEROV &&
             (!(d.nesterov_lipschitz > 0.0) || !std::isfinite(d.nesterov_lipschitz) || d.nesterov_start < 0))
@@ -176,8 +176,11 @@ inline void validate_descs(pbgb_vbd_desc const* descs, int32_t nMeshes)
             char const* name = d.acceleration == PBGB_ACCEL_ANDERSON ? "Anderson" : "Broyden";
             if (d.window_size < 1 || d.window_size > kAndersonMaxWindow)
                 bad(std::string(name) + " window must be in [1, 16]");
-            if (nMeshes != 1 || d.n_collision_triangles > 0)
-                bad(std::string(name) + " acceleration needs a single mesh without contact");
+            // The reference's GPU integrator runs Anderson with contact; Broyden is a CPU-integrator
+            // strategy, whose integrator has no contact.
+            if (nMeshes != 1 || (d.acceleration == PBGB_ACCEL_BROYDEN && d.n_collision_triangles > 0))
+                bad(std::string(name) + (d.acceleration == PBGB_ACCEL_BROYDEN ? " acceleration needs a single mesh without contact"
+                                                                              : " acceleration needs a single mesh"));
         }
         if (d.init_strategy < 0 || d.init_strategy > 4)
             bad("invalid initialization strategy");
@@ -1200,6 +1203,21 @@ class VbdSystem
                 tp.nV       = nV;
                 tp.eta      = trEta;
                 tp.tau      = trTau;
+                if (contact)
+                {
+                    tp.nActive = cstate.nActive;
+                    tp.av      = cstate.av;
+                    tp.cV      = cmesh.V;
+                    tp.fc      = cFc.get();
+                    tp.cF      = cF.get();
+                    tp.FA      = cFA.get();
+                    tp.XVA     = cXVA.get();
+                    tp.xt      = xt.get();
+                    tp.muC     = muC;
+                    tp.muF     = muF;
+                    tp.epsv    = epsv;
+                    tp.h       = h;
+                }
                 // TrustRegionIntegrator::SolveWithLinearAcceleratedPath (:48-170): f at the initial guess.
                 check(launch_trust_objective(tp, kTrustInitial, 0, 0, stream), "trust_objective");
             }
@@ -1242,6 +1260,10 @@ class VbdSystem
                     w.hprev = H[(k + 1) % 2];
                     w.hcur  = H[k % 2];
                 }
+                // With contact the two-buffer sweep keeps the iterate in x and in H[k % 2]; the
+                // accelerations update both.
+                ap.xh = twoBuffer ? H[k % 2] : nullptr;
+                tp.xh = twoBuffer ? H[k % 2] : nullptr;
                 if (trust)
                     check(launch_trust_begin(tp, k, stream), "trust_begin");
                 bool const neActive = nesterov && nesterovStart < k;

@@ -128,7 +128,7 @@ __device__ __forceinline__ void finish_vertex(SweepParams const& p, VertexBlock<
     float dx[3];
     bool const moved = inertia_solve(H, g, xl, xt4.w, p.h2, p.detHZero, xi, static_cast<float*>(nullptr),
                                      static_cast<float*>(nullptr), dx);
-    if (!CHEB && p.step)
+    if (p.step)
         p.step[i] = make_float4(dx[0], dx[1], dx[2], 0.f);
     if (REC)
     {

@@ -344,9 +344,22 @@ class OracleContactVbd(OracleVbd):
         Cc.wmax[:] = [float(c) for c in X.max(axis=0).astype(np.float32)]
         self.C = Cc
 
-    def step(self, dt, iterations, substeps=1, nsteps=1, use_ref=False):
-        rc = lib().orc_run_contact(C.byref(self.P), C.addressof(self.C), self.x, self.v, self.vprev, dt,
-                                   iterations, substeps, nsteps)
+    def step(self, dt, iterations, substeps=1, nsteps=1, use_ref=False, trust_region_log=None):
+        own = np.zeros((nsteps * substeps * iterations, 4))
+        self.P.tr_log = own.ctypes.data
+        self.trust_region_log = own
+        forced = None
+        if trust_region_log is not None:
+            forced = np.ascontiguousarray(trust_region_log, dtype=np.float64)
+            if forced.shape != (nsteps * substeps * iterations, 4):
+                raise ValueError("trust_region_log must hold nsteps x substeps x iterations rows of 4")
+            self.P.tr_forced = forced.ctypes.data
+        try:
+            rc = lib().orc_run_contact(C.byref(self.P), C.addressof(self.C), self.x, self.v, self.vprev, dt,
+                                       iterations, substeps, nsteps)
+        finally:
+            self.P.tr_forced = None
+            self.P.tr_log = None
         if rc != 0:
             raise RuntimeError(f"oracle run failed: {rc}")
 

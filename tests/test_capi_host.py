@@ -155,16 +155,30 @@ def _desc_with_contact(accel):
     return desc, keep
 
 
-@pytest.mark.parametrize("accel,name", [(2, "Anderson"), (3, "Nesterov"), (4, "Broyden"), (5, "trust-region")])
-def test_window_and_nesterov_accelerations_need_a_single_mesh_without_contact(accel, name):
+@pytest.mark.parametrize("accel,name", [(3, "Nesterov"), (4, "Broyden")])
+def test_cpu_strategies_need_a_single_mesh_without_contact(accel, name):
+    """Nesterov and Broyden are CPU-integrator strategies, whose integrator has no contact."""
     desc, keep = _desc_with_contact(accel)
-    desc.tr_tau = 2.0
     desc.nesterov_lipschitz = 1.0
     desc.window_size = 5
     h = C.c_void_p()
     rc = _capi.lib().pbgb_vbd_create(C.byref(desc), C.byref(h))
     assert rc == 1
     assert name in _capi.lib().pbgb_last_error(None).decode()
+
+
+@pytest.mark.parametrize("accel", [2, 5])
+def test_gpu_strategies_accept_contact(accel):
+    """The reference's GPU integrator runs Anderson and the trust region with contact: the
+    descriptor passes validation (creation then needs a device)."""
+    desc, keep = _desc_with_contact(accel)
+    desc.tr_eta, desc.tr_tau, desc.tr_curved = 0.2, 2.0, 0
+    desc.window_size = 5
+    h = C.c_void_p()
+    rc = _capi.lib().pbgb_vbd_create(C.byref(desc), C.byref(h))
+    if rc == 0:
+        _capi.lib().pbgb_vbd_destroy(h)
+    assert rc in (0, 6), _capi.lib().pbgb_last_error(None)
 
 
 def test_cpu_integrator_has_no_contact():
@@ -206,11 +220,6 @@ def test_trust_region_settings_are_validated():
         pbat.sim.vbd.Data().with_volume_mesh(P, T).with_trust_region_acceleration(-0.1, 2.0, False).construct()
     with pytest.raises(ValueError):
         pbat.sim.vbd.Data().with_volume_mesh(P, T).with_trust_region_acceleration(0.2, 1.0, True).construct()
-    d = (pbat.sim.vbd.Data().with_volume_mesh(P, T).with_surface_mesh(V, F)
-         .with_trust_region_acceleration(0.2, 2.0, False).construct())
-    with pytest.raises(_capi.PbgbError) as e:
-        pbat.gpu.vbd.Integrator(d)
-    assert e.value.code == 1 and "trust-region" in str(e.value)
 
 
 def _cube_data():

@@ -202,3 +202,57 @@ def _sqdist(p, a, b, c):
         return float(r @ r)
 
     return min(seg(a, b), seg(b, c), seg(c, a))
+
+
+def test_anderson_with_contact_matches_oracle():
+    """gpu/vbd/Integrator.cu:15-33 builds the Anderson integrator for contact scenes too: window 5
+    on the two-buffer contact sweep (the iterate updated in both position buffers), 12 steps
+    against the FP64 contact oracle running the same Anderson loop."""
+    w = small_scene()
+    d = (pbat.sim.vbd.Data().with_volume_mesh(w["X"].T, w["T"].T).with_surface_mesh(w["V"], w["F"].T)
+         .with_bodies(w["B"]).with_material(w["rho"], w["mu"], w["lam"]).with_dirichlet_vertices(w["dbc"])
+         .with_contact_parameters(1e7, 0.3, 1e-3).with_initialization_strategy(2)
+         .with_anderson_acceleration(5).construct())
+    I = pbat.gpu.vbd.Integrator(d)
+    R = O.OracleContactVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], w["V"], w["F"], w["B"],
+                           muC=1e7, strategy=2, anderson_window=5)
+    diag = np.linalg.norm(w["X"].max(0) - w["X"].min(0))
+    errs = []
+    for _ in range(12):
+        I.x, I.v = R.x.T.copy(), R.v.T.copy()
+        I.step(1 / 60, 15, 1)
+        R.step(1 / 60, 15, 1, 1)
+        errs.append(np.abs(I.x.T - R.x).max() / diag)
+    fc, active = I.contacts()
+    assert R.active.sum() > 0
+    assert max(errs) <= 1e-4, errs
+
+
+def test_trust_region_with_contact_matches_oracle_on_the_device_decisions():
+    """The trust region with contact (the objective adds the active vertices' contact energy,
+    gpu/impl/vbd/TrustRegionIntegrator.cu:265-360): the oracle replays the device's logged decisions
+    step by step; positions within 1e-4 of the diagonal over the first 10 steps (measured up to
+    6e-6).  A stretched step multiplies the FP32/FP64 difference of the VBD step by t (up to ~16),
+    and the penalty switching on below a triangle's plane amplifies it further: at step 11 of this
+    scene, where the active set drops from 99 to 78 vertices, the replayed oracle lands 6.7e-3 of
+    the diagonal away (FP64 trust-region and plain VBD differ by 2.6e-3 there), so the check stops
+    before it."""
+    w = small_scene()
+    d = (pbat.sim.vbd.Data().with_volume_mesh(w["X"].T, w["T"].T).with_surface_mesh(w["V"], w["F"].T)
+         .with_bodies(w["B"]).with_material(w["rho"], w["mu"], w["lam"]).with_dirichlet_vertices(w["dbc"])
+         .with_contact_parameters(1e7, 0.3, 1e-3).with_initialization_strategy(2)
+         .with_trust_region_acceleration(0.2, 2.0, False).construct())
+    I = pbat.gpu.vbd.Integrator(d)
+    R = O.OracleContactVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], w["V"], w["F"], w["B"],
+                           muC=1e7, strategy=2, trust_region=(0.2, 2.0, False))
+    diag = np.linalg.norm(w["X"].max(0) - w["X"].min(0))
+    tried = 0
+    for _ in range(10):
+        I.x, I.v = R.x.T.copy(), R.v.T.copy()
+        I.step(1 / 60, 15, 1)
+        log = I.trust_region_log()
+        tried += int((log[:, 3] > 0).sum())
+        R.step(1 / 60, 15, 1, 1, trust_region_log=log)
+        err = np.abs(I.x.T - R.x).max() / diag
+        assert err <= 1e-4, err
+    assert tried > 0 and R.active.sum() > 0
