@@ -480,8 +480,9 @@ struct NearestSmem
 // Warp-cooperative form of the same query, one warp per active vertex.  The traversal is what
 // bounds the kernel: a query's loads form one dependent chain per thread, so spreading it over 32
 // lanes shortens the longest chain about as many times.
-//   1. breadth first, collect every leaf whose box lies within the reference's initial bound
-//      dupper + eps, with its triangle's squared distance (only these can ever be listed);
+//   1. breadth first, collect every leaf whose box lies within min(dupper + eps, the distance to
+//      the vertex's current list plus the margin), with its triangle's squared distance (no
+//      other leaf can be listed: see above);
 //   2. d* = the warp minimum over other bodies; keep the candidates with d <= d* + margin (see
 //      above: no other leaf can restart the scan's final list or join it);
 //   3. order them by decreasing leaf index (the reference's visit order) and run its scan.
@@ -502,10 +503,27 @@ __global__ void __launch_bounds__(32 * kNearestWarps) nearest_kernel(ContactMesh
     int const body     = M.B[i];
     float const eps    = FLT_EPSILON;
     float const d0     = S.dupper[v];
-    float const bound  = d0 + eps;
+    // Any triangle of another body bounds d* from above; the vertex's current list (from the last
+    // update) usually holds the nearest ones, so the collection can stop at that bound plus the
+    // margin the scan needs instead of the warm-start radius.
+    float U = FLT_MAX;
+    if (lane < kMaxContacts)
+    {
+        int32_t const f = S.fc[i * kMaxContacts + lane];
+        if (f >= 0)
+        {
+            int4 const t = M.F[f];
+            if (M.B[t.x] != body)
+                U = point_triangle_sqdist(p, f3(x[t.x]), f3(x[t.y]), f3(x[t.z]));
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1)
+        U = fminf(U, __shfl_xor_sync(all, U, off));
+    float const bound = fminf(d0 + eps, U * (1.f + 16.f * eps) + 8.f * eps);
     int32_t const leafBegin = T.n - 1;
 
-    // 1. Breadth-first collection.
+    // 1. Breadth-first collection (every leaf with d <= bound: they include all those with
+    //    d <= d* + margin, as U >= d*).
     int cur = 0, nf = 1, nc = 0;
     bool overflow = false;
     if (lane == 0)
@@ -584,7 +602,7 @@ __global__ void __launch_bounds__(32 * kNearestWarps) nearest_kernel(ContactMesh
         dstar = fminf(dstar, __shfl_xor_sync(all, dstar, off));
     int32_t list[kMaxContacts];
     int count = 0;
-    if (dstar <= bound)
+    if (dstar <= d0 + eps)
     {
         float const cap = dstar * (1.f + 16.f * eps) + 8.f * eps;
         // Compact the kept candidates to the front (order does not matter yet).
