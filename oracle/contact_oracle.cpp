@@ -647,4 +647,166 @@ int orc_dcd_contacts(
     return 0;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Continuous half, vertex-triangle part (sim/contact/MultibodyMeshMixedCcdDcd.h
+// ReportVertexTriangleCcdContacts; geometry/PointTriangleCcd.h:125-160): the earliest time
+// t in [0, 1] at which a linearly moving point lies in a linearly moving triangle.  The
+// coplanarity condition ((b - a) x (c - a)) . (x - a) = 0 is a cubic in t; its roots in [0, 1] are
+// visited in increasing order and the first one whose barycentric coordinates
+// (geometry/IntersectionQueries.h:50-67) all lie in [0, 1] is the time of impact.  The reference
+// finds the roots with the solver of its math/polynomial/Roots.h; this restatement brackets them
+// between the cubic's critical points and bisects each bracket to full precision.  Brute force over
+// the triangles of other bodies whose swept boxes overlap the vertex's swept box: for test-sized
+// scenes.  t[q] = earliest time of impact of collision vertex q (-1: none), f[q] = its triangle.
+// The edge-edge part of the reference detector is not restated: the VBD path has no edge contacts.
+
+namespace {
+
+// Roots of c0 + c1 t + c2 t^2 + c3 t^3 in [0, 1], increasing.
+int cubic_roots_01(Real const c[4], Real* roots)
+{
+    auto f = [&](Real t) { return ((c[3] * t + c[2]) * t + c[1]) * t + c[0]; };
+    // Breakpoints: 0, the real critical points inside (0, 1), 1.
+    Real bp[4];
+    int nb   = 0;
+    bp[nb++] = 0;
+    Real const qa = 3 * c[3], qb = 2 * c[2], qc = c[1];
+    Real crit[2];
+    int nc = 0;
+    if (qa != 0)
+    {
+        Real const disc = qb * qb - 4 * qa * qc;
+        if (disc >= 0)
+        {
+            Real const sq = std::sqrt(disc);
+            Real const r0 = (-qb - sq) / (2 * qa), r1 = (-qb + sq) / (2 * qa);
+            crit[nc++] = std::min(r0, r1);
+            crit[nc++] = std::max(r0, r1);
+        }
+    }
+    else if (qb != 0)
+        crit[nc++] = -qc / qb;
+    for (int k = 0; k < nc; ++k)
+        if (crit[k] > 0 && crit[k] < 1)
+            bp[nb++] = crit[k];
+    bp[nb++] = 1;
+    int n = 0;
+    for (int k = 0; k + 1 < nb; ++k)
+    {
+        Real lo = bp[k], hi = bp[k + 1];
+        Real flo = f(lo), fhi = f(hi);
+        if (flo == 0)
+        {
+            if (n == 0 || roots[n - 1] != lo)
+                roots[n++] = lo;
+            continue;
+        }
+        if (fhi == 0)
+        {
+            roots[n++] = hi;
+            continue;
+        }
+        if ((flo < 0) == (fhi < 0))
+            continue;
+        for (int it = 0; it < 200 && hi - lo > 0; ++it)
+        {
+            Real const mid = Real(0.5) * (lo + hi);
+            if (mid <= lo || mid >= hi)
+                break;
+            Real const fm = f(mid);
+            if ((fm < 0) == (flo < 0))
+                lo = mid, flo = fm;
+            else
+                hi = mid;
+        }
+        roots[n++] = Real(0.5) * (lo + hi);
+    }
+    return n;
+}
+
+Real point_triangle_ccd(V3 xt, V3 at, V3 bt, V3 ct, V3 x, V3 a, V3 b, V3 c)
+{
+    V3 const E1 = sub(bt, at), E2 = sub(ct, at), Q = sub(xt, at);
+    V3 const D1 = sub(sub(b, a), E1), D2 = sub(sub(c, a), E2), DQ = sub(sub(x, a), Q);
+    V3 const n0 = cross(E1, E2);
+    V3 const n1 = add(cross(E1, D2), cross(D1, E2));
+    V3 const n2 = cross(D1, D2);
+    Real const coeff[4] = {dot(n0, Q), dot(n0, DQ) + dot(n1, Q), dot(n1, DQ) + dot(n2, Q), dot(n2, DQ)};
+    Real roots[3];
+    int const nr = cubic_roots_01(coeff, roots);
+    for (int k = 0; k < nr; ++k)
+    {
+        Real const t = roots[k];
+        auto lerp    = [&](V3 p0, V3 p1) { return add(p0, mul(t, sub(p1, p0))); };
+        V3 const P = lerp(xt, x), A = lerp(at, a), B = lerp(bt, b), Cc = lerp(ct, c);
+        V3 const ab = sub(B, A), ac = sub(Cc, A), ap = sub(P, A);
+        Real const d00 = dot(ab, ab), d01 = dot(ab, ac), d11 = dot(ac, ac), d20 = dot(ap, ab), d21 = dot(ap, ac);
+        Real const den = d00 * d11 - d01 * d01;
+        Real const v = (d11 * d20 - d01 * d21) / den, w = (d00 * d21 - d01 * d20) / den, u = 1 - v - w;
+        if (u >= 0 && u <= 1 && v >= 0 && v <= 1 && w >= 0 && w <= 1)
+            return t;
+    }
+    return -1;
+}
+
+} // namespace
+
+int orc_ccd_vertex_triangle(
+    int32_t nV,
+    double const* xt,
+    double const* x,
+    int32_t nF,
+    int32_t const* F,
+    int32_t nCV,
+    int32_t const* V,
+    int32_t const* B,
+    double* toi,
+    int32_t* tri)
+{
+    (void)nV;
+    std::vector<V3> flo(static_cast<size_t>(nF)), fhi(static_cast<size_t>(nF));
+    for (int32_t f = 0; f < nF; ++f)
+    {
+        int32_t const* t = F + 3 * size_t(f);
+        V3 l = at(xt, t[0]), u = l;
+        for (int k = 0; k < 3; ++k)
+            for (double const* src : {xt, x})
+            {
+                V3 const p = at(src, t[k]);
+                l = {std::min(l.x, p.x), std::min(l.y, p.y), std::min(l.z, p.z)};
+                u = {std::max(u.x, p.x), std::max(u.y, p.y), std::max(u.z, p.z)};
+            }
+        flo[size_t(f)] = l;
+        fhi[size_t(f)] = u;
+    }
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int32_t q = 0; q < nCV; ++q)
+    {
+        int32_t const i = V[q];
+        V3 const p0 = at(xt, i), p1 = at(x, i);
+        V3 const l{std::min(p0.x, p1.x), std::min(p0.y, p1.y), std::min(p0.z, p1.z)};
+        V3 const u{std::max(p0.x, p1.x), std::max(p0.y, p1.y), std::max(p0.z, p1.z)};
+        Real best    = -1;
+        int32_t bestF = -1;
+        for (int32_t f = 0; f < nF; ++f)
+        {
+            int32_t const* t = F + 3 * size_t(f);
+            if (B[t[0]] == B[i])
+                continue;
+            if (!(l.x <= fhi[size_t(f)].x && l.y <= fhi[size_t(f)].y && l.z <= fhi[size_t(f)].z && flo[size_t(f)].x <= u.x &&
+                  flo[size_t(f)].y <= u.y && flo[size_t(f)].z <= u.z))
+                continue;
+            Real const tc = point_triangle_ccd(p0, at(xt, t[0]), at(xt, t[1]), at(xt, t[2]), p1, at(x, t[0]), at(x, t[1]), at(x, t[2]));
+            if (tc >= 0 && (best < 0 || tc < best))
+            {
+                best  = tc;
+                bestF = f;
+            }
+        }
+        toi[q] = best;
+        tri[q] = bestF;
+    }
+    return 0;
+}
+
 } // extern "C"

@@ -118,6 +118,9 @@ def lib():
                                       C.c_int32, C.c_int32, C.c_int32]
         L.orc_overlaps.restype = C.c_int64
         L.orc_overlaps.argtypes = [C.c_int32, _f32p, _f32p, C.c_int32, _f32p, _f32p, _i32p, C.c_int64]
+        L.orc_ccd_vertex_triangle.restype = C.c_int
+        L.orc_ccd_vertex_triangle.argtypes = [C.c_int32, _f64p, _f64p, C.c_int32, _i32p, C.c_int32, _i32p, _i32p,
+                                              _f64p, _i32p]
         L.orc_dcd_contacts.restype = C.c_int
         L.orc_dcd_contacts.argtypes = [C.c_int32, _f64p, C.c_int32, _i32p, C.c_int32, _i32p, C.c_int32, _i32p,
                                        _i32p, _i32p, _i32p, _f64p]
@@ -444,3 +447,21 @@ def dcd_contacts(x, T, F, V, B):
     if rc != 0:
         raise RuntimeError("orc_dcd_contacts failed")
     return body, nearest, d2
+
+
+def ccd_vertex_triangle(xt, x, F, V, B):
+    """Vertex-triangle CCD of the CPU multibody detector (oracle/contact_oracle.cpp
+    orc_ccd_vertex_triangle): for each collision vertex V[q], the earliest time of impact in [0, 1]
+    of its linear trajectory xt -> x with a linearly moving triangle of another body (-1: none) and
+    that triangle."""
+    xt = np.ascontiguousarray(xt, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    F = np.ascontiguousarray(F, dtype=np.int32)
+    V = np.ascontiguousarray(V, dtype=np.int32)
+    B = np.ascontiguousarray(B, dtype=np.int32)
+    toi = np.empty(V.size, np.float64)
+    tri = np.empty(V.size, np.int32)
+    rc = lib().orc_ccd_vertex_triangle(x.shape[0], xt, x, F.shape[0], F, V.size, V, B, toi, tri)
+    if rc != 0:
+        raise RuntimeError("orc_ccd_vertex_triangle failed")
+    return toi, tri

@@ -142,3 +142,54 @@ def O_point_triangle(p, a, b, c):
         return float(r @ r)
 
     return min(seg(p, a, b), seg(p, b, c), seg(p, c, a))
+
+
+def _toi_by_scan(p0, p1, tri0, tri1, n=20001):
+    """Earliest time in [0, 1] at which the point lies in the triangle, by a dense scan of the
+    coplanarity sign with barycentric checks at the crossings (reference-free check)."""
+    t = np.linspace(0.0, 1.0, n)
+    P = p0 + t[:, None] * (p1 - p0)
+    A, Bv, Cc = (tri0[k] + t[:, None] * (tri1[k] - tri0[k]) for k in range(3))
+    f = np.einsum("ij,ij->i", np.cross(Bv - A, Cc - A), P - A)
+    for j in np.nonzero(np.sign(f[:-1]) * np.sign(f[1:]) <= 0)[0]:
+        # linear interpolation of the crossing inside [t_j, t_j+1]
+        tc = t[j] if f[j] == f[j + 1] else t[j] + (t[j + 1] - t[j]) * f[j] / (f[j] - f[j + 1])
+        a, b, c = (tri0[k] + tc * (tri1[k] - tri0[k]) for k in range(3))
+        x = p0 + tc * (p1 - p0)
+        ab, ac, ap = b - a, c - a, x - a
+        d00, d01, d11, d20, d21 = ab @ ab, ab @ ac, ac @ ac, ap @ ab, ap @ ac
+        den = d00 * d11 - d01 * d01
+        v, w = (d11 * d20 - d01 * d21) / den, (d00 * d21 - d01 * d20) / den
+        if min(1 - v - w, v, w) >= -1e-6 and max(1 - v - w, v, w) <= 1 + 1e-6:
+            return tc
+    return -1.0
+
+
+def test_vertex_triangle_ccd_oracle():
+    """The vertex-triangle CCD of the multibody detector (geometry/PointTriangleCcd.h:125-160): a
+    point falling through a fixed triangle hits it at the crossing time; one passing beside it
+    does not; seeded random linear motions agree with a dense scan of the coplanarity sign."""
+    tri = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0]])
+    pts = np.array([[0.2, 0.2, 1.0], [0.2, 0.2, -1.0], [2.0, 2.0, 1.0], [2.0, 2.0, -1.0]])
+
+    def one(p0, p1, t0, t1):
+        xt = np.vstack([p0, t0])
+        x = np.vstack([p1, t1])
+        F = np.array([[1, 2, 3]])
+        toi, f = O.ccd_vertex_triangle(xt, x, F, np.array([0]), np.array([0, 1, 1, 1]))
+        return toi[0]
+
+    assert abs(one(pts[0], pts[1], tri, tri) - 0.5) < 1e-12
+    assert one(pts[2], pts[3], tri, tri) == -1.0
+    rng = np.random.default_rng(7)
+    hits = 0
+    for _ in range(300):
+        p0, p1 = rng.normal(size=3), rng.normal(size=3)
+        t0 = rng.normal(size=(3, 3))
+        t1 = t0 + 0.8 * rng.normal(size=(3, 3))
+        got, want = one(p0, p1, t0, t1), _toi_by_scan(p0, p1, t0, t1)
+        assert (got < 0) == (want < 0), (got, want)
+        if got >= 0:
+            hits += 1
+            assert abs(got - want) < 1e-3
+    assert hits > 10

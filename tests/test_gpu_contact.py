@@ -256,3 +256,25 @@ def test_trust_region_with_contact_matches_oracle_on_the_device_decisions():
         err = np.abs(I.x.T - R.x).max() / diag
         assert err <= 1e-4, err
     assert tried > 0 and R.active.sum() > 0
+
+
+def test_active_set_covers_cpu_ccd_hits():
+    """The swept-box broad phase of the GPU active set against the vertex-triangle CCD of the CPU
+    multibody detector: a cube moved in one step from 5 cm above a slab to 25 cm into it (its
+    bottom vertices pass through the slab's top face, the slab's top vertices through its bottom
+    face).  Every collision vertex whose trajectory meets a triangle of another body during the step
+    (exact CCD, oracle/contact_oracle.cpp) is active after the GPU initialization."""
+    w = meshgen.contact_scene_workload(n_cubes_side=1, cube_hexes=4, slab_hexes=(8, 8, 1), cell=1.0)
+    XT, F, V, B = w["X"].copy(), w["F"], w["V"], w["B"]
+    X = XT.copy()
+    X[B == 1, 2] -= 0.3
+    toi, tri = O.ccd_vertex_triangle(XT, X, F, V, B)
+    hits = toi >= 0
+    assert hits.sum() > 20
+    assert (B[F[tri[hits], 0]] != B[V[hits]]).all()
+    c = Ccd(X.shape[0], V, F, B)
+    lo, hi = np.minimum(XT.min(0), X.min(0)), np.maximum(XT.max(0), X.max(0))
+    c.call("pbgb_ccd_initialize", XT, X, lo, hi)
+    active, nn, dup, na = c.get()
+    missed = np.nonzero(hits & ~active.astype(bool))[0]
+    assert missed.size == 0, missed
