@@ -278,7 +278,8 @@ class VbdSystem
     ContactMesh cmesh{};
     ContactState cstate{};
     DeviceArray<int32_t> cV, cB, vcolorD, cAv, cNActive, cNn, cFc, cFlags;
-    DeviceArray<int4> cF;
+    DeviceArray<int4> cF, cRec;
+    DeviceArray<float> cPen;
     DeviceArray<float> cXVA, cFA, cDupper;
     DeviceArray<float4> cTlo, cThi, cVlo, cVhi, xpred;
     DeviceArray<uint8_t> cActive;
@@ -811,6 +812,8 @@ class VbdSystem
             cNActive.allocate(1);
             cNn.allocate(size_t(nS) * kMaxContacts);
             cFc.allocate(size_t(nV) * kMaxContacts);
+            cRec.allocate(size_t(nV) * kMaxContacts);
+            cPen.allocate(size_t(nV) * kMaxContacts);
             check(bvh_allocate(cstate.bvh, nF), "cudaMalloc");
             cV.upload(hV.data(), nS, stream);
             cF.upload(hF.data(), nF, stream);
@@ -1161,6 +1164,8 @@ class VbdSystem
             w.XVA    = cXVA.get();
             w.FA     = cFA.get();
             w.vcolor = vcolorD.get();
+            w.crec   = cRec.get();
+            w.cpen   = cPen.get();
             w.muC    = muC;
             w.muF    = muF;
             w.epsv   = epsv;
@@ -1180,7 +1185,12 @@ class VbdSystem
         {
             check(launch_begin_substep(sp, stream), "begin_substep");
             if (contact && s % activeSetFreq == 0)
+            {
                 check(contact_update(cmesh, cstate, x.get(), stream), "contact_update");
+                check(launch_contact_records(nV, cFc.get(), cF.get(), cFA.get(), cXVA.get(), vcolorD.get(), muC,
+                                             cRec.get(), cPen.get(), stream),
+                      "contact_records");
+            }
             if (hooks && hooks->substepBegin)
                 hooks->substepBegin(s);
             double omega      = 0.0;
@@ -1548,9 +1558,11 @@ class VbdSystem
         if (contact)
         {
             // predict, vertex and triangle boxes, Morton, 4 x (count, scan, scatter), Karras, leaf
-            // gather, internal boxes, overlaps, compaction; then 4 per update and 4 at finalize.
+            // gather, internal boxes, overlaps, compaction; then 5 per update (refit: triangle
+            // boxes and internal boxes, the nn reset, the nearest query, the contact records) and 4
+            // at finalize.
             int64_t const updates = (substeps + activeSetFreq - 1) / activeSetFreq;
-            n += 21 + 4 * updates + 4;
+            n += 21 + 5 * updates + 4;
         }
         return n;
     }

@@ -24,56 +24,45 @@ __device__ __forceinline__ uint32_t corner(uint4 const& t, int a)
 }
 
 // Contact terms of one vertex-triangle pair (gpu/impl/vbd/Kernels.cuh:80-114,203-223): the
-// triangle's corners at t and now (from x if their colour is solved before this one, else from
-// hprev), then the normal penalty and friction of vertex_triangle_contact with penalty kCf.
-__device__ __noinline__ void contact_pair(SweepParams const& p, int32_t f, float kCf, float const* xt, float const* xi, float* H, float* g)
+// triangle's corners at t and now (from x when their colour is solved before this one, else from
+// hprev: bit 31 of the record), then the normal penalty and friction of vertex_triangle_contact
+// with the record's penalty.
+__device__ __noinline__ void contact_pair(SweepParams const& p, int4 r, float kCf, float const* xt, float const* xi, float* H, float* g)
 {
-    int4 const t   = p.F[f];
-    int const v[3] = {t.x, t.y, t.z};
+    uint32_t const v[3] = {uint32_t(r.x), uint32_t(r.y), uint32_t(r.z)};
     float xtf[3][3], xf[3][3];
     for (int k = 0; k < 3; ++k)
     {
-        float4 const a = p.xt[v[k]];
-        float4 const b = __ldcg((p.vcolor[v[k]] < p.color ? p.x : p.hprev) + v[k]);
+        uint32_t const j = v[k] & 0x7FFFFFFFu;
+        float4 const a   = p.xt[j];
+        float4 const b   = __ldcg(((v[k] >> 31) ? p.x : p.hprev) + j);
         xtf[k][0] = a.x, xtf[k][1] = a.y, xtf[k][2] = a.z;
         xf[k][0] = b.x, xf[k][1] = b.y, xf[k][2] = b.z;
     }
     vertex_triangle_contact(xt, xi, xtf, xf, p.h, kCf, p.muF, p.epsv, FLT_EPSILON, g, H);
 }
 
-// Contact energy of vertex i, spread over the vertex's L lanes: lane l takes the listed triangles
-// l, l + L, ... (at most kMaxContactsPerVertex), the penalty is scaled by the vertex area over the
-// summed areas of the listed triangles, and the lanes' gradients and Hessians are summed with xor
-// shuffles inside the group (every lane of the warp takes part in the shuffles).  cH, cg: the
+// Contact energy of vertex i, spread over the vertex's L lanes: lane l takes the record slots
+// l, l + L, ... (kMaxContactsPerVertex of them); the lanes' gradients and Hessians are summed with
+// xor shuffles inside the group (every lane of the warp takes part in the shuffles).  cH, cg: the
 // group's sum, in every lane.
 template <int L>
 __device__ __forceinline__ void contact_terms(SweepParams const& p, bool valid, int lane, int i, float const* xt, float const* xi, float* cH, float* cg)
 {
-    int32_t f[(kMaxContactsPerVertex + L - 1) / L];
-    float fa[(kMaxContactsPerVertex + L - 1) / L];
-    float sumfa = 0.f;
-#pragma unroll
-    for (int c = 0; c < (kMaxContactsPerVertex + L - 1) / L; ++c)
-    {
-        int const k = lane + c * L;
-        f[c]        = valid && k < kMaxContactsPerVertex ? p.fc[i * kMaxContactsPerVertex + k] : -1;
-        fa[c]       = f[c] >= 0 ? p.FA[f[c]] : 0.f;
-        sumfa += fa[c];
-    }
-#pragma unroll
-    for (int off = L / 2; off > 0; off >>= 1)
-        sumfa += __shfl_xor_sync(0xffffffffu, sumfa, off);
 #pragma unroll
     for (int r = 0; r < 6; ++r)
         cH[r] = 0.f;
     cg[0] = cg[1] = cg[2] = 0.f;
-    if (sumfa > 0.f)
-    {
-        float const kC = (p.XVA[i] * p.muC) / sumfa;
 #pragma unroll
-        for (int c = 0; c < (kMaxContactsPerVertex + L - 1) / L; ++c)
-            if (f[c] >= 0)
-                contact_pair(p, f[c], kC * fa[c], xt, xi, cH, cg);
+    for (int c = 0; c < (kMaxContactsPerVertex + L - 1) / L; ++c)
+    {
+        int const k = lane + c * L;
+        if (valid && k < kMaxContactsPerVertex)
+        {
+            int4 const r = p.crec[i * kMaxContactsPerVertex + k];
+            if (r.w >= 0)
+                contact_pair(p, r, p.cpen[i * kMaxContactsPerVertex + k], xt, xi, cH, cg);
+        }
     }
 #pragma unroll
     for (int off = L / 2; off > 0; off >>= 1)
@@ -506,6 +495,46 @@ __global__ void unpack3_kernel(float4 const* __restrict__ in4, float* __restrict
     }
 }
 
+// Contact records of vertex i (SweepParams::crec): the area-scaled penalty of every listed
+// triangle (the vertex area over the summed areas of its listed triangles, times muC and the
+// triangle's area) and the corners' read rule for the colour sweep.
+__global__ void contact_records_kernel(int32_t nV, int32_t const* __restrict__ fc, int4 const* __restrict__ F,
+                                       float const* __restrict__ FA, float const* __restrict__ XVA,
+                                       int32_t const* __restrict__ vcolor, float muC, int4* __restrict__ crec,
+                                       float* __restrict__ cpen)
+{
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nV)
+        return;
+    int32_t f[kMaxContactsPerVertex];
+    float sumfa = 0.f;
+    for (int c = 0; c < kMaxContactsPerVertex; ++c)
+    {
+        f[c] = fc[i * kMaxContactsPerVertex + c];
+        if (f[c] >= 0)
+            sumfa += FA[f[c]];
+    }
+    float const kC  = sumfa > 0.f ? (XVA[i] * muC) / sumfa : 0.f;
+    int32_t const own = vcolor[i];
+    for (int c = 0; c < kMaxContactsPerVertex; ++c)
+    {
+        int4 r   = make_int4(0, 0, 0, -1);
+        float pn = 0.f;
+        if (f[c] >= 0)
+        {
+            int4 const t     = F[f[c]];
+            int const v[3]   = {t.x, t.y, t.z};
+            uint32_t code[3];
+            for (int k = 0; k < 3; ++k)
+                code[k] = uint32_t(v[k]) | (vcolor[v[k]] < own ? 0x80000000u : 0u);
+            r  = make_int4(int(code[0]), int(code[1]), int(code[2]), f[c]);
+            pn = kC * FA[f[c]];
+        }
+        crec[i * kMaxContactsPerVertex + c] = r;
+        cpen[i * kMaxContactsPerVertex + c] = pn;
+    }
+}
+
 inline int blocks_for(int64_t n, int block)
 {
     return int((n + block - 1) / block);
@@ -666,6 +695,15 @@ cudaError_t launch_pack3(float const* in3, float4* out4, int32_t n, cudaStream_t
     if (n <= 0)
         return cudaSuccess;
     pack3_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in3, out4, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_contact_records(int32_t nV, int32_t const* fc, int4 const* F, float const* FA, float const* XVA,
+                                   int32_t const* vcolor, float muC, int4* crec, float* cpen, cudaStream_t s)
+{
+    if (nV <= 0)
+        return cudaSuccess;
+    contact_records_kernel<<<blocks_for(nV, 256), 256, 0, s>>>(nV, fc, F, FA, XVA, vcolor, muC, crec, cpen);
     return cudaGetLastError();
 }
 
