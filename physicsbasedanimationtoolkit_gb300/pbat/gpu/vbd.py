@@ -8,7 +8,6 @@ with one launch sequence per step (an addition: the reference has one mesh per i
 
 from __future__ import annotations
 
-import ctypes as C
 
 import numpy as np
 

@@ -8,7 +8,6 @@ only.  ``build_oracle()`` compiles the oracle on first use (g++ -fopenmp, a few 
 from __future__ import annotations
 
 import ctypes as C
-import os
 import pathlib
 import subprocess
 

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import oracle_lib as O
-from physicsbasedanimationtoolkit_gb300 import _capi, meshgen, pbat
+from physicsbasedanimationtoolkit_gb300 import meshgen, pbat
 
 pytestmark = pytest.mark.gpu
 
