@@ -2,8 +2,9 @@
  * pbat_gb300.h — C ABI of the GB300-native Vertex Block Descent (VBD) library.
  *
  * One hot path of PhysicsBasedAnimationToolkit (PBAT) is implemented here: the VBD time step of
- * tetrahedral Stable Neo-Hookean meshes, with Chebyshev acceleration, a batched multi-mesh form
- * and the LBVH used by vertex-triangle contact.  Every entry point takes plain pointers and sizes,
+ * tetrahedral Stable Neo-Hookean meshes, with the reference's Chebyshev, Anderson, Broyden,
+ * Nesterov and trust-region accelerations, vertex-triangle contact (and the LBVH it uses), a
+ * batched multi-mesh form and a hand-written adjoint.  Every entry point takes plain pointers and sizes,
  * returns an int status (PBGB_OK = 0) and never lets a C++ exception cross the boundary.  Handles
  * are not thread-safe; each owns one CUDA stream.  Array layouts follow the reference's Eigen
  * column-major matrices: a "3 x n" array stores entity j at [3j, 3j+1, 3j+2].
@@ -17,6 +18,15 @@
  *   pbgb_vbd_{get,set}_*         Get/SetPositions, Get/SetVelocities,  gpu/vbd/Integrator.h:95-144
  *                                SetExternalAcceleration, Set* knobs
  *   pbgb_vbd_objective/gradient  Integrator::ObjectiveFunction(Grad)  sim/vbd/Integrator.cpp:138-200
+ *   pbgb_vbd_traced_step         Integrator::TracedStep               gpu/impl/vbd/Integrator.cu:105-148
+ *   pbgb_vbd_trace_next_step     Integrator::TraceNextStep            sim/vbd/Integrator.cpp:47-52
+ *   pbgb_vbd_trust_region_log    the trust-region decisions the reference logs through its
+ *                                profiler                             gpu/impl/vbd/TrustRegionIntegrator.cu:71-160
+ *   pbgb_bvh_*                   gpu::geometry::Bvh (build, overlaps) gpu/impl/geometry/Bvh.cu/.cuh
+ *   pbgb_ccd_*                   VertexTriangleMixedCcdDcd            gpu/impl/contact/VertexTriangleMixedCcdDcd.cu
+ * Beyond the reference: pbgb_vbd_create_batched (many meshes, one launch per colour),
+ * pbgb_vbd_step_record / pbgb_vbd_step_adjoint (reverse-mode derivatives), pbgb_vbd_save_state /
+ * pbgb_vbd_load_state (checkpoints), *_device variants (device pointers), pbgb_vbd_autotune.
  */
 #ifndef PBAT_GB300_H
 #define PBAT_GB300_H
