@@ -27,7 +27,7 @@ __device__ __forceinline__ uint32_t corner(uint4 const& t, int a)
 // triangle's corners at t and now (from x when their colour is solved before this one, else from
 // hprev: bit 31 of the record), then the normal penalty and friction of vertex_triangle_contact
 // with the record's penalty.
-__device__ __noinline__ void contact_pair(SweepParams const& p, int4 r, float kCf, float const* xt, float const* xi, float* H, float* g)
+__device__ __forceinline__ void contact_pair(SweepParams const& p, int4 r, float kCf, float const* xt, float const* xi, float* H, float* g)
 {
     uint32_t const v[3] = {uint32_t(r.x), uint32_t(r.y), uint32_t(r.z)};
     float xtf[3][3], xf[3][3];
@@ -171,7 +171,7 @@ __device__ __forceinline__ void finish_vertex(SweepParams const& p, VertexBlock<
 // REC (without CHEB): also writes the inverse Newton matrix of every solved vertex to p.tape for
 // the adjoint sweep.
 template <int L, bool CHEB, bool REC = false, bool CONTACT = false>
-__global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
+__global__ void __launch_bounds__(256, CONTACT ? 2 : 4) sweep_kernel(SweepParams p)
 {
     int const tid    = blockIdx.x * blockDim.x + threadIdx.x;
     int const s      = p.begin + tid / L;
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(256, 4) sweep_kernel(SweepParams p)
 // stride spreads random slots over all shared-memory banks); the lanes of a vertex share a warp,
 // so __syncwarp orders the staging.
 template <int L, bool CHEB, bool REC = false, bool CONTACT = false>
-__global__ void __launch_bounds__(256, 4) staged_sweep_kernel(SweepParams p)
+__global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(SweepParams p)
 {
     extern __shared__ float4 slab[]; // positions [0, p.slab), rest positions [p.slab, 2 p.slab)
     float4* const rest = slab + p.slab;
