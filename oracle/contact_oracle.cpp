@@ -548,7 +548,8 @@ void orc_vertex_triangle_contact(double const* xtv, double const* xv, double con
 //     at most 8, in triangle index order.
 // Brute force over tetrahedra and triangles with box prefilters: for test-sized scenes.
 // body[q] = penetrated body or -1; nearest[8 q ..] = triangles (-1 pad); d2[q] = their squared
-// distance (or -1).  The continuous half (vertex-triangle and edge-edge CCD) is not restated.
+// distance (or -1).  The continuous half follows below (orc_ccd_vertex_triangle,
+// orc_ccd_vertex_triangle_pairs, orc_ccd_edge_edge).
 int orc_dcd_contacts(
     int32_t nV,
     double const* x,
@@ -658,14 +659,20 @@ int orc_dcd_contacts(
 // between the cubic's critical points and bisects each bracket to full precision.  Brute force over
 // the triangles of other bodies whose swept boxes overlap the vertex's swept box: for test-sized
 // scenes.  t[q] = earliest time of impact of collision vertex q (-1: none), f[q] = its triangle.
-// The edge-edge part of the reference detector is not restated: the VBD path has no edge contacts.
+// orc_ccd_vertex_triangle_pairs reports every hit pair instead, as the reference's callback does.
 
 namespace {
 
-// Roots of c0 + c1 t + c2 t^2 + c3 t^3 in [0, 1], increasing.
+// Roots of c0 + c1 t + c2 t^2 + c3 t^3 in [0, 1], increasing.  As in the reference's root finder
+// (math/polynomial/Roots.h, the cubic method of C. Yuksel, "High-Performance Polynomial Root
+// Finding for Graphics", HPG 2022), [0, 1] is cut at the real critical points and a piece holds a
+// root when the sign bits of its end values differ (a value of exactly 0 counts as positive, so a
+// root exactly at t = 0 is not reported unless the cubic goes negative after it).  Each such piece
+// is bisected to full precision, stopping early at an exact zero.
 int cubic_roots_01(Real const c[4], Real* roots)
 {
-    auto f = [&](Real t) { return ((c[3] * t + c[2]) * t + c[1]) * t + c[0]; };
+    auto f  = [&](Real t) { return ((c[3] * t + c[2]) * t + c[1]) * t + c[0]; };
+    auto df = [&](Real t) { return (3 * c[3] * t + 2 * c[2]) * t + c[1]; };
     // Breakpoints: 0, the real critical points inside (0, 1), 1.
     Real bp[4];
     int nb   = 0;
@@ -676,7 +683,7 @@ int cubic_roots_01(Real const c[4], Real* roots)
     if (qa != 0)
     {
         Real const disc = qb * qb - 4 * qa * qc;
-        if (disc >= 0)
+        if (disc > 0)
         {
             Real const sq = std::sqrt(disc);
             Real const r0 = (-qb - sq) / (2 * qa), r1 = (-qb + sq) / (2 * qa);
@@ -695,25 +702,37 @@ int cubic_roots_01(Real const c[4], Real* roots)
     {
         Real lo = bp[k], hi = bp[k + 1];
         Real flo = f(lo), fhi = f(hi);
-        if (flo == 0)
-        {
-            if (n == 0 || roots[n - 1] != lo)
-                roots[n++] = lo;
-            continue;
-        }
-        if (fhi == 0)
-        {
-            roots[n++] = hi;
-            continue;
-        }
         if ((flo < 0) == (fhi < 0))
             continue;
+        // Newton from the middle of the piece, clamped to it, while it moves (at most 16 steps).
+        Real xr = Real(0.5) * (lo + hi);
+        bool done = false;
+        for (int it = 0; it < 16; ++it)
+        {
+            Real const xn = std::min(std::max(xr - f(xr) / df(xr), lo), hi);
+            if (xn == xr)
+            {
+                done = true;
+                break;
+            }
+            xr = xn;
+        }
+        if (done && std::isfinite(xr))
+        {
+            roots[n++] = xr;
+            continue;
+        }
         for (int it = 0; it < 200 && hi - lo > 0; ++it)
         {
             Real const mid = Real(0.5) * (lo + hi);
             if (mid <= lo || mid >= hi)
                 break;
             Real const fm = f(mid);
+            if (fm == 0)
+            {
+                lo = hi = mid;
+                break;
+            }
             if ((fm < 0) == (flo < 0))
                 lo = mid, flo = fm;
             else
@@ -747,6 +766,95 @@ Real point_triangle_ccd(V3 xt, V3 at, V3 bt, V3 ct, V3 x, V3 a, V3 b, V3 c)
             return t;
     }
     return -1;
+}
+
+// Closest points of two lines p1 + a (q1 - p1) and p2 + b (q2 - p2) (geometry/ClosestPointQueries.h
+// Lines, 448-485): a line whose squared length is <= eps is a point; lines whose Gram determinant
+// lies in [-eps, eps] are parallel and keep a = 0.
+void closest_on_lines(V3 p1, V3 q1, V3 p2, V3 q2, Real eps, Real& a, Real& b)
+{
+    V3 const d1 = sub(q1, p1), d2 = sub(q2, p2), r = sub(p1, p2);
+    Real const d1sq = dot(d1, d1), d2sq = dot(d2, d2), d12 = dot(d1, d2);
+    Real const gram = d1sq * d2sq - d12 * d12;
+    bool const point1 = d1sq <= eps, point2 = d2sq <= eps, parallel = -eps <= gram && gram <= eps;
+    a = 0;
+    b = 0;
+    if (point1 && point2)
+        return;
+    if (point1)
+        b = dot(r, d2) / d2sq;
+    else if (point2)
+        a = -dot(r, d1) / d1sq;
+    else
+    {
+        if (!parallel)
+            a = dot(r, sub(mul(d12, d2), mul(d2sq, d1))) / gram;
+        b = dot(add(r, mul(a, d1)), d2) / d2sq;
+    }
+}
+
+// Edge-edge CCD (geometry/EdgeEdgeCcd.h:125-161): the candidate times are the roots in [0, 1] of
+// the cubic ((q1 - p1) x (q2 - p2)) . (p2 - p1), visited in increasing order; at each, the closest
+// points of the two lines are taken with eps = DBL_MIN and the root is a hit when both parameters
+// lie in [0, 1] and the squared distance of the two points is <= DBL_MIN (only crossings that are
+// exact in floating point count).  As written, the cubic's generator (python/geometry/ccd.py:55,
+// expanded in EdgeEdgeCcd.h's EdgeEdgeCcdUnivariatePolynomial) moves the second edge's far end
+// as q2(t) = Q2T + t (Q2 - P2T) instead of Q2T + t (Q2 - Q2T), so q2 - p2 = (Q2T - P2T) +
+// t (Q2 - P2); the hit test at each root uses the true positions.  Both are kept as written.
+// Returns t (-1: none) and the two edge parameters (on a miss, those of the last root visited,
+// as in the reference's result vector; 0 without roots).
+Real edge_edge_ccd(V3 p1t, V3 q1t, V3 p2t, V3 q2t, V3 p1, V3 q1, V3 p2, V3 q2, Real& u, Real& v)
+{
+    V3 const A0 = sub(q1t, p1t), B0 = sub(q2t, p2t), C0 = sub(p2t, p1t);
+    V3 const A1 = sub(sub(q1, p1), A0), B1 = sub(q2, p2), C1 = sub(sub(p2, p1), C0);
+    V3 const n0 = cross(A0, B0);
+    V3 const n1 = add(cross(A0, B1), cross(A1, B0));
+    V3 const n2 = cross(A1, B1);
+    Real const coeff[4] = {dot(n0, C0), dot(n0, C1) + dot(n1, C0), dot(n1, C1) + dot(n2, C0), dot(n2, C1)};
+    Real roots[3];
+    int const nr = cubic_roots_01(coeff, roots);
+    Real constexpr tiny = std::numeric_limits<Real>::min();
+    for (int k = 0; k < nr; ++k)
+    {
+        Real const t = roots[k];
+        auto lerp    = [&](V3 a0, V3 a1) { return add(a0, mul(t, sub(a1, a0))); };
+        V3 const P1 = lerp(p1t, p1), Q1 = lerp(q1t, q1), P2 = lerp(p2t, p2), Q2 = lerp(q2t, q2);
+        Real a, b;
+        closest_on_lines(P1, Q1, P2, Q2, tiny, a, b);
+        V3 const d    = sub(add(P1, mul(a, sub(Q1, P1))), add(P2, mul(b, sub(Q2, P2))));
+        bool const in = a >= 0 && a <= 1 && b >= 0 && b <= 1;
+        u = a;
+        v = b;
+        if (in && dot(d, d) <= tiny)
+            return t;
+    }
+    if (nr == 0)
+        u = v = 0;
+    return -1;
+}
+
+struct Box
+{
+    V3 lo, hi;
+};
+
+Box swept_box(double const* xt, double const* x, int32_t const* idx, int n)
+{
+    Box b{at(xt, idx[0]), at(xt, idx[0])};
+    for (int k = 0; k < n; ++k)
+        for (double const* src : {xt, x})
+        {
+            V3 const p = at(src, idx[k]);
+            b.lo = {std::min(b.lo.x, p.x), std::min(b.lo.y, p.y), std::min(b.lo.z, p.z)};
+            b.hi = {std::max(b.hi.x, p.x), std::max(b.hi.y, p.y), std::max(b.hi.z, p.z)};
+        }
+    return b;
+}
+
+bool boxes_overlap(Box const& a, Box const& b)
+{
+    return a.lo.x <= b.hi.x && a.lo.y <= b.hi.y && a.lo.z <= b.hi.z && b.lo.x <= a.hi.x && b.lo.y <= a.hi.y &&
+           b.lo.z <= a.hi.z;
 }
 
 } // namespace
@@ -807,6 +915,129 @@ int orc_ccd_vertex_triangle(
         tri[q] = bestF;
     }
     return 0;
+}
+
+// Every vertex-triangle CCD hit (sim/contact/MultibodyMeshMixedCcdDcd.h
+// ReportVertexTriangleCcdContacts 884-932): collision vertex V[q] of one body against each triangle
+// of another body whose swept box overlaps the vertex's swept box; vertices flagged in
+// penetrating[] (nullable; the discrete half's vertices) are skipped.  Pairs come out ordered by
+// (vertex, triangle); at most capacity are written, the return value is the total count.
+int64_t orc_ccd_vertex_triangle_pairs(
+    int32_t nV,
+    double const* xt,
+    double const* x,
+    int32_t nF,
+    int32_t const* F,
+    int32_t nCV,
+    int32_t const* V,
+    int32_t const* B,
+    uint8_t const* penetrating,
+    int64_t capacity,
+    int32_t* vertex,
+    int32_t* triangle,
+    double* toi)
+{
+    (void)nV;
+    std::vector<Box> fb(static_cast<size_t>(nF));
+    for (int32_t f = 0; f < nF; ++f)
+        fb[size_t(f)] = swept_box(xt, x, F + 3 * size_t(f), 3);
+    int64_t n = 0;
+    for (int32_t q = 0; q < nCV; ++q)
+    {
+        int32_t const i = V[q];
+        if (penetrating && penetrating[i])
+            continue;
+        Box const vb = swept_box(xt, x, &i, 1);
+        V3 const p0 = at(xt, i), p1 = at(x, i);
+        for (int32_t f = 0; f < nF; ++f)
+        {
+            int32_t const* t = F + 3 * size_t(f);
+            if (B[t[0]] == B[i] || !boxes_overlap(vb, fb[size_t(f)]))
+                continue;
+            Real const tc = point_triangle_ccd(p0, at(xt, t[0]), at(xt, t[1]), at(xt, t[2]), p1, at(x, t[0]), at(x, t[1]), at(x, t[2]));
+            if (tc < 0)
+                continue;
+            if (n < capacity)
+            {
+                vertex[n]   = i;
+                triangle[n] = f;
+                toi[n]      = tc;
+            }
+            ++n;
+        }
+    }
+    return n;
+}
+
+// Every edge-edge CCD hit (sim/contact/MultibodyMeshMixedCcdDcd.h ReportEdgeEdgeCcdContacts
+// 934-985): collision edges E[2 e ..] of two different bodies whose swept boxes overlap, neither
+// with an end point flagged in penetrating[] (nullable).  Each unordered pair is visited once, with
+// the edge of the lower body first (the reference visits each overlapping body pair once, in its
+// body tree's order); pairs come out ordered by (first edge, second edge).  tuv[3 n ..] = time of
+// impact and the parameters along the first and second edge.  At most capacity are written; the
+// return value is the total count.
+int64_t orc_ccd_edge_edge(
+    int32_t nV,
+    double const* xt,
+    double const* x,
+    int32_t nE,
+    int32_t const* E,
+    int32_t const* B,
+    uint8_t const* penetrating,
+    int64_t capacity,
+    int32_t* ei,
+    int32_t* ej,
+    double* tuv)
+{
+    (void)nV;
+    std::vector<Box> eb(static_cast<size_t>(nE));
+    for (int32_t e = 0; e < nE; ++e)
+        eb[size_t(e)] = swept_box(xt, x, E + 2 * size_t(e), 2);
+    auto masked = [&](int32_t const* e) { return penetrating && (penetrating[e[0]] || penetrating[e[1]]); };
+    int64_t n = 0;
+    for (int32_t a = 0; a < nE; ++a)
+    {
+        int32_t const* ea = E + 2 * size_t(a);
+        if (masked(ea))
+            continue;
+        for (int32_t b = 0; b < nE; ++b)
+        {
+            int32_t const* e2 = E + 2 * size_t(b);
+            if (B[ea[0]] >= B[e2[0]] || masked(e2) || !boxes_overlap(eb[size_t(a)], eb[size_t(b)]))
+                continue;
+            Real u, v;
+            Real const tc = edge_edge_ccd(at(xt, ea[0]), at(xt, ea[1]), at(xt, e2[0]), at(xt, e2[1]), at(x, ea[0]),
+                                          at(x, ea[1]), at(x, e2[0]), at(x, e2[1]), u, v);
+            if (tc < 0)
+                continue;
+            if (n < capacity)
+            {
+                ei[n]          = a;
+                ej[n]          = b;
+                tuv[3 * n]     = tc;
+                tuv[3 * n + 1] = u;
+                tuv[3 * n + 2] = v;
+            }
+            ++n;
+        }
+    }
+    return n;
+}
+
+// One edge-edge CCD query on explicit end points (12 doubles each at t and at t + 1, ordered
+// p1, q1, p2, q2); out = (t, u, v), t = -1 when the edges do not cross.
+void orc_edge_edge_ccd(double const* xt, double const* x, double* out)
+{
+    Real u, v;
+    out[0] = edge_edge_ccd(at(xt, 0), at(xt, 1), at(xt, 2), at(xt, 3), at(x, 0), at(x, 1), at(x, 2), at(x, 3), u, v);
+    out[1] = u;
+    out[2] = v;
+}
+
+// One vertex-triangle CCD query on explicit end points (x, a, b, c at t and at t + 1); returns t or -1.
+double orc_point_triangle_ccd(double const* xt, double const* x)
+{
+    return point_triangle_ccd(at(xt, 0), at(xt, 1), at(xt, 2), at(xt, 3), at(x, 0), at(x, 1), at(x, 2), at(x, 3));
 }
 
 } // extern "C"

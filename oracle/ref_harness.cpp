@@ -21,7 +21,9 @@
 using std::max;
 using std::min;
 
+#include "pbat/geometry/EdgeEdgeCcd.h"
 #include "pbat/geometry/Morton.h"
+#include "pbat/geometry/PointTriangleCcd.h"
 #include "pbat/graph/Color.h"
 #include "pbat/physics/StableNeoHookeanEnergy.h"
 #include "pbat/sim/vbd/Kernels.h"
@@ -395,6 +397,38 @@ int ref_run(orc_problem const* Pp, double* x, double* v, double* vprev, double d
             }
         }
     return 0;
+}
+
+// The reference's own CCD queries (geometry/PointTriangleCcd.h:125-160, geometry/EdgeEdgeCcd.h:
+// 125-161) in FP64.  xt, x: four points at the start and the end of the step, 3 doubles each
+// (point-triangle: x, a, b, c; edge-edge: p1, q1, p2, q2).  out: the reference's result vector
+// (point-triangle: t and three barycentric coordinates; edge-edge: t and two edge parameters).
+void ref_point_triangle_ccd(double const* xt, double const* x, double* out)
+{
+    mini::SVector<double, 3> P[8];
+    for (int k = 0; k < 4; ++k)
+        for (int r = 0; r < 3; ++r)
+        {
+            P[k](r)     = xt[3 * k + r];
+            P[4 + k](r) = x[3 * k + r];
+        }
+    mini::SVector<double, 4> const r = pbat::geometry::PointTriangleCcd(P[0], P[1], P[2], P[3], P[4], P[5], P[6], P[7]);
+    for (int k = 0; k < 4; ++k)
+        out[k] = r(k);
+}
+
+void ref_edge_edge_ccd(double const* xt, double const* x, double* out)
+{
+    mini::SVector<double, 3> P[8];
+    for (int k = 0; k < 4; ++k)
+        for (int r = 0; r < 3; ++r)
+        {
+            P[k](r)     = xt[3 * k + r];
+            P[4 + k](r) = x[3 * k + r];
+        }
+    mini::SVector<double, 3> const r = pbat::geometry::EdgeEdgeCcd(P[0], P[1], P[2], P[3], P[4], P[5], P[6], P[7]);
+    for (int k = 0; k < 3; ++k)
+        out[k] = r(k);
 }
 
 } // extern "C"

@@ -3,7 +3,8 @@
 Run in a checkout where the reference sources are available (``make -C oracle ref`` builds
 ``oracle/_ref/libpbat_ref.so`` from them):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # every fixture
+    python tests/golden/make_golden.py ccd      # only ccd.npz
 
 Every fixture is produced by calling the reference's header-only kernels through the harness
 (oracle/ref_harness.cpp), on seeded inputs, so the oracle can be pinned on machines without the
@@ -220,11 +221,65 @@ def contact_cases(R, rng):
     np.savez_compressed(HERE / "contact.npz", **{k: np.array(v) for k, v in out.items()})
 
 
-def main():
+def _ccd_families(rng, n):
+    """Seeded CCD inputs, four points at the start (xt) and the end (x) of the step, in four
+    families: generic random motions; exact dyadic crossings (the reference doctests' configurations
+    under random power-of-two scales, integer shifts and axis permutations, where the arithmetic is
+    exact); the same crossings with the second edge also turning (exact at the crossing time, where
+    the reference's edge-edge cubic misses them as written); near misses offset by 1e-9."""
+    g_pt = np.array([[0, 0.25, 0.25], [1, 0, 0], [1, 1, 0], [1, 0, 1]], float)
+    d_pt = np.array([[1, 0, 0], [-1, 0, 0], [-1, 0, 0], [-1, 0, 0]], float)
+    g_ee = np.array([[0, 0, 0], [0, 1, 1], [1, 0, 1], [1, 1, 0]], float)
+    d_ee = np.array([[1, 0, 0], [1, 0, 0], [-1, 0, 0], [-1, 0, 0]], float)
+    fam = {"pt": [], "ee": []}
+    for key, g0, d0 in (("pt", g_pt, d_pt), ("ee", g_ee, d_ee)):
+        for k in range(n):
+            kind = k % 4
+            if kind == 0:
+                xt = rng.uniform(-1, 1, (4, 3))
+                x = xt + rng.uniform(-1, 1, (4, 3))
+            else:
+                perm = rng.permutation(3)
+                s = 2.0 ** int(rng.integers(-3, 4))
+                sh = rng.integers(-8, 8, 3).astype(float)
+                xt = (g0 * s)[:, perm] + sh
+                x = xt + (d0 * s)[:, perm]
+                if kind == 2:
+                    turn = (rng.integers(-2, 3, 3) * s)[perm].astype(float)
+                    xt[3] -= 0.5 * turn  # the last point turns about the crossing time t = 1/2
+                    x[3] += 0.5 * turn
+                elif kind == 3:
+                    x[0] += 1e-9 * rng.standard_normal(3)
+            fam[key].append((np.ascontiguousarray(xt), np.ascontiguousarray(x)))
+    return fam
+
+
+def ccd_cases(R, rng):
+    """The reference's own point-triangle and edge-edge CCD queries (geometry/PointTriangleCcd.h,
+    geometry/EdgeEdgeCcd.h) in FP64 on the families of _ccd_families."""
+    fam = _ccd_families(rng, 400)
+    out = {}
+    for key, fn, width in (("pt", R.ref_point_triangle_ccd, 4), ("ee", R.ref_edge_edge_ccd, 3)):
+        xs, xe, r = [], [], []
+        for xt, x in fam[key]:
+            o = np.zeros(width)
+            fn(xt, x, o)
+            xs.append(xt)
+            xe.append(x)
+            r.append(o)
+        out[key + "_xt"], out[key + "_x"], out[key + "_r"] = np.array(xs), np.array(xe), np.array(r)
+    np.savez_compressed(HERE / "ccd.npz", **out)
+
+
+def main(only=None):
     O.build_oracle(ref=True)
     R = O.ref()
     if R is None:
         raise SystemExit("the reference harness was not built")
+    if only == "ccd":
+        ccd_cases(R, np.random.default_rng(20261204))
+        print("fixtures written to", HERE)
+        return
     rng = np.random.default_rng(20261203)
     snh(R, rng)
     vertex_solves(R, rng)
@@ -234,8 +289,9 @@ def main():
     trajectories(R)
     morton_codes(R, rng)
     contact_cases(R, rng)
+    ccd_cases(R, np.random.default_rng(20261204))
     print("fixtures written to", HERE)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

@@ -120,6 +120,16 @@ def lib():
         L.orc_ccd_vertex_triangle.restype = C.c_int
         L.orc_ccd_vertex_triangle.argtypes = [C.c_int32, _f64p, _f64p, C.c_int32, _i32p, C.c_int32, _i32p, _i32p,
                                               _f64p, _i32p]
+        _u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+        L.orc_ccd_vertex_triangle_pairs.restype = C.c_int64
+        L.orc_ccd_vertex_triangle_pairs.argtypes = [C.c_int32, _f64p, _f64p, C.c_int32, _i32p, C.c_int32, _i32p,
+                                                    _i32p, _u8p, C.c_int64, _i32p, _i32p, _f64p]
+        L.orc_ccd_edge_edge.restype = C.c_int64
+        L.orc_ccd_edge_edge.argtypes = [C.c_int32, _f64p, _f64p, C.c_int32, _i32p, _i32p, _u8p, C.c_int64,
+                                        _i32p, _i32p, _f64p]
+        L.orc_edge_edge_ccd.argtypes = [_f64p, _f64p, _f64p]
+        L.orc_point_triangle_ccd.restype = C.c_double
+        L.orc_point_triangle_ccd.argtypes = [_f64p, _f64p]
         L.orc_dcd_contacts.restype = C.c_int
         L.orc_dcd_contacts.argtypes = [C.c_int32, _f64p, C.c_int32, _i32p, C.c_int32, _i32p, C.c_int32, _i32p,
                                        _i32p, _i32p, _i32p, _f64p]
@@ -156,6 +166,8 @@ def ref():
         fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
         L.ref_vertex_triangle_contact_d.restype = C.c_double
         L.ref_vertex_triangle_contact_d.argtypes = [_f64p] * 4 + [C.c_double] * 4 + [_f64p, _f64p]
+        L.ref_point_triangle_ccd.argtypes = [_f64p, _f64p, _f64p]
+        L.ref_edge_edge_ccd.argtypes = [_f64p, _f64p, _f64p]
         L.ref_vertex_triangle_contact.restype = C.c_float
         L.ref_vertex_triangle_contact.argtypes = [
             fp, fp, fp, fp, C.c_float, C.c_float, C.c_float, C.c_float, fp, fp,
@@ -446,6 +458,92 @@ def dcd_contacts(x, T, F, V, B):
     if rc != 0:
         raise RuntimeError("orc_dcd_contacts failed")
     return body, nearest, d2
+
+
+def edge_edge_ccd(xt, x):
+    """One edge-edge CCD query of the oracle (oracle/contact_oracle.cpp edge_edge_ccd): xt, x are
+    4 x 3 (p1, q1, p2, q2 at the start and the end of the step); returns (t, u, v), t = -1 for no
+    crossing."""
+    out = np.zeros(3)
+    lib().orc_edge_edge_ccd(np.ascontiguousarray(xt, dtype=np.float64), np.ascontiguousarray(x, dtype=np.float64), out)
+    return out
+
+
+def point_triangle_ccd(xt, x):
+    """One point-triangle CCD query of the oracle: xt, x are 4 x 3 (x, a, b, c); returns t or -1."""
+    return lib().orc_point_triangle_ccd(np.ascontiguousarray(xt, dtype=np.float64),
+                                        np.ascontiguousarray(x, dtype=np.float64))
+
+
+def _grow(call):
+    """Runs a capacity-bounded pair query twice when the first capacity was short."""
+    cap = 1024
+    while True:
+        n, out = call(cap)
+        if n <= cap:
+            return n, out
+        cap = int(n)
+
+
+def ccd_vertex_triangle_pairs(xt, x, F, V, B, penetrating=None):
+    """Every vertex-triangle CCD hit of the CPU multibody detector (oracle/contact_oracle.cpp
+    orc_ccd_vertex_triangle_pairs): (vertex, triangle, time of impact) arrays, ordered by
+    (vertex, triangle).  penetrating: optional bool per vertex (skipped vertices)."""
+    xt = np.ascontiguousarray(xt, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    F = np.ascontiguousarray(F, dtype=np.int32)
+    V = np.ascontiguousarray(V, dtype=np.int32)
+    B = np.ascontiguousarray(B, dtype=np.int32)
+    mask = np.ascontiguousarray(np.zeros(x.shape[0], bool) if penetrating is None else penetrating, dtype=np.uint8)
+
+    def call(cap):
+        v, f, t = np.empty(cap, np.int32), np.empty(cap, np.int32), np.empty(cap, np.float64)
+        n = lib().orc_ccd_vertex_triangle_pairs(x.shape[0], xt, x, F.shape[0], F, V.size, V, B, mask, cap, v, f, t)
+        return n, (v, f, t)
+
+    n, (v, f, t) = _grow(call)
+    return v[:n].copy(), f[:n].copy(), t[:n].copy()
+
+
+def ccd_edge_edge(xt, x, E, B, penetrating=None):
+    """Every edge-edge CCD hit of the CPU multibody detector (oracle/contact_oracle.cpp
+    orc_ccd_edge_edge): (first edge, second edge, (t, u, v)) with the first edge on the lower
+    body, ordered by (first, second).  E: nE x 2 collision edges; penetrating as above."""
+    xt = np.ascontiguousarray(xt, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    E = np.ascontiguousarray(E, dtype=np.int32)
+    B = np.ascontiguousarray(B, dtype=np.int32)
+    mask = np.ascontiguousarray(np.zeros(x.shape[0], bool) if penetrating is None else penetrating, dtype=np.uint8)
+
+    def call(cap):
+        a, b, r = np.empty(cap, np.int32), np.empty(cap, np.int32), np.empty((cap, 3), np.float64)
+        n = lib().orc_ccd_edge_edge(x.shape[0], xt, x, E.shape[0], E, B, mask, cap, a, b, r)
+        return n, (a, b, r)
+
+    n, (a, b, r) = _grow(call)
+    return a[:n].copy(), b[:n].copy(), r[:n].copy()
+
+
+def multibody_all_pairs(XT, X, XK, V, E, F, T, B):
+    """The CPU multibody detector's active-set update (sim/contact/MultibodyMeshMixedCcdDcd.h
+    UpdateActiveSet 561-583; the Python binding's all_pairs): the discrete half at XK marks
+    penetrating vertices and reports each with its nearest triangles of the body it penetrates;
+    the continuous half on XT -> X reports every vertex-triangle hit of the other collision
+    vertices and every edge-edge hit of edges without a penetrating end point.  Returns
+    (VTv, VTf, EEei, EEej) like the binding; the order is the oracle's (sets match the
+    reference's)."""
+    body, nearest, _ = dcd_contacts(XK, T, F, V, B)
+    pen = np.zeros(np.asarray(XK).shape[0], bool)
+    pen[np.asarray(V)[body >= 0]] = True
+    vt_v, vt_f = [], []
+    for q in np.nonzero(body >= 0)[0]:
+        for f in nearest[q][nearest[q] >= 0]:
+            vt_v.append(int(V[q]))
+            vt_f.append(int(f))
+    cv, cf, _ = ccd_vertex_triangle_pairs(XT, X, F, V, B, pen)
+    ei, ej, _ = ccd_edge_edge(XT, X, E, B, pen)
+    return (np.array(vt_v + cv.tolist(), np.int64), np.array(vt_f + cf.tolist(), np.int64),
+            ei.astype(np.int64), ej.astype(np.int64))
 
 
 def ccd_vertex_triangle(xt, x, F, V, B):

@@ -193,3 +193,148 @@ def test_vertex_triangle_ccd_oracle():
             hits += 1
             assert abs(got - want) < 1e-3
     assert hits > 10
+
+
+# ---------------------------------------------------------------------------------------------
+# Continuous half of the CPU multibody detector: point-triangle and edge-edge CCD.
+
+def test_ccd_reference_doctest_cases():
+    """Known answers of the reference's doctests (geometry/PointTriangleCcd.cpp:13-31,
+    geometry/EdgeEdgeCcd.cpp:13-33): both crossings happen at t = 1/2, the edge-edge one at the
+    middle of both edges."""
+    pt_t = np.array([[0, 0.25, 0.25], [1, 0, 0], [1, 1, 0], [1, 0, 1]], float)
+    pt_x = pt_t + np.array([[1, 0, 0], [-1, 0, 0], [-1, 0, 0], [-1, 0, 0]], float)
+    assert O.point_triangle_ccd(pt_t, pt_x) == 0.5
+    ee_t = np.array([[0, 0, 0], [0, 1, 1], [1, 0, 1], [1, 1, 0]], float)
+    ee_x = ee_t + np.array([[1, 0, 0], [1, 0, 0], [-1, 0, 0], [-1, 0, 0]], float)
+    np.testing.assert_array_equal(O.edge_edge_ccd(ee_t, ee_x), [0.5, 0.5, 0.5])
+
+
+def _check_ccd_against(xts, xs, rs, pt):
+    """Oracle CCD against the reference's results.  Point-triangle: hit or no hit everywhere, times
+    of impact to 1e-9.  Edge-edge: both return the parameters of the last root visited, which agree
+    to 1e-9 everywhere (the same roots are visited); hit or no hit agrees everywhere but on near
+    misses (every fourth case, index % 4 == 3: one end point moved by 1e-9), where the hit test
+    (closest distance exactly 0 in floating point) is decided by rounding: there the cubic is
+    nearly degenerate and last-bit differences of its coefficients move the root by ~1e-12."""
+    decided_by_rounding = 0
+    for i, (xt, x, r) in enumerate(zip(xts, xs, rs)):
+        if pt:
+            t = O.point_triangle_ccd(xt, x)
+            assert (t >= 0) == (r[0] >= 0), (i, t, r)
+            if t >= 0:
+                assert abs(t - r[0]) <= 1e-9
+            continue
+        got = O.edge_edge_ccd(xt, x)
+        np.testing.assert_allclose(got[1:], r[1:], rtol=0, atol=1e-9)
+        if (got[0] >= 0) != (r[0] >= 0):
+            assert i % 4 == 3, (i, got, r)
+            decided_by_rounding += 1
+        elif got[0] >= 0:
+            assert abs(got[0] - r[0]) <= 1e-9
+    assert decided_by_rounding <= len(rs) // 8
+    return decided_by_rounding
+
+
+def test_ccd_oracle_matches_reference_fixture():
+    """The oracle's CCD queries against the reference's own (fixture made from its FP64 build):
+    generic motions, exact dyadic crossings, crossings whose second edge turns (which the
+    reference's edge-edge cubic misses as written) and near misses (the agreement bar is in
+    _check_ccd_against)."""
+    g = np.load(GOLD / "ccd.npz")
+    assert (g["ee_r"][:, 0] >= 0).sum() > 100 and (g["pt_r"][:, 0] >= 0).sum() > 300
+    _check_ccd_against(g["pt_xt"], g["pt_x"], g["pt_r"], pt=True)
+    _check_ccd_against(g["ee_xt"], g["ee_x"], g["ee_r"], pt=False)
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference harness not built")
+def test_ccd_oracle_matches_reference_directly():
+    import sys
+    sys.path.insert(0, str(GOLD))
+    import make_golden
+
+    R = O.ref()
+    fam = make_golden._ccd_families(np.random.default_rng(99), 2000)
+    for key, fn, width in (("pt", R.ref_point_triangle_ccd, 4), ("ee", R.ref_edge_edge_ccd, 3)):
+        rs = []
+        for xt, x in fam[key]:
+            o = np.zeros(width)
+            fn(xt, x, o)
+            rs.append(o)
+        _check_ccd_against([a for a, _ in fam[key]], [b for _, b in fam[key]], rs, pt=key == "pt")
+
+
+def _two_box_scene():
+    """Two 2x2x2-hex boxes on dyadic coordinates: box 0 fixed on [0, 1]^3, box 1 above it, offset
+    by (1/4, 3/8) in x and y, falling by 1/2 during the step; its bottom face reaches box 0's top
+    face at t = 1/4, where axis-aligned edges cross exactly."""
+    X0, T0 = meshgen.hex_grid(2, 2, 2, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
+    X1, T1 = meshgen.hex_grid(2, 2, 2, (0.25, 0.375, 1.125), (1.25, 1.375, 2.125))
+    X = np.vstack([X0, X1]).astype(np.float64)
+    T = np.vstack([T0, T1 + X0.shape[0]]).astype(np.int32)
+    B = np.repeat([0, 1], [X0.shape[0], X1.shape[0]]).astype(np.int32)
+    F = meshgen.boundary_faces(T).astype(np.int32)
+    E = np.unique(np.sort(np.vstack([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]]), axis=1), axis=0).astype(np.int32)
+    V = np.unique(F).astype(np.int32)
+    Xe = X.copy()
+    Xe[B == 1, 2] -= 0.5
+    return X, Xe, T, F, E, V, B
+
+
+def test_multibody_edge_edge_pairs_match_pairwise_queries():
+    """orc_ccd_edge_edge over two boxes' surface edges: the box prefilter and the body rule lose no
+    hit of the pairwise query run over every cross-body pair, the faces' exact crossings are found
+    at t = 1/4, and edges with a penetrating end point drop out."""
+    X, Xe, T, F, E, V, B = _two_box_scene()
+    ei, ej, tuv = O.ccd_edge_edge(X, Xe, E, B)
+
+    def brute(mask):
+        out = {}
+        for a in range(E.shape[0]):
+            for b in range(E.shape[0]):
+                if B[E[a, 0]] != 0 or B[E[b, 0]] != 1 or mask[E[a]].any() or mask[E[b]].any():
+                    continue
+                r = O.edge_edge_ccd(np.vstack([X[E[a]], X[E[b]]]), np.vstack([Xe[E[a]], Xe[E[b]]]))
+                if r[0] >= 0:
+                    out[(a, b)] = r
+        return out
+
+    want = brute(np.zeros(X.shape[0], bool))
+    assert len(want) >= 4
+    assert set(zip(ei.tolist(), ej.tolist())) == set(want)
+    for a, b, r in zip(ei, ej, tuv):
+        np.testing.assert_array_equal(r, want[(a, b)])
+    assert (tuv[:, 0] == 0.25).sum() >= 4  # the two faces meet; later crossings lie inside box 0
+    # Penetrating vertices: box 1's bottom layer.
+    pen = np.zeros(X.shape[0], bool)
+    pen[(B == 1) & (X[:, 2] == 1.125)] = True
+    ei2, ej2, _ = O.ccd_edge_edge(X, Xe, E, B, pen)
+    assert set(zip(ei2.tolist(), ej2.tolist())) == set(brute(pen))
+    assert not pen[E[ei2]].any() and not pen[E[ej2]].any()
+    assert len(ei2) < len(ei)
+
+
+def test_multibody_all_pairs_composition():
+    """The active-set update of the CPU multibody detector (UpdateActiveSet): the discrete half's
+    vertices (box 1 moved at XK by 3/4 in x and sunk 1/16 into box 0's corner) report their nearest
+    triangles and take no part in the continuous half; every continuous vertex-triangle pair is a
+    hit of the pairwise query."""
+    X, Xe, T, F, E, V, B = _two_box_scene()
+    XK = X.copy()
+    XK[B == 1] += [0.75, 0.0, -0.1875]
+    VTv, VTf, EEei, EEej = O.multibody_all_pairs(X, Xe, XK, V, E, F, T, B)
+    body, nearest, _ = O.dcd_contacts(XK, T, F, V, B)
+    pen_vertices = set(V[body >= 0].tolist())
+    assert len(pen_vertices) > 0
+    n_dcd = sum(int((nearest[q] >= 0).sum()) for q in np.nonzero(body >= 0)[0])
+    assert set(VTv[:n_dcd].tolist()) == pen_vertices
+    for v, f in zip(VTv[n_dcd:], VTf[n_dcd:]):
+        assert v not in pen_vertices and B[v] != B[F[f, 0]]
+        assert O.point_triangle_ccd(np.vstack([X[v], X[F[f]]]), np.vstack([Xe[v], Xe[F[f]]])) >= 0
+    mask = np.zeros(X.shape[0], bool)
+    mask[list(pen_vertices)] = True
+    ei, ej, _ = O.ccd_edge_edge(X, Xe, E, B, mask)
+    assert set(zip(EEei.tolist(), EEej.tolist())) == set(zip(ei.tolist(), ej.tolist()))
+    for a, b in zip(EEei, EEej):
+        assert not set(E[a].tolist()) & pen_vertices and not set(E[b].tolist()) & pen_vertices
+    assert len(VTv) > n_dcd
