@@ -397,6 +397,7 @@ def run_accelerated(args, pbat, torch, kind):
         # Broyden is a CPU-integrator strategy in the reference (the GPU integrator runs plain VBD).
         cls = pbat.sim.vbd.Integrator if accel == "broyden" else pbat.gpu.vbd.Integrator
         I = cls(d.construct())
+        I.autotune(dt, iters, 1)  # lanes and block size per strategy; the state is restored
         x0, v0 = I.x.copy(), I.v.copy()
         I.step(dt, iters, 1)
         g = I.gradient(dt).reshape(-1, 3)
@@ -580,7 +581,8 @@ def main():
     ap.add_argument("--nx", type=int, default=160)
     ap.add_argument("--ny", type=int, default=40)
     ap.add_argument("--nz", type=int, default=40)
-    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--lanes", type=int, default=0, help="headline: lanes per vertex instead of autotuning")
+    ap.add_argument("--block", type=int, default=0, help="headline with --lanes: block size (default 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", dest="batch", action="store_true", default=True,
                     help="also measure the batched multi-mesh form against one launch per mesh")
@@ -639,26 +641,33 @@ def main():
     w = workload_beam(args)
     data = make_data(pbat, w)
     vbd = pbat.gpu.vbd.Integrator(data)
-    if args.lanes:
-        vbd.lanes_per_vertex = args.lanes
     L = _capi.lib()
     h = vbd.handle
+    dt, iters = 1 / 60, args.iterations
+    if args.lanes:
+        vbd.lanes_per_vertex = args.lanes
+        if args.block:
+            _capi.check(L.pbgb_vbd_set_block_size(h, args.block), h)
+        tuned = None
+    else:
+        # The integrator's own autotuner (public API; restores the state after each candidate).
+        t_lanes, t_block, t_ms = vbd.autotune(dt, iters, 1)
+        tuned = {"lanes": t_lanes, "block": t_block, "ms_per_step": t_ms}
     n_free = vbd.n_free
-    _capi.check(L.pbgb_vbd_set_sweep_timing(h, 1), h)
     sp = C.c_void_p()
     _capi.check(L.pbgb_vbd_stream(h, C.byref(sp)), h)
     stream = torch.cuda.ExternalStream(sp.value)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    dt, iters = 1 / 60, args.iterations
 
     for _ in range(args.warmup):
         vbd.step(dt, iters, 1)
     vbd.synchronize()
 
     # ---- device-resident throughput -------------------------------------------------------------
+    # The step graph carries no per-launch events here: event nodes between the colour launches
+    # would cut the programmatic-dependent-launch overlap of consecutive colours (5.07 -> 5.59 ms on
+    # the beam).  Per-launch times come from a separate instrumented pass below.
     t_total = 0.0
-    sweep_ms = 0.0
-    sweep_launches = 0
     ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     group.barrier()
@@ -672,11 +681,6 @@ def main():
             ev1[k].record(stream)
             vbd.synchronize()
             t_total += ev0[k].elapsed_time(ev1[k])
-            ms = C.c_double()
-            nl = C.c_int64()
-            _capi.check(L.pbgb_vbd_sweep_timing(h, C.byref(ms), C.byref(nl)), h)
-            sweep_ms += ms.value
-            sweep_launches += nl.value
         torch.cuda.synchronize()
     group.barrier()
     t_total = group.max(t_total)
@@ -686,8 +690,22 @@ def main():
 
     launches_per_step = vbd.launches_per_step(iters, 1)
     n_colors = vbd.n_colors
-    # ---- end to end through the C ABI with host buffers -----------------------------------------
+    # ---- instrumented pass: CUDA events around every colour launch (same stream) ----------------
+    _capi.check(L.pbgb_vbd_set_sweep_timing(h, 1), h)
+    sweep_ms, sweep_launches, instr_steps = 0.0, 0, max(3, args.steps // 10)
+    for k in range(instr_steps + 1):
+        flush.add_(1.0)
+        torch.cuda.synchronize()
+        vbd.step(dt, iters, 1)
+        vbd.synchronize()
+        ms = C.c_double()
+        nl = C.c_int64()
+        _capi.check(L.pbgb_vbd_sweep_timing(h, C.byref(ms), C.byref(nl)), h)
+        if k > 0:  # the first step re-captures the graph
+            sweep_ms += ms.value
+            sweep_launches += nl.value
     _capi.check(L.pbgb_vbd_set_sweep_timing(h, 0), h)
+    # ---- end to end through the C ABI with host buffers -----------------------------------------
     nV = vbd.n_vertices
     xh = torch.empty((nV, 3), dtype=torch.float32, pin_memory=True)
     vh = torch.empty((nV, 3), dtype=torch.float32, pin_memory=True)
@@ -711,9 +729,13 @@ def main():
     if rank == 0:
         peak, peak_kind = peak_hbm()
         bytes_per_iter = algorithmic_bytes(data)
-        n_sweeps_per_iter = sweep_launches / max(1, iters * args.steps)
+        sweeps_per_step = sweep_launches / max(1, instr_steps)
+        n_sweeps_per_iter = sweeps_per_step / max(1, iters)
         bytes_per_launch = bytes_per_iter / max(n_sweeps_per_iter, 1)
-        avg_launch_ms = sweep_ms / max(1, sweep_launches)
+        # Launch duration over the timed region: the event-timed step divided by its colour
+        # launches (an upper bound: the sweep is ~98% of the step, the rest is counted against it).
+        avg_launch_ms = ms_per_step / max(sweeps_per_step, 1)
+        instr_launch_ms = sweep_ms / max(1, sweep_launches)
         achieved = bytes_per_launch / (avg_launch_ms * 1e-3) / 1e9
         traffic = traffic_from_profiles()
         cpu = None if args.no_cpu_baseline else cpu_baseline(w, iters)
@@ -751,7 +773,12 @@ def main():
                          "peak_kind": peak_kind,
                          "kernel": "sweep_kernel (per-colour vertex Newton sweep)",
                          "algorithmic_bytes_per_launch": bytes_per_launch,
-                         "avg_launch_us": avg_launch_ms * 1e3},
+                         "avg_launch_us": avg_launch_ms * 1e3,
+                         "avg_launch_us_basis": "timed steps (CUDA events on the integrator's stream) / colour launches per step",
+                         "instrumented_launch_us": instr_launch_ms * 1e3,
+                         "instrumented_basis": "separate pass, CUDA events around each colour launch in the step graph"},
+            "launch_config": {"autotuned": tuned is not None, "lanes": vbd.lanes_per_vertex,
+                              "block": tuned["block"] if tuned else (args.block or 256)},
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "clocks": clocks.summary(),

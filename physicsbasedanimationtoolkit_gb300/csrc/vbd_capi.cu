@@ -1705,7 +1705,9 @@ class VbdSystem
         try
         {
             int32_t const laneSet[]  = {1, 2, 4, 8, 16, 32};
-            int32_t const blockSet[] = {64, 128, 256};
+            // Odd warp multiples as well: a colour's blocks then spread more evenly over the SMs
+            // (the beam's 33.6k-vertex colours: 601 blocks of 224 against 525 of 256 on 152 SMs).
+            int32_t const blockSet[] = {64, 96, 128, 160, 192, 224, 256};
             for (int32_t L : laneSet)
                 for (int32_t B : blockSet)
                 {
