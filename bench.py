@@ -411,11 +411,13 @@ def run_accelerated(args, pbat, torch, kind):
         stream = torch.cuda.ExternalStream(sp.value)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         I.synchronize()
+        torch.cuda.nvtx.range_push(f"timed_{accel or 'plain'}")  # lets ncu --nvtx-include select these steps
         e0.record(stream)
         for _ in range(args.steps):
             I.step(dt, iters, 1)
         e1.record(stream)
         I.synchronize()
+        torch.cuda.nvtx.range_pop()
         return e0.elapsed_time(e1) / args.steps, gnorm, I.n_free
 
     ms_a, g_a, n_free = measure(kind)
@@ -672,6 +674,7 @@ def main():
     ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     group.barrier()
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("timed_headline")  # lets ncu --nvtx-include select the timed steps
     with ClockSampler(local) as clocks:
         for k in range(args.steps):
             flush.add_(1.0)  # L2 flush outside the timed interval
@@ -682,6 +685,7 @@ def main():
             vbd.synchronize()
             t_total += ev0[k].elapsed_time(ev1[k])
         torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     group.barrier()
     t_total = group.max(t_total)
     ms_per_step = t_total / args.steps
@@ -738,6 +742,8 @@ def main():
         instr_launch_ms = sweep_ms / max(1, sweep_launches)
         achieved = bytes_per_launch / (avg_launch_ms * 1e-3) / 1e9
         traffic = traffic_from_profiles()
+        launch_config = {"autotuned": tuned is not None, "lanes": vbd.lanes_per_vertex,
+                         "block": tuned["block"] if tuned else (args.block or 256)}
         cpu = None if args.no_cpu_baseline else cpu_baseline(w, iters)
         batched = None
         if args.batch:
@@ -777,8 +783,7 @@ def main():
                          "avg_launch_us_basis": "timed steps (CUDA events on the integrator's stream) / colour launches per step",
                          "instrumented_launch_us": instr_launch_ms * 1e3,
                          "instrumented_basis": "separate pass, CUDA events around each colour launch in the step graph"},
-            "launch_config": {"autotuned": tuned is not None, "lanes": vbd.lanes_per_vertex,
-                              "block": tuned["block"] if tuned else (args.block or 256)},
+            "launch_config": launch_config,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "clocks": clocks.summary(),

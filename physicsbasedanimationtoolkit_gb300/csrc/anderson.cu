@@ -1,16 +1,13 @@
 // Anderson acceleration kernels (see anderson.cuh).
 #include "anderson.cuh"
+#include "dfloat.cuh"
 
 namespace pbgb {
 
 namespace {
 
 int constexpr kWindowThreads = 256;
-
-__device__ __forceinline__ double dot3(float4 a, float4 b)
-{
-    return double(a.x) * double(b.x) + double(a.y) * double(b.y) + double(a.z) * double(b.z);
-}
+int constexpr kWindowVerticesPerThread = 4;
 
 __global__ void anderson_start_kernel(AndersonParams p)
 {
@@ -24,25 +21,26 @@ __global__ void anderson_start_kernel(AndersonParams p)
     p.Fkm1[i] = p.step[i];
 }
 
-// One vertex per thread; 2 mk FP64 partial sums reduced per block (warp shuffles, then the warps'
-// sums in order), written to partials[block * 2 m + t].
+// kWindowVerticesPerThread vertices per thread (grid-stride); the mk + 1 products are carried as
+// double-float sums (exact products, compensated additions on the FP32 pipe), reduced over the
+// warp in the same form, converted to FP64 once per warp, and the warps' sums added in order:
+// partials[block * 2 m + t].
 __global__ void __launch_bounds__(kWindowThreads) anderson_window_kernel(AndersonParams p)
 {
     __shared__ double warpSums[kWindowThreads / 32][2 * kAndersonMaxWindow];
-    int const i  = blockIdx.x * blockDim.x + threadIdx.x;
     int const mk = p.mk;
     // Dots with the new column (accA, indices known at compile time so that the accumulators stay
     // in registers) and the new column's dot with F_k (accF).
-    double accA[kAndersonMaxWindow], accF = 0.0;
+    DFloat accA[kAndersonMaxWindow], accF = {0.f, 0.f};
 #pragma unroll
     for (int t = 0; t < kAndersonMaxWindow; ++t)
-        accA[t] = 0.0;
-    if (i < p.n)
+        accA[t] = {0.f, 0.f};
+    size_t const n = size_t(p.n);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x)
     {
         float4 const f  = p.step[i];
         float4 const fp = p.Fkm1[i];
         float4 const df = make_float4(f.x - fp.x, f.y - fp.y, f.z - fp.z, 0.f);
-        size_t const n  = size_t(p.n);
         if (!p.broyden)
         {
             // Broyden's X column was written by the previous update.
@@ -56,26 +54,21 @@ __global__ void __launch_bounds__(kWindowThreads) anderson_window_kernel(Anderso
 #pragma unroll
         for (int j = 0; j < kAndersonMaxWindow; ++j)
             if (j < mk)
-                accA[j] = dot3(j == p.dkl ? df : p.DF[size_t(j) * n + i], df);
-        accF = dot3(df, f);
+                accA[j] = df_add(accA[j], df_dot3(j == p.dkl ? df : p.DF[size_t(j) * n + i], df));
+        accF = df_add(accF, df_dot3(df, f));
     }
     int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int t = 0; t < kAndersonMaxWindow; ++t)
         if (t < mk)
         {
-            double a = accA[t];
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1)
-                a += __shfl_xor_sync(0xffffffffu, a, off);
+            DFloat const a = df_warp_sum(accA[t]);
             if (lane == 0)
-                warpSums[warp][t] = a;
+                warpSums[warp][t] = df_to_double(a);
         }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-        accF += __shfl_xor_sync(0xffffffffu, accF, off);
+    accF = df_warp_sum(accF);
     if (lane == 0)
-        warpSums[warp][mk] = accF;
+        warpSums[warp][mk] = df_to_double(accF);
     __syncthreads();
     if (threadIdx.x < mk + 1)
     {
@@ -243,6 +236,11 @@ __global__ void __launch_bounds__(kSolveThreads) anderson_solve_kernel(AndersonP
 
 __global__ void anderson_update_kernel(AndersonParams p)
 {
+    // The coefficients once per block in FP32 (the update itself is FP32).
+    __shared__ float alpha[kAndersonMaxWindow];
+    if (threadIdx.x < p.mk)
+        alpha[threadIdx.x] = float(p.alpha[threadIdx.x]);
+    __syncthreads();
     int const i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n)
         return;
@@ -254,7 +252,7 @@ __global__ void anderson_update_kernel(AndersonParams p)
         float cx = 0.f, cy = 0.f, cz = 0.f;
         for (int j = 0; j < p.mk; ++j)
         {
-            float const a   = float(p.alpha[j]);
+            float const a   = alpha[j];
             float4 const X  = p.DG[size_t(j) * n + i];
             float4 const Df = p.DF[size_t(j) * n + i];
             cx += a * (X.x + Df.x);
@@ -273,7 +271,7 @@ __global__ void anderson_update_kernel(AndersonParams p)
     }
     for (int j = 0; j < p.mk; ++j)
     {
-        float const a  = float(p.alpha[j]);
+        float const a  = alpha[j];
         float4 const d = p.DG[size_t(j) * n + i];
         u.x -= a * d.x;
         u.y -= a * d.y;
@@ -294,7 +292,7 @@ inline int blocks_of(int64_t n, int b)
 
 int anderson_window_blocks(int32_t n)
 {
-    return blocks_of(n > 0 ? n : 1, kWindowThreads);
+    return blocks_of(n > 0 ? n : 1, kWindowThreads * kWindowVerticesPerThread);
 }
 
 cudaError_t launch_anderson_start(AndersonParams const& p, cudaStream_t s)

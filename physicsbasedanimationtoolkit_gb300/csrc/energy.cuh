@@ -78,14 +78,17 @@ __device__ __forceinline__ void tet_D(EnergyParams const& p, int e, float D[3][3
 // so every term left scales with the strain and keeps its relative precision in FP32 (relative
 // error ~1e-7 of the strain energy, not of the rest-state constant); the sum is FP64.  GB300's
 // FP64 rate is a small fraction of its FP32 rate, so FP64 is kept to the accumulation.
-__device__ __forceinline__ double objective_term(EnergyParams const& p, int j)
+// The two FP32 parts of entry j: the inertial term of vertex j (kin, 0 past nV) and the elastic
+// term of tet j before its dt^2 factor (elas, 0 past nT).
+__device__ __forceinline__ void objective_parts(EnergyParams const& p, int j, float& kin, float& elas)
 {
-    double acc = 0.0;
+    kin  = 0.f;
+    elas = 0.f;
     if (j < p.nV)
     {
         float4 const x = p.x[j], y = p.xtilde[j];
         float const dx = x.x - y.x, dy = x.y - y.y, dz = x.z - y.z;
-        acc += double(0.5f * p.m[j] * (dx * dx + dy * dy + dz * dz));
+        kin            = 0.5f * p.m[j] * (dx * dx + dy * dy + dz * dz);
     }
     if (j < p.nT)
     {
@@ -104,8 +107,19 @@ __device__ __forceinline__ double objective_term(EnergyParams const& p, int j)
                            D[2][0] * (D[0][1] * D[1][2] - D[0][2] * D[1][1]);
         float const Jm1 = tr + minors + detD;
         float const c   = mat.z - 1.f;
-        acc += p.dt2 * double(mat.y * Jm1 * (0.5f * Jm1 - c) + 0.5f * mat.x * (2.f * tr + n2));
+        elas            = mat.y * Jm1 * (0.5f * Jm1 - c) + 0.5f * mat.x * (2.f * tr + n2);
     }
+}
+
+__device__ __forceinline__ double objective_term(EnergyParams const& p, int j)
+{
+    float kin, elas;
+    objective_parts(p, j, kin, elas);
+    double acc = 0.0;
+    if (j < p.nV)
+        acc += double(kin);
+    if (j < p.nT)
+        acc += p.dt2 * double(elas);
     return acc;
 }
 

@@ -1,5 +1,6 @@
 // Trust-region accelerated VBD kernels (see trust_region.cuh).
 #include "trust_region.cuh"
+#include "dfloat.cuh"
 #include "energy.cuh"
 
 #include <cfloat>
@@ -33,6 +34,21 @@ __device__ __forceinline__ double block_sum(double v)
         r = threadIdx.x < (blockDim.x >> 5) ? warps[threadIdx.x] : 0.0;
         r = warp_sum(r);
     }
+    return r;
+}
+
+// Block total from one FP64 value per warp (valid in lane 0), added over the warps in order; the
+// result is valid in thread 0.
+__device__ __forceinline__ double block_sum_of_warps(double w)
+{
+    __shared__ double warps[kTrustBlock / 32];
+    if ((threadIdx.x & 31) == 0)
+        warps[threadIdx.x >> 5] = w;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < int(blockDim.x >> 5); ++k)
+            r += warps[k];
     return r;
 }
 
@@ -111,15 +127,19 @@ __global__ void trust_begin_kernel(TrustParams p, int32_t k)
 
 __global__ void trust_step_size_kernel(TrustParams p, int32_t entry)
 {
-    double acc = 0.0;
+    // |x - x_{k-1}|^2 as double-float sums (exact differences and squares; see dfloat.cuh).
+    DFloat acc = {0.f, 0.f};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.nV; i += gridDim.x * blockDim.x)
     {
         float4 const a = p.x[i], b = p.xkm1[i];
-        double const dx = double(a.x) - b.x, dy = double(a.y) - b.y, dz = double(a.z) - b.z;
-        acc += dx * dx + dy * dy + dz * dz;
+        acc = df_add(acc, df_sq_diff(a.x, b.x));
+        acc = df_add(acc, df_sq_diff(a.y, b.y));
+        acc = df_add(acc, df_sq_diff(a.z, b.z));
     }
-    double total = 0.0;
-    if (!grid_sum_last(p, block_sum(acc), total) || threadIdx.x != 0)
+    DFloat const sum = df_warp_sum(acc); // all lanes shuffle; lane 0 converts
+    double const w   = (threadIdx.x & 31) == 0 ? df_to_double(sum) : 0.0;
+    double total     = 0.0;
+    if (!grid_sum_last(p, block_sum_of_warps(w), total) || threadIdx.x != 0)
         return;
     TrustState& S    = *p.state;
     double const dx2 = total;
@@ -169,8 +189,9 @@ __global__ void trust_apply_kernel(TrustParams p, bool rollback)
 // Contact energy of active vertex av[q] (TrustRegionIntegrator.cu:310-350): the area-scaled
 // penalty over its listed triangles and vertex_triangle_contact's energy for each, at the current
 // positions against those at t.
-__device__ double contact_energy(TrustParams const& p, int q)
+__device__ DFloat contact_energy(TrustParams const& p, int q)
 {
+    DFloat e = {0.f, 0.f};
     int const i = p.cV[p.av[q]];
     float sumfa = 0.f;
     int32_t f[8];
@@ -181,11 +202,10 @@ __device__ double contact_energy(TrustParams const& p, int q)
             sumfa += p.FA[f[c]];
     }
     if (!(sumfa > 0.f))
-        return 0.0;
+        return e;
     float const kC     = p.XVA[i] * p.muC / sumfa;
     float4 const xti4  = p.xt[i], xi4 = p.x[i];
     float const xti[3] = {xti4.x, xti4.y, xti4.z}, xi[3] = {xi4.x, xi4.y, xi4.z};
-    double e = 0.0;
     for (int c = 0; c < 8; ++c)
     {
         if (f[c] < 0)
@@ -200,7 +220,7 @@ __device__ double contact_energy(TrustParams const& p, int q)
             xf[k][0] = b.x, xf[k][1] = b.y, xf[k][2] = b.z;
         }
         float g[3] = {0.f, 0.f, 0.f}, H[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        e += double(vertex_triangle_contact(xti, xi, xtf, xf, p.h, kC * p.FA[f[c]], p.muF, p.epsv, FLT_EPSILON, g, H));
+        e = df_add(e, vertex_triangle_contact(xti, xi, xtf, xf, p.h, kC * p.FA[f[c]], p.muF, p.epsv, FLT_EPSILON, g, H));
     }
     return e;
 }
@@ -210,20 +230,29 @@ __global__ void trust_objective_kernel(TrustParams p, TrustObjectivePhase phase,
     TrustState& S = *p.state;
     if ((phase == kTrustTrial && !S.tryStep) || (phase == kTrustFinal && !S.needObjective))
         return;
-    double acc  = 0.0;
+    // FP32 terms (energy.cuh objective_parts) summed as double-float values: the inertial and
+    // contact terms in accV, the elastic terms in accT (scaled by dt^2 once per warp, in FP64).
+    DFloat accV = {0.f, 0.f}, accT = {0.f, 0.f};
     int const n = p.energy.nV > p.energy.nT ? p.energy.nV : p.energy.nT;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-        acc += objective_term(p.energy, j);
+    {
+        float kin, elas;
+        objective_parts(p.energy, j, kin, elas);
+        accV = df_add(accV, kin);
+        accT = df_add(accT, elas);
+    }
     if (p.nActive)
     {
         int const na = *p.nActive;
         for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < na; q += gridDim.x * blockDim.x)
-            acc += contact_energy(p, q);
+            accV = df_add(accV, contact_energy(p, q));
     }
+    DFloat const sv = df_warp_sum(accV), st = df_warp_sum(accT); // all lanes shuffle; lane 0 converts
+    double w        = (threadIdx.x & 31) == 0 ? df_to_double(sv) + p.energy.dt2 * df_to_double(st) : 0.0;
     if (blockIdx.x == 0 && threadIdx.x == 0)
-        acc += p.energy.dt2 * p.energy.restEnergy;
+        w += p.energy.dt2 * p.energy.restEnergy;
     double f = 0.0;
-    if (!grid_sum_last(p, block_sum(acc), f) || threadIdx.x != 0)
+    if (!grid_sum_last(p, block_sum_of_warps(w), f) || threadIdx.x != 0)
         return;
     switch (phase)
     {
