@@ -22,7 +22,9 @@
  *   pbgb_vbd_trace_next_step     Integrator::TraceNextStep            sim/vbd/Integrator.cpp:47-52
  *   pbgb_vbd_trust_region_log    the trust-region decisions the reference logs through its
  *                                profiler                             gpu/impl/vbd/TrustRegionIntegrator.cu:71-160
- *   pbgb_bvh_*                   gpu::geometry::Bvh (build, overlaps) gpu/impl/geometry/Bvh.cu/.cuh
+ *   pbgb_bvh_*                   gpu::geometry::Bvh (build, overlaps, self-overlaps, nearest
+ *                                simplices, visits) gpu/geometry/Bvh.cu, gpu/impl/geometry/Bvh.cu/.cuh
+ *   pbgb_simplex_boxes           gpu::geometry::Aabb::Construct(P, S) gpu/geometry/Aabb.cu
  *   pbgb_ccd_*                   VertexTriangleMixedCcdDcd            gpu/impl/contact/VertexTriangleMixedCcdDcd.cu
  * Beyond the reference: pbgb_vbd_create_batched (many meshes, one launch per colour),
  * pbgb_vbd_step_record / pbgb_vbd_step_adjoint (reverse-mode derivatives), pbgb_vbd_save_state /
@@ -377,6 +379,23 @@ PBGB_API int pbgb_bvh_overlaps(
     int32_t* pairs,
     int64_t capacity,
     int64_t* count);
+/* Self-overlaps of the built boxes (gpu/geometry/Bvh.cu:68-121, Bvh::DetectOverlaps with and
+ * without a set; traversal gpu/impl/geometry/Bvh.cuh:206-281): each unordered pair once, as
+ * (box of the leaf earlier in Morton order, other box), in no particular order.  set (nullable)
+ * holds one int per box; pairs within one set are dropped.  pairs: 2 * capacity ints; count = all
+ * pairs found (call again with a larger capacity when count > capacity). */
+PBGB_API int pbgb_bvh_self_overlaps(pbgb_bvh* b, const int32_t* set, int32_t* pairs, int64_t capacity, int64_t* count);
+/* Nearest simplex to each of nq points X (3 floats each) among the nS = built boxes' simplices
+ * S (k = 3: triangles, gpu/geometry/Bvh.cu:123-190 PointTriangleNearestNeighbors; k = 4:
+ * tetrahedra, :192-260 PointTetrahedronNearestNeighbors) over nP points P: nn[q] = simplex index,
+ * among exact ties the one the reference's callback writes last. */
+PBGB_API int pbgb_bvh_nearest_simplices(pbgb_bvh* b, int32_t nq, const float* X, int32_t nP, const float* P, int32_t nS,
+                                        const int32_t* S, int32_t k, int32_t* nn);
+/* Visit counters of the last box pass (n - 1 ints; gpu/geometry/Bvh.cu Visits, each 2 after a build). */
+PBGB_API int pbgb_bvh_visits(pbgb_bvh* b, int32_t* visits);
+/* Boxes of nS simplices of k (1..4) vertices over nP points (gpu/geometry/Aabb.cu:56-80,
+ * Aabb::Construct(P, S)): lower / upper 3 floats per simplex. */
+PBGB_API int pbgb_simplex_boxes(int32_t nP, const float* P, int32_t nS, const int32_t* S, int32_t k, float* lower, float* upper);
 PBGB_API const char* pbgb_bvh_last_error(pbgb_bvh* b);
 
 /*

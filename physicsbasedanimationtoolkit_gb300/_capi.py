@@ -141,6 +141,10 @@ _SIGNATURES = [
     ("pbgb_bvh_stream", C.c_int, [_vp, C.POINTER(_vp)]),
     ("pbgb_bvh_topology", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("pbgb_bvh_overlaps", C.c_int, [_vp, _i32, _vp, _vp, _vp, C.c_int64, C.POINTER(C.c_int64)]),
+    ("pbgb_bvh_self_overlaps", C.c_int, [_vp, _vp, _vp, C.c_int64, C.POINTER(C.c_int64)]),
+    ("pbgb_bvh_nearest_simplices", C.c_int, [_vp, _i32, _vp, _i32, _vp, _i32, _vp, _i32, _vp]),
+    ("pbgb_bvh_visits", C.c_int, [_vp, _vp]),
+    ("pbgb_simplex_boxes", C.c_int, [_i32, _vp, _i32, _vp, _i32, _vp, _vp]),
     ("pbgb_bvh_last_error", C.c_char_p, [_vp]),
     ("pbgb_ccd_create", C.c_int, [_i32, _i32, _vp, _i32, _vp, _vp, C.POINTER(_vp)]),
     ("pbgb_ccd_destroy", C.c_int, [_vp]),

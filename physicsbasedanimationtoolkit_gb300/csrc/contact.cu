@@ -666,6 +666,85 @@ __global__ void __launch_bounds__(32 * kNearestWarps) nearest_kernel(ContactMesh
         nearest_write<FINALIZE>(M, S, x, v, i, p, list, count);
 }
 
+// Point in closed tetrahedron abcd (geometry/OverlapQueries.h:562-587): outside when strictly on
+// the positive side of one of the faces (a, b, d), (b, c, d), (c, a, d), (a, c, b).
+__device__ __forceinline__ bool point_in_tet(float3 p, float3 a, float3 b, float3 c, float3 d)
+{
+    auto outside = [&](float3 u, float3 v, float3 w) { return dot(sub(p, u), cross(sub(v, u), sub(w, u))) > 0.f; };
+    return !(outside(a, b, d) || outside(b, c, d) || outside(c, a, d) || outside(a, c, b));
+}
+
+// Squared point-tetrahedron distance (geometry/DistanceQueries.h:230-249): 0 inside, else the
+// nearest of the four faces.
+__device__ __forceinline__ float point_tet_sqdist(float3 p, float3 a, float3 b, float3 c, float3 d)
+{
+    if (point_in_tet(p, a, b, c, d))
+        return 0.f;
+    return fminf(fminf(point_triangle_sqdist(p, a, b, d), point_triangle_sqdist(p, b, c, d)),
+                 fminf(point_triangle_sqdist(p, c, a, d), point_triangle_sqdist(p, a, c, b)));
+}
+
+// Nearest simplex to each query point (gpu/impl/geometry/Bvh.cuh:347-474 with the callbacks of
+// gpu/geometry/Bvh.cu:123-260): depth-first branch and bound from the root (children pushed left
+// then right, so the right child is visited first), leaves pruned by their box, exact ties (eps 0)
+// kept in a list of 8 in visit order; the reference's callback writes every listed simplex in turn,
+// so the last one stays.  Squared distances order the candidates as distances do.
+template <int K>
+__global__ void nearest_simplex_kernel(BvhView V, int32_t nq, float4 const* __restrict__ X, float4 const* __restrict__ P, int32_t const* __restrict__ S, int32_t* __restrict__ nn, int32_t* __restrict__ flags)
+{
+    int const q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq)
+        return;
+    if (V.n < 1)
+    {
+        nn[q] = -1;
+        return;
+    }
+    float3 const x          = f3(X[q]);
+    int32_t const leafBegin = V.n - 1;
+    int32_t stack[kBvhStack];
+    int top      = 0;
+    stack[top++] = 0;
+    int32_t list[kMaxContacts];
+    int count  = 0;
+    float dmin = FLT_MAX;
+    while (top > 0)
+    {
+        int32_t const node = stack[--top];
+        if (node < leafBegin)
+        {
+            if (point_box_sqdist(x, V.ilo[node], V.ihi[node]) <= dmin)
+            {
+                if (top + 2 > kBvhStack)
+                {
+                    atomicOr(flags, kBvhErrStackOverflow);
+                    nn[q] = -1;
+                    return;
+                }
+                stack[top++] = V.child[2 * node];
+                stack[top++] = V.child[2 * node + 1];
+            }
+            continue;
+        }
+        int32_t const sl = node - leafBegin;
+        if (point_box_sqdist(x, V.llo[sl], V.lhi[sl]) > dmin)
+            continue;
+        int32_t const i      = V.inds[sl];
+        int32_t const* const c = S + size_t(i) * K;
+        float const d = K == 3 ? point_triangle_sqdist(x, f3(P[c[0]]), f3(P[c[1]]), f3(P[c[2]]))
+                               : point_tet_sqdist(x, f3(P[c[0]]), f3(P[c[1]]), f3(P[c[2]]), f3(P[c[K - 1]]));
+        if (d < dmin)
+        {
+            count     = 0;
+            list[count++] = i;
+            dmin      = d;
+        }
+        else if (d <= dmin && count < kMaxContacts)
+            list[count++] = i;
+    }
+    nn[q] = count > 0 ? list[count - 1] : -1;
+}
+
 inline int blocks(int64_t n, int b)
 {
     return int((n + b - 1) / b);
@@ -733,6 +812,28 @@ cudaError_t contact_finalize(ContactMesh const& M, ContactState const& S, float4
         return e;
     nearest_kernel<true><<<blocks(M.nSurfV, kNearestWarps), 32 * kNearestWarps, sizeof(NearestSmem) * kNearestWarps, s>>>(
         M, S, view_of(S.bvh, M.nF), x);
+    return cudaGetLastError();
+}
+
+cudaError_t bvh_nearest_simplices(
+    BvhView const& V,
+    int32_t nq,
+    float4 const* X,
+    float4 const* P,
+    int32_t const* S,
+    int32_t k,
+    int32_t* nn,
+    int32_t* flags,
+    cudaStream_t s)
+{
+    if (nq <= 0)
+        return cudaSuccess;
+    if (k == 3)
+        nearest_simplex_kernel<3><<<blocks(nq, 128), 128, 0, s>>>(V, nq, X, P, S, nn, flags);
+    else if (k == 4)
+        nearest_simplex_kernel<4><<<blocks(nq, 128), 128, 0, s>>>(V, nq, X, P, S, nn, flags);
+    else
+        return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 

@@ -453,6 +453,80 @@ __global__ void overlaps_kernel(BvhView V, int32_t nq, float4 const* __restrict_
     }
 }
 
+// Self-overlaps of the built leaves (gpu/impl/geometry/Bvh.cuh:206-281): leaf s walks the tree
+// from the root and only descends into subtrees whose rightmost leaf lies after its own, so each
+// unordered pair is met once, from the leaf earlier in Morton order, and reported as (its box,
+// the other box).  With set != nullptr, pairs of boxes in the same set are dropped
+// (gpu/geometry/Bvh.cu:91-121).
+__global__ void self_overlaps_kernel(BvhView V, int32_t const* __restrict__ set, int32_t* __restrict__ pairs, int64_t capacity, unsigned long long* __restrict__ count, int32_t* __restrict__ flags)
+{
+    int const s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= V.n || V.n < 2)
+        return;
+    int32_t const leafBegin = V.n - 1;
+    int32_t const leaf      = leafBegin + s;
+    float4 const L = V.llo[s], U = V.lhi[s];
+    int32_t const bi = V.inds[s];
+    int32_t stack[kBvhStack];
+    int top      = 0;
+    stack[top++] = 0;
+    while (top > 0)
+    {
+        int32_t const node = stack[--top];
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+        {
+            int32_t const ch = V.child[2 * node + c];
+            if (V.rightmost[2 * node + c] <= leaf)
+                continue;
+            bool const isLeaf = ch >= leafBegin;
+            float4 const cl   = isLeaf ? V.llo[ch - leafBegin] : V.ilo[ch];
+            float4 const cu   = isLeaf ? V.lhi[ch - leafBegin] : V.ihi[ch];
+            if (!boxes_overlap(L, U, cl, cu))
+                continue;
+            if (isLeaf)
+            {
+                int32_t const bj = V.inds[ch - leafBegin];
+                if (set && set[bi] == set[bj])
+                    continue;
+                unsigned long long const slot = atomicAdd(count, 1ull);
+                if (slot < (unsigned long long)capacity)
+                {
+                    pairs[2 * slot]     = bi;
+                    pairs[2 * slot + 1] = bj;
+                }
+            }
+            else
+            {
+                if (top + 1 > kBvhStack)
+                {
+                    atomicOr(flags, kBvhErrStackOverflow);
+                    return;
+                }
+                stack[top++] = ch;
+            }
+        }
+    }
+}
+
+// Boxes of simplices with k vertices each (gpu/impl/geometry/Aabb.cuh Construct): component-wise
+// minimum and maximum of the corners.
+__global__ void simplex_boxes_kernel(int32_t nS, int32_t k, float4 const* __restrict__ P, int32_t const* __restrict__ S, float4* __restrict__ lo, float4* __restrict__ hi)
+{
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nS)
+        return;
+    float4 l = P[S[size_t(i) * k]], u = l;
+    for (int a = 1; a < k; ++a)
+    {
+        float4 const q = P[S[size_t(i) * k + a]];
+        l              = make_float4(fminf(l.x, q.x), fminf(l.y, q.y), fminf(l.z, q.z), 0.f);
+        u              = make_float4(fmaxf(u.x, q.x), fmaxf(u.y, q.y), fmaxf(u.z, q.z), 0.f);
+    }
+    lo[i] = make_float4(l.x, l.y, l.z, 0.f);
+    hi[i] = make_float4(u.x, u.y, u.z, 0.f);
+}
+
 inline int blocks(int64_t n, int b)
 {
     return int((n + b - 1) / b);
@@ -603,6 +677,32 @@ cudaError_t bvh_overlaps(
     if (e != cudaSuccess || nq <= 0)
         return e;
     overlaps_kernel<<<blocks(nq, 128), 128, 0, s>>>(V, nq, qlo, qhi, pairs, capacity, count, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t bvh_self_overlaps(
+    BvhView const& V,
+    int32_t const* set,
+    int32_t* pairs,
+    int64_t capacity,
+    unsigned long long* count,
+    int32_t* flags,
+    cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess || V.n < 2)
+        return e;
+    self_overlaps_kernel<<<blocks(V.n, 128), 128, 0, s>>>(V, set, pairs, capacity, count, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t simplex_boxes(int32_t nS, int32_t k, float4 const* P, int32_t const* S, float4* lo, float4* hi, cudaStream_t s)
+{
+    if (nS <= 0)
+        return cudaSuccess;
+    if (k < 1 || k > 4)
+        return cudaErrorInvalidValue;
+    simplex_boxes_kernel<<<blocks(nS, 256), 256, 0, s>>>(nS, k, P, S, lo, hi);
     return cudaGetLastError();
 }
 

@@ -81,6 +81,35 @@ cudaError_t bvh_overlaps(
     int32_t* flags,
     cudaStream_t s);
 
+// Self-overlaps of the built boxes (each unordered pair once, from the leaf earlier in Morton
+// order); set (nullable, one entry per box) drops pairs within one set.  Pairs beyond capacity are
+// counted, not written.
+cudaError_t bvh_self_overlaps(
+    BvhView const& V,
+    int32_t const* set,
+    int32_t* pairs,
+    int64_t capacity,
+    unsigned long long* count,
+    int32_t* flags,
+    cudaStream_t s);
+
+// Boxes of nS simplices of k (1..4) vertices each: S[k i + a] indexes P.
+cudaError_t simplex_boxes(int32_t nS, int32_t k, float4 const* P, int32_t const* S, float4* lo, float4* hi, cudaStream_t s);
+
+// Nearest simplex to each query point (gpu/geometry/Bvh.cu PointTriangleNearestNeighbors /
+// PointTetrahedronNearestNeighbors): k = 3 (triangles) or 4 (tetrahedra) vertices per simplex;
+// nn[q] = the simplex the reference's callback leaves there (the last of the exact-tie list).
+cudaError_t bvh_nearest_simplices(
+    BvhView const& V,
+    int32_t nq,
+    float4 const* X,
+    float4 const* P,
+    int32_t const* S,
+    int32_t k,
+    int32_t* nn,
+    int32_t* flags,
+    cudaStream_t s);
+
 inline BvhView view_of(BvhBuffers const& B, int32_t n)
 {
     return BvhView{n, B.inds, B.child, B.rightmost, B.ilo, B.ihi, B.llo, B.lhi};

@@ -39,6 +39,33 @@ T* dalloc(size_t n)
     return p;
 }
 
+// A device array freed on scope exit (per-call staging of query inputs).
+template <class T>
+struct Scratch
+{
+    T* p = nullptr;
+    explicit Scratch(size_t n) : p(dalloc<T>(n)) {}
+    ~Scratch()
+    {
+        if (p)
+            cudaFree(p);
+    }
+    Scratch(Scratch const&)            = delete;
+    Scratch& operator=(Scratch const&) = delete;
+};
+
+// Host 3-vectors -> device float4 (w = 0), on the given stream.
+void upload_points(float const* h3, int32_t n, float4* d, cudaStream_t s)
+{
+    if (n <= 0)
+        return;
+    std::vector<float4> tmp(static_cast<size_t>(n));
+    for (int32_t i = 0; i < n; ++i)
+        tmp[size_t(i)] = make_float4(h3[3 * size_t(i)], h3[3 * size_t(i) + 1], h3[3 * size_t(i) + 2], 0.f);
+    ck(cudaMemcpyAsync(d, tmp.data(), sizeof(float4) * size_t(n), cudaMemcpyHostToDevice, s), "H2D");
+    ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+}
+
 } // namespace
 
 struct pbgb_bvh
@@ -329,6 +356,133 @@ PBGB_API int pbgb_bvh_overlaps(
         *count = int64_t(c);
         return b->check_flags();
     });
+}
+
+PBGB_API int pbgb_bvh_self_overlaps(pbgb_bvh* b, const int32_t* set, int32_t* pairs, int64_t capacity, int64_t* count)
+{
+    if (!b)
+        return bvh_fail(nullptr, PBGB_ERR_INVALID_ARGUMENT, "null BVH");
+    if (b->n < 1 || !count || capacity < 0 || (capacity > 0 && !pairs))
+        return bvh_fail(b, PBGB_ERR_INVALID_ARGUMENT, "pbgb_bvh_self_overlaps: invalid argument");
+    return bvh_guard(b, [&] {
+        if (capacity > b->pcap)
+        {
+            if (b->pairs)
+                cudaFree(b->pairs);
+            b->pairs = nullptr;
+            b->pairs = dalloc<int32_t>(2 * size_t(capacity));
+            b->pcap  = capacity;
+        }
+        Scratch<int32_t> dset{set ? size_t(b->n) : size_t(0)};
+        if (set)
+            ck(cudaMemcpyAsync(dset.p, set, sizeof(int32_t) * size_t(b->n), cudaMemcpyHostToDevice, b->stream), "H2D");
+        ck(pbgb::bvh_self_overlaps(pbgb::view_of(b->B, b->n), set ? dset.p : nullptr, b->pairs, capacity, b->count,
+                                   b->B.flags, b->stream),
+           "bvh_self_overlaps");
+        unsigned long long c = 0;
+        ck(cudaMemcpyAsync(&c, b->count, sizeof(c), cudaMemcpyDeviceToHost, b->stream), "D2H");
+        ck(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+        int64_t const m = int64_t(c) < capacity ? int64_t(c) : capacity;
+        if (m > 0)
+            ck(cudaMemcpy(pairs, b->pairs, sizeof(int32_t) * 2 * size_t(m), cudaMemcpyDeviceToHost), "D2H");
+        *count = int64_t(c);
+        return b->check_flags();
+    });
+}
+
+PBGB_API int pbgb_bvh_nearest_simplices(
+    pbgb_bvh* b,
+    int32_t nq,
+    const float* X,
+    int32_t nP,
+    const float* P,
+    int32_t nS,
+    const int32_t* S,
+    int32_t k,
+    int32_t* nn)
+{
+    if (!b)
+        return bvh_fail(nullptr, PBGB_ERR_INVALID_ARGUMENT, "null BVH");
+    if (b->n < 1 || nq < 0 || (nq > 0 && (!X || !nn)) || nP < 1 || !P || nS != b->n || !S || (k != 3 && k != 4))
+        return bvh_fail(b, PBGB_ERR_INVALID_ARGUMENT,
+                        "pbgb_bvh_nearest_simplices: expected the built BVH's simplices (nS = boxes), k = 3 or 4");
+    for (int64_t i = 0; i < int64_t(nS) * k; ++i)
+        if (S[i] < 0 || S[i] >= nP)
+            return bvh_fail(b, PBGB_ERR_INVALID_ARGUMENT, "pbgb_bvh_nearest_simplices: simplex index out of range");
+    return bvh_guard(b, [&] {
+        Scratch<float4> dX{size_t(nq)}, dP{size_t(nP)};
+        Scratch<int32_t> dS{size_t(nS) * size_t(k)}, dnn{size_t(nq)};
+        upload_points(X, nq, dX.p, b->stream);
+        upload_points(P, nP, dP.p, b->stream);
+        ck(cudaMemcpyAsync(dS.p, S, sizeof(int32_t) * size_t(nS) * size_t(k), cudaMemcpyHostToDevice, b->stream), "H2D");
+        ck(pbgb::bvh_nearest_simplices(pbgb::view_of(b->B, b->n), nq, dX.p, dP.p, dS.p, k, dnn.p, b->B.flags, b->stream),
+           "bvh_nearest_simplices");
+        if (nq > 0)
+            ck(cudaMemcpyAsync(nn, dnn.p, sizeof(int32_t) * size_t(nq), cudaMemcpyDeviceToHost, b->stream), "D2H");
+        ck(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+        return b->check_flags();
+    });
+}
+
+PBGB_API int pbgb_bvh_visits(pbgb_bvh* b, int32_t* visits)
+{
+    if (!b)
+        return bvh_fail(nullptr, PBGB_ERR_INVALID_ARGUMENT, "null BVH");
+    if (b->n < 1 || !visits)
+        return bvh_fail(b, PBGB_ERR_INVALID_ARGUMENT, "pbgb_bvh_visits: invalid argument");
+    return bvh_guard(b, [&] {
+        if (b->n > 1)
+            ck(cudaMemcpyAsync(visits, b->B.visits, sizeof(int32_t) * size_t(b->n - 1), cudaMemcpyDeviceToHost, b->stream),
+               "D2H");
+        ck(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+        return int(PBGB_OK);
+    });
+}
+
+PBGB_API int pbgb_simplex_boxes(int32_t nP, const float* P, int32_t nS, const int32_t* S, int32_t k, float* lower, float* upper)
+{
+    if (nP < 1 || !P || nS < 0 || (nS > 0 && (!S || !lower || !upper)) || k < 1 || k > 4)
+        return bvh_fail(nullptr, PBGB_ERR_INVALID_ARGUMENT, "pbgb_simplex_boxes: invalid argument");
+    for (int64_t i = 0; i < int64_t(nS) * k; ++i)
+        if (S[i] < 0 || S[i] >= nP)
+            return bvh_fail(nullptr, PBGB_ERR_INVALID_ARGUMENT, "pbgb_simplex_boxes: simplex index out of range");
+    try
+    {
+        cudaStream_t s = nullptr;
+        ck(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+        struct StreamGuard
+        {
+            cudaStream_t s;
+            ~StreamGuard() { cudaStreamDestroy(s); }
+        } guard{s};
+        Scratch<float4> dP{size_t(nP)}, lo{size_t(nS)}, hi{size_t(nS)};
+        Scratch<int32_t> dS{size_t(nS) * size_t(k)};
+        upload_points(P, nP, dP.p, s);
+        if (nS > 0)
+            ck(cudaMemcpyAsync(dS.p, S, sizeof(int32_t) * size_t(nS) * size_t(k), cudaMemcpyHostToDevice, s), "H2D");
+        ck(pbgb::simplex_boxes(nS, k, dP.p, dS.p, lo.p, hi.p, s), "simplex_boxes");
+        std::vector<float4> hl(static_cast<size_t>(nS)), hu(static_cast<size_t>(nS));
+        if (nS > 0)
+        {
+            ck(cudaMemcpyAsync(hl.data(), lo.p, sizeof(float4) * size_t(nS), cudaMemcpyDeviceToHost, s), "D2H");
+            ck(cudaMemcpyAsync(hu.data(), hi.p, sizeof(float4) * size_t(nS), cudaMemcpyDeviceToHost, s), "D2H");
+        }
+        ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        for (int32_t i = 0; i < nS; ++i)
+        {
+            lower[3 * size_t(i)] = hl[size_t(i)].x, lower[3 * size_t(i) + 1] = hl[size_t(i)].y, lower[3 * size_t(i) + 2] = hl[size_t(i)].z;
+            upper[3 * size_t(i)] = hu[size_t(i)].x, upper[3 * size_t(i) + 1] = hu[size_t(i)].y, upper[3 * size_t(i) + 2] = hu[size_t(i)].z;
+        }
+        return PBGB_OK;
+    }
+    catch (CudaError const& e)
+    {
+        return bvh_fail(nullptr, PBGB_ERR_CUDA, std::string(e.what) + ": " + cudaGetErrorString(e.e));
+    }
+    catch (std::exception const& e)
+    {
+        return bvh_fail(nullptr, PBGB_ERR_INTERNAL, e.what());
+    }
 }
 
 PBGB_API const char* pbgb_bvh_last_error(pbgb_bvh* b)

@@ -141,3 +141,136 @@ def test_build_from_device_boxes_equals_host_build():
     dev = bvh._topology()
     assert_same(dev, host)
     assert_same(dev, O.bvh_build(lo, hi, wmin, wmax))
+
+
+# ---------------------------------------------------------------------------------------------
+# The reference binding's remaining queries (bindings/pypbat/gpu/geometry/Bvh.cpp, Aabb.cpp).
+
+def _brute_self_overlaps(lo, hi, sets=None):
+    """Unordered pairs {i, j}, i != j, of closed boxes that overlap (numpy, exact comparisons)."""
+    ov = np.all((lo[:, None, :] <= hi[None, :, :]) & (lo[None, :, :] <= hi[:, None, :]), axis=2)
+    i, j = np.nonzero(np.triu(ov, 1))
+    keep = np.ones(i.size, bool) if sets is None else sets[i] != sets[j]
+    return {frozenset((a, b)) for a, b in zip(i[keep].tolist(), j[keep].tolist())}
+
+
+def test_detect_overlaps_between_sets_reference_case():
+    """The reference's doctest (gpu/geometry/Bvh.cu:336-404): three edges (set 0) and one
+    triangle (set 1); the triangle overlaps edges 1 and 0, each pair reported once."""
+    V = np.array([[0, 1, 2, 3, 0, 2, 0], [0, 0.1, 0.2, 0.3, 0, 0.1, 0], [0, 10, 20, 30, 0, 10, 0]], np.float32)
+    E1 = np.array([[1, 0, 2], [2, 1, 3]])
+    F2 = np.array([[4], [5], [6]])
+    edges, tris = pbat.gpu.geometry.Aabb(3, 3), pbat.gpu.geometry.Aabb(3, 1)
+    edges.construct(V, E1)
+    tris.construct(V, F2)
+    L = np.hstack([edges.min, tris.min])
+    U = np.hstack([edges.max, tris.max])
+    aabbs = pbat.gpu.geometry.Aabb(3, 4)
+    aabbs.construct(L, U)
+    sets = np.array([0, 0, 0, 1], np.int32)
+    bvh = pbat.gpu.geometry.Bvh(4, 4)
+    bvh.build(aabbs, L.min(axis=1), U.max(axis=1))
+    O2 = bvh.detect_overlaps(aabbs, sets)
+    assert O2.shape == (2, 2)
+    assert {frozenset(c) for c in O2.T.tolist()} == {frozenset((3, 1)), frozenset((3, 0))}
+    assert (bvh.visits == 2).all()
+
+
+@pytest.mark.parametrize("n", [2, 3, 50, 2000])
+def test_self_overlaps_equal_brute_force(n):
+    rng = np.random.default_rng(n)
+    c = rng.uniform(0, 1, (n, 3)).astype(np.float32)
+    r = rng.uniform(0.005, 0.05, (n, 3)).astype(np.float32)
+    lo, hi = c - r, c + r
+    lo[: n // 10] = lo[n // 10: 2 * (n // 10)]  # duplicated boxes (equal Morton codes)
+    hi[: n // 10] = hi[n // 10: 2 * (n // 10)]
+    bvh = pbat.gpu.geometry.Bvh(n, 16)
+    bvh.build(lo.T, hi.T, lo.min(axis=0), hi.max(axis=0))
+    O1 = bvh.detect_overlaps(lo.T, upper=hi.T)
+    got = [frozenset(p) for p in O1.T.tolist()]
+    assert len(got) == len(set(got))  # each pair once
+    assert set(got) == _brute_self_overlaps(lo, hi)
+    sets = rng.integers(0, 3, n).astype(np.int32)
+    O2 = bvh.detect_overlaps(lo.T, sets, upper=hi.T)
+    got2 = [frozenset(p) for p in O2.T.tolist()]
+    assert len(got2) == len(set(got2))
+    assert set(got2) == _brute_self_overlaps(lo, hi, sets)
+
+
+def _np_point_triangle(p, a, b, c):
+    """FP64 point-triangle distance by Voronoi regions (independent of the device code)."""
+    ab, ac, ap = b - a, c - a, p - a
+    d1, d2 = ab @ ap, ac @ ap
+    if d1 <= 0 and d2 <= 0:
+        return np.linalg.norm(p - a)
+    bp = p - b
+    d3, d4 = ab @ bp, ac @ bp
+    if d3 >= 0 and d4 <= d3:
+        return np.linalg.norm(p - b)
+    vc = d1 * d4 - d3 * d2
+    if vc <= 0 and d1 >= 0 and d3 <= 0:
+        return np.linalg.norm(p - (a + d1 / (d1 - d3) * ab))
+    cp = p - c
+    d5, d6 = ab @ cp, ac @ cp
+    if d6 >= 0 and d5 <= d6:
+        return np.linalg.norm(p - c)
+    vb = d5 * d2 - d1 * d6
+    if vb <= 0 and d2 >= 0 and d6 <= 0:
+        return np.linalg.norm(p - (a + d2 / (d2 - d6) * ac))
+    va = d3 * d6 - d5 * d4
+    if va <= 0 and (d4 - d3) >= 0 and (d5 - d6) >= 0:
+        return np.linalg.norm(p - (b + (d4 - d3) / ((d4 - d3) + (d5 - d6)) * (c - b)))
+    den = 1.0 / (va + vb + vc)
+    return np.linalg.norm(p - (a + ab * vb * den + ac * vc * den))
+
+
+def _np_point_tet(p, a, b, c, d):
+    def outside(u, v, w):
+        return (p - u) @ np.cross(v - u, w - u) > 0
+    if not (outside(a, b, d) or outside(b, c, d) or outside(c, a, d) or outside(a, c, b)):
+        return 0.0
+    return min(_np_point_triangle(p, a, b, d), _np_point_triangle(p, b, c, d), _np_point_triangle(p, c, a, d),
+               _np_point_triangle(p, a, c, b))
+
+
+def test_point_triangle_nearest_neighbours_are_nearest():
+    """Nearest surface triangle of a jittered cube to points inside, near and far from it: the
+    triangle returned is at the FP64 brute-force minimum distance (to FP32 rounding)."""
+    w = meshgen.unit_cube_workload(n=6, seed=4)
+    X = w["X"].astype(np.float64)
+    F = meshgen.boundary_faces(w["T"]).astype(np.int32)
+    aabbs = pbat.gpu.geometry.Aabb(3, F.shape[0])
+    aabbs.construct(X.T, F.T)
+    lo, hi = aabbs.min, aabbs.max
+    np.testing.assert_array_equal(lo, X[F].min(axis=1).T.astype(np.float32))
+    np.testing.assert_array_equal(hi, X[F].max(axis=1).T.astype(np.float32))
+    bvh = pbat.gpu.geometry.Bvh(F.shape[0], 0)
+    bvh.build(aabbs, lo.min(axis=1) - 1, hi.max(axis=1) + 1)
+    rng = np.random.default_rng(2)
+    P = np.vstack([rng.uniform(-0.5, 1.5, (300, 3)), rng.uniform(0.1, 0.9, (100, 3))]).astype(np.float32)
+    nn = bvh.point_triangle_nearest_neighbours(aabbs, P.T, X.T, F.T)
+    X32 = X.astype(np.float32).astype(np.float64)
+    for q, f in enumerate(nn):
+        d = np.array([_np_point_triangle(P[q].astype(np.float64), *X32[F[j]]) for j in range(F.shape[0])])
+        assert 0 <= f < F.shape[0]
+        assert d[f] <= d.min() + 1e-5
+
+
+def test_point_tetrahedron_nearest_neighbours_are_nearest():
+    """Nearest tetrahedron of a jittered cube: points inside get a tetrahedron that contains them
+    (distance 0), points outside one at the FP64 brute-force minimum distance."""
+    w = meshgen.unit_cube_workload(n=4, seed=6)
+    X = w["X"].astype(np.float32)
+    T = w["T"].astype(np.int32)
+    aabbs = pbat.gpu.geometry.Aabb(3, T.shape[0])
+    aabbs.construct(X.T, T.T)
+    bvh = pbat.gpu.geometry.Bvh(T.shape[0], 0)
+    bvh.build(aabbs, aabbs.min.min(axis=1), aabbs.max.max(axis=1))
+    rng = np.random.default_rng(3)
+    P = np.vstack([rng.uniform(0.05, 0.95, (200, 3)), rng.uniform(-0.4, 1.4, (100, 3))]).astype(np.float32)
+    nn = bvh.point_tetrahedron_nearest_neighbours(aabbs, P.T, X.T, T.T)
+    X64 = X.astype(np.float64)
+    for q, t in enumerate(nn):
+        d = np.array([_np_point_tet(P[q].astype(np.float64), *X64[T[j]]) for j in range(T.shape[0])])
+        assert 0 <= t < T.shape[0]
+        assert d[t] <= d.min() + 1e-5
