@@ -1716,13 +1716,20 @@ class VbdSystem
                     invalidate();
                     step(dt, iterations, substeps); // capture + warm-up
                     restore();
-                    check(cudaEventRecord(e0, stream), "cudaEventRecord");
-                    step(dt, iterations, substeps);
-                    check(cudaEventRecord(e1, stream), "cudaEventRecord");
-                    restore();
-                    check(cudaEventSynchronize(e1), "cudaEventSynchronize");
-                    float ms = 0.f;
-                    check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+                    // The faster of two timed steps from the same state (one step alone picked a
+                    // 17 % slower launch for the contact scene now and then).
+                    float ms = -1.f;
+                    for (int rep = 0; rep < 2; ++rep)
+                    {
+                        check(cudaEventRecord(e0, stream), "cudaEventRecord");
+                        step(dt, iterations, substeps);
+                        check(cudaEventRecord(e1, stream), "cudaEventRecord");
+                        restore();
+                        check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+                        float t = 0.f;
+                        check(cudaEventElapsedTime(&t, e0, e1), "cudaEventElapsedTime");
+                        ms = ms < 0.f || t < ms ? t : ms;
+                    }
                     if (best < 0.f || ms < best)
                     {
                         best = ms;

@@ -260,14 +260,23 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) sweep_kernel(SweepParams
 // the block's slab (rest positions before griddepcontrol.wait: no launch writes them; current
 // positions after it), and the incidence loop reads them back through the three slot bytes of its
 // packed incidence word.  The slab slice of solve entry s starts at nbrPtr[s] - nbrPtr[first
-// entry of the block]; positions and rest positions are two arrays of p.slab float4 each (a 16-byte
-// stride spreads random slots over all shared-memory banks); the lanes of a vertex share a warp,
-// so __syncwarp orders the staging.
+// entry of the block]; a slot of the plain and Chebyshev sweeps is 24 bytes, a float4 (position,
+// rest x) in the first array of p.slab float4 and a float2 (rest y, rest z) in the second (a
+// 16-byte stride spreads random slots over all shared-memory banks; an incidence reads a 16- and
+// an 8-byte word per corner instead of two 16-byte words), and the same lane writes both parts of
+// a slot (rest x before the wait, the position after it, disjoint bytes); the contact variant keeps
+// two float4 arrays.  The lanes of a vertex share a warp, so __syncwarp orders the staging.
 template <int L, bool CHEB, bool REC = false, bool CONTACT = false>
 __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(SweepParams p)
 {
-    extern __shared__ float4 slab[]; // positions [0, p.slab), rest positions [p.slab, 2 p.slab)
-    float4* const rest = slab + p.slab;
+    // Neighbour slot j.  Plain and Chebyshev sweeps: slab[j] = (x, y, z, rest x) and
+    // restYZ[j] = (rest y, rest z), 24 bytes a slot.  Contact variant: slab[j] = position and
+    // rest[j] = rest position, 32 bytes a slot (measured faster for that variant: 2.22 against
+    // 2.35 ms per contact step, where the packed slots took the Chebyshev beam step from 4.87 to
+    // 4.77 ms).
+    extern __shared__ float4 slab[];
+    float2* const restYZ = reinterpret_cast<float2*>(slab + p.slab);
+    float4* const rest   = slab + p.slab;
     int const tid    = blockIdx.x * blockDim.x + threadIdx.x;
     int const s      = p.begin + tid / L;
     int const lane   = tid & (L - 1);
@@ -292,7 +301,16 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(Swee
         n1   = __ldg(p.nbrPtr + s + 1);
         base = n0 - nb0;
         for (int j = n0 + lane; j < n1; j += L)
-            rest[base + j - n0] = __ldg(p.X + (__ldg(p.nbr + j) & kIndexMask));
+        {
+            float4 const Xa = __ldg(p.X + (__ldg(p.nbr + j) & kIndexMask));
+            if constexpr (CONTACT)
+                rest[base + j - n0] = Xa;
+            else
+            {
+                restYZ[base + j - n0]                               = make_float2(Xa.y, Xa.z);
+                reinterpret_cast<float*>(slab + base + j - n0)[3] = Xa.x;
+            }
+        }
         k1 = __ldg(p.incPtr + s + 1);
         k  = __ldg(p.incPtr + s) + lane;
         if (k < k1)
@@ -312,7 +330,15 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(Swee
             float4 const* src = p.x;
             if (CHEB && !(a >> 31))
                 src = p.hprev;
-            slab[base + j - n0] = __ldg(src + (a & kIndexMask));
+            float4 const xa = __ldg(src + (a & kIndexMask));
+            if constexpr (CONTACT)
+                slab[base + j - n0] = xa;
+            else
+            {
+                float* const dst                = reinterpret_cast<float*>(slab + base + j - n0);
+                *reinterpret_cast<float2*>(dst) = make_float2(xa.x, xa.y);
+                dst[2]                          = xa.z;
+            }
         }
     }
     __syncwarp();
@@ -332,14 +358,24 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(Swee
             for (int m = 0; m < 3; ++m)
             {
                 int const slot   = base + int((q.y >> (8 * m)) & 0xFFu);
-                float4 const xa  = slab[slot];
-                float4 const Xa  = rest[slot];
+                float4 const xa = slab[slot];
+                float Xa[3];
+                if constexpr (CONTACT)
+                {
+                    float4 const r = rest[slot];
+                    Xa[0] = r.x, Xa[1] = r.y, Xa[2] = r.z;
+                }
+                else
+                {
+                    float2 const r = restYZ[slot];
+                    Xa[0] = xa.w, Xa[1] = r.x, Xa[2] = r.y;
+                }
                 d[m][0] = xa.x - xi[0];
                 d[m][1] = xa.y - xi[1];
                 d[m][2] = xa.z - xi[2];
-                e[m][0] = Xa.x - Xi[0];
-                e[m][1] = Xa.y - Xi[1];
-                e[m][2] = Xa.z - Xi[2];
+                e[m][0] = Xa[0] - Xi[0];
+                e[m][1] = Xa[1] - Xi[1];
+                e[m][2] = Xa[2] - Xi[2];
             }
             float G[3][3];
             rest_gradients(e, G);
@@ -548,7 +584,8 @@ cudaError_t launch_sweep_l(SweepParams const& p, int g, int block, bool pdl, cud
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim            = dim3(unsigned(g));
     cfg.blockDim           = dim3(unsigned(block));
-    cfg.dynamicSmemBytes   = stagedBytes;
+    // stagedBytes sizes the largest slot; this variant's slots may be smaller (staged_sweep_kernel).
+    cfg.dynamicSmemBytes   = stagedBytes > 0 ? size_t(p.slab) * kStagedSlotBytes<CONTACT> : 0;
     cfg.stream             = s;
     cudaLaunchAttribute attr[1];
     attr[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -584,7 +621,7 @@ cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebys
         return cudaErrorInvalidValue;
     int const g   = blocks_for(n, block);
     SweepParams q = p;
-    q.slab        = int32_t(stagedBytes / (2 * sizeof(float4)));
+    q.slab        = int32_t(stagedBytes / kStagedSlotBytesMax);
     if (chebyshev && q.fc)
         return launch_sweep_t<true, false, true>(q, lanes, g, block, pdl, s, stagedBytes);
     return chebyshev ? launch_sweep_t<true, false>(q, lanes, g, block, pdl, s, stagedBytes)
@@ -599,7 +636,7 @@ cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool
     if (!p.tape || stagedBytes > kStagedMaxBytes || (stagedBytes > 0 && (!p.nbrPtr || !p.nbr || !p.incPack || !p.mats)))
         return cudaErrorInvalidValue;
     SweepParams q = p;
-    q.slab        = int32_t(stagedBytes / (2 * sizeof(float4)));
+    q.slab        = int32_t(stagedBytes / kStagedSlotBytesMax);
     return launch_sweep_t<false, true>(q, lanes, blocks_for(n, block), block, pdl, s, stagedBytes);
 }
 
@@ -614,7 +651,7 @@ size_t staged_sweep_bytes(int32_t const* nbrPtr, int32_t begin, int32_t end, int
         int32_t const b1 = b0 + per < end ? b0 + per : end;
         most             = std::max<int64_t>(most, int64_t(nbrPtr[b1]) - nbrPtr[b0]);
     }
-    return size_t(most) * 2 * sizeof(float4);
+    return size_t(most) * kStagedSlotBytesMax;
 }
 
 namespace {

@@ -131,8 +131,9 @@ struct EnergyParams
 // pdl: launch with programmatic stream serialization, so that the kernel's mesh-table prologue
 // overlaps the tail of the previous launch on the stream (the kernel waits before reading
 // positions).
-// stagedBytes > 0: the staged sweep (neighbours in shared memory), with that much dynamic shared
-// memory per block (staged_sweep_bytes); 0: the sweep that gathers every incidence's corners.  Both
+// stagedBytes > 0: the staged sweep (neighbours in shared memory), stagedBytes from
+// staged_sweep_bytes (each variant launches with its own slot size, at most that much dynamic
+// shared memory per block); 0: the sweep that gathers every incidence's corners.  Both
 // compute the same arithmetic in the same order.
 cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, bool pdl, cudaStream_t s, size_t stagedBytes = 0);
 // The plain (one-buffer) sweep that also writes p.tape; the same arithmetic as launch_sweep with
@@ -145,6 +146,11 @@ size_t staged_sweep_bytes(int32_t const* nbrPtr, int32_t begin, int32_t end, int
 // Largest dynamic shared memory a staged sweep may use (set on the current device by
 // prepare_staged_sweeps); larger launches fall back to the gathering sweep.
 size_t constexpr kStagedMaxBytes = 200 * 1024;
+// Bytes of one staged neighbour: position and rest position packed in 24 bytes, or two float4 in
+// the contact variant; staged_sweep_bytes sizes slabs by the larger.
+template <bool CONTACT>
+size_t constexpr kStagedSlotBytes = CONTACT ? 2 * sizeof(float4) : sizeof(float4) + sizeof(float2);
+size_t constexpr kStagedSlotBytesMax = 2 * sizeof(float4);
 cudaError_t prepare_staged_sweeps();
 cudaError_t launch_begin_substep(SubstepParams const& p, cudaStream_t s);
 cudaError_t launch_end_substep(SubstepParams const& p, cudaStream_t s);
