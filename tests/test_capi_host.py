@@ -276,3 +276,25 @@ def test_nesterov_settings_are_validated():
         pbat.sim.vbd.Data().with_volume_mesh(P, T).with_nesterov_acceleration(0.0, 3).construct()
     with pytest.raises(ValueError):
         pbat.sim.vbd.Data().with_volume_mesh(P, T).with_nesterov_acceleration(1.0, -1).construct()
+
+
+def test_bvh_queries_validate_arguments_before_the_device():
+    """The LBVH query entry points refuse bad arguments with PBGB_ERR_INVALID_ARGUMENT before any
+    device work: null handles, simplices indexing past the points, unsupported simplex sizes."""
+    L = _capi.lib()
+    count = C.c_int64()
+    assert L.pbgb_bvh_self_overlaps(None, None, None, 0, C.byref(count)) == 1
+    assert L.pbgb_bvh_nearest_simplices(None, 0, None, 0, None, 0, None, 3, None) == 1
+    assert L.pbgb_bvh_visits(None, None) == 1
+    P = np.zeros((4, 3), np.float32)
+    S = np.array([[0, 1, 2], [1, 2, 7]], np.int32)  # index 7 is past the 4 points
+    lo = np.zeros((2, 3), np.float32)
+    hi = np.zeros((2, 3), np.float32)
+    rc = L.pbgb_simplex_boxes(4, P.ctypes.data, 2, S.ctypes.data, 3, lo.ctypes.data, hi.ctypes.data)
+    assert rc == 1 and b"out of range" in L.pbgb_bvh_last_error(None)
+    rc = L.pbgb_simplex_boxes(4, P.ctypes.data, 2, S.ctypes.data, 5, lo.ctypes.data, hi.ctypes.data)
+    assert rc == 1
+    with pytest.raises(ValueError):
+        pbat.gpu.geometry.Aabb(2, 4)
+    with pytest.raises(ValueError):
+        pbat.gpu.geometry.Aabb(3, 0).construct(np.zeros((3, 4), np.float32), np.zeros((5, 2), np.int32))
