@@ -64,13 +64,15 @@ extern "C" {
 #define PBGB_INIT_KINETIC_ENERGY_MINIMUM 2
 #define PBGB_INIT_ADAPTIVE_VBD 3
 #define PBGB_INIT_ADAPTIVE_PBAT 4
-/* sim/vbd/Enums.h:21-28 (only None and Chebyshev are implemented) */
+/* sim/vbd/Enums.h:21-28 (all six are implemented; which integrator runs a strategy follows the
+   reference's dispatch: the GPU integrator runs plain VBD for Nesterov and Broyden) */
 #define PBGB_ACCEL_NONE 0
 #define PBGB_ACCEL_CHEBYSHEV 1
-#define PBGB_ACCEL_ANDERSON 2 /* single mesh without contact; window_size columns */
-#define PBGB_ACCEL_NESTEROV 3 /* nesterov_lipschitz, nesterov_start */
-#define PBGB_ACCEL_BROYDEN 4 /* single mesh without contact; window_size columns */
-#define PBGB_ACCEL_TRUST_REGION 5 /* tr_eta, tr_tau, tr_curved; single mesh without contact */
+#define PBGB_ACCEL_ANDERSON 2 /* single mesh (contact allowed); window_size columns */
+#define PBGB_ACCEL_NESTEROV 3 /* nesterov_lipschitz, nesterov_start; single mesh without contact (a
+                                 CPU-integrator strategy) */
+#define PBGB_ACCEL_BROYDEN 4 /* single mesh without contact (a CPU-integrator strategy); window_size columns */
+#define PBGB_ACCEL_TRUST_REGION 5 /* tr_eta, tr_tau, tr_curved; single mesh (contact allowed) */
 /* graph/Enums.h:20-33 */
 #define PBGB_COLOR_ORDER_NATURAL 0
 #define PBGB_COLOR_ORDER_SMALLEST_DEGREE 1
@@ -266,6 +268,22 @@ PBGB_API int pbgb_vbd_stream(pbgb_vbd* h, void** stream);
 /* Contact lists after the last step: fc[8 nV] contact triangles per vertex (-1 = none) and
  * active[|V|] (1 if the collision vertex is in the active set).  Either may be NULL. */
 PBGB_API int pbgb_vbd_get_contacts(pbgb_vbd* h, int32_t* fc, uint8_t* active);
+/* The LBVH the last step built over the swept collision-triangle boxes (the active-set query of
+ * VertexTriangleMixedCcdDcd, gpu/impl/contact/VertexTriangleMixedCcdDcd.cu:51-136, on the
+ * hierarchy of gpu/impl/geometry/Bvh.cu:130-229): codes[nF] sorted Morton codes, inds[nF] the
+ * stable sort order, child[2(nF-1)], parent[2nF-1], rightmost[2(nF-1)] in the reference's node
+ * numbering; xpred[3 x nV] the full-step prediction the boxes were swept to (from the positions
+ * at the step's start) and scene_box[6] (min, max) the Morton normalisation box.  Any output may
+ * be NULL.  PBGB_ERR_INVALID_ARGUMENT without contact. */
+PBGB_API int pbgb_vbd_get_contact_bvh(
+    pbgb_vbd* h,
+    uint32_t* codes,
+    int32_t* inds,
+    int32_t* child,
+    int32_t* parent,
+    int32_t* rightmost,
+    float* xpred,
+    float* scene_box);
 
 /* Backward-Euler objective f(x) = 1/2 |x - xtilde|_M^2 + dt^2 sum wg Psi and its gradient at
  * the current positions against the last step's inertial target; FP64 device reductions. */
@@ -286,14 +304,17 @@ PBGB_API int pbgb_vbd_trust_region_log(pbgb_vbd* h, double* out, int32_t capacit
  * as applications whose device memory is owned and budgeted by another runtime or engine, or
  * frame loops that forbid allocation after start-up.  pbgb_vbd_gradient allocates its FP64
  * accumulation buffer on its first call; this variant accumulates in a fixed device array built
- * into the library instead (PBGB_NOALLOC_MAX_VERTICES x 3 doubles, 6 MiB, held by every device
- * that loads the library until the process exits).
+ * into the library instead (PBGB_NOALLOC_MAX_VERTICES x 3 doubles, 6 MiB per device).
+ *   - The array is reserved on a device during set-up: pbgb_vbd_create (and _create_batched) looks
+ *     up its device address there (cudaGetSymbolAddress, which loads the library's module on that
+ *     device), and the device keeps the 6 MiB until the process exits.  This entry point's own
+ *     calls allocate nothing and load nothing.
  *   - Meshes (or batches) with more than PBGB_NOALLOC_MAX_VERTICES vertices are rejected with
  *     PBGB_ERR_INVALID_ARGUMENT.
- *   - The first call on a device looks up that array's device address (cudaGetSymbolAddress,
- *     with the handle's device made current); make that first call before any stream capture.
  *   - All calls share the one array: the used part is cleared at the start of every call, and
  *     calls whose work overlaps on the GPU (different handles or streams at the same time) race.
+ *   - The address is kept by the handle: a device reset (cudaDeviceReset) invalidates the handle
+ *     together with its other device resources; create a new handle after one.
  *   - Output and blocking behaviour are those of pbgb_vbd_gradient: grad (3 x nV, host) is
  *     written and the call returns once the handle's stream is idle.
  */

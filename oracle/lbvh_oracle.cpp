@@ -232,9 +232,78 @@ void orc_bvh_boxes(int32_t n, int32_t const* child, int32_t const* inds, float c
     }
 }
 
-// All (query, box) pairs with overlapping closed boxes, brute force.  Returns the count; writes at
-// most `capacity` pairs, ordered by query then box.
+// All (query, box) pairs with overlapping closed boxes.  Returns the count; writes at most
+// `capacity` pairs, ordered by query then box.  Every pair is decided by the full closed-box test;
+// the boxes are only pre-sorted by their lower x so that each query tests the boxes whose lower x
+// lies in [q.lo.x - w, q.hi.x] (w: the widest box in x, in FP64), which contains every box that
+// can overlap it.  Queries run in parallel (OpenMP); each query's pairs are written at its prefix
+// offset, so the output does not depend on threading.
 int64_t orc_overlaps(int32_t n, float const* lo, float const* hi, int32_t nq, float const* qlo, float const* qhi, int32_t* pairs, int64_t capacity)
+{
+    auto overlap = [&](int32_t q, int32_t i) {
+        bool ov = true;
+        for (int d = 0; d < 3; ++d)
+            ov = ov && qlo[3 * size_t(q) + d] <= hi[3 * size_t(i) + d] && lo[3 * size_t(i) + d] <= qhi[3 * size_t(q) + d];
+        return ov;
+    };
+    std::vector<int32_t> order(size_t(std::max(n, 0)));
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return lo[3 * size_t(a)] < lo[3 * size_t(b)]; });
+    std::vector<float> keys(order.size());
+    double width = 0.0;
+    for (size_t k = 0; k < order.size(); ++k)
+    {
+        keys[k] = lo[3 * size_t(order[k])];
+        width   = std::max(width, double(hi[3 * size_t(order[k])]) - double(keys[k]));
+    }
+    auto candidates = [&](int32_t q, std::vector<int32_t>& hits) {
+        hits.clear();
+        double const from = double(qlo[3 * size_t(q)]) - width;
+        auto b = std::lower_bound(keys.begin(), keys.end(), from, [](float k, double v) { return double(k) < v; });
+        auto e = std::upper_bound(keys.begin(), keys.end(), qhi[3 * size_t(q)]);
+        for (auto it = b; it < e; ++it)
+        {
+            int32_t const i = order[size_t(it - keys.begin())];
+            if (overlap(q, i))
+                hits.push_back(i);
+        }
+        std::sort(hits.begin(), hits.end());
+    };
+    std::vector<int64_t> start(size_t(nq) + 1, 0);
+#pragma omp parallel
+    {
+        std::vector<int32_t> hits;
+#pragma omp for schedule(dynamic, 64)
+        for (int32_t q = 0; q < nq; ++q)
+        {
+            candidates(q, hits);
+            start[size_t(q) + 1] = int64_t(hits.size());
+        }
+    }
+    for (int32_t q = 0; q < nq; ++q)
+        start[size_t(q) + 1] += start[size_t(q)];
+#pragma omp parallel
+    {
+        std::vector<int32_t> hits;
+#pragma omp for schedule(dynamic, 64)
+        for (int32_t q = 0; q < nq; ++q)
+        {
+            int64_t k = start[size_t(q)];
+            if (k >= capacity || start[size_t(q) + 1] == k)
+                continue;
+            candidates(q, hits);
+            for (size_t j = 0; j < hits.size() && k < capacity; ++j, ++k)
+            {
+                pairs[2 * k]     = q;
+                pairs[2 * k + 1] = hits[j];
+            }
+        }
+    }
+    return start[size_t(nq)];
+}
+
+// The same pairs by testing every (query, box) pair (used to check orc_overlaps).
+int64_t orc_overlaps_all_pairs(int32_t n, float const* lo, float const* hi, int32_t nq, float const* qlo, float const* qhi, int32_t* pairs, int64_t capacity)
 {
     int64_t count = 0;
     for (int32_t q = 0; q < nq; ++q)

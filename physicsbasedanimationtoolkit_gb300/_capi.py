@@ -127,6 +127,7 @@ _SIGNATURES = [
     ("pbgb_vbd_set_sweep_timing", C.c_int, [_vp, _i32]),
     ("pbgb_vbd_sweep_timing", C.c_int, [_vp, C.POINTER(_f64), C.POINTER(C.c_int64)]),
     ("pbgb_vbd_get_contacts", C.c_int, [_vp, _vp, _vp]),
+    ("pbgb_vbd_get_contact_bvh", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("pbgb_vbd_objective", C.c_int, [_vp, _f64, C.POINTER(_f64)]),
     ("pbgb_vbd_trust_region_log", C.c_int, [_vp, _vp, _i32, C.POINTER(_i32)]),
     ("pbgb_vbd_gradient", C.c_int, [_vp, _f64, _vp]),

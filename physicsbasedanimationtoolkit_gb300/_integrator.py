@@ -208,6 +208,27 @@ class IntegratorBase:
         _capi.check(_capi.lib().pbgb_vbd_get_contacts(self._h, fc.ctypes.data, active.ctypes.data), self._h)
         return fc, active[:nS]
 
+    def contact_bvh(self):
+        """The LBVH the last step built over the swept collision-triangle boxes: a dict of the
+        sorted Morton codes, the sort order (inds), child / rightmost ((nF-1) x 2), parent, the
+        full-step prediction xpred (|#vertices| x 3) the boxes were swept to from the positions at
+        the step's start, and the scene box (min, max) the codes were normalised by."""
+        nF = int(np.asarray(self.data.F).shape[1])
+        nV = self.n_vertices
+        out = dict(codes=np.zeros(nF, np.uint32), inds=np.zeros(nF, np.int32),
+                   child=np.zeros(max(2 * (nF - 1), 1), np.int32), parent=np.zeros(max(2 * nF - 1, 1), np.int32),
+                   rightmost=np.zeros(max(2 * (nF - 1), 1), np.int32), xpred=np.zeros((nV, 3), np.float32),
+                   scene=np.zeros(6, np.float32))
+        _capi.check(_capi.lib().pbgb_vbd_get_contact_bvh(
+            self._h, out["codes"].ctypes.data, out["inds"].ctypes.data, out["child"].ctypes.data,
+            out["parent"].ctypes.data, out["rightmost"].ctypes.data, out["xpred"].ctypes.data,
+            out["scene"].ctypes.data), self._h)
+        out["child"] = out["child"][: 2 * (nF - 1)].reshape(-1, 2)
+        out["rightmost"] = out["rightmost"][: 2 * (nF - 1)].reshape(-1, 2)
+        out["parent"] = out["parent"][: 2 * nF - 1]
+        out["wmin"], out["wmax"] = out["scene"][:3].copy(), out["scene"][3:].copy()
+        return out
+
     def save_state(self):
         """Checkpoint of the step state (positions, velocities, previous velocities, external
         accelerations, contact active set and lists) as bytes."""

@@ -264,7 +264,7 @@ class VbdSystem
     DeviceArray<uint32_t> nbr;
     DeviceArray<uint2> incPack;
     DeviceArray<float4> mats;
-    DeviceArray<double> red, gradBuf;
+    DeviceArray<double> red, gradBuf, objPartials;
 
     // Sweep timing: with `profiling` on, the captured step records an event pair around the colour
     // sweeps of every iteration (event-record nodes in the graph).
@@ -691,6 +691,7 @@ class VbdSystem
         inc.allocate(hInc.size());
         flags.allocate(4);
         red.allocate(1);
+        objPartials.allocate(size_t(kObjectiveMaxBlocks));
         if (acceleration == PBGB_ACCEL_CHEBYSHEV)
         {
             h0.allocate(nV);
@@ -1503,7 +1504,6 @@ class VbdSystem
         std::vector<double> fs, gs, xs;
         StepHooks hooks;
         hooks.iterate = [&](int32_t, int32_t, float4 const* current) {
-            check(cudaMemsetAsync(red.get(), 0, sizeof(double), stream), "memset");
             check(launch_objective(energyParams(h, red.get(), current), stream), "objective");
             check(cudaMemsetAsync(gradBuf.get(), 0, sizeof(double) * 3 * size_t(nV), stream), "memset");
             check(launch_gradient(energyParams(h, gradBuf.get(), current), stream), "gradient");
@@ -1803,6 +1803,7 @@ class VbdSystem
         p.nT     = nT;
         p.dt2    = dt * dt;
         p.out    = out;
+        p.partials = objPartials.get();
         p.restEnergy = restEnergy();
         return p;
     }
@@ -1830,6 +1831,9 @@ class VbdSystem
 struct pbgb_vbd
 {
     pbgb::VbdSystem sys;
+    // Device address of the fixed accumulation array of pbgb_vbd_gradient_noalloc on the handle's
+    // device, looked up when the handle is created.
+    double* noallocScratch = nullptr;
 };
 
 namespace {
@@ -1878,6 +1882,21 @@ int guarded(pbgb_vbd* h, F&& f)
     }
 }
 
+// Fixed device array of pbgb_vbd_gradient_noalloc: one FP64 accumulator per vertex coordinate.
+// Every device on which this library's module is loaded holds it until the process exits.
+__device__ __align__(256) double gNoAllocGradient[3 * PBGB_NOALLOC_MAX_VERTICES];
+
+// Looks up the array's address on the current device.  In host code gNoAllocGradient is only a
+// stand-in for the symbol, not an address the GPU can use; cudaGetSymbolAddress also loads the
+// module on the device (the array is reserved there then), so that the entry point's own calls
+// neither allocate nor load anything.
+double* noalloc_scratch_address()
+{
+    void* p = nullptr;
+    check(cudaGetSymbolAddress(&p, gNoAllocGradient), "cudaGetSymbolAddress");
+    return static_cast<double*>(p);
+}
+
 int create_impl(pbgb_vbd_desc const* descs, int32_t n, pbgb_vbd** out)
 {
     if (!descs || n < 1 || !out)
@@ -1899,6 +1918,8 @@ int create_impl(pbgb_vbd_desc const* descs, int32_t n, pbgb_vbd** out)
     auto h = std::make_unique<pbgb_vbd>();
     int const rc = guarded(h.get(), [&] {
         h->sys.build(descs, n);
+        // build() made no device current other than the one the handle lives on.
+        h->noallocScratch = noalloc_scratch_address();
         return int(kOk);
     });
     if (rc != kOk)
@@ -2389,13 +2410,63 @@ PBGB_API int pbgb_vbd_get_contacts(pbgb_vbd* h, int32_t* fc, uint8_t* active)
     });
 }
 
+PBGB_API int pbgb_vbd_get_contact_bvh(
+    pbgb_vbd* h,
+    uint32_t* codes,
+    int32_t* inds,
+    int32_t* child,
+    int32_t* parent,
+    int32_t* rightmost,
+    float* xpred,
+    float* scene_box)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    return guarded(h, [&] {
+        auto& s = h->sys;
+        if (!s.contact)
+            throw std::invalid_argument("pbgb_vbd_get_contact_bvh: the integrator has no contact");
+        check(cudaStreamSynchronize(s.stream), "cudaStreamSynchronize");
+        auto const& B   = s.cstate.bvh;
+        size_t const nF = size_t(s.cmesh.nF);
+        auto get = [&](void* dst, void const* src, size_t bytes) {
+            if (dst && bytes > 0)
+                check(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost), "D2H");
+        };
+        get(codes, B.codes, sizeof(uint32_t) * nF);
+        get(inds, B.inds, sizeof(int32_t) * nF);
+        if (nF > 1)
+        {
+            get(child, B.child, sizeof(int32_t) * 2 * (nF - 1));
+            get(rightmost, B.rightmost, sizeof(int32_t) * 2 * (nF - 1));
+        }
+        get(parent, B.parent, sizeof(int32_t) * (2 * nF - 1));
+        if (xpred)
+        {
+            std::vector<float4> const p4 = s.deviceToHost(s.xpred.get());
+            for (size_t i = 0; i < p4.size(); ++i)
+            {
+                xpred[3 * i]     = p4[i].x;
+                xpred[3 * i + 1] = p4[i].y;
+                xpred[3 * i + 2] = p4[i].z;
+            }
+        }
+        if (scene_box)
+            for (int k = 0; k < 3; ++k)
+            {
+                scene_box[k]     = s.sceneMin[k];
+                scene_box[3 + k] = s.sceneMax[k];
+            }
+        return int(kOk);
+    });
+}
+
 PBGB_API int pbgb_vbd_objective(pbgb_vbd* h, double dt, double* f)
 {
     if (!h || !f)
         return fail(h, kInvalid, "null argument");
     return guarded(h, [&] {
         auto& s = h->sys;
-        pbgb::check(cudaMemsetAsync(s.red.get(), 0, sizeof(double), s.stream), "memset");
         pbgb::check(pbgb::launch_objective(s.energyParams(dt, s.red.get()), s.stream), "objective");
         pbgb::check(cudaMemcpyAsync(f, s.red.get(), sizeof(double), cudaMemcpyDeviceToHost, s.stream), "D2H");
         pbgb::check(cudaStreamSynchronize(s.stream), "sync");
@@ -2443,32 +2514,6 @@ PBGB_API int pbgb_vbd_gradient(pbgb_vbd* h, double dt, double* grad)
 
 } // extern "C"
 
-namespace {
-
-// Fixed device scratch of pbgb_vbd_gradient_noalloc: one FP64 accumulator per vertex coordinate.
-__device__ __align__(256) double gNoAllocGradient[3 * PBGB_NOALLOC_MAX_VERTICES];
-
-// Device address of gNoAllocGradient per device, looked up on the first call on that device (the
-// host-side name is only a stand-in for the symbol, not an address the GPU can use).
-std::mutex gNoAllocMutex;
-double* gNoAllocAddress[256] = {};
-
-double* noalloc_scratch(int device)
-{
-    if (device < 0 || device >= 256)
-        throw std::invalid_argument("device ordinal out of range");
-    std::lock_guard<std::mutex> lock(gNoAllocMutex);
-    if (!gNoAllocAddress[device])
-    {
-        void* p = nullptr;
-        check(cudaGetSymbolAddress(&p, gNoAllocGradient), "cudaGetSymbolAddress");
-        gNoAllocAddress[device] = static_cast<double*>(p);
-    }
-    return gNoAllocAddress[device];
-}
-
-} // namespace
-
 extern "C" {
 
 PBGB_API int pbgb_vbd_gradient_noalloc(pbgb_vbd* h, double dt, double* grad)
@@ -2481,30 +2526,18 @@ PBGB_API int pbgb_vbd_gradient_noalloc(pbgb_vbd* h, double dt, double* grad)
             kInvalid,
             "pbgb_vbd_gradient_noalloc: " + std::to_string(h->sys.nV) + " vertices exceed the fixed scratch of " +
                 std::to_string(PBGB_NOALLOC_MAX_VERTICES) + " vertices; use pbgb_vbd_gradient");
+    if (!h->noallocScratch)
+        return fail(h, kInternal, "pbgb_vbd_gradient_noalloc: the handle has no scratch address");
     return guarded(h, [&] {
         auto& s  = h->sys;
-        int prev = 0;
-        check(cudaGetDevice(&prev), "cudaGetDevice");
-        if (prev != s.device)
-            check(cudaSetDevice(s.device), "cudaSetDevice");
-        int rc = kOk;
-        try
-        {
-            double* d = noalloc_scratch(s.device);
-            check(cudaMemsetAsync(d, 0, sizeof(double) * 3 * size_t(s.nV), s.stream), "cudaMemsetAsync");
-            check(pbgb::launch_gradient(s.energyParams(dt, d), s.stream), "gradient");
-            check(cudaMemcpyAsync(grad, d, sizeof(double) * 3 * size_t(s.nV), cudaMemcpyDeviceToHost, s.stream), "D2H");
-            check(cudaStreamSynchronize(s.stream), "cudaStreamSynchronize");
-        }
-        catch (...)
-        {
-            if (prev != s.device)
-                cudaSetDevice(prev);
-            throw;
-        }
-        if (prev != s.device)
-            check(cudaSetDevice(prev), "cudaSetDevice");
-        return rc;
+        double* d = h->noallocScratch;
+        // Stream-ordered calls on the handle's own stream: no device switch is needed (the stream
+        // belongs to the handle's device).  The used part of the shared array starts at zero.
+        check(cudaMemsetAsync(d, 0, sizeof(double) * 3 * size_t(s.nV), s.stream), "cudaMemsetAsync");
+        check(pbgb::launch_gradient(s.energyParams(dt, d), s.stream), "gradient");
+        check(cudaMemcpyAsync(grad, d, sizeof(double) * 3 * size_t(s.nV), cudaMemcpyDeviceToHost, s.stream), "D2H");
+        check(cudaStreamSynchronize(s.stream), "cudaStreamSynchronize");
+        return int(kOk);
     });
 }
 

@@ -448,18 +448,37 @@ __global__ void end_substep_kernel(SubstepParams p)
 }
 
 // Objective of the backward-Euler step (sim/vbd/Integrator.cpp:138-165): per-entity terms in FP32,
-// the global sum in FP64.
-__global__ void objective_kernel(EnergyParams p)
+// the global sum in FP64.  Entity j is always summed by the same thread of the same block of a
+// fixed grid, warps and blocks are added in index order, so the value is the same on every run.
+__global__ void __launch_bounds__(256) objective_kernel(EnergyParams p)
 {
+    __shared__ double warps[8];
     double acc  = 0.0;
     int const n = p.nV > p.nT ? p.nV : p.nT;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
         acc += objective_term(p, j);
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        acc += p.dt2 * p.restEnergy;
     acc = warp_sum(acc);
     if ((threadIdx.x & 31) == 0)
-        atomicAdd(p.out, acc);
+        warps[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        double b = 0.0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w)
+            b += warps[w];
+        p.partials[blockIdx.x] = b;
+    }
+}
+
+// Sum of the objective's block partials in block order, plus the rest-state energy.
+__global__ void __launch_bounds__(32) objective_finish_kernel(EnergyParams p, int32_t blocks)
+{
+    double acc = 0.0;
+    for (int b = int(threadIdx.x); b < blocks; b += 32)
+        acc += p.partials[b];
+    acc = warp_sum(acc);
+    if (threadIdx.x == 0)
+        p.out[0] = acc + p.dt2 * p.restEnergy;
 }
 
 // Gradient of the objective (sim/vbd/Integrator.cpp:167-200): inertial part per vertex, elastic
@@ -619,6 +638,10 @@ cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebys
         return cudaSuccess;
     if (stagedBytes > kStagedMaxBytes || (stagedBytes > 0 && (!p.nbrPtr || !p.nbr || !p.incPack || !p.mats)))
         return cudaErrorInvalidValue;
+    // Contact terms exist only in the two-buffer sweep (a contact partner of the same colour is
+    // read as it was before the pass): a one-buffer launch with contact lists is a caller error.
+    if (p.fc && !chebyshev)
+        return cudaErrorInvalidValue;
     int const g   = blocks_for(n, block);
     SweepParams q = p;
     q.slab        = int32_t(stagedBytes / kStagedSlotBytesMax);
@@ -705,13 +728,19 @@ cudaError_t launch_end_substep(SubstepParams const& p, cudaStream_t s)
 
 cudaError_t launch_objective(EnergyParams const& p, cudaStream_t s)
 {
+    if (!p.partials || !p.out)
+        return cudaErrorInvalidValue;
     int const n = p.nV > p.nT ? p.nV : p.nT;
     int g       = blocks_for(n, 256);
-    if (g > 4096)
-        g = 4096;
+    if (g > kObjectiveMaxBlocks)
+        g = kObjectiveMaxBlocks;
     if (g < 1)
         g = 1;
     objective_kernel<<<g, 256, 0, s>>>(p);
+    cudaError_t const e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    objective_finish_kernel<<<1, 32, 0, s>>>(p, g);
     return cudaGetLastError();
 }
 

@@ -122,6 +122,9 @@ struct EnergyParams
     int32_t nT;
     double dt2;
     double* __restrict__ out; // objective: out[0]; gradient: 3 x nV
+    // Objective only: kObjectiveMaxBlocks per-block partial sums, added in block order into out[0]
+    // (a fixed grid and fixed orders make the value identical from run to run).
+    double* __restrict__ partials;
     // sum_e wg_e mu_e^2 / (2 lambda_e): the elastic energy of the rest state, which the objective
     // adds once (times dt^2) so that per-tet terms carry only what varies with x.
     double restEnergy;
@@ -154,6 +157,9 @@ size_t constexpr kStagedSlotBytesMax = 2 * sizeof(float4);
 cudaError_t prepare_staged_sweeps();
 cudaError_t launch_begin_substep(SubstepParams const& p, cudaStream_t s);
 cudaError_t launch_end_substep(SubstepParams const& p, cudaStream_t s);
+// Blocks of the objective's reduction grid (p.partials holds this many doubles).
+int constexpr kObjectiveMaxBlocks = 1024;
+// Writes the objective to p.out[0] (no prior clearing needed); deterministic.
 cudaError_t launch_objective(EnergyParams const& p, cudaStream_t s);
 cudaError_t launch_gradient(EnergyParams const& p, cudaStream_t s);
 cudaError_t launch_pack3(float const* in3, float4* out4, int32_t n, cudaStream_t s);

@@ -1,10 +1,10 @@
 """Generates the golden fixtures of tests/golden/ from the reference's own code.
 
-Run in a checkout where the reference sources are available (``make -C oracle ref`` builds
-``oracle/_ref/libpbat_ref.so`` from them):
+Run where the reference sources are available, with PBAT_REF_SRC naming the reference checkout's
+``source/`` directory (``make -C oracle ref`` then builds ``oracle/_ref/libpbat_ref.so`` from them):
 
-    python tests/golden/make_golden.py          # every fixture
-    python tests/golden/make_golden.py ccd      # only ccd.npz
+    PBAT_REF_SRC=/root/reference/source python tests/golden/make_golden.py      # every fixture
+    PBAT_REF_SRC=/root/reference/source python tests/golden/make_golden.py ccd  # only ccd.npz
 
 Every fixture is produced by calling the reference's header-only kernels through the harness
 (oracle/ref_harness.cpp), on seeded inputs, so the oracle can be pinned on machines without the

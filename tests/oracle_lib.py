@@ -117,6 +117,8 @@ def lib():
                                       C.c_int32, C.c_int32, C.c_int32]
         L.orc_overlaps.restype = C.c_int64
         L.orc_overlaps.argtypes = [C.c_int32, _f32p, _f32p, C.c_int32, _f32p, _f32p, _i32p, C.c_int64]
+        L.orc_overlaps_all_pairs.restype = C.c_int64
+        L.orc_overlaps_all_pairs.argtypes = [C.c_int32, _f32p, _f32p, C.c_int32, _f32p, _f32p, _i32p, C.c_int64]
         L.orc_ccd_vertex_triangle.restype = C.c_int
         L.orc_ccd_vertex_triangle.argtypes = [C.c_int32, _f64p, _f64p, C.c_int32, _i32p, C.c_int32, _i32p, _i32p,
                                               _f64p, _i32p]
@@ -413,16 +415,18 @@ def morton(lo, hi, wmin, wmax):
     return codes
 
 
-def overlaps(lo, hi, qlo, qhi):
-    """Brute-force overlapping (query, box) pairs as a set of tuples."""
+def overlaps(lo, hi, qlo, qhi, all_pairs=False):
+    """Overlapping (query, box) pairs (n x 2, ordered by query then box), every candidate decided
+    by the closed-box test; ``all_pairs`` tests every pair instead of the x-sorted candidates."""
     lo = np.ascontiguousarray(lo, np.float32)
     hi = np.ascontiguousarray(hi, np.float32)
     qlo = np.ascontiguousarray(qlo, np.float32)
     qhi = np.ascontiguousarray(qhi, np.float32)
+    fn = lib().orc_overlaps_all_pairs if all_pairs else lib().orc_overlaps
     cap = 1 << 20
     while True:
         pairs = np.zeros(2 * cap, np.int32)
-        c = lib().orc_overlaps(lo.shape[0], lo, hi, qlo.shape[0], qlo, qhi, pairs, cap)
+        c = fn(lo.shape[0], lo, hi, qlo.shape[0], qlo, qhi, pairs, cap)
         if c <= cap:
             return pairs[: 2 * c].reshape(-1, 2)
         cap = int(c)

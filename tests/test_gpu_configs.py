@@ -1,0 +1,158 @@
+"""Parity at the benchmark configurations, full size, against the FP64 oracle.
+
+These are the workloads every throughput figure of bench.py is measured on:
+
+* the beam: [0,4]x[0,1]^2 as 160x40x40 hexes x 6 tets (270,641 vertices), E 5e5, nu 0.48, the
+  x=0 face pinned, initial velocities U(-0.1, 0.1), Chebyshev rho 0.95 (the reference's weight
+  recurrence), 50 iterations, 60 steps of 1/60 s, on the GPU integrator;
+* the batch: 256 cube grids with side U{6..32} hexes, E log-uniform in [1e5, 1e7], nu U(0.30,
+  0.48), one face pinned, gravity, 20 iterations, stepped together by one batched integrator;
+* the contact scene: 16 cubes of 16^3 hexes above a pinned 64x64x2 slab, vertex-triangle
+  contact (muC 1e7, muF 0.3, epsv 1e-3), 30 iterations, 120 steps, the LBVH over the swept
+  collision triangles rebuilt every step.
+
+Tolerance: positions within 1e-4 of the bounding-box diagonal (FP32 device arithmetic against
+the FP64 oracle on the same mesh, colouring and iteration count); the LBVH's Morton codes, sort
+order, topology and overlap pairs bit for bit.
+"""
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from physicsbasedanimationtoolkit_gb300 import meshgen, pbat
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4  # of the bounding-box diagonal
+
+
+def diag(X):
+    return float(np.linalg.norm(X.max(0) - X.min(0)))
+
+
+def test_beam_160x40x40_chebyshev_60_steps_matches_oracle():
+    w = meshgen.beam_workload(nx=160, ny=40, nz=40, seed=0)
+    data = (pbat.sim.vbd.Data().with_volume_mesh(w["X"].T, w["T"].T).with_material(w["rho"], w["mu"], w["lam"])
+            .with_dirichlet_vertices(w["dbc"]).with_velocity(w["v"].T).with_chebyshev_acceleration(0.95)
+            .construct())
+    I = pbat.gpu.vbd.Integrator(data)
+    R = O.OracleVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], v=w["v"], strategy=4,
+                    rho_chebyshev=0.95, chebyshev_formula=0, semantics=1)
+    d = diag(w["X"])
+    errs = []
+    for _ in range(6):
+        for _ in range(10):
+            I.step(1 / 60, 50, 1)
+        R.step(1 / 60, 50, 1, 10)
+        errs.append(float(np.abs(I.x.T.astype(np.float64) - R.x).max() / d))
+    assert max(errs) <= TOL, errs
+    # The beam moved: its free end swings by centimetres under gravity and the initial velocities.
+    assert np.abs(R.x - w["X"]).max() > 1e-2
+
+
+def test_batch_of_256_meshes_matches_oracle_per_mesh():
+    """The whole 256-mesh batch is stepped by one batched integrator; a seeded subset of meshes
+    that includes the smallest and the largest is checked against its own oracle after every
+    step."""
+    meshes = meshgen.batch_workload(n_meshes=256, nmin=6, nmax=32, seed=0)
+    datas = [pbat.sim.vbd.Data().with_volume_mesh(m["X"].T, m["T"].T).with_material(m["rho"], m["mu"], m["lam"])
+             .with_dirichlet_vertices(m["dbc"]).construct() for m in meshes]
+    B = pbat.gpu.vbd.BatchedIntegrator(datas)
+    sides = np.array([m["side"] for m in meshes])
+    rng = np.random.default_rng(5)
+    pick = {int(np.argmin(sides)), int(np.argmax(sides))}
+    pick |= set(int(b) for b in rng.choice(len(meshes), 6, replace=False))
+    pick = sorted(pick)
+    assert sides[pick].min() == 6 and sides[pick].max() == 32
+    oracles = {b: O.OracleVbd(meshes[b]["X"], meshes[b]["T"], meshes[b]["rho"], meshes[b]["mu"], meshes[b]["lam"],
+                              meshes[b]["dbc"], v=meshes[b]["v"], strategy=4, semantics=1) for b in pick}
+    off = B.vertex_offsets
+    worst = 0.0
+    for _ in range(3):
+        B.step(1 / 60, 20, 1)
+        x = B.x
+        for b in pick:
+            oracles[b].step(1 / 60, 20, 1, 1)
+            xb = x[:, off[b]: off[b + 1]].T.astype(np.float64)
+            worst = max(worst, float(np.abs(xb - oracles[b].x).max() / diag(meshes[b]["X"])))
+    assert worst <= TOL, worst
+    # Every mesh of the batch moved and stayed finite.
+    x = B.x
+    assert np.isfinite(x).all()
+    for b in range(len(meshes)):
+        assert np.abs(x[:, off[b]: off[b + 1]].T - meshes[b]["X"]).max() > 1e-4
+
+
+def contact_scene_integrator():
+    w = meshgen.contact_scene_workload()
+    data = (pbat.sim.vbd.Data().with_volume_mesh(w["X"].T, w["T"].T).with_surface_mesh(w["V"], w["F"].T)
+            .with_bodies(w["B"]).with_material(w["rho"], w["mu"], w["lam"]).with_dirichlet_vertices(w["dbc"])
+            .with_contact_parameters(1e7, 0.3, 1e-3).with_initialization_strategy(2).construct())
+    return w, pbat.gpu.vbd.Integrator(data)
+
+
+def sorted_pairs(p):
+    p = np.asarray(p).reshape(-1, 2)
+    return p[np.lexsort((p[:, 1], p[:, 0]))]
+
+
+def test_contact_scene_lbvh_bit_exact_at_every_step_of_120():
+    """At every one of the 120 steps, the hierarchy the step built over its swept triangle boxes
+    (from the positions at the step's start and the full-step prediction) has the oracle's Morton
+    codes, stable sort order, child / parent / rightmost topology, and the overlap pairs of the
+    swept vertex boxes against those triangle boxes are the all-pairs set, bit for bit."""
+    w, I = contact_scene_integrator()
+    F = np.asarray(w["F"])
+    V = np.asarray(w["V"])
+    nF = F.shape[0]
+    bvh = pbat.gpu.geometry.Bvh(nF, 0)
+    q_total = 0
+    for step in range(120):
+        x0 = I.x.T.copy()  # float32 positions at the step's start
+        I.step(1 / 60, 30, 1)
+        bv = I.contact_bvh()
+        xp = bv["xpred"]
+        lo, hi = meshgen.triangle_boxes(x0, F, xp)
+        lo, hi = lo.astype(np.float32), hi.astype(np.float32)
+        o = O.bvh_build(lo, hi, bv["wmin"], bv["wmax"])
+        np.testing.assert_array_equal(bv["codes"], o["codes"], err_msg=f"step {step}: Morton codes")
+        np.testing.assert_array_equal(bv["inds"], o["inds"], err_msg=f"step {step}: sort order")
+        np.testing.assert_array_equal(bv["child"], o["child"], err_msg=f"step {step}: children")
+        np.testing.assert_array_equal(bv["parent"], o["parent"], err_msg=f"step {step}: parents")
+        np.testing.assert_array_equal(bv["rightmost"], o["rightmost"], err_msg=f"step {step}: rightmost")
+        # Overlap pairs of the swept collision-vertex boxes on the same boxes: the public Bvh (the
+        # same build and query kernels) against all pairs.
+        qlo = np.minimum(x0[V], xp[V]).astype(np.float32)
+        qhi = np.maximum(x0[V], xp[V]).astype(np.float32)
+        bvh.build(lo.T, hi.T, bv["wmin"], bv["wmax"])
+        t = bvh._topology()
+        np.testing.assert_array_equal(t["inds"], bv["inds"])
+        np.testing.assert_array_equal(t["child"], bv["child"])
+        got = sorted_pairs(bvh.overlaps(qlo.T, qhi.T).T)
+        exp = O.overlaps(lo, hi, qlo, qhi)
+        np.testing.assert_array_equal(got, exp, err_msg=f"step {step}: overlap pairs")
+        q_total += exp.shape[0]
+    assert q_total > 120 * V.size  # every vertex box overlaps at least its own triangles' boxes
+    x = I.x.T
+    assert np.isfinite(x).all()
+    fc, active = I.contacts()
+    assert active.sum() > 100  # the cubes rest on the slab
+
+
+def test_contact_scene_positions_match_contact_oracle_through_first_contact():
+    """The first 20 steps (the cubes start 5 cm above the slab and touch it at about step 6)
+    against the FP64 contact oracle."""
+    w, I = contact_scene_integrator()
+    R = O.OracleContactVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], w["V"], w["F"], w["B"],
+                           muC=1e7, muF=0.3, epsv=1e-3, strategy=2)
+    d = diag(w["X"])
+    errs, first_contact = [], None
+    for step in range(20):
+        I.step(1 / 60, 30, 1)
+        R.step(1 / 60, 30, 1, 1)
+        errs.append(float(np.abs(I.x.T.astype(np.float64) - R.x).max() / d))
+        if first_contact is None and R.active.any():
+            first_contact = step
+    assert first_contact is not None and first_contact < 15, first_contact
+    assert max(errs) <= TOL, errs

@@ -142,6 +142,15 @@ def test_objective_and_gradient_fp64_reductions_match_oracle():
     assert np.abs(g_gpu - g_orc).max() <= 1e-3 * np.abs(g_orc).max()
 
 
+def test_objective_is_deterministic():
+    """Fixed grid, fixed summation orders: repeated evaluations give the same bits."""
+    w = meshgen.unit_cube_workload(n=12, seed=6)
+    I = pbat.gpu.vbd.Integrator(make_data(w))
+    I.step(1 / 60, 10, 1)
+    f = [I.objective(1 / 60) for _ in range(8)]
+    assert all(np.float64(v).tobytes() == np.float64(f[0]).tobytes() for v in f), f
+
+
 @pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32])
 def test_lanes_per_vertex_do_not_change_results(lanes):
     w = meshgen.unit_cube_workload(n=6, seed=4)

@@ -87,3 +87,31 @@ def test_brute_force_overlaps():
     qhi = np.array([[2, 2, 2], [1.6, 1.6, 1.6], [2.6, 4, 2.6]], np.float32)
     pairs = O.overlaps(lo, hi, qlo, qhi)
     assert {tuple(p) for p in pairs} == {(0, 0), (0, 1), (2, 1)}
+    np.testing.assert_array_equal(pairs, O.overlaps(lo, hi, qlo, qhi, all_pairs=True))
+
+
+@pytest.mark.parametrize("case", ["random", "touching", "duplicates", "wide", "negative"])
+def test_pruned_overlaps_equal_all_pairs(case):
+    """The x-sorted candidate search returns exactly the pairs of the all-pairs test, in the same
+    order (query, then box index)."""
+    rng = np.random.default_rng(len(case))
+    n, nq = 3000, 1500
+    lo = rng.uniform(0, 1, (n, 3)).astype(np.float32)
+    hi = (lo + rng.uniform(0, 0.03, (n, 3))).astype(np.float32)
+    qlo = rng.uniform(0, 1, (nq, 3)).astype(np.float32)
+    qhi = (qlo + rng.uniform(0, 0.03, (nq, 3))).astype(np.float32)
+    if case == "touching":  # queries whose lower x equals a box's upper x (closed boxes)
+        qlo[:500, 0] = hi[:500, 0]
+        qlo[:500, 1:] = lo[:500, 1:]
+        qhi[:500] = np.maximum(qhi[:500], qlo[:500])
+    elif case == "duplicates":
+        lo[: n // 2] = lo[n // 2:]
+        hi[: n // 2] = hi[n // 2:]
+    elif case == "wide":  # one very wide box widens every candidate range
+        lo[7], hi[7] = [-5, 0, 0], [5, 1, 1]
+    elif case == "negative":
+        lo, hi, qlo, qhi = lo - 2.0, hi - 2.0, qlo - 2.0, qhi - 2.0
+    got = O.overlaps(lo, hi, qlo, qhi)
+    exp = O.overlaps(lo, hi, qlo, qhi, all_pairs=True)
+    assert exp.shape[0] > 0
+    np.testing.assert_array_equal(got, exp)
