@@ -230,12 +230,10 @@ def run_reference(args):
     return 0
 
 
-def run_batch(args, pbat, _capi, torch):
-    """Batched uneven meshes: 256 cube grids with side n ~ U{6..32} hexes (6 tets per hex),
-    E log-uniform in [1e5, 1e7], nu ~ U(0.30, 0.48), density 1000, one face pinned, gravity,
-    20 iterations per step, dt = 1/60.  One captured launch sequence steps the whole batch; the
-    comparison steps one integrator per mesh (each on its own stream, all launched before one
-    wait).  Returns the batch figures and the agreement between the two."""
+def batch_workload(args, pbat):
+    """The batched workload: 256 cube grids with side n ~ U{6..32} hexes (6 tets per hex), E
+    log-uniform in [1e5, 1e7], nu ~ U(0.30, 0.48), density 1000, one face pinned, gravity, 20
+    iterations per step, dt = 1/60."""
     from physicsbasedanimationtoolkit_gb300 import meshgen
 
     meshes = meshgen.batch_workload(n_meshes=args.batch_meshes, nmin=6, nmax=32, seed=0)
@@ -244,78 +242,126 @@ def run_batch(args, pbat, _capi, torch):
         .with_dirichlet_vertices(m["dbc"]).construct()
         for m in meshes
     ]
+    return meshes, datas
+
+
+def batch_algorithmic_bytes(datas, iterations):
+    """Algorithmic bytes of one batched step: per iteration the sum over every mesh's free vertices
+    of (60 + 120 deg(i)) bytes (the vertex-update formula of the sweep), plus per substep the
+    inertial target and initial guess (48 B read, 64 B written per vertex) and the velocity update
+    (48 B read, 32 B written per vertex)."""
+    per_iter = sum(algorithmic_bytes(d) for d in datas)
+    nV = sum(int(d.X.shape[1]) for d in datas)
+    return iterations * per_iter + (112 + 80) * nV
+
+
+def time_single_launch(singles, dt, iters, steps, torch):
+    """One integrator per mesh, each on its own stream: all steps of all meshes are launched, then
+    waited for.  Timed with CUDA events: a start event on a master stream that every integrator's
+    stream waits on, an end event on every integrator's stream that the master waits on."""
+    from physicsbasedanimationtoolkit_gb300 import _capi
+
+    master = torch.cuda.Stream()
+    streams = []
+    for s in singles:
+        sp = C.c_void_p()
+        _capi.check(_capi.lib().pbgb_vbd_stream(s.handle, C.byref(sp)), s.handle)
+        streams.append(torch.cuda.ExternalStream(sp.value))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(master)
+    for st in streams:
+        st.wait_event(e0)
+    for _ in range(steps):
+        for s in singles:
+            s.step(dt, iters, 1)
+    for st in streams:
+        ev = torch.cuda.Event()
+        ev.record(st)
+        master.wait_event(ev)
+    e1.record(master)
+    e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3
+
+
+def run_batch(args, pbat, _capi, torch, with_single=True):
+    """Batched uneven meshes (batch_workload): one persistent launch per step advances the whole
+    batch; the comparison steps one integrator per mesh, one launch per colour, each on its own
+    stream (all launched before one wait).  Both arms are timed with CUDA events on their streams.
+    Returns the batch figures and the agreement between the two (bit for bit: same lanes, block
+    size and per-vertex arithmetic)."""
+    meshes, datas = batch_workload(args, pbat)
     dt, iters = 1 / 60, args.batch_iterations
     B = pbat.gpu.vbd.BatchedIntegrator(datas)
     lanes, block, tuned_ms = B.autotune(dt, iters, 1)
-    singles = []
-    for d in datas:
-        s = pbat.gpu.vbd.Integrator(d)
-        s.lanes_per_vertex = lanes
-        _capi.check(_capi.lib().pbgb_vbd_set_block_size(s.handle, block), s.handle)
-        singles.append(s)
     n_free = B.n_free
-    for _ in range(args.warmup):
-        B.step(dt, iters, 1)
-        for s in singles:
-            s.step(dt, iters, 1)
-    B.synchronize()
-    for s in singles:
-        s.synchronize()
     sp = C.c_void_p()
     _capi.check(_capi.lib().pbgb_vbd_stream(B.handle, C.byref(sp)), B.handle)
     stream = torch.cuda.ExternalStream(sp.value)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(args.warmup):
         B.step(dt, iters, 1)
-    e1.record(stream)
     B.synchronize()
-    t_batched = e0.elapsed_time(e1) * 1e-3
-    t0 = time.perf_counter()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t_batched = 0.0
     for _ in range(args.steps):
-        for s in singles:
-            s.step(dt, iters, 1)
-    for s in singles:
-        s.synchronize()
-    t_single = time.perf_counter() - t0
-    # Agreement between the two forms (same lanes and block size: same arithmetic per vertex).
-    xb = B.x
-    off = B.vertex_offsets
-    worst = 0.0
-    for b, s in enumerate(singles):
-        X = meshes[b]["X"]
-        diag = np.linalg.norm(X.max(0) - X.min(0))
-        worst = max(worst, float(np.abs(xb[:, off[b]: off[b + 1]] - s.x).max() / diag))
-    # One mesh at a time (each step waited for before the next mesh's), as separate integrators
-    # run by a caller that does not overlap them.  After the agreement check: it advances the
-    # single integrators further.
-    serial_steps = min(args.steps, 10)  # ~0.25 s per step: bounded so the leg stays short
-    t0 = time.perf_counter()
-    for _ in range(serial_steps):
-        for s in singles:
-            s.step(dt, iters, 1)
-            s.synchronize()
-    t_serial = (time.perf_counter() - t0) * args.steps / serial_steps
-    launches = B.launches_per_step(iters, 1)
-    return {
+        flush.add_(1.0)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        B.step(dt, iters, 1)
+        e1.record(stream)
+        B.synchronize()
+        t_batched += e0.elapsed_time(e1) * 1e-3
+    out = {
         "workload": f"{len(meshes)} cube grids, side U{{6..32}} hexes x 6 tets, {iters} iterations, no acceleration",
         "n_meshes": len(meshes),
         "n_vertices": int(B.n_vertices),
         "n_tets": int(B.n_tets),
+        "n_free_vertices": int(n_free),
+        "persistent": bool(B.persistent),
         "batched_value": n_free * iters * args.steps / t_batched,
-        "single_launch_value": n_free * iters * args.steps / t_single,
-        "speedup": t_single / t_batched,
-        "single_launch_serial_value": n_free * iters * args.steps / t_serial,
-        "speedup_vs_serial": t_serial / t_batched,
         "batched_ms_per_step": 1e3 * t_batched / args.steps,
-        "single_launch_ms_per_step": 1e3 * t_single / args.steps,
-        "max_rel_diff_batched_vs_single": worst,
         "autotuned": {"lanes": lanes, "block": block, "ms_per_step": tuned_ms},
-        "batched_launches_per_step": int(launches),
-        "single_launches_per_step": int(sum(s.launches_per_step(iters, 1) for s in singles)),
+        "batched_launches_per_step": int(B.launches_per_step(iters, 1)),
+        "algorithmic_bytes_per_step": batch_algorithmic_bytes(datas, iters),
+        "timing": "CUDA events on each arm's streams; L2 flushed before every batched step",
         "unit": UNIT,
     }
+    if with_single:
+        singles = []
+        for d in datas:
+            s = pbat.gpu.vbd.Integrator(d)
+            s.lanes_per_vertex = lanes
+            _capi.check(_capi.lib().pbgb_vbd_set_block_size(s.handle, block), s.handle)
+            singles.append(s)
+        for _ in range(args.warmup):
+            for s in singles:
+                s.step(dt, iters, 1)
+        for s in singles:
+            s.synchronize()
+        # Agreement from the same number of steps: a fresh batch against the single integrators.
+        off = B.vertex_offsets
+        B2 = pbat.gpu.vbd.BatchedIntegrator(datas)
+        B2.lanes_per_vertex = lanes
+        _capi.check(_capi.lib().pbgb_vbd_set_block_size(B2.handle, block), B2.handle)
+        for _ in range(args.warmup):
+            B2.step(dt, iters, 1)
+        xb = B2.x
+        worst = 0.0
+        for b, s in enumerate(singles):
+            X = meshes[b]["X"]
+            diag = np.linalg.norm(X.max(0) - X.min(0))
+            worst = max(worst, float(np.abs(xb[:, off[b]: off[b + 1]] - s.x).max() / diag))
+        del B2
+        t_single = time_single_launch(singles, dt, iters, args.steps, torch)
+        out.update({
+            "single_launch_value": n_free * iters * args.steps / t_single,
+            "single_launch_ms_per_step": 1e3 * t_single / args.steps,
+            "speedup": t_single / t_batched,
+            "single_launches_per_step": int(sum(s.launches_per_step(iters, 1) for s in singles)),
+            "max_rel_diff_batched_vs_single": worst,
+        })
+    return out
 
 
 def run_adjoint(args, pbat, torch):

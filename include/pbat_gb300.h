@@ -262,6 +262,17 @@ PBGB_API int pbgb_vbd_launches_per_step(pbgb_vbd* h, int32_t iterations, int32_t
  * summed sweep intervals in milliseconds and the number of sweep kernel launches they cover. */
 PBGB_API int pbgb_vbd_set_sweep_timing(pbgb_vbd* h, int32_t enable);
 PBGB_API int pbgb_vbd_sweep_timing(pbgb_vbd* h, double* milliseconds, int64_t* sweep_launches);
+/* Persistent batched step (handles of several meshes; no counterpart in the reference, which steps
+ * one mesh per integrator, gpu/impl/vbd/Integrator.cu:82-103).  On by default: one kernel launch
+ * per step advances every mesh, each mesh moving to its next colour as soon as its own previous
+ * colour is done (per-mesh completion counters, bounded waits: a wait that gives up makes the next
+ * synchronizing call return PBGB_ERR_TIMEOUT).  Used for plain VBD and Chebyshev without contact
+ * when every colour's neighbours fit in shared memory; otherwise, or when disabled, a batch steps
+ * with one launch per colour.  pbgb_vbd_persistent reports whether the next step uses it.
+ * pbgb_vbd_set_batch_tile: sweep work items of subtiles x (block / lanes) vertices (default 1). */
+PBGB_API int pbgb_vbd_set_persistent(pbgb_vbd* h, int32_t enable);
+PBGB_API int pbgb_vbd_persistent(pbgb_vbd* h, int32_t* active);
+PBGB_API int pbgb_vbd_set_batch_tile(pbgb_vbd* h, int32_t subtiles);
 /* The handle's CUDA stream (cudaStream_t) so callers can order their own work after a step. */
 PBGB_API int pbgb_vbd_stream(pbgb_vbd* h, void** stream);
 
@@ -458,6 +469,12 @@ PBGB_API int pbgb_debug_adjoint_tet(
     double* dphi,
     double* dlogmu,
     double* dloglambda);
+
+/* Test hook of the persistent batched step's bounded waits: the time limit of one wait (1 us ..
+ * 2 s; default 2 s) and one work item whose requirement is never met (-1: none), for the steps that
+ * follow.  With a poisoned item the step's wait gives up after wait_ns, the step ends with invalid
+ * positions and the next synchronizing call returns PBGB_ERR_TIMEOUT; the context stays usable. */
+PBGB_API int pbgb_debug_batched_wait(pbgb_vbd* h, int64_t wait_ns, int32_t poison_item);
 
 /* Host self-check of the closed-form vertex block (FP64): accumulates n incident tets and
  * applies damping, inertia and the Newton step exactly like the device sweep.  Arguments as the

@@ -198,6 +198,10 @@ struct orc_contact
     uint8_t* active;  // nSurfV
     double* dupper;   // nSurfV
     int32_t* fc;      // nV * 8
+    // Replay (nullable): contact lists to use at every list update instead of the oracle's own
+    // nearest-triangle queries, nV * 8 per update (the device's lists), so that positions can be
+    // compared with the discrete decisions held equal.
+    int32_t const* forced_fc;
 };
 
 namespace {
@@ -373,7 +377,12 @@ int orc_run_contact(orc_problem const* Pp, orc_contact const* Cp, double* x, dou
                 for (int d = 0; d < 3; ++d)
                     xo[d] = tt[d] + sdt * vv[d] + sdt2 * atl * aa[d];
             }
-            if (s % C.freq == 0)
+            if (s % C.freq == 0 && C.forced_fc)
+            {
+                size_t const update = (size_t(step) * size_t(substeps) + size_t(s)) / size_t(C.freq);
+                std::memcpy(C.fc, C.forced_fc + update * 8 * size_t(nV), sizeof(int32_t) * 8 * size_t(nV));
+            }
+            else if (s % C.freq == 0)
             {
                 for (int32_t q = 0; q < C.nSurfV; ++q)
                 {

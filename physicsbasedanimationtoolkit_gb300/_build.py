@@ -35,7 +35,7 @@ NVCC_FLAGS = ARCH + [
 ]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fvisibility=hidden", f"-I{INCLUDE}", f"-I{CSRC}"]
 
-CUDA_SOURCES = ["vbd_kernels.cu", "vbd_capi.cu", "adjoint.cu", "anderson.cu", "nesterov.cu", "trust_region.cu", "lbvh.cu", "lbvh_capi.cu", "contact.cu", "contact_capi.cu"]
+CUDA_SOURCES = ["vbd_kernels.cu", "batched.cu", "vbd_capi.cu", "adjoint.cu", "anderson.cu", "nesterov.cu", "trust_region.cu", "lbvh.cu", "lbvh_capi.cu", "contact.cu", "contact_capi.cu"]
 CXX_SOURCES = ["vbd_construct.cpp"]
 
 

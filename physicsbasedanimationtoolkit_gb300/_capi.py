@@ -120,6 +120,10 @@ _SIGNATURES = [
     ("pbgb_vbd_set_programmatic_launch", C.c_int, [_vp, _i32]),
     ("pbgb_vbd_set_staged_sweep", C.c_int, [_vp, _i32]),
     ("pbgb_vbd_staged_sweep", C.c_int, [_vp, C.POINTER(_i32), C.POINTER(_i32)]),
+    ("pbgb_vbd_set_persistent", C.c_int, [_vp, _i32]),
+    ("pbgb_vbd_persistent", C.c_int, [_vp, C.POINTER(_i32)]),
+    ("pbgb_vbd_set_batch_tile", C.c_int, [_vp, _i32]),
+    ("pbgb_debug_batched_wait", C.c_int, [_vp, C.c_int64, _i32]),
     ("pbgb_vbd_set_scene_bounding_box", C.c_int, [_vp, _vp, _vp]),
     ("pbgb_vbd_sizes", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     ("pbgb_vbd_launches_per_step", C.c_int, [_vp, _i32, _i32, C.POINTER(C.c_int64)]),

@@ -7,6 +7,7 @@
 // from a CUDA graph, tets packed into 64-byte records, the in-place colour sweep (no xb copy-back
 // pass), and several meshes concatenated into one system for the batched form.
 #include "adjoint.cuh"
+#include "batched.cuh"
 #include "anderson.cuh"
 #include "nesterov.cuh"
 #include "trust_region.cuh"
@@ -263,7 +264,11 @@ class VbdSystem
     DeviceArray<int32_t> nbrPtr;
     DeviceArray<uint32_t> nbr;
     DeviceArray<uint2> incPack;
-    DeviceArray<float4> mats;
+    // Per-incidence stiffness of the sweeps (TetStiffness resolved for the incidence's own corner):
+    // incStiff[k] = (b0, b1, b2, kappa_o) and incPack[k].y = sigma.  Host copies of the incidence
+    // words and neighbour slots let pbgb_vbd_set_material rebuild them.
+    DeviceArray<float4> incStiff;
+    std::vector<uint32_t> hostInc, hostSlots;
     DeviceArray<double> red, gradBuf, objPartials;
 
     // Sweep timing: with `profiling` on, the captured step records an event pair around the colour
@@ -308,6 +313,36 @@ class VbdSystem
     // do not depend on the caller's pointers.
     DeviceArray<float> adjX, adjV;
     DeviceArray<double> adjMu, adjLa;
+
+    // Batch layout: mesh b's vertices are [meshV0[b], meshV0[b+1]); its free vertices of colour c
+    // are solve entries [meshSolve[b][2c], meshSolve[b][2c+1]) (inside colour c of the system,
+    // meshes in order).
+    int32_t nMeshes = 1;
+    std::vector<int32_t> meshV0;
+    // Positions of a batch are stored relative to their mesh's origin (the centre of its rest box,
+    // rounded to FP32), so that FP32 differences of nearby positions keep their precision however
+    // far from the world origin a mesh lies; the position entry points add and subtract it.
+    // Single meshes (and contact, which needs world coordinates for its boxes and Morton codes)
+    // use the world frame: origin is empty then.
+    std::vector<float4> meshOrigin;
+    DeviceArray<float4> origin;
+    std::vector<std::vector<int32_t>> meshSolve;
+    // Persistent batched step (batched.cuh): on for batches by default.  The work items are
+    // rebuilt when the step shape or the launch changes.
+    bool persistent = true;
+    struct PersistentPlan
+    {
+        int32_t iters = -1, sub = -1, lanes = 0, block = 0, tile = 0;
+        float dt      = 0.f;
+        int32_t nItems = 0, grid = 0;
+        size_t smem = 0;
+    } plan;
+    int32_t batchTile = 1; // sub-tiles of blockDim / lanes vertices per sweep item
+    long long batchWaitNs = kBatchWaitNs;
+    int32_t batchPoison   = -1;
+    DeviceArray<BatchItemWords> batchItems;
+    DeviceArray<int32_t> batchCounters; // [0] ticket, [1] abort, then one completion counter per mesh
+    DeviceArray<float> batchOmega;
 
     // Graph cache for Step(dt, iterations, substeps)
     cudaGraphExec_t graph = nullptr;
@@ -423,7 +458,6 @@ class VbdSystem
         w.nbrPtr  = nbrPtr.get();
         w.nbr     = nbr.get();
         w.incPack = incPack.get();
-        w.mats    = mats.get();
     }
     size_t stagedBytes(int32_t c, int L) const
     {
@@ -504,14 +538,31 @@ class VbdSystem
                 vb += d.n_vertices;
             }
         }
+        meshOrigin.assign(size_t(nMeshes), make_float4(0.f, 0.f, 0.f, 0.f));
+        if (nMeshes > 1)
+            for (int32_t b = 0; b < nMeshes; ++b)
+            {
+                auto const& d = descs[b];
+                double const* R = d.X ? d.X : d.x;
+                double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+                for (int32_t i = 0; i < d.n_vertices; ++i)
+                    for (int k = 0; k < 3; ++k)
+                    {
+                        lo[k] = std::min(lo[k], R[3 * size_t(i) + k]);
+                        hi[k] = std::max(hi[k], R[3 * size_t(i) + k]);
+                    }
+                meshOrigin[b] = make_float4(float(0.5 * (lo[0] + hi[0])), float(0.5 * (lo[1] + hi[1])),
+                                            float(0.5 * (lo[2] + hi[2])), 0.f);
+            }
         int32_t v0 = 0, t0 = 0;
         for (int32_t b = 0; b < nMeshes; ++b)
         {
             auto const& d = descs[b];
+            double const o[3] = {meshOrigin[b].x, meshOrigin[b].y, meshOrigin[b].z};
             for (int32_t i = 0; i < d.n_vertices; ++i)
             {
                 double const* p = d.x + 3 * size_t(i);
-                hx[v0 + i]      = make_float4(float(p[0]), float(p[1]), float(p[2]), 0.f);
+                hx[v0 + i]      = make_float4(float(p[0] - o[0]), float(p[1] - o[1]), float(p[2] - o[2]), 0.f);
                 if (d.v)
                 {
                     double const* q = d.v + 3 * size_t(i);
@@ -529,7 +580,7 @@ class VbdSystem
                 hm[v0 + i]    = float(d.m[i]);
                 hostM[v0 + i] = d.m[i];
                 double const* R = (d.X ? d.X : d.x) + 3 * size_t(i);
-                hX[v0 + i]      = make_float4(float(R[0]), float(R[1]), float(R[2]), 0.f);
+                hX[v0 + i]      = make_float4(float(R[0] - o[0]), float(R[1] - o[1]), float(R[2] - o[2]), 0.f);
             }
             for (int32_t e = 0; e < d.n_tets; ++e)
             {
@@ -598,24 +649,31 @@ class VbdSystem
         }
         // Colour-major solve list: colour c = union of every mesh's partition c; inside a colour,
         // stable order by decreasing degree so that lanes of a warp see similar trip counts.
+        // Inside a colour the meshes follow one another, each mesh's entries in stable order of
+        // decreasing degree, so that a (mesh, colour) pair is one range of the list.
         std::vector<int32_t> hsolve;
         hsolve.reserve(nFree);
         colorPtr.assign(size_t(nColors) + 1, 0);
+        this->nMeshes = nMeshes;
+        meshV0.assign(size_t(nMeshes) + 1, 0);
+        for (int32_t b = 0; b < nMeshes; ++b)
+            meshV0[b + 1] = meshV0[b] + descs[b].n_vertices;
+        meshSolve.assign(size_t(nMeshes), std::vector<int32_t>(2 * size_t(nColors), 0));
         for (int32_t c = 0; c < nColors; ++c)
         {
-            size_t const start = hsolve.size();
-            v0                 = 0;
             for (int32_t b = 0; b < nMeshes; ++b)
             {
-                auto const& d = descs[b];
+                auto const& d      = descs[b];
+                size_t const start = hsolve.size();
+                meshSolve[b][2 * c] = int32_t(start);
                 if (c < d.n_partitions)
                     for (int32_t k = d.Pptr[c]; k < d.Pptr[c + 1]; ++k)
-                        hsolve.push_back(d.Padj[k] + v0);
-                v0 += d.n_vertices;
+                        hsolve.push_back(d.Padj[k] + meshV0[b]);
+                std::stable_sort(hsolve.begin() + start, hsolve.end(), [&](int32_t a, int32_t q) {
+                    return deg[a] > deg[q];
+                });
+                meshSolve[b][2 * c + 1] = int32_t(hsolve.size());
             }
-            std::stable_sort(hsolve.begin() + start, hsolve.end(), [&](int32_t a, int32_t b) {
-                return deg[a] > deg[b];
-            });
             colorPtr[c + 1] = int32_t(hsolve.size());
         }
         std::vector<int32_t> hIncPtr(size_t(nFree) + 1, 0);
@@ -634,12 +692,12 @@ class VbdSystem
         // Neighbour lists of the staged sweep, in first-use order over the vertex's incidences and
         // corners ((local + 1 + m) & 3, the order the sweep visits them).
         std::vector<uint32_t> hNbr;
-        std::vector<uint2> hPack(hInc.size());
+        hostSlots.assign(hInc.size(), 0u);
         hostNbrPtr.assign(size_t(nFree) + 1, 0);
         stagedOk = true;
         {
             std::vector<uint32_t> list;
-            for (int32_t s = 0; s < nFree && stagedOk; ++s)
+            for (int32_t s = 0; s < nFree; ++s)
             {
                 list.clear();
                 for (int32_t k = hIncPtr[s]; k < hIncPtr[s + 1]; ++k)
@@ -661,17 +719,21 @@ class VbdSystem
                             list.push_back(a);
                         slots |= uint32_t(idx) << (8 * m);
                     }
-                    hPack[k] = make_uint2(q >> 2, slots);
+                    hostSlots[k] = slots; // meaningful only while the list has at most 256 entries
                 }
                 if (list.size() > 256)
                     stagedOk = false;
-                hNbr.insert(hNbr.end(), list.begin(), list.end());
-                hostNbrPtr[s + 1] = int32_t(hNbr.size());
+                if (stagedOk)
+                {
+                    hNbr.insert(hNbr.end(), list.begin(), list.end());
+                    hostNbrPtr[s + 1] = int32_t(hNbr.size());
+                }
             }
         }
-        std::vector<float4> hMats(hrec.size());
-        for (size_t e = 0; e < hrec.size(); ++e)
-            hMats[e] = hrec[e].mat;
+        hostInc = hInc;
+        std::vector<float4> hStiff;
+        std::vector<uint2> hPack;
+        incidenceRecords(hStiff, hPack);
 
         // Device allocation and upload.
         check(cudaGetDevice(&device), "cudaGetDevice");
@@ -730,20 +792,31 @@ class VbdSystem
         m.upload(hm.data(), nV, stream);
         tets.upload(hrec.data(), nT, stream);
         X.upload(hX.data(), nV, stream);
+        std::vector<float4> hOrigin;
+        if (nMeshes > 1)
+        {
+            hOrigin.resize(size_t(nV));
+            for (int32_t b = 0; b < nMeshes; ++b)
+                std::fill(hOrigin.begin() + meshV0[b], hOrigin.begin() + meshV0[b + 1], meshOrigin[b]);
+            origin.allocate(size_t(nV));
+            origin.upload(hOrigin.data(), size_t(nV), stream);
+        }
         solve.upload(hsolve.data(), nFree, stream);
+        incStiff.allocate(hStiff.size());
+        incStiff.upload(hStiff.data(), hStiff.size(), stream);
+        incPack.allocate(hPack.size());
+        incPack.upload(hPack.data(), hPack.size(), stream);
         incPtr.upload(hIncPtr.data(), hIncPtr.size(), stream);
         inc.upload(hInc.data(), hInc.size(), stream);
         if (stagedOk)
         {
             nbrPtr.allocate(hostNbrPtr.size());
             nbr.allocate(hNbr.size());
-            incPack.allocate(hPack.size());
-            mats.allocate(hMats.size());
             nbrPtr.upload(hostNbrPtr.data(), hostNbrPtr.size(), stream);
             nbr.upload(hNbr.data(), hNbr.size(), stream);
-            incPack.upload(hPack.data(), hPack.size(), stream);
-            mats.upload(hMats.data(), hMats.size(), stream);
             check(prepare_staged_sweeps(), "cudaFuncSetAttribute");
+            if (nMeshes > 1)
+                check(prepare_batched_step(), "cudaFuncSetAttribute");
         }
         else
             hostNbrPtr.clear();
@@ -864,6 +937,35 @@ class VbdSystem
         hostRecords = std::move(hrec);
     }
 
+    // Per-incidence stiffness of all solved incidences (solve order) from the host copies of the
+    // shape-function gradients, quadrature weights and Lame coefficients: stiff[k] = (b0, b1, b2,
+    // kappa_o) of incidence k's own corner o, pack[k] = (neighbour slots, sigma as bits).
+    void incidenceRecords(std::vector<float4>& stiffOut, std::vector<uint2>& packOut) const
+    {
+        std::vector<double> words(8 * size_t(nT));
+        for (int32_t e = 0; e < nT; ++e)
+        {
+            double w[8];
+            tet_stiffness_words(hostGP.data() + 12 * size_t(e), hostWg[e], hostMu[e], hostLambda[e], w);
+            std::copy(w, w + 8, words.begin() + 8 * size_t(e));
+        }
+        stiffOut.resize(hostInc.size());
+        packOut.resize(hostInc.size());
+        for (size_t k = 0; k < hostInc.size(); ++k)
+        {
+            uint32_t const q   = hostInc[k];
+            double const* w    = words.data() + 8 * size_t(q >> 2);
+            double const bw[6] = {w[0], w[1], w[2], w[3], w[4], w[5]};
+            double b0, b1, b2, kappa;
+            corner_stiffness(bw, w[7], int(q & 3u), b0, b1, b2, kappa);
+            stiffOut[k]        = make_float4(float(b0), float(b1), float(b2), float(kappa));
+            float const sigma  = float(w[6]);
+            uint32_t sbits     = 0;
+            std::memcpy(&sbits, &sigma, sizeof(sbits));
+            packOut[k] = make_uint2(hostSlots[k], sbits);
+        }
+    }
+
     // Per-tet Lame coefficients (system order); the records keep (wg mu, wg lambda, 1 + mu/lambda).
     void setMaterial(double const* mu, double const* lambda)
     {
@@ -879,13 +981,11 @@ class VbdSystem
             hostLambda[e]      = lambda[e];
         }
         tets.upload(hostRecords.data(), size_t(nT), stream);
-        std::vector<float4> hMats(static_cast<size_t>(nT));
-        if (stagedOk)
-        {
-            for (int32_t e = 0; e < nT; ++e)
-                hMats[e] = hostRecords[e].mat;
-            mats.upload(hMats.data(), size_t(nT), stream);
-        }
+        std::vector<float4> hStiff;
+        std::vector<uint2> hPack;
+        incidenceRecords(hStiff, hPack);
+        incStiff.upload(hStiff.data(), hStiff.size(), stream);
+        incPack.upload(hPack.data(), hPack.size(), stream);
         // The uploads read the host arrays asynchronously.
         check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
     }
@@ -974,7 +1074,8 @@ class VbdSystem
         w.xt       = xt.get();
         w.xtilde   = xtilde.get();
         w.tets     = tets.get();
-        w.X        = X.get();
+        w.stiff    = incStiff.get();
+        w.incPack  = incPack.get();
         w.solve    = solve.get();
         w.incPtr   = incPtr.get();
         w.inc      = inc.get();
@@ -1112,6 +1213,134 @@ class VbdSystem
         return p;
     }
 
+    // Whether step() runs the persistent batched kernel (batched.cuh): batches without contact,
+    // plain or Chebyshev, every colour staged, and no per-launch sweep timing.
+    bool persistentActive() const
+    {
+        return nMeshes > 1 && persistent && !contact &&
+               (acceleration == PBGB_ACCEL_NONE || acceleration == PBGB_ACCEL_CHEBYSHEV) && stagedOk && staged &&
+               !profiling;
+    }
+
+    // Work items of the persistent step for (iterations, substeps) and the current launch shape,
+    // in stage-time order (substep, then begin / iteration and colour / end), meshes in order inside
+    // a stage, tiles in order inside a mesh; each item records how many of its mesh's items must be
+    // complete first.  Built and uploaded outside any stream capture.  Returns false when the batch
+    // cannot run persistently with this launch (the colour-launch path is used then).
+    bool preparePersistent(int32_t iterations, int32_t substeps)
+    {
+        int const L = lanesToUse();
+        int const B = std::min(block, 256);
+        if (plan.iters == iterations && plan.sub == substeps && plan.lanes == L && plan.block == B &&
+            plan.tile == batchTile)
+            return plan.grid > 0;
+        plan       = PersistentPlan{};
+        plan.iters = iterations;
+        plan.sub   = substeps;
+        plan.lanes = L;
+        plan.block = B;
+        plan.tile  = batchTile;
+        int const per = B / L;
+        if (per < 1 || B % 32 != 0)
+            return false;
+        int const tileE = per * batchTile, tileV = 4 * B;
+        std::vector<BatchItemWords> items;
+        std::vector<int32_t> count(size_t(nMeshes), 0);
+        size_t smem = 0;
+        auto emit = [&](int32_t b, int kind, int32_t k, int32_t lo, int32_t hi, int32_t step) {
+            int32_t const need = count[b];
+            for (int32_t f = lo; f < hi; f += step)
+            {
+                int32_t const e = std::min(f + step, hi);
+                items.push_back(BatchItemWords{make_int4(b, kind | (k << 2), f, e), make_int4(need, 0, 0, 0)});
+                ++count[b];
+                if (kind == kBatchSweep)
+                    for (int32_t g = f; g < e; g += per)
+                        smem = std::max(smem, size_t(hostNbrPtr[std::min(g + per, e)] - hostNbrPtr[g]) * kStagedSlotBytes);
+            }
+        };
+        for (int32_t s = 0; s < substeps; ++s)
+        {
+            for (int32_t b = 0; b < nMeshes; ++b)
+                emit(b, kBatchBegin, 0, meshV0[b], meshV0[b + 1], tileV);
+            for (int32_t k = 0; k < iterations; ++k)
+                for (int32_t c = 0; c < nColors; ++c)
+                    for (int32_t b = 0; b < nMeshes; ++b)
+                        emit(b, kBatchSweep, k, meshSolve[b][2 * c], meshSolve[b][2 * c + 1], tileE);
+            for (int32_t b = 0; b < nMeshes; ++b)
+                emit(b, kBatchEnd, 0, meshV0[b], meshV0[b + 1], tileV);
+        }
+        if (items.size() > size_t(INT32_MAX) || smem > kStagedMaxBytes)
+            return false;
+        bool const cheb = acceleration == PBGB_ACCEL_CHEBYSHEV;
+        int const perSM = batched_step_blocks_per_sm(L, B, smem, cheb);
+        if (perSM < 1)
+            return false;
+        int sms = 0;
+        check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
+        check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+        batchItems.allocate(std::max<size_t>(items.size(), 1));
+        if (!items.empty())
+            check(cudaMemcpy(batchItems.get(), items.data(), sizeof(BatchItemWords) * items.size(), cudaMemcpyHostToDevice),
+                  "H2D");
+        batchCounters.allocate(2 + size_t(nMeshes));
+        std::vector<float> om(size_t(std::max(iterations, 1)), 1.f);
+        double omega = 0.0;
+        for (int32_t k = 0; k < iterations; ++k)
+        {
+            omega          = chebyshev_omega<double>(k, rho * rho, omega, chebFormula);
+            om[size_t(k)] = float(omega);
+        }
+        batchOmega.allocate(om.size());
+        check(cudaMemcpy(batchOmega.get(), om.data(), sizeof(float) * om.size(), cudaMemcpyHostToDevice), "H2D");
+        plan.nItems = int32_t(items.size());
+        plan.smem   = smem;
+        plan.grid   = int32_t(std::min<int64_t>(int64_t(perSM) * sms, std::max<int64_t>(plan.nItems, 1)));
+        return true;
+    }
+
+    // One persistent launch for the whole step (after the counters are cleared).
+    void enqueuePersistentStep(float dt, int32_t iterations, int32_t substeps)
+    {
+        float const h    = dt / float(substeps);
+        bool const cheb  = acceleration == PBGB_ACCEL_CHEBYSHEV;
+        SubstepParams sp = substepParams(h);
+        if (!cheb)
+            sp.h0 = sp.h1 = nullptr;
+        else if (iterations > 0)
+            sp.result = ((iterations - 1) % 2 == 0) ? h0.get() : h1.get();
+        BatchedStepParams bp{};
+        SweepParams& w = bp.sweep;
+        w.x        = x.get();
+        w.xt       = xt.get();
+        w.xtilde   = xtilde.get();
+        w.stiff    = incStiff.get();
+        w.incPack  = incPack.get();
+        w.tets     = tets.get();
+        w.solve    = solve.get();
+        w.incPtr   = incPtr.get();
+        w.inc      = inc.get();
+        stagedFields(w);
+        w.h        = h;
+        w.h2       = h * h;
+        w.kD       = kD;
+        w.detHZero = detHZero;
+        w.omega    = 1.f;
+        bp.sub     = sp;
+        bp.H0      = cheb ? h0.get() : nullptr;
+        bp.H1      = cheb ? h1.get() : nullptr;
+        bp.omega   = batchOmega.get();
+        bp.items   = batchItems.get();
+        bp.nItems  = plan.nItems;
+        bp.control = batchCounters.get();
+        bp.done    = batchCounters.get() + 2;
+        bp.flags   = flags.get();
+        bp.waitNs  = batchWaitNs;
+        bp.poison  = batchPoison;
+        check(cudaMemsetAsync(batchCounters.get(), 0, sizeof(int32_t) * (2 + size_t(nMeshes)), stream), "memset");
+        check(launch_batched_step(bp, plan.lanes, plan.block, plan.grid, plan.smem, cheb, stream), "batched_step");
+    }
+
     // Enqueue one full step on `stream` (captured into a graph by step()).  Order of the
     // reference GPU integrator (gpu/impl/vbd/Integrator.cu:82-103): contact active set initialised
     // on the full-step prediction, per substep inertial target + initial guess, contact list update,
@@ -1130,6 +1359,12 @@ class VbdSystem
 
     void enqueueStep(float dt, int32_t iterations, int32_t substeps, StepHooks const* hooks = nullptr)
     {
+        if (!hooks && persistentActive() && plan.iters == iterations && plan.sub == substeps && plan.grid > 0 &&
+            plan.lanes == lanesToUse() && plan.block == std::min(block, 256) && plan.tile == batchTile)
+        {
+            enqueuePersistentStep(dt, iterations, substeps);
+            return;
+        }
         float const h    = dt / float(substeps);
         float const h2   = h * h;
         bool const plainOnly = hooks && hooks->plain;
@@ -1147,7 +1382,8 @@ class VbdSystem
         w.xt       = xt.get();
         w.xtilde   = xtilde.get();
         w.tets     = tets.get();
-        w.X        = X.get();
+        w.stiff    = incStiff.get();
+        w.incPack  = incPack.get();
         w.solve    = solve.get();
         w.incPtr   = incPtr.get();
         w.inc      = inc.get();
@@ -1441,6 +1677,21 @@ class VbdSystem
         check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
     }
 
+    // deviceToHost of a position array, in world coordinates (mesh origins added).
+    std::vector<float4> positionsToHost(float4 const* src)
+    {
+        std::vector<float4> out = deviceToHost(src);
+        if (nMeshes > 1)
+            for (int32_t b = 0; b < nMeshes; ++b)
+                for (int32_t i = meshV0[b]; i < meshV0[b + 1]; ++i)
+                {
+                    out[size_t(i)].x += meshOrigin[b].x;
+                    out[size_t(i)].y += meshOrigin[b].y;
+                    out[size_t(i)].z += meshOrigin[b].z;
+                }
+        return out;
+    }
+
     std::vector<float4> deviceToHost(float4 const* src)
     {
         std::vector<float4> out(static_cast<size_t>(nV));
@@ -1478,12 +1729,12 @@ class VbdSystem
         StepHooks hooks;
         hooks.plain        = true;
         hooks.substepBegin = [&](int32_t s) {
-            std::vector<float4> const xt4 = deviceToHost(xtilde.get());
+            std::vector<float4> const xt4 = positionsToHost(xtilde.get());
             writeMarket(at("xtilde.t." + std::to_string(t) + ".s." + std::to_string(s) + ".mtx"), nV, 3, false,
                         [&](int64_t i, int64_t c) { return (&xt4[size_t(i)].x)[c]; });
         };
         hooks.iterate = [&](int32_t s, int32_t k, float4 const* current) {
-            std::vector<float4> const x4 = deviceToHost(current);
+            std::vector<float4> const x4 = positionsToHost(current);
             writeMarket(at("x.t." + std::to_string(t) + ".s." + std::to_string(s) + ".k." + std::to_string(k) + ".mtx"),
                         nV, 3, false, [&](int64_t i, int64_t c) { return (&x4[size_t(i)].x)[c]; });
         };
@@ -1512,7 +1763,7 @@ class VbdSystem
             check(cudaMemcpyAsync(&f, red.get(), sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H");
             if (nV > 0)
                 check(cudaMemcpyAsync(g.data(), gradBuf.get(), sizeof(double) * g.size(), cudaMemcpyDeviceToHost, stream), "D2H");
-            std::vector<float4> const x4 = deviceToHost(current);
+            std::vector<float4> const x4 = positionsToHost(current);
             fs.push_back(f);
             gs.insert(gs.end(), g.begin(), g.end());
             for (auto const& q : x4)
@@ -1544,6 +1795,8 @@ class VbdSystem
 
     int64_t launchesPerStep(int32_t iterations, int32_t substeps) const
     {
+        if (persistentActive() && plan.iters == iterations && plan.sub == substeps && plan.grid > 0)
+            return plan.nItems > 0 ? 1 : 0;
         int64_t perIter = 0;
         for (int32_t c = 0; c < nColors; ++c)
             perIter += colorPtr[c + 1] > colorPtr[c] ? 1 : 0;
@@ -1584,6 +1837,15 @@ class VbdSystem
     void step(float dt, int32_t iterations, int32_t substeps)
     {
         reserveTrustLog(iterations, substeps);
+        if (persistentActive())
+        {
+            int32_t const before = plan.nItems, beforeGrid = plan.grid;
+            bool const same = plan.iters == iterations && plan.sub == substeps && plan.lanes == lanesToUse() &&
+                              plan.block == std::min(block, 256) && plan.tile == batchTile;
+            preparePersistent(iterations, substeps);
+            if (!same || before != plan.nItems || beforeGrid != plan.grid)
+                graphValid = false;
+        }
         if (traceNext)
         {
             traceNext = false;
@@ -1631,10 +1893,11 @@ class VbdSystem
         int64_t nV, nT, nC, iters, sub;
         int32_t accel;
         bool contact;
+        bool persistent;
         bool operator==(TuneKey const& o) const
         {
             return nV == o.nV && nT == o.nT && nC == o.nC && iters == o.iters && sub == o.sub && accel == o.accel &&
-                   contact == o.contact;
+                   contact == o.contact && persistent == o.persistent;
         }
     };
     struct TuneEntry
@@ -1659,7 +1922,7 @@ class VbdSystem
                 b <<= 1;
             return b;
         };
-        TuneKey const key{bucket(nV), bucket(nT), nColors, iterations, substeps, acceleration, contact};
+        TuneKey const key{bucket(nV), bucket(nT), nColors, iterations, substeps, acceleration, contact, persistentActive()};
         {
             std::lock_guard<std::mutex> lock(cacheMutex);
             for (auto const& e : tuneCache())
@@ -1769,9 +2032,15 @@ class VbdSystem
     int synchronize()
     {
         check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
-        int32_t f = 0;
-        check(cudaMemcpy(&f, flags.get(), sizeof(int32_t), cudaMemcpyDeviceToHost), "cudaMemcpy");
-        if (f != 0)
+        int32_t f[2] = {0, 0};
+        check(cudaMemcpy(f, flags.get(), sizeof(f), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        if (f[1] != 0)
+        {
+            check(cudaMemset(flags.get(), 0, sizeof(f)), "cudaMemset");
+            lastError = "a bounded device wait of the persistent batched step gave up; the step's positions are not valid";
+            return kTimeout;
+        }
+        if (f[0] != 0)
         {
             check(cudaMemset(flags.get(), 0, sizeof(int32_t)), "cudaMemset");
             lastError = "non-finite positions or velocities detected on the device";
@@ -1780,15 +2049,16 @@ class VbdSystem
         return kOk;
     }
 
-    void getVec(DeviceArray<float4> const& src, float* host)
+    // Host transfers of a per-vertex vector; positions = true adds / subtracts the mesh origins.
+    void getVec(DeviceArray<float4> const& src, float* host, bool positions = false)
     {
-        check(launch_unpack3(src.get(), staging.get(), nV, stream), "unpack");
+        check(launch_unpack3(src.get(), staging.get(), nV, stream, positions ? origin.get() : nullptr), "unpack");
         check(cudaMemcpyAsync(host, staging.get(), sizeof(float) * 3 * size_t(nV), cudaMemcpyDeviceToHost, stream), "D2H");
     }
-    void setVec(DeviceArray<float4>& dst, float const* host)
+    void setVec(DeviceArray<float4>& dst, float const* host, bool positions = false)
     {
         check(cudaMemcpyAsync(staging.get(), host, sizeof(float) * 3 * size_t(nV), cudaMemcpyHostToDevice, stream), "H2D");
-        check(launch_pack3(staging.get(), dst.get(), nV, stream), "pack");
+        check(launch_pack3(staging.get(), dst.get(), nV, stream, positions ? origin.get() : nullptr), "pack");
     }
 
     EnergyParams energyParams(double dt, double* out, float4 const* at = nullptr) const
@@ -2052,7 +2322,7 @@ PBGB_API int pbgb_vbd_get_positions(pbgb_vbd* h, float* x)
 {
     PBGB_CHECK_HANDLE_PTR(h, x)
     return guarded(h, [&] {
-        h->sys.getVec(h->sys.x, x);
+        h->sys.getVec(h->sys.x, x, true);
         return h->sys.synchronize();
     });
 }
@@ -2061,7 +2331,7 @@ PBGB_API int pbgb_vbd_set_positions(pbgb_vbd* h, const float* x)
 {
     PBGB_CHECK_HANDLE_PTR(h, x)
     return guarded(h, [&] {
-        h->sys.setVec(h->sys.x, x);
+        h->sys.setVec(h->sys.x, x, true);
         return int(kOk);
     });
 }
@@ -2097,7 +2367,7 @@ PBGB_API int pbgb_vbd_get_positions_device(pbgb_vbd* h, float* x_dev)
 {
     PBGB_CHECK_HANDLE_PTR(h, x_dev)
     return guarded(h, [&] {
-        pbgb::check(pbgb::launch_unpack3(h->sys.x.get(), x_dev, h->sys.nV, h->sys.stream), "unpack");
+        pbgb::check(pbgb::launch_unpack3(h->sys.x.get(), x_dev, h->sys.nV, h->sys.stream, h->sys.origin.get()), "unpack");
         return int(kOk);
     });
 }
@@ -2106,7 +2376,7 @@ PBGB_API int pbgb_vbd_set_positions_device(pbgb_vbd* h, const float* x_dev)
 {
     PBGB_CHECK_HANDLE_PTR(h, x_dev)
     return guarded(h, [&] {
-        pbgb::check(pbgb::launch_pack3(x_dev, h->sys.x.get(), h->sys.nV, h->sys.stream), "pack");
+        pbgb::check(pbgb::launch_pack3(x_dev, h->sys.x.get(), h->sys.nV, h->sys.stream, h->sys.origin.get()), "pack");
         return int(kOk);
     });
 }
@@ -2313,6 +2583,46 @@ PBGB_API int pbgb_vbd_set_programmatic_launch(pbgb_vbd* h, int32_t enable)
     if (!h)
         return fail(nullptr, kInvalid, "null handle");
     h->sys.pdl = enable != 0;
+    h->sys.invalidate();
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_set_persistent(pbgb_vbd* h, int32_t enable)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    h->sys.persistent = enable != 0;
+    h->sys.invalidate();
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_persistent(pbgb_vbd* h, int32_t* active)
+{
+    if (!h || !active)
+        return fail(h, kInvalid, "null argument");
+    *active = h->sys.persistentActive() ? 1 : 0;
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_set_batch_tile(pbgb_vbd* h, int32_t subtiles)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (subtiles < 1 || subtiles > 64)
+        return fail(h, kInvalid, "pbgb_vbd_set_batch_tile: expected 1 <= subtiles <= 64");
+    h->sys.batchTile = subtiles;
+    h->sys.invalidate();
+    return kOk;
+}
+
+PBGB_API int pbgb_debug_batched_wait(pbgb_vbd* h, int64_t wait_ns, int32_t poison_item)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (wait_ns < 1000 || wait_ns > pbgb::kBatchWaitNs || poison_item < -1)
+        return fail(h, kInvalid, "pbgb_debug_batched_wait: expected 1 us <= wait_ns <= 2 s and poison_item >= -1");
+    h->sys.batchWaitNs = wait_ns;
+    h->sys.batchPoison = poison_item;
     h->sys.invalidate();
     return kOk;
 }
@@ -2663,18 +2973,20 @@ PBGB_API int pbgb_debug_vertex_block(
         double const* G4 = GPs + 12 * size_t(q);
         if (il[q] < 0 || il[q] > 3)
             return fail(nullptr, kInvalid, "local index out of range");
-        // Same own-corner-relative form as the device sweep.
-        double d[3][3], G[3][3];
+        // Same own-corner-relative form and per-tet record as the device sweep (in FP64).
+        double d[3][3];
         for (int m = 0; m < 3; ++m)
         {
             int const a = (il[q] + 1 + m) & 3;
             for (int r = 0; r < 3; ++r)
-            {
                 d[m][r] = xq[3 * a + r] - xq[3 * il[q] + r];
-                G[m][r] = G4[3 * a + r];
-            }
         }
-        pbgb::accumulate_tet(b, d, G, wg[q] * mu[q], wg[q] * lambda[q], 1.0 + mu[q] / lambda[q]);
+        double w[8];
+        pbgb::tet_stiffness_words(G4, wg[q], mu[q], lambda[q], w);
+        double const bw[6] = {w[0], w[1], w[2], w[3], w[4], w[5]};
+        double b0, b1, b2, kappa;
+        pbgb::corner_stiffness(bw, w[7], il[q], b0, b1, b2, kappa);
+        pbgb::accumulate_incidence(b, d, b0, b1, b2, w[6], kappa);
     }
     pbgb::newton_update(b, xt, xtilde, m, h, h2, kD, detHZero, x, g, H);
     return kOk;

@@ -1,165 +1,22 @@
 // CUDA kernels of the VBD step (sm_103a).  See vbd_kernels.cuh for the data layout.
 #include "vbd_kernels.cuh"
 #include "energy.cuh"
+#include "sweep_device.cuh"
 
 #include <algorithm>
 #include <cfloat>
 
 namespace pbgb {
 
-int constexpr kMaxContactsPerVertex = 8;
-
 namespace {
-
-__device__ __forceinline__ void load3(float4 const v, float* o)
-{
-    o[0] = v.x;
-    o[1] = v.y;
-    o[2] = v.z;
-}
-
-__device__ __forceinline__ uint32_t corner(uint4 const& t, int a)
-{
-    return a == 0 ? t.x : (a == 1 ? t.y : (a == 2 ? t.z : t.w));
-}
-
-// Contact terms of one vertex-triangle pair (gpu/impl/vbd/Kernels.cuh:80-114,203-223): the
-// triangle's corners at t and now (from x when their colour is solved before this one, else from
-// hprev: bit 31 of the record), then the normal penalty and friction of vertex_triangle_contact
-// with the record's penalty.
-__device__ __forceinline__ void contact_pair(SweepParams const& p, int4 r, float kCf, float const* xt, float const* xi, float* H, float* g)
-{
-    uint32_t const v[3] = {uint32_t(r.x), uint32_t(r.y), uint32_t(r.z)};
-    float xtf[3][3], xf[3][3];
-    for (int k = 0; k < 3; ++k)
-    {
-        uint32_t const j = v[k] & 0x7FFFFFFFu;
-        float4 const a   = p.xt[j];
-        float4 const b   = __ldcg(((v[k] >> 31) ? p.x : p.hprev) + j);
-        xtf[k][0] = a.x, xtf[k][1] = a.y, xtf[k][2] = a.z;
-        xf[k][0] = b.x, xf[k][1] = b.y, xf[k][2] = b.z;
-    }
-    vertex_triangle_contact(xt, xi, xtf, xf, p.h, kCf, p.muF, p.epsv, FLT_EPSILON, g, H);
-}
-
-// Contact energy of vertex i, spread over the vertex's L lanes: lane l takes the record slots
-// l, l + L, ... (kMaxContactsPerVertex of them); the lanes' gradients and Hessians are summed with
-// xor shuffles inside the group (every lane of the warp takes part in the shuffles).  cH, cg: the
-// group's sum, in every lane.
-template <int L>
-__device__ __forceinline__ void contact_terms(SweepParams const& p, bool valid, int lane, int i, float const* xt, float const* xi, float* cH, float* cg)
-{
-#pragma unroll
-    for (int r = 0; r < 6; ++r)
-        cH[r] = 0.f;
-    cg[0] = cg[1] = cg[2] = 0.f;
-#pragma unroll
-    for (int c = 0; c < (kMaxContactsPerVertex + L - 1) / L; ++c)
-    {
-        int const k = lane + c * L;
-        if (valid && k < kMaxContactsPerVertex)
-        {
-            int4 const r = p.crec[i * kMaxContactsPerVertex + k];
-            if (r.w >= 0)
-                contact_pair(p, r, p.cpen[i * kMaxContactsPerVertex + k], xt, xi, cH, cg);
-        }
-    }
-#pragma unroll
-    for (int off = L / 2; off > 0; off >>= 1)
-    {
-#pragma unroll
-        for (int r = 0; r < 6; ++r)
-            cH[r] += __shfl_xor_sync(0xffffffffu, cH[r], off);
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-            cg[r] += __shfl_xor_sync(0xffffffffu, cg[r], off);
-    }
-}
-
-// The end of a vertex solve, shared by both sweep kernels: xor-shuffle reduction of the lanes'
-// 10 accumulated floats, then lane 0 applies damping, contact, inertia and the 3x3 Newton step and
-// writes the iterate(s).
-template <int L, bool CHEB, bool REC, bool CONTACT>
-__device__ __forceinline__ void finish_vertex(SweepParams const& p, VertexBlock<float>& b, bool valid, int lane, int i, int s, float* xi)
-{
-#pragma unroll
-    for (int off = L / 2; off > 0; off >>= 1)
-    {
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-            b.g[r] += __shfl_xor_sync(0xffffffffu, b.g[r], off);
-        b.s += __shfl_xor_sync(0xffffffffu, b.s, off);
-#pragma unroll
-        for (int r = 0; r < 6; ++r)
-            b.C[r] += __shfl_xor_sync(0xffffffffu, b.C[r], off);
-    }
-    float4 const xt4  = p.xt[i];
-    float const xt[3] = {xt4.x, xt4.y, xt4.z};
-    float cH[6], cg[3];
-    bool constexpr contact = CHEB && CONTACT;
-    if constexpr (contact)
-        contact_terms<L>(p, valid, lane, i, xt, xi, cH, cg);
-    if (!valid || lane != 0)
-        return;
-    float4 const xl4  = p.xtilde[i];
-    float const xl[3] = {xl4.x, xl4.y, xl4.z};
-    float H[6], g[3];
-    elastic_system(b, xt, xi, p.h, p.kD, H, g);
-    if constexpr (contact)
-    {
-#pragma unroll
-        for (int r = 0; r < 6; ++r)
-            H[r] += cH[r];
-        g[0] += cg[0];
-        g[1] += cg[1];
-        g[2] += cg[2];
-    }
-    float dx[3];
-    bool const moved = inertia_solve(H, g, xl, xt4.w, p.h2, p.detHZero, xi, static_cast<float*>(nullptr),
-                                     static_cast<float*>(nullptr), dx);
-    if (p.step)
-        p.step[i] = make_float4(dx[0], dx[1], dx[2], 0.f);
-    if (REC)
-    {
-        // H now includes the inertia term; its inverse by the adjugate, as in inertia_solve.
-        float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
-        if (moved)
-        {
-            float const a00 = H[3] * H[5] - H[4] * H[4];
-            float const a01 = H[2] * H[4] - H[1] * H[5];
-            float const a02 = H[1] * H[4] - H[2] * H[3];
-            float const a11 = H[0] * H[5] - H[2] * H[2];
-            float const a12 = H[1] * H[2] - H[0] * H[4];
-            float const a22 = H[0] * H[3] - H[1] * H[1];
-            float const inv = 1.f / (H[0] * a00 + H[1] * a01 + H[2] * a02);
-            r0 = make_float4(inv * a00, inv * a01, inv * a02, inv * a11);
-            r1 = make_float4(inv * a12, inv * a22, 0.f, 0.f);
-        }
-        p.tape[2 * s]     = r0;
-        p.tape[2 * s + 1] = r1;
-    }
-    if (CHEB)
-    {
-        // Raw iterate k (even when the Newton step was skipped: later colours read it).
-        p.x[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
-        if (p.k > 1)
-        {
-            float4 const km2 = p.hcur[i];
-            xi[0]            = p.omega * (xi[0] - km2.x) + km2.x;
-            xi[1]            = p.omega * (xi[1] - km2.y) + km2.y;
-            xi[2]            = p.omega * (xi[2] - km2.z) + km2.z;
-        }
-        p.hcur[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
-    }
-    else if (moved)
-        p.x[i] = make_float4(xi[0], xi[1], xi[2], 0.f);
-}
 
 // Per-colour Gauss-Seidel sweep (reference: VbdIteration, gpu/impl/vbd/Kernels.cuh:148-233, and
 // Integrator::SolveVertex, sim/vbd/Integrator.cpp:98-136).  L lanes cooperate on one vertex: lane
 // l takes incidences l, l+L, ...; the 10 accumulated floats are then reduced with xor shuffles
 // and lane 0 applies damping, inertia and the 3x3 Newton step, writing x in place.  Vertices of a
-// colour share no tet, so the in-place write races with no reader of this launch.
+// colour share no tet, so the in-place write races with no reader of this launch.  Each incidence
+// reads its 20 bytes of rest-state stiffness (b0, b1, b2, kappa, sigma; TetStiffness resolved for
+// the vertex's corner) and the three other corners' current positions: no rest position is read.
 //
 // CHEB: the Chebyshev update of the reference (applied to all vertices after each full sweep,
 // sim/vbd/ChebyshevIntegrator.cpp:15-32) is fused in.  Only vertex i's own values enter its
@@ -182,27 +39,27 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) sweep_kernel(SweepParams
     zero(b);
     int i       = 0;
     float xi[3] = {0.f, 0.f, 0.f};
-    float Xi[3] = {0.f, 0.f, 0.f};
     int k = 0, k1 = 0;
     uint32_t q0 = 0u, q1 = 0u;
     uint4 t     = make_uint4(0u, 0u, 0u, 0u);
-    float4 mat  = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 st   = make_float4(0.f, 0.f, 0.f, 0.f);
+    float sg    = 0.f;
     // Prologue on data no earlier launch writes (mesh tables): with programmatic dependent launch
     // it overlaps the previous colour's tail.
     if (valid)
     {
         i  = __ldg(p.solve + s);
-        load3(__ldg(p.X + i), Xi);
         k1 = __ldg(p.incPtr + s + 1);
         k  = __ldg(p.incPtr + s) + lane;
-        // Software pipeline: the record of incidence k+L and the incidence word of k+2L are in
+        // Software pipeline: the records of incidence k+L and the incidence word of k+2L are in
         // flight while incidence k's corners are gathered and its block accumulated.
         q0 = k < k1 ? __ldg(p.inc + k) : 0u;
         q1 = k + L < k1 ? __ldg(p.inc + k + L) : 0u;
         if (k < k1)
         {
-            t   = __ldg(&p.tets[q0 >> 2].v);
-            mat = __ldg(&p.tets[q0 >> 2].mat);
+            t  = __ldg(&p.tets[q0 >> 2].v);
+            st = __ldg(p.stiff + k);
+            sg = __uint_as_float(__ldg(&p.incPack[k].y));
         }
     }
     // Positions are written by the previous launches: wait for them (no-op without PDL), then let
@@ -216,15 +73,17 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) sweep_kernel(SweepParams
         {
             int const il = int(q0 & 3u);
             uint4 tn     = make_uint4(0u, 0u, 0u, 0u);
-            float4 matn  = make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 stn   = make_float4(0.f, 0.f, 0.f, 0.f);
+            float sgn    = 0.f;
             if (k + L < k1)
             {
-                tn   = __ldg(&p.tets[q1 >> 2].v);
-                matn = __ldg(&p.tets[q1 >> 2].mat);
+                tn  = __ldg(&p.tets[q1 >> 2].v);
+                stn = __ldg(p.stiff + k + L);
+                sgn = __uint_as_float(__ldg(&p.incPack[k + L].y));
             }
             uint32_t const q2 = k + 2 * L < k1 ? __ldg(p.inc + k + 2 * L) : 0u;
             uint32_t const own = corner(t, il) >> 30;
-            float d[3][3], e[3][3];
+            float d[3][3];
 #pragma unroll
             for (int m = 0; m < 3; ++m)
             {
@@ -234,49 +93,31 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) sweep_kernel(SweepParams
                 if (CHEB && (ta >> 30) > own)
                     src = p.hprev;
                 float4 const xa = __ldg(src + j);
-                float4 const Xa = __ldg(p.X + j);
                 d[m][0] = xa.x - xi[0];
                 d[m][1] = xa.y - xi[1];
                 d[m][2] = xa.z - xi[2];
-                e[m][0] = Xa.x - Xi[0];
-                e[m][1] = Xa.y - Xi[1];
-                e[m][2] = Xa.z - Xi[2];
             }
-            float G[3][3];
-            rest_gradients(e, G);
-            accumulate_tet(b, d, G, mat.x, mat.y, mat.z);
-            q0  = q1;
-            q1  = q2;
-            t   = tn;
-            mat = matn;
+            accumulate_incidence(b, d, st.x, st.y, st.z, sg, st.w);
+            q0 = q1;
+            q1 = q2;
+            t  = tn;
+            st = stn;
+            sg = sgn;
         }
     }
     finish_vertex<L, CHEB, REC, CONTACT>(p, b, valid, lane, i, s, xi);
 }
 
 // The same sweep with each vertex's neighbours staged in shared memory.  A vertex's ~23 incident
-// tets reference only ~14 distinct neighbours, so instead of gathering three corners' current
-// and rest positions per incidence, the vertex's lanes load each neighbour once into its slice of
-// the block's slab (rest positions before griddepcontrol.wait: no launch writes them; current
-// positions after it), and the incidence loop reads them back through the three slot bytes of its
-// packed incidence word.  The slab slice of solve entry s starts at nbrPtr[s] - nbrPtr[first
-// entry of the block]; a slot of the plain and Chebyshev sweeps is 24 bytes, a float4 (position,
-// rest x) in the first array of p.slab float4 and a float2 (rest y, rest z) in the second (a
-// 16-byte stride spreads random slots over all shared-memory banks; an incidence reads a 16- and
-// an 8-byte word per corner instead of two 16-byte words), and the same lane writes both parts of
-// a slot (rest x before the wait, the position after it, disjoint bytes); the contact variant keeps
-// two float4 arrays.  The lanes of a vertex share a warp, so __syncwarp orders the staging.
+// tets reference only ~14 distinct neighbours, so instead of gathering three corners' positions
+// per incidence, the vertex's lanes load each neighbour's current position once into its slice of
+// the block's slab (a float4 per neighbour) after griddepcontrol.wait, and the incidence loop reads
+// them back through the three slot bytes of its packed incidence word.  The slab slice of solve entry s starts at nbrPtr[s] - nbrPtr[first entry of the block].
+// The lanes of a vertex share a warp, so __syncwarp orders the staging.
 template <int L, bool CHEB, bool REC = false, bool CONTACT = false>
 __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(SweepParams p)
 {
-    // Neighbour slot j.  Plain and Chebyshev sweeps: slab[j] = (x, y, z, rest x) and
-    // restYZ[j] = (rest y, rest z), 24 bytes a slot.  Contact variant: slab[j] = position and
-    // rest[j] = rest position, 32 bytes a slot (measured faster for that variant: 2.22 against
-    // 2.35 ms per contact step, where the packed slots took the Chebyshev beam step from 4.87 to
-    // 4.77 ms).
     extern __shared__ float4 slab[];
-    float2* const restYZ = reinterpret_cast<float2*>(slab + p.slab);
-    float4* const rest   = slab + p.slab;
     int const tid    = blockIdx.x * blockDim.x + threadIdx.x;
     int const s      = p.begin + tid / L;
     int const lane   = tid & (L - 1);
@@ -289,34 +130,21 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(Swee
     zero(b);
     int i       = 0;
     float xi[3] = {0.f, 0.f, 0.f};
-    float Xi[3] = {0.f, 0.f, 0.f};
     int k = 0, k1 = 0, n0 = 0, n1 = 0, base = 0;
-    uint2 q     = make_uint2(0u, 0u);
-    float4 mat  = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint2 q   = make_uint2(0u, 0u);
+    float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
     if (valid)
     {
-        i  = __ldg(p.solve + s);
-        load3(__ldg(p.X + i), Xi);
+        i    = __ldg(p.solve + s);
         n0   = __ldg(p.nbrPtr + s);
         n1   = __ldg(p.nbrPtr + s + 1);
         base = n0 - nb0;
-        for (int j = n0 + lane; j < n1; j += L)
-        {
-            float4 const Xa = __ldg(p.X + (__ldg(p.nbr + j) & kIndexMask));
-            if constexpr (CONTACT)
-                rest[base + j - n0] = Xa;
-            else
-            {
-                restYZ[base + j - n0]                               = make_float2(Xa.y, Xa.z);
-                reinterpret_cast<float*>(slab + base + j - n0)[3] = Xa.x;
-            }
-        }
-        k1 = __ldg(p.incPtr + s + 1);
-        k  = __ldg(p.incPtr + s) + lane;
+        k1   = __ldg(p.incPtr + s + 1);
+        k    = __ldg(p.incPtr + s) + lane;
         if (k < k1)
         {
-            q   = __ldg(p.incPack + k);
-            mat = __ldg(p.mats + q.x);
+            q  = __ldg(p.incPack + k);
+            st = __ldg(p.stiff + k);
         }
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
@@ -330,15 +158,7 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(Swee
             float4 const* src = p.x;
             if (CHEB && !(a >> 31))
                 src = p.hprev;
-            float4 const xa = __ldg(src + (a & kIndexMask));
-            if constexpr (CONTACT)
-                slab[base + j - n0] = xa;
-            else
-            {
-                float* const dst                = reinterpret_cast<float*>(slab + base + j - n0);
-                *reinterpret_cast<float2*>(dst) = make_float2(xa.x, xa.y);
-                dst[2]                          = xa.z;
-            }
+            slab[base + j - n0] = __ldg(src + (a & kIndexMask));
         }
     }
     __syncwarp();
@@ -346,105 +166,44 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(Swee
     {
         for (; k < k1; k += L)
         {
-            uint2 qn     = make_uint2(0u, 0u);
-            float4 matn  = make_float4(0.f, 0.f, 0.f, 0.f);
+            uint2 qn   = make_uint2(0u, 0u);
+            float4 stn = make_float4(0.f, 0.f, 0.f, 0.f);
             if (k + L < k1)
             {
-                qn   = __ldg(p.incPack + k + L);
-                matn = __ldg(p.mats + qn.x);
+                qn  = __ldg(p.incPack + k + L);
+                stn = __ldg(p.stiff + k + L);
             }
-            float d[3][3], e[3][3];
+            float d[3][3];
 #pragma unroll
             for (int m = 0; m < 3; ++m)
             {
-                int const slot   = base + int((q.y >> (8 * m)) & 0xFFu);
-                float4 const xa = slab[slot];
-                float Xa[3];
-                if constexpr (CONTACT)
-                {
-                    float4 const r = rest[slot];
-                    Xa[0] = r.x, Xa[1] = r.y, Xa[2] = r.z;
-                }
-                else
-                {
-                    float2 const r = restYZ[slot];
-                    Xa[0] = xa.w, Xa[1] = r.x, Xa[2] = r.y;
-                }
+                float4 const xa = slab[base + int((q.x >> (8 * m)) & 0xFFu)];
                 d[m][0] = xa.x - xi[0];
                 d[m][1] = xa.y - xi[1];
                 d[m][2] = xa.z - xi[2];
-                e[m][0] = Xa[0] - Xi[0];
-                e[m][1] = Xa[1] - Xi[1];
-                e[m][2] = Xa[2] - Xi[2];
             }
-            float G[3][3];
-            rest_gradients(e, G);
-            accumulate_tet(b, d, G, mat.x, mat.y, mat.z);
-            q   = qn;
-            mat = matn;
+            accumulate_incidence(b, d, st.x, st.y, st.z, __uint_as_float(q.y), st.w);
+            q  = qn;
+            st = stn;
         }
     }
     finish_vertex<L, CHEB, REC, CONTACT>(p, b, valid, lane, i, s, xi);
 }
 
-// Start of a substep (sim/vbd/Integrator.cpp:31-34,54-71; gpu/impl/vbd/Integrator.cu:190-248):
-// xt <- x, xtilde = xt + h v + h^2 aext, x <- initial guess.
+// Start of a substep, one thread per vertex (begin_substep_vertex).
 __global__ void begin_substep_kernel(SubstepParams p)
 {
     int const i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n)
-        return;
-    float4 const x4 = p.x[i];
-    float4 const v4 = p.v[i];
-    float4 const a4 = p.aext[i];
-    float const xt[3] = {x4.x, x4.y, x4.z};
-    float const vt[3] = {v4.x, v4.y, v4.z};
-    float const a[3]  = {a4.x, a4.y, a4.z};
-    float vm[3]       = {vt[0], vt[1], vt[2]};
-    if (p.gpuSemantics)
-    {
-        float4 const w = p.vprev[i];
-        vm[0] = w.x, vm[1] = w.y, vm[2] = w.z;
-    }
-    p.xt[i]     = make_float4(xt[0], xt[1], xt[2], p.m[i]);
-    p.xtilde[i] = make_float4(
-        xt[0] + p.h * vt[0] + p.h2 * a[0],
-        xt[1] + p.h * vt[1] + p.h2 * a[1],
-        xt[2] + p.h * vt[2] + p.h2 * a[2],
-        0.f);
-    float x0[3];
-    initial_position(xt, vm, vt, a, p.h, p.h2, p.strategy, FLT_MIN, x0);
-    float4 const x04 = make_float4(x0[0], x0[1], x0[2], 0.f);
-    p.x[i]           = x04;
-    if (p.h0)
-    {
-        p.h0[i] = x04;
-        p.h1[i] = x04;
-    }
+    if (i < p.n)
+        begin_substep_vertex(p, i);
 }
 
-// End of a substep: v = (x - xt)/h (sim/vbd/Kernels.h:121-129); the previous velocity is kept
-// for the GPU integrator's AdaptiveVbd (gpu/impl/vbd/Integrator.cu:329-347).  Non-finite state
-// raises flags[0].
+// End of a substep, one thread per vertex (end_substep_vertex).
 __global__ void end_substep_kernel(SubstepParams p)
 {
     int const i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n)
-        return;
-    float4 const x4  = p.result[i];
-    float4 const xt4 = p.xt[i];
-    float4 const vo  = p.v[i];
-    if (p.result != p.x)
-        p.x[i] = x4;
-    float const inv  = 1.f / p.h;
-    float4 const vn  = make_float4((x4.x - xt4.x) * inv, (x4.y - xt4.y) * inv, (x4.z - xt4.z) * inv, 0.f);
-    if (p.gpuSemantics)
-        p.vprev[i] = vo;
-    p.v[i] = vn;
-    bool const finite = isfinite(x4.x) && isfinite(x4.y) && isfinite(x4.z) && isfinite(vn.x) &&
-                        isfinite(vn.y) && isfinite(vn.z);
-    if (!finite)
-        atomicOr(p.flags, 1);
+    if (i < p.n)
+        end_substep_vertex(p, i);
 }
 
 // Objective of the backward-Euler step (sim/vbd/Integrator.cpp:138-165): per-entity terms in FP32,
@@ -531,19 +290,39 @@ __global__ void gradient_kernel(EnergyParams p)
     }
 }
 
-__global__ void pack3_kernel(float const* __restrict__ in3, float4* __restrict__ out4, int32_t n)
-{
-    int const i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n)
-        out4[i] = make_float4(in3[3 * i], in3[3 * i + 1], in3[3 * i + 2], 0.f);
-}
-
-__global__ void unpack3_kernel(float4 const* __restrict__ in4, float* __restrict__ out3, int32_t n)
+// 3 x n floats -> float4 per vertex, minus the vertex's origin when given (positions of a batch,
+// stored relative to their mesh's origin).
+__global__ void pack3_kernel(float const* __restrict__ in3, float4* __restrict__ out4, int32_t n, float4 const* __restrict__ origin)
 {
     int const i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n)
     {
-        float4 const v = in4[i];
+        float4 v = make_float4(in3[3 * i], in3[3 * i + 1], in3[3 * i + 2], 0.f);
+        if (origin)
+        {
+            float4 const o = origin[i];
+            v.x -= o.x;
+            v.y -= o.y;
+            v.z -= o.z;
+        }
+        out4[i] = v;
+    }
+}
+
+// float4 per vertex -> 3 x n floats, plus the vertex's origin when given.
+__global__ void unpack3_kernel(float4 const* __restrict__ in4, float* __restrict__ out3, int32_t n, float4 const* __restrict__ origin)
+{
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        float4 v = in4[i];
+        if (origin)
+        {
+            float4 const o = origin[i];
+            v.x += o.x;
+            v.y += o.y;
+            v.z += o.z;
+        }
         out3[3 * i]     = v.x;
         out3[3 * i + 1] = v.y;
         out3[3 * i + 2] = v.z;
@@ -604,7 +383,7 @@ cudaError_t launch_sweep_l(SweepParams const& p, int g, int block, bool pdl, cud
     cfg.gridDim            = dim3(unsigned(g));
     cfg.blockDim           = dim3(unsigned(block));
     // stagedBytes sizes the largest slot; this variant's slots may be smaller (staged_sweep_kernel).
-    cfg.dynamicSmemBytes   = stagedBytes > 0 ? size_t(p.slab) * kStagedSlotBytes<CONTACT> : 0;
+    cfg.dynamicSmemBytes   = stagedBytes;
     cfg.stream             = s;
     cudaLaunchAttribute attr[1];
     attr[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -636,7 +415,7 @@ cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebys
     int64_t const n = int64_t(p.end - p.begin) * lanes;
     if (n <= 0)
         return cudaSuccess;
-    if (stagedBytes > kStagedMaxBytes || (stagedBytes > 0 && (!p.nbrPtr || !p.nbr || !p.incPack || !p.mats)))
+    if (!p.stiff || !p.incPack || stagedBytes > kStagedMaxBytes || (stagedBytes > 0 && (!p.nbrPtr || !p.nbr)))
         return cudaErrorInvalidValue;
     // Contact terms exist only in the two-buffer sweep (a contact partner of the same colour is
     // read as it was before the pass): a one-buffer launch with contact lists is a caller error.
@@ -644,7 +423,6 @@ cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebys
         return cudaErrorInvalidValue;
     int const g   = blocks_for(n, block);
     SweepParams q = p;
-    q.slab        = int32_t(stagedBytes / kStagedSlotBytesMax);
     if (chebyshev && q.fc)
         return launch_sweep_t<true, false, true>(q, lanes, g, block, pdl, s, stagedBytes);
     return chebyshev ? launch_sweep_t<true, false>(q, lanes, g, block, pdl, s, stagedBytes)
@@ -656,10 +434,9 @@ cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool
     int64_t const n = int64_t(p.end - p.begin) * lanes;
     if (n <= 0)
         return cudaSuccess;
-    if (!p.tape || stagedBytes > kStagedMaxBytes || (stagedBytes > 0 && (!p.nbrPtr || !p.nbr || !p.incPack || !p.mats)))
+    if (!p.tape || !p.stiff || !p.incPack || stagedBytes > kStagedMaxBytes || (stagedBytes > 0 && (!p.nbrPtr || !p.nbr)))
         return cudaErrorInvalidValue;
     SweepParams q = p;
-    q.slab        = int32_t(stagedBytes / kStagedSlotBytesMax);
     return launch_sweep_t<false, true>(q, lanes, blocks_for(n, block), block, pdl, s, stagedBytes);
 }
 
@@ -674,7 +451,7 @@ size_t staged_sweep_bytes(int32_t const* nbrPtr, int32_t begin, int32_t end, int
         int32_t const b1 = b0 + per < end ? b0 + per : end;
         most             = std::max<int64_t>(most, int64_t(nbrPtr[b1]) - nbrPtr[b0]);
     }
-    return size_t(most) * kStagedSlotBytesMax;
+    return size_t(most) * kStagedSlotBytes;
 }
 
 namespace {
@@ -756,11 +533,11 @@ cudaError_t launch_gradient(EnergyParams const& p, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t launch_pack3(float const* in3, float4* out4, int32_t n, cudaStream_t s)
+cudaError_t launch_pack3(float const* in3, float4* out4, int32_t n, cudaStream_t s, float4 const* origin)
 {
     if (n <= 0)
         return cudaSuccess;
-    pack3_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in3, out4, n);
+    pack3_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in3, out4, n, origin);
     return cudaGetLastError();
 }
 
@@ -773,11 +550,11 @@ cudaError_t launch_contact_records(int32_t nV, int32_t const* fc, int4 const* F,
     return cudaGetLastError();
 }
 
-cudaError_t launch_unpack3(float4 const* in4, float* out3, int32_t n, cudaStream_t s)
+cudaError_t launch_unpack3(float4 const* in4, float* out3, int32_t n, cudaStream_t s, float4 const* origin)
 {
     if (n <= 0)
         return cudaSuccess;
-    unpack3_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in4, out3, n);
+    unpack3_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in4, out3, n, origin);
     return cudaGetLastError();
 }
 

@@ -41,7 +41,6 @@ struct SweepParams
     float4* __restrict__ hcur;         // Chebyshev: iterate k-2 in, accelerated iterate k out
     float4 const* __restrict__ xt;     // .w = lumped mass
     float4 const* __restrict__ xtilde; // inertial target
-    float4 const* __restrict__ X;      // rest positions
     TetRecord const* __restrict__ tets;
     int32_t const* __restrict__ solve;
     int32_t const* __restrict__ incPtr;
@@ -71,16 +70,18 @@ struct SweepParams
     float muC;
     float muF;
     float epsv;
+    // Per-incidence stiffness (solve order, TetStiffness resolved for the incidence's own corner):
+    // stiff[k] = (b0, b1, b2, kappa_o); incPack[k] = (neighbour slots, sigma as bits): the three
+    // other corners' positions in the vertex's neighbour list in bytes 0-2 of .x (corner order
+    // (local + 1 + m) & 3; staged sweep only).  Every incidence reads these instead of rest
+    // positions.
+    float4 const* __restrict__ stiff;
+    uint2 const* __restrict__ incPack;
     // Neighbour staging (staged sweep only): for solve-list entry s, its distinct neighbours
     // nbr[nbrPtr[s] .. nbrPtr[s+1]) (vertex index in bits 0-29, bit 31 set when the neighbour has a
-    // lower colour, so that the two-buffer sweep reads it from x rather than hprev); per incidence
-    // k, incPack[k] = (tet, slots) with the three other corners' positions in that list in bytes
-    // 0-2 (corner order (local + 1 + m) & 3); mats[tet] = the record's material words.
+    // lower colour, so that the two-buffer sweep reads it from x rather than hprev).
     int32_t const* __restrict__ nbrPtr;
     uint32_t const* __restrict__ nbr;
-    uint2 const* __restrict__ incPack;
-    float4 const* __restrict__ mats;
-    int32_t slab; // staged entries per block (set by launch_sweep): positions [0, slab), rest positions [slab, 2 slab)
     // Applied Newton increments (one-buffer sweeps only, nullptr: not written): step[i] = x_new -
     // x_old for every solved vertex, the residual Anderson acceleration mixes (exact to FP32
     // relative precision, unlike the difference of two rounded positions).
@@ -143,17 +144,14 @@ cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebys
 // chebyshev = false, so a recorded step reproduces an unrecorded one.
 cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool pdl, cudaStream_t s, size_t stagedBytes = 0);
 // Dynamic shared memory of the staged sweep over solve entries [begin, end) with `lanes` lanes per
-// vertex and `block` threads per block: 32 bytes per staged neighbour of the block that stages the
+// vertex and `block` threads per block: 16 bytes per staged neighbour of the block that stages the
 // most (nbrPtr on the host).
 size_t staged_sweep_bytes(int32_t const* nbrPtr, int32_t begin, int32_t end, int lanes, int block);
 // Largest dynamic shared memory a staged sweep may use (set on the current device by
 // prepare_staged_sweeps); larger launches fall back to the gathering sweep.
 size_t constexpr kStagedMaxBytes = 200 * 1024;
-// Bytes of one staged neighbour: position and rest position packed in 24 bytes, or two float4 in
-// the contact variant; staged_sweep_bytes sizes slabs by the larger.
-template <bool CONTACT>
-size_t constexpr kStagedSlotBytes = CONTACT ? 2 * sizeof(float4) : sizeof(float4) + sizeof(float2);
-size_t constexpr kStagedSlotBytesMax = 2 * sizeof(float4);
+// Bytes of one staged neighbour: its current position (float4).
+size_t constexpr kStagedSlotBytes = sizeof(float4);
 cudaError_t prepare_staged_sweeps();
 cudaError_t launch_begin_substep(SubstepParams const& p, cudaStream_t s);
 cudaError_t launch_end_substep(SubstepParams const& p, cudaStream_t s);
@@ -162,10 +160,12 @@ int constexpr kObjectiveMaxBlocks = 1024;
 // Writes the objective to p.out[0] (no prior clearing needed); deterministic.
 cudaError_t launch_objective(EnergyParams const& p, cudaStream_t s);
 cudaError_t launch_gradient(EnergyParams const& p, cudaStream_t s);
-cudaError_t launch_pack3(float const* in3, float4* out4, int32_t n, cudaStream_t s);
+// origin (nullable, one float4 per vertex): positions are stored relative to it (pack subtracts,
+// unpack adds).
+cudaError_t launch_pack3(float const* in3, float4* out4, int32_t n, cudaStream_t s, float4 const* origin = nullptr);
 // Contact records of all nV vertices from their lists fc (see SweepParams::crec).
 cudaError_t launch_contact_records(int32_t nV, int32_t const* fc, int4 const* F, float const* FA, float const* XVA,
                                    int32_t const* vcolor, float muC, int4* crec, float* cpen, cudaStream_t s);
-cudaError_t launch_unpack3(float4 const* in4, float* out3, int32_t n, cudaStream_t s);
+cudaError_t launch_unpack3(float4 const* in4, float* out3, int32_t n, cudaStream_t s, float4 const* origin = nullptr);
 
 } // namespace pbgb

@@ -107,6 +107,100 @@ PBGB_HD void accumulate_tet(VertexBlock<T>& b, T const (&d)[3][3], T const (&G)[
     b.C[5] += law * c[2] * c[2];
 }
 
+// Rest-state constants of one tetrahedron for the vertex solves of its four corners, so that an
+// incidence needs only the current positions (the sweep's form of the closed-form block above).
+// With G_a = grad N_a (rows of the reference's GP), for corner o and its other corners a_m =
+// (o + 1 + m) & 3 and d_m = x_{a_m} - x_o:
+//   F w      = sum_m (G_{a_m} . w) d_m,                 w = G_o,
+//   cof(F) w = dJ/dx_o = -gamma_o n,  J = gamma_o (d_0 . n),  n = (d_1 - d_0) x (d_2 - d_0),
+// where gamma_o = 1 / det[X_{a_0} - X_o, X_{a_1} - X_o, X_{a_2} - X_o] = (-1)^o gamma_0 (a cyclic
+// shift of the four corners is an odd permutation) and gamma_0 = det[G_1; G_2; G_3].  So with
+// p = sigma n, sigma = sqrt(lambda') |gamma_0| and kappa_o = (-1)^o alpha sqrt(lambda') sign(gamma_0)
+// (lambda' = wg lambda, mu' = wg mu, alpha = 1 + mu/lambda):
+//   g_o += sum_m b_{o a_m} d_m + (kappa_o - d_0 . p) p,   C_o += p p^T,   s_o += -sum_m b_{o a_m}
+// with b_ab = mu' G_a . G_b (mu' |w|^2 = -sum_m b_{o a_m} because the G_a sum to zero).  The record
+// holds b01 b02 b03 b12 b13 b23, sigma, kappa_0: 32 bytes, shared by the four corners.
+struct TetStiffness
+{
+    float b[6];
+    float sigma;
+    float kappa;
+};
+
+// The record's eight words in FP64 (b01 b02 b03 b12 b13 b23 sigma kappa_0) from a tet's
+// shape-function gradients G4 (row-major 4 x 3, row a = grad N_a), quadrature weight and Lame
+// coefficients.
+PBGB_HD void tet_stiffness_words(double const* G4, double wg, double mu, double lambda, double (&w)[8])
+{
+    auto dot = [&](int a, int c) {
+        return G4[3 * a] * G4[3 * c] + G4[3 * a + 1] * G4[3 * c + 1] + G4[3 * a + 2] * G4[3 * c + 2];
+    };
+    double const* g1 = G4 + 3;
+    double const* g2 = G4 + 6;
+    double const* g3 = G4 + 9;
+    double const gamma0 = g1[0] * (g2[1] * g3[2] - g2[2] * g3[1]) - g1[1] * (g2[0] * g3[2] - g2[2] * g3[0]) +
+                          g1[2] * (g2[0] * g3[1] - g2[1] * g3[0]);
+    double const mup = wg * mu, lap = wg * lambda, alpha = 1.0 + mu / lambda;
+    double const rl  = sqrt(lap);
+    w[0] = mup * dot(0, 1);
+    w[1] = mup * dot(0, 2);
+    w[2] = mup * dot(0, 3);
+    w[3] = mup * dot(1, 2);
+    w[4] = mup * dot(1, 3);
+    w[5] = mup * dot(2, 3);
+    w[6] = rl * fabs(gamma0);
+    w[7] = gamma0 < 0.0 ? -alpha * rl : alpha * rl;
+}
+
+// The FP32 record (each word rounded once).
+PBGB_HD TetStiffness tet_stiffness(double const* G4, double wg, double mu, double lambda)
+{
+    double w[8];
+    tet_stiffness_words(G4, wg, mu, lambda, w);
+    TetStiffness r{};
+    for (int k = 0; k < 6; ++k)
+        r.b[k] = float(w[k]);
+    r.sigma = float(w[6]);
+    r.kappa = float(w[7]);
+    return r;
+}
+
+// The three b_{o a_m} of corner o (m = 0, 1, 2) and kappa_o, from the record's words.
+template <class T>
+PBGB_HD void corner_stiffness(T const (&b)[6], T kappa0, int o, T& b0, T& b1, T& b2, T& kappa)
+{
+    // o = 0: (01, 02, 03); o = 1: (12, 13, 01); o = 2: (23, 02, 12); o = 3: (03, 13, 23).
+    b0    = o == 0 ? b[0] : (o == 1 ? b[3] : (o == 2 ? b[5] : b[2]));
+    b1    = o == 0 ? b[1] : (o == 1 ? b[4] : (o == 2 ? b[1] : b[4]));
+    b2    = o == 0 ? b[2] : (o == 1 ? b[0] : (o == 2 ? b[3] : b[5]));
+    kappa = (o & 1) ? -kappa0 : kappa0;
+}
+
+// Adds one incidence to the vertex block (the sweep's arithmetic; see TetStiffness).
+//   d[m] = x_{a_m} - x_o in the corner order (o + 1 + m) & 3.
+template <class T>
+PBGB_HD void accumulate_incidence(VertexBlock<T>& b, T const (&d)[3][3], T b0, T b1, T b2, T sigma, T kappa)
+{
+    T u[3], v[3];
+    for (int r = 0; r < 3; ++r)
+    {
+        u[r] = d[1][r] - d[0][r];
+        v[r] = d[2][r] - d[0][r];
+    }
+    T const p[3] = {sigma * (u[1] * v[2] - u[2] * v[1]), sigma * (u[2] * v[0] - u[0] * v[2]),
+                    sigma * (u[0] * v[1] - u[1] * v[0])};
+    T const coef = kappa - (d[0][0] * p[0] + d[0][1] * p[1] + d[0][2] * p[2]);
+    for (int r = 0; r < 3; ++r)
+        b.g[r] += b0 * d[0][r] + b1 * d[1][r] + b2 * d[2][r] + coef * p[r];
+    b.s -= b0 + b1 + b2;
+    b.C[0] += p[0] * p[0];
+    b.C[1] += p[0] * p[1];
+    b.C[2] += p[0] * p[2];
+    b.C[3] += p[1] * p[1];
+    b.C[4] += p[1] * p[2];
+    b.C[5] += p[2] * p[2];
+}
+
 // Elastic block with Rayleigh damping (sim/vbd/Kernels.h:179-191): H = s I + C, g from the
 // accumulated block; damping adds (kD/h) H (x - xt) to g and scales H by 1 + kD/h.
 // H is symmetric (xx xy xz yy yz zz).

@@ -3,11 +3,13 @@ bindings/pypbat/gpu/vbd/Integrator.cpp:26-103; C++ API gpu/vbd/Integrator.h:33-1
 
 ``Integrator(data)`` reproduces the reference GPU integrator's step semantics (AdaptiveVbd uses
 the previous step's velocity).  ``BatchedIntegrator([data, ...])`` advances many independent meshes
-with one launch sequence per step (an addition: the reference has one mesh per integrator).
+with one persistent kernel launch per step (an addition: the reference has one mesh per
+integrator).
 """
 
 from __future__ import annotations
 
+import ctypes as C
 
 import numpy as np
 
@@ -79,9 +81,12 @@ class Integrator(IntegratorBase):
 
 
 class BatchedIntegrator(IntegratorBase):
-    """Many meshes of uneven size advanced together: their arrays are concatenated, colour c of
-    the batch is the union of every mesh's colour c, and one captured launch sequence steps all
-    of them.  ``x``/``v`` address the concatenation (mesh b's vertices follow mesh b-1's)."""
+    """Many meshes of uneven size advanced together: their arrays are concatenated, and one
+    persistent kernel launch per step advances every mesh, each through its own colours (a mesh
+    moves on as soon as its own previous colour is done).  With ``persistent = False``, or where
+    the persistent step does not apply, colour c of the batch is the union of every mesh's colour c,
+    one launch per colour.  ``x``/``v`` address the concatenation (mesh b's vertices follow mesh
+    b-1's)."""
 
     def __init__(self, datas, semantics=SEMANTICS_GPU):
         datas = list(datas)
@@ -93,6 +98,27 @@ class BatchedIntegrator(IntegratorBase):
 
     def step(self, dt=0.01, iterations=20, substeps=1):
         self._step(dt, iterations, substeps)
+
+    @property
+    def persistent(self):
+        """Whether the next step runs as one persistent launch."""
+        active = C.c_int32()
+        _capi.check(_capi.lib().pbgb_vbd_persistent(self._h, C.byref(active)), self._h)
+        return bool(active.value)
+
+    @persistent.setter
+    def persistent(self, enable):
+        _capi.check(_capi.lib().pbgb_vbd_set_persistent(self._h, int(bool(enable))), self._h)
+
+    @property
+    def batch_tile(self):
+        return getattr(self, "_batch_tile", 1)
+
+    @batch_tile.setter
+    def batch_tile(self, subtiles):
+        """Sweep work items of ``subtiles`` x (block size / lanes per vertex) vertices."""
+        _capi.check(_capi.lib().pbgb_vbd_set_batch_tile(self._h, int(subtiles)), self._h)
+        self._batch_tile = int(subtiles)
 
     @property
     def x(self):

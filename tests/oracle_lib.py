@@ -325,7 +325,7 @@ class OrcContact(C.Structure):
         ("nSurfV", C.c_int32), ("V", C.c_void_p), ("nF", C.c_int32), ("F", C.c_void_p), ("B", C.c_void_p),
         ("XVA", C.c_void_p), ("FA", C.c_void_p), ("muC", C.c_double), ("muF", C.c_double),
         ("epsv", C.c_double), ("freq", C.c_int32), ("wmin", C.c_float * 3), ("wmax", C.c_float * 3),
-        ("active", C.c_void_p), ("dupper", C.c_void_p), ("fc", C.c_void_p),
+        ("active", C.c_void_p), ("dupper", C.c_void_p), ("fc", C.c_void_p), ("forced_fc", C.c_void_p),
     ]
 
 
@@ -360,10 +360,19 @@ class OracleContactVbd(OracleVbd):
         Cc.wmax[:] = [float(c) for c in X.max(axis=0).astype(np.float32)]
         self.C = Cc
 
-    def step(self, dt, iterations, substeps=1, nsteps=1, use_ref=False, trust_region_log=None):
+    def step(self, dt, iterations, substeps=1, nsteps=1, use_ref=False, trust_region_log=None, contact_lists=None):
+        """contact_lists (replay): the lists (|#vertices| x 8 per list update, e.g. the device's) to
+        use instead of the oracle's own nearest-triangle queries."""
         own = np.zeros((nsteps * substeps * iterations, 4))
         self.P.tr_log = own.ctypes.data
         self.trust_region_log = own
+        lists = None
+        if contact_lists is not None:
+            updates = (nsteps * substeps + self.C.freq - 1) // self.C.freq
+            lists = np.ascontiguousarray(contact_lists, dtype=np.int32).reshape(-1)
+            if lists.size != updates * 8 * self.X.shape[0]:
+                raise ValueError("contact_lists must hold |#vertices| x 8 entries per list update")
+            self.C.forced_fc = lists.ctypes.data
         forced = None
         if trust_region_log is not None:
             forced = np.ascontiguousarray(trust_region_log, dtype=np.float64)
@@ -376,6 +385,7 @@ class OracleContactVbd(OracleVbd):
         finally:
             self.P.tr_forced = None
             self.P.tr_log = None
+            self.C.forced_fc = None
         if rc != 0:
             raise RuntimeError(f"oracle run failed: {rc}")
 

@@ -140,19 +140,95 @@ def test_contact_scene_lbvh_bit_exact_at_every_step_of_120():
     assert active.sum() > 100  # the cubes rest on the slab
 
 
-def test_contact_scene_positions_match_contact_oracle_through_first_contact():
-    """The first 20 steps (the cubes start 5 cm above the slab and touch it at about step 6)
-    against the FP64 contact oracle."""
+def device_contact_state(I, nV, nS):
+    """(x, v, vprev, active, dupper, fc) of the device integrator, from its checkpoint blob
+    (header of 6 int32; x, v, vprev, aext as nV float4; active flags padded to 4 bytes; search
+    radii as nS float32; contact lists as 8 nV int32)."""
+    blob = I.save_state()
+    off = 24
+    arrays = []
+    for _ in range(4):
+        arrays.append(np.frombuffer(blob, np.float32, 4 * nV, off).reshape(nV, 4)[:, :3].astype(np.float64))
+        off += 16 * nV
+    active = np.frombuffer(blob, np.uint8, nS, off).copy()
+    off += (nS + 3) & ~3
+    dupper = np.frombuffer(blob, np.float32, nS, off).astype(np.float64)
+    off += 4 * nS
+    fc = np.frombuffer(blob, np.int32, 8 * nV, off).copy()
+    return arrays[0], arrays[1], arrays[2], active, dupper, fc
+
+
+def point_triangle_distance(p, a, b, c):
+    """Distance from p to triangle abc (closest point by Voronoi regions of the triangle)."""
+    ab, ac, ap = b - a, c - a, p - a
+    d1, d2 = ab @ ap, ac @ ap
+    if d1 <= 0 and d2 <= 0:
+        return np.linalg.norm(p - a)
+    bp = p - b
+    d3, d4 = ab @ bp, ac @ bp
+    if d3 >= 0 and d4 <= d3:
+        return np.linalg.norm(p - b)
+    vc = d1 * d4 - d3 * d2
+    if vc <= 0 and d1 >= 0 and d3 <= 0:
+        return np.linalg.norm(p - (a + d1 / (d1 - d3) * ab))
+    cp = p - c
+    d5, d6 = ab @ cp, ac @ cp
+    if d6 >= 0 and d5 <= d6:
+        return np.linalg.norm(p - c)
+    vb = d5 * d2 - d1 * d6
+    if vb <= 0 and d2 >= 0 and d6 <= 0:
+        return np.linalg.norm(p - (a + d2 / (d2 - d6) * ac))
+    va = d3 * d6 - d5 * d4
+    if va <= 0 and (d4 - d3) >= 0 and (d5 - d6) >= 0:
+        return np.linalg.norm(p - (b + (d4 - d3) / ((d4 - d3) + (d5 - d6)) * (c - b)))
+    den = 1.0 / (va + vb + vc)
+    return np.linalg.norm(p - (a + ab * vb * den + ac * vc * den))
+
+
+def test_contact_scene_matches_contact_oracle_through_contact():
+    """30 steps (the cubes start 5 cm above the slab and touch it at about step 6).
+
+    * Until the first contact, free-running positions agree within 1e-4 of the diagonal.
+    * Every step, the contact lists the device chose agree with the lists the FP64 oracle chooses
+      from the same state (the device's positions, velocities and active set at the step's
+      start), except where the two differ only by triangles whose distances to the vertex are
+      tied within 1e-5 of the scene diagonal: the reference's list keeps triangles within
+      FLT_EPSILON of the nearest, so a tie is decided by the last bits of the arithmetic.
+    * With the device's lists replayed in the oracle (its own positions, the device's discrete
+      decisions), positions agree within 1e-4 of the diagonal at every step."""
     w, I = contact_scene_integrator()
-    R = O.OracleContactVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], w["V"], w["F"], w["B"],
-                           muC=1e7, muF=0.3, epsv=1e-3, strategy=2)
+    kw = dict(muC=1e7, muF=0.3, epsv=1e-3, strategy=2)
+    R = O.OracleContactVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], w["V"], w["F"], w["B"], **kw)
+    D = O.OracleContactVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], w["V"], w["F"], w["B"], **kw)
+    nV, V, F = w["X"].shape[0], np.asarray(w["V"]), np.asarray(w["F"])
     d = diag(w["X"])
-    errs, first_contact = [], None
-    for step in range(20):
+    replay, free, first_contact, mismatched, listed = [], [], None, 0, 0
+    for step in range(30):
+        x0, v0, vp0, act0, dup0, fc0 = device_contact_state(I, nV, V.size)
         I.step(1 / 60, 30, 1)
-        R.step(1 / 60, 30, 1, 1)
-        errs.append(float(np.abs(I.x.T.astype(np.float64) - R.x).max() / d))
-        if first_contact is None and R.active.any():
+        fc_dev = I.contacts()[0].reshape(-1)
+        # The oracle's own decisions from the device's state.
+        D.x[:], D.v[:], D.vprev[:] = x0, v0, vp0
+        D.active[:], D.dupper[:], D.fc[:] = act0, dup0, fc0
+        D.step(1 / 60, 30, 1, 1)
+        dev, orc = fc_dev.reshape(nV, 8), D.fc.reshape(nV, 8)
+        xs = x0 + (1 / 60) * v0 + (1 / 60) ** 2 * D.aext  # the initial guess the lists were taken at
+        for i in np.nonzero((dev != orc).any(axis=1))[0]:
+            a, b = set(dev[i][dev[i] >= 0]), set(orc[i][orc[i] >= 0])
+            dist = {f: point_triangle_distance(xs[i], *xs[F[f]]) for f in a | b}
+            best = min(dist.values())
+            assert all(dist[f] - best <= 1e-5 * d for f in a ^ b), (step, i, dist)
+            mismatched += 1
+        listed += int((dev >= 0).any(axis=1).sum())
+        # Replay: the oracle's positions under the device's lists.
+        R.step(1 / 60, 30, 1, 1, contact_lists=fc_dev)
+        x = I.x.T.astype(np.float64)
+        replay.append(float(np.abs(x - R.x).max() / d))
+        if first_contact is None and (fc_dev >= 0).any():
             first_contact = step
+        if first_contact is None:
+            free.append(replay[-1])
     assert first_contact is not None and first_contact < 15, first_contact
-    assert max(errs) <= TOL, errs
+    assert max(free) <= TOL, free
+    assert max(replay) <= TOL, replay
+    assert listed > 1000 and mismatched <= 0.01 * listed, (mismatched, listed)
