@@ -1,16 +1,22 @@
 #!/usr/bin/env python3
 """Benchmark of the VBD step on one GB300 (replicas on N GPUs under torchrun).
 
-Workload (default ``beam``): the [0,4]x[0,1]x[0,1] beam as a 160x40x40 hex grid split into 6 tets
-per hex (270,641 vertices, 1,536,000 tets), E=5e5, nu=0.48, density 1000, x=0 face pinned,
-initial velocities U(-0.1, 0.1) from a seed, gravity on; Chebyshev acceleration rho=0.95 (the
-reference's weight recurrence), 50 iterations per step, dt=1/60.  A "step" is one time step.
-Metric: vertex-updates/s = free vertices x iterations x substeps x steps / time.
+Headline workload (the metric's configuration): 256 cube grids with side n ~ U{6..32} hexes split
+into 6 tets per hex (3,252,189 vertices, 17,350,662 tets), E log-uniform in [1e5, 1e7], nu
+U(0.30, 0.48), density 1000, one face pinned, gravity, 20 VBD iterations per step, dt = 1/60, all
+meshes stepped together by the batched integrator (one persistent launch per step); beside it the
+same meshes stepped by one integrator per mesh (one launch per colour, each on its own stream).
+A "step" is one time step of the whole batch.  Metric: vertex-updates/s = free vertices x
+iterations x substeps x steps / time.
+
+Secondary legs: the [0,4]x[0,1]^2 beam at 160x40x40 hexes (270,641 vertices, Chebyshev rho 0.95, 50
+iterations), the adjoint on the 40x10x10 differentiation beam, the 16-cube contact scene, a
+4.19M-box LBVH build and the Anderson / trust-region / Broyden accelerations on the beam.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 ``--impl reference`` times the reference algorithm's CPU implementation (the FP64 oracle port, all
-host threads) on the same workload and prints the same JSON line with "impl": "reference".
+host threads) on the same batched workload and prints the same JSON line with "impl": "reference".
 """
 
 from __future__ import annotations
@@ -138,76 +144,107 @@ def peak_hbm():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def traffic_from_profiles():
-    """DRAM bytes per sweep launch from the committed ncu summary (warm-L2 capture; None if
-    absent)."""
-    f = ROOT / "profiles" / "vbd_sweep_beam160x40x40.md"
+KERNEL_SOURCES = {
+    "batched_step_cfg3.md": ["batched.cu", "batched.cuh", "sweep_device.cuh", "vbd_math.cuh", "vbd_kernels.cuh"],
+    "vbd_sweep_beam160x40x40.md": ["vbd_kernels.cu", "sweep_device.cuh", "vbd_math.cuh", "vbd_kernels.cuh"],
+}
+
+
+def kernel_source_sha(name):
+    """sha256 (first 16 hex digits) of the sources the kernel of a profile summary is built from."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES[name]:
+        h.update((ROOT / "physicsbasedanimationtoolkit_gb300" / "csrc" / f).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def traffic_from_profiles(name):
+    """DRAM bytes per launch from the committed ncu summary profiles/<name>, when the summary was
+    captured from the current kernel sources (its `source_sha` line equals their hash); otherwise
+    (None, reason)."""
+    f = ROOT / "profiles" / name
     try:
-        for line in f.read_text().splitlines():
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1].strip())
+        lines = f.read_text().splitlines()
     except OSError:
-        pass
-    return None
+        return None, "no profile summary"
+    traffic, sha = None, None
+    for line in lines:
+        if line.startswith("traffic_bytes_per_launch:"):
+            traffic = float(line.split(":", 1)[1].strip())
+        elif line.startswith("source_sha:"):
+            sha = line.split(":", 1)[1].strip()
+    if traffic is None:
+        return None, "the profile summary has no traffic figure"
+    if sha != kernel_source_sha(name):
+        return None, "the profile summary was captured from other kernel sources"
+    return traffic, f"ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/{name}"
 
 
-def cpu_baseline(w, iterations, seconds_budget=20.0):
-    """The FP64 oracle (port of the reference's CPU integrator) on all host threads, on a bounded
-    sample of the same workload: whole time steps while they fit the budget, else one step with
-    fewer iterations."""
+def batch_oracles(meshes):
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_lib as O
 
     O.build_oracle()
     threads = O.lib().orc_num_threads()
-    I = O.OracleVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], v=w["v"], rho_chebyshev=0.95)
-    n_free = I.data["Padj"].size
-    # Probe with a few iterations to size the sample.
+    oracles = [O.OracleVbd(m["X"], m["T"], m["rho"], m["mu"], m["lam"], m["dbc"], v=m["v"], strategy=4, semantics=1)
+               for m in meshes]
+    return oracles, int(threads)
+
+
+def cpu_batch_step(oracles, iterations):
+    """One time step of every mesh with the FP64 oracle, one mesh after the other (the reference
+    steps one mesh per integrator), each mesh's colour sweeps on all host threads."""
+    for R in oracles:
+        R.step(1 / 60, iterations, 1, 1)
+
+
+def cpu_baseline(meshes, iterations, seconds_budget=20.0):
+    """The FP64 oracle (port of the reference's CPU integrator) on all host threads, on a bounded
+    sample of the batched workload: one time step of all meshes with as many of the iterations as
+    fit the budget."""
+    oracles, threads = batch_oracles(meshes)
+    n_free = sum(int(R.data["Padj"].size) for R in oracles)
     t0 = time.perf_counter()
-    I.step(1 / 60, 2, 1, 1)
-    t_iter = (time.perf_counter() - t0) / 2
+    cpu_batch_step(oracles, 1)
+    t_iter = time.perf_counter() - t0
     iters = max(1, min(iterations, int(seconds_budget / max(t_iter, 1e-9))))
-    steps = max(1, int(seconds_budget / max(t_iter * iters, 1e-9))) if iters == iterations else 1
-    steps = min(steps, 3)
     t0 = time.perf_counter()
-    I.step(1 / 60, iters, 1, steps)
+    cpu_batch_step(oracles, iters)
     dt = time.perf_counter() - t0
-    updates = n_free * iters * steps
-    sample = (f"{steps} time step(s) x {iters} iterations of the {w['X'].shape[0]}-vertex beam "
-              f"(Chebyshev rho=0.95), FP64, {threads} OpenMP threads")
-    return {"value": updates / dt, "unit": UNIT, "cores": int(threads), "kind": "port", "sample": sample,
+    sample = (f"1 time step x {iters} of {iterations} iterations of all {len(meshes)} meshes (one after the "
+              f"other), FP64, {threads} OpenMP threads")
+    return {"value": n_free * iters / dt, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
             "seconds": dt}
 
 
 def run_reference(args):
-    """--impl reference: the CPU implementation of the path (oracle port), rank 0 only."""
+    """--impl reference: the CPU implementation of the path (oracle port) on the batched workload,
+    rank 0 only.  Each step is a bounded sample: one time step of all meshes with as many of the
+    iterations as keep warmup + steps within a few minutes."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    w = workload_beam(args)
-    sys.path.insert(0, str(ROOT / "tests"))
-    import oracle_lib as O
+    from physicsbasedanimationtoolkit_gb300 import meshgen
 
-    O.build_oracle()
-    threads = O.lib().orc_num_threads()
-    I = O.OracleVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], v=w["v"], rho_chebyshev=0.95)
-    n_free = I.data["Padj"].size
-    # Each step is a bounded sample of the workload: one time step with at most `iters` iterations
-    # so that warmup + steps fit a few minutes.
+    meshes = meshgen.batch_workload(n_meshes=args.batch_meshes, nmin=6, nmax=32, seed=0)
+    oracles, threads = batch_oracles(meshes)
+    n_free = sum(int(R.data["Padj"].size) for R in oracles)
     t0 = time.perf_counter()
-    I.step(1 / 60, 1, 1, 1)
+    cpu_batch_step(oracles, 1)
     t_iter = time.perf_counter() - t0
     budget = 150.0 / max(1, args.steps + args.warmup)
-    iters = max(1, min(args.iterations, int(budget / max(t_iter, 1e-9))))
+    iters = max(1, min(args.batch_iterations, int(budget / max(t_iter, 1e-9))))
     for _ in range(args.warmup):
-        I.step(1 / 60, iters, 1, 1)
+        cpu_batch_step(oracles, iters)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        I.step(1 / 60, iters, 1, 1)
+        cpu_batch_step(oracles, iters)
     el = time.perf_counter() - t0
     value = n_free * iters * args.steps / el
-    sample = (f"each step: 1 time step x {iters} of {args.iterations} iterations of the "
-              f"{w['X'].shape[0]}-vertex beam, FP64, {threads} OpenMP threads")
+    sample = (f"each step: 1 time step x {iters} of {args.batch_iterations} iterations of all {len(meshes)} "
+              f"meshes (one after the other), FP64, {threads} OpenMP threads")
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -222,8 +259,8 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": config_of(args, w),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(threads), "kind": "port", "sample": sample},
+        "config": config_of(args, meshes),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -605,7 +642,147 @@ def run_lbvh(args, _capi, torch):
     }
 
 
-def config_of(args, w):
+def run_single_launch(args, pbat, _capi, torch, meshes, datas, launch_config):
+    """The comparison arm of the headline: one single-mesh integrator per mesh (one launch per
+    colour), each on its own stream, with the headline's lanes and block size; CUDA events on the
+    streams (time_single_launch).  Also the agreement with a fresh batch after the same steps."""
+    dt, iters = 1 / 60, args.batch_iterations
+    lanes, block = launch_config["lanes"], launch_config["block"]
+    singles = []
+    for d in datas:
+        s = pbat.gpu.vbd.Integrator(d)
+        s.lanes_per_vertex = lanes
+        _capi.check(_capi.lib().pbgb_vbd_set_block_size(s.handle, block), s.handle)
+        singles.append(s)
+    for _ in range(args.warmup):
+        for s in singles:
+            s.step(dt, iters, 1)
+    for s in singles:
+        s.synchronize()
+    B = pbat.gpu.vbd.BatchedIntegrator(datas)
+    B.lanes_per_vertex = lanes
+    _capi.check(_capi.lib().pbgb_vbd_set_block_size(B.handle, block), B.handle)
+    for _ in range(args.warmup):
+        B.step(dt, iters, 1)
+    xb, off = B.x, B.vertex_offsets
+    worst = 0.0
+    for b, s in enumerate(singles):
+        X = meshes[b]["X"]
+        diag = np.linalg.norm(X.max(0) - X.min(0))
+        worst = max(worst, float(np.abs(xb[:, off[b]: off[b + 1]] - s.x).max() / diag))
+    del B
+    n_free = sum(s.n_free for s in singles)
+    t = time_single_launch(singles, dt, iters, args.steps, torch)
+    out = {
+        "value": n_free * iters * args.steps / t,
+        "ms_per_step": 1e3 * t / args.steps,
+        "launches_per_step": int(sum(s.launches_per_step(iters, 1) for s in singles)),
+        "max_rel_diff_batched_vs_single": worst,
+        "timing": "CUDA events: a start event all 256 streams wait on, an end event on every stream",
+        "unit": UNIT,
+    }
+    del singles
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_beam(args, pbat, _capi, torch):
+    """The single large beam: [0,4]x[0,1]^2 at 160x40x40 hexes (270,641 vertices, 1,536,000 tets),
+    E 5e5, nu 0.48, x=0 face pinned, initial velocities U(-0.1, 0.1), Chebyshev rho 0.95, 50
+    iterations per step, dt 1/60; the single-mesh integrator, launch autotuned.  Device-resident
+    rate (CUDA events, L2 flushed between steps), the colour-sweep roofline, and the rate through
+    the C ABI with host buffers."""
+    w = workload_beam(args)
+    data = make_data(pbat, w)
+    vbd = pbat.gpu.vbd.Integrator(data)
+    L = _capi.lib()
+    h = vbd.handle
+    dt, iters = 1 / 60, args.iterations
+    t_lanes, t_block, t_ms = vbd.autotune(dt, iters, 1)
+    n_free = vbd.n_free
+    sp = C.c_void_p()
+    _capi.check(L.pbgb_vbd_stream(h, C.byref(sp)), h)
+    stream = torch.cuda.ExternalStream(sp.value)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        vbd.step(dt, iters, 1)
+    vbd.synchronize()
+    steps = args.steps
+    t_total = 0.0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed_beam")
+    for _ in range(steps):
+        flush.add_(1.0)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        vbd.step(dt, iters, 1)
+        e1.record(stream)
+        vbd.synchronize()
+        t_total += e0.elapsed_time(e1)
+    torch.cuda.nvtx.range_pop()
+    ms_per_step = t_total / steps
+    launches_per_step = vbd.launches_per_step(iters, 1)
+    sweeps_per_step = iters * vbd.n_colors
+    nV = vbd.n_vertices
+    xh = torch.empty((nV, 3), dtype=torch.float32, pin_memory=True)
+    vh = torch.empty((nV, 3), dtype=torch.float32, pin_memory=True)
+    _capi.check(L.pbgb_vbd_get_positions(h, xh.data_ptr()), h)
+    _capi.check(L.pbgb_vbd_get_velocities(h, vh.data_ptr()), h)
+    e2e_steps = max(3, steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        _capi.check(L.pbgb_vbd_set_positions(h, xh.data_ptr()), h)
+        _capi.check(L.pbgb_vbd_set_velocities(h, vh.data_ptr()), h)
+        _capi.check(L.pbgb_vbd_step(h, dt, iters, 1), h)
+        _capi.check(L.pbgb_vbd_get_positions(h, xh.data_ptr()), h)
+        _capi.check(L.pbgb_vbd_get_velocities(h, vh.data_ptr()), h)
+    e2e_s = time.perf_counter() - t0
+    peak, peak_kind = peak_hbm()
+    bytes_per_launch = algorithmic_bytes(data) / vbd.n_colors
+    # Launch duration: the event-timed step over its colour launches (an upper bound: the substep
+    # kernels, ~2 % of the step, are counted against the sweeps).
+    avg_launch_ms = ms_per_step / sweeps_per_step
+    achieved = bytes_per_launch / (avg_launch_ms * 1e-3) / 1e9
+    traffic, traffic_basis = traffic_from_profiles("vbd_sweep_beam160x40x40.md")
+    out = {
+        "config": beam_config(args, w),
+        "value": n_free * iters / (ms_per_step * 1e-3),
+        "unit": UNIT,
+        "ms_per_step": ms_per_step,
+        "steps": steps,
+        "e2e": {"value": n_free * iters * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nV * 24,
+                "d2h_bytes_per_step": nV * 24},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "traffic_basis": traffic_basis, "peak_kind": peak_kind,
+                     "kernel": "staged_sweep_kernel (per-colour vertex Newton sweep)",
+                     "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_launch_ms * 1e3},
+        "launch_config": {"lanes": t_lanes, "block": t_block, "tuned_ms_per_step": t_ms},
+        "launches_per_step": int(launches_per_step),
+    }
+    del vbd, flush
+    torch.cuda.empty_cache()
+    return out
+
+
+def config_of(args, meshes):
+    nV = sum(int(m["X"].shape[0]) for m in meshes)
+    nT = sum(int(m["T"].shape[0]) for m in meshes)
+    return {
+        "workload": f"batch of {len(meshes)} cube grids, side U{{6..32}} hexes x 6 tets (seed 0), "
+                    f"{args.batch_iterations} iterations, no acceleration, one persistent launch per step",
+        "n_meshes": len(meshes),
+        "n_vertices": nV,
+        "n_tets": nT,
+        "iterations": args.batch_iterations,
+        "substeps": 1,
+        "dt": 1 / 60,
+        "material": "SNH, E log-uniform [1e5, 1e7], nu U(0.30, 0.48), rho 1000",
+        "parallelism": f"replicas x{args.gpus}",
+        "l2": "working set (~3 GB) > L2 (129 MB); L2 flushed (512 MB write) before every timed step",
+    }
+
+
+def beam_config(args, w):
     return {
         "workload": f"beam [0,4]x[0,1]^2 {args.nx}x{args.ny}x{args.nz} hexes x 6 tets, Chebyshev rho=0.95",
         "n_vertices": int(w["X"].shape[0]),
@@ -614,8 +791,6 @@ def config_of(args, w):
         "substeps": 1,
         "dt": 1 / 60,
         "material": "SNH E=5e5 nu=0.48 rho=1000",
-        "parallelism": f"replicas x{args.gpus}",
-        "l2": "working set > L2 (129 MB); L2 flushed (512 MB write) between timed steps",
     }
 
 
@@ -629,12 +804,11 @@ def main():
     ap.add_argument("--nx", type=int, default=160)
     ap.add_argument("--ny", type=int, default=40)
     ap.add_argument("--nz", type=int, default=40)
-    ap.add_argument("--lanes", type=int, default=0, help="headline: lanes per vertex instead of autotuning")
+    ap.add_argument("--lanes", type=int, default=0, help="headline (batch): lanes per vertex instead of autotuning")
     ap.add_argument("--block", type=int, default=0, help="headline with --lanes: block size (default 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--batch", dest="batch", action="store_true", default=True,
-                    help="also measure the batched multi-mesh form against one launch per mesh")
-    ap.add_argument("--no-batch", dest="batch", action="store_false")
+    ap.add_argument("--no-beam", dest="beam", action="store_false", default=True,
+                    help="skip the single large beam (Chebyshev, 50 iterations) leg")
     ap.add_argument("--batch-meshes", type=int, default=256)
     ap.add_argument("--batch-iterations", type=int, default=20)
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false", default=True,
@@ -652,7 +826,7 @@ def main():
                     "of autotuning (for profiling runs that must launch what a timed run launched)")
     ap.add_argument("--no-broyden", dest="broyden", action="store_false", default=True,
                     help="skip the Broyden-acceleration measurement")
-    ap.add_argument("--only", choices=["batch", "adjoint", "contact", "lbvh", "anderson", "broyden", "trust_region"],
+    ap.add_argument("--only", choices=["batch", "beam", "adjoint", "contact", "lbvh", "anderson", "broyden", "trust_region"],
                     default=None,
                     help="run only this secondary measurement and print its figures (no benchmark line)")
     args = ap.parse_args()
@@ -674,6 +848,7 @@ def main():
     if args.only:
         legs = {
             "batch": lambda: run_batch(args, pbat, _capi, torch),
+            "beam": lambda: run_beam(args, pbat, _capi, torch),
             "adjoint": lambda: run_adjoint(args, pbat, torch),
             "contact": lambda: run_contact(args, pbat, torch),
             "lbvh": lambda: run_lbvh(args, _capi, torch),
@@ -686,35 +861,30 @@ def main():
         group.close()
         return 0
 
-    w = workload_beam(args)
-    data = make_data(pbat, w)
-    vbd = pbat.gpu.vbd.Integrator(data)
+    meshes, datas = batch_workload(args, pbat)
     L = _capi.lib()
-    h = vbd.handle
-    dt, iters = 1 / 60, args.iterations
+    dt, iters = 1 / 60, args.batch_iterations
+    B = pbat.gpu.vbd.BatchedIntegrator(datas)
+    h = B.handle
     if args.lanes:
-        vbd.lanes_per_vertex = args.lanes
+        B.lanes_per_vertex = args.lanes
         if args.block:
             _capi.check(L.pbgb_vbd_set_block_size(h, args.block), h)
         tuned = None
     else:
         # The integrator's own autotuner (public API; restores the state after each candidate).
-        t_lanes, t_block, t_ms = vbd.autotune(dt, iters, 1)
+        t_lanes, t_block, t_ms = B.autotune(dt, iters, 1)
         tuned = {"lanes": t_lanes, "block": t_block, "ms_per_step": t_ms}
-    n_free = vbd.n_free
+    n_free = B.n_free
     sp = C.c_void_p()
     _capi.check(L.pbgb_vbd_stream(h, C.byref(sp)), h)
     stream = torch.cuda.ExternalStream(sp.value)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-
     for _ in range(args.warmup):
-        vbd.step(dt, iters, 1)
-    vbd.synchronize()
+        B.step(dt, iters, 1)
+    B.synchronize()
 
-    # ---- device-resident throughput -------------------------------------------------------------
-    # The step graph carries no per-launch events here: event nodes between the colour launches
-    # would cut the programmatic-dependent-launch overlap of consecutive colours (5.07 -> 5.59 ms on
-    # the beam).  Per-launch times come from a separate instrumented pass below.
+    # ---- device-resident throughput (CUDA events on the integrator's stream) --------------------
     t_total = 0.0
     ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -726,9 +896,9 @@ def main():
             flush.add_(1.0)  # L2 flush outside the timed interval
             torch.cuda.synchronize()
             ev0[k].record(stream)
-            vbd.step(dt, iters, 1)
+            B.step(dt, iters, 1)
             ev1[k].record(stream)
-            vbd.synchronize()
+            B.synchronize()
             t_total += ev0[k].elapsed_time(ev1[k])
         torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
@@ -737,32 +907,14 @@ def main():
     ms_per_step = t_total / args.steps
     updates_per_step = n_free * iters
     value = group.sum(updates_per_step * args.steps) / (t_total * 1e-3)
+    launches_per_step = B.launches_per_step(iters, 1)
 
-    launches_per_step = vbd.launches_per_step(iters, 1)
-    n_colors = vbd.n_colors
-    # ---- instrumented pass: CUDA events around every colour launch (same stream) ----------------
-    _capi.check(L.pbgb_vbd_set_sweep_timing(h, 1), h)
-    sweep_ms, sweep_launches, instr_steps = 0.0, 0, max(3, args.steps // 10)
-    for k in range(instr_steps + 1):
-        flush.add_(1.0)
-        torch.cuda.synchronize()
-        vbd.step(dt, iters, 1)
-        vbd.synchronize()
-        ms = C.c_double()
-        nl = C.c_int64()
-        _capi.check(L.pbgb_vbd_sweep_timing(h, C.byref(ms), C.byref(nl)), h)
-        if k > 0:  # the first step re-captures the graph
-            sweep_ms += ms.value
-            sweep_launches += nl.value
-    _capi.check(L.pbgb_vbd_set_sweep_timing(h, 0), h)
     # ---- end to end through the C ABI with host buffers -----------------------------------------
-    nV = vbd.n_vertices
+    nV = B.n_vertices
     xh = torch.empty((nV, 3), dtype=torch.float32, pin_memory=True)
     vh = torch.empty((nV, 3), dtype=torch.float32, pin_memory=True)
     _capi.check(L.pbgb_vbd_get_positions(h, xh.data_ptr()), h)
     _capi.check(L.pbgb_vbd_get_velocities(h, vh.data_ptr()), h)
-    vbd.step(dt, iters, 1)  # re-capture the graph without timing events
-    vbd.synchronize()
     e2e_steps = max(3, args.steps // 2)
     group.barrier()
     t0 = time.perf_counter()
@@ -775,27 +927,24 @@ def main():
     e2e_s = group.max(time.perf_counter() - t0)
     e2e_value = group.sum(updates_per_step * e2e_steps) / e2e_s
     io_bytes = nV * 3 * 4 * 2
+    persistent = B.persistent
+    lanes_used = B.lanes_per_vertex
+    del B, flush
+    torch.cuda.empty_cache()
 
     if rank == 0:
         peak, peak_kind = peak_hbm()
-        bytes_per_iter = algorithmic_bytes(data)
-        sweeps_per_step = sweep_launches / max(1, instr_steps)
-        n_sweeps_per_iter = sweeps_per_step / max(1, iters)
-        bytes_per_launch = bytes_per_iter / max(n_sweeps_per_iter, 1)
-        # Launch duration over the timed region: the event-timed step divided by its colour
-        # launches (an upper bound: the sweep is ~98% of the step, the rest is counted against it).
-        avg_launch_ms = ms_per_step / max(sweeps_per_step, 1)
-        instr_launch_ms = sweep_ms / max(1, sweep_launches)
-        achieved = bytes_per_launch / (avg_launch_ms * 1e-3) / 1e9
-        traffic = traffic_from_profiles()
-        launch_config = {"autotuned": tuned is not None, "lanes": vbd.lanes_per_vertex,
-                         "block": tuned["block"] if tuned else (args.block or 256)}
-        cpu = None if args.no_cpu_baseline else cpu_baseline(w, iters)
-        batched = None
-        if args.batch:
-            del vbd
-            torch.cuda.empty_cache()
-            batched = run_batch(args, pbat, _capi, torch)
+        bytes_per_step = batch_algorithmic_bytes(datas, iters)
+        # One persistent launch per step: the launch duration is the event-timed step (the
+        # counters' memset node before it, ~2 us, is counted against it).
+        avg_launch_ms = ms_per_step / max(launches_per_step, 1)
+        achieved = bytes_per_step / max(launches_per_step, 1) / (avg_launch_ms * 1e-3) / 1e9
+        traffic, traffic_basis = traffic_from_profiles("batched_step_cfg3.md")
+        launch_config = {"autotuned": tuned is not None, "lanes": lanes_used,
+                         "block": tuned["block"] if tuned else (args.block or 256), "persistent": persistent}
+        single = run_single_launch(args, pbat, _capi, torch, meshes, datas, launch_config)
+        cpu = None if args.no_cpu_baseline else cpu_baseline(meshes, iters)
+        beam = run_beam(args, pbat, _capi, torch) if args.beam else None
         adjoint = run_adjoint(args, pbat, torch) if args.adjoint else None
         contact = run_contact(args, pbat, torch) if args.contact else None
         lbvh = run_lbvh(args, _capi, torch) if args.lbvh else None
@@ -816,26 +965,26 @@ def main():
             "vs_baseline": None,
             "dtype": "f32",
             "data": "synthetic",
-            "config": config_of(args, w),
+            "config": config_of(args, meshes),
+            "single_launch_value": single["value"],
+            "speedup_vs_single_launch": single["value"] and value / single["value"],
+            "single_launch": single,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes,
                     "d2h_bytes_per_step": io_bytes,
                     "path": "C ABI pbgb_vbd_set_positions/velocities + step + get_positions/velocities, pinned host buffers"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
+                         "frac": achieved / peak, "traffic": traffic, "traffic_basis": traffic_basis,
                          "peak_kind": peak_kind,
-                         "kernel": "sweep_kernel (per-colour vertex Newton sweep)",
-                         "algorithmic_bytes_per_launch": bytes_per_launch,
+                         "kernel": "batched_step_kernel (persistent step of the whole batch)",
+                         "algorithmic_bytes_per_launch": bytes_per_step / max(launches_per_step, 1),
                          "avg_launch_us": avg_launch_ms * 1e3,
-                         "avg_launch_us_basis": "timed steps (CUDA events on the integrator's stream) / colour launches per step",
-                         "instrumented_launch_us": instr_launch_ms * 1e3,
-                         "instrumented_basis": "separate pass, CUDA events around each colour launch in the step graph"},
+                         "avg_launch_us_basis": "timed steps (CUDA events on the integrator's stream) / launches per step"},
             "launch_config": launch_config,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "clocks": clocks.summary(),
             "n_free_vertices": n_free,
-            "n_colors": n_colors,
-            "batched": batched,
+            "beam": beam,
             "adjoint": adjoint,
             "contact": contact,
             "lbvh": lbvh,

@@ -26,8 +26,8 @@
  *                                simplices, visits) gpu/geometry/Bvh.cu, gpu/impl/geometry/Bvh.cu/.cuh
  *   pbgb_simplex_boxes           gpu::geometry::Aabb::Construct(P, S) gpu/geometry/Aabb.cu
  *   pbgb_ccd_*                   VertexTriangleMixedCcdDcd            gpu/impl/contact/VertexTriangleMixedCcdDcd.cu
- * Beyond the reference: pbgb_vbd_create_batched (many meshes, one launch per colour),
- * pbgb_vbd_step_record / pbgb_vbd_step_adjoint (reverse-mode derivatives), pbgb_vbd_save_state /
+ * Beyond the reference: pbgb_vbd_create_batched (many meshes, one persistent launch per step),
+ * pbgb_vbd_step_record / pbgb_vbd_step_adjoint(_state) (reverse-mode derivatives), pbgb_vbd_save_state /
  * pbgb_vbd_load_state (checkpoints), *_device variants (device pointers), pbgb_vbd_autotune.
  */
 #ifndef PBAT_GB300_H
@@ -340,22 +340,33 @@ PBGB_API int pbgb_vbd_gradient_noalloc(pbgb_vbd* h, double dt, double* grad /* 3
  * When the forward iterations converge it becomes the adjoint of the converged step,
  * (M/h^2 + d2E/dx2) lambda = dL/dx.
  *
- * Supported forward settings: no acceleration, kD = 0, no contact, initial guess Position, Inertia
- * or KineticEnergyMinimum; other settings return PBGB_ERR_INVALID_ARGUMENT.
+ * Supported forward settings: plain VBD or Chebyshev acceleration (either weight recurrence), any
+ * Rayleigh damping kD, every initial guess (Position, Inertia, KineticEnergyMinimum, AdaptiveVbd,
+ * AdaptivePbat: the adaptive guesses' acceleration factor is differentiated on the branch the
+ * forward took), CPU or GPU step semantics; no contact and no Anderson, Nesterov, Broyden or
+ * trust-region acceleration (PBGB_ERR_INVALID_ARGUMENT).  AdaptivePbat's factor
+ * |v.a| / (|v| |a|^2) has no derivative at v = 0 (it jumps), where its derivative is taken as zero.
  *
  *   pbgb_vbd_adjoint_reserve: device tape for `slots` recorded substeps of `iterations` iterations:
- *     (iterations + 1) x nV iterates and iterations x n_free inverse 3x3 Newton matrices per slot
- *     (16 (iterations + 1) nV + 32 iterations n_free bytes).
+ *     per slot (iterations + 1) x nV iterates, the start positions, velocities and previous
+ *     velocities, iterations x n_free inverse 3x3 Newton matrices, and with Chebyshev iterations x
+ *     nV raw sweep results (16 (iterations + 4) nV + 32 iterations n_free bytes, plus 16 iterations
+ *     nV with Chebyshev).
  *   pbgb_vbd_step_record: one pbgb_vbd_step(dt, iterations, substeps) (the same positions) that
  *     records substep s into slot `slot` + s.  Launched directly, not from the step's graph.
- *   pbgb_vbd_step_adjoint: reverses the substeps in slots slot + substeps - 1 down to slot.
- *     xbar_dev, vbar_dev (device, 3 x nV): on entry the adjoints dL/dx, dL/dv of the state after
- *     the recorded step, on return those of the state before it.  dlogmu_dev, dloglambda_dev
- *     (device, nT, FP64): dL/dlog(mu), dL/dlog(lambda) of every tet, added to what they hold
- *     (with a fixed Poisson ratio, dL/dlog(E) is their sum).  Each is a sum over every iteration
- *     of terms that largely cancel, so it is accumulated in FP64; the terms are FP32.
- * All three are asynchronous on the handle's stream; the tape is overwritten by the next record
- * into the same slot.
+ *   pbgb_vbd_step_adjoint_state: reverses the substeps in slots slot + substeps - 1 down to slot.
+ *     xbar_dev, vbar_dev, vprevbar_dev (device, 3 x nV): on entry the adjoints dL/dx, dL/dv and
+ *     dL/dvprev of the state after the recorded step (vprev: the previous velocity the GPU
+ *     semantics keep for AdaptiveVbd), on return those of the state before it.  dlogmu_dev,
+ *     dloglambda_dev (device, nT, FP64): dL/dlog(mu), dL/dlog(lambda) of every tet, added to what
+ *     they hold (with a fixed Poisson ratio, dL/dlog(E) is their sum).  Each is a sum over every
+ *     iteration of terms that largely cancel, so it is accumulated in FP64; the terms are FP32.
+ *   pbgb_vbd_step_adjoint: the same with the previous velocity's adjoint taken as zero and not
+ *     returned; rejected for AdaptiveVbd with the GPU semantics, whose guess reads it.
+ *   pbgb_vbd_{get,set}_previous_velocities_device: the previous velocities (3 x nV, device), for
+ *     checkpoints of that state.
+ * All are asynchronous on the handle's stream; the tape is overwritten by the next record into
+ * the same slot.
  */
 PBGB_API int pbgb_vbd_adjoint_reserve(pbgb_vbd* h, int32_t slots, int32_t iterations);
 PBGB_API int pbgb_vbd_step_record(pbgb_vbd* h, float dt, int32_t iterations, int32_t substeps, int32_t slot);
@@ -367,6 +378,17 @@ PBGB_API int pbgb_vbd_step_adjoint(
     float* vbar_dev,
     double* dlogmu_dev,
     double* dloglambda_dev);
+PBGB_API int pbgb_vbd_step_adjoint_state(
+    pbgb_vbd* h,
+    int32_t slot,
+    int32_t substeps,
+    float* xbar_dev,
+    float* vbar_dev,
+    float* vprevbar_dev,
+    double* dlogmu_dev,
+    double* dloglambda_dev);
+PBGB_API int pbgb_vbd_get_previous_velocities_device(pbgb_vbd* h, float* vprev_dev);
+PBGB_API int pbgb_vbd_set_previous_velocities_device(pbgb_vbd* h, const float* vprev_dev);
 
 /*
  * Linear BVH over axis-aligned boxes (reference: gpu::geometry::Bvh, gpu/geometry/Bvh.cu, and its

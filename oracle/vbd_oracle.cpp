@@ -1123,46 +1123,68 @@ int orc_adjoint(
     orc_problem const* Pp,
     double const* x0,
     double const* v0,
+    double const* vprev0,
     double dt,
     int32_t iterations,
     int32_t substeps,
     int32_t nsteps,
     double* xbar,
     double* vbar,
+    double* vprevbar,
     double* dlogmu,
     double* dloglambda)
 {
     orc_problem const& P = *Pp;
-    if (P.acceleration != 0 || P.kD != 0.0 || P.strategy > 2 || substeps < 1 || iterations < 0 || nsteps < 0)
+    if ((P.acceleration != 0 && P.acceleration != 1) || P.strategy < 0 || P.strategy > 4 || substeps < 1 ||
+        iterations < 0 || nsteps < 0)
         return 2;
-    int32_t const nV = P.nV;
-    size_t const n3  = size_t(nV) * 3;
-    int32_t const N  = nsteps * substeps;
+    bool const cheb      = P.acceleration == 1;
+    bool const gpuSem    = P.semantics == 1;
+    int32_t const nV     = P.nV;
+    size_t const n3      = size_t(nV) * 3;
+    int32_t const N      = nsteps * substeps;
     Real const h = dt / Real(substeps), h2 = h * h;
+    Real const D = P.kD / h;
     int32_t const K = iterations;
+    // Chebyshev weights of the iterations (the same recurrence as the forward).
+    std::vector<Real> omega(size_t(std::max(K, 1)), 1);
+    {
+        Real om = 0;
+        for (int32_t k = 0; k < K; ++k)
+            omega[size_t(k)] = om = orc_chebyshev_omega(k, P.rho * P.rho, om, P.chebyshev_formula);
+    }
     // Colour of every vertex (-1: pinned, never solved).
     std::vector<int32_t> colour(size_t(nV), -1);
     for (int32_t p = 0; p < P.nPartitions; ++p)
         for (int32_t kk = P.Pptr[p]; kk < P.Pptr[p + 1]; ++kk)
             colour[P.Padj[kk]] = p;
-    // Forward: the state at the start of every substep.
-    std::vector<Real> xs(size_t(N + 1) * n3), vs(size_t(N + 1) * n3);
+    // Forward: the state at the start of every substep (positions, velocities, previous velocities).
+    std::vector<Real> xs(size_t(N + 1) * n3), vs(size_t(N + 1) * n3), ps(size_t(N + 1) * n3);
     std::copy(x0, x0 + n3, xs.begin());
     std::copy(v0, v0 + n3, vs.begin());
-    std::vector<Real> xt(n3), xtilde(n3), snaps(size_t(K + 1) * n3), hinv(size_t(K) * size_t(nV) * 9);
+    std::copy(vprev0, vprev0 + n3, ps.begin());
+    // Recorded substep: ys[k + 1] = y_k, the iterate after iteration k (ys[0] = the initial guess,
+    // y_{-1}); raws[k] = the raw sweep result of iteration k (equal to y_k without Chebyshev).
+    std::vector<Real> xt(n3), xtilde(n3), ys(size_t(K + 1) * n3), raws(size_t(std::max(K, 1)) * n3),
+        hinv(size_t(K) * size_t(nV) * 9);
     auto substep = [&](int32_t t, bool record) {
         Real const* xa = xs.data() + size_t(t) * n3;
         Real const* va = vs.data() + size_t(t) * n3;
-        std::vector<Real> x(xa, xa + n3);
+        Real const* pa = ps.data() + size_t(t) * n3;
+        std::vector<Real> x(xa, xa + n3), km1(n3), km2(n3);
         std::copy(xa, xa + n3, xt.begin());
         for (int32_t i = 0; i < nV; ++i)
         {
             for (int d = 0; d < 3; ++d)
                 xtilde[3 * i + d] = xt[3 * i + d] + h * va[3 * i + d] + h2 * P.aext[3 * i + d];
-            initial_positions(&xt[3 * size_t(i)], va + 3 * size_t(i), va + 3 * size_t(i), P.aext + 3 * size_t(i), h, h2, P.strategy, &x[3 * size_t(i)]);
+            Real const* vtm1 = (gpuSem ? pa : va) + 3 * size_t(i);
+            initial_positions(&xt[3 * size_t(i)], vtm1, va + 3 * size_t(i), P.aext + 3 * size_t(i), h, h2, P.strategy,
+                              &x[3 * size_t(i)]);
         }
         if (record)
-            std::copy(x.begin(), x.end(), snaps.begin());
+            std::copy(x.begin(), x.end(), ys.begin());
+        km1 = x;
+        km2 = x;
         for (int32_t k = 0; k < K; ++k)
         {
             for (int32_t p = 0; p < P.nPartitions; ++p)
@@ -1176,49 +1198,86 @@ int orc_adjoint(
                 }
             }
             if (record)
-                std::copy(x.begin(), x.end(), snaps.begin() + size_t(k + 1) * n3);
+                std::copy(x.begin(), x.end(), raws.begin() + size_t(k) * n3);
+            if (cheb)
+                for (size_t q = 0; q < n3; ++q)
+                {
+                    if (k > 1)
+                        x[q] = omega[size_t(k)] * (x[q] - km2[q]) + km2[q];
+                    km2[q] = km1[q];
+                    km1[q] = x[q];
+                }
+            if (record)
+                std::copy(x.begin(), x.end(), ys.begin() + size_t(k + 1) * n3);
         }
         if (!record)
         {
             Real* xn = xs.data() + size_t(t + 1) * n3;
             Real* vn = vs.data() + size_t(t + 1) * n3;
+            Real* pn = ps.data() + size_t(t + 1) * n3;
             for (size_t q = 0; q < n3; ++q)
             {
                 xn[q] = x[q];
                 vn[q] = (x[q] - xt[q]) / h;
+                pn[q] = va[q];
             }
         }
     };
     for (int32_t t = 0; t < N; ++t)
         substep(t, false);
     // Reverse.
-    std::vector<Real> ubar(n3), xtbar(n3);
+    std::vector<Real> ubar(n3), xtbar(n3), xsbar(n3), yp(n3), ypp(n3);
     Real const s1 = P.strategy == 0 ? Real(0) : Real(1);
     for (int32_t t = N - 1; t >= 0; --t)
     {
         substep(t, true);
+        Real const* va = vs.data() + size_t(t) * n3;
+        Real const* pa = ps.data() + size_t(t) * n3;
         for (size_t q = 0; q < n3; ++q)
         {
             ubar[q]  = xbar[q] + vbar[q] / h;
             xtbar[q] = 0;
+            xsbar[q] = 0;
+            yp[q]    = 0;
+            ypp[q]   = 0;
         }
-        for (int32_t k = K; k >= 1; --k)
+        for (int32_t k = K - 1; k >= 0; --k)
         {
-            Real const* Xk   = snaps.data() + size_t(k) * n3;
-            Real const* Xkm1 = snaps.data() + size_t(k - 1) * n3;
+            // Chebyshev: y_k = omega (raw_k - y_{k-2}) + y_{k-2} for k > 1.  ubar holds the
+            // adjoint of y_k once yp (earlier contributions to it) is added; it is split into the
+            // raw iterate's adjoint and a contribution to y_{k-2} (ypp, two iterations back).
+            if (cheb)
+            {
+                Real const c1 = k > 1 ? omega[size_t(k)] : Real(1), c2 = k > 1 ? 1 - omega[size_t(k)] : Real(0);
+                for (size_t q = 0; q < n3; ++q)
+                {
+                    Real const yc = yp[q] + ubar[q];
+                    ubar[q]       = c1 * yc;
+                    yp[q]         = ypp[q];
+                    ypp[q]        = c2 * yc;
+                }
+            }
+            Real const* Xk   = raws.data() + size_t(k) * n3; // lower colours: this iteration's results
+            Real const* Xkm1 = ys.data() + size_t(k) * n3;   // own and higher colours: y_{k-1}
             for (int32_t p = P.nPartitions - 1; p >= 0; --p)
             {
 #pragma omp parallel for schedule(dynamic, 32)
                 for (int32_t kk = P.Pptr[p]; kk < P.Pptr[p + 1]; ++kk)
                 {
                     int32_t const o = P.Padj[kk];
-                    Real const* Hi  = &hinv[(size_t(k - 1) * nV + o) * 9];
+                    Real const* Hi  = &hinv[(size_t(k) * nV + o) * 9];
                     Real w[3], delta[3];
+                    Real const u[3] = {ubar[3 * o], ubar[3 * o + 1], ubar[3 * o + 2]};
                     for (int r = 0; r < 3; ++r)
                     {
-                        w[r]     = Hi[r] * ubar[3 * o] + Hi[3 + r] * ubar[3 * o + 1] + Hi[6 + r] * ubar[3 * o + 2];
-                        delta[r] = Xkm1[3 * o + r] - Xk[3 * o + r];
+                        w[r] = Hi[r] * u[0] + Hi[3 + r] * u[1] + Hi[6 + r] * u[2];
+                        // Applied step delta = x_o - x_o' (zero when the step was skipped); with
+                        // damping the elastic part of the Newton system sees (1 + D) delta - D (x_o - xt_o).
+                        Real const dl = Xkm1[3 * o + r] - Xk[3 * o + r];
+                        delta[r]      = (1 + D) * dl - D * (Xkm1[3 * o + r] - xt[3 * o + r]);
                     }
+                    if (Hi[0] == 0 && Hi[4] == 0 && Hi[8] == 0)
+                        continue; // the Newton step was skipped: x_o' = x_o, nothing else depends on it
                     Real own[3] = {0, 0, 0};
                     for (int32_t n = P.GVGp[o]; n < P.GVGp[o + 1]; ++n)
                     {
@@ -1229,11 +1288,11 @@ int orc_adjoint(
                         Real F[9] = {0};
                         for (int a = 0; a < 4; ++a)
                         {
-                            int32_t const va = tv[a];
-                            Real const* src  = (a == il) ? Xkm1 : (colour[va] < p ? Xk : Xkm1);
+                            int32_t const va2 = tv[a];
+                            Real const* src   = (a == il) ? Xkm1 : (colour[va2] < p ? Xk : Xkm1);
                             for (int d = 0; d < 3; ++d)
                                 for (int r = 0; r < 3; ++r)
-                                    F[3 * d + r] += src[3 * va + r] * GPe[3 * a + d];
+                                    F[3 * d + r] += src[3 * va2 + r] * GPe[3 * a + d];
                         }
                         Real const mu = P.mu[e], la = P.lambda[e], wg = P.wg[e];
                         Real gF[9], HF[81];
@@ -1259,7 +1318,7 @@ int orc_adjoint(
                         Real Fi[9];
                         inv3(F, Fi);
                         // D_X = J (tr(F^-1 X) F^-T - (F^-1 X F^-1)^T)
-                        auto dJ2 = [&](Real const* Xm, Real* D) {
+                        auto dJ2 = [&](Real const* Xm, Real* Dm) {
                             Real FX[9] = {0}, FXF[9] = {0};
                             for (int c = 0; c < 3; ++c)
                                 for (int r = 0; r < 3; ++r)
@@ -1272,7 +1331,7 @@ int orc_adjoint(
                             Real const tr = FX[0] + FX[4] + FX[8];
                             for (int c = 0; c < 3; ++c)
                                 for (int r = 0; r < 3; ++r)
-                                    D[3 * c + r] = J * (tr * Fi[3 * r + c] - FXF[3 * r + c]);
+                                    Dm[3 * c + r] = J * (tr * Fi[3 * r + c] - FXF[3 * r + c]);
                         };
                         Real DA[9], DB[9];
                         dJ2(A, DA);
@@ -1304,28 +1363,80 @@ int orc_adjoint(
                                     own[r] += gphi[r];
                                 continue;
                             }
-                            int32_t const va = tv[a];
+                            int32_t const va2 = tv[a];
                             for (int r = 0; r < 3; ++r)
                             {
 #pragma omp atomic
-                                ubar[3 * va + r] -= gphi[r];
+                                ubar[3 * va2 + r] -= gphi[r];
                             }
                         }
                     }
+                    // Inertia K w (K = m/h^2); damping D H_e w with H_e w = (u - K w) / (1 + D)
+                    // (H w = u for the full Newton matrix (1 + D) H_e + K I).
                     Real const Km = P.m[o] / h2;
                     for (int r = 0; r < 3; ++r)
                     {
-                        ubar[3 * o + r] -= Km * w[r] + own[r];
+                        Real const dHw = D * (u[r] - Km * w[r]) / (1 + D);
+                        ubar[3 * o + r] -= Km * w[r] + dHw + own[r];
                         xtbar[3 * o + r] += Km * w[r];
+                        xsbar[3 * o + r] += dHw;
                     }
                 }
             }
         }
-        for (size_t q = 0; q < n3; ++q)
+        if (cheb)
+            for (size_t q = 0; q < n3; ++q)
+                ubar[q] += yp[q];
+        // The initial guess x0 = xt + s1 h v + h^2 a_t(v, vtm1) a and xtilde = xt + h v + h^2 a;
+        // v_end = (x_end - xt) / h; with GPU semantics the substep also passes v on as the next
+        // vtm1 (vprev_end = v).
+        for (int32_t i = 0; i < nV; ++i)
         {
-            Real const vb = vbar[q];
-            xbar[q]       = -vb / h + ubar[q] + xtbar[q];
-            vbar[q]       = s1 * h * ubar[q] + h * xtbar[q];
+            Real const* vv = va + 3 * size_t(i);
+            Real const* a  = P.aext + 3 * size_t(i);
+            Real const* vm = (gpuSem ? pa : va) + 3 * size_t(i);
+            Real const an2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+            Real dAv[3] = {0, 0, 0}, dAvm[3] = {0, 0, 0}; // d a_t / d v, d a_t / d vtm1
+            if (an2 != 0 && P.strategy == 3 && gpuSem)
+            {
+                Real dd = 0;
+                for (int d = 0; d < 3; ++d)
+                    dd += ((vv[d] - vm[d]) / h) * a[d];
+                Real const s = dd / an2;
+                if (s > 0 && s < 1)
+                    for (int d = 0; d < 3; ++d)
+                    {
+                        dAv[d]  = a[d] / (h * an2);
+                        dAvm[d] = -a[d] / (h * an2);
+                    }
+            }
+            else if (an2 != 0 && P.strategy == 4)
+            {
+                Real const nv = std::sqrt(vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+                Real const vn = nv + std::numeric_limits<Real>::min();
+                Real va2 = 0;
+                for (int d = 0; d < 3; ++d)
+                    va2 += vv[d] * a[d];
+                Real const s = va2 / (vn * an2);
+                if (nv > 0 && std::abs(s) < 1)
+                {
+                    Real const sg = s > 0 ? Real(1) : (s < 0 ? Real(-1) : Real(0));
+                    for (int d = 0; d < 3; ++d)
+                        dAv[d] = sg * (a[d] / vn - va2 * vv[d] / (vn * vn * nv)) / an2;
+                }
+            }
+            Real au = 0;
+            for (int d = 0; d < 3; ++d)
+                au += a[d] * ubar[3 * size_t(i) + d];
+            for (int d = 0; d < 3; ++d)
+            {
+                size_t const q = 3 * size_t(i) + d;
+                Real const vb  = vbar[q];
+                Real const pb  = vprevbar[q];
+                xbar[q]        = -vb / h + ubar[q] + xtbar[q] + xsbar[q];
+                vbar[q]        = s1 * h * ubar[q] + h * xtbar[q] + h2 * au * dAv[d] + (gpuSem ? pb : Real(0));
+                vprevbar[q]    = h2 * au * dAvm[d];
+            }
         }
     }
     return 0;

@@ -111,6 +111,9 @@ _SIGNATURES = [
     ("pbgb_vbd_adjoint_reserve", C.c_int, [_vp, _i32, _i32]),
     ("pbgb_vbd_step_record", C.c_int, [_vp, _f32, _i32, _i32, _i32]),
     ("pbgb_vbd_step_adjoint", C.c_int, [_vp, _i32, _i32, _vp, _vp, _vp, _vp]),
+    ("pbgb_vbd_step_adjoint_state", C.c_int, [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp]),
+    ("pbgb_vbd_get_previous_velocities_device", C.c_int, [_vp, _vp]),
+    ("pbgb_vbd_set_previous_velocities_device", C.c_int, [_vp, _vp]),
     ("pbgb_vbd_set_detH_zero", C.c_int, [_vp, _f32]),
     ("pbgb_vbd_set_damping", C.c_int, [_vp, _f32]),
     ("pbgb_vbd_set_strategy", C.c_int, [_vp, _i32]),

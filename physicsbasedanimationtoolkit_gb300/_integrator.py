@@ -254,11 +254,13 @@ class IntegratorBase:
     # Device-pointer state access (|#vertices| x 3 float32 on the handle's device).  Stream-ordered
     # on the handle's stream: callers order their own work around them (synchronize()).
     def _get_device(self, which, ptr):
-        fn = {"x": "pbgb_vbd_get_positions_device", "v": "pbgb_vbd_get_velocities_device"}[which]
+        fn = {"x": "pbgb_vbd_get_positions_device", "v": "pbgb_vbd_get_velocities_device",
+              "vprev": "pbgb_vbd_get_previous_velocities_device"}[which]
         _capi.check(getattr(_capi.lib(), fn)(self._h, C.c_void_p(ptr)), self._h)
 
     def _set_device(self, which, ptr):
-        fn = {"x": "pbgb_vbd_set_positions_device", "v": "pbgb_vbd_set_velocities_device"}[which]
+        fn = {"x": "pbgb_vbd_set_positions_device", "v": "pbgb_vbd_set_velocities_device",
+              "vprev": "pbgb_vbd_set_previous_velocities_device"}[which]
         _capi.check(getattr(_capi.lib(), fn)(self._h, C.c_void_p(ptr)), self._h)
 
     def adjoint_reserve(self, slots, iterations):
@@ -268,10 +270,18 @@ class IntegratorBase:
         _capi.check(_capi.lib().pbgb_vbd_step_record(self._h, float(dt), int(iterations), int(substeps), int(slot)),
                     self._h)
 
-    def step_adjoint(self, slot, substeps, xbar_ptr, vbar_ptr, dlogmu_ptr, dloglambda_ptr):
-        _capi.check(_capi.lib().pbgb_vbd_step_adjoint(self._h, int(slot), int(substeps), C.c_void_p(xbar_ptr),
-                                                     C.c_void_p(vbar_ptr), C.c_void_p(dlogmu_ptr),
-                                                     C.c_void_p(dloglambda_ptr)), self._h)
+    def step_adjoint(self, slot, substeps, xbar_ptr, vbar_ptr, dlogmu_ptr, dloglambda_ptr, vprevbar_ptr=None):
+        """Reverses recorded substeps (device pointers); with ``vprevbar_ptr`` the adjoint of the
+        previous velocities is carried too (pbgb_vbd_step_adjoint_state)."""
+        L = _capi.lib()
+        if vprevbar_ptr is None:
+            rc = L.pbgb_vbd_step_adjoint(self._h, int(slot), int(substeps), C.c_void_p(xbar_ptr), C.c_void_p(vbar_ptr),
+                                         C.c_void_p(dlogmu_ptr), C.c_void_p(dloglambda_ptr))
+        else:
+            rc = L.pbgb_vbd_step_adjoint_state(self._h, int(slot), int(substeps), C.c_void_p(xbar_ptr),
+                                               C.c_void_p(vbar_ptr), C.c_void_p(vprevbar_ptr), C.c_void_p(dlogmu_ptr),
+                                               C.c_void_p(dloglambda_ptr))
+        _capi.check(rc, self._h)
 
     def trust_region_log(self):
         """Trust-region decisions of the last step: an (entries, 4) array, one row per (substep,

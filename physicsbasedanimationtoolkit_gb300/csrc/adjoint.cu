@@ -1,6 +1,8 @@
 // Adjoint sweep kernels (see adjoint.cuh).
 #include "adjoint.cuh"
 
+#include <cfloat>
+
 namespace pbgb {
 
 namespace {
@@ -58,7 +60,7 @@ __global__ void __launch_bounds__(256) adjoint_sweep_kernel(AdjointSweepParams p
     int i = 0, k = 0, k1 = 0;
     float4 pre = make_float4(0.f, 0.f, 0.f, 0.f), pst = pre, Xo = pre, r0 = pre, r1 = pre;
     AdjointIncidence a;
-    bool has = false;
+    bool has = false, skipped = true;
     if (valid)
     {
         i   = p.solve[s];
@@ -82,7 +84,19 @@ __global__ void __launch_bounds__(256) adjoint_sweep_kernel(AdjointSweepParams p
         w[0] = r0.x * u.x + r0.y * u.y + r0.z * u.z;
         w[1] = r0.y * u.x + r0.w * u.y + r1.x * u.z;
         w[2] = r0.z * u.x + r1.x * u.y + r1.y * u.z;
-        float const delta[3] = {pre.x - pst.x, pre.y - pst.y, pre.z - pst.z};
+        // The step was skipped (singular Newton matrix, tape entry zero): x_o' = x_o, and nothing
+        // else of the update depends on its inputs.
+        skipped = r0.x == 0.f && r0.w == 0.f && r1.y == 0.f;
+        float delta[3] = {pre.x - pst.x, pre.y - pst.y, pre.z - pst.z};
+        if (p.D != 0.f)
+        {
+            float4 const xs = p.xs[i];
+            delta[0]        = (1.f + p.D) * delta[0] - p.D * (pre.x - xs.x);
+            delta[1]        = (1.f + p.D) * delta[1] - p.D * (pre.y - xs.y);
+            delta[2]        = (1.f + p.D) * delta[2] - p.D * (pre.z - xs.z);
+        }
+        if (skipped)
+            has = false;
         while (has)
         {
             float G[3][3];
@@ -111,41 +125,92 @@ __global__ void __launch_bounds__(256) adjoint_sweep_kernel(AdjointSweepParams p
 #pragma unroll
         for (int r = 0; r < 3; ++r)
             own[r] += __shfl_xor_sync(0xffffffffu, own[r], off);
-    if (!valid || lane != 0)
+    if (!valid || lane != 0 || skipped)
         return;
-    // d(phi)/dx_o = K w - sum_e (own contributions) with K = m/h^2 from the inertia term.
+    // d(phi)/dx_o = K w + D H_e w - sum_e (own contributions) with K = m/h^2 from the inertia term
+    // and H_e w = (u - K w)/(1 + D) from the damping term.
     float const K  = p.m[i] / p.h2;
     float4 const u = p.ubar[i];
-    p.ubar[i]      = make_float4(u.x - K * w[0] + own[0], u.y - K * w[1] + own[1], u.z - K * w[2] + own[2], 0.f);
+    float dHw[3]   = {0.f, 0.f, 0.f};
+    if (p.D != 0.f)
+    {
+        float const s = p.D / (1.f + p.D);
+        dHw[0]        = s * (u.x - K * w[0]);
+        dHw[1]        = s * (u.y - K * w[1]);
+        dHw[2]        = s * (u.z - K * w[2]);
+        float4 const q = p.xsbar[i];
+        p.xsbar[i]     = make_float4(q.x + dHw[0], q.y + dHw[1], q.z + dHw[2], 0.f);
+    }
+    p.ubar[i] = make_float4(u.x - K * w[0] - dHw[0] + own[0], u.y - K * w[1] - dHw[1] + own[1],
+                            u.z - K * w[2] - dHw[2] + own[2], 0.f);
     float4 const t = p.xtbar[i];
     p.xtbar[i]     = make_float4(t.x + K * w[0], t.y + K * w[1], t.z + K * w[2], 0.f);
 }
 
-__global__ void adjoint_begin_kernel(int32_t n, float const* __restrict__ xbar, float const* __restrict__ vbar, float4* __restrict__ ubar, float4* __restrict__ xtbar, float invh)
+__global__ void adjoint_begin_kernel(int32_t n, float const* __restrict__ xbar, float const* __restrict__ vbar, float4* __restrict__ ubar,
+                                     float4* __restrict__ xtbar, float4* __restrict__ xsbar, float4* __restrict__ yp,
+                                     float4* __restrict__ ypp, float invh)
 {
     int const i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     ubar[i] = make_float4(xbar[3 * i] + invh * vbar[3 * i], xbar[3 * i + 1] + invh * vbar[3 * i + 1],
                           xbar[3 * i + 2] + invh * vbar[3 * i + 2], 0.f);
-    xtbar[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 const z = make_float4(0.f, 0.f, 0.f, 0.f);
+    xtbar[i]       = z;
+    xsbar[i]       = z;
+    if (yp)
+    {
+        yp[i]  = z;
+        ypp[i] = z;
+    }
 }
 
-__global__ void adjoint_end_kernel(int32_t n, float* __restrict__ xbar, float* __restrict__ vbar, float4 const* __restrict__ ubar, float4 const* __restrict__ xtbar, float h, float s1)
+__global__ void adjoint_cheb_mix_kernel(int32_t n, float4* __restrict__ ubar, float4* __restrict__ yp, float4* __restrict__ ypp, float c1, float c2)
 {
     int const i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
-    float const invh = 1.f / h;
-    float4 const u   = ubar[i];
-    float4 const t   = xtbar[i];
+    float4 const u = ubar[i], a = yp[i], b = ypp[i];
+    float4 const y = make_float4(a.x + u.x, a.y + u.y, a.z + u.z, 0.f);
+    ubar[i]        = make_float4(c1 * y.x, c1 * y.y, c1 * y.z, 0.f);
+    yp[i]          = b;
+    ypp[i]         = make_float4(c2 * y.x, c2 * y.y, c2 * y.z, 0.f);
+}
+
+__global__ void adjoint_end_kernel(int32_t n, float* __restrict__ xbar, float* __restrict__ vbar, float* __restrict__ pbar,
+                                   float4 const* __restrict__ ubar, float4 const* __restrict__ xtbar,
+                                   float4 const* __restrict__ xsbar, float4 const* __restrict__ v0,
+                                   float4 const* __restrict__ p0, float4 const* __restrict__ a0, float h,
+                                   int32_t strategy, int32_t gpuSemantics)
+{
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    float const invh  = 1.f / h;
+    float const s1    = strategy == 0 ? 0.f : 1.f;
+    float4 const u    = ubar[i];
+    float4 const t    = xtbar[i];
+    float4 const q    = xsbar[i];
+    float4 const v4   = v0[i];
+    float4 const a4   = a0[i];
+    float4 const m4   = gpuSemantics ? p0[i] : v4;
     float const uu[3] = {u.x, u.y, u.z};
     float const tt[3] = {t.x, t.y, t.z};
+    float const qq[3] = {q.x, q.y, q.z};
+    float const vt[3] = {v4.x, v4.y, v4.z};
+    float const vm[3] = {m4.x, m4.y, m4.z};
+    float const a[3]  = {a4.x, a4.y, a4.z};
+    float dAv[3], dAvm[3];
+    initial_position_factor_derivatives(vm, vt, a, h, strategy, FLT_MIN, dAv, dAvm);
+    float const au = a[0] * uu[0] + a[1] * uu[1] + a[2] * uu[2];
     for (int r = 0; r < 3; ++r)
     {
-        float const vb   = vbar[3 * i + r];
-        xbar[3 * i + r]  = -invh * vb + uu[r] + tt[r];
-        vbar[3 * i + r]  = s1 * h * uu[r] + h * tt[r];
+        float const vb  = vbar[3 * i + r];
+        float const pb  = pbar[3 * i + r];
+        xbar[3 * i + r] = -invh * vb + uu[r] + tt[r] + qq[r];
+        vbar[3 * i + r] = s1 * h * uu[r] + h * tt[r] + h * h * au * dAv[r] + (gpuSemantics ? pb : 0.f);
+        pbar[3 * i + r] = h * h * au * dAvm[r];
     }
 }
 
@@ -190,19 +255,33 @@ cudaError_t launch_adjoint_sweep(AdjointSweepParams const& p, int lanes, int blo
     }
 }
 
-cudaError_t launch_adjoint_begin(int32_t n, float const* xbar, float const* vbar, float4* ubar, float4* xtbar, float h, cudaStream_t s)
+cudaError_t launch_adjoint_begin(int32_t n, float const* xbar, float const* vbar, float4* ubar, float4* xtbar, float4* xsbar,
+                                 float4* yp, float4* ypp, float h, cudaStream_t s)
 {
     if (n <= 0)
         return cudaSuccess;
-    adjoint_begin_kernel<<<blocks_of(n, 256), 256, 0, s>>>(n, xbar, vbar, ubar, xtbar, 1.f / h);
+    if ((yp == nullptr) != (ypp == nullptr))
+        return cudaErrorInvalidValue;
+    adjoint_begin_kernel<<<blocks_of(n, 256), 256, 0, s>>>(n, xbar, vbar, ubar, xtbar, xsbar, yp, ypp, 1.f / h);
     return cudaGetLastError();
 }
 
-cudaError_t launch_adjoint_end(int32_t n, float* xbar, float* vbar, float4 const* ubar, float4 const* xtbar, float h, float s1, cudaStream_t s)
+cudaError_t launch_adjoint_cheb_mix(int32_t n, float4* ubar, float4* yp, float4* ypp, float c1, float c2, cudaStream_t s)
 {
     if (n <= 0)
         return cudaSuccess;
-    adjoint_end_kernel<<<blocks_of(n, 256), 256, 0, s>>>(n, xbar, vbar, ubar, xtbar, h, s1);
+    adjoint_cheb_mix_kernel<<<blocks_of(n, 256), 256, 0, s>>>(n, ubar, yp, ypp, c1, c2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_end(int32_t n, float* xbar, float* vbar, float* pbar, float4 const* ubar, float4 const* xtbar,
+                               float4 const* xsbar, float4 const* v0, float4 const* p0, float4 const* a, float h,
+                               int32_t strategy, int32_t gpuSemantics, cudaStream_t s)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    adjoint_end_kernel<<<blocks_of(n, 256), 256, 0, s>>>(n, xbar, vbar, pbar, ubar, xtbar, xsbar, v0, p0, a, h, strategy,
+                                                         gpuSemantics);
     return cudaGetLastError();
 }
 

@@ -10,8 +10,16 @@
 // saw before its update is rebuilt from the tape by the colour rank bits of the tet record: a
 // corner of lower rank from X_k, one of higher rank (and o itself) from X_{k-1}.
 //
-// Supported forward settings: no acceleration, no damping, no contact, initial guess Position,
-// Inertia or KineticEnergyMinimum (the others depend on the previous velocity through clamps).
+// Rayleigh damping (D = kD / h) makes the Newton matrix (1 + D) H_e + K I and adds D H_e (x_o - xt_o)
+// to the gradient, so the tet terms use delta' = (1 + D) delta - D (x_o - xt_o), the own vertex
+// loses D H_e w = D (u - K w) / (1 + D) more, and xt_o gains it.  Chebyshev (y_k = omega (raw_k -
+// y_{k-2}) + y_{k-2}) is reversed by splitting each iterate's adjoint between its raw sweep result
+// and the iterate two back (launch_adjoint_cheb_mix), the reversed sweep reading raw_k for lower
+// colours and y_{k-1} for its own and higher colours.  The initial guess enters through
+// launch_adjoint_end, including the derivative of the adaptive guesses' acceleration factor on the
+// branch the forward took.
+//
+// Not supported: contact, Anderson, Nesterov, Broyden and trust-region acceleration.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -38,6 +46,11 @@ struct AdjointSweepParams
     // cancel (about 4 x iterations x steps of them), which FP32 accumulation does not resolve.
     double* __restrict__ dlogmu;
     double* __restrict__ dloglambda;
+    // Damping: D = kD / h (0: none), xs = the substep's start positions, xsbar = their adjoint
+    // through the damping term (accumulated).
+    float4 const* __restrict__ xs;
+    float4* __restrict__ xsbar;
+    float D;
     int32_t begin;
     int32_t end;
     float h2;
@@ -46,14 +59,26 @@ struct AdjointSweepParams
 // pdl: programmatic dependent launch (the kernel waits before reading the adjoints).
 cudaError_t launch_adjoint_sweep(AdjointSweepParams const& p, int lanes, int block, bool pdl, cudaStream_t s);
 
-// Start of a reversed substep: ubar = xbar + vbar / h (v = (x - xt)/h), xtbar = 0.
-//   xbar, vbar: n x 3 adjoints of the substep's end positions and velocities.
-cudaError_t launch_adjoint_begin(int32_t n, float const* xbar, float const* vbar, float4* ubar, float4* xtbar, float h, cudaStream_t s);
+// Start of a reversed substep: ubar = xbar + vbar / h (v = (x - xt)/h), xtbar = xsbar = 0, and the
+// Chebyshev carries yp = ypp = 0 (nullable).
+cudaError_t launch_adjoint_begin(int32_t n, float const* xbar, float const* vbar, float4* ubar, float4* xtbar, float4* xsbar,
+                                 float4* yp, float4* ypp, float h, cudaStream_t s);
 
-// End of a reversed substep: the adjoints of the substep's start positions and velocities, in
-// place of xbar and vbar.  With xtilde = xt + h v + h^2 a and the initial guess
-// x0 = xt + s1 h v + s2 h^2 a (s1 = 0 for Position, 1 otherwise):
-//   xbar <- -vbar / h + ubar + xtbar,   vbar <- s1 h ubar + h xtbar.
-cudaError_t launch_adjoint_end(int32_t n, float* xbar, float* vbar, float4 const* ubar, float4 const* xtbar, float h, float s1, cudaStream_t s);
+// Before reversing Chebyshev iteration k: y = yp + ubar (the complete adjoint of y_k), ubar = c1 y
+// (raw_k's), yp = ypp (y_{k-1}'s so far), ypp = c2 y (y_{k-2}'s); c1 = omega_k, c2 = 1 - omega_k for
+// k > 1, else 1 and 0.
+cudaError_t launch_adjoint_cheb_mix(int32_t n, float4* ubar, float4* yp, float4* ypp, float c1, float c2, cudaStream_t s);
+
+// End of a reversed substep: the adjoints of the substep's start positions, velocities and
+// previous velocities, in place of xbar, vbar and pbar (n x 3 each).  With xtilde = xt + h v + h^2 a,
+// the initial guess x0 = xt + s1 h v + h^2 a_t(v, vtm1) a (vtm1: the previous velocity with GPU
+// semantics, v otherwise) and the next previous velocity = v (GPU semantics):
+//   xbar <- -vbar/h + ubar + xtbar + xsbar
+//   vbar <- s1 h ubar + h xtbar + h^2 (a . ubar) da_t/dv + [GPU] pbar
+//   pbar <- h^2 (a . ubar) da_t/dvtm1
+// v0, p0, a: the substep's start velocities, previous velocities and external accelerations.
+cudaError_t launch_adjoint_end(int32_t n, float* xbar, float* vbar, float* pbar, float4 const* ubar, float4 const* xtbar,
+                               float4 const* xsbar, float4 const* v0, float4 const* p0, float4 const* a, float h,
+                               int32_t strategy, int32_t gpuSemantics, cudaStream_t s);
 
 } // namespace pbgb

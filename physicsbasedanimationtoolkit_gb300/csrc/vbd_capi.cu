@@ -309,9 +309,14 @@ class VbdSystem
     std::vector<float> slotH;
     std::vector<int32_t> slotStrategy;
     DeviceArray<float4> tapeX, tapeH, ubar, xtbar;
+    // Per slot: the substep's start positions, velocities and previous velocities (3 nV float4),
+    // and with Chebyshev the raw sweep result of every iteration (K nV float4).  Reversal buffers:
+    // the damping term's adjoint of the start positions and the Chebyshev carries.
+    DeviceArray<float4> tapeS, tapeRaw, xsbar, ycarry, ycarry2;
+    std::vector<float> slotKD;
     // Reversed steps run on these (the caller's arrays are copied in and out), so that their graphs
     // do not depend on the caller's pointers.
-    DeviceArray<float> adjX, adjV;
+    DeviceArray<float> adjX, adjV, adjP, adjZero;
     DeviceArray<double> adjMu, adjLa;
 
     // Batch layout: mesh b's vertices are [meshV0[b], meshV0[b+1]); its free vertices of colour c
@@ -319,11 +324,11 @@ class VbdSystem
     // meshes in order).
     int32_t nMeshes = 1;
     std::vector<int32_t> meshV0;
-    // Positions of a batch are stored relative to their mesh's origin (the centre of its rest box,
-    // rounded to FP32), so that FP32 differences of nearby positions keep their precision however
-    // far from the world origin a mesh lies; the position entry points add and subtract it.
-    // Single meshes (and contact, which needs world coordinates for its boxes and Morton codes)
-    // use the world frame: origin is empty then.
+    // Positions are stored relative to their mesh's origin (the centre of its rest box, rounded to
+    // FP32), so that FP32 differences of nearby positions keep their precision however far from the
+    // world origin a mesh lies; the position entry points add and subtract it.  A mesh with contact
+    // uses the world frame (its boxes, Morton codes and scene box are world quantities): origin is
+    // empty then.
     std::vector<float4> meshOrigin;
     DeviceArray<float4> origin;
     std::vector<std::vector<int32_t>> meshSolve;
@@ -377,6 +382,7 @@ class VbdSystem
         int32_t iters = -1, sub = -1;
         std::vector<float> h; // reversed steps: the step size of every covered slot
         std::vector<int32_t> strategy;
+        std::vector<float> kd;
     };
     std::vector<SlotGraph> recGraphs, adjGraphs;
 
@@ -539,7 +545,8 @@ class VbdSystem
             }
         }
         meshOrigin.assign(size_t(nMeshes), make_float4(0.f, 0.f, 0.f, 0.f));
-        if (nMeshes > 1)
+        bool const useOrigins = !(nMeshes == 1 && d0.n_collision_triangles > 0);
+        if (useOrigins)
             for (int32_t b = 0; b < nMeshes; ++b)
             {
                 auto const& d = descs[b];
@@ -793,7 +800,7 @@ class VbdSystem
         tets.upload(hrec.data(), nT, stream);
         X.upload(hX.data(), nV, stream);
         std::vector<float4> hOrigin;
-        if (nMeshes > 1)
+        if (useOrigins)
         {
             hOrigin.resize(size_t(nV));
             for (int32_t b = 0; b < nMeshes; ++b)
@@ -1001,15 +1008,28 @@ class VbdSystem
         dropSlotGraphs();
         adjX.allocate(size_t(nV) * 3);
         adjV.allocate(size_t(nV) * 3);
+        adjP.allocate(size_t(nV) * 3);
+        adjZero.allocate(size_t(nV) * 3);
         adjMu.allocate(size_t(nT));
         adjLa.allocate(size_t(nT));
         tapeX.allocate(size_t(slots) * size_t(iterations + 1) * size_t(nV));
         tapeH.allocate(size_t(slots) * size_t(iterations) * size_t(nFree) * 2);
+        tapeS.allocate(size_t(slots) * 3 * size_t(nV));
+        if (acceleration == PBGB_ACCEL_CHEBYSHEV)
+        {
+            tapeRaw.allocate(size_t(slots) * size_t(iterations) * size_t(nV));
+            ycarry.allocate(size_t(nV));
+            ycarry2.allocate(size_t(nV));
+        }
         ubar.allocate(size_t(nV));
         xtbar.allocate(size_t(nV));
+        xsbar.allocate(size_t(nV));
+        if (nV > 0)
+            check(cudaMemsetAsync(adjZero.get(), 0, sizeof(float) * 3 * size_t(nV), stream), "memset");
         tapeSlots = slots;
         tapeIters = iterations;
         slotH.assign(size_t(slots), 0.f);
+        slotKD.assign(size_t(slots), 0.f);
         slotStrategy.assign(size_t(slots), -1);
     }
 
@@ -1017,12 +1037,8 @@ class VbdSystem
     {
         if (contact)
             throw std::invalid_argument("the adjoint does not support contact");
-        if (acceleration != PBGB_ACCEL_NONE)
-            throw std::invalid_argument("the adjoint does not support acceleration strategies");
-        if (kD != 0.f)
-            throw std::invalid_argument("the adjoint does not support damping (kD != 0)");
-        if (strategy > PBGB_INIT_KINETIC_ENERGY_MINIMUM)
-            throw std::invalid_argument("the adjoint supports the Position, Inertia and KineticEnergyMinimum initial guesses");
+        if (acceleration != PBGB_ACCEL_NONE && acceleration != PBGB_ACCEL_CHEBYSHEV)
+            throw std::invalid_argument("the adjoint supports plain VBD and Chebyshev acceleration only");
     }
 
     float4* slotX(int32_t slot, int32_t k) const
@@ -1032,6 +1048,18 @@ class VbdSystem
     float4* slotTape(int32_t slot, int32_t k) const
     {
         return tapeH.get() + (size_t(slot) * size_t(tapeIters) + size_t(k)) * size_t(nFree) * 2;
+    }
+    // q = 0: start positions, 1: start velocities, 2: start previous velocities.
+    float4* slotStart(int32_t slot, int32_t q) const
+    {
+        return tapeS.get() + (size_t(slot) * 3 + size_t(q)) * size_t(nV);
+    }
+    // Raw sweep result of iteration k (Chebyshev); without acceleration it is the iterate itself.
+    float4* slotRaw(int32_t slot, int32_t k) const
+    {
+        if (acceleration != PBGB_ACCEL_CHEBYSHEV)
+            return slotX(slot, k + 1);
+        return tapeRaw.get() + (size_t(slot) * size_t(tapeIters) + size_t(k)) * size_t(nV);
     }
 
     // One step like step(), with every substep recorded into slots slot0, slot0 + 1, ...  Launched
@@ -1045,30 +1073,38 @@ class VbdSystem
         if (recGraphs.size() < size_t(tapeSlots))
             recGraphs.resize(size_t(tapeSlots));
         SlotGraph& g = recGraphs[slot0];
-        if (!g.exec || g.dt != dt || g.iters != iterations || g.sub != substeps)
+        if (!g.exec || g.dt != dt || g.iters != iterations || g.sub != substeps || g.kd != std::vector<float>{kD} ||
+            g.strategy != std::vector<int32_t>{strategy})
         {
             if (g.exec)
                 cudaGraphExecDestroy(g.exec);
-            g.exec  = nullptr;
-            g.exec  = capture([&] { enqueueRecord(dt, iterations, substeps, slot0); });
-            g.dt    = dt;
-            g.iters = iterations;
-            g.sub   = substeps;
+            g.exec     = nullptr;
+            g.exec     = capture([&] { enqueueRecord(dt, iterations, substeps, slot0); });
+            g.dt       = dt;
+            g.iters    = iterations;
+            g.sub      = substeps;
+            g.kd       = {kD};
+            g.strategy = {strategy};
         }
         check(cudaGraphLaunch(g.exec, stream), "cudaGraphLaunch");
         float const h = dt / float(substeps);
         for (int32_t s = 0; s < substeps; ++s)
         {
             slotH[slot0 + s]        = h;
+            slotKD[slot0 + s]       = kD;
             slotStrategy[slot0 + s] = strategy;
         }
     }
 
     void enqueueRecord(float dt, int32_t iterations, int32_t substeps, int32_t slot0)
     {
-        float const h   = dt / float(substeps);
+        float const h    = dt / float(substeps);
+        bool const cheb  = acceleration == PBGB_ACCEL_CHEBYSHEV;
         SubstepParams sp = substepParams(h);
-        sp.h0 = sp.h1 = nullptr;
+        if (!cheb)
+            sp.h0 = sp.h1 = nullptr;
+        else if (iterations > 0)
+            sp.result = ((iterations - 1) % 2 == 0) ? h0.get() : h1.get();
         SweepParams w{};
         w.x        = x.get();
         w.xt       = xt.get();
@@ -1087,40 +1123,64 @@ class VbdSystem
         w.omega    = 1.f;
         int const L = lanesToUse();
         size_t const bytes = sizeof(float4) * size_t(nV);
+        float4* H[2] = {h0.get(), h1.get()};
+        auto copy = [&](float4* dst, float4 const* src) {
+            if (nV > 0)
+                check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, stream), "tape copy");
+        };
         for (int32_t s = 0; s < substeps; ++s)
         {
             int32_t const slot = slot0 + s;
+            copy(slotStart(slot, 0), x.get());
+            copy(slotStart(slot, 1), v.get());
+            copy(slotStart(slot, 2), vprev.get());
             check(launch_begin_substep(sp, stream), "begin_substep");
-            if (nV > 0)
-                check(cudaMemcpyAsync(slotX(slot, 0), x.get(), bytes, cudaMemcpyDeviceToDevice, stream), "tape copy");
+            copy(slotX(slot, 0), x.get());
+            double omega      = 0.0;
+            double const rho2 = rho * rho;
             for (int32_t k = 0; k < iterations; ++k)
             {
                 w.tape = slotTape(slot, k);
+                if (cheb)
+                {
+                    omega   = chebyshev_omega<double>(k, rho2, omega, chebFormula);
+                    w.omega = float(omega);
+                    w.k     = k;
+                    w.hprev = H[(k + 1) % 2];
+                    w.hcur  = H[k % 2];
+                }
                 for (int32_t c = 0; c < nColors; ++c)
                 {
                     w.begin = colorPtr[c];
                     w.end   = colorPtr[c + 1];
                     w.color = c;
-                    // The first colour follows the copy of x into the tape (not a kernel): no programmatic
-                    // launch there, so that it cannot overwrite x while the copy reads it.
-                    check(launch_sweep_record(w, L, block, pdl && c > 0, stream, stagedBytes(c, L)), "sweep_record");
+                    // The first colour follows a copy into the tape (not a kernel): no programmatic
+                    // launch there, so that it cannot overwrite what the copy reads.
+                    check(launch_sweep_record(w, L, block, cheb, pdl && c > 0, stream, stagedBytes(c, L)), "sweep_record");
                 }
-                if (nV > 0)
-                    check(cudaMemcpyAsync(slotX(slot, k + 1), x.get(), bytes, cudaMemcpyDeviceToDevice, stream), "tape copy");
+                if (cheb)
+                {
+                    copy(slotRaw(slot, k), x.get());
+                    copy(slotX(slot, k + 1), H[k % 2]);
+                }
+                else
+                    copy(slotX(slot, k + 1), x.get());
             }
             check(launch_end_substep(sp, stream), "end_substep");
         }
     }
 
-    // Reverses the substeps recorded in slots slot0 + substeps - 1, ..., slot0.  xbar, vbar
-    // (device, nV x 3): adjoints of the positions and velocities after the last substep on entry,
-    // before the first on return.  dlogmu, dloglambda (device, nT, FP64): accumulated.
-    void adjointStep(int32_t slot0, int32_t substeps, float* xbar, float* vbar, double* dlogmu, double* dloglambda)
+    // Reverses the substeps recorded in slots slot0 + substeps - 1, ..., slot0.  xbar, vbar, pbar
+    // (device, nV x 3): adjoints of the positions, velocities and previous velocities after the
+    // last substep on entry, before the first on return.  dlogmu, dloglambda (device, nT, FP64):
+    // accumulated.
+    void adjointStep(int32_t slot0, int32_t substeps, float* xbar, float* vbar, float* pbar, double* dlogmu, double* dloglambda)
     {
         checkDifferentiable();
         if (slot0 < 0 || substeps < 1 || int64_t(slot0) + substeps > tapeSlots)
             throw std::invalid_argument("pbgb_vbd_step_adjoint: slot range outside the reserved tape");
         std::vector<float> hs(slotH.begin() + slot0, slotH.begin() + slot0 + substeps);
+        std::vector<float> kds(slotKD.begin() + slot0, slotKD.begin() + slot0 + substeps);
         std::vector<int32_t> st(slotStrategy.begin() + slot0, slotStrategy.begin() + slot0 + substeps);
         for (int32_t v : st)
             if (v < 0)
@@ -1128,15 +1188,16 @@ class VbdSystem
         if (adjGraphs.size() < size_t(tapeSlots))
             adjGraphs.resize(size_t(tapeSlots));
         SlotGraph& g = adjGraphs[slot0];
-        if (!g.exec || g.sub != substeps || g.h != hs || g.strategy != st)
+        if (!g.exec || g.sub != substeps || g.h != hs || g.strategy != st || g.kd != kds)
         {
             if (g.exec)
                 cudaGraphExecDestroy(g.exec);
             g.exec     = nullptr;
-            g.exec     = capture([&] { enqueueAdjoint(slot0, substeps, adjX.get(), adjV.get(), adjMu.get(), adjLa.get()); });
+            g.exec     = capture([&] { enqueueAdjoint(slot0, substeps, adjX.get(), adjV.get(), adjP.get(), adjMu.get(), adjLa.get()); });
             g.sub      = substeps;
             g.h        = hs;
             g.strategy = st;
+            g.kd       = kds;
         }
         size_t const b3 = sizeof(float) * 3 * size_t(nV), bt = sizeof(double) * size_t(nT);
         auto copy = [&](void* dst, void const* src, size_t n) {
@@ -1145,23 +1206,38 @@ class VbdSystem
         };
         copy(adjX.get(), xbar, b3);
         copy(adjV.get(), vbar, b3);
+        copy(adjP.get(), pbar, b3);
         copy(adjMu.get(), dlogmu, bt);
         copy(adjLa.get(), dloglambda, bt);
         check(cudaGraphLaunch(g.exec, stream), "cudaGraphLaunch");
         copy(xbar, adjX.get(), b3);
         copy(vbar, adjV.get(), b3);
+        copy(pbar, adjP.get(), b3);
         copy(dlogmu, adjMu.get(), bt);
         copy(dloglambda, adjLa.get(), bt);
     }
 
-    void enqueueAdjoint(int32_t slot0, int32_t substeps, float* xbar, float* vbar, double* dlogmu, double* dloglambda)
+    void enqueueAdjoint(int32_t slot0, int32_t substeps, float* xbar, float* vbar, float* pbar, double* dlogmu, double* dloglambda)
     {
-        int const L = lanesToUse();
+        int const L     = lanesToUse();
+        bool const cheb = acceleration == PBGB_ACCEL_CHEBYSHEV;
+        // Chebyshev weights of the iterations, as the forward formed them.
+        std::vector<float> om(size_t(std::max(tapeIters, 1)), 1.f);
+        {
+            double omega = 0.0;
+            for (int32_t k = 0; k < tapeIters; ++k)
+            {
+                omega         = chebyshev_omega<double>(k, rho * rho, omega, chebFormula);
+                om[size_t(k)] = float(omega);
+            }
+        }
         for (int32_t s = substeps - 1; s >= 0; --s)
         {
             int32_t const slot = slot0 + s;
             float const h      = slotH[slot];
-            check(launch_adjoint_begin(nV, xbar, vbar, ubar.get(), xtbar.get(), h, stream), "adjoint_begin");
+            check(launch_adjoint_begin(nV, xbar, vbar, ubar.get(), xtbar.get(), xsbar.get(), cheb ? ycarry.get() : nullptr,
+                                       cheb ? ycarry2.get() : nullptr, h, stream),
+                  "adjoint_begin");
             AdjointSweepParams a{};
             a.X          = X.get();
             a.tets       = tets.get();
@@ -1174,20 +1250,32 @@ class VbdSystem
             a.dlogmu     = dlogmu;
             a.dloglambda = dloglambda;
             a.h2         = h * h;
-            for (int32_t k = tapeIters; k >= 1; --k)
+            a.D          = slotKD[slot] / h;
+            a.xs         = slotStart(slot, 0);
+            a.xsbar      = xsbar.get();
+            for (int32_t k = tapeIters - 1; k >= 0; --k)
             {
-                a.xk   = slotX(slot, k);
-                a.xkm1 = slotX(slot, k - 1);
-                a.tape = slotTape(slot, k - 1);
+                if (cheb)
+                    check(launch_adjoint_cheb_mix(nV, ubar.get(), ycarry.get(), ycarry2.get(), k > 1 ? om[size_t(k)] : 1.f,
+                                                  k > 1 ? 1.f - om[size_t(k)] : 0.f, stream),
+                          "adjoint_cheb_mix");
+                a.xk   = slotRaw(slot, k);
+                a.xkm1 = slotX(slot, k);
+                a.tape = slotTape(slot, k);
                 for (int32_t c = nColors - 1; c >= 0; --c)
                 {
                     a.begin = colorPtr[c];
                     a.end   = colorPtr[c + 1];
-                    check(launch_adjoint_sweep(a, L, std::min(block, 256), pdl, stream), "adjoint_sweep");
+                    // A mix kernel precedes the last colour of an iteration: no programmatic launch
+                    // across it.
+                    check(launch_adjoint_sweep(a, L, std::min(block, 256), pdl && !(cheb && c == nColors - 1), stream),
+                          "adjoint_sweep");
                 }
             }
-            float const s1 = slotStrategy[slot] == PBGB_INIT_POSITION ? 0.f : 1.f;
-            check(launch_adjoint_end(nV, xbar, vbar, ubar.get(), xtbar.get(), h, s1, stream), "adjoint_end");
+            check(launch_adjoint_end(nV, xbar, vbar, pbar, ubar.get(), xtbar.get(), xsbar.get(), slotStart(slot, 1),
+                                     slotStart(slot, 2), aext.get(), h, slotStrategy[slot],
+                                     semantics == PBGB_SEMANTICS_GPU ? 1 : 0, stream),
+                  "adjoint_end");
         }
     }
 
@@ -1681,7 +1769,7 @@ class VbdSystem
     std::vector<float4> positionsToHost(float4 const* src)
     {
         std::vector<float4> out = deviceToHost(src);
-        if (nMeshes > 1)
+        if (origin.get())
             for (int32_t b = 0; b < nMeshes; ++b)
                 for (int32_t i = meshV0[b]; i < meshV0[b + 1]; ++i)
                 {
@@ -2475,7 +2563,54 @@ PBGB_API int pbgb_vbd_step_adjoint(
     if (!xbar_dev || !vbar_dev || (h->sys.nT > 0 && (!dlogmu_dev || !dloglambda_dev)))
         return fail(h, kInvalid, "null argument");
     return guarded(h, [&] {
-        h->sys.adjointStep(slot, substeps, xbar_dev, vbar_dev, dlogmu_dev, dloglambda_dev);
+        auto& s = h->sys;
+        if (s.strategy == PBGB_INIT_ADAPTIVE_VBD && s.semantics == PBGB_SEMANTICS_GPU)
+            throw std::invalid_argument(
+                "pbgb_vbd_step_adjoint: AdaptiveVbd with the GPU integrator's semantics reads the previous velocity; "
+                "use pbgb_vbd_step_adjoint_state, which carries its adjoint");
+        if (s.nV > 0)
+            check(cudaMemsetAsync(s.adjZero.get(), 0, sizeof(float) * 3 * size_t(s.nV), s.stream), "memset");
+        s.adjointStep(slot, substeps, xbar_dev, vbar_dev, s.adjZero.get(), dlogmu_dev, dloglambda_dev);
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_step_adjoint_state(
+    pbgb_vbd* h,
+    int32_t slot,
+    int32_t substeps,
+    float* xbar_dev,
+    float* vbar_dev,
+    float* vprevbar_dev,
+    double* dlogmu_dev,
+    double* dloglambda_dev)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (!xbar_dev || !vbar_dev || !vprevbar_dev || (h->sys.nT > 0 && (!dlogmu_dev || !dloglambda_dev)))
+        return fail(h, kInvalid, "null argument");
+    return guarded(h, [&] {
+        h->sys.adjointStep(slot, substeps, xbar_dev, vbar_dev, vprevbar_dev, dlogmu_dev, dloglambda_dev);
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_get_previous_velocities_device(pbgb_vbd* h, float* p_dev)
+{
+    if (!h || !p_dev)
+        return fail(h, kInvalid, "null argument");
+    return guarded(h, [&] {
+        pbgb::check(pbgb::launch_unpack3(h->sys.vprev.get(), p_dev, h->sys.nV, h->sys.stream), "unpack");
+        return int(kOk);
+    });
+}
+
+PBGB_API int pbgb_vbd_set_previous_velocities_device(pbgb_vbd* h, const float* p_dev)
+{
+    if (!h || !p_dev)
+        return fail(h, kInvalid, "null argument");
+    return guarded(h, [&] {
+        pbgb::check(pbgb::launch_pack3(p_dev, h->sys.vprev.get(), h->sys.nV, h->sys.stream), "pack");
         return int(kOk);
     });
 }

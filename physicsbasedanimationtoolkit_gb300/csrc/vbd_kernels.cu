@@ -429,15 +429,16 @@ cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebys
                      : launch_sweep_t<false, false>(q, lanes, g, block, pdl, s, stagedBytes);
 }
 
-cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool pdl, cudaStream_t s, size_t stagedBytes)
+cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool chebyshev, bool pdl, cudaStream_t s, size_t stagedBytes)
 {
     int64_t const n = int64_t(p.end - p.begin) * lanes;
     if (n <= 0)
         return cudaSuccess;
-    if (!p.tape || !p.stiff || !p.incPack || stagedBytes > kStagedMaxBytes || (stagedBytes > 0 && (!p.nbrPtr || !p.nbr)))
+    if (!p.tape || !p.stiff || !p.incPack || p.fc || stagedBytes > kStagedMaxBytes || (stagedBytes > 0 && (!p.nbrPtr || !p.nbr)))
         return cudaErrorInvalidValue;
-    SweepParams q = p;
-    return launch_sweep_t<false, true>(q, lanes, blocks_for(n, block), block, pdl, s, stagedBytes);
+    int const g = blocks_for(n, block);
+    return chebyshev ? launch_sweep_t<true, true>(p, lanes, g, block, pdl, s, stagedBytes)
+                     : launch_sweep_t<false, true>(p, lanes, g, block, pdl, s, stagedBytes);
 }
 
 size_t staged_sweep_bytes(int32_t const* nbrPtr, int32_t begin, int32_t end, int lanes, int block)
@@ -482,6 +483,8 @@ cudaError_t prepare_staged_sweeps()
         e = allow_staged_smem<true, false>();
     if (e == cudaSuccess)
         e = allow_staged_smem<false, true>();
+    if (e == cudaSuccess)
+        e = allow_staged_smem<true, true>();
     if (e == cudaSuccess)
         e = allow_staged_smem<true, false, true>();
     return e;

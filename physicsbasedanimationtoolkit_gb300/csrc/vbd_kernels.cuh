@@ -140,9 +140,9 @@ struct EnergyParams
 // shared memory per block); 0: the sweep that gathers every incidence's corners.  Both
 // compute the same arithmetic in the same order.
 cudaError_t launch_sweep(SweepParams const& p, int lanes, int block, bool chebyshev, bool pdl, cudaStream_t s, size_t stagedBytes = 0);
-// The plain (one-buffer) sweep that also writes p.tape; the same arithmetic as launch_sweep with
-// chebyshev = false, so a recorded step reproduces an unrecorded one.
-cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool pdl, cudaStream_t s, size_t stagedBytes = 0);
+// The sweep that also writes p.tape (no contact); the same arithmetic as launch_sweep with the same
+// chebyshev flag, so a recorded step reproduces an unrecorded one.
+cudaError_t launch_sweep_record(SweepParams const& p, int lanes, int block, bool chebyshev, bool pdl, cudaStream_t s, size_t stagedBytes = 0);
 // Dynamic shared memory of the staged sweep over solve entries [begin, end) with `lanes` lanes per
 // vertex and `block` threads per block: 16 bytes per staged neighbour of the block that stages the
 // most (nbrPtr on the host).

@@ -448,6 +448,47 @@ PBGB_HD void initial_position(
         x[r] = xt[r] + dt * vt[r] + dt2 * at * a[r];
 }
 
+// Derivatives of initial_position's acceleration factor a_t (x0 = xt + dt vt + dt^2 a_t a) with
+// respect to vt and vtm1 on the branch the forward took: AdaptiveVbd's clamp((vt - vtm1)/dt . a /
+// |a|^2, 0, 1) inside (0, 1), AdaptivePbat's min(|vt . a| / (|vt| |a|^2), 1) below 1 and away from
+// vt = 0 (where the factor jumps and has no derivative).  Zero otherwise (constant factors, clamped
+// branches).
+template <class T>
+PBGB_HD void initial_position_factor_derivatives(
+    T const* vtm1, T const* vt, T const* a, T dt, int strategy, T tiny, T* dAv, T* dAvm)
+{
+    for (int r = 0; r < 3; ++r)
+        dAv[r] = dAvm[r] = T(0);
+    T const an2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+    if (an2 == T(0))
+        return;
+    if (strategy == 3)
+    {
+        T const dot = ((vt[0] - vtm1[0]) / dt) * a[0] + ((vt[1] - vtm1[1]) / dt) * a[1] +
+                      ((vt[2] - vtm1[2]) / dt) * a[2];
+        T const q = dot / an2;
+        if (q > T(0) && q < T(1))
+            for (int r = 0; r < 3; ++r)
+            {
+                dAv[r]  = a[r] / (dt * an2);
+                dAvm[r] = -a[r] / (dt * an2);
+            }
+    }
+    else if (strategy == 4)
+    {
+        T const nv  = sqrt(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+        T const vn  = nv + tiny;
+        T const va  = vt[0] * a[0] + vt[1] * a[1] + vt[2] * a[2];
+        T const q   = va / (vn * an2);
+        if (nv > T(0) && fabs(q) < T(1))
+        {
+            T const sg = q > T(0) ? T(1) : (q < T(0) ? T(-1) : T(0));
+            for (int r = 0; r < 3; ++r)
+                dAv[r] = sg * (a[r] / vn - va * vt[r] / (vn * vn * nv)) / an2;
+        }
+    }
+}
+
 // Chebyshev weight (sim/vbd/Kernels.h:96-102).  formula 0 reproduces the reference's expression
 // as written, `4/4 - rho2*omega`; formula 1 is the textbook recurrence 4/(4 - rho2*omega).
 template <class T>

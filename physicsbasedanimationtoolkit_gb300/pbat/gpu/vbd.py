@@ -167,19 +167,23 @@ class _Rollout:
                     if t % every == 0:
                         cx = torch.empty((nV, 3), dtype=torch.float32, device=dev)
                         cv = torch.empty_like(cx)
+                        cp = torch.empty_like(cx)
                         integ._get_device("x", cx.data_ptr())
                         integ._get_device("v", cv.data_ptr())
-                        checkpoints.append((cx, cv))
+                        integ._get_device("vprev", cp.data_ptr())
+                        checkpoints.append((cx, cv, cp))
                     integ.step(dt, iterations, substeps)
                 xT = torch.empty((nV, 3), dtype=torch.float32, device=dev)
                 vT = torch.empty_like(xT)
+                pT = torch.empty_like(xT)
                 integ._get_device("x", xT.data_ptr())
                 integ._get_device("v", vT.data_ptr())
+                integ._get_device("vprev", pT.data_ptr())
                 integ.synchronize()
                 ctx.integ = integ
                 ctx.args = (dt, iterations, substeps, steps, every)
                 ctx.checkpoints = checkpoints
-                ctx.final = (xT.clone(), vT.clone())
+                ctx.final = (xT.clone(), vT.clone(), pT)
                 ctx.save_for_backward(mu, lam)
                 return xT, vT
 
@@ -192,6 +196,9 @@ class _Rollout:
                 nV, nT = integ.n_vertices, integ.n_tets
                 xbar = (torch.zeros((nV, 3), device=dev) if gx is None else gx.detach().to(dev, torch.float32)).contiguous().clone()
                 vbar = (torch.zeros((nV, 3), device=dev) if gv is None else gv.detach().to(dev, torch.float32)).contiguous().clone()
+                # The previous velocities (read by AdaptiveVbd under the GPU semantics) are state
+                # too: their adjoint is carried from step to step; nothing depends on the last ones.
+                pbar = torch.zeros((nV, 3), dtype=torch.float32, device=dev)
                 dlogmu = torch.zeros(nT, dtype=torch.float64, device=dev)
                 dloglambda = torch.zeros_like(dlogmu)
                 integ.adjoint_reserve(min(every, steps) * substeps, iterations)
@@ -199,17 +206,19 @@ class _Rollout:
                 for seg in reversed(range(len(ctx.checkpoints))):
                     start = seg * every
                     end = min(start + every, steps)
-                    cx, cv = ctx.checkpoints[seg]
+                    cx, cv, cp = ctx.checkpoints[seg]
                     integ._set_device("x", cx.data_ptr())
                     integ._set_device("v", cv.data_ptr())
+                    integ._set_device("vprev", cp.data_ptr())
                     for t in range(start, end):
                         integ.step_record(dt, iterations, substeps, (t - start) * substeps)
                     for t in reversed(range(start, end)):
                         integ.step_adjoint((t - start) * substeps, substeps, xbar.data_ptr(), vbar.data_ptr(),
-                                           dlogmu.data_ptr(), dloglambda.data_ptr())
+                                           dlogmu.data_ptr(), dloglambda.data_ptr(), pbar.data_ptr())
                 # Leave the integrator at the end of the forward rollout.
                 integ._set_device("x", ctx.final[0].data_ptr())
                 integ._set_device("v", ctx.final[1].data_ptr())
+                integ._set_device("vprev", ctx.final[2].data_ptr())
                 integ.synchronize()
                 dmu = dlogmu.to(mu.dtype).to(mu.device) / mu.detach()
                 dlam = dloglambda.to(lam.dtype).to(lam.device) / lam.detach()
@@ -228,9 +237,11 @@ def rollout(integrator, mu, lam, x0, v0, dt=0.01, iterations=20, steps=1, subste
     and velocities after the last step.  Backward runs the adjoint kernels: the positions are
     checkpointed every ``checkpoint_every`` steps in the forward pass, and each checkpoint segment
     is re-run with recording before it is reversed.  The gradient is the exact derivative of the
-    computed iterations (FP32).  Supported: no acceleration, kD = 0, no contact, initial guess
-    Position, Inertia or KineticEnergyMinimum.  Backward leaves the integrator at the rollout's
-    end state.
+    computed iterations (FP32).  Supported: plain VBD or Chebyshev acceleration, any Rayleigh
+    damping, every initial guess (the adaptive guesses' factor is differentiated on the branch the
+    forward took), no contact.  The previous velocities the integrator holds at the start (read by
+    AdaptiveVbd) are part of the start state but not differentiated.  Backward leaves the
+    integrator at the rollout's end state.
     """
     if checkpoint_every < 1:
         raise ValueError("checkpoint_every must be >= 1")

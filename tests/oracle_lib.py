@@ -86,8 +86,8 @@ def lib():
         ]
         L.orc_objective.restype = C.c_double
         L.orc_adjoint.restype = C.c_int
-        L.orc_adjoint.argtypes = [C.POINTER(OrcProblem), _f64p, _f64p, C.c_double, C.c_int32, C.c_int32,
-                                  C.c_int32, _f64p, _f64p, _f64p, _f64p]
+        L.orc_adjoint.argtypes = [C.POINTER(OrcProblem), _f64p, _f64p, _f64p, C.c_double, C.c_int32, C.c_int32,
+                                  C.c_int32, _f64p, _f64p, _f64p, _f64p, _f64p]
         L.orc_objective.argtypes = [C.POINTER(OrcProblem), _f64p, _f64p, C.c_double]
         L.orc_gradient.restype = None
         L.orc_gradient.argtypes = [C.POINTER(OrcProblem), _f64p, _f64p, C.c_double, _f64p]
@@ -295,19 +295,21 @@ class OracleVbd:
         if rc != 0:
             raise RuntimeError(f"oracle run failed: {rc}")
 
-    def adjoint(self, dt, iterations, substeps, nsteps, xbar, vbar):
+    def adjoint(self, dt, iterations, substeps, nsteps, xbar, vbar, vprevbar=None, with_vprev=False):
         """Reverse-mode derivative of ``nsteps`` steps from the current state (not advanced).
-        xbar, vbar (nV x 3): dL/dx, dL/dv of the final state.  Returns dL/dx0, dL/dv0 and
-        dL/dlog(mu), dL/dlog(lambda) per tet."""
+        xbar, vbar (nV x 3): dL/dx, dL/dv of the final state (vprevbar: dL/d of the final previous
+        velocity, zero by default).  Returns dL/dx0, dL/dv0, dL/dlog(mu), dL/dlog(lambda) per tet
+        (and dL/dvprev0 with ``with_vprev``)."""
         xb = np.array(xbar, dtype=np.float64, order="C")
         vb = np.array(vbar, dtype=np.float64, order="C")
+        pb = np.zeros_like(xb) if vprevbar is None else np.array(vprevbar, dtype=np.float64, order="C")
         dmu = np.zeros(self.T.shape[0])
         dla = np.zeros(self.T.shape[0])
-        rc = lib().orc_adjoint(C.byref(self.P), np.ascontiguousarray(self.x), np.ascontiguousarray(self.v), dt,
-                               iterations, substeps, nsteps, xb, vb, dmu, dla)
+        rc = lib().orc_adjoint(C.byref(self.P), np.ascontiguousarray(self.x), np.ascontiguousarray(self.v),
+                               np.ascontiguousarray(self.vprev), dt, iterations, substeps, nsteps, xb, vb, pb, dmu, dla)
         if rc != 0:
             raise RuntimeError(f"oracle adjoint failed: {rc}")
-        return xb, vb, dmu, dla
+        return (xb, vb, dmu, dla, pb) if with_vprev else (xb, vb, dmu, dla)
 
     def objective(self, x, xtilde, dt):
         return lib().orc_objective(C.byref(self.P), np.ascontiguousarray(x), np.ascontiguousarray(xtilde), dt)

@@ -17,28 +17,54 @@ def small_beam(seed=3):
     return w, v0
 
 
-def oracle(w, logE, v0, strategy):
+def oracle(w, logE, v0, strategy, semantics=1, **kw):
     nT = w["T"].shape[0]
     mu, lam = meshgen.lame(np.exp(logE), np.full(nT, w["nu"]))
-    return O.OracleVbd(w["X"], w["T"], w["rho"], mu, lam, w["dbc"], v=v0, strategy=strategy, semantics=1)
+    return O.OracleVbd(w["X"], w["T"], w["rho"], mu, lam, w["dbc"], v=v0, strategy=strategy, semantics=semantics, **kw)
 
 
-@pytest.mark.parametrize("strategy", [0, 1, 2])
-def test_oracle_adjoint_matches_central_differences(strategy):
+# (strategy, semantics, extra settings): every initial guess with both step semantics where they
+# differ, Rayleigh damping and Chebyshev (the reference's weight recurrence and the textbook one).
+SETTINGS = [
+    (0, 1, {}), (1, 1, {}), (2, 1, {}),
+    (3, 1, {}), (3, 0, {}), (4, 1, {}), (4, 0, {}),
+    (2, 1, dict(kD=1e-2)), (4, 1, dict(kD=5e-3)),
+    (2, 1, dict(rho_chebyshev=0.9)), (4, 1, dict(rho_chebyshev=0.9, chebyshev_formula=1)),
+    (3, 1, dict(rho_chebyshev=0.85, kD=1e-2)),
+]
+
+
+@pytest.mark.parametrize("strategy,semantics,kw", SETTINGS)
+def test_oracle_adjoint_matches_central_differences(strategy, semantics, kw):
+    """Loss of the tip vertices after 5 steps; central differences along 6 random directions of
+    (log E, v0, x0, and the previous velocity for AdaptiveVbd under the GPU integrator's semantics,
+    which reads it).  Random non-zero initial velocities keep AdaptivePbat away from v = 0, where
+    its clamp factor |v.a| / (|v| |a|^2) is not differentiable."""
     w, v0 = small_beam()
+    rng0 = np.random.default_rng(17)
+    p0 = rng0.uniform(-0.5, 0.5, v0.shape)
+    p0[w["dbc"]] = 0.0
     dt, iters, nsteps = 1 / 60, 10, 5
     tip, target = w["tip"], w["target"]
 
-    def loss(logE, v, dx):
-        I = oracle(w, logE, v, strategy)
+    def make(logE, v, p):
+        I = oracle(w, logE, v, strategy, semantics, **kw)
+        I.vprev[:] = p
+        return I
+
+    def loss(logE, v, dx, p):
+        I = make(logE, v, p)
         I.x = I.x + dx
         I.step(dt, iters, 1, nsteps)
         return np.sum((I.x[tip] - target) ** 2), I
 
-    L0, I = loss(w["logE"], v0, 0.0)
+    L0, I = loss(w["logE"], v0, 0.0, p0)
     xb = np.zeros_like(w["X"])
     xb[tip] = 2.0 * (I.x[tip] - target)
-    gx, gv, gmu, gla = oracle(w, w["logE"], v0, strategy).adjoint(dt, iters, 1, nsteps, xb, np.zeros_like(xb))
+    gx, gv, gmu, gla, gp = make(w["logE"], v0, p0).adjoint(dt, iters, 1, nsteps, xb, np.zeros_like(xb),
+                                                            with_vprev=True)
+    if not (strategy == 3 and semantics == 1):
+        assert not gp.any()
     glogE = gmu + gla
     rng = np.random.default_rng(11)
     eps = 1e-5
@@ -46,11 +72,13 @@ def test_oracle_adjoint_matches_central_differences(strategy):
         dE = rng.standard_normal(glogE.size)
         dv = rng.standard_normal(v0.shape)
         dv[w["dbc"]] = 0.0
+        dp = rng.standard_normal(v0.shape)
+        dp[w["dbc"]] = 0.0
         dx = 0.01 * rng.standard_normal(v0.shape)
-        fp = loss(w["logE"] + eps * dE, v0 + eps * dv, eps * dx)[0]
-        fm = loss(w["logE"] - eps * dE, v0 - eps * dv, -eps * dx)[0]
+        fp = loss(w["logE"] + eps * dE, v0 + eps * dv, eps * dx, p0 + eps * dp)[0]
+        fm = loss(w["logE"] - eps * dE, v0 - eps * dv, -eps * dx, p0 - eps * dp)[0]
         fd = (fp - fm) / (2 * eps)
-        ad = glogE @ dE + np.sum(gv * dv) + np.sum(gx * dx)
+        ad = glogE @ dE + np.sum(gv * dv) + np.sum(gx * dx) + np.sum(gp * dp)
         assert abs(ad - fd) <= 1e-6 * abs(fd) + 1e-9, (ad, fd)
 
 
@@ -78,8 +106,8 @@ def test_oracle_adjoint_rejects_unsupported_settings():
     w, v0 = small_beam()
     nT = w["T"].shape[0]
     mu, lam = meshgen.lame(np.exp(w["logE"]), np.full(nT, w["nu"]))
-    for kw in (dict(strategy=4), dict(strategy=2, kD=1e-3), dict(strategy=2, rho_chebyshev=0.9)):
-        I = O.OracleVbd(w["X"], w["T"], w["rho"], mu, lam, w["dbc"], v=v0, semantics=1, **kw)
+    for kw in (dict(anderson_window=3), dict(broyden_window=3)):
+        I = O.OracleVbd(w["X"], w["T"], w["rho"], mu, lam, w["dbc"], v=v0, semantics=1, strategy=2, **kw)
         with pytest.raises(RuntimeError):
             I.adjoint(1 / 60, 5, 1, 1, np.zeros_like(v0), np.zeros_like(v0))
 
