@@ -330,7 +330,15 @@ def run_batch(args, pbat, _capi, torch, with_single=True):
     meshes, datas = batch_workload(args, pbat)
     dt, iters = 1 / 60, args.batch_iterations
     B = pbat.gpu.vbd.BatchedIntegrator(datas)
-    lanes, block, tuned_ms = B.autotune(dt, iters, 1)
+    if args.lanes:
+        # A fixed launch (profiling runs launch exactly what a timed run launched, without the
+        # autotuner's candidates).
+        B.lanes_per_vertex = args.lanes
+        block = args.block or 256
+        _capi.check(_capi.lib().pbgb_vbd_set_block_size(B.handle, block), B.handle)
+        lanes, tuned_ms = args.lanes, None
+    else:
+        lanes, block, tuned_ms = B.autotune(dt, iters, 1)
     n_free = B.n_free
     sp = C.c_void_p()
     _capi.check(_capi.lib().pbgb_vbd_stream(B.handle, C.byref(sp)), B.handle)
@@ -341,6 +349,7 @@ def run_batch(args, pbat, _capi, torch, with_single=True):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t_batched = 0.0
+    torch.cuda.nvtx.range_push("timed_batch")  # lets ncu --nvtx-include select the timed steps
     for _ in range(args.steps):
         flush.add_(1.0)
         torch.cuda.synchronize()
@@ -349,6 +358,7 @@ def run_batch(args, pbat, _capi, torch, with_single=True):
         e1.record(stream)
         B.synchronize()
         t_batched += e0.elapsed_time(e1) * 1e-3
+    torch.cuda.nvtx.range_pop()
     out = {
         "workload": f"{len(meshes)} cube grids, side U{{6..32}} hexes x 6 tets, {iters} iterations, no acceleration",
         "n_meshes": len(meshes),
@@ -698,7 +708,13 @@ def run_beam(args, pbat, _capi, torch):
     L = _capi.lib()
     h = vbd.handle
     dt, iters = 1 / 60, args.iterations
-    t_lanes, t_block, t_ms = vbd.autotune(dt, iters, 1)
+    if args.beam_launch:
+        t_lanes, t_block = args.beam_launch
+        vbd.lanes_per_vertex = t_lanes
+        _capi.check(L.pbgb_vbd_set_block_size(h, t_block), h)
+        t_ms = None
+    else:
+        t_lanes, t_block, t_ms = vbd.autotune(dt, iters, 1)
     n_free = vbd.n_free
     sp = C.c_void_p()
     _capi.check(L.pbgb_vbd_stream(h, C.byref(sp)), h)
@@ -804,12 +820,14 @@ def main():
     ap.add_argument("--nx", type=int, default=160)
     ap.add_argument("--ny", type=int, default=40)
     ap.add_argument("--nz", type=int, default=40)
-    ap.add_argument("--lanes", type=int, default=0, help="headline (batch): lanes per vertex instead of autotuning")
+    ap.add_argument("--lanes", type=int, default=0, help="headline and --only batch: lanes per vertex instead of autotuning")
     ap.add_argument("--block", type=int, default=0, help="headline with --lanes: block size (default 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-beam", dest="beam", action="store_false", default=True,
                     help="skip the single large beam (Chebyshev, 50 iterations) leg")
     ap.add_argument("--batch-meshes", type=int, default=256)
+    ap.add_argument("--no-single", action="store_true",
+                    help="--only batch: skip the one-integrator-per-mesh comparison (profiling runs)")
     ap.add_argument("--batch-iterations", type=int, default=20)
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false", default=True,
                     help="skip the adjoint (bwd/fwd) measurement on the differentiation beam")
@@ -824,6 +842,9 @@ def main():
     ap.add_argument("--contact-launch", type=lambda t: tuple(int(v) for v in t.split(",")), default=None,
                     metavar="LANES,BLOCK", help="contact leg: use these lanes per vertex and block size instead "
                     "of autotuning (for profiling runs that must launch what a timed run launched)")
+    ap.add_argument("--beam-launch", type=lambda t: tuple(int(v) for v in t.split(",")), default=None,
+                    metavar="LANES,BLOCK", help="beam leg: use these lanes per vertex and block size instead of "
+                    "autotuning (profiling runs)")
     ap.add_argument("--no-broyden", dest="broyden", action="store_false", default=True,
                     help="skip the Broyden-acceleration measurement")
     ap.add_argument("--only", choices=["batch", "beam", "adjoint", "contact", "lbvh", "anderson", "broyden", "trust_region"],
@@ -847,7 +868,7 @@ def main():
 
     if args.only:
         legs = {
-            "batch": lambda: run_batch(args, pbat, _capi, torch),
+            "batch": lambda: run_batch(args, pbat, _capi, torch, with_single=not args.no_single),
             "beam": lambda: run_beam(args, pbat, _capi, torch),
             "adjoint": lambda: run_adjoint(args, pbat, torch),
             "contact": lambda: run_contact(args, pbat, torch),

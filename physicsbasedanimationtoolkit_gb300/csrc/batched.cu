@@ -53,7 +53,10 @@ __device__ bool wait_for(BatchedStepParams const& p, int32_t const* counter, int
 }
 
 // Colour sweep of solve entries [begin, end) by the whole block: sub-tiles of blockDim / L vertices,
-// each staged and solved like staged_sweep_kernel, with the block's positions read through L2.
+// each staged and solved like staged_sweep_kernel (the same arithmetic in the same order), with the
+// block's positions read through L2.  The incidence loop keeps two incidences' records in flight
+// (this one's and the next two's loads overlap its arithmetic): the batch's incidence records
+// stream from DRAM, and one record ahead per lane left too few bytes in flight per SM.
 template <int L, bool CHEB>
 __device__ __forceinline__ void sweep_tile(SweepParams const& p, int begin, int end, float4* slab)
 {
@@ -69,8 +72,8 @@ __device__ __forceinline__ void sweep_tile(SweepParams const& p, int begin, int 
         int i       = 0;
         float xi[3] = {0.f, 0.f, 0.f};
         int k = 0, k1 = 0, n0 = 0, n1 = 0, base = 0;
-        uint2 q   = make_uint2(0u, 0u);
-        float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint2 q0 = make_uint2(0u, 0u), q1 = q0;
+        float4 st0 = make_float4(0.f, 0.f, 0.f, 0.f), st1 = st0;
         if (valid)
         {
             i    = __ldg(p.solve + s);
@@ -81,8 +84,13 @@ __device__ __forceinline__ void sweep_tile(SweepParams const& p, int begin, int 
             k    = __ldg(p.incPtr + s) + lane;
             if (k < k1)
             {
-                q  = __ldg(p.incPack + k);
-                st = __ldg(p.stiff + k);
+                q0  = __ldg(p.incPack + k);
+                st0 = __ldg(p.stiff + k);
+            }
+            if (k + L < k1)
+            {
+                q1  = __ldg(p.incPack + k + L);
+                st1 = __ldg(p.stiff + k + L);
             }
             load3(Mem<true>::ld((CHEB ? p.hprev : p.x) + i), xi);
             for (int j = n0 + lane; j < n1; j += L)
@@ -99,25 +107,27 @@ __device__ __forceinline__ void sweep_tile(SweepParams const& p, int begin, int 
         {
             for (; k < k1; k += L)
             {
-                uint2 qn   = make_uint2(0u, 0u);
-                float4 stn = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (k + L < k1)
+                uint2 q2   = make_uint2(0u, 0u);
+                float4 st2 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (k + 2 * L < k1)
                 {
-                    qn  = __ldg(p.incPack + k + L);
-                    stn = __ldg(p.stiff + k + L);
+                    q2  = __ldg(p.incPack + k + 2 * L);
+                    st2 = __ldg(p.stiff + k + 2 * L);
                 }
                 float d[3][3];
 #pragma unroll
                 for (int m = 0; m < 3; ++m)
                 {
-                    float4 const xa = slab[base + int((q.x >> (8 * m)) & 0xFFu)];
+                    float4 const xa = slab[base + int((q0.x >> (8 * m)) & 0xFFu)];
                     d[m][0] = xa.x - xi[0];
                     d[m][1] = xa.y - xi[1];
                     d[m][2] = xa.z - xi[2];
                 }
-                accumulate_incidence(b, d, st.x, st.y, st.z, __uint_as_float(q.y), st.w);
-                q  = qn;
-                st = stn;
+                accumulate_incidence(b, d, st0.x, st0.y, st0.z, __uint_as_float(q0.y), st0.w);
+                q0  = q1;
+                st0 = st1;
+                q1  = q2;
+                st1 = st2;
             }
         }
         finish_vertex<L, CHEB, false, false, true>(p, b, valid, lane, i, s, xi);

@@ -356,20 +356,26 @@ __device__ __forceinline__ float4 fmax4(float4 a, float4 b)
     return make_float4(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), 0.f);
 }
 
-// Atomic add with release and acquire semantics at device scope: the caller's earlier stores are
-// visible to the thread that later reads the counter's new value, and the caller sees the stores
-// of the threads whose additions it reads.
-__device__ __forceinline__ int atomic_add_acq_rel(int32_t* p, int v)
+// Atomic add with release semantics at device scope: the caller's earlier stores are visible to
+// a thread that reads the counter's new value and then acquires (acquire_fence).
+__device__ __forceinline__ int atomic_add_release(int32_t* p, int v)
 {
     int old;
-    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    asm volatile("atom.release.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
     return old;
+}
+
+// Together with the preceding atomic read of the counter, an acquire: the stores released by the
+// thread whose addition was read are visible after it.
+__device__ __forceinline__ void acquire_fence()
+{
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
 }
 
 // Leaf boxes in sorted order and the bottom-up internal boxes (gpu/impl/geometry/Bvh.cu:175-229).
 // Thread s gathers leaf s's box, then climbs: the first thread to reach a node stops; the second
 // unites the box it carries in registers with its sibling's (stored by the first thread before
-// that thread's counter update) and continues.  At most 64 levels; deeper trees raise
+// its releasing counter update; the second acquires after reading the counter) and continues.  At most 64 levels; deeper trees raise
 // kBvhErrDepth instead of looping on.  Min and max are exact and commutative, so the boxes do not
 // depend on which child's thread goes on.
 __global__ void boxes_kernel(int32_t n, BvhBuffers B, float4 const* __restrict__ lo, float4 const* __restrict__ hi)
@@ -388,8 +394,10 @@ __global__ void boxes_kernel(int32_t n, BvhBuffers B, float4 const* __restrict__
     int k        = 0;
     for (; k < 64 && p >= 0; ++k)
     {
-        if (atomic_add_acq_rel(&B.visits[p], 1) == 0)
+        // Both arrivals release their box; only the second, which goes on, acquires the first's.
+        if (atomic_add_release(&B.visits[p], 1) == 0)
             return;
+        acquire_fence();
         int32_t const lc  = B.child[2 * p];
         int32_t const rc  = B.child[2 * p + 1];
         int32_t const sib = lc == node ? rc : lc;
