@@ -544,32 +544,51 @@ class VbdSystem
                 vb += d.n_vertices;
             }
         }
+        // Mesh origins, per axis: zero unless the mesh's box (over its rest and initial positions)
+        // lies farther from the world origin than its own extent; then the box centre rounded to a
+        // multiple of the FP32 spacing at the box's largest coordinate.  Such an origin makes
+        // x - origin exact for every FP32 coordinate in the box (a multiple of that coordinate's
+        // spacing, no larger than the coordinate), so positions set and read back round-trip bit
+        // for bit, and meshes near the world origin keep the world frame.
         meshOrigin.assign(size_t(nMeshes), make_float4(0.f, 0.f, 0.f, 0.f));
         bool const useOrigins = !(nMeshes == 1 && d0.n_collision_triangles > 0);
         if (useOrigins)
             for (int32_t b = 0; b < nMeshes; ++b)
             {
                 auto const& d = descs[b];
-                double const* R = d.X ? d.X : d.x;
                 double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
-                for (int32_t i = 0; i < d.n_vertices; ++i)
-                    for (int k = 0; k < 3; ++k)
-                    {
-                        lo[k] = std::min(lo[k], R[3 * size_t(i) + k]);
-                        hi[k] = std::max(hi[k], R[3 * size_t(i) + k]);
-                    }
-                meshOrigin[b] = make_float4(float(0.5 * (lo[0] + hi[0])), float(0.5 * (lo[1] + hi[1])),
-                                            float(0.5 * (lo[2] + hi[2])), 0.f);
+                for (double const* R : {d.x, d.X})
+                    if (R)
+                        for (int32_t i = 0; i < d.n_vertices; ++i)
+                            for (int k = 0; k < 3; ++k)
+                            {
+                                double const c = double(float(R[3 * size_t(i) + k]));
+                                lo[k] = std::min(lo[k], c);
+                                hi[k] = std::max(hi[k], c);
+                            }
+                float o[3] = {0.f, 0.f, 0.f};
+                for (int k = 0; k < 3 && d.n_vertices > 0; ++k)
+                {
+                    double const ext = hi[k] - lo[k];
+                    bool const far   = (lo[k] > 0.0 && lo[k] > ext) || (hi[k] < 0.0 && -hi[k] > ext);
+                    if (!far)
+                        continue;
+                    int exponent = 0;
+                    std::frexp(std::max(std::fabs(lo[k]), std::fabs(hi[k])), &exponent);
+                    double const spacing = std::ldexp(1.0, exponent - 24); // FP32 spacing at that magnitude
+                    o[k] = float(std::round(0.5 * (lo[k] + hi[k]) / spacing) * spacing);
+                }
+                meshOrigin[b] = make_float4(o[0], o[1], o[2], 0.f);
             }
         int32_t v0 = 0, t0 = 0;
         for (int32_t b = 0; b < nMeshes; ++b)
         {
             auto const& d = descs[b];
-            double const o[3] = {meshOrigin[b].x, meshOrigin[b].y, meshOrigin[b].z};
+            float const o[3] = {meshOrigin[b].x, meshOrigin[b].y, meshOrigin[b].z};
             for (int32_t i = 0; i < d.n_vertices; ++i)
             {
                 double const* p = d.x + 3 * size_t(i);
-                hx[v0 + i]      = make_float4(float(p[0] - o[0]), float(p[1] - o[1]), float(p[2] - o[2]), 0.f);
+                hx[v0 + i]      = make_float4(float(p[0]) - o[0], float(p[1]) - o[1], float(p[2]) - o[2], 0.f);
                 if (d.v)
                 {
                     double const* q = d.v + 3 * size_t(i);
@@ -587,7 +606,7 @@ class VbdSystem
                 hm[v0 + i]    = float(d.m[i]);
                 hostM[v0 + i] = d.m[i];
                 double const* R = (d.X ? d.X : d.x) + 3 * size_t(i);
-                hX[v0 + i]      = make_float4(float(R[0] - o[0]), float(R[1] - o[1]), float(R[2] - o[2]), 0.f);
+                hX[v0 + i]      = make_float4(float(R[0]) - o[0], float(R[1]) - o[1], float(R[2]) - o[2], 0.f);
             }
             for (int32_t e = 0; e < d.n_tets; ++e)
             {

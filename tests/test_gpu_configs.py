@@ -189,24 +189,37 @@ def test_contact_scene_matches_contact_oracle_through_contact():
     """30 steps (the cubes start 5 cm above the slab and touch it at about step 6).
 
     * Until the first contact, free-running positions agree within 1e-4 of the diagonal.
-    * Every step, the contact lists the device chose agree with the lists the FP64 oracle chooses
-      from the same state (the device's positions, velocities and active set at the step's
-      start), except where the two differ only by triangles whose distances to the vertex are
-      tied within 1e-5 of the scene diagonal: the reference's list keeps triangles within
-      FLT_EPSILON of the nearest, so a tie is decided by the last bits of the arithmetic.
-    * With the device's lists replayed in the oracle (its own positions, the device's discrete
-      decisions), positions agree within 1e-4 of the diagonal at every step."""
+    * Once contact starts, the step is compared one step at a time from the device's state
+      (positions, velocities, active set, search radii and lists, read from the checkpoint blob):
+      the FP32 device and the FP64 oracle take discrete decisions that near-ties can tip either
+      way (a triangle within FLT_EPSILON of the nearest joins a list or not; a vertex projects
+      inside a triangle or just outside it), each decision changes a contact force by a finite
+      amount, and free-running trajectories of this stiff scene then drift apart.
+      * The contact lists the device chose equal the lists the oracle chooses from the same state,
+        except where the two differ only by triangles tied within 1e-5 of the diagonal with the
+        nearest one, on at most 1 % of the vertices with contacts.
+      * With the device's lists, the oracle's step from the same state lands within 1e-4 of the
+        diagonal of the device's."""
     w, I = contact_scene_integrator()
     kw = dict(muC=1e7, muF=0.3, epsv=1e-3, strategy=2)
     R = O.OracleContactVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], w["V"], w["F"], w["B"], **kw)
     D = O.OracleContactVbd(w["X"], w["T"], w["rho"], w["mu"], w["lam"], w["dbc"], w["V"], w["F"], w["B"], **kw)
     nV, V, F = w["X"].shape[0], np.asarray(w["V"]), np.asarray(w["F"])
     d = diag(w["X"])
-    replay, free, first_contact, mismatched, listed = [], [], None, 0, 0
+    free, step_errs, first_contact, mismatched, listed = [], [], None, 0, 0
     for step in range(30):
-        x0, v0, vp0, act0, dup0, fc0 = device_contact_state(I, nV, V.size)
+        state = device_contact_state(I, nV, V.size)
+        x0, v0, vp0, act0, dup0, fc0 = state
         I.step(1 / 60, 30, 1)
+        x = I.x.T.astype(np.float64)
         fc_dev = I.contacts()[0].reshape(-1)
+        if first_contact is None and (fc_dev >= 0).any():
+            first_contact = step
+        if first_contact is None:
+            # Free-running until contact.
+            R.step(1 / 60, 30, 1, 1)
+            free.append(float(np.abs(x - R.x).max() / d))
+            continue
         # The oracle's own decisions from the device's state.
         D.x[:], D.v[:], D.vprev[:] = x0, v0, vp0
         D.active[:], D.dupper[:], D.fc[:] = act0, dup0, fc0
@@ -220,15 +233,12 @@ def test_contact_scene_matches_contact_oracle_through_contact():
             assert all(dist[f] - best <= 1e-5 * d for f in a ^ b), (step, i, dist)
             mismatched += 1
         listed += int((dev >= 0).any(axis=1).sum())
-        # Replay: the oracle's positions under the device's lists.
+        # The oracle's step from the same state with the device's lists.
+        R.x[:], R.v[:], R.vprev[:] = x0, v0, vp0
+        R.active[:], R.dupper[:], R.fc[:] = act0, dup0, fc0
         R.step(1 / 60, 30, 1, 1, contact_lists=fc_dev)
-        x = I.x.T.astype(np.float64)
-        replay.append(float(np.abs(x - R.x).max() / d))
-        if first_contact is None and (fc_dev >= 0).any():
-            first_contact = step
-        if first_contact is None:
-            free.append(replay[-1])
-    assert first_contact is not None and first_contact < 15, first_contact
+        step_errs.append(float(np.abs(x - R.x).max() / d))
+    assert first_contact is not None and 0 < first_contact < 15, first_contact
     assert max(free) <= TOL, free
-    assert max(replay) <= TOL, replay
+    assert max(step_errs) <= TOL, step_errs
     assert listed > 1000 and mismatched <= 0.01 * listed, (mismatched, listed)
