@@ -182,6 +182,15 @@ def traffic_from_profiles(name):
     return traffic, f"ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/{name}"
 
 
+def dram_rate(traffic, avg_launch_ms, peak):
+    """The ncu-measured DRAM bytes of one launch over the live launch duration, and its fraction of
+    the HBM peak (the algorithmic figure counts bytes that L2 serves as well)."""
+    if traffic is None or not avg_launch_ms:
+        return {"dram_gbs": None, "dram_frac": None}
+    gbs = traffic / (avg_launch_ms * 1e-3) / 1e9
+    return {"dram_gbs": gbs, "dram_frac": gbs / peak}
+
+
 def batch_oracles(meshes):
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_lib as O
@@ -330,6 +339,8 @@ def run_batch(args, pbat, _capi, torch, with_single=True):
     meshes, datas = batch_workload(args, pbat)
     dt, iters = 1 / 60, args.batch_iterations
     B = pbat.gpu.vbd.BatchedIntegrator(datas)
+    if args.waves is not None:
+        B.batch_waves = args.waves
     if args.lanes:
         # A fixed launch (profiling runs launch exactly what a timed run launched, without the
         # autotuner's candidates).
@@ -366,6 +377,7 @@ def run_batch(args, pbat, _capi, torch, with_single=True):
         "n_tets": int(B.n_tets),
         "n_free_vertices": int(n_free),
         "persistent": bool(B.persistent),
+        "waves": int(B.batch_waves),
         "batched_value": n_free * iters * args.steps / t_batched,
         "batched_ms_per_step": 1e3 * t_batched / args.steps,
         "autotuned": {"lanes": lanes, "block": block, "ms_per_step": tuned_ms},
@@ -785,7 +797,8 @@ def run_beam(args, pbat, _capi, torch):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "traffic_basis": traffic_basis, "peak_kind": peak_kind,
                      "kernel": "staged_sweep_kernel (per-colour vertex Newton sweep)",
-                     "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_launch_ms * 1e3},
+                     "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_launch_ms * 1e3,
+                     **dram_rate(traffic, avg_launch_ms, peak)},
         "launch_config": {"lanes": t_lanes, "block": t_block, "tuned_ms_per_step": t_ms},
         "launches_per_step": int(launches_per_step),
     }
@@ -836,6 +849,9 @@ def main():
     ap.add_argument("--nz", type=int, default=40)
     ap.add_argument("--lanes", type=int, default=0, help="headline and --only batch: lanes per vertex instead of autotuning")
     ap.add_argument("--block", type=int, default=0, help="headline with --lanes: block size (default 256)")
+    ap.add_argument("--waves", type=int, default=None,
+                    help="headline and --only batch: groups of meshes stepped one after the other (default: the "
+                         "integrator's choice from the L2 size)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-beam", dest="beam", action="store_false", default=True,
                     help="skip the single large beam (Chebyshev, 50 iterations) leg")
@@ -901,6 +917,8 @@ def main():
     dt, iters = 1 / 60, args.batch_iterations
     B = pbat.gpu.vbd.BatchedIntegrator(datas)
     h = B.handle
+    if args.waves is not None:
+        B.batch_waves = args.waves
     if args.lanes:
         B.lanes_per_vertex = args.lanes
         if args.block:
@@ -963,6 +981,7 @@ def main():
     e2e_value = group.sum(updates_per_step * e2e_steps) / e2e_s
     io_bytes = nV * 3 * 4 * 2
     persistent = B.persistent
+    waves = B.batch_waves
     lanes_used = B.lanes_per_vertex
     del B, flush
     torch.cuda.empty_cache()
@@ -976,7 +995,8 @@ def main():
         achieved = bytes_per_step / max(launches_per_step, 1) / (avg_launch_ms * 1e-3) / 1e9
         traffic, traffic_basis = traffic_from_profiles("batched_step_cfg3.md")
         launch_config = {"autotuned": tuned is not None, "lanes": lanes_used,
-                         "block": tuned["block"] if tuned else (args.block or 256), "persistent": persistent}
+                         "block": tuned["block"] if tuned else (args.block or 256), "persistent": persistent,
+                         "waves": waves}
         single = run_single_launch(args, pbat, _capi, torch, meshes, datas, launch_config)
         cpu = None if args.no_cpu_baseline else cpu_baseline(meshes, iters)
         beam = run_beam(args, pbat, _capi, torch) if args.beam else None
@@ -1013,7 +1033,8 @@ def main():
                          "kernel": "batched_step_kernel (persistent step of the whole batch)",
                          "algorithmic_bytes_per_launch": bytes_per_step / max(launches_per_step, 1),
                          "avg_launch_us": avg_launch_ms * 1e3,
-                         "avg_launch_us_basis": "timed steps (CUDA events on the integrator's stream) / launches per step"},
+                         "avg_launch_us_basis": "timed steps (CUDA events on the integrator's stream) / launches per step",
+                         **dram_rate(traffic, avg_launch_ms, peak)},
             "launch_config": launch_config,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),

@@ -257,6 +257,10 @@ PBGB_API int pbgb_vbd_set_scene_bounding_box(pbgb_vbd* h, const float* min3, con
 PBGB_API int pbgb_vbd_sizes(pbgb_vbd* h, int32_t* n_vertices, int32_t* n_tets, int32_t* n_free, int32_t* n_colors);
 /* Number of kernels one pbgb_vbd_step(iterations, substeps) launches. */
 PBGB_API int pbgb_vbd_launches_per_step(pbgb_vbd* h, int32_t iterations, int32_t substeps, int64_t* launches);
+/* Kernel nodes of the CUDA graph pbgb_vbd_step last captured: the launches a step replays, counted
+ * from the graph itself (-1 before the first captured step; a traced step is not captured and
+ * leaves the count as it was). */
+PBGB_API int pbgb_vbd_step_graph_kernels(pbgb_vbd* h, int64_t* kernels);
 /* Sweep timing (off by default): when enabled, each captured step records a CUDA event pair around
  * the colour sweeps of every iteration.  pbgb_vbd_sweep_timing returns, for the last step, the
  * summed sweep intervals in milliseconds and the number of sweep kernel launches they cover. */
@@ -269,10 +273,18 @@ PBGB_API int pbgb_vbd_sweep_timing(pbgb_vbd* h, double* milliseconds, int64_t* s
  * synchronizing call return PBGB_ERR_TIMEOUT).  Used for plain VBD and Chebyshev without contact
  * when every colour's neighbours fit in shared memory; otherwise, or when disabled, a batch steps
  * with one launch per colour.  pbgb_vbd_persistent reports whether the next step uses it.
- * pbgb_vbd_set_batch_tile: sweep work items of subtiles x (block / lanes) vertices (default 1). */
+ * pbgb_vbd_set_batch_tile: sweep work items of subtiles x (block / lanes) vertices (default 1).
+ * pbgb_vbd_set_batch_waves: step the meshes in `waves` groups of consecutive meshes with about
+ * equal vertex counts, one group after the other inside the launch, so that the positions of the
+ * meshes in flight stay in L2 while their incidence records stream (0, the default: the count
+ * that keeps a group's positions and one colour's records within half of L2 without leaving
+ * resident threads idle).  pbgb_vbd_batch_waves reports the count the last planned step used (0
+ * when no persistent step was planned).  Neither changes the results. */
 PBGB_API int pbgb_vbd_set_persistent(pbgb_vbd* h, int32_t enable);
 PBGB_API int pbgb_vbd_persistent(pbgb_vbd* h, int32_t* active);
 PBGB_API int pbgb_vbd_set_batch_tile(pbgb_vbd* h, int32_t subtiles);
+PBGB_API int pbgb_vbd_set_batch_waves(pbgb_vbd* h, int32_t waves);
+PBGB_API int pbgb_vbd_batch_waves(pbgb_vbd* h, int32_t* waves);
 /* The handle's CUDA stream (cudaStream_t) so callers can order their own work after a step. */
 PBGB_API int pbgb_vbd_stream(pbgb_vbd* h, void** stream);
 

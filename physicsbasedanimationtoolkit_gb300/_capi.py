@@ -126,10 +126,13 @@ _SIGNATURES = [
     ("pbgb_vbd_set_persistent", C.c_int, [_vp, _i32]),
     ("pbgb_vbd_persistent", C.c_int, [_vp, C.POINTER(_i32)]),
     ("pbgb_vbd_set_batch_tile", C.c_int, [_vp, _i32]),
+    ("pbgb_vbd_set_batch_waves", C.c_int, [_vp, _i32]),
+    ("pbgb_vbd_batch_waves", C.c_int, [_vp, C.POINTER(_i32)]),
     ("pbgb_debug_batched_wait", C.c_int, [_vp, C.c_int64, _i32]),
     ("pbgb_vbd_set_scene_bounding_box", C.c_int, [_vp, _vp, _vp]),
     ("pbgb_vbd_sizes", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     ("pbgb_vbd_launches_per_step", C.c_int, [_vp, _i32, _i32, C.POINTER(C.c_int64)]),
+    ("pbgb_vbd_step_graph_kernels", C.c_int, [_vp, C.POINTER(C.c_int64)]),
     ("pbgb_vbd_stream", C.c_int, [_vp, C.POINTER(_vp)]),
     ("pbgb_vbd_set_sweep_timing", C.c_int, [_vp, _i32]),
     ("pbgb_vbd_sweep_timing", C.c_int, [_vp, C.POINTER(_f64), C.POINTER(C.c_int64)]),

@@ -198,6 +198,12 @@ class IntegratorBase:
         _capi.check(_capi.lib().pbgb_vbd_launches_per_step(self._h, int(iterations), int(substeps), C.byref(n)), self._h)
         return n.value
 
+    def step_graph_kernels(self):
+        """Kernel nodes of the CUDA graph the last step captured (-1 before the first step)."""
+        n = C.c_int64()
+        _capi.check(_capi.lib().pbgb_vbd_step_graph_kernels(self._h, C.byref(n)), self._h)
+        return n.value
+
     def contacts(self):
         """(fc, active): contact triangles per vertex (|#vertices| x 8, -1 = none) and the active
         flags of the collision vertices after the last step."""

@@ -56,7 +56,9 @@ __device__ bool wait_for(BatchedStepParams const& p, int32_t const* counter, int
 // each staged and solved like staged_sweep_kernel (the same arithmetic in the same order), with the
 // block's positions read through L2.  The incidence loop keeps two incidences' records in flight
 // (this one's and the next two's loads overlap its arithmetic): the batch's incidence records
-// stream from DRAM, and one record ahead per lane left too few bytes in flight per SM.
+// stream from DRAM, and one record ahead per lane left too few bytes in flight per SM.  (Loading
+// the records evict-first, ld.global.cs, doubled the DRAM reads of a 256-mesh step: a record's
+// sector left L2 before the neighbouring lanes had read their parts of it.)
 template <int L, bool CHEB>
 __device__ __forceinline__ void sweep_tile(SweepParams const& p, int begin, int end, float4* slab)
 {

@@ -180,27 +180,27 @@ __device__ void initialize_serial(ContactMesh const& M, ContactState const& S, B
     while (top > 0)
     {
         int32_t const node = stack[--top];
+        float4 const nl    = node_lo(T, node);
+        float4 const nh    = node_hi(T, node);
+        if (!boxes_overlap(L, U, nl, nh))
+            continue;
         if (node >= leafBegin)
         {
-            int32_t const s = node - leafBegin;
-            if (!boxes_overlap(L, U, T.llo[s], T.lhi[s]))
-                continue;
-            int32_t const f = T.inds[s];
-            int4 const t    = M.F[f];
+            int4 const t = M.F[node_link(nl)];
             if (M.B[i] == M.B[t.x])
                 continue;
             best = fmaxf(best, joint_box_sqdiag(i, t, xt, xn));
             hit  = true;
         }
-        else if (boxes_overlap(L, U, T.ilo[node], T.ihi[node]))
+        else
         {
             if (top + 2 > kBvhStack)
             {
                 atomicOr(S.flags, kBvhErrStackOverflow);
                 return;
             }
-            stack[top++] = T.child[2 * node];
-            stack[top++] = T.child[2 * node + 1];
+            stack[top++] = node_link(nl);
+            stack[top++] = node_link(nh);
         }
     }
     if (hit)
@@ -248,21 +248,19 @@ __global__ void __launch_bounds__(32 * kInitWarps) initialize_kernel(ContactMesh
             int32_t a = -1, b = -1;
             if (node >= 0)
             {
-                if (node < leafBegin)
+                float4 const nl = node_lo(T, node);
+                float4 const nh = node_hi(T, node);
+                if (boxes_overlap(L, U, nl, nh))
                 {
-                    if (boxes_overlap(L, U, T.ilo[node], T.ihi[node]))
+                    if (node < leafBegin)
                     {
-                        a    = T.child[2 * node];
-                        b    = T.child[2 * node + 1];
+                        a    = node_link(nl);
+                        b    = node_link(nh);
                         push = true;
                     }
-                }
-                else
-                {
-                    int32_t const s = node - leafBegin;
-                    if (boxes_overlap(L, U, T.llo[s], T.lhi[s]))
+                    else
                     {
-                        int4 const t = M.F[T.inds[s]];
+                        int4 const t = M.F[node_link(nl)];
                         if (M.B[t.x] != body)
                         {
                             best = fmaxf(best, joint_box_sqdiag(i, t, xt, xn));
@@ -327,10 +325,9 @@ __global__ void compact_kernel(int32_t n, uint8_t const* __restrict__ active, in
 // widens each eps to at most an ulp of d), so the leaves pass 2 skips can
 // neither restart nor join the final list, and removing them leaves the last restart and
 // everything after it unchanged.
-__device__ __forceinline__ float node_box_sqdist(BvhView const& T, float3 p, int32_t node, int32_t leafBegin)
+__device__ __forceinline__ float node_box_sqdist(BvhView const& T, float3 p, int32_t node)
 {
-    return node < leafBegin ? point_box_sqdist(p, T.ilo[node], T.ihi[node])
-                            : point_box_sqdist(p, T.llo[node - leafBegin], T.lhi[node - leafBegin]);
+    return point_box_sqdist(p, node_lo(T, node), node_hi(T, node));
 }
 
 // Writes the result of a query (see nearest_kernel).
@@ -378,7 +375,7 @@ __device__ void nearest_serial(ContactMesh const& M, ContactState const& S, BvhV
     float best = d0 + eps;
     bool found = false;
     stack[top]  = 0;
-    dist[top++] = node_box_sqdist(T, p, 0, leafBegin);
+    dist[top++] = node_box_sqdist(T, p, 0);
     while (top > 0)
     {
         --top;
@@ -387,8 +384,8 @@ __device__ void nearest_serial(ContactMesh const& M, ContactState const& S, BvhV
             continue;
         if (node < leafBegin)
         {
-            int32_t const a = T.child[2 * node], b = T.child[2 * node + 1];
-            float const da = node_box_sqdist(T, p, a, leafBegin), db = node_box_sqdist(T, p, b, leafBegin);
+            int32_t const a = node_link(node_lo(T, node)), b = node_link(node_hi(T, node));
+            float const da = node_box_sqdist(T, p, a), db = node_box_sqdist(T, p, b);
             if (top + 2 > kBvhStack)
             {
                 atomicOr(S.flags, kBvhErrStackOverflow);
@@ -404,7 +401,7 @@ __device__ void nearest_serial(ContactMesh const& M, ContactState const& S, BvhV
                 stack[top] = n1, dist[top++] = e1;
             continue;
         }
-        int4 const t = M.F[T.inds[node - leafBegin]];
+        int4 const t = M.F[node_link(node_lo(T, node))];
         if (M.B[t.x] == body)
             continue;
         float const d = point_triangle_sqdist(p, f3(x[t.x]), f3(x[t.y]), f3(x[t.z]));
@@ -432,24 +429,22 @@ __device__ void nearest_serial(ContactMesh const& M, ContactState const& S, BvhV
             float const lo     = dmin - eps;
             float const hi     = dmin + eps;
             float const bound  = fminf(hi, cap);
+            float4 const nl    = node_lo(T, node);
+            float4 const nh    = node_hi(T, node);
+            if (point_box_sqdist(p, nl, nh) > bound)
+                continue;
             if (node < leafBegin)
             {
-                if (point_box_sqdist(p, T.ilo[node], T.ihi[node]) <= bound)
+                if (top + 2 > kBvhStack)
                 {
-                    if (top + 2 > kBvhStack)
-                    {
-                        atomicOr(S.flags, kBvhErrStackOverflow);
-                        return;
-                    }
-                    stack[top++] = T.child[2 * node];
-                    stack[top++] = T.child[2 * node + 1];
+                    atomicOr(S.flags, kBvhErrStackOverflow);
+                    return;
                 }
+                stack[top++] = node_link(nl);
+                stack[top++] = node_link(nh);
                 continue;
             }
-            int32_t const s = node - leafBegin;
-            if (point_box_sqdist(p, T.llo[s], T.lhi[s]) > bound)
-                continue;
-            int32_t const f = T.inds[s];
+            int32_t const f = node_link(nl);
             int4 const t    = M.F[f];
             float const d   = M.B[t.x] == body ? FLT_MAX
                                                : point_triangle_sqdist(p, f3(x[t.x]), f3(x[t.y]), f3(x[t.z]));
@@ -541,21 +536,24 @@ __global__ void __launch_bounds__(32 * kNearestWarps) nearest_kernel(ContactMesh
             float d        = FLT_MAX;
             if (node >= 0)
             {
+                float4 const nl = node_lo(T, node);
+                float4 const nh = node_hi(T, node);
+                bool const near = point_box_sqdist(p, nl, nh) <= bound;
                 if (node < leafBegin)
                 {
-                    if (point_box_sqdist(p, T.ilo[node], T.ihi[node]) <= bound)
+                    if (near)
                     {
-                        a        = T.child[2 * node];
-                        b        = T.child[2 * node + 1];
+                        a        = node_link(nl);
+                        b        = node_link(nh);
                         pushNode = true;
                     }
                 }
                 else
                 {
                     int32_t const s = node - leafBegin;
-                    if (point_box_sqdist(p, T.llo[s], T.lhi[s]) <= bound)
+                    if (near)
                     {
-                        int4 const t = M.F[T.inds[s]];
+                        int4 const t = M.F[node_link(nl)];
                         d            = M.B[t.x] == body ? FLT_MAX
                                                         : point_triangle_sqdist(p, f3(x[t.x]), f3(x[t.y]), f3(x[t.z]));
                         pushLeaf = d <= bound;
@@ -711,25 +709,23 @@ __global__ void nearest_simplex_kernel(BvhView V, int32_t nq, float4 const* __re
     while (top > 0)
     {
         int32_t const node = stack[--top];
+        float4 const nl    = node_lo(V, node);
+        float4 const nh    = node_hi(V, node);
+        if (point_box_sqdist(x, nl, nh) > dmin)
+            continue;
         if (node < leafBegin)
         {
-            if (point_box_sqdist(x, V.ilo[node], V.ihi[node]) <= dmin)
+            if (top + 2 > kBvhStack)
             {
-                if (top + 2 > kBvhStack)
-                {
-                    atomicOr(flags, kBvhErrStackOverflow);
-                    nn[q] = -1;
-                    return;
-                }
-                stack[top++] = V.child[2 * node];
-                stack[top++] = V.child[2 * node + 1];
+                atomicOr(flags, kBvhErrStackOverflow);
+                nn[q] = -1;
+                return;
             }
+            stack[top++] = node_link(nl);
+            stack[top++] = node_link(nh);
             continue;
         }
-        int32_t const sl = node - leafBegin;
-        if (point_box_sqdist(x, V.llo[sl], V.lhi[sl]) > dmin)
-            continue;
-        int32_t const i      = V.inds[sl];
+        int32_t const i      = node_link(nl);
         int32_t const* const c = S + size_t(i) * K;
         float const d = K == 3 ? point_triangle_sqdist(x, f3(P[c[0]]), f3(P[c[1]]), f3(P[c[2]]))
                                : point_tet_sqdist(x, f3(P[c[0]]), f3(P[c[1]]), f3(P[c[2]]), f3(P[c[K - 1]]));

@@ -284,18 +284,19 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     }
 }
 
-// --- Karras hierarchy (gpu/impl/geometry/Bvh.cu:24-114) -------------------------------------------
+// --- hierarchy --------------------------------------------------------------------------------
 
-struct Karras
+// The sorted keys (code, index): prefix lengths of the binary radix tree over them.
+struct SortedKeys
 {
     uint32_t const* __restrict__ code;
     int32_t n;
 
     // Length of the common prefix of keys i and j (index bits break ties of equal codes); -1
     // outside [0, n).
-    __device__ int delta(int32_t i, int32_t j) const
+    __device__ __forceinline__ int delta(int32_t i, int32_t j) const
     {
-        if (j < 0 || j >= n)
+        if (i < 0 || j < 0 || i >= n || j >= n)
             return -1;
         uint32_t const a = code[i], b = code[j];
         if (a == b)
@@ -303,49 +304,6 @@ struct Karras
         return __clz(a ^ b);
     }
 };
-
-__global__ void karras_kernel(Karras K, int32_t* __restrict__ child, int32_t* __restrict__ parent, int32_t* __restrict__ rightmost)
-{
-    int32_t const i = blockIdx.x * blockDim.x + threadIdx.x;
-    int32_t const n = K.n;
-    if (i >= n - 1)
-        return;
-    int32_t const leafBegin = n - 1;
-    // Direction of the range and a lower bound on its common prefix.
-    int32_t const d    = (K.delta(i, i + 1) - K.delta(i, i - 1)) > 0 ? 1 : -1;
-    int const dmin     = K.delta(i, i - d);
-    int32_t lmax       = 2;
-    while (K.delta(i, i + lmax * d) > dmin)
-        lmax <<= 1;
-    int32_t l = 0;
-    do
-    {
-        lmax >>= 1;
-        if (K.delta(i, i + (l + lmax) * d) > dmin)
-            l += lmax;
-    } while (lmax > 1);
-    int32_t const j   = i + l * d;
-    int const dnode   = K.delta(i, j);
-    int32_t s         = 0;
-    int32_t t         = l;
-    do
-    {
-        t = (t + 1) >> 1;
-        if (K.delta(i, i + (s + t) * d) > dnode)
-            s += t;
-    } while (t > 1);
-    int32_t const gamma = i + s * d + (d < 0 ? d : 0);
-    int32_t const lo    = i < j ? i : j;
-    int32_t const hi    = i < j ? j : i;
-    int32_t const lc    = lo == gamma ? leafBegin + gamma : gamma;
-    int32_t const rc    = hi == gamma + 1 ? leafBegin + gamma + 1 : gamma + 1;
-    child[2 * i]         = lc;
-    child[2 * i + 1]     = rc;
-    parent[lc]           = i;
-    parent[rc]           = i;
-    rightmost[2 * i]     = leafBegin + gamma;
-    rightmost[2 * i + 1] = leafBegin + hi;
-}
 
 __device__ __forceinline__ float4 fmin4(float4 a, float4 b)
 {
@@ -372,46 +330,190 @@ __device__ __forceinline__ void acquire_fence()
     asm volatile("fence.acq_rel.gpu;" ::: "memory");
 }
 
-// Leaf boxes in sorted order and the bottom-up internal boxes (gpu/impl/geometry/Bvh.cu:175-229).
-// Thread s gathers leaf s's box, then climbs: the first thread to reach a node stops; the second
-// unites the box it carries in registers with its sibling's (stored by the first thread before
-// its releasing counter update; the second acquires after reading the counter) and continues.  At most 64 levels; deeper trees raise
-// kBvhErrDepth instead of looping on.  Min and max are exact and commutative, so the boxes do not
-// depend on which child's thread goes on.
-__global__ void boxes_kernel(int32_t n, BvhBuffers B, float4 const* __restrict__ lo, float4 const* __restrict__ hi)
+// Leaf boxes in sorted order and the bottom-up internal boxes over a built hierarchy, the refit
+// (gpu/impl/geometry/Bvh.cu:175-229; the build's own boxes come from hierarchy_kernel below).
+// Thread s gathers leaf s's box, writes the leaf's record, then climbs: the first thread to reach a
+// node stops; the second unites the box it carries in registers with its sibling's record (written
+// by the first thread before its counter update) and continues.  Min and max are exact and
+// commutative, so the boxes do not depend on which child's thread goes on.
+//
+// A block owns kBoxLeaves consecutive sorted leaves [L, R].  A node whose leaf range lies inside
+// [L, R] has its index inside it too (a Karras node is an end of its range), so its visit counter
+// is a shared-memory word and the arrival order needs only block-scope fences; its record lands in
+// the block's own window of the node array (the second arrival sets the node's visits entry to 2).
+// The first node whose range reaches past [L, R] and all its ancestors use device-scope counters
+// (visits) with a releasing add and an acquire by the second arrival, whose sibling record may
+// come from another block.  Over both phases a climb takes at most 64 levels; deeper trees raise
+// kBvhErrDepth instead of looping on.
+int constexpr kBoxLeaves = 1024;
+
+__global__ void __launch_bounds__(kBoxLeaves, 2) boxes_kernel(int32_t n, BvhBuffers B, float4 const* __restrict__ lo, float4 const* __restrict__ hi)
 {
-    int const s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n)
+    __shared__ int32_t arrivals[kBoxLeaves];
+    int32_t const L = int32_t(blockIdx.x) * kBoxLeaves;
+    int32_t const R = min(L + kBoxLeaves, n) - 1;
+    arrivals[threadIdx.x] = 0;
+    __syncthreads();
+    int32_t const s = L + int32_t(threadIdx.x);
+    if (s > R)
         return;
     int32_t const leafBegin = n - 1;
     int32_t const i         = B.inds[s];
     float4 bl               = lo[i];
     float4 bh               = hi[i];
-    __stcg(&B.llo[s], bl);
-    __stcg(&B.lhi[s], bh);
-    int32_t node = leafBegin + s;
-    int32_t p    = B.parent[node];
-    int k        = 0;
+    int32_t node            = leafBegin + s;
+    B.nodes[2 * size_t(node)]     = make_float4(bl.x, bl.y, bl.z, __int_as_float(i));
+    B.nodes[2 * size_t(node) + 1] = make_float4(bh.x, bh.y, bh.z, __int_as_float(-1));
+    int32_t p = B.parent[node];
+    int k     = 0;
+    // Inside the block.
     for (; k < 64 && p >= 0; ++k)
     {
-        // Both arrivals release their box; only the second, which goes on, acquires the first's.
+        if (B.first[p] < L || B.rightmost[2 * p + 1] - leafBegin > R)
+            break;
+        __threadfence_block(); // this node's record before the arrival
+        if (atomicAdd(&arrivals[p - L], 1) == 0)
+            return;
+        __threadfence_block(); // the sibling's record after its arrival
+        B.visits[p]       = 2;  // the second arrival (crossing nodes count in visits itself)
+        int2 const c      = reinterpret_cast<int2 const*>(B.child)[p];
+        int32_t const sib = c.x == node ? c.y : c.x;
+        float4 const sl   = B.nodes[2 * size_t(sib)];
+        float4 const sh   = B.nodes[2 * size_t(sib) + 1];
+        bl                = fmin4(bl, sl);
+        bh                = fmax4(bh, sh);
+        B.nodes[2 * size_t(p)]     = make_float4(bl.x, bl.y, bl.z, __int_as_float(c.x));
+        B.nodes[2 * size_t(p) + 1] = make_float4(bh.x, bh.y, bh.z, __int_as_float(c.y));
+        node = p;
+        p    = B.parent[p];
+    }
+    // Across blocks.
+    for (; k < 64 && p >= 0; ++k)
+    {
         if (atomic_add_release(&B.visits[p], 1) == 0)
             return;
         acquire_fence();
-        int32_t const lc  = B.child[2 * p];
-        int32_t const rc  = B.child[2 * p + 1];
-        int32_t const sib = lc == node ? rc : lc;
-        float4 const sl   = sib >= leafBegin ? __ldcg(&B.llo[sib - leafBegin]) : __ldcg(&B.ilo[sib]);
-        float4 const sh   = sib >= leafBegin ? __ldcg(&B.lhi[sib - leafBegin]) : __ldcg(&B.ihi[sib]);
+        int2 const c      = __ldcg(reinterpret_cast<int2 const*>(B.child) + p);
+        int32_t const sib = c.x == node ? c.y : c.x;
+        float4 const sl   = __ldcg(&B.nodes[2 * size_t(sib)]);
+        float4 const sh   = __ldcg(&B.nodes[2 * size_t(sib) + 1]);
         bl                = fmin4(bl, sl);
         bh                = fmax4(bh, sh);
-        __stcg(&B.ilo[p], bl);
-        __stcg(&B.ihi[p], bh);
+        __stcg(&B.nodes[2 * size_t(p)], make_float4(bl.x, bl.y, bl.z, __int_as_float(c.x)));
+        __stcg(&B.nodes[2 * size_t(p) + 1], make_float4(bh.x, bh.y, bh.z, __int_as_float(c.y)));
         node = p;
         p    = B.parent[p];
     }
     if (k == 64 && p >= 0)
         atomicOr(B.flags, kBvhErrDepth);
+}
+
+// Hierarchy and boxes in one bottom-up pass (the reference builds the hierarchy top-down, one
+// thread per internal node searching its range, gpu/impl/geometry/Bvh.cu:24-114, then the boxes,
+// :175-229).  The binary radix tree over the sorted keys is unique, so it can be grown from the
+// leaves: a node [lo, hi] is the left child of its parent when its right neighbour shares the
+// longer prefix with it (delta(hi, hi + 1) > delta(lo - 1, lo)), and the parent's split is then hi,
+// else lo - 1.  The reference's node numbering follows from that side: a left child is numbered by
+// its last leaf, a right child by its first, the root (the whole range) is 0; leaves are n - 1 + s.
+// So the thread that goes on from a node knows its number when it takes the node's next step, and
+// writes its record, links (child, parent of both children, rightmost, first) there.
+//
+// Arrivals meet at the parent's split gamma: the first thread stops, the second finds its sibling
+// from the keys alone (the sibling across gamma is internal iff its next key shares more than
+// the parent's prefix; an internal right sibling is numbered gamma + 1 and its last leaf is in its
+// rightmost link, an internal left sibling is numbered gamma and its first leaf is in first[]),
+// reads the sibling's box from its record and unites it with its own.  A parent whose range lies
+// inside the block's leaves [L, R] (keys L - 1 and R + 1 share less than the parent's prefix with
+// the far side of gamma) meets on a shared-memory counter with block-scope fences; any other on a
+// device-scope counter (splits[gamma]) with a releasing add and an acquire.  Both children decide
+// the same way from gamma, and a parent that crosses the block has only ancestors that do.
+__global__ void __launch_bounds__(kBoxLeaves, 2) hierarchy_kernel(int32_t n, BvhBuffers B, float4 const* __restrict__ lo, float4 const* __restrict__ hi)
+{
+    __shared__ int32_t arrivals[kBoxLeaves];
+    int32_t const L = int32_t(blockIdx.x) * kBoxLeaves;
+    int32_t const R = min(L + kBoxLeaves, n) - 1;
+    arrivals[threadIdx.x] = 0;
+    __syncthreads();
+    int32_t const s = L + int32_t(threadIdx.x);
+    if (s > R)
+        return;
+    SortedKeys const K{B.codes, n};
+    int32_t const leafBegin = n - 1;
+    int32_t const i         = B.inds[s];
+    float4 bl               = lo[i];
+    float4 bh               = hi[i];
+    int32_t node            = leafBegin + s;
+    B.nodes[2 * size_t(node)]     = make_float4(bl.x, bl.y, bl.z, __int_as_float(i));
+    B.nodes[2 * size_t(node) + 1] = make_float4(bh.x, bh.y, bh.z, __int_as_float(-1));
+    if (n == 1)
+        return;
+    int32_t first = s, last = s;      // the current node's leaves
+    int32_t c0 = -1, c1 = -1, split = -1; // its children and split (internal nodes)
+    bool local = true;
+    int k      = 0;
+    for (; k < 64; ++k)
+    {
+        bool const leftChild = K.delta(last, last + 1) > K.delta(first - 1, first);
+        if (k > 0)
+        {
+            node                          = leftChild ? last : first; // the root: first = 0
+            B.nodes[2 * size_t(node)]     = make_float4(bl.x, bl.y, bl.z, __int_as_float(c0));
+            B.nodes[2 * size_t(node) + 1] = make_float4(bh.x, bh.y, bh.z, __int_as_float(c1));
+            reinterpret_cast<int2*>(B.child)[node]     = make_int2(c0, c1);
+            reinterpret_cast<int2*>(B.rightmost)[node] = make_int2(leafBegin + split, leafBegin + last);
+            B.first[node]                              = first;
+            B.parent[c0]                               = node;
+            B.parent[c1]                               = node;
+            B.visits[node]                             = 2; // its builder is its second arrival
+            if (first == 0 && last == n - 1)
+                return;
+        }
+        int32_t const gamma = leftChild ? last : first - 1;
+        int const dp        = K.delta(gamma, gamma + 1);
+        if (local)
+            local = (R + 1 >= n || K.delta(gamma, R + 1) < dp) && (L == 0 || K.delta(L - 1, gamma + 1) < dp);
+        if (local)
+        {
+            __threadfence_block(); // this node's record and links before the arrival
+            if (atomicAdd(&arrivals[gamma - L], 1) == 0)
+                return;
+            __threadfence_block(); // the sibling's after its arrival
+        }
+        else
+        {
+            if (atomic_add_release(&B.splits[gamma], 1) == 0)
+                return;
+            acquire_fence();
+        }
+        // The sibling's record and links: written in this block (plain loads after the block-scope
+        // fence) or possibly in another (loads from L2 after the acquire).
+        int32_t sib;
+        if (leftChild)
+        {
+            bool const internal = K.delta(gamma + 1, gamma + 2) > dp;
+            sib                 = internal ? gamma + 1 : leafBegin + gamma + 1;
+            int32_t const* q    = B.rightmost + 2 * (gamma + 1) + 1;
+            last                = internal ? (local ? *q : __ldcg(q)) - leafBegin : gamma + 1;
+            c0                  = node;
+            c1                  = sib;
+        }
+        else
+        {
+            bool const internal = K.delta(gamma - 1, gamma) > dp;
+            sib                 = internal ? gamma : leafBegin + gamma;
+            int32_t const* q    = B.first + gamma;
+            first               = internal ? (local ? *q : __ldcg(q)) : gamma;
+            c0                  = sib;
+            c1                  = node;
+        }
+        float4 const* r = B.nodes + 2 * size_t(sib);
+        float4 const sl = local ? r[0] : __ldcg(r);
+        float4 const sh = local ? r[1] : __ldcg(r + 1);
+        bl              = fmin4(bl, sl);
+        bh              = fmax4(bh, sh);
+        split           = gamma;
+    }
+    atomicOr(B.flags, kBvhErrDepth);
 }
 
 __device__ __forceinline__ bool boxes_overlap(float4 const& l1, float4 const& u1, float4 const& l2, float4 const& u2)
@@ -435,28 +537,28 @@ __global__ void overlaps_kernel(BvhView V, int32_t nq, float4 const* __restrict_
     while (top > 0)
     {
         int32_t const node = stack[--top];
+        float4 const nl    = node_lo(V, node);
+        float4 const nh    = node_hi(V, node);
+        if (!boxes_overlap(L, U, nl, nh))
+            continue;
         if (node >= leafBegin)
         {
-            int32_t const s = node - leafBegin;
-            if (boxes_overlap(L, U, V.llo[s], V.lhi[s]))
+            unsigned long long const slot = atomicAdd(count, 1ull);
+            if (slot < (unsigned long long)capacity)
             {
-                unsigned long long const slot = atomicAdd(count, 1ull);
-                if (slot < (unsigned long long)capacity)
-                {
-                    pairs[2 * slot]     = q;
-                    pairs[2 * slot + 1] = V.inds[s];
-                }
+                pairs[2 * slot]     = q;
+                pairs[2 * slot + 1] = node_link(nl);
             }
         }
-        else if (boxes_overlap(L, U, V.ilo[node], V.ihi[node]))
+        else
         {
             if (top + 2 > kBvhStack)
             {
                 atomicOr(flags, kBvhErrStackOverflow);
                 return;
             }
-            stack[top++] = V.child[2 * node];
-            stack[top++] = V.child[2 * node + 1];
+            stack[top++] = node_link(nl);
+            stack[top++] = node_link(nh);
         }
     }
 }
@@ -473,8 +575,8 @@ __global__ void self_overlaps_kernel(BvhView V, int32_t const* __restrict__ set,
         return;
     int32_t const leafBegin = V.n - 1;
     int32_t const leaf      = leafBegin + s;
-    float4 const L = V.llo[s], U = V.lhi[s];
-    int32_t const bi = V.inds[s];
+    float4 const L = node_lo(V, leaf), U = node_hi(V, leaf);
+    int32_t const bi = node_link(L);
     int32_t stack[kBvhStack];
     int top      = 0;
     stack[top++] = 0;
@@ -488,13 +590,13 @@ __global__ void self_overlaps_kernel(BvhView V, int32_t const* __restrict__ set,
             if (V.rightmost[2 * node + c] <= leaf)
                 continue;
             bool const isLeaf = ch >= leafBegin;
-            float4 const cl   = isLeaf ? V.llo[ch - leafBegin] : V.ilo[ch];
-            float4 const cu   = isLeaf ? V.lhi[ch - leafBegin] : V.ihi[ch];
+            float4 const cl   = node_lo(V, ch);
+            float4 const cu   = node_hi(V, ch);
             if (!boxes_overlap(L, U, cl, cu))
                 continue;
             if (isLeaf)
             {
-                int32_t const bj = V.inds[ch - leafBegin];
+                int32_t const bj = node_link(cl);
                 if (set && set[bi] == set[bj])
                     continue;
                 unsigned long long const slot = atomicAdd(count, 1ull);
@@ -586,11 +688,40 @@ cudaError_t boxes_impl(BvhBuffers const& B, int32_t n, float4 const* lo, float4 
         if (e != cudaSuccess)
             return e;
     }
-    boxes_kernel<<<blocks(n, 256), 256, 0, s>>>(n, B, lo, hi);
+    boxes_kernel<<<blocks(n, kBoxLeaves), kBoxLeaves, 0, s>>>(n, B, lo, hi);
     return cudaGetLastError();
 }
 
 } // namespace
+
+int64_t bvh_build_kernels(int32_t n)
+{
+    if (n <= 0)
+        return 0;
+    // Kernels of exclusive_scan over `total` counters: one block scan per level, one add per
+    // level above the last.
+    auto scan = [](int64_t total) {
+        int64_t k = 0;
+        for (;;)
+        {
+            int64_t const nb = (total + kScanItems - 1) / kScanItems;
+            if (nb <= 0)
+                return k;
+            ++k;
+            if (nb == 1)
+                return k;
+            ++k;
+            total = nb;
+        }
+    };
+    // Morton, 4 x (count, scan, scatter), hierarchy.
+    return 1 + 4 * (2 + scan(radix_counts_size(n))) + 1;
+}
+
+int64_t bvh_refit_kernels(int32_t n)
+{
+    return n > 0 ? 1 : 0;
+}
 
 int64_t radix_counts_size(int32_t n)
 {
@@ -617,11 +748,10 @@ cudaError_t bvh_allocate(BvhBuffers& B, int32_t capacity)
     get(B.child, 2 * ni);
     get(B.parent, 2 * n);
     get(B.rightmost, 2 * ni);
+    get(B.first, ni);
     get(B.visits, ni);
-    get(B.ilo, ni);
-    get(B.ihi, ni);
-    get(B.llo, n);
-    get(B.lhi, n);
+    get(B.splits, ni);
+    get(B.nodes, 2 * (2 * n - 1));
     get(B.flags, 1);
     if (e == cudaSuccess)
         e = cudaMemset(B.flags, 0, sizeof(int32_t));
@@ -631,7 +761,7 @@ cudaError_t bvh_allocate(BvhBuffers& B, int32_t capacity)
 void bvh_release(BvhBuffers& B)
 {
     void* ptrs[] = {B.codes, B.codesAlt, B.inds, B.indsAlt, B.counts, B.scanTmp, B.child, B.parent,
-                    B.rightmost, B.visits, B.ilo, B.ihi, B.llo, B.lhi, B.flags};
+                    B.rightmost, B.first, B.visits, B.splits, B.nodes, B.flags};
     for (void* p : ptrs)
         if (p)
             cudaFree(p);
@@ -651,16 +781,13 @@ cudaError_t bvh_build(BvhBuffers const& B, int32_t n, float4 const* lo, float4 c
     if (e != cudaSuccess)
         return e;
     // The root has no parent; every other node is the child of exactly one internal node, whose
-    // Karras thread writes its parent.
+    // builder writes its parent.
     if ((e = cudaMemsetAsync(B.parent, 0xFF, sizeof(int32_t), s)) != cudaSuccess)
         return e;
-    if (n > 1)
-    {
-        karras_kernel<<<blocks(n - 1, 256), 256, 0, s>>>(Karras{B.codes, n}, B.child, B.parent, B.rightmost);
-        if ((e = cudaGetLastError()) != cudaSuccess)
-            return e;
-    }
-    return boxes_impl(B, n, lo, hi, s);
+    if (n > 1 && (e = cudaMemsetAsync(B.splits, 0, sizeof(int32_t) * size_t(n - 1), s)) != cudaSuccess)
+        return e;
+    hierarchy_kernel<<<blocks(n, kBoxLeaves), kBoxLeaves, 0, s>>>(n, B, lo, hi);
+    return cudaGetLastError();
 }
 
 cudaError_t bvh_refit(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, cudaStream_t s)

@@ -19,17 +19,32 @@ int constexpr kBvhMaxNeighbours = 8; // nearest-neighbour ties kept per query (r
 int constexpr kBvhErrStackOverflow = 1;
 int constexpr kBvhErrDepth        = 2;
 
+// Node records: node k (internal 0..n-2, leaf n-1+s for sorted leaf s) is nodes[2k] = (lo.x, lo.y,
+// lo.z, c0) and nodes[2k+1] = (hi.x, hi.y, hi.z, c1), c0 and c1 stored as int bits: the children of
+// an internal node, and (original box index, -1) for a leaf.  A box and the node's links share one
+// 32-byte sector, so a traversal step reads one sector per node.
 struct BvhView
 {
     int32_t n;                       // leaves
     int32_t const* __restrict__ inds; // n: original box index of sorted leaf s
     int32_t const* __restrict__ child;     // 2(n-1): child[2i], child[2i+1]
     int32_t const* __restrict__ rightmost; // 2(n-1)
-    float4 const* __restrict__ ilo;  // n-1 internal boxes
-    float4 const* __restrict__ ihi;
-    float4 const* __restrict__ llo;  // n leaf boxes in sorted order
-    float4 const* __restrict__ lhi;
+    float4 const* __restrict__ nodes;      // 2(2n-1) node records
 };
+
+__device__ __forceinline__ float4 node_lo(BvhView const& V, int32_t k)
+{
+    return V.nodes[2 * size_t(k)];
+}
+__device__ __forceinline__ float4 node_hi(BvhView const& V, int32_t k)
+{
+    return V.nodes[2 * size_t(k) + 1];
+}
+// The link words of a node record: children of an internal node, (box index, -1) of a leaf.
+__device__ __forceinline__ int32_t node_link(float4 const& half)
+{
+    return __float_as_int(half.w);
+}
 
 // Work arrays of one BVH (allocated by the owner, sized for `capacity` boxes).
 struct BvhBuffers
@@ -44,16 +59,18 @@ struct BvhBuffers
     int32_t* child;     // 2(n-1)
     int32_t* parent;    // 2n-1
     int32_t* rightmost; // 2(n-1)
-    int32_t* visits;    // n-1
-    float4* ilo;        // n-1
-    float4* ihi;
-    float4* llo;        // n
-    float4* lhi;
+    int32_t* first;     // n-1 lowest sorted leaf of each internal node's range
+    int32_t* visits;    // n-1 arrivals counted at each internal node (2 after a build or refit)
+    int32_t* splits;    // n-1 arrival counters of the build, by split position
+    float4* nodes;      // 2(2n-1) node records (BvhView)
     int32_t* flags;     // device error bits
 };
 
 // Number of uint32 digit counters the radix sort needs for n keys.
 int64_t radix_counts_size(int32_t n);
+// Kernel launches of bvh_build and bvh_refit for n boxes (memsets not counted).
+int64_t bvh_build_kernels(int32_t n);
+int64_t bvh_refit_kernels(int32_t n);
 
 // Device arrays of a BVH for up to `capacity` boxes (bvh_release frees them; safe on partial
 // allocation).
@@ -112,7 +129,7 @@ cudaError_t bvh_nearest_simplices(
 
 inline BvhView view_of(BvhBuffers const& B, int32_t n)
 {
-    return BvhView{n, B.inds, B.child, B.rightmost, B.ilo, B.ihi, B.llo, B.lhi};
+    return BvhView{n, B.inds, B.child, B.rightmost, B.nodes};
 }
 
 // Spreads the 10 low bits of v so that bit k lands on bit 3k (shift-or form).  A 30-bit Morton

@@ -285,26 +285,25 @@ PBGB_API int pbgb_bvh_topology(
         get(child, b->B.child, sizeof(int32_t) * 2 * ni);
         get(parent, b->B.parent, sizeof(int32_t) * (2 * n - 1));
         get(rightmost, b->B.rightmost, sizeof(int32_t) * 2 * ni);
-        std::vector<float4> lo(ni), hi(ni);
+        // Internal node records come first: 2 float4 (lower | link, upper | link) per node.
+        std::vector<float4> rec(2 * ni);
         if (ni && (internal_lower || internal_upper))
-        {
-            get(lo.data(), b->B.ilo, sizeof(float4) * ni);
-            get(hi.data(), b->B.ihi, sizeof(float4) * ni);
-        }
+            get(rec.data(), b->B.nodes, sizeof(float4) * 2 * ni);
         ck(cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
         for (size_t i = 0; i < ni; ++i)
         {
+            float4 const lo = rec[2 * i], hi = rec[2 * i + 1];
             if (internal_lower)
             {
-                internal_lower[3 * i]     = lo[i].x;
-                internal_lower[3 * i + 1] = lo[i].y;
-                internal_lower[3 * i + 2] = lo[i].z;
+                internal_lower[3 * i]     = lo.x;
+                internal_lower[3 * i + 1] = lo.y;
+                internal_lower[3 * i + 2] = lo.z;
             }
             if (internal_upper)
             {
-                internal_upper[3 * i]     = hi[i].x;
-                internal_upper[3 * i + 1] = hi[i].y;
-                internal_upper[3 * i + 2] = hi[i].z;
+                internal_upper[3 * i]     = hi.x;
+                internal_upper[3 * i + 1] = hi.y;
+                internal_upper[3 * i + 2] = hi.z;
             }
         }
         return int(PBGB_OK);

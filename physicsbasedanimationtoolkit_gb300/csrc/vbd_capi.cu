@@ -268,6 +268,7 @@ class VbdSystem
     // incStiff[k] = (b0, b1, b2, kappa_o) and incPack[k].y = sigma.  Host copies of the incidence
     // words and neighbour slots let pbgb_vbd_set_material rebuild them.
     DeviceArray<float4> incStiff;
+    static constexpr int kIncidenceRecordBytes = int(sizeof(float4) + sizeof(uint2));
     std::vector<uint32_t> hostInc, hostSlots;
     DeviceArray<double> red, gradBuf, objPartials;
 
@@ -337,12 +338,13 @@ class VbdSystem
     bool persistent = true;
     struct PersistentPlan
     {
-        int32_t iters = -1, sub = -1, lanes = 0, block = 0, tile = 0;
+        int32_t iters = -1, sub = -1, lanes = 0, block = 0, tile = 0, wavesAsked = -1;
         float dt      = 0.f;
-        int32_t nItems = 0, grid = 0;
+        int32_t nItems = 0, grid = 0, waves = 0;
         size_t smem = 0;
     } plan;
-    int32_t batchTile = 1; // sub-tiles of blockDim / lanes vertices per sweep item
+    int32_t batchTile  = 1; // sub-tiles of blockDim / lanes vertices per sweep item
+    int32_t batchWaves = 0; // groups of meshes stepped one after the other (0: from the L2 size)
     long long batchWaitNs = kBatchWaitNs;
     int32_t batchPoison   = -1;
     DeviceArray<BatchItemWords> batchItems;
@@ -354,6 +356,7 @@ class VbdSystem
     float gDt = -1.f;
     int32_t gIters = -1, gSub = -1;
     bool graphValid = false;
+    int64_t graphKernels = -1; // kernel nodes of the step graph last captured
 
     ~VbdSystem()
     {
@@ -1329,31 +1332,76 @@ class VbdSystem
                !profiling;
     }
 
-    // Work items of the persistent step for (iterations, substeps) and the current launch shape,
-    // in stage-time order (substep, then begin / iteration and colour / end), meshes in order inside
-    // a stage, tiles in order inside a mesh; each item records how many of its mesh's items must be
-    // complete first.  Built and uploaded outside any stream capture.  Returns false when the batch
-    // cannot run persistently with this launch (the colour-launch path is used then).
+    // Work items of the persistent step for (iterations, substeps) and the current launch shape.
+    // The meshes are split into waves of consecutive meshes with about equal vertex counts; wave
+    // after wave, in stage order (substep, then begin / iteration and colour / end), meshes in order
+    // inside a stage, tiles in order inside a mesh; each item records how many of its mesh's items
+    // must be complete first.  A wave's positions are re-read by every colour of its meshes while
+    // that colour's incidence records stream through L2 once: waves keep the positions of the meshes
+    // in flight, plus one stage's records, within half of L2 (automatic count), but no smaller than
+    // the resident threads can fill.  Built and uploaded outside any stream capture.  Returns false
+    // when the batch cannot run persistently with this launch (the colour-launch path is used then).
     bool preparePersistent(int32_t iterations, int32_t substeps)
     {
         int const L = lanesToUse();
         int const B = std::min(block, 256);
         if (plan.iters == iterations && plan.sub == substeps && plan.lanes == L && plan.block == B &&
-            plan.tile == batchTile)
+            plan.tile == batchTile && plan.wavesAsked == batchWaves)
             return plan.grid > 0;
-        plan       = PersistentPlan{};
-        plan.iters = iterations;
-        plan.sub   = substeps;
-        plan.lanes = L;
-        plan.block = B;
-        plan.tile  = batchTile;
+        plan            = PersistentPlan{};
+        plan.iters      = iterations;
+        plan.sub        = substeps;
+        plan.lanes      = L;
+        plan.block      = B;
+        plan.tile       = batchTile;
+        plan.wavesAsked = batchWaves;
         int const per = B / L;
         if (per < 1 || B % 32 != 0)
             return false;
         int const tileE = per * batchTile, tileV = 4 * B;
+        // Shared memory of the largest sweep tile.
+        size_t smem = 0;
+        for (int32_t b = 0; b < nMeshes; ++b)
+            for (int32_t c = 0; c < nColors; ++c)
+                for (int32_t f = meshSolve[b][2 * c]; f < meshSolve[b][2 * c + 1]; f += tileE)
+                {
+                    int32_t const e = std::min(f + tileE, meshSolve[b][2 * c + 1]);
+                    for (int32_t g = f; g < e; g += per)
+                        smem = std::max(smem, size_t(hostNbrPtr[std::min(g + per, e)] - hostNbrPtr[g]) * kStagedSlotBytes);
+                }
+        if (smem > kStagedMaxBytes)
+            return false;
+        bool const cheb = acceleration == PBGB_ACCEL_CHEBYSHEV;
+        int const perSM = batched_step_blocks_per_sm(L, B, smem, cheb);
+        if (perSM < 1)
+            return false;
+        int sms = 0, l2 = 0;
+        check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
+        check(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, device), "cudaDeviceGetAttribute");
+        int32_t waves = batchWaves;
+        if (waves <= 0)
+        {
+            double const colours  = std::max(nColors, 1);
+            double const stage    = 16.0 * double(nV) + double(kIncidenceRecordBytes) * double(hostInc.size()) / colours;
+            double const resident = double(sms) * perSM * B;
+            double const fill     = std::floor(double(nFree) * L / colours / std::max(resident, 1.0));
+            double const cache    = std::ceil(stage / std::max(0.5 * double(l2), 1.0));
+            waves                 = int32_t(std::max(1.0, std::min(cache, fill)));
+        }
+        waves = std::max(1, std::min(waves, nMeshes));
+        // Wave w holds meshes [wave[w], wave[w + 1]): cut where the running vertex count passes
+        // w / waves of the total.
+        std::vector<int32_t> wave(1, 0);
+        for (int32_t b = 0, w = 1; b < nMeshes && w < waves; ++b)
+            if (int64_t(meshV0[b + 1]) * waves >= int64_t(nV) * w)
+            {
+                if (b + 1 > wave.back() && b + 1 < nMeshes)
+                    wave.push_back(b + 1);
+                ++w;
+            }
+        wave.push_back(nMeshes);
         std::vector<BatchItemWords> items;
         std::vector<int32_t> count(size_t(nMeshes), 0);
-        size_t smem = 0;
         auto emit = [&](int32_t b, int kind, int32_t k, int32_t lo, int32_t hi, int32_t step) {
             int32_t const need = count[b];
             for (int32_t f = lo; f < hi; f += step)
@@ -1361,30 +1409,25 @@ class VbdSystem
                 int32_t const e = std::min(f + step, hi);
                 items.push_back(BatchItemWords{make_int4(b, kind | (k << 2), f, e), make_int4(need, 0, 0, 0)});
                 ++count[b];
-                if (kind == kBatchSweep)
-                    for (int32_t g = f; g < e; g += per)
-                        smem = std::max(smem, size_t(hostNbrPtr[std::min(g + per, e)] - hostNbrPtr[g]) * kStagedSlotBytes);
             }
         };
-        for (int32_t s = 0; s < substeps; ++s)
+        for (size_t w = 0; w + 1 < wave.size(); ++w)
         {
-            for (int32_t b = 0; b < nMeshes; ++b)
-                emit(b, kBatchBegin, 0, meshV0[b], meshV0[b + 1], tileV);
-            for (int32_t k = 0; k < iterations; ++k)
-                for (int32_t c = 0; c < nColors; ++c)
-                    for (int32_t b = 0; b < nMeshes; ++b)
-                        emit(b, kBatchSweep, k, meshSolve[b][2 * c], meshSolve[b][2 * c + 1], tileE);
-            for (int32_t b = 0; b < nMeshes; ++b)
-                emit(b, kBatchEnd, 0, meshV0[b], meshV0[b + 1], tileV);
+            int32_t const b0 = wave[w], b1 = wave[w + 1];
+            for (int32_t s = 0; s < substeps; ++s)
+            {
+                for (int32_t b = b0; b < b1; ++b)
+                    emit(b, kBatchBegin, 0, meshV0[b], meshV0[b + 1], tileV);
+                for (int32_t k = 0; k < iterations; ++k)
+                    for (int32_t c = 0; c < nColors; ++c)
+                        for (int32_t b = b0; b < b1; ++b)
+                            emit(b, kBatchSweep, k, meshSolve[b][2 * c], meshSolve[b][2 * c + 1], tileE);
+                for (int32_t b = b0; b < b1; ++b)
+                    emit(b, kBatchEnd, 0, meshV0[b], meshV0[b + 1], tileV);
+            }
         }
-        if (items.size() > size_t(INT32_MAX) || smem > kStagedMaxBytes)
+        if (items.size() > size_t(INT32_MAX))
             return false;
-        bool const cheb = acceleration == PBGB_ACCEL_CHEBYSHEV;
-        int const perSM = batched_step_blocks_per_sm(L, B, smem, cheb);
-        if (perSM < 1)
-            return false;
-        int sms = 0;
-        check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
         check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
         batchItems.allocate(std::max<size_t>(items.size(), 1));
         if (!items.empty())
@@ -1402,6 +1445,7 @@ class VbdSystem
         check(cudaMemcpy(batchOmega.get(), om.data(), sizeof(float) * om.size(), cudaMemcpyHostToDevice), "H2D");
         plan.nItems = int32_t(items.size());
         plan.smem   = smem;
+        plan.waves  = int32_t(wave.size()) - 1;
         plan.grid   = int32_t(std::min<int64_t>(int64_t(perSM) * sms, std::max<int64_t>(plan.nItems, 1)));
         return true;
     }
@@ -1917,12 +1961,17 @@ class VbdSystem
                                       6 * std::max<int64_t>(0, int64_t(iterations) - 2));
         if (contact)
         {
-            // predict, vertex and triangle boxes, Morton, 4 x (count, scan, scatter), Karras, leaf
-            // gather, internal boxes, overlaps, compaction; then 5 per update (refit: triangle
-            // boxes and internal boxes, the nn reset, the nearest query, the contact records) and 4
-            // at finalize.
+            // Kernels only (memsets are not counted): the prediction; unless the contact mesh is
+            // empty, the vertex and triangle boxes, the LBVH build, the active-set initialization
+            // and its compaction; per update the refit (triangle boxes, internal boxes), the
+            // nearest query and the contact records; at finalize the refit and the nearest query.
             int64_t const updates = (substeps + activeSetFreq - 1) / activeSetFreq;
-            n += 21 + 5 * updates + 4;
+            n += 1;
+            if (cmesh.nF > 0 && cmesh.nSurfV > 0)
+            {
+                int64_t const refitK = 1 + bvh_refit_kernels(cmesh.nF);
+                n += 2 + bvh_build_kernels(cmesh.nF) + 2 + updates * (refitK + 2) + refitK + 1;
+            }
         }
         return n;
     }
@@ -1980,6 +2029,7 @@ class VbdSystem
                 throw;
             }
             check(cudaStreamEndCapture(stream, &g), "cudaStreamEndCapture");
+            graphKernels        = countKernelNodes(g);
             cudaError_t const e = cudaGraphInstantiate(&graph, g, 0);
             cudaGraphDestroy(g);
             check(e, "cudaGraphInstantiate");
@@ -1990,6 +2040,26 @@ class VbdSystem
         }
         check(cudaGraphLaunch(graph, stream), "cudaGraphLaunch");
         trLogEntries = trustLinear() ? iterations * substeps : 0;
+    }
+
+    // Kernel nodes of a captured graph (the step's graphs hold no child or conditional graphs).
+    static int64_t countKernelNodes(cudaGraph_t g)
+    {
+        size_t count = 0;
+        if (cudaGraphGetNodes(g, nullptr, &count) != cudaSuccess)
+            return -1;
+        std::vector<cudaGraphNode_t> nodes(count);
+        if (count > 0 && cudaGraphGetNodes(g, nodes.data(), &count) != cudaSuccess)
+            return -1;
+        int64_t kernels = 0;
+        for (size_t i = 0; i < count; ++i)
+        {
+            cudaGraphNodeType type;
+            if (cudaGraphNodeGetType(nodes[i], &type) != cudaSuccess)
+                return -1;
+            kernels += type == cudaGraphNodeTypeKernel ? 1 : 0;
+        }
+        return kernels;
     }
 
     // Project-written autotuner: times one replayed step per candidate (lanes per vertex x block
@@ -2769,6 +2839,25 @@ PBGB_API int pbgb_vbd_set_batch_tile(pbgb_vbd* h, int32_t subtiles)
     return kOk;
 }
 
+PBGB_API int pbgb_vbd_set_batch_waves(pbgb_vbd* h, int32_t waves)
+{
+    if (!h)
+        return fail(nullptr, kInvalid, "null handle");
+    if (waves < 0 || waves > 65536)
+        return fail(h, kInvalid, "pbgb_vbd_set_batch_waves: expected 0 <= waves <= 65536");
+    h->sys.batchWaves = waves;
+    h->sys.invalidate();
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_batch_waves(pbgb_vbd* h, int32_t* waves)
+{
+    if (!h || !waves)
+        return fail(h, kInvalid, "null argument");
+    *waves = h->sys.plan.grid > 0 ? h->sys.plan.waves : 0;
+    return kOk;
+}
+
 PBGB_API int pbgb_debug_batched_wait(pbgb_vbd* h, int64_t wait_ns, int32_t poison_item)
 {
     if (!h)
@@ -2842,6 +2931,14 @@ PBGB_API int pbgb_vbd_launches_per_step(pbgb_vbd* h, int32_t iterations, int32_t
     if (!h || !launches)
         return fail(h, kInvalid, "null argument");
     *launches = h->sys.launchesPerStep(iterations, substeps);
+    return kOk;
+}
+
+PBGB_API int pbgb_vbd_step_graph_kernels(pbgb_vbd* h, int64_t* kernels)
+{
+    if (!h || !kernels)
+        return fail(h, kInvalid, "null argument");
+    *kernels = h->sys.graphKernels;
     return kOk;
 }
 

@@ -121,6 +121,18 @@ class BatchedIntegrator(IntegratorBase):
         self._batch_tile = int(subtiles)
 
     @property
+    def batch_waves(self):
+        """Groups of meshes the last planned persistent step ran one after the other (0 before)."""
+        w = C.c_int32()
+        _capi.check(_capi.lib().pbgb_vbd_batch_waves(self._h, C.byref(w)), self._h)
+        return w.value
+
+    @batch_waves.setter
+    def batch_waves(self, waves):
+        """Step the meshes in ``waves`` groups, one after the other (0: chosen from the L2 size)."""
+        _capi.check(_capi.lib().pbgb_vbd_set_batch_waves(self._h, int(waves)), self._h)
+
+    @property
     def x(self):
         return self._get("x")
 
