@@ -339,8 +339,6 @@ def run_batch(args, pbat, _capi, torch, with_single=True):
     meshes, datas = batch_workload(args, pbat)
     dt, iters = 1 / 60, args.batch_iterations
     B = pbat.gpu.vbd.BatchedIntegrator(datas)
-    if args.waves is not None:
-        B.batch_waves = args.waves
     if args.lanes:
         # A fixed launch (profiling runs launch exactly what a timed run launched, without the
         # autotuner's candidates).
@@ -377,7 +375,6 @@ def run_batch(args, pbat, _capi, torch, with_single=True):
         "n_tets": int(B.n_tets),
         "n_free_vertices": int(n_free),
         "persistent": bool(B.persistent),
-        "waves": int(B.batch_waves),
         "batched_value": n_free * iters * args.steps / t_batched,
         "batched_ms_per_step": 1e3 * t_batched / args.steps,
         "autotuned": {"lanes": lanes, "block": block, "ms_per_step": tuned_ms},
@@ -428,7 +425,9 @@ def run_adjoint(args, pbat, torch):
     tets), per-tet log E ~ N(log 1e6, 0.3^2), nu 0.45, 30 steps of 20 iterations at dt = 1/60, the
     reference Data's default initial guess (AdaptivePbat), loss on the 121 tip vertices;
     checkpoints every 5 steps.  Forward = the rollout (graph-replayed steps plus checkpoint
-    copies), backward = re-recording each segment and reversing it.  Both are timed with CUDA
+    copies, the last segment recorded), backward = re-recording every other segment and reversing
+    all of them.  `taped`: the same with the whole rollout recorded in the forward pass
+    (checkpoint_every = 30; 153 MB of tape), so backward only reverses.  Both are timed with CUDA
     events on the integrator's stream, where all of their device work runs (the host's launch gaps
     included); the host clock around a synchronize is reported beside them."""
     from physicsbasedanimationtoolkit_gb300 import _capi, meshgen
@@ -449,46 +448,48 @@ def run_adjoint(args, pbat, torch):
     v0 = torch.zeros_like(x0, requires_grad=True)
     tip = torch.tensor(w["tip"], device="cuda")
     target = torch.tensor(w["target"], dtype=torch.float32, device="cuda")
-    fwd, bwd, fwd_host, bwd_host = [], [], [], []
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-    for k in range(args.warmup + args.steps):
-        logE.grad = None
-        x0.grad = None
-        v0.grad = None
-        E = torch.exp(logE)
-        mu = E / (2 * (1 + nu))
-        lam = E * nu / ((1 + nu) * (1 - 2 * nu))
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ev[0].record(stream)
-        xT, _ = pbat.gpu.vbd.rollout(I, mu, lam, x0, v0, dt=dt, iterations=iters, steps=steps, checkpoint_every=every)
-        ev[1].record(stream)
-        loss = ((xT[tip] - target) ** 2).sum()
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        ev[2].record(stream)
-        loss.backward()
-        ev[3].record(stream)
-        torch.cuda.synchronize()
-        t2 = time.perf_counter()
-        if k >= args.warmup:
-            fwd.append(ev[0].elapsed_time(ev[1]))
-            bwd.append(ev[2].elapsed_time(ev[3]))
-            fwd_host.append(1e3 * (t1 - t0))
-            bwd_host.append(1e3 * (t2 - t1))
-    f, b = float(np.median(fwd)), float(np.median(bwd))
-    return {
-        "workload": "beam [0,4]x[0,1]^2 40x10x10 hexes x 6 tets, log E ~ N(log 1e6, 0.3^2), nu 0.45, "
-                    "30 steps x 20 iterations, dt 1/60, AdaptivePbat initial guess, tip-face loss, checkpoints every 5 steps",
-        "fwd_ms": f,
-        "bwd_ms": b,
-        "bwd_over_fwd": b / f,
-        "host_fwd_ms": float(np.median(fwd_host)),
-        "host_bwd_ms": float(np.median(bwd_host)),
-        "loss": float(loss.detach()),
-        "grad_norms": {"log_E": float(logE.grad.norm()), "v0": float(v0.grad.norm()), "x0": float(x0.grad.norm())},
-        "timing": "CUDA events on the integrator's stream around the rollout and around backward, median of the timed repetitions",
-    }
+    def timed(every):
+        fwd, bwd, fwd_host, bwd_host = [], [], [], []
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        for k in range(args.warmup + args.steps):
+            logE.grad = None
+            x0.grad = None
+            v0.grad = None
+            E = torch.exp(logE)
+            mu = E / (2 * (1 + nu))
+            lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ev[0].record(stream)
+            xT, _ = pbat.gpu.vbd.rollout(I, mu, lam, x0, v0, dt=dt, iterations=iters, steps=steps, checkpoint_every=every)
+            ev[1].record(stream)
+            loss = ((xT[tip] - target) ** 2).sum()
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            ev[2].record(stream)
+            loss.backward()
+            ev[3].record(stream)
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            if k >= args.warmup:
+                fwd.append(ev[0].elapsed_time(ev[1]))
+                bwd.append(ev[2].elapsed_time(ev[3]))
+                fwd_host.append(1e3 * (t1 - t0))
+                bwd_host.append(1e3 * (t2 - t1))
+        f, b = float(np.median(fwd)), float(np.median(bwd))
+        return {"checkpoint_every": every, "fwd_ms": f, "bwd_ms": b, "bwd_over_fwd": b / f,
+                "host_fwd_ms": float(np.median(fwd_host)), "host_bwd_ms": float(np.median(bwd_host)),
+                "loss": float(loss.detach()),
+                "grad_norms": {"log_E": float(logE.grad.norm()), "v0": float(v0.grad.norm()),
+                               "x0": float(x0.grad.norm())}}
+
+    out = timed(every)
+    out["taped"] = timed(steps)
+    out["workload"] = ("beam [0,4]x[0,1]^2 40x10x10 hexes x 6 tets, log E ~ N(log 1e6, 0.3^2), nu 0.45, "
+                       "30 steps x 20 iterations, dt 1/60, AdaptivePbat initial guess, tip-face loss, checkpoints every 5 steps")
+    out["timing"] = ("CUDA events on the integrator's stream around the rollout and around backward, median of the "
+                     "timed repetitions")
+    return out
 
 
 def run_accelerated(args, pbat, torch, kind):
@@ -849,9 +850,6 @@ def main():
     ap.add_argument("--nz", type=int, default=40)
     ap.add_argument("--lanes", type=int, default=0, help="headline and --only batch: lanes per vertex instead of autotuning")
     ap.add_argument("--block", type=int, default=0, help="headline with --lanes: block size (default 256)")
-    ap.add_argument("--waves", type=int, default=None,
-                    help="headline and --only batch: groups of meshes stepped one after the other (default: the "
-                         "integrator's choice from the L2 size)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-beam", dest="beam", action="store_false", default=True,
                     help="skip the single large beam (Chebyshev, 50 iterations) leg")
@@ -917,8 +915,6 @@ def main():
     dt, iters = 1 / 60, args.batch_iterations
     B = pbat.gpu.vbd.BatchedIntegrator(datas)
     h = B.handle
-    if args.waves is not None:
-        B.batch_waves = args.waves
     if args.lanes:
         B.lanes_per_vertex = args.lanes
         if args.block:
@@ -981,7 +977,6 @@ def main():
     e2e_value = group.sum(updates_per_step * e2e_steps) / e2e_s
     io_bytes = nV * 3 * 4 * 2
     persistent = B.persistent
-    waves = B.batch_waves
     lanes_used = B.lanes_per_vertex
     del B, flush
     torch.cuda.empty_cache()
@@ -995,8 +990,7 @@ def main():
         achieved = bytes_per_step / max(launches_per_step, 1) / (avg_launch_ms * 1e-3) / 1e9
         traffic, traffic_basis = traffic_from_profiles("batched_step_cfg3.md")
         launch_config = {"autotuned": tuned is not None, "lanes": lanes_used,
-                         "block": tuned["block"] if tuned else (args.block or 256), "persistent": persistent,
-                         "waves": waves}
+                         "block": tuned["block"] if tuned else (args.block or 256), "persistent": persistent}
         single = run_single_launch(args, pbat, _capi, torch, meshes, datas, launch_config)
         cpu = None if args.no_cpu_baseline else cpu_baseline(meshes, iters)
         beam = run_beam(args, pbat, _capi, torch) if args.beam else None

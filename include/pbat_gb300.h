@@ -273,18 +273,10 @@ PBGB_API int pbgb_vbd_sweep_timing(pbgb_vbd* h, double* milliseconds, int64_t* s
  * synchronizing call return PBGB_ERR_TIMEOUT).  Used for plain VBD and Chebyshev without contact
  * when every colour's neighbours fit in shared memory; otherwise, or when disabled, a batch steps
  * with one launch per colour.  pbgb_vbd_persistent reports whether the next step uses it.
- * pbgb_vbd_set_batch_tile: sweep work items of subtiles x (block / lanes) vertices (default 1).
- * pbgb_vbd_set_batch_waves: step the meshes in `waves` groups of consecutive meshes with about
- * equal vertex counts, one group after the other inside the launch, so that the positions of the
- * meshes in flight stay in L2 while their incidence records stream (0, the default: the count
- * that keeps a group's positions and one colour's records within half of L2 without leaving
- * resident threads idle).  pbgb_vbd_batch_waves reports the count the last planned step used (0
- * when no persistent step was planned).  Neither changes the results. */
+ * pbgb_vbd_set_batch_tile: sweep work items of subtiles x (block / lanes) vertices (default 1). */
 PBGB_API int pbgb_vbd_set_persistent(pbgb_vbd* h, int32_t enable);
 PBGB_API int pbgb_vbd_persistent(pbgb_vbd* h, int32_t* active);
 PBGB_API int pbgb_vbd_set_batch_tile(pbgb_vbd* h, int32_t subtiles);
-PBGB_API int pbgb_vbd_set_batch_waves(pbgb_vbd* h, int32_t waves);
-PBGB_API int pbgb_vbd_batch_waves(pbgb_vbd* h, int32_t* waves);
 /* The handle's CUDA stream (cudaStream_t) so callers can order their own work after a step. */
 PBGB_API int pbgb_vbd_stream(pbgb_vbd* h, void** stream);
 

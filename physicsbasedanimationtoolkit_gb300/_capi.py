@@ -126,8 +126,6 @@ _SIGNATURES = [
     ("pbgb_vbd_set_persistent", C.c_int, [_vp, _i32]),
     ("pbgb_vbd_persistent", C.c_int, [_vp, C.POINTER(_i32)]),
     ("pbgb_vbd_set_batch_tile", C.c_int, [_vp, _i32]),
-    ("pbgb_vbd_set_batch_waves", C.c_int, [_vp, _i32]),
-    ("pbgb_vbd_batch_waves", C.c_int, [_vp, C.POINTER(_i32)]),
     ("pbgb_debug_batched_wait", C.c_int, [_vp, C.c_int64, _i32]),
     ("pbgb_vbd_set_scene_bounding_box", C.c_int, [_vp, _vp, _vp]),
     ("pbgb_vbd_sizes", C.c_int, [_vp, _vp, _vp, _vp, _vp]),

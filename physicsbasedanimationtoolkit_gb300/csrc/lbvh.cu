@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     }
 }
 
-// --- hierarchy --------------------------------------------------------------------------------
+// --- Karras hierarchy (gpu/impl/geometry/Bvh.cu:24-114) -------------------------------------------
 
 // The sorted keys (code, index): prefix lengths of the binary radix tree over them.
 struct SortedKeys
@@ -304,6 +304,50 @@ struct SortedKeys
         return __clz(a ^ b);
     }
 };
+
+__global__ void karras_kernel(SortedKeys K, int32_t* __restrict__ child, int32_t* __restrict__ parent, int32_t* __restrict__ rightmost, int32_t* __restrict__ first)
+{
+    int32_t const i = blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t const n = K.n;
+    if (i >= n - 1)
+        return;
+    int32_t const leafBegin = n - 1;
+    // Direction of the range and a lower bound on its common prefix.
+    int32_t const d    = (K.delta(i, i + 1) - K.delta(i, i - 1)) > 0 ? 1 : -1;
+    int const dmin     = K.delta(i, i - d);
+    int32_t lmax       = 2;
+    while (K.delta(i, i + lmax * d) > dmin)
+        lmax <<= 1;
+    int32_t l = 0;
+    do
+    {
+        lmax >>= 1;
+        if (K.delta(i, i + (l + lmax) * d) > dmin)
+            l += lmax;
+    } while (lmax > 1);
+    int32_t const j   = i + l * d;
+    int const dnode   = K.delta(i, j);
+    int32_t s         = 0;
+    int32_t t         = l;
+    do
+    {
+        t = (t + 1) >> 1;
+        if (K.delta(i, i + (s + t) * d) > dnode)
+            s += t;
+    } while (t > 1);
+    int32_t const gamma = i + s * d + (d < 0 ? d : 0);
+    int32_t const lo    = i < j ? i : j;
+    int32_t const hi    = i < j ? j : i;
+    int32_t const lc    = lo == gamma ? leafBegin + gamma : gamma;
+    int32_t const rc    = hi == gamma + 1 ? leafBegin + gamma + 1 : gamma + 1;
+    child[2 * i]         = lc;
+    child[2 * i + 1]     = rc;
+    parent[lc]           = i;
+    parent[rc]           = i;
+    rightmost[2 * i]     = leafBegin + gamma;
+    rightmost[2 * i + 1] = leafBegin + hi;
+    first[i]             = lo;
+}
 
 __device__ __forceinline__ float4 fmin4(float4 a, float4 b)
 {
@@ -330,8 +374,7 @@ __device__ __forceinline__ void acquire_fence()
     asm volatile("fence.acq_rel.gpu;" ::: "memory");
 }
 
-// Leaf boxes in sorted order and the bottom-up internal boxes over a built hierarchy, the refit
-// (gpu/impl/geometry/Bvh.cu:175-229; the build's own boxes come from hierarchy_kernel below).
+// Leaf boxes in sorted order and the bottom-up internal boxes (gpu/impl/geometry/Bvh.cu:175-229).
 // Thread s gathers leaf s's box, writes the leaf's record, then climbs: the first thread to reach a
 // node stops; the second unites the box it carries in registers with its sibling's record (written
 // by the first thread before its counter update) and continues.  Min and max are exact and
@@ -406,114 +449,6 @@ __global__ void __launch_bounds__(kBoxLeaves, 2) boxes_kernel(int32_t n, BvhBuff
     }
     if (k == 64 && p >= 0)
         atomicOr(B.flags, kBvhErrDepth);
-}
-
-// Hierarchy and boxes in one bottom-up pass (the reference builds the hierarchy top-down, one
-// thread per internal node searching its range, gpu/impl/geometry/Bvh.cu:24-114, then the boxes,
-// :175-229).  The binary radix tree over the sorted keys is unique, so it can be grown from the
-// leaves: a node [lo, hi] is the left child of its parent when its right neighbour shares the
-// longer prefix with it (delta(hi, hi + 1) > delta(lo - 1, lo)), and the parent's split is then hi,
-// else lo - 1.  The reference's node numbering follows from that side: a left child is numbered by
-// its last leaf, a right child by its first, the root (the whole range) is 0; leaves are n - 1 + s.
-// So the thread that goes on from a node knows its number when it takes the node's next step, and
-// writes its record, links (child, parent of both children, rightmost, first) there.
-//
-// Arrivals meet at the parent's split gamma: the first thread stops, the second finds its sibling
-// from the keys alone (the sibling across gamma is internal iff its next key shares more than
-// the parent's prefix; an internal right sibling is numbered gamma + 1 and its last leaf is in its
-// rightmost link, an internal left sibling is numbered gamma and its first leaf is in first[]),
-// reads the sibling's box from its record and unites it with its own.  A parent whose range lies
-// inside the block's leaves [L, R] (keys L - 1 and R + 1 share less than the parent's prefix with
-// the far side of gamma) meets on a shared-memory counter with block-scope fences; any other on a
-// device-scope counter (splits[gamma]) with a releasing add and an acquire.  Both children decide
-// the same way from gamma, and a parent that crosses the block has only ancestors that do.
-__global__ void __launch_bounds__(kBoxLeaves, 2) hierarchy_kernel(int32_t n, BvhBuffers B, float4 const* __restrict__ lo, float4 const* __restrict__ hi)
-{
-    __shared__ int32_t arrivals[kBoxLeaves];
-    int32_t const L = int32_t(blockIdx.x) * kBoxLeaves;
-    int32_t const R = min(L + kBoxLeaves, n) - 1;
-    arrivals[threadIdx.x] = 0;
-    __syncthreads();
-    int32_t const s = L + int32_t(threadIdx.x);
-    if (s > R)
-        return;
-    SortedKeys const K{B.codes, n};
-    int32_t const leafBegin = n - 1;
-    int32_t const i         = B.inds[s];
-    float4 bl               = lo[i];
-    float4 bh               = hi[i];
-    int32_t node            = leafBegin + s;
-    B.nodes[2 * size_t(node)]     = make_float4(bl.x, bl.y, bl.z, __int_as_float(i));
-    B.nodes[2 * size_t(node) + 1] = make_float4(bh.x, bh.y, bh.z, __int_as_float(-1));
-    if (n == 1)
-        return;
-    int32_t first = s, last = s;      // the current node's leaves
-    int32_t c0 = -1, c1 = -1, split = -1; // its children and split (internal nodes)
-    bool local = true;
-    int k      = 0;
-    for (; k < 64; ++k)
-    {
-        bool const leftChild = K.delta(last, last + 1) > K.delta(first - 1, first);
-        if (k > 0)
-        {
-            node                          = leftChild ? last : first; // the root: first = 0
-            B.nodes[2 * size_t(node)]     = make_float4(bl.x, bl.y, bl.z, __int_as_float(c0));
-            B.nodes[2 * size_t(node) + 1] = make_float4(bh.x, bh.y, bh.z, __int_as_float(c1));
-            reinterpret_cast<int2*>(B.child)[node]     = make_int2(c0, c1);
-            reinterpret_cast<int2*>(B.rightmost)[node] = make_int2(leafBegin + split, leafBegin + last);
-            B.first[node]                              = first;
-            B.parent[c0]                               = node;
-            B.parent[c1]                               = node;
-            B.visits[node]                             = 2; // its builder is its second arrival
-            if (first == 0 && last == n - 1)
-                return;
-        }
-        int32_t const gamma = leftChild ? last : first - 1;
-        int const dp        = K.delta(gamma, gamma + 1);
-        if (local)
-            local = (R + 1 >= n || K.delta(gamma, R + 1) < dp) && (L == 0 || K.delta(L - 1, gamma + 1) < dp);
-        if (local)
-        {
-            __threadfence_block(); // this node's record and links before the arrival
-            if (atomicAdd(&arrivals[gamma - L], 1) == 0)
-                return;
-            __threadfence_block(); // the sibling's after its arrival
-        }
-        else
-        {
-            if (atomic_add_release(&B.splits[gamma], 1) == 0)
-                return;
-            acquire_fence();
-        }
-        // The sibling's record and links: written in this block (plain loads after the block-scope
-        // fence) or possibly in another (loads from L2 after the acquire).
-        int32_t sib;
-        if (leftChild)
-        {
-            bool const internal = K.delta(gamma + 1, gamma + 2) > dp;
-            sib                 = internal ? gamma + 1 : leafBegin + gamma + 1;
-            int32_t const* q    = B.rightmost + 2 * (gamma + 1) + 1;
-            last                = internal ? (local ? *q : __ldcg(q)) - leafBegin : gamma + 1;
-            c0                  = node;
-            c1                  = sib;
-        }
-        else
-        {
-            bool const internal = K.delta(gamma - 1, gamma) > dp;
-            sib                 = internal ? gamma : leafBegin + gamma;
-            int32_t const* q    = B.first + gamma;
-            first               = internal ? (local ? *q : __ldcg(q)) : gamma;
-            c0                  = sib;
-            c1                  = node;
-        }
-        float4 const* r = B.nodes + 2 * size_t(sib);
-        float4 const sl = local ? r[0] : __ldcg(r);
-        float4 const sh = local ? r[1] : __ldcg(r + 1);
-        bl              = fmin4(bl, sl);
-        bh              = fmax4(bh, sh);
-        split           = gamma;
-    }
-    atomicOr(B.flags, kBvhErrDepth);
 }
 
 __device__ __forceinline__ bool boxes_overlap(float4 const& l1, float4 const& u1, float4 const& l2, float4 const& u2)
@@ -714,8 +649,8 @@ int64_t bvh_build_kernels(int32_t n)
             total = nb;
         }
     };
-    // Morton, 4 x (count, scan, scatter), hierarchy.
-    return 1 + 4 * (2 + scan(radix_counts_size(n))) + 1;
+    // Morton, 4 x (count, scan, scatter), Karras (two or more boxes), boxes.
+    return 1 + 4 * (2 + scan(radix_counts_size(n))) + (n > 1 ? 1 : 0) + 1;
 }
 
 int64_t bvh_refit_kernels(int32_t n)
@@ -750,7 +685,6 @@ cudaError_t bvh_allocate(BvhBuffers& B, int32_t capacity)
     get(B.rightmost, 2 * ni);
     get(B.first, ni);
     get(B.visits, ni);
-    get(B.splits, ni);
     get(B.nodes, 2 * (2 * n - 1));
     get(B.flags, 1);
     if (e == cudaSuccess)
@@ -761,7 +695,7 @@ cudaError_t bvh_allocate(BvhBuffers& B, int32_t capacity)
 void bvh_release(BvhBuffers& B)
 {
     void* ptrs[] = {B.codes, B.codesAlt, B.inds, B.indsAlt, B.counts, B.scanTmp, B.child, B.parent,
-                    B.rightmost, B.first, B.visits, B.splits, B.nodes, B.flags};
+                    B.rightmost, B.first, B.visits, B.nodes, B.flags};
     for (void* p : ptrs)
         if (p)
             cudaFree(p);
@@ -781,13 +715,16 @@ cudaError_t bvh_build(BvhBuffers const& B, int32_t n, float4 const* lo, float4 c
     if (e != cudaSuccess)
         return e;
     // The root has no parent; every other node is the child of exactly one internal node, whose
-    // builder writes its parent.
+    // Karras thread writes its parent.
     if ((e = cudaMemsetAsync(B.parent, 0xFF, sizeof(int32_t), s)) != cudaSuccess)
         return e;
-    if (n > 1 && (e = cudaMemsetAsync(B.splits, 0, sizeof(int32_t) * size_t(n - 1), s)) != cudaSuccess)
-        return e;
-    hierarchy_kernel<<<blocks(n, kBoxLeaves), kBoxLeaves, 0, s>>>(n, B, lo, hi);
-    return cudaGetLastError();
+    if (n > 1)
+    {
+        karras_kernel<<<blocks(n - 1, 256), 256, 0, s>>>(SortedKeys{B.codes, n}, B.child, B.parent, B.rightmost, B.first);
+        if ((e = cudaGetLastError()) != cudaSuccess)
+            return e;
+    }
+    return boxes_impl(B, n, lo, hi, s);
 }
 
 cudaError_t bvh_refit(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, cudaStream_t s)

@@ -268,7 +268,6 @@ class VbdSystem
     // incStiff[k] = (b0, b1, b2, kappa_o) and incPack[k].y = sigma.  Host copies of the incidence
     // words and neighbour slots let pbgb_vbd_set_material rebuild them.
     DeviceArray<float4> incStiff;
-    static constexpr int kIncidenceRecordBytes = int(sizeof(float4) + sizeof(uint2));
     std::vector<uint32_t> hostInc, hostSlots;
     DeviceArray<double> red, gradBuf, objPartials;
 
@@ -338,13 +337,12 @@ class VbdSystem
     bool persistent = true;
     struct PersistentPlan
     {
-        int32_t iters = -1, sub = -1, lanes = 0, block = 0, tile = 0, wavesAsked = -1;
+        int32_t iters = -1, sub = -1, lanes = 0, block = 0, tile = 0;
         float dt      = 0.f;
-        int32_t nItems = 0, grid = 0, waves = 0;
+        int32_t nItems = 0, grid = 0;
         size_t smem = 0;
     } plan;
-    int32_t batchTile  = 1; // sub-tiles of blockDim / lanes vertices per sweep item
-    int32_t batchWaves = 0; // groups of meshes stepped one after the other (0: from the L2 size)
+    int32_t batchTile = 1; // sub-tiles of blockDim / lanes vertices per sweep item
     long long batchWaitNs = kBatchWaitNs;
     int32_t batchPoison   = -1;
     DeviceArray<BatchItemWords> batchItems;
@@ -1332,29 +1330,26 @@ class VbdSystem
                !profiling;
     }
 
-    // Work items of the persistent step for (iterations, substeps) and the current launch shape.
-    // The meshes are split into waves of consecutive meshes with about equal vertex counts; wave
-    // after wave, in stage order (substep, then begin / iteration and colour / end), meshes in order
-    // inside a stage, tiles in order inside a mesh; each item records how many of its mesh's items
-    // must be complete first.  A wave's positions are re-read by every colour of its meshes while
-    // that colour's incidence records stream through L2 once: waves keep the positions of the meshes
-    // in flight, plus one stage's records, within half of L2 (automatic count), but no smaller than
-    // the resident threads can fill.  Built and uploaded outside any stream capture.  Returns false
-    // when the batch cannot run persistently with this launch (the colour-launch path is used then).
+    // Work items of the persistent step for (iterations, substeps) and the current launch shape,
+    // in stage order (substep, then begin / iteration and colour / end), meshes in order inside a
+    // stage, tiles in order inside a mesh; each item records how many of its mesh's items must be
+    // complete first.  Stage order keeps a whole stage of items (every mesh's colour) between two
+    // stages of one mesh, so a block rarely takes an item whose mesh is still on the previous
+    // colour.  Built and uploaded outside any stream capture.  Returns false when the batch cannot
+    // run persistently with this launch (the colour-launch path is used then).
     bool preparePersistent(int32_t iterations, int32_t substeps)
     {
         int const L = lanesToUse();
         int const B = std::min(block, 256);
         if (plan.iters == iterations && plan.sub == substeps && plan.lanes == L && plan.block == B &&
-            plan.tile == batchTile && plan.wavesAsked == batchWaves)
+            plan.tile == batchTile)
             return plan.grid > 0;
-        plan            = PersistentPlan{};
-        plan.iters      = iterations;
-        plan.sub        = substeps;
-        plan.lanes      = L;
-        plan.block      = B;
-        plan.tile       = batchTile;
-        plan.wavesAsked = batchWaves;
+        plan       = PersistentPlan{};
+        plan.iters = iterations;
+        plan.sub   = substeps;
+        plan.lanes = L;
+        plan.block = B;
+        plan.tile  = batchTile;
         int const per = B / L;
         if (per < 1 || B % 32 != 0)
             return false;
@@ -1375,31 +1370,8 @@ class VbdSystem
         int const perSM = batched_step_blocks_per_sm(L, B, smem, cheb);
         if (perSM < 1)
             return false;
-        int sms = 0, l2 = 0;
+        int sms = 0;
         check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
-        check(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, device), "cudaDeviceGetAttribute");
-        int32_t waves = batchWaves;
-        if (waves <= 0)
-        {
-            double const colours  = std::max(nColors, 1);
-            double const stage    = 16.0 * double(nV) + double(kIncidenceRecordBytes) * double(hostInc.size()) / colours;
-            double const resident = double(sms) * perSM * B;
-            double const fill     = std::floor(double(nFree) * L / colours / std::max(resident, 1.0));
-            double const cache    = std::ceil(stage / std::max(0.5 * double(l2), 1.0));
-            waves                 = int32_t(std::max(1.0, std::min(cache, fill)));
-        }
-        waves = std::max(1, std::min(waves, nMeshes));
-        // Wave w holds meshes [wave[w], wave[w + 1]): cut where the running vertex count passes
-        // w / waves of the total.
-        std::vector<int32_t> wave(1, 0);
-        for (int32_t b = 0, w = 1; b < nMeshes && w < waves; ++b)
-            if (int64_t(meshV0[b + 1]) * waves >= int64_t(nV) * w)
-            {
-                if (b + 1 > wave.back() && b + 1 < nMeshes)
-                    wave.push_back(b + 1);
-                ++w;
-            }
-        wave.push_back(nMeshes);
         std::vector<BatchItemWords> items;
         std::vector<int32_t> count(size_t(nMeshes), 0);
         auto emit = [&](int32_t b, int kind, int32_t k, int32_t lo, int32_t hi, int32_t step) {
@@ -1411,20 +1383,16 @@ class VbdSystem
                 ++count[b];
             }
         };
-        for (size_t w = 0; w + 1 < wave.size(); ++w)
+        for (int32_t s = 0; s < substeps; ++s)
         {
-            int32_t const b0 = wave[w], b1 = wave[w + 1];
-            for (int32_t s = 0; s < substeps; ++s)
-            {
-                for (int32_t b = b0; b < b1; ++b)
-                    emit(b, kBatchBegin, 0, meshV0[b], meshV0[b + 1], tileV);
-                for (int32_t k = 0; k < iterations; ++k)
-                    for (int32_t c = 0; c < nColors; ++c)
-                        for (int32_t b = b0; b < b1; ++b)
-                            emit(b, kBatchSweep, k, meshSolve[b][2 * c], meshSolve[b][2 * c + 1], tileE);
-                for (int32_t b = b0; b < b1; ++b)
-                    emit(b, kBatchEnd, 0, meshV0[b], meshV0[b + 1], tileV);
-            }
+            for (int32_t b = 0; b < nMeshes; ++b)
+                emit(b, kBatchBegin, 0, meshV0[b], meshV0[b + 1], tileV);
+            for (int32_t k = 0; k < iterations; ++k)
+                for (int32_t c = 0; c < nColors; ++c)
+                    for (int32_t b = 0; b < nMeshes; ++b)
+                        emit(b, kBatchSweep, k, meshSolve[b][2 * c], meshSolve[b][2 * c + 1], tileE);
+            for (int32_t b = 0; b < nMeshes; ++b)
+                emit(b, kBatchEnd, 0, meshV0[b], meshV0[b + 1], tileV);
         }
         if (items.size() > size_t(INT32_MAX))
             return false;
@@ -1445,7 +1413,6 @@ class VbdSystem
         check(cudaMemcpy(batchOmega.get(), om.data(), sizeof(float) * om.size(), cudaMemcpyHostToDevice), "H2D");
         plan.nItems = int32_t(items.size());
         plan.smem   = smem;
-        plan.waves  = int32_t(wave.size()) - 1;
         plan.grid   = int32_t(std::min<int64_t>(int64_t(perSM) * sms, std::max<int64_t>(plan.nItems, 1)));
         return true;
     }
@@ -2836,25 +2803,6 @@ PBGB_API int pbgb_vbd_set_batch_tile(pbgb_vbd* h, int32_t subtiles)
         return fail(h, kInvalid, "pbgb_vbd_set_batch_tile: expected 1 <= subtiles <= 64");
     h->sys.batchTile = subtiles;
     h->sys.invalidate();
-    return kOk;
-}
-
-PBGB_API int pbgb_vbd_set_batch_waves(pbgb_vbd* h, int32_t waves)
-{
-    if (!h)
-        return fail(nullptr, kInvalid, "null handle");
-    if (waves < 0 || waves > 65536)
-        return fail(h, kInvalid, "pbgb_vbd_set_batch_waves: expected 0 <= waves <= 65536");
-    h->sys.batchWaves = waves;
-    h->sys.invalidate();
-    return kOk;
-}
-
-PBGB_API int pbgb_vbd_batch_waves(pbgb_vbd* h, int32_t* waves)
-{
-    if (!h || !waves)
-        return fail(h, kInvalid, "null argument");
-    *waves = h->sys.plan.grid > 0 ? h->sys.plan.waves : 0;
     return kOk;
 }
 

@@ -121,18 +121,6 @@ class BatchedIntegrator(IntegratorBase):
         self._batch_tile = int(subtiles)
 
     @property
-    def batch_waves(self):
-        """Groups of meshes the last planned persistent step ran one after the other (0 before)."""
-        w = C.c_int32()
-        _capi.check(_capi.lib().pbgb_vbd_batch_waves(self._h, C.byref(w)), self._h)
-        return w.value
-
-    @batch_waves.setter
-    def batch_waves(self, waves):
-        """Step the meshes in ``waves`` groups, one after the other (0: chosen from the L2 size)."""
-        _capi.check(_capi.lib().pbgb_vbd_set_batch_waves(self._h, int(waves)), self._h)
-
-    @property
     def x(self):
         return self._get("x")
 
@@ -175,6 +163,9 @@ class _Rollout:
                 integ._set_device("x", x.data_ptr())
                 integ._set_device("v", v.data_ptr())
                 checkpoints = []
+                # The last segment is recorded on the way (a recorded step computes exactly what a
+                # plain step does), so backward reverses it without running it again.
+                last = ((steps - 1) // every) * every
                 for t in range(steps):
                     if t % every == 0:
                         cx = torch.empty((nV, 3), dtype=torch.float32, device=dev)
@@ -184,7 +175,10 @@ class _Rollout:
                         integ._get_device("v", cv.data_ptr())
                         integ._get_device("vprev", cp.data_ptr())
                         checkpoints.append((cx, cv, cp))
-                    integ.step(dt, iterations, substeps)
+                    if t >= last:
+                        integ.step_record(dt, iterations, substeps, (t - last) * substeps)
+                    else:
+                        integ.step(dt, iterations, substeps)
                 xT = torch.empty((nV, 3), dtype=torch.float32, device=dev)
                 vT = torch.empty_like(xT)
                 pT = torch.empty_like(xT)
@@ -195,6 +189,7 @@ class _Rollout:
                 ctx.integ = integ
                 ctx.args = (dt, iterations, substeps, steps, every)
                 ctx.checkpoints = checkpoints
+                ctx.taped = True  # the tape holds the last segment until a backward reuses its slots
                 ctx.final = (xT.clone(), vT.clone(), pT)
                 ctx.save_for_backward(mu, lam)
                 return xT, vT
@@ -215,15 +210,18 @@ class _Rollout:
                 dloglambda = torch.zeros_like(dlogmu)
                 integ.adjoint_reserve(min(every, steps) * substeps, iterations)
                 torch.cuda.synchronize(dev)
-                for seg in reversed(range(len(ctx.checkpoints))):
+                nseg = len(ctx.checkpoints)
+                for seg in reversed(range(nseg)):
                     start = seg * every
                     end = min(start + every, steps)
                     cx, cv, cp = ctx.checkpoints[seg]
                     integ._set_device("x", cx.data_ptr())
                     integ._set_device("v", cv.data_ptr())
                     integ._set_device("vprev", cp.data_ptr())
-                    for t in range(start, end):
-                        integ.step_record(dt, iterations, substeps, (t - start) * substeps)
+                    if not (seg == nseg - 1 and ctx.taped):
+                        for t in range(start, end):
+                            integ.step_record(dt, iterations, substeps, (t - start) * substeps)
+                    ctx.taped = False
                     for t in reversed(range(start, end)):
                         integ.step_adjoint((t - start) * substeps, substeps, xbar.data_ptr(), vbar.data_ptr(),
                                            dlogmu.data_ptr(), dloglambda.data_ptr(), pbar.data_ptr())
@@ -247,8 +245,10 @@ def rollout(integrator, mu, lam, x0, v0, dt=0.01, iterations=20, steps=1, subste
     mu, lam: per-tet Lame coefficients (|#tets|, torch tensors; set on the integrator);
     x0, v0: |#vertices| x 3 start positions and velocities (CUDA tensors).  Returns the positions
     and velocities after the last step.  Backward runs the adjoint kernels: the positions are
-    checkpointed every ``checkpoint_every`` steps in the forward pass, and each checkpoint segment
-    is re-run with recording before it is reversed.  The gradient is the exact derivative of the
+    checkpointed every ``checkpoint_every`` steps in the forward pass, the last segment is
+    recorded on the way (the tape holds ``checkpoint_every`` steps), and every other segment is
+    re-run with recording before it is reversed; with ``checkpoint_every >= steps`` the whole
+    rollout is taped in the forward pass and backward re-runs nothing.  The gradient is the exact derivative of the
     computed iterations (FP32).  Supported: plain VBD or Chebyshev acceleration, any Rayleigh
     damping, every initial guess (the adaptive guesses' factor is differentiated on the branch the
     forward took), no contact.  The previous velocities the integrator holds at the start (read by

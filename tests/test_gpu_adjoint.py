@@ -121,6 +121,29 @@ def test_checkpoint_interval_does_not_change_the_gradient():
         assert rel(a, b) <= 1e-3
 
 
+@pytest.mark.parametrize("every", [2, 5])
+def test_a_second_backward_re_records_the_taped_segment(every):
+    """The forward pass tapes its last segment and the first backward reverses it directly; the
+    other segments reuse the tape's slots, so a second backward (retain_graph) records every segment
+    again and must give the same gradients."""
+    w = meshgen.adjoint_beam_workload(nx=8, ny=2, nz=2, seed=4)
+    I = gpu_integrator(w)
+    nu = w["nu"]
+    logE = torch.tensor(w["logE"], dtype=torch.float64, requires_grad=True)
+    E = torch.exp(logE)
+    mu, lam = E / (2 * (1 + nu)), E * nu / ((1 + nu) * (1 - 2 * nu))
+    x0 = torch.tensor(w["X"], dtype=torch.float32, device="cuda", requires_grad=True)
+    v0 = torch.zeros_like(x0, requires_grad=True)
+    xT, _ = pbat.gpu.vbd.rollout(I, mu, lam, x0, v0, dt=1 / 60, iterations=8, steps=5, checkpoint_every=every)
+    L = (xT ** 2).sum()
+    L.backward(retain_graph=True)
+    g1 = (logE.grad.clone(), x0.grad.clone(), v0.grad.clone())
+    logE.grad, x0.grad, v0.grad = None, None, None
+    L.backward()
+    for a, b in zip(g1, (logE.grad, x0.grad, v0.grad)):
+        assert rel(b.cpu().numpy(), a.cpu().numpy()) <= 1e-4
+
+
 def fd_check(w, v0, gE, gv, gx, dt, iters, steps, strategy, directions=32, with_v=True, with_x=False, eps=1e-5):
     rng = np.random.default_rng(20261203)
     ad, fd = [], []

@@ -115,27 +115,3 @@ def test_debug_hook_rejects_out_of_range_limits():
     assert L.pbgb_debug_batched_wait(B.handle, 5_000_000_000, -1) == 1
     assert L.pbgb_debug_batched_wait(B.handle, 1_000_000, -2) == 1
 
-
-@pytest.mark.parametrize("waves", [0, 1, 2, 4, 9])
-def test_mesh_waves_do_not_change_the_positions(waves):
-    """Stepping the meshes in groups, one group after the other inside the launch, changes only
-    the order in which meshes are taken up: the positions equal the colour-launch batch's."""
-    meshes = meshgen.batch_workload(n_meshes=9, nmin=2, nmax=9, seed=5)
-    datas = make_datas(meshes, 0.9)
-    P = pbat.gpu.vbd.BatchedIntegrator(datas)
-    U = pbat.gpu.vbd.BatchedIntegrator(datas)
-    P.batch_waves = waves
-    U.persistent = False
-    for _ in range(3):
-        for I in (P, U):
-            I.step(1 / 60, 6, 2)
-    P.synchronize()
-    assert 1 <= P.batch_waves <= (waves if waves > 0 else 9)
-    np.testing.assert_array_equal(P.x, U.x)
-    np.testing.assert_array_equal(P.v, U.v)
-
-
-def test_batch_waves_rejects_negative_counts():
-    B = pbat.gpu.vbd.BatchedIntegrator(make_datas(meshgen.batch_workload(n_meshes=2, nmin=2, nmax=3, seed=1)))
-    with pytest.raises(_capi.PbgbError):
-        B.batch_waves = -1
