@@ -380,7 +380,8 @@ __device__ __forceinline__ void acquire_fence()
 // by the first thread before its counter update) and continues.  Min and max are exact and
 // commutative, so the boxes do not depend on which child's thread goes on.
 //
-// A block owns kBoxLeaves consecutive sorted leaves [L, R].  A node whose leaf range lies inside
+// A block owns K consecutive sorted leaves [L, R] (1,024; 256 below a million boxes, so that a
+// small hierarchy, such as a contact mesh's, still spreads over every SM).  A node whose leaf range lies inside
 // [L, R] has its index inside it too (a Karras node is an end of its range), so its visit counter
 // is a shared-memory word and the arrival order needs only block-scope fences; its record lands in
 // the block's own window of the node array (the second arrival sets the node's visits entry to 2).
@@ -388,13 +389,14 @@ __device__ __forceinline__ void acquire_fence()
 // (visits) with a releasing add and an acquire by the second arrival, whose sibling record may
 // come from another block.  Over both phases a climb takes at most 64 levels; deeper trees raise
 // kBvhErrDepth instead of looping on.
-int constexpr kBoxLeaves = 1024;
+int constexpr kBoxSmallLimit = 1 << 20;
 
-__global__ void __launch_bounds__(kBoxLeaves, 2) boxes_kernel(int32_t n, BvhBuffers B, float4 const* __restrict__ lo, float4 const* __restrict__ hi)
+template <int K>
+__global__ void __launch_bounds__(K, 2048 / K) boxes_kernel(int32_t n, BvhBuffers B, float4 const* __restrict__ lo, float4 const* __restrict__ hi)
 {
-    __shared__ int32_t arrivals[kBoxLeaves];
-    int32_t const L = int32_t(blockIdx.x) * kBoxLeaves;
-    int32_t const R = min(L + kBoxLeaves, n) - 1;
+    __shared__ int32_t arrivals[K];
+    int32_t const L = int32_t(blockIdx.x) * K;
+    int32_t const R = min(L + K, n) - 1;
     arrivals[threadIdx.x] = 0;
     __syncthreads();
     int32_t const s = L + int32_t(threadIdx.x);
@@ -623,7 +625,10 @@ cudaError_t boxes_impl(BvhBuffers const& B, int32_t n, float4 const* lo, float4 
         if (e != cudaSuccess)
             return e;
     }
-    boxes_kernel<<<blocks(n, kBoxLeaves), kBoxLeaves, 0, s>>>(n, B, lo, hi);
+    if (n < kBoxSmallLimit)
+        boxes_kernel<256><<<blocks(n, 256), 256, 0, s>>>(n, B, lo, hi);
+    else
+        boxes_kernel<1024><<<blocks(n, 1024), 1024, 0, s>>>(n, B, lo, hi);
     return cudaGetLastError();
 }
 

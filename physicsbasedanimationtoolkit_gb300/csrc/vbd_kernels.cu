@@ -131,8 +131,16 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(Swee
     int i       = 0;
     float xi[3] = {0.f, 0.f, 0.f};
     int k = 0, k1 = 0, n0 = 0, n1 = 0, base = 0;
-    uint2 q   = make_uint2(0u, 0u);
-    float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint2 q0 = make_uint2(0u, 0u), q1 = q0;
+    float4 st0 = make_float4(0.f, 0.f, 0.f, 0.f), st1 = st0;
+    // The mesh tables are not written by any launch of the step: the vertex's first neighbour
+    // indices and first two incidence records are loaded before griddepcontrol.wait, so that
+    // only the position loads remain on the path after it.
+    int constexpr kPreNbr = 4;
+    uint32_t pre[kPreNbr];
+#pragma unroll
+    for (int m = 0; m < kPreNbr; ++m)
+        pre[m] = 0u;
     if (valid)
     {
         i    = __ldg(p.solve + s);
@@ -141,10 +149,19 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(Swee
         base = n0 - nb0;
         k1   = __ldg(p.incPtr + s + 1);
         k    = __ldg(p.incPtr + s) + lane;
+#pragma unroll
+        for (int m = 0; m < kPreNbr; ++m)
+            if (n0 + lane + m * L < n1)
+                pre[m] = __ldg(p.nbr + n0 + lane + m * L);
         if (k < k1)
         {
-            q  = __ldg(p.incPack + k);
-            st = __ldg(p.stiff + k);
+            q0  = __ldg(p.incPack + k);
+            st0 = __ldg(p.stiff + k);
+        }
+        if (k + L < k1)
+        {
+            q1  = __ldg(p.incPack + k + L);
+            st1 = __ldg(p.stiff + k + L);
         }
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
@@ -152,7 +169,19 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(Swee
     if (valid)
     {
         load3(CHEB ? p.hprev[i] : p.x[i], xi);
-        for (int j = n0 + lane; j < n1; j += L)
+#pragma unroll
+        for (int m = 0; m < kPreNbr; ++m)
+        {
+            int const j = n0 + lane + m * L;
+            if (j < n1)
+            {
+                float4 const* src = p.x;
+                if (CHEB && !(pre[m] >> 31))
+                    src = p.hprev;
+                slab[base + j - n0] = __ldg(src + (pre[m] & kIndexMask));
+            }
+        }
+        for (int j = n0 + lane + kPreNbr * L; j < n1; j += L)
         {
             uint32_t const a  = __ldg(p.nbr + j);
             float4 const* src = p.x;
@@ -164,27 +193,30 @@ __global__ void __launch_bounds__(256, CONTACT ? 2 : 4) staged_sweep_kernel(Swee
     __syncwarp();
     if (valid)
     {
+        // Two incidences' records in flight ahead of the one being accumulated.
         for (; k < k1; k += L)
         {
-            uint2 qn   = make_uint2(0u, 0u);
-            float4 stn = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (k + L < k1)
+            uint2 q2   = make_uint2(0u, 0u);
+            float4 st2 = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k + 2 * L < k1)
             {
-                qn  = __ldg(p.incPack + k + L);
-                stn = __ldg(p.stiff + k + L);
+                q2  = __ldg(p.incPack + k + 2 * L);
+                st2 = __ldg(p.stiff + k + 2 * L);
             }
             float d[3][3];
 #pragma unroll
             for (int m = 0; m < 3; ++m)
             {
-                float4 const xa = slab[base + int((q.x >> (8 * m)) & 0xFFu)];
+                float4 const xa = slab[base + int((q0.x >> (8 * m)) & 0xFFu)];
                 d[m][0] = xa.x - xi[0];
                 d[m][1] = xa.y - xi[1];
                 d[m][2] = xa.z - xi[2];
             }
-            accumulate_incidence(b, d, st.x, st.y, st.z, __uint_as_float(q.y), st.w);
-            q  = qn;
-            st = stn;
+            accumulate_incidence(b, d, st0.x, st0.y, st0.z, __uint_as_float(q0.y), st0.w);
+            q0  = q1;
+            st0 = st1;
+            q1  = q2;
+            st1 = st2;
         }
     }
     finish_vertex<L, CHEB, REC, CONTACT>(p, b, valid, lane, i, s, xi);

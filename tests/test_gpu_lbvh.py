@@ -73,7 +73,7 @@ def test_scene_triangle_bvh_bit_exact(swept):
     assert_same(g, o)
 
 
-@pytest.mark.parametrize("n", [2, 3, 1000, 1024, 1025, 2049, 200_000])
+@pytest.mark.parametrize("n", [2, 3, 1000, 1024, 1025, 2049, 200_000, 1_100_000])
 def test_random_boxes_with_duplicate_codes(n):
     rng = np.random.default_rng(n)
     lo = rng.uniform(0, 1, (n, 3)).astype(np.float32)
