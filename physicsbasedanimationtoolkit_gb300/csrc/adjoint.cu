@@ -44,10 +44,10 @@ __device__ __forceinline__ void load_incidence(AdjointSweepParams const& p, uint
 
 // L lanes per vertex o of the colour, as in the forward sweep: lane l takes incidences l, l+L, ...
 // Everything but o's own adjoint comes from the tape and the mesh tables, which no launch of the
-// reversed step writes: the vertex's tape entries and its lane's first incidence are loaded before
-// griddepcontrol.wait, so that with programmatic dependent launch they overlap the previous
-// colour's tail; the adjoint is read, and the neighbours' adjoints and the tets' sensitivities
-// written, only after it.
+// reversed step writes: the vertex's tape entries, its lane's first incidence and that
+// incidence's w-independent terms (adjoint_tet_prepare) are formed before griddepcontrol.wait, so
+// that with programmatic dependent launch they overlap the previous colour's tail; the adjoint is
+// read, and the neighbours' adjoints and the tets' sensitivities written, only after it.
 template <int L>
 __global__ void __launch_bounds__(256) adjoint_sweep_kernel(AdjointSweepParams p)
 {
@@ -60,6 +60,8 @@ __global__ void __launch_bounds__(256) adjoint_sweep_kernel(AdjointSweepParams p
     int i = 0, k = 0, k1 = 0;
     float4 pre = make_float4(0.f, 0.f, 0.f, 0.f), pst = pre, Xo = pre, r0 = pre, r1 = pre;
     AdjointIncidence a;
+    AdjointTetPre<float> q;
+    float delta[3] = {0.f, 0.f, 0.f};
     bool has = false, skipped = true;
     if (valid)
     {
@@ -72,8 +74,28 @@ __global__ void __launch_bounds__(256) adjoint_sweep_kernel(AdjointSweepParams p
         k   = p.incPtr[s] + lane;
         k1  = p.incPtr[s + 1];
         has = k < k1;
+        // The step was skipped (singular Newton matrix, tape entry zero): x_o' = x_o, and nothing
+        // else of the update depends on its inputs.
+        skipped = r0.x == 0.f && r0.w == 0.f && r1.y == 0.f;
+        delta[0] = pre.x - pst.x, delta[1] = pre.y - pst.y, delta[2] = pre.z - pst.z;
+        if (p.D != 0.f)
+        {
+            float4 const xs = p.xs[i];
+            delta[0]        = (1.f + p.D) * delta[0] - p.D * (pre.x - xs.x);
+            delta[1]        = (1.f + p.D) * delta[1] - p.D * (pre.y - xs.y);
+            delta[2]        = (1.f + p.D) * delta[2] - p.D * (pre.z - xs.z);
+        }
+        if (skipped)
+            has = false;
+        // The first incidence's w-independent terms (positions, rest state, delta: all from the
+        // tape and the tables) are formed before the wait as well.
         if (has)
+        {
             load_incidence(p, p.inc[k], pre, Xo, a);
+            float G[3][3];
+            rest_gradients(a.E, G);
+            adjoint_tet_prepare(a.d, a.E, G, delta, q);
+        }
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
@@ -84,25 +106,10 @@ __global__ void __launch_bounds__(256) adjoint_sweep_kernel(AdjointSweepParams p
         w[0] = r0.x * u.x + r0.y * u.y + r0.z * u.z;
         w[1] = r0.y * u.x + r0.w * u.y + r1.x * u.z;
         w[2] = r0.z * u.x + r1.x * u.y + r1.y * u.z;
-        // The step was skipped (singular Newton matrix, tape entry zero): x_o' = x_o, and nothing
-        // else of the update depends on its inputs.
-        skipped = r0.x == 0.f && r0.w == 0.f && r1.y == 0.f;
-        float delta[3] = {pre.x - pst.x, pre.y - pst.y, pre.z - pst.z};
-        if (p.D != 0.f)
-        {
-            float4 const xs = p.xs[i];
-            delta[0]        = (1.f + p.D) * delta[0] - p.D * (pre.x - xs.x);
-            delta[1]        = (1.f + p.D) * delta[1] - p.D * (pre.y - xs.y);
-            delta[2]        = (1.f + p.D) * delta[2] - p.D * (pre.z - xs.z);
-        }
-        if (skipped)
-            has = false;
         while (has)
         {
-            float G[3][3];
-            rest_gradients(a.E, G);
             float c[3][3], dmu = 0.f, dla = 0.f;
-            adjoint_tet(a.d, a.E, G, w, delta, a.mat.x, a.mat.y, c, dmu, dla);
+            adjoint_tet_finish(q, w, delta, a.mat.x, a.mat.y, c, dmu, dla);
 #pragma unroll
             for (int m = 0; m < 3; ++m)
             {
@@ -117,7 +124,12 @@ __global__ void __launch_bounds__(256) adjoint_sweep_kernel(AdjointSweepParams p
             k += L;
             has = k < k1;
             if (has)
+            {
                 load_incidence(p, p.inc[k], pre, Xo, a);
+                float G[3][3];
+                rest_gradients(a.E, G);
+                adjoint_tet_prepare(a.d, a.E, G, delta, q);
+            }
         }
     }
 #pragma unroll

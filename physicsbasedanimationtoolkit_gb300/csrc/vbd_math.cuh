@@ -531,6 +531,115 @@ PBGB_HD T chebyshev_omega(int k, T rho2, T omega, int formula)
 //   c[k]: d(phi_e)/d(x_{a_k}).
 //   dlogmu, dloglambda: d(phi_e)/d(log mu), d(phi_e)/d(log lambda), with alpha = 1 + mu/lambda
 //   varying with both.
+// Column c of D_a = d(cof F : a g_o^T)/dF (closed form by cross products).
+template <class T>
+PBGB_HD void adjoint_dcol(T const (&f)[3][3], T const (&go)[3], T const* a, int c, T* out)
+{
+    int const c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+    T u[3], v[3];
+    u[0] = a[1] * f[c2][2] - a[2] * f[c2][1]; // a x f_{c+2}
+    u[1] = a[2] * f[c2][0] - a[0] * f[c2][2];
+    u[2] = a[0] * f[c2][1] - a[1] * f[c2][0];
+    v[0] = f[c1][1] * a[2] - f[c1][2] * a[1]; // f_{c+1} x a
+    v[1] = f[c1][2] * a[0] - f[c1][0] * a[2];
+    v[2] = f[c1][0] * a[1] - f[c1][1] * a[0];
+    for (int r = 0; r < 3; ++r)
+        out[r] = go[c1] * u[r] + go[c2] * v[r];
+}
+
+// The part of adjoint_tet that does not depend on w: everything formed from the positions, the
+// rest state and delta.  Split off so that a kernel can form it while it waits for w.
+template <class T>
+struct AdjointTetPre
+{
+    T G[3][3];  // rest gradients of the other corners
+    T f[3][3];  // F by columns
+    T go[3];    // -(G[0] + G[1] + G[2]), the solved corner's gradient
+    T k[3][3];  // cofactor columns
+    T dB[3][3]; // D_B columns: d(cof F : B)/dF for B = delta g_o^T
+    T cg[3];    // (cof F) g_o
+    T sg[3];    // (F - cof F) g_o in the displacement-gradient form
+    T Jm1, cB, gg;
+};
+
+template <class T>
+PBGB_HD void adjoint_tet_prepare(T const (&d)[3][3], T const (&e)[3][3], T const (&G)[3][3], T const* delta, AdjointTetPre<T>& q)
+{
+    for (int m = 0; m < 3; ++m)
+        for (int r = 0; r < 3; ++r)
+            q.G[m][r] = G[m][r];
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r)
+            q.f[c][r] = d[0][r] * G[0][c] + d[1][r] * G[1][c] + d[2][r] * G[2][c];
+    for (int c = 0; c < 3; ++c)
+        q.go[c] = -(G[0][c] + G[1][c] + G[2][c]);
+    q.k[0][0] = q.f[1][1] * q.f[2][2] - q.f[1][2] * q.f[2][1];
+    q.k[0][1] = q.f[1][2] * q.f[2][0] - q.f[1][0] * q.f[2][2];
+    q.k[0][2] = q.f[1][0] * q.f[2][1] - q.f[1][1] * q.f[2][0];
+    q.k[1][0] = q.f[2][1] * q.f[0][2] - q.f[2][2] * q.f[0][1];
+    q.k[1][1] = q.f[2][2] * q.f[0][0] - q.f[2][0] * q.f[0][2];
+    q.k[1][2] = q.f[2][0] * q.f[0][1] - q.f[2][1] * q.f[0][0];
+    q.k[2][0] = q.f[0][1] * q.f[1][2] - q.f[0][2] * q.f[1][1];
+    q.k[2][1] = q.f[0][2] * q.f[1][0] - q.f[0][0] * q.f[1][2];
+    q.k[2][2] = q.f[0][0] * q.f[1][1] - q.f[0][1] * q.f[1][0];
+    // Displacement gradient D[col][row].
+    T D[3][3];
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r)
+            D[c][r] = (d[0][r] - e[0][r]) * G[0][c] + (d[1][r] - e[1][r]) * G[1][c] + (d[2][r] - e[2][r]) * G[2][c];
+    // cof D (columns D1 x D2, D2 x D0, D0 x D1), J - 1 and F - cof F.
+    T cd[3][3];
+    for (int c = 0; c < 3; ++c)
+    {
+        T const* u = D[(c + 1) % 3];
+        T const* v = D[(c + 2) % 3];
+        cd[c][0] = u[1] * v[2] - u[2] * v[1];
+        cd[c][1] = u[2] * v[0] - u[0] * v[2];
+        cd[c][2] = u[0] * v[1] - u[1] * v[0];
+    }
+    T const trD  = D[0][0] + D[1][1] + D[2][2];
+    T const min2 = (D[0][0] * D[1][1] - D[1][0] * D[0][1]) + (D[0][0] * D[2][2] - D[2][0] * D[0][2]) +
+                   (D[1][1] * D[2][2] - D[2][1] * D[1][2]);
+    T const detD = D[0][0] * cd[0][0] + D[0][1] * cd[0][1] + D[0][2] * cd[0][2];
+    q.Jm1        = trD + min2 + detD;
+    for (int r = 0; r < 3; ++r)
+    {
+        q.cg[r] = q.go[0] * q.k[0][r] + q.go[1] * q.k[1][r] + q.go[2] * q.k[2][r];
+        T acc   = T(0);
+        for (int c = 0; c < 3; ++c)
+            acc += q.go[c] * (D[c][r] + D[r][c] - cd[c][r] - (c == r ? trD : T(0)));
+        q.sg[r] = acc;
+    }
+    q.cB = delta[0] * q.cg[0] + delta[1] * q.cg[1] + delta[2] * q.cg[2];
+    q.gg = q.go[0] * q.go[0] + q.go[1] * q.go[1] + q.go[2] * q.go[2];
+    for (int c = 0; c < 3; ++c)
+        adjoint_dcol(q.f, q.go, delta, c, q.dB[c]);
+}
+
+// The part of adjoint_tet that depends on w.
+template <class T>
+PBGB_HD void adjoint_tet_finish(AdjointTetPre<T> const& q, T const* w, T const* delta, T muw, T law, T (&c)[3][3], T& dlogmu, T& dloglambda)
+{
+    T const cA  = w[0] * q.cg[0] + w[1] * q.cg[1] + w[2] * q.cg[2];
+    T const FmC = w[0] * q.sg[0] + w[1] * q.sg[1] + w[2] * q.sg[2];
+    T const wd  = w[0] * delta[0] + w[1] * delta[1] + w[2] * delta[2];
+    dlogmu      = muw * (FmC - q.gg * wd);
+    dloglambda  = law * (q.Jm1 * cA - cA * q.cB);
+    T const sA  = law * (q.Jm1 - q.cB) - muw;
+    T const sC  = law * cA;
+    T M[3][3]; // M[col][row]
+    for (int col = 0; col < 3; ++col)
+    {
+        T dA[3];
+        adjoint_dcol(q.f, q.go, w, col, dA);
+        for (int r = 0; r < 3; ++r)
+            M[col][r] = muw * q.go[col] * w[r] + sC * (q.k[col][r] - q.dB[col][r]) + sA * dA[r];
+    }
+    for (int m = 0; m < 3; ++m)
+        for (int r = 0; r < 3; ++r)
+            c[m][r] = M[0][r] * q.G[m][0] + M[1][r] * q.G[m][1] + M[2][r] * q.G[m][2];
+}
+
 template <class T>
 PBGB_HD void adjoint_tet(
     T const (&d)[3][3],
@@ -544,88 +653,9 @@ PBGB_HD void adjoint_tet(
     T& dlogmu,
     T& dloglambda)
 {
-    T f[3][3]; // f[col][row] = F(row, col)
-    for (int q = 0; q < 3; ++q)
-        for (int r = 0; r < 3; ++r)
-            f[q][r] = d[0][r] * G[0][q] + d[1][r] * G[1][q] + d[2][r] * G[2][q];
-    T go[3];
-    for (int q = 0; q < 3; ++q)
-        go[q] = -(G[0][q] + G[1][q] + G[2][q]);
-    T k[3][3]; // cofactor columns
-    k[0][0] = f[1][1] * f[2][2] - f[1][2] * f[2][1];
-    k[0][1] = f[1][2] * f[2][0] - f[1][0] * f[2][2];
-    k[0][2] = f[1][0] * f[2][1] - f[1][1] * f[2][0];
-    k[1][0] = f[2][1] * f[0][2] - f[2][2] * f[0][1];
-    k[1][1] = f[2][2] * f[0][0] - f[2][0] * f[0][2];
-    k[1][2] = f[2][0] * f[0][1] - f[2][1] * f[0][0];
-    k[2][0] = f[0][1] * f[1][2] - f[0][2] * f[1][1];
-    k[2][1] = f[0][2] * f[1][0] - f[0][0] * f[1][2];
-    k[2][2] = f[0][0] * f[1][1] - f[0][1] * f[1][0];
-    // Displacement gradient D[col][row].
-    T D[3][3];
-    for (int q = 0; q < 3; ++q)
-        for (int r = 0; r < 3; ++r)
-            D[q][r] = (d[0][r] - e[0][r]) * G[0][q] + (d[1][r] - e[1][r]) * G[1][q] + (d[2][r] - e[2][r]) * G[2][q];
-    // cof D (columns D1 x D2, D2 x D0, D0 x D1), J - 1 and F - cof F.
-    T cd[3][3];
-    for (int q = 0; q < 3; ++q)
-    {
-        T const* u = D[(q + 1) % 3];
-        T const* v = D[(q + 2) % 3];
-        cd[q][0] = u[1] * v[2] - u[2] * v[1];
-        cd[q][1] = u[2] * v[0] - u[0] * v[2];
-        cd[q][2] = u[0] * v[1] - u[1] * v[0];
-    }
-    T const trD  = D[0][0] + D[1][1] + D[2][2];
-    T const min2 = (D[0][0] * D[1][1] - D[1][0] * D[0][1]) + (D[0][0] * D[2][2] - D[2][0] * D[0][2]) +
-                   (D[1][1] * D[2][2] - D[2][1] * D[1][2]);
-    T const detD = D[0][0] * cd[0][0] + D[0][1] * cd[0][1] + D[0][2] * cd[0][2];
-    T const Jm1  = trD + min2 + detD;
-    // cof:A = w . (cof g_o), cof:B = delta . (cof g_o), (F - cof):A = w . ((F - cof) g_o)
-    T cg[3], sg[3];
-    for (int r = 0; r < 3; ++r)
-    {
-        cg[r] = go[0] * k[0][r] + go[1] * k[1][r] + go[2] * k[2][r];
-        T acc = T(0);
-        for (int q = 0; q < 3; ++q)
-            acc += go[q] * (D[q][r] + D[r][q] - cd[q][r] - (q == r ? trD : T(0)));
-        sg[r] = acc;
-    }
-    T const cA  = w[0] * cg[0] + w[1] * cg[1] + w[2] * cg[2];
-    T const cB  = delta[0] * cg[0] + delta[1] * cg[1] + delta[2] * cg[2];
-    T const FmC = w[0] * sg[0] + w[1] * sg[1] + w[2] * sg[2];
-    T const wd  = w[0] * delta[0] + w[1] * delta[1] + w[2] * delta[2];
-    T const gg  = go[0] * go[0] + go[1] * go[1] + go[2] * go[2];
-    dlogmu      = muw * (FmC - gg * wd);
-    dloglambda  = law * (Jm1 * cA - cA * cB);
-    // Columns of D_a for a rank-one direction a g_o^T.
-    auto dcol = [&](T const* a, int q, T* out) {
-        auto cross = [](T const* u, T const* v, T* o) {
-            o[0] = u[1] * v[2] - u[2] * v[1];
-            o[1] = u[2] * v[0] - u[0] * v[2];
-            o[2] = u[0] * v[1] - u[1] * v[0];
-        };
-        int const q1 = (q + 1) % 3, q2 = (q + 2) % 3;
-        T u[3], v[3];
-        cross(a, f[q2], u); // a x f_{q+2}
-        cross(f[q1], a, v); // f_{q+1} x a
-        for (int r = 0; r < 3; ++r)
-            out[r] = go[q1] * u[r] + go[q2] * v[r];
-    };
-    T const sA = law * (Jm1 - cB) - muw;
-    T const sC = law * cA;
-    T M[3][3]; // M[col][row]
-    for (int q = 0; q < 3; ++q)
-    {
-        T dA[3], dB[3];
-        dcol(w, q, dA);
-        dcol(delta, q, dB);
-        for (int r = 0; r < 3; ++r)
-            M[q][r] = muw * go[q] * w[r] + sC * (k[q][r] - dB[r]) + sA * dA[r];
-    }
-    for (int m = 0; m < 3; ++m)
-        for (int r = 0; r < 3; ++r)
-            c[m][r] = M[0][r] * G[m][0] + M[1][r] * G[m][1] + M[2][r] * G[m][2];
+    AdjointTetPre<T> q;
+    adjoint_tet_prepare(d, e, G, delta, q);
+    adjoint_tet_finish(q, w, delta, muw, law, c, dlogmu, dloglambda);
 }
 
 } // namespace pbgb
