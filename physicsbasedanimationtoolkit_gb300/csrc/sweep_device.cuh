@@ -77,11 +77,12 @@ __device__ __forceinline__ void contact_terms(SweepParams const& p, bool valid, 
     for (int r = 0; r < 6; ++r)
         cH[r] = 0.f;
     cg[0] = cg[1] = cg[2] = 0.f;
+    int const n = valid ? __ldg(p.ccount + i) : 0;
 #pragma unroll
     for (int c = 0; c < (kMaxContactsPerVertex + L - 1) / L; ++c)
     {
         int const k = lane + c * L;
-        if (valid && k < kMaxContactsPerVertex)
+        if (k < n)
         {
             int4 const r = p.crec[i * kMaxContactsPerVertex + k];
             if (r.w >= 0)

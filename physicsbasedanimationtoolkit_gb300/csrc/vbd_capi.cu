@@ -285,6 +285,7 @@ class VbdSystem
     DeviceArray<int32_t> cV, cB, vcolorD, cAv, cNActive, cNn, cFc, cFlags;
     DeviceArray<int4> cF, cRec;
     DeviceArray<float> cPen;
+    DeviceArray<int32_t> cCount; // listed triangles per vertex (its records come first)
     DeviceArray<float> cXVA, cFA, cDupper;
     DeviceArray<float4> cTlo, cThi, cVlo, cVhi, xpred;
     DeviceArray<uint8_t> cActive;
@@ -915,6 +916,8 @@ class VbdSystem
             cFc.allocate(size_t(nV) * kMaxContacts);
             cRec.allocate(size_t(nV) * kMaxContacts);
             cPen.allocate(size_t(nV) * kMaxContacts);
+            cCount.allocate(size_t(nV));
+            check(cudaMemset(cCount.get(), 0, sizeof(int32_t) * size_t(nV)), "cudaMemset");
             check(bvh_allocate(cstate.bvh, nF), "cudaMalloc");
             cV.upload(hV.data(), nS, stream);
             cF.upload(hF.data(), nF, stream);
@@ -1524,6 +1527,7 @@ class VbdSystem
             w.vcolor = vcolorD.get();
             w.crec   = cRec.get();
             w.cpen   = cPen.get();
+            w.ccount = cCount.get();
             w.muC    = muC;
             w.muF    = muF;
             w.epsv   = epsv;
@@ -1546,7 +1550,7 @@ class VbdSystem
             {
                 check(contact_update(cmesh, cstate, x.get(), stream), "contact_update");
                 check(launch_contact_records(nV, cFc.get(), cF.get(), cFA.get(), cXVA.get(), vcolorD.get(), muC,
-                                             cRec.get(), cPen.get(), stream),
+                                             cRec.get(), cPen.get(), cCount.get(), stream),
                       "contact_records");
             }
             if (hooks && hooks->substepBegin)

@@ -367,7 +367,7 @@ __global__ void unpack3_kernel(float4 const* __restrict__ in4, float* __restrict
 __global__ void contact_records_kernel(int32_t nV, int32_t const* __restrict__ fc, int4 const* __restrict__ F,
                                        float const* __restrict__ FA, float const* __restrict__ XVA,
                                        int32_t const* __restrict__ vcolor, float muC, int4* __restrict__ crec,
-                                       float* __restrict__ cpen)
+                                       float* __restrict__ cpen, int32_t* __restrict__ ccount)
 {
     int const i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nV)
@@ -382,23 +382,27 @@ __global__ void contact_records_kernel(int32_t nV, int32_t const* __restrict__ f
     }
     float const kC  = sumfa > 0.f ? (XVA[i] * muC) / sumfa : 0.f;
     int32_t const own = vcolor[i];
+    // Listed triangles first, in list order (the lists hold no gaps, so this keeps every slot).
+    int n = 0;
     for (int c = 0; c < kMaxContactsPerVertex; ++c)
     {
-        int4 r   = make_int4(0, 0, 0, -1);
-        float pn = 0.f;
-        if (f[c] >= 0)
-        {
-            int4 const t     = F[f[c]];
-            int const v[3]   = {t.x, t.y, t.z};
-            uint32_t code[3];
-            for (int k = 0; k < 3; ++k)
-                code[k] = uint32_t(v[k]) | (vcolor[v[k]] < own ? 0x80000000u : 0u);
-            r  = make_int4(int(code[0]), int(code[1]), int(code[2]), f[c]);
-            pn = kC * FA[f[c]];
-        }
-        crec[i * kMaxContactsPerVertex + c] = r;
-        cpen[i * kMaxContactsPerVertex + c] = pn;
+        if (f[c] < 0)
+            continue;
+        int4 const t   = F[f[c]];
+        int const v[3] = {t.x, t.y, t.z};
+        uint32_t code[3];
+        for (int k = 0; k < 3; ++k)
+            code[k] = uint32_t(v[k]) | (vcolor[v[k]] < own ? 0x80000000u : 0u);
+        crec[i * kMaxContactsPerVertex + n] = make_int4(int(code[0]), int(code[1]), int(code[2]), f[c]);
+        cpen[i * kMaxContactsPerVertex + n] = kC * FA[f[c]];
+        ++n;
     }
+    for (int c = n; c < kMaxContactsPerVertex; ++c)
+    {
+        crec[i * kMaxContactsPerVertex + c] = make_int4(0, 0, 0, -1);
+        cpen[i * kMaxContactsPerVertex + c] = 0.f;
+    }
+    ccount[i] = n;
 }
 
 inline int blocks_for(int64_t n, int block)
@@ -577,11 +581,12 @@ cudaError_t launch_pack3(float const* in3, float4* out4, int32_t n, cudaStream_t
 }
 
 cudaError_t launch_contact_records(int32_t nV, int32_t const* fc, int4 const* F, float const* FA, float const* XVA,
-                                   int32_t const* vcolor, float muC, int4* crec, float* cpen, cudaStream_t s)
+                                   int32_t const* vcolor, float muC, int4* crec, float* cpen, int32_t* ccount,
+                                   cudaStream_t s)
 {
     if (nV <= 0)
         return cudaSuccess;
-    contact_records_kernel<<<blocks_for(nV, 256), 256, 0, s>>>(nV, fc, F, FA, XVA, vcolor, muC, crec, cpen);
+    contact_records_kernel<<<blocks_for(nV, 256), 256, 0, s>>>(nV, fc, F, FA, XVA, vcolor, muC, crec, cpen, ccount);
     return cudaGetLastError();
 }
 

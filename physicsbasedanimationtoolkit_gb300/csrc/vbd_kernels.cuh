@@ -64,9 +64,11 @@ struct SweepParams
     // Contact records, rebuilt at each active-set update (launch_contact_records): per vertex and
     // slot, the triangle's corners with bit 31 set when the corner's colour is below the vertex's
     // (read from x, else from hprev) and w = the triangle (-1: none); cpen = its penalty
-    // XVA_i muC FA_f / sum of the listed FA.
+    // XVA_i muC FA_f / sum of the listed FA.  The listed triangles come first; ccount holds how
+    // many a vertex has, so that the vertices without contact read no record.
     int4 const* __restrict__ crec;
     float const* __restrict__ cpen;
+    int32_t const* __restrict__ ccount;
     float muC;
     float muF;
     float epsv;
@@ -165,7 +167,8 @@ cudaError_t launch_gradient(EnergyParams const& p, cudaStream_t s);
 cudaError_t launch_pack3(float const* in3, float4* out4, int32_t n, cudaStream_t s, float4 const* origin = nullptr);
 // Contact records of all nV vertices from their lists fc (see SweepParams::crec).
 cudaError_t launch_contact_records(int32_t nV, int32_t const* fc, int4 const* F, float const* FA, float const* XVA,
-                                   int32_t const* vcolor, float muC, int4* crec, float* cpen, cudaStream_t s);
+                                   int32_t const* vcolor, float muC, int4* crec, float* cpen, int32_t* ccount,
+                                   cudaStream_t s);
 cudaError_t launch_unpack3(float4 const* in4, float* out3, int32_t n, cudaStream_t s, float4 const* origin = nullptr);
 
 } // namespace pbgb
