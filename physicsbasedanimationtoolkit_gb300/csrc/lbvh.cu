@@ -182,7 +182,7 @@ cudaError_t exclusive_scan(uint32_t* a, int64_t total, uint32_t* tmp, cudaStream
     return cudaGetLastError();
 }
 
-__global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
+__global__ void __launch_bounds__(kSortThreads, 3) radix_scatter_kernel(
     uint32_t const* __restrict__ kin,
     int32_t const* __restrict__ vin,
     uint32_t* __restrict__ kout,
@@ -192,37 +192,63 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     uint32_t const* __restrict__ offsets,
     int tiles)
 {
-    // The tile is first sorted by digit in shared memory (stable), then each digit's run is
-    // written to its global range, so consecutive threads write consecutive addresses.
+    // The tile is first ordered by digit in shared memory (stably), then each digit's run is
+    // written to its global range, so consecutive threads write consecutive addresses.  Warp w
+    // ranks its own kSortRounds * 32 consecutive keys of the tile in one pass (round r, lane l:
+    // key w * kSortRounds * 32 + r * 32 + l): a key's rank among its warp's equal digits is the
+    // warp's running count of the digit before the round plus its peers in lower lanes
+    // (__match_any_sync); the lowest peer then adds the group to the count.  One block scan over
+    // (digit, warp) turns the warps' counts into each warp's first position per digit, so the
+    // tile needs three block barriers whatever its rounds.
     __shared__ uint32_t skey[kTile];
     __shared__ int32_t sval[kTile];
-    __shared__ uint32_t run[kBuckets];
+    __shared__ uint32_t wcount[kWarps][kBuckets]; // the warp's count per digit, then its first position
     __shared__ uint32_t localStart[kBuckets];
-    __shared__ uint32_t warpCount[kWarps][kBuckets];
+    __shared__ uint32_t warpTotal[kWarps];
     int const tile = blockIdx.x;
     int const t    = threadIdx.x;
     int const lane = t & 31;
     int const warp = t >> 5;
-    int const base = tile * kTile;
-    uint32_t key[kSortRounds];
-    int32_t val[kSortRounds];
-    for (int d = t; d < kBuckets; d += blockDim.x)
-        run[d] = 0;
+    for (int q = t; q < kWarps * kBuckets; q += blockDim.x)
+        (&wcount[0][0])[q] = 0;
     __syncthreads();
+    int const base = tile * kTile + warp * (kSortRounds * 32) + lane;
+    uint32_t key[kSortRounds];
+    uint32_t rank[kSortRounds]; // rank among the warp's equal digits, bits 8..; digit, bits 0..7
+    unsigned const lanesBelow = (1u << lane) - 1u;
 #pragma unroll
     for (int r = 0; r < kSortRounds; ++r)
     {
-        int const i = base + r * kSortThreads + t;
+        int const i = base + r * 32;
         key[r]      = i < n ? kin[i] : 0u;
-        val[r]      = i < n ? vin[i] : 0;
-        if (i < n)
-            atomicAdd(&run[(key[r] >> shift) & 0xFFu], 1u);
+    }
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r)
+    {
+        bool const valid     = base + r * 32 < n;
+        uint32_t const d     = valid ? (key[r] >> shift) & 0xFFu : uint32_t(kBuckets);
+        unsigned const peers = __match_any_sync(0xffffffffu, d);
+        unsigned const below = __popc(peers & lanesBelow);
+        uint32_t const before = valid ? wcount[warp][d] : 0u;
+        rank[r]              = ((before + below) << 8) | (d & 0xFFu);
+        __syncwarp();
+        if (valid && below == 0)
+            wcount[warp][d] = before + __popc(peers);
+        __syncwarp();
     }
     __syncthreads();
-    // Exclusive scan of the tile's digit counts (kBuckets == kSortThreads: one digit per thread).
+    // Digit t: the tile's exclusive prefix over digits (kBuckets == kSortThreads), then each warp's
+    // first position for the digit.
     {
-        uint32_t const c = run[t];
-        uint32_t inc     = c;
+        uint32_t cw[kWarps];
+        uint32_t c = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w)
+        {
+            cw[w] = wcount[w][t];
+            c += cw[w];
+        }
+        uint32_t inc = c;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1)
         {
@@ -231,49 +257,36 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
                 inc += y;
         }
         if (lane == 31)
-            warpCount[0][warp] = inc;
+            warpTotal[warp] = inc;
         __syncthreads();
         uint32_t start = inc - c;
         for (int w = 0; w < warp; ++w)
-            start += warpCount[0][w];
-        __syncthreads();
+            start += warpTotal[w];
         localStart[t] = start;
-        run[t]        = start;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w)
+        {
+            wcount[w][t] = start;
+            start += cw[w];
+        }
     }
-    unsigned const lanesBelow = (1u << lane) - 1u;
+    __syncthreads();
+    // The values are read only now (coalesced, like the keys), which keeps them out of registers
+    // across the ranking.
 #pragma unroll
     for (int r = 0; r < kSortRounds; ++r)
     {
-        for (int q = t; q < kWarps * kBuckets; q += blockDim.x)
-            (&warpCount[0][0])[q] = 0;
-        __syncthreads();
-        int const i          = base + r * kSortThreads + t;
-        bool const valid     = i < n;
-        uint32_t const d     = valid ? ((key[r] >> shift) & 0xFFu) : uint32_t(kBuckets);
-        unsigned const peers = __match_any_sync(0xffffffffu, d);
-        unsigned const rank  = __popc(peers & lanesBelow);
-        if (valid && rank == 0)
-            warpCount[warp][d] = __popc(peers);
-        __syncthreads();
-        if (valid)
+        int const i = base + r * 32;
+        if (i < n)
         {
-            uint32_t pos = run[d] + rank;
-            for (int w = 0; w < warp; ++w)
-                pos += warpCount[w][d];
-            skey[pos] = key[r];
-            sval[pos] = val[r];
+            uint32_t const pos = wcount[warp][rank[r] & 0xFFu] + (rank[r] >> 8);
+            skey[pos]          = key[r];
+            sval[pos]          = vin[i];
         }
-        __syncthreads();
-        for (int dd = t; dd < kBuckets; dd += blockDim.x)
-        {
-            uint32_t add = 0;
-            for (int w = 0; w < kWarps; ++w)
-                add += warpCount[w][dd];
-            run[dd] += add;
-        }
-        __syncthreads();
     }
-    int const count = n - base < kTile ? n - base : kTile;
+    __syncthreads();
+    int const first = tile * kTile;
+    int const count = n - first < kTile ? n - first : kTile;
     for (int j = t; j < count; j += kSortThreads)
     {
         uint32_t const k = skey[j];
