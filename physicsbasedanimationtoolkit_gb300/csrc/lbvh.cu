@@ -50,10 +50,8 @@ __global__ void morton_kernel(int32_t n, float4 const* __restrict__ lo, float4 c
 
 // --- stable LSD radix sort, 8-bit digits ------------------------------------------------------
 // Pass = count digits per tile -> exclusive scan (digit-major, so tiles keep their order inside a
-// digit) -> scatter with each key's rank inside its tile.  The rank inside a tile is built round by
-// round (kSortThreads consecutive keys per round): warp-level peers from __match_any_sync, then the
-// earlier warps' counts of the same digit, then the running count of earlier rounds, so equal
-// digits keep their input order and every pass is stable.
+// digit) -> scatter with each key's rank inside its tile (radix_scatter_kernel), in which equal
+// digits keep their input order, so every pass is stable.
 
 __global__ void radix_count_kernel(uint32_t const* __restrict__ keys, int32_t n, int shift, uint32_t* __restrict__ counts, int tiles)
 {
@@ -198,8 +196,8 @@ __global__ void __launch_bounds__(kSortThreads, 3) radix_scatter_kernel(
     // written to its global range, so consecutive threads write consecutive addresses.  Warp w
     // ranks its own kSortRounds * 32 consecutive keys of the tile in one pass (round r, lane l:
     // key w * kSortRounds * 32 + r * 32 + l): a key's rank among its warp's equal digits is the
-    // warp's running count of the digit before the round plus its peers in lower lanes
-    // (__match_any_sync); the lowest peer then adds the group to the count.  One block scan over
+    // warp's running count of the digit before the round plus its peers in lower lanes; the lowest
+    // peer then adds the group to the count.  One block scan over
     // (digit, warp) turns the warps' counts into each warp's first position per digit, so the
     // tile needs three block barriers whatever its rounds.
     __shared__ uint32_t skey[kTile];
@@ -229,7 +227,15 @@ __global__ void __launch_bounds__(kSortThreads, 3) radix_scatter_kernel(
     {
         bool const valid     = base + r * 32 < n;
         uint32_t const d     = valid ? (key[r] >> shift) & 0xFFu : uint32_t(kBuckets);
-        unsigned const peers = __match_any_sync(0xffffffffu, d);
+        // Lanes with the same digit: nine ballots, one per bit of d (bit 8 marks the lanes past n);
+        // on this GPU they cost less than one __match_any_sync.
+        unsigned peers = 0xffffffffu;
+#pragma unroll
+        for (int bit = 0; bit < 9; ++bit)
+        {
+            unsigned const m = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+            peers &= ((d >> bit) & 1u) ? m : ~m;
+        }
         unsigned const below = __popc(peers & lanesBelow);
         uint32_t const before = valid ? wcount[warp][d] : 0u;
         rank[r]              = ((before + below) << 8) | (d & 0xFFu);
