@@ -333,27 +333,35 @@ __global__ void karras_kernel(SortedKeys K, int32_t* __restrict__ child, int32_t
     if (i >= n - 1)
         return;
     int32_t const leafBegin = n - 1;
+    // delta(i, j) with key i held in a register (the searches only vary j; i is in range).
+    uint32_t const ci = K.code[i];
+    auto delta = [&](int32_t j) -> int {
+        if (uint32_t(j) >= uint32_t(n))
+            return -1;
+        uint32_t const x = ci ^ K.code[j];
+        return x ? __clz(x) : 32 + __clz(uint32_t(i) ^ uint32_t(j));
+    };
     // Direction of the range and a lower bound on its common prefix.
-    int32_t const d    = (K.delta(i, i + 1) - K.delta(i, i - 1)) > 0 ? 1 : -1;
-    int const dmin     = K.delta(i, i - d);
+    int32_t const d    = (delta(i + 1) - delta(i - 1)) > 0 ? 1 : -1;
+    int const dmin     = delta(i - d);
     int32_t lmax       = 2;
-    while (K.delta(i, i + lmax * d) > dmin)
+    while (delta(i + lmax * d) > dmin)
         lmax <<= 1;
     int32_t l = 0;
     do
     {
         lmax >>= 1;
-        if (K.delta(i, i + (l + lmax) * d) > dmin)
+        if (delta(i + (l + lmax) * d) > dmin)
             l += lmax;
     } while (lmax > 1);
     int32_t const j   = i + l * d;
-    int const dnode   = K.delta(i, j);
+    int const dnode   = delta(j);
     int32_t s         = 0;
     int32_t t         = l;
     do
     {
         t = (t + 1) >> 1;
-        if (K.delta(i, i + (s + t) * d) > dnode)
+        if (delta(i + (s + t) * d) > dnode)
             s += t;
     } while (t > 1);
     int32_t const gamma = i + s * d + (d < 0 ? d : 0);
