@@ -35,12 +35,16 @@ __device__ __forceinline__ uint32_t quantise(float c)
     return static_cast<uint32_t>(q);
 }
 
-__global__ void morton_kernel(int32_t n, float4 const* __restrict__ lo, float4 const* __restrict__ hi, float3 wmin, float3 ext, uint32_t* __restrict__ codes, int32_t* __restrict__ inds)
+// Also copies each box into one 32-byte record (lower, upper), so that the box pass gathers one
+// sector per leaf where it would read two half-used ones from the two input arrays.
+__global__ void morton_kernel(int32_t n, float4 const* __restrict__ lo, float4 const* __restrict__ hi, float3 wmin, float3 ext, uint32_t* __restrict__ codes, int32_t* __restrict__ inds, float4* __restrict__ packed)
 {
     int const i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     float4 const b = lo[i], e = hi[i];
+    packed[2 * size_t(i)]     = b;
+    packed[2 * size_t(i) + 1] = e;
     uint32_t const x = quantise(normalised(b.x, e.x, wmin.x, ext.x));
     uint32_t const y = quantise(normalised(b.y, e.y, wmin.y, ext.y));
     uint32_t const z = quantise(normalised(b.z, e.z, wmin.z, ext.z));
@@ -437,7 +441,9 @@ struct BoxesSmem
     int32_t arrivals[K];
 };
 
-__global__ void __launch_bounds__(kBoxLeaves, 2048 / kBoxLeaves) boxes_kernel(int32_t n, BvhBuffers B, float4 const* __restrict__ lo, float4 const* __restrict__ hi)
+// packed (nullable): the boxes as 32-byte records (lower, upper) in input order, read instead of
+// lo and hi.
+__global__ void __launch_bounds__(kBoxLeaves, 2048 / kBoxLeaves) boxes_kernel(int32_t n, BvhBuffers B, float4 const* __restrict__ lo, float4 const* __restrict__ hi, float4 const* __restrict__ packed)
 {
     int constexpr K = kBoxLeaves;
     __shared__ BoxesSmem S;
@@ -460,9 +466,9 @@ __global__ void __launch_bounds__(kBoxLeaves, 2048 / kBoxLeaves) boxes_kernel(in
     float4 bl{}, bh{};
     if (s <= R)
     {
-        i                 = B.inds[s];
-        bl                = lo[i];
-        bh                = hi[i];
+        i  = B.inds[s];
+        bl = packed ? packed[2 * size_t(i)] : lo[i];
+        bh = packed ? packed[2 * size_t(i) + 1] : hi[i];
         S.leafParent[t]   = B.parent[leafBegin + s];
         S.leaf[2 * t]     = bl;
         S.leaf[2 * t + 1] = bh;
@@ -659,7 +665,7 @@ cudaError_t sort_impl(BvhBuffers const& B, int32_t n, float4 const* lo, float4 c
     if (n <= 0)
         return cudaSuccess;
     float3 const ext = make_float3(wmax.x - wmin.x, wmax.y - wmin.y, wmax.z - wmin.z);
-    morton_kernel<<<blocks(n, 256), 256, 0, s>>>(n, lo, hi, wmin, ext, B.codes, B.inds);
+    morton_kernel<<<blocks(n, 256), 256, 0, s>>>(n, lo, hi, wmin, ext, B.codes, B.inds, B.packed);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
@@ -690,7 +696,7 @@ cudaError_t sort_impl(BvhBuffers const& B, int32_t n, float4 const* lo, float4 c
     return cudaSuccess;
 }
 
-cudaError_t boxes_impl(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, cudaStream_t s)
+cudaError_t boxes_impl(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, float4 const* packed, cudaStream_t s)
 {
     if (n < 1)
         return cudaSuccess;
@@ -700,7 +706,7 @@ cudaError_t boxes_impl(BvhBuffers const& B, int32_t n, float4 const* lo, float4 
         if (e != cudaSuccess)
             return e;
     }
-    boxes_kernel<<<blocks(n, kBoxLeaves), kBoxLeaves, 0, s>>>(n, B, lo, hi);
+    boxes_kernel<<<blocks(n, kBoxLeaves), kBoxLeaves, 0, s>>>(n, B, lo, hi, packed);
     return cudaGetLastError();
 }
 
@@ -762,6 +768,7 @@ cudaError_t bvh_allocate(BvhBuffers& B, int32_t capacity)
     get(B.rightmost, 2 * ni);
     get(B.first, ni);
     get(B.visits, ni);
+    get(B.packed, 2 * n);
     get(B.nodes, 2 * (2 * n - 1));
     get(B.flags, 1);
     if (e == cudaSuccess)
@@ -772,7 +779,7 @@ cudaError_t bvh_allocate(BvhBuffers& B, int32_t capacity)
 void bvh_release(BvhBuffers& B)
 {
     void* ptrs[] = {B.codes, B.codesAlt, B.inds, B.indsAlt, B.counts, B.scanTmp, B.child, B.parent,
-                    B.rightmost, B.first, B.visits, B.nodes, B.flags};
+                    B.rightmost, B.first, B.visits, B.packed, B.nodes, B.flags};
     for (void* p : ptrs)
         if (p)
             cudaFree(p);
@@ -801,14 +808,14 @@ cudaError_t bvh_build(BvhBuffers const& B, int32_t n, float4 const* lo, float4 c
         if ((e = cudaGetLastError()) != cudaSuccess)
             return e;
     }
-    return boxes_impl(B, n, lo, hi, s);
+    return boxes_impl(B, n, lo, hi, B.packed, s);
 }
 
 cudaError_t bvh_refit(BvhBuffers const& B, int32_t n, float4 const* lo, float4 const* hi, cudaStream_t s)
 {
     if (n <= 0)
         return cudaSuccess;
-    return boxes_impl(B, n, lo, hi, s);
+    return boxes_impl(B, n, lo, hi, nullptr, s);
 }
 
 cudaError_t bvh_overlaps(

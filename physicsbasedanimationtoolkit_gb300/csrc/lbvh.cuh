@@ -61,6 +61,7 @@ struct BvhBuffers
     int32_t* rightmost; // 2(n-1)
     int32_t* first;     // n-1 lowest sorted leaf of each internal node's range
     int32_t* visits;    // n-1 arrivals counted at each internal node (2 after a build or refit)
+    float4* packed;     // 2n  the build's input boxes, (lower, upper) per box in input order
     float4* nodes;      // 2(2n-1) node records (BvhView)
     int32_t* flags;     // device error bits
 };
