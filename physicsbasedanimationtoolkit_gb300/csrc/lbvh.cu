@@ -65,12 +65,18 @@ __global__ void radix_count_kernel(uint32_t const* __restrict__ keys, int32_t n,
         hist[d] = 0;
     __syncthreads();
     int const base = tile * kTile;
+    // All of the thread's keys are loaded before the first addition, so the loads overlap.
+    uint32_t d[kSortRounds];
+#pragma unroll
     for (int r = 0; r < kSortRounds; ++r)
     {
         int const i = base + r * kSortThreads + threadIdx.x;
-        if (i < n)
-            atomicAdd(&hist[(keys[i] >> shift) & 0xFFu], 1u);
+        d[r]        = i < n ? (keys[i] >> shift) & 0xFFu : uint32_t(kBuckets);
     }
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r)
+        if (d[r] < uint32_t(kBuckets))
+            atomicAdd(&hist[d[r]], 1u);
     __syncthreads();
     for (int d = threadIdx.x; d < kBuckets; d += blockDim.x)
         counts[size_t(d) * tiles + tile] = hist[d];
