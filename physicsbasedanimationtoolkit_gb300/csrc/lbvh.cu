@@ -317,23 +317,11 @@ __global__ void __launch_bounds__(kSortThreads, 3) radix_scatter_kernel(
 
 // --- Karras hierarchy (gpu/impl/geometry/Bvh.cu:24-114) -------------------------------------------
 
-// The sorted keys (code, index): prefix lengths of the binary radix tree over them.
+// The sorted keys (code, index) the binary radix tree is built over.
 struct SortedKeys
 {
     uint32_t const* __restrict__ code;
     int32_t n;
-
-    // Length of the common prefix of keys i and j (index bits break ties of equal codes); -1
-    // outside [0, n).
-    __device__ __forceinline__ int delta(int32_t i, int32_t j) const
-    {
-        if (i < 0 || j < 0 || i >= n || j >= n)
-            return -1;
-        uint32_t const a = code[i], b = code[j];
-        if (a == b)
-            return 32 + __clz(uint32_t(i) ^ uint32_t(j));
-        return __clz(a ^ b);
-    }
 };
 
 __global__ void karras_kernel(SortedKeys K, int32_t* __restrict__ child, int32_t* __restrict__ parent, int32_t* __restrict__ rightmost, int32_t* __restrict__ first)
@@ -343,7 +331,8 @@ __global__ void karras_kernel(SortedKeys K, int32_t* __restrict__ child, int32_t
     if (i >= n - 1)
         return;
     int32_t const leafBegin = n - 1;
-    // delta(i, j) with key i held in a register (the searches only vary j; i is in range).
+    // delta(j): the length of the common prefix of keys i and j, the index bits breaking ties of
+    // equal codes, -1 outside [0, n); key i is held in a register (the searches only vary j).
     uint32_t const ci = K.code[i];
     auto delta = [&](int32_t j) -> int {
         if (uint32_t(j) >= uint32_t(n))
